@@ -1,0 +1,260 @@
+/*
+ * prender_gpu.h — C ABI of the GB300 (sm_103a) radiance estimator and Kerr
+ * geodesic tracer that drops in for prender's render loop.
+ *
+ * Every entry point is plain C: pointers, sizes and status codes.  All calls
+ * return an int status: PR_OK (0) or a negative PR_E* code; pr_last_error()
+ * gives a human-readable reason.  Nothing aborts or traps.  A context owns one
+ * CUDA device and is not thread-safe (one context per host thread).
+ *
+ * Output buffers are caller-allocated.  Functions whose name ends in _dev
+ * take device pointers; the others take host pointers and copy.
+ *
+ * Each declaration cites the reference interface it replaces
+ * (paths are inside Sanaxen/prender).
+ */
+#ifndef PRENDER_GPU_H
+#define PRENDER_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PR_ABI_VERSION 1
+
+/* ---- status codes --------------------------------------------------- */
+enum {
+  PR_OK = 0,
+  PR_E_ARG = -1,        /* bad argument (null pointer, size out of range)   */
+  PR_E_CUDA = -2,       /* a CUDA runtime call failed                        */
+  PR_E_SCENE = -3,      /* scene description is invalid or not uploaded      */
+  PR_E_BUILD = -4,      /* acceleration structure could not be built         */
+  PR_E_DEVICE = -5,     /* a device-side check fired (see pr_last_error)     */
+  PR_E_NOMEM = -6,      /* allocation failed                                 */
+  PR_E_UNSUPPORTED = -7 /* feature outside this build                        */
+};
+
+/* device-side error bits, reported through PR_E_DEVICE */
+enum {
+  PR_DEV_STACK_OVERFLOW = 1,  /* QBVH traversal stack exceeded its capacity  */
+  PR_DEV_LOOP_CAP = 2,        /* a bounded device loop hit its iteration cap */
+  PR_DEV_BAD_INDEX = 4,       /* a node/primitive index was out of range     */
+  PR_DEV_QUEUE_OVERFLOW = 8,  /* a wavefront queue exceeded its capacity     */
+  PR_DEV_NONFINITE = 16       /* a non-finite value was produced             */
+};
+
+/* ---- scene description (semantics of SceneEnv, scene_env.h:155-261) ---- */
+
+/* material.h:19-29 ReflectionType, same numbering */
+enum {
+  PR_MAT_DIFFUSE = 0,
+  PR_MAT_SPECULAR = 1,
+  PR_MAT_REFRACTION = 2,
+  PR_MAT_WARD = 3,
+  PR_MAT_PHONG = 4,
+  PR_MAT_SSS_REFRACTION = 5,
+  PR_MAT_SSS_DIFFUSE = 6,
+  PR_MAT_SSS_WARD = 7,
+  PR_MAT_REFRACTION_FRESNEL = 8
+};
+
+/* entity.h:18-25 EntityType, same numbering */
+enum {
+  PR_ENT_SPHERE = 1,
+  PR_ENT_UVPLANE = 3,
+  PR_ENT_CIRCLE = 4,
+  PR_ENT_POLYGON = 5
+};
+
+/* Per-object homogeneous medium (ParticipatingMediaPrm.h:85-131): the
+ * *_rgb colours are the raw keyword values; the host derives the scalar
+ * means and transmittance exactly as setup_Scattering does. */
+typedef struct pr_medium {
+  double sigma_s_rgb[3];   /* SCATTERING colour line                         */
+  double sigma_a_rgb[3];   /* ABSORBING colour line                          */
+  double phase_g[3];       /* PAHASE (HG g per RGB channel)                  */
+  double eta;              /* refractive index of the medium (BSSRDF)        */
+  double scale;            /* MATERIAL_SCALE                                 */
+  double r_max;            /* MATERIAL_R_MAX                                 */
+  int32_t level;           /* -2 dipole, -1 single+multi, >=0 volumetric walk */
+  int32_t use_bssrdf;
+} pr_medium;
+
+/* material.h:54-240 Material (texture fields out of scope) */
+typedef struct pr_material {
+  int32_t type;            /* PR_MAT_*                                       */
+  int32_t pad0;
+  double color[3];
+  double emission[3];
+  double specular[3];
+  double roughness;        /* 'reflection diffuse' sets 1, 'specular' sets 0  */
+  double refractive_index; /* default 1.5 (REFRACTIVE_INDEX_OF_GLASS)         */
+  pr_medium medium;        /* used by the SSS material types                 */
+} pr_material;
+
+/* One OBJECT block (scene_env.h:854-1851) after its transforms. */
+typedef struct pr_entity {
+  int32_t type;            /* PR_ENT_*                                       */
+  int32_t material;        /* index into pr_scene_desc.materials             */
+  int32_t normal_inverse;  /* 'normal' keyword: 1 or -1                      */
+  int32_t mesh;            /* PR_ENT_POLYGON: index into meshes              */
+  double p[3];             /* sphere centre / uvplane origin / disk centre   */
+  double radius;           /* sphere or disk radius                          */
+  double u[3], v[3];       /* uvplane U and V edge vectors (unnormalised)    */
+  double normal[3];        /* disk normal                                    */
+  double radius_inner;     /* disk2 inner radius                             */
+} pr_entity;
+
+/* Triangle mesh as ObjLoader keeps it (ObjLoader.h:153-233): float vertices,
+ * 0-based faces.  face_normals may be NULL, in which case they are derived
+ * with the loader's rule (ObjLoader.cpp:577-700). */
+typedef struct pr_mesh {
+  int32_t n_vertices;
+  int32_t n_faces;
+  const float* vertices;      /* 3 * n_vertices                              */
+  const int32_t* faces;       /* 3 * n_faces                                 */
+  const float* face_normals;  /* 3 * n_faces or NULL                         */
+} pr_mesh;
+
+/* KerrBlackHole constructor inputs (KerrBlackHole.h:86-151, scene_env.h:701-766,2056-2098) */
+typedef struct pr_kerr {
+  int32_t enabled;
+  int32_t max_steps;          /* geodesics_max_length                        */
+  double position[3];         /* black hole centre (world)                   */
+  double a;                   /* angular_momentum (spin, M = 1)              */
+  double map_coef[4];         /* background (theta, phi) affine coefficients */
+  double escape_radius;       /* 0 = reference behaviour (no escape test)    */
+} pr_kerr;
+
+typedef struct pr_scene_desc {
+  int32_t n_materials;
+  int32_t n_entities;
+  int32_t n_meshes;
+  int32_t participating_media;  /* 'participatingMedia' keyword            */
+  const pr_material* materials;
+  const pr_entity* entities;
+  const pr_mesh* meshes;
+  double background[3];         /* BACKGROUND                               */
+  double environment_light[3];  /* ENVLIGHT                                 */
+  pr_medium medium;             /* global SCATTERING / ABSORBING / PAHASE   */
+  pr_kerr kerr;
+} pr_scene_desc;
+
+/* CameraScreenPram (render.h:70-158) inputs, after SceneEnv::Load. */
+typedef struct pr_camera {
+  double position[3];
+  double dir[3];              /* normalised by SceneEnv::Load (scene_env.h:1920) */
+  double up[3];
+  double screen_width;        /* world_screen_width  (CAMERA_ANGLE rule applied) */
+  double screen_height;       /* world_screen_height                             */
+  double screen_dist;         /* world_screen_dist                               */
+  int32_t width, height;      /* IMAGE                                           */
+} pr_camera;
+
+/* render modes */
+enum { PR_MODE_MEGAKERNEL = 0, PR_MODE_WAVEFRONT = 1 };
+
+/* Render::Run (render.h:1125-1455) parameters. */
+typedef struct pr_render_params {
+  int32_t samples;            /* SAMPLING                                    */
+  int32_t supersamples;       /* SUPERSAMPLING                               */
+  int32_t tent_filter;        /* tentfilter                                  */
+  int32_t depth;              /* DEPTH (RR starts after it)                  */
+  int32_t depth_limit;        /* DEPTH_LIMIT                                 */
+  int32_t nee;                /* nextEventEstimation                         */
+  int32_t media;              /* participatingMedia (global medium on/off)   */
+  int32_t mode;               /* PR_MODE_*                                   */
+  uint64_t seed;              /* counter-based stream key                    */
+  double luminance_cutoff;    /* per-sample clamp (default 0.025)            */
+  double sensor_response;     /* final image scale (default 1)               */
+  int32_t max_path_vertices;  /* device cap on path length (0 = 512)         */
+  int32_t flags;              /* PR_FLAG_*                                   */
+} pr_render_params;
+
+enum {
+  PR_FLAG_HG_CORRECT = 1,     /* sample HG with cos = 1/(2g)(...) instead of
+                                 the reference's (g/2)(...) (sampler.h:55)   */
+  PR_FLAG_EXACT_HITS = 2      /* FP64-confirmed closest hits while rendering */
+};
+
+typedef struct pr_ctx pr_ctx;
+
+/* ---- context ---------------------------------------------------------- */
+/* Replaces process start-up in main.cpp:21-60. */
+pr_ctx* pr_create(int device, int* status);
+void pr_destroy(pr_ctx* ctx);
+const char* pr_last_error(const pr_ctx* ctx);
+int pr_abi_version(void);
+
+/* ---- scene -------------------------------------------------------------- */
+/* Replaces SceneEnv::Load + CreateEntList (scene_env.h:357, scene.cpp:38):
+ * uploads entities, materials, lights (light list built as in
+ * LightList::random_light_setup, light.h:95) and builds one QBVH per mesh
+ * with the reference's SAH rules (BVH.cpp:194-348, QBVH.cpp:161-302). */
+int pr_scene_upload(pr_ctx* ctx, const pr_scene_desc* scene);
+
+/* QBVH statistics of a mesh entity: node count and leaf-array length.
+ * Replaces QBVH::Construct bookkeeping (QBVH.cpp:161-186). */
+int pr_qbvh_info(pr_ctx* ctx, int entity, int64_t* n_nodes, int64_t* n_leaf_slots);
+
+/* Copies a mesh QBVH in the reference's layout (QBVH.h:53-61): per node
+ * 24 floats of boxes [min/max][xyz][4], 4 int64 children (leaf = top bit |
+ * leaf start, invalid = -1) and 3 int32 axes; leaf slots hold face ids with
+ * -1 terminators.  Used to check the build against the reference. */
+int pr_qbvh_export(pr_ctx* ctx, int entity, float* boxes, int64_t* children,
+                   int32_t* axes, int32_t* leaf_faces);
+
+/* ---- closest hit ---------------------------------------------------------- */
+/* intersect_scene_ (scene.cpp:83-214) for n rays, including the 1e-6 origin
+ * push, the linear entity loop and QBVH::CheckIntersection (QBVH.cpp:17-137).
+ * Rays are FP64 (org xyz, dir xyz interleaved, 6 per ray).  Outputs: entity
+ * index (-1 = miss), face id for meshes (-1 otherwise), distance from the
+ * pushed origin (FP64, bit-exact with the reference).  Host buffers. */
+int pr_first_hit(pr_ctx* ctx, const double* rays, int64_t n, int32_t* entity,
+                 int32_t* prim, double* t);
+/* same, device buffers */
+int pr_first_hit_dev(pr_ctx* ctx, const double* rays, int64_t n, int32_t* entity,
+                     int32_t* prim, double* t);
+
+/* ---- rendering -------------------------------------------------------- */
+/* Render::Run (render.h:1125-1455): accumulates samples [sample_offset,
+ * sample_offset + samples*supersamples^2) of every pixel into rgb_accum
+ * (W*H*3 floats, row order of the reference image: index (H-y-1)*W+x),
+ * already multiplied by 1/(total samples) and by sensor_response.  With
+ * sample_offset = 0 and accumulate = 0 the buffer is overwritten. */
+int pr_render(pr_ctx* ctx, const pr_camera* cam, const pr_render_params* prm,
+              float* rgb_accum, uint64_t sample_offset, int accumulate);
+int pr_render_dev(pr_ctx* ctx, const pr_camera* cam, const pr_render_params* prm,
+                  float* rgb_accum_dev, uint64_t sample_offset, int accumulate);
+
+/* Per-launch statistics of the last render: paths, path segments (extension
+ * plus shadow rays), QBVH nodes visited, triangle tests, device milliseconds. */
+typedef struct pr_render_stats {
+  uint64_t paths;
+  uint64_t segments;
+  uint64_t nodes_visited;
+  uint64_t tri_tests;
+  double device_ms;
+} pr_render_stats;
+int pr_last_render_stats(pr_ctx* ctx, pr_render_stats* stats);
+
+/* ---- Kerr geodesics --------------------------------------------------- */
+/* The Kerr branch of intersect_scene (scene.cpp:448-732) for n camera rays
+ * (FP64, 6 per ray).  Per ray: status (0 reached background, 1 hit an
+ * entity, 2 event horizon, 3 initial-condition failure, 4 step underflow),
+ * final Boyer-Lindquist (r, theta, phi), final polyline direction, steps
+ * taken, hit entity and hit distance.  Host buffers. */
+int pr_kerr_trace(pr_ctx* ctx, const double* rays, int64_t n, int32_t* status,
+                  double* final_bl, double* exit_dir, int32_t* steps,
+                  int32_t* hit_entity, double* hit_t);
+int pr_kerr_trace_dev(pr_ctx* ctx, const double* rays, int64_t n, int32_t* status,
+                      double* final_bl, double* exit_dir, int32_t* steps,
+                      int32_t* hit_entity, double* hit_t);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PRENDER_GPU_H */

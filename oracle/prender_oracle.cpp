@@ -1,0 +1,1191 @@
+// CPU restatement of prender's radiance estimator — TEST INFRASTRUCTURE ONLY.
+//
+// The oracle the GPU path is checked against.  Every function cites the
+// reference file:line it restates (paths inside Sanaxen/prender, proj/).  It
+// is loaded only by tests/, the smoke check and bench.py's CPU-baseline leg;
+// the product never links or calls it.
+//
+// Arithmetic is FP64 in the reference's own operation order (see
+// oracle_math.h), so that with one thread and the same MT19937-64 seeds the
+// images equal the reference's bit for bit.
+#include <omp.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../include/prender_gpu.h"
+#include "oracle_math.h"
+
+using namespace orc;
+
+namespace {
+
+// ---------------------------------------------------------------- materials
+struct Medium {  // ParticipatingMediaPrm.h:85-131 (fields used on the path)
+  double scattering = 0, absorbing = 0, transmittance = 0;
+  V3 scatteringColor, absorbingColor, transmittanceColor, albedoColor;
+  double phase[3] = {0, 0, 0};
+  double eta = 0, r_max = 1;
+  int level = -1, use_bssrdf = 1;
+  // setup_Scattering (ParticipatingMediaPrm.h:133-160)
+  void setup(double material_scale) {
+    scatteringColor = scatteringColor * material_scale;
+    absorbingColor = absorbingColor * material_scale;
+    scattering = (scatteringColor.x + scatteringColor.y + scatteringColor.z) / 3;
+    absorbing = (absorbingColor.x + absorbingColor.y + absorbingColor.z) / 3;
+    transmittance = scattering + absorbing;
+    transmittanceColor = scatteringColor + absorbingColor;
+    if (transmittance < 1.0e-12) {
+      scattering = 0;
+      absorbing = 0;
+      transmittance = 0.0;
+      scatteringColor = V3(1.0, 1.0, 1.0);
+      absorbingColor = V3(1.0, 1.0, 1.0);
+      albedoColor = V3(1.0, 1.0, 1.0);
+    } else {
+      albedoColor = V3(scatteringColor.x / transmittanceColor.x, scatteringColor.y / transmittanceColor.y,
+                       scatteringColor.z / transmittanceColor.z);
+    }
+  }
+  // transmittanceRatio (ParticipatingMediaPrm.h:336-340)
+  V3 tr(double d) const { return vexp(-1.0 * transmittanceColor * d); }
+};
+
+struct Material {  // material.h:54-240
+  int type = PR_MAT_DIFFUSE;
+  V3 color, emission, specular;
+  double roughness = 0.0;
+  double refractive_index = 1.5;
+  Medium medium;
+  // Material::isLight (material.h): diffuse, dark, emissive
+  bool isLight() const {
+    return type == PR_MAT_DIFFUSE && length(color) < 0.001 && length(emission) > 0.001;
+  }
+};
+
+// ------------------------------------------------------------------ entities
+struct Hit {  // IntersectionPos (intersection.h:11-30) + object_id
+  double distance = INF;
+  V3 normal, position;
+  int material = -1;
+  int object_id = -1;
+  int prim = -1;
+};
+
+struct Mesh {
+  std::vector<float> vert;   // ObjLoader vert (float)
+  std::vector<int> face;     // 0-based
+  std::vector<float> fnorm;  // face normals (float, ObjLoader.cpp:577-700)
+};
+
+struct Tri {  // Triangle (polygon.h:22-708)
+  int mesh, face;
+  V3 bmin, bmax, center;  // padded bounding box and its centre
+};
+
+struct BVHNode {  // BVH_structure (BVH.h:18-28)
+  double box[2][3];
+  int children[2] = {-1, -1};
+  int axis = 0;
+  std::vector<int> objects;  // triangle indices (leaf only)
+};
+
+struct QNode {  // QBVH_structure (QBVH.h:53-61)
+  float bboxes[2][3][4];
+  int64_t children[4];
+  int axis_top, axis_left, axis_right;
+};
+
+constexpr int64_t QTOP = (int64_t)1 << 63;  // QBVH_TOP_BIT with 64-bit long (QBVH.h:11)
+
+struct QBVH {
+  std::vector<QNode> nodes;
+  std::vector<int> leaf;  // triangle index, -1 = terminator
+};
+
+struct Entity {
+  int type = 0, material = -1, normal_inverse = 1;
+  // sphere
+  V3 position;
+  double radius = 0;
+  // uvplane (plane.h:129-167)
+  V3 org, u_axis, v_axis, normal;
+  double u_length = 0, v_length = 0;
+  // circle
+  double radius_inner = 0;
+  // mesh
+  int mesh = -1;
+  std::vector<Tri> tris;
+  QBVH qbvh;
+  double area = INF;
+  bool light = false;
+  int light_id = -1;
+};
+
+struct Light {  // light.h:13-74 (area lights only)
+  double power = 0;
+  int entity = -1;
+};
+
+struct Scene {
+  std::vector<Material> mats;
+  std::vector<Entity> ents;
+  std::vector<Mesh> meshes;
+  std::vector<Light> lights;
+  V3 background, env_light;
+  Medium medium;
+  int media_on = 0;
+};
+
+thread_local uint64_t tl_nodes = 0, tl_tris = 0, tl_segments = 0;
+
+// -------------------------------------------------------------- primitives
+// Sphere::intersect core (sphere.h:68-96)
+bool sphere_hit(const Entity& e, V3 org, V3 dir, Hit& h) {
+  const V3 p_o = e.position - org;
+  const double b = dot(p_o, dir);
+  const double D4 = b * b - dot(p_o, p_o) + e.radius * e.radius;
+  if (D4 < 0.0) return false;
+  const double sqrt_D4 = std::sqrt(D4);
+  const double t1 = b - sqrt_D4, t2 = b + sqrt_D4;
+  if (t1 < EPS && t2 < EPS) return false;
+  h.distance = (t1 > EPS) ? t1 : t2;
+  h.position = org + h.distance * dir;
+  h.normal = normalize(h.position - e.position);
+  if (e.normal_inverse < 0) h.normal = h.normal * -1.0;
+  h.material = e.material;
+  return true;
+}
+
+// UVPlane::intersect (plane.h:220-239) over Plane::intersect (plane.h:86-110)
+bool uvplane_hit(const Entity& e, V3 org, V3 dir, Hit& h) {
+  V3 normal2 = e.normal;
+  if (e.normal_inverse < 0) normal2 = e.normal * -1.0;
+  const double d = dot(dir, normal2);
+  if (std::fabs(d) < EPS14) return false;
+  h.distance = dot((e.org - org), normal2) / d;
+  h.normal = normal2;
+  h.position = dir * h.distance + org;
+  h.material = e.material;
+  if (h.distance < EPS) return false;
+  const double u = dot(V3(h.position - e.org), e.u_axis) / e.u_length;
+  const double v = dot(V3(h.position - e.org), e.v_axis) / e.v_length;
+  if (u < 0 || u > e.u_length) return false;
+  if (v < 0 || v > e.v_length) return false;
+  return true;
+}
+
+inline V3 vtx(const Mesh& m, int id) {
+  return V3(m.vert[3 * id], m.vert[3 * id + 1], m.vert[3 * id + 2]);
+}
+
+// Triangle::CheckIntersection2 (polygon.h:78-129) + Triangle::intersect (:131-173)
+bool tri_hit(const Scene& s, const Entity& e, const Tri& tr, V3 org, V3 dir, Hit& h) {
+  tl_tris++;
+  const Mesh& m = s.meshes[tr.mesh];
+  const int* f = &m.face[3 * tr.face];
+  const V3 v0 = vtx(m, f[0]);
+  const V3 edge1 = vtx(m, f[1]) - v0;
+  const V3 edge2 = vtx(m, f[2]) - v0;
+  const V3 p = cross(dir, edge2);
+  const double det = dot(edge1, p);
+  const V3 tv = org - v0;
+  const V3 q = cross(tv, edge1);
+  const double eps = EPS * 0.1;
+  double inv_det, u, v;
+  if (det > eps) {
+    inv_det = 1.0 / det;
+    u = dot(tv, p);
+    if (u < 0.0 || u > det) return false;
+    v = dot(dir, q);
+    if (v < 0.0 || u + v > det) return false;
+  } else if (det < -eps) {
+    inv_det = 1.0 / det;
+    u = dot(tv, p);
+    if (u > 0.0 || u < det) return false;
+    v = dot(dir, q);
+    if (v > 0.0 || u + v < det) return false;
+  } else {
+    return false;
+  }
+  const double t = dot(edge2, q) * inv_det;
+  if (!(t > EPS)) return false;
+  h.distance = t;
+  h.position = org + dir * t;
+  h.normal = V3(m.fnorm[3 * tr.face], m.fnorm[3 * tr.face + 1], m.fnorm[3 * tr.face + 2]);
+  if (e.normal_inverse < 0) h.normal = h.normal * -1.0;
+  h.material = e.material;
+  h.prim = tr.face;
+  return true;
+}
+
+// --------------------------------------------------------------- SAH build
+// BoundingBox::CalcSurfaceArea member form (BoundingBox.h:29-33)
+inline double area_member(V3 mn, V3 mx) {
+  double dx = mx.x - mn.x, dy = mx.y - mn.y, dz = mx.z - mn.z;
+  return dx * dy + dx * dz + dy * dz;
+}
+// BoundingBox::CalcSurfaceArea template form (BoundingBox.h:35-39)
+inline double area_template(const double mn[3], const double mx[3]) {
+  double d[3] = {mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2]};
+  return d[0] * d[1] + d[1] * d[2] + d[0] * d[2];
+}
+
+struct Builder {
+  const std::vector<Tri>& tris;
+  std::vector<BVHNode> nodes;
+  explicit Builder(const std::vector<Tri>& t) : tris(t) {}
+
+  // CalcBoundingBoxOfObjects, Vector3d form (BVH.cpp:137-154)
+  void bbox(const std::vector<int>& objs, V3& mn, V3& mx) const {
+    mn = tris[objs[0]].bmin;
+    mx = tris[objs[0]].bmax;
+    for (size_t i = 1; i < objs.size(); i++) {
+      const Tri& a = tris[objs[i]];
+      if (a.bmin.x < mn.x) mn.x = a.bmin.x;
+      if (a.bmin.y < mn.y) mn.y = a.bmin.y;
+      if (a.bmin.z < mn.z) mn.z = a.bmin.z;
+      if (a.bmax.x > mx.x) mx.x = a.bmax.x;
+      if (a.bmax.y > mx.y) mx.y = a.bmax.y;
+      if (a.bmax.z > mx.z) mx.z = a.bmax.z;
+    }
+  }
+  // BoundingBox::MergeAnotherBox (BoundingBox.h:229-238)
+  static void merge(V3& mn, V3& mx, const Tri& b) {
+    mn.x = std::min(mn.x, b.bmin.x);
+    mn.y = std::min(mn.y, b.bmin.y);
+    mn.z = std::min(mn.z, b.bmin.z);
+    mx.x = std::max(mx.x, b.bmax.x);
+    mx.y = std::max(mx.y, b.bmax.y);
+    mx.z = std::max(mx.z, b.bmax.z);
+  }
+  void sort_axis(std::vector<int>& v, int axis) const {
+    const std::vector<Tri>& t = tris;
+    std::sort(v.begin(), v.end(), [&t, axis](int a, int b) -> bool {
+      return t[a].center[axis] < t[b].center[axis];
+    });
+  }
+  // BVH::Construct_internal, CONSTRUCTION_OBJECT_SAH (BVH.cpp:194-348)
+  void build(const std::vector<int>& targets, int index) {
+    {
+      V3 mn, mx;
+      bbox(targets, mn, mx);
+      nodes[index].box[0][0] = mn.x; nodes[index].box[0][1] = mn.y; nodes[index].box[0][2] = mn.z;
+      nodes[index].box[1][0] = mx.x; nodes[index].box[1][1] = mx.y; nodes[index].box[1][2] = mx.z;
+    }
+    const double surf = area_template(nodes[index].box[0], nodes[index].box[1]);
+    const double surf_inv = 1.0 / surf;
+    int bestAxis = -1, bestIndex = -1;
+    double bestCost = -1;
+    const size_t n = targets.size();
+    std::vector<double> leftAreas(n), rightAreas(n);
+    for (int axis = 0; axis < 3; axis++) {
+      std::vector<int> L = targets, R;
+      sort_axis(L, axis);
+      rightAreas[n - 1] = INF;
+      R.push_back(L.back());
+      L.pop_back();
+      V3 mn, mx;
+      bbox(R, mn, mx);
+      const int sz = (int)L.size();
+      for (int i = sz - 1; i >= 0; i--) {
+        rightAreas[i] = area_member(mn, mx);
+        merge(mn, mx, tris[L[i]]);
+        R.push_back(L.back());
+        L.pop_back();
+      }
+      L.push_back(R.back());
+      R.pop_back();
+      bbox(L, mn, mx);
+      const double leafCost = 1.0 * (double)n;
+      const int sz2 = (int)R.size();
+      for (int i = sz2 - 1, cut = 0; i >= 0; i--, cut++) {
+        leftAreas[cut] = area_member(mn, mx);
+        merge(mn, mx, tris[R.back()]);
+        L.push_back(R.back());
+        R.pop_back();
+        const double cost = 2 * 1.0 + (leftAreas[cut] * (double)L.size() + rightAreas[cut] * (double)R.size()) * surf_inv * 1.0;
+        if ((cost < bestCost || bestCost == -1) && cost < leafCost) {
+          bestCost = cost;
+          bestIndex = cut;
+          bestAxis = axis;
+        }
+      }
+    }
+    if (bestAxis == -1) {  // MakeLeaf_internal (BVH.cpp:181-191)
+      nodes[index].children[0] = nodes[index].children[1] = -1;
+      nodes[index].objects = targets;
+      return;
+    }
+    std::vector<int> lefts = targets;
+    sort_axis(lefts, bestAxis);
+    std::vector<int> rights(lefts.begin() + bestIndex + 1, lefts.end());
+    lefts.resize(bestIndex + 1);
+    nodes[index].axis = bestAxis;
+    const int c0 = (int)nodes.size();
+    nodes[index].children[0] = c0;
+    nodes[index].children[1] = c0 + 1;
+    nodes.emplace_back();
+    nodes.emplace_back();
+    build(lefts, c0);
+    build(rights, c0 + 1);
+  }
+};
+
+bool is_leaf(const BVHNode& n) { return n.children[0] == -1; }
+
+struct Flattener {  // QBVH::Construct_internal / MakeLeaf_internal (QBVH.cpp:202-302)
+  const std::vector<BVHNode>& bvh;
+  QBVH& q;
+  Flattener(const std::vector<BVHNode>& b, QBVH& qq) : bvh(b), q(qq) {}
+  void make_leaf(size_t index, const BVHNode& leaf, int childindex) {
+    const int64_t start = (int64_t)q.leaf.size();
+    for (int o : leaf.objects) q.leaf.push_back(o);
+    q.leaf.push_back(-1);
+    q.nodes[index].children[childindex] = QTOP | start;
+  }
+  void flatten(size_t nextindex, int target) {
+    const BVHNode& nt = bvh[target];
+    QNode& cur0 = q.nodes[nextindex];
+    memset(&cur0, 0, sizeof(QNode));
+    cur0.axis_top = nt.axis;
+    const BVHNode* ch[2] = {&bvh[nt.children[0]], &bvh[nt.children[1]]};
+    cur0.axis_left = is_leaf(*ch[0]) ? 0 : ch[0]->axis;
+    cur0.axis_right = is_leaf(*ch[1]) ? 0 : ch[1]->axis;
+    float four[2][3][4];
+    memset(four, 0, sizeof(four));
+    auto insert = [&four](const BVHNode& b, int slot) {
+      for (int xyz = 0; xyz < 3; xyz++) {
+        four[0][xyz][slot] = (float)b.box[0][xyz];
+        four[1][xyz][slot] = (float)b.box[1][xyz];
+      }
+    };
+    for (int i = 0; i < 2; i++) {
+      const BVHNode& child = *ch[i];
+      if (is_leaf(child)) {
+        const int slot = i * 2;
+        make_leaf(nextindex, child, slot);
+        q.nodes[nextindex].children[1 + slot] = -1;
+        insert(child, slot);
+      } else {
+        const BVHNode* gc[2] = {&bvh[child.children[0]], &bvh[child.children[1]]};
+        const int gci[2] = {child.children[0], child.children[1]};
+        for (int j = 0; j < 2; j++) {
+          const int slot = i * 2 + j;
+          insert(*gc[j], slot);
+          if (is_leaf(*gc[j])) {
+            make_leaf(nextindex, *gc[j], slot);
+          } else {
+            const size_t nn = q.nodes.size();
+            q.nodes.emplace_back();
+            q.nodes[nextindex].children[slot] = (int64_t)nn;
+            flatten(nn, gci[j]);
+          }
+        }
+      }
+    }
+    memcpy(q.nodes[nextindex].bboxes, four, sizeof(four));
+  }
+};
+
+// ------------------------------------------------------------ traversal
+// CheckIntersection4floatAABB (BoundingBox.h:137-178): SSE max/min return
+// the second operand when the comparison fails (NaN included).
+inline float mx_ps(float a, float b) { return a > b ? a : b; }
+inline float mn_ps(float a, float b) { return a < b ? a : b; }
+
+// QBVH::CheckIntersection + CheckIntersection_Leaf (QBVH.cpp:17-159)
+bool qbvh_hit(const Scene& s, const Entity& e, V3 org, V3 dir, Hit& out) {
+  const int sign[3] = {dir.x >= 0 ? 0 : 1, dir.y >= 0 ? 0 : 1, dir.z >= 0 ? 0 : 1};
+  const float ro[3] = {(float)org.x, (float)org.y, (float)org.z};
+  const float inf_f = (float)INF;
+  const float rid[3] = {dir.x == 0 ? inf_f : (float)(1.0f / dir.x), dir.y == 0 ? inf_f : (float)(1.0f / dir.y),
+                        dir.z == 0 ? inf_f : (float)(1.0f / dir.z)};
+  const float fmaxv = 3.402823466e+38F;
+  std::vector<int64_t> stack;
+  stack.push_back(0);
+  double dist = -1.0;
+  const QBVH& q = e.qbvh;
+  while (!stack.empty()) {
+    const int64_t ni = stack.back();
+    stack.pop_back();
+    const QNode& nd = q.nodes[(size_t)ni];
+    tl_nodes++;
+    bool res[4];
+    int any = 0;
+    for (int c = 0; c < 4; c++) {
+      float tmin = 0.0f, tmax = fmaxv;
+      for (int a = 0; a < 3; a++) {
+        tmin = mx_ps(tmin, (nd.bboxes[sign[a]][a][c] - ro[a]) * rid[a]);
+        tmax = mn_ps(tmax, (nd.bboxes[1 - sign[a]][a][c] - ro[a]) * rid[a]);
+      }
+      res[c] = tmax >= tmin;
+      any |= res[c];
+    }
+    if (!any) continue;
+    int order[4];
+    const bool isLeft = sign[nd.axis_top] == 0;
+    const int lf = isLeft ? 0 : 2;
+    const int rf = (lf + 2) % 4;
+    if (sign[nd.axis_left] == 0) { order[lf] = 0; order[lf + 1] = 1; }
+    else { order[lf] = 1; order[lf + 1] = 0; }
+    if (sign[nd.axis_right] == 0) { order[rf] = 2; order[rf + 1] = 3; }
+    else { order[rf] = 3; order[rf + 1] = 2; }
+    for (int i = 0; i < 4; i++) {
+      const int c = order[i];
+      const int64_t ch = nd.children[c];
+      if (!res[c] || ch == -1) continue;
+      if (ch & QTOP) {
+        const int64_t start = ch ^ QTOP;
+        double nearest = -1;
+        Hit tmp;
+        bool got = false;
+        for (int64_t k = start; q.leaf[(size_t)k] >= 0; k++) {
+          Hit h;
+          if (tri_hit(s, e, e.tris[q.leaf[(size_t)k]], org, dir, h) && h.distance > 0 &&
+              (nearest < 0 || h.distance < nearest)) {
+            tmp = h;
+            nearest = h.distance;
+            got = true;
+          }
+        }
+        if (got && tmp.distance > EPS) {
+          if (dist < 0 || dist > tmp.distance) {
+            out = tmp;
+            dist = out.distance;
+          }
+        }
+      } else {
+        stack.push_back(ch);
+      }
+    }
+  }
+  return dist > 0;
+}
+
+// intersect_scene_ without a black hole (scene.cpp:83-214)
+bool intersect(const Scene& s, V3 org, V3 dir, Hit& isect) {
+  tl_segments++;
+  isect = Hit();
+  isect.distance = INF;
+  isect.object_id = -1;
+  const V3 o2 = org + dir * 0.000001;
+  for (int i = 0; i < (int)s.ents.size(); i++) {
+    const Entity& e = s.ents[i];
+    Hit h;
+    bool got = false;
+    switch (e.type) {
+      case PR_ENT_SPHERE: got = sphere_hit(e, o2, dir, h); break;
+      case PR_ENT_UVPLANE: got = uvplane_hit(e, o2, dir, h); break;
+      case PR_ENT_POLYGON: got = qbvh_hit(s, e, o2, dir, h); break;
+      default: break;
+    }
+    if (got && h.distance < isect.distance) {
+      isect = h;
+      isect.object_id = i;
+    }
+  }
+  return isect.object_id >= 0;
+}
+
+// ------------------------------------------------------------------ setup
+int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
+  if (!d || d->n_entities < 0 || d->n_materials < 0 || d->n_meshes < 0) { err = "bad scene"; return PR_E_ARG; }
+  for (int i = 0; i < d->n_materials; i++) {
+    const pr_material& pm = d->materials[i];
+    Material m;
+    m.type = pm.type;
+    m.color = V3(pm.color[0], pm.color[1], pm.color[2]);
+    m.emission = V3(pm.emission[0], pm.emission[1], pm.emission[2]);
+    m.specular = V3(pm.specular[0], pm.specular[1], pm.specular[2]);
+    m.roughness = pm.roughness;
+    m.refractive_index = pm.refractive_index;
+    s.mats.push_back(m);
+  }
+  for (int i = 0; i < d->n_meshes; i++) {
+    const pr_mesh& pm = d->meshes[i];
+    Mesh m;
+    m.vert.assign(pm.vertices, pm.vertices + 3 * (size_t)pm.n_vertices);
+    m.face.assign(pm.faces, pm.faces + 3 * (size_t)pm.n_faces);
+    m.fnorm.resize(3 * (size_t)pm.n_faces);
+    if (pm.face_normals) {
+      memcpy(m.fnorm.data(), pm.face_normals, sizeof(float) * 3 * (size_t)pm.n_faces);
+    } else {
+      // Obj::CalcNormalVector, no 'vn' lines (ObjLoader.cpp:582-598, :686-697)
+      for (int f = 0; f < pm.n_faces; f++) {
+        const int* fc = &m.face[3 * f];
+        const float* V = m.vert.data();
+        float dx1 = V[3 * fc[1]] - V[3 * fc[0]], dy1 = V[3 * fc[1] + 1] - V[3 * fc[0] + 1],
+              dz1 = V[3 * fc[1] + 2] - V[3 * fc[0] + 2];
+        float dx2 = V[3 * fc[2]] - V[3 * fc[0]], dy2 = V[3 * fc[2] + 1] - V[3 * fc[0] + 1],
+              dz2 = V[3 * fc[2] + 2] - V[3 * fc[0] + 2];
+        float nx = dy1 * dz2 - dz1 * dy2, ny = dz1 * dx2 - dx1 * dz2, nz = dx1 * dy2 - dy1 * dx2;
+        float a = std::sqrt(nx * nx + ny * ny + nz * nz);
+        if (a != 0.0) { nx /= a; ny /= a; nz /= a; }
+        m.fnorm[3 * f] = nx; m.fnorm[3 * f + 1] = ny; m.fnorm[3 * f + 2] = nz;
+      }
+    }
+    s.meshes.push_back(std::move(m));
+  }
+  s.background = V3(d->background[0], d->background[1], d->background[2]);
+  s.env_light = V3(d->environment_light[0], d->environment_light[1], d->environment_light[2]);
+  s.medium.scatteringColor = V3(d->medium.sigma_s_rgb[0], d->medium.sigma_s_rgb[1], d->medium.sigma_s_rgb[2]);
+  s.medium.absorbingColor = V3(d->medium.sigma_a_rgb[0], d->medium.sigma_a_rgb[1], d->medium.sigma_a_rgb[2]);
+  for (int k = 0; k < 3; k++) s.medium.phase[k] = d->medium.phase_g[k];
+  s.medium.setup(1.0);  // scene_env.h:1892
+  s.media_on = d->participating_media && !(s.medium.transmittance < EPS12);  // scene_env.h:1893-1896
+
+  for (int i = 0; i < d->n_entities; i++) {
+    const pr_entity& pe = d->entities[i];
+    if (pe.material < 0 || pe.material >= (int)s.mats.size()) { err = "entity material out of range"; return PR_E_SCENE; }
+    Entity e;
+    e.type = pe.type;
+    e.material = pe.material;
+    e.normal_inverse = pe.normal_inverse < 0 ? -1 : 1;
+    const Material& m = s.mats[pe.material];
+    if (pe.type == PR_ENT_SPHERE) {
+      e.position = V3(pe.p[0], pe.p[1], pe.p[2]);
+      e.radius = pe.radius;
+      e.area = FORPI * e.radius * e.radius;  // Sphere::CalcArea (sphere.h:23-27)
+    } else if (pe.type == PR_ENT_UVPLANE) {  // UVPlane ctor (plane.h:146-167)
+      e.org = V3(pe.p[0], pe.p[1], pe.p[2]);
+      V3 U(pe.u[0], pe.u[1], pe.u[2]), V(pe.v[0], pe.v[1], pe.v[2]);
+      e.u_length = length(U);
+      e.v_length = length(V);
+      e.u_axis = normalize(U);
+      e.v_axis = normalize(V);
+      e.normal = normalize(cross(e.u_axis, e.v_axis));
+      // UVPlane::CalcArea (plane.h:174-177)
+      e.area = length(e.u_axis * e.u_length) * length(e.v_axis * e.v_length) *
+               (1.0 - std::pow(dot(e.u_axis, e.v_axis), 2.0));
+    } else if (pe.type == PR_ENT_POLYGON) {
+      if (pe.mesh < 0 || pe.mesh >= (int)s.meshes.size()) { err = "entity mesh out of range"; return PR_E_SCENE; }
+      e.mesh = pe.mesh;
+      const Mesh& mesh = s.meshes[pe.mesh];
+      const int nf = (int)mesh.face.size() / 3;
+      // Polygon::MakeTrianglesEntity + Triangle::CreateBoundingBox (polygon.h:686-703, :912-969)
+      for (int f = 0; f < nf; f++) {
+        Tri t;
+        t.mesh = pe.mesh;
+        t.face = f;
+        V3 mn(INF, INF, INF), mx(-INF, -INF, -INF);
+        for (int k = 0; k < 3; k++) {
+          V3 v = vtx(mesh, mesh.face[3 * f + k]);
+          if (mn.x > v.x) mn.x = v.x;
+          if (mn.y > v.y) mn.y = v.y;
+          if (mn.z > v.z) mn.z = v.z;
+          if (mx.x < v.x) mx.x = v.x;
+          if (mx.y < v.y) mx.y = v.y;
+          if (mx.z < v.z) mx.z = v.z;
+        }
+        const V3 eps(0.01, 0.01, 0.01);
+        t.bmin = mn - eps;
+        t.bmax = mx + eps;
+        t.center = (t.bmin + t.bmax) / 2.0;
+        e.tris.push_back(t);
+      }
+      if (nf == 0) { err = "empty mesh"; return PR_E_SCENE; }
+      // QBVH::Construct (QBVH.cpp:161-186)
+      Builder b(e.tris);
+      b.nodes.emplace_back();
+      std::vector<int> all(nf);
+      for (int f = 0; f < nf; f++) all[f] = f;
+      b.build(all, 0);
+      if (is_leaf(b.nodes[0])) { err = "mesh too small for a QBVH root (reference falls back to BVH)"; return PR_E_BUILD; }
+      e.qbvh.nodes.emplace_back();
+      Flattener fl(b.nodes, e.qbvh);
+      fl.flatten(0, 0);
+      if (m.isLight()) { err = "mesh lights are not sampled by the reference's NEE"; return PR_E_UNSUPPORTED; }
+    } else {
+      err = "entity type not supported by the oracle";
+      return PR_E_UNSUPPORTED;
+    }
+    s.ents.push_back(std::move(e));
+  }
+  // light registration (scene_env.h:1567-1586, :1692-1719) + random_light_setup sort (light.h:97)
+  for (int i = 0; i < (int)s.ents.size(); i++) {
+    Entity& e = s.ents[i];
+    const Material& m = s.mats[e.material];
+    if (m.isLight()) {
+      e.light = true;
+      Light l;
+      l.entity = i;
+      l.power = e.area * length(m.emission);
+      e.light_id = (int)s.lights.size();
+      s.lights.push_back(l);
+    }
+  }
+  std::sort(s.lights.begin(), s.lights.end(), [](const Light& a, const Light& b) { return a.power > b.power; });
+  for (int k = 0; k < (int)s.lights.size(); k++) s.ents[s.lights[k].entity].light_id = k;
+  return PR_OK;
+}
+
+// --------------------------------------------------------------- radiance
+struct Ctx {
+  const Scene& s;
+  MT64& rnd;
+  int nee, media;
+  int depth_cfg, depth_limit;
+  int hg_correct;
+};
+
+V3 radiance(Ctx& c, V3 org, V3 dir, int depth);
+
+// LightList::randomLight (light.h:132-155): probability reported as 1
+const Light& random_light(Ctx& c) {
+  const double next = c.rnd.next01();
+  const int n = (int)c.s.lights.size();
+  int index = (int)((next) * (double)(n - 1) + 0.5);
+  if (index >= n) index = n - 1;
+  if (index < 0) index = 0;
+  return c.s.lights[index];
+}
+
+// eval_direct_radiance for area lights and a diffuse receiver (directLight_radiance.h:19-313)
+V3 eval_direct(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, V3 light_pos, int depth) {
+  const Entity& le = c.s.ents[light.entity];
+  V3 light_normal;
+  double pdf = 1.0;
+  if (le.type == PR_ENT_SPHERE) {
+    light_normal = normalize(light_pos - le.position);
+    if (le.normal_inverse < 0) light_normal = light_normal * -1.0;
+    pdf = 1.0 / le.area;
+  } else if (le.type == PR_ENT_UVPLANE) {
+    light_normal = le.normal;
+    if (le.normal_inverse < 0) light_normal = light_normal * -1.0;
+    pdf = 1.0 / le.area;
+  }
+  V3 emission = c.s.mats[le.material].emission;
+  const V3 light_dir = normalize(light_pos - v0.position);
+  const double dist2 = sqr(light_pos - v0.position);
+  const double dot0 = dot(orienting_normal, light_dir);
+  const double dot1 = dot(light_normal, -1.0 * light_dir);
+  V3 rad;
+  if (dot0 >= 0 && dot1 >= 0) {
+    const double G = dot0 * dot1 / dist2;
+    Hit is;
+    const bool isect = intersect(c.s, v0.position, light_dir, is);
+    if (isect) {
+      const bool cond = std::fabs(std::sqrt(dist2) - is.distance) < 1e-3;
+      if (cond) {
+        if (is.object_id >= 0 && is.object_id != light.entity) return V3();
+        if (c.media) {  // env->participatingMedia (directLight_radiance.h:188-204)
+          const double t = length(v0.position - light_pos);
+          emission = emission * c.s.medium.tr(t);
+        }
+        rad = (emission * (c.s.mats[v0.material].color * INV_PI)) * G / pdf;
+      }
+    }
+  }
+  return rad;
+}
+
+// direct_radiance_sample (directLight_radiance.h:318-387), area lights
+V3 direct_sample(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, int depth) {
+  const Entity& le = c.s.ents[light.entity];
+  V3 light_pos;
+  if (le.type == PR_ENT_SPHERE) {
+    const double r1 = TWOPI * c.rnd.next01();
+    const double r2 = 1.0 - 2.0 * c.rnd.next01();
+    const double sq = std::sqrt(1.0 - r2 * r2);
+    light_pos = le.position + ((le.radius + EPS) * V3(sq * std::cos(r1), sq * std::sin(r1), r2));
+  } else if (le.type == PR_ENT_UVPLANE) {
+    const double t = le.v_length * c.rnd.next01();
+    const double s = le.u_length * c.rnd.next01();
+    light_pos = le.org + le.u_axis * s + le.v_axis * t + le.normal * EPS;
+  }
+  return eval_direct(c, light, v0, orienting_normal, light_pos, depth);
+}
+
+// direct_light_perfect_refrection (directLight_radiance.h:516-556), no
+// parallel/spot/infinity lights
+V3 direct_perfect(Ctx& c, V3 org, V3 dir, int depth) {
+  Hit lid;
+  const bool isect = intersect(c.s, org, dir, lid);
+  V3 d;
+  if (isect && c.s.ents[lid.object_id].light) {
+    d = c.s.mats[lid.material].emission;
+    if (c.media) d = c.s.medium.tr(lid.distance) * d;
+  }
+  return d;
+}
+
+// Entity::isInsideDir (entity.h:98-114); media_ignore_front_back is 0
+bool inside_dir(V3 normal, V3 raydir) {
+  const V3 on = dot(normal, raydir) < 0.0 ? normal : (-1.0 * normal);
+  return dot(on, normal) > 0;
+}
+
+// BRDF_Diffuse (brdf.h:408-700), no bump / shadow planes / IBL
+V3 brdf_diffuse(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, double p_scat, int depth) {
+  const Scene& s = c.s;
+  const Entity& obj = s.ents[ent];
+  const Material& mat = s.mats[hp.material];
+  const bool ins = inside_dir(hp.normal, raydir);
+  V3 emission = mat.emission;
+  V3 trr(1, 1, 1);
+  if (c.media) trr = s.medium.tr(hp.distance);
+  if (obj.light && obj.type == PR_ENT_UVPLANE) {
+    if (dot(hp.normal, raydir) >= 0.0) return V3();
+  }
+  if (c.nee) {
+    if (obj.light) {
+      if (depth == 0) return (trr * mat.emission) / p_rr / (1.0 - p_scat);
+      return V3();
+    }
+  } else if (obj.light) {
+    return (trr * mat.emission) / p_rr / (1.0 - p_scat);
+  }
+  V3 w, u, v;
+  onb(on, w, u, v);
+  const double r1 = TWOPI * c.rnd.next01();
+  const double r2 = c.rnd.next01(), r2s = std::sqrt(r2);
+  const V3 dir = normalize((u * std::cos(r1) * r2s + v * std::sin(r1) * r2s + w * std::sqrt(1.0 - r2)));
+  V3 incoming = radiance(c, hp.position, dir, depth + 1);
+  V3 weight = mat.color / p_rr / (1.0 - p_scat);
+  V3 direct;
+  if (c.nee && !s.lights.empty()) {
+    for (int i = 0; i < 3; i++) {  // SHADOW_RAY_SAMPLING (def.h:10)
+      const Light& l = random_light(c);
+      direct = direct + direct_sample(c, l, hp, on, depth) / 1.0;
+    }
+    direct = direct / 3;
+    direct = direct / p_rr / (1.0 - p_scat);
+  }
+  if (!c.nee && !s.lights.empty()) {
+    for (int i = 0; i < 3; i++) (void)random_light(c);  // only parallel/spot/infinity lights contribute
+    direct = direct / 3;
+    direct = direct / p_rr / (1.0 - p_scat);
+  }
+  if (c.media && ins) {
+    direct = trr * direct;
+    emission = trr * emission;
+    incoming = trr * incoming;
+  }
+  return s.env_light + emission + direct + weight * incoming;
+}
+
+// BRDF_Specular (brdf.h:702-761)
+V3 brdf_specular(Ctx& c, V3 raydir, const Hit& hp, double p_rr, double p_scat, int depth) {
+  const Scene& s = c.s;
+  const Material& mat = s.mats[hp.material];
+  const bool ins = inside_dir(hp.normal, raydir);
+  V3 emission = mat.emission;
+  V3 trr(1, 1, 1);
+  if (c.media) trr = s.medium.tr(hp.distance);
+  const V3 dir = normalize(raydir - hp.normal * 2.0 * dot(hp.normal, raydir));
+  V3 incoming = radiance(c, hp.position, dir, depth + 1);
+  V3 weight = mat.color / p_rr / (1.0 - p_scat);
+  if (c.nee) incoming = incoming + direct_perfect(c, hp.position, dir, depth);
+  if (c.media && ins) {
+    emission = trr * emission;
+    incoming = trr * incoming;
+  }
+  return s.env_light + emission + weight * incoming;
+}
+
+// BRDF_Refraction (brdf.h:763-953), no bump
+V3 brdf_refraction(Ctx& c, V3 raydir, const Hit& hp, int mat_type, V3 on, double p_rr, double p_scat, int depth) {
+  const Scene& s = c.s;
+  const Material& mat = s.mats[hp.material];
+  const bool ins = inside_dir(hp.normal, raydir);
+  V3 emission = mat.emission;
+  V3 trr(1, 1, 1);
+  if (c.media) trr = s.medium.tr(hp.distance);
+  V3 incoming, weight(1, 1, 1), direct, direct_r;
+  const V3 refl = normalize(raydir - hp.normal * 2.0 * dot(hp.normal, raydir));
+  const bool into = dot(hp.normal, on) > 0.0;
+  if (c.nee) direct = direct_perfect(c, hp.position, refl, depth);
+  const double nc = 1.0;
+  const double nt = mat.refractive_index;  // FORMULA0 (material.h)
+  const double nnt = into ? nc / nt : nt / nc;
+  const double ddn = dot(raydir, on);
+  const double cos2t = 1.0 - nnt * nnt * (1.0 - ddn * ddn);
+  if (cos2t < 0.0) {
+    incoming = radiance(c, hp.position, refl, depth + 1);
+    weight = mat.color / p_rr / (1.0 - p_scat);
+    incoming = incoming + direct;
+  } else {
+    const V3 tdir = normalize(raydir * nnt - hp.normal * (into ? 1.0 : -1.0) * (ddn * nnt + std::sqrt(std::fabs(cos2t))));
+    const double a = nt - nc, b = nt + nc;
+    const double R0 = (a * a) / (b * b);
+    const double cc = 1.0 - (into ? -ddn : dot(tdir, -1.0 * on));
+    double Re = R0 + (1.0 - R0) * std::pow(cc, 5.0);
+    const double nnt2 = std::pow(into ? nc / nt : nt / nc, 2.0);
+    double Tr = (1.0 - Re) * nnt2;
+    double probability = 0.25 + 0.5 * Re;
+    if (mat_type == PR_MAT_REFRACTION_FRESNEL) {
+      if (into) { probability = 1.0; Re = 1.0; Tr = 0.0; }
+      else { probability = 0.0; Re = 0.0; Tr = 1.0; }
+    }
+    if (c.nee) direct_r = direct_perfect(c, hp.position, tdir, depth);
+    if (depth > 2) {
+      if (c.rnd.next01() < probability) {
+        incoming = (radiance(c, hp.position, refl, depth + 1)) * Re;
+        weight = mat.color / (probability * p_rr) / (1.0 - p_scat);
+        incoming = incoming + direct;
+      } else {
+        incoming = (radiance(c, hp.position, tdir, depth + 1)) * Tr;
+        weight = mat.color / ((1.0 - probability) * p_rr) / (1.0 - p_scat);
+        incoming = incoming + direct_r;
+      }
+    } else {
+      // g++ evaluates the right operand of the reference's
+      // 'radiance(refl)*Re + radiance(tdir)*Tr' first (brdf.h:928-930)
+      const V3 l2 = radiance(c, hp.position, tdir, depth + 1);
+      const V3 l1 = radiance(c, hp.position, refl, depth + 1);
+      incoming = l1 * Re + l2 * Tr;
+      weight = mat.color / (p_rr) / (1.0 - p_scat);
+      incoming = incoming + direct + direct_r;
+    }
+  }
+  if (c.media && ins) {
+    emission = trr * emission;
+    incoming = trr * incoming;
+  }
+  return s.env_light + emission + weight * incoming;
+}
+
+// sampleSphere / sampleHG (sampler.h:24-93)
+V3 sample_sphere(Ctx& c) {
+  const double r1 = TWOPI * c.rnd.next01();
+  const double r2 = 1.0 - 2.0 * c.rnd.next01();
+  const double r22 = (r2 < 1.0) ? 1.0 - r2 * r2 : 0.0;
+  const double sq = std::sqrt(r22);
+  return normalize(V3(sq * std::cos(r1), sq * std::sin(r1), r2));
+}
+V3 sample_hg(Ctx& c, V3 raydir, double g) {
+  if (g == 0.0) return sample_sphere(c);
+  V3 w, u, v;
+  onb(raydir, w, u, v);
+  const double r1 = TWOPI * c.rnd.next01();
+  const double r2 = c.rnd.next01();
+  const double s = (1.0 - g * g) / (1.0 - g + 2.0 * g * r2);
+  // the reference parses (1.0 / 2.0*g) as (1/2)*g (sampler.h:55-56)
+  const double cost = c.hg_correct ? (1.0 / (2.0 * g)) * (1.0 + g * g - s * s) : (1.0 / 2.0 * g) * (1.0 + g * g - s * s);
+  const double sint = std::sqrt(std::max(0.0, 1.0 - cost * cost));
+  return normalize(sint * std::cos(r1) * u + sint * std::sin(r1) * v + cost * w);
+}
+// PhaseFunction_HenyeyGreenstein (phase.h:14-20)
+double phase_hg(double g, double costheta) {
+  const double w = 1.0 + g * g - 2.0 * g * costheta;
+  if (std::fabs(w) < EPS12) return 0.0;
+  return (INV_FORPI) * (1.0 - g * g) / std::pow(w, 3.0 / 2.0);
+}
+
+// eval_direct_radiance_media / direct_radiance_sample_media (ParticipatingMedia.h:27-268)
+V3 direct_media(Ctx& c, const Light& light, V3 pos, int depth) {
+  const Entity& le = c.s.ents[light.entity];
+  V3 light_pos, light_normal;
+  double pdf = 1.0;
+  if (le.type == PR_ENT_SPHERE) {
+    const double r1 = 2 * PI * c.rnd.next01();
+    const double r2 = 1.0 - 2.0 * c.rnd.next01();
+    light_pos = le.position + ((le.radius + EPS) * V3(std::sqrt(1.0 - r2 * r2) * std::cos(r1), std::sqrt(1.0 - r2 * r2) * std::sin(r1), r2));
+  } else if (le.type == PR_ENT_UVPLANE) {
+    const double t = le.v_length * c.rnd.next01();
+    const double s = le.u_length * c.rnd.next01();
+    light_pos = le.org + le.u_axis * s + le.v_axis * t;
+  }
+  const V3 trr = c.s.medium.tr(length(pos - light_pos));
+  // eval_direct_radiance_media
+  if (le.type == PR_ENT_SPHERE) {
+    light_normal = normalize(light_pos - le.position);
+    pdf = 1.0 / le.area;
+  } else {
+    light_normal = le.normal;
+    pdf = 1.0 / le.area;
+  }
+  const V3 emission = c.s.mats[le.material].emission;
+  const V3 light_dir = normalize(light_pos - pos);
+  const double dist2 = sqr(light_pos - pos);
+  const double dot1 = dot(light_normal, -1.0 * light_dir);
+  V3 rad;
+  if (dot1 >= 0) {
+    const double G = dot1 / dist2;
+    Hit is;
+    if (intersect(c.s, pos, light_dir, is)) {
+      if (std::fabs(std::sqrt(dist2) - is.distance) < 1e-3) {
+        if (!(is.object_id >= 0 && is.object_id != light.entity)) rad = emission * (1.0 / PI) * G / pdf;
+      }
+    }
+  }
+  return rad * trr;
+}
+
+// participatingMedia_radiance (ParticipatingMedia.h:300-461)
+V3 media_radiance(Ctx& c, V3 org, V3 raydir, const Hit& hp, int ent, double p_rr, double p_scat, int depth) {
+  const Scene& s = c.s;
+  const Medium& md = s.medium;
+  const Entity& obj = s.ents[ent];
+  const int select = std::min(2, (int)(3.0 * c.rnd.next01()));
+  const double u = c.rnd.next01();
+  const double d = -std::log(1.0 + u * (std::exp(-md.transmittance * hp.distance) - 1.0)) / md.transmittance;
+  const double pdf = std::exp(-md.transmittance * d) * (-md.transmittance / (std::exp(-md.transmittance * hp.distance) - 1.0));
+  V3 next_dir;
+  double phase;
+  const double g = md.phase[select];
+  if (g == 0.0 || std::fabs(g) > 1.0) {
+    next_dir = sample_sphere(c);
+    phase = INV_FORPI;
+  } else {
+    next_dir = sample_hg(c, raydir, g);
+    phase = phase_hg(g, dot(next_dir, raydir));
+  }
+  const double dirPdf = phase;
+  const V3 npos = org + d * raydir;
+  const V3 trr = md.tr(d);
+  V3 direct;
+  if (!obj.light) {
+    if (!s.lights.empty()) {
+      for (int i = 0; i < 3; i++) {
+        const Light& l = random_light(c);
+        direct = direct + direct_media(c, l, npos, depth) / 1.0;
+      }
+      direct = direct / 3;
+    }
+  }
+  if (pdf == 0.0) return V3();
+  if (obj.light) {
+    if (depth == 0) return trr * s.mats[hp.material].emission;
+    return V3();
+  }
+  V3 L = direct + radiance(c, npos, next_dir, depth + 1);
+  L = trr * md.scatteringColor * L * phase / pdf / dirPdf / p_scat / p_rr;
+  return L;
+}
+
+// radiance() (radiance.h:25-556): diffuse / specular / refraction / media
+V3 radiance(Ctx& c, V3 org, V3 dir, int depth) {
+  const Scene& s = c.s;
+  Hit hp;
+  if (!intersect(s, org, dir, hp)) return s.background;
+  const Material& mat = s.mats[hp.material];
+  const V3 on = dot(hp.normal, dir) < 0.0 ? hp.normal : (-1.0 * hp.normal);
+  V3 rw = mat.emission;
+  switch (mat.type) {
+    case PR_MAT_WARD: rw = rw + mat.color + mat.specular; break;
+    case PR_MAT_PHONG: rw = rw + mat.specular; break;
+    default: rw = rw + mat.color; break;
+  }
+  // RGB_MAX (def.h): std::max(x, std::max(y, z))
+  const double myz = (rw.y < rw.z) ? rw.z : rw.y;
+  double p_rr = (rw.x < myz) ? myz : rw.x;
+  if (depth > c.depth_limit) p_rr *= std::pow(0.5, depth - c.depth_limit);
+  if (depth > c.depth_cfg) {
+    if (c.rnd.next01() >= p_rr) {
+      V3 trr(1, 1, 1);
+      if (c.media) trr = s.medium.tr(hp.distance);
+      return trr * mat.emission;
+    }
+  } else {
+    p_rr = 1.0;
+  }
+  const bool from_outside = inside_dir(hp.normal, dir);
+  double p_scat = 0.0;
+  if (c.media && from_outside) {
+    p_scat = 1.0 - std::exp(-s.medium.scattering * hp.distance);
+    if (p_scat < 0.01) p_scat = 0.01;
+    else if (p_scat > 0.99) p_scat = 0.99;
+    if (c.rnd.next01() < p_scat) return media_radiance(c, org, dir, hp, hp.object_id, p_rr, p_scat, depth);
+  }
+  switch (mat.type) {
+    case PR_MAT_DIFFUSE:
+      if (c.rnd.next01() < mat.roughness) return brdf_diffuse(c, dir, hp, hp.object_id, on, p_rr, p_scat, depth);
+      return brdf_specular(c, dir, hp, p_rr, p_scat, depth);
+    case PR_MAT_SPECULAR:
+      if (c.rnd.next01() < 1.0 - mat.roughness) return brdf_specular(c, dir, hp, p_rr, p_scat, depth);
+      return brdf_diffuse(c, dir, hp, hp.object_id, on, p_rr, p_scat, depth);
+    case PR_MAT_REFRACTION:
+    case PR_MAT_REFRACTION_FRESNEL:
+      return brdf_refraction(c, dir, hp, mat.type, on, p_rr, p_scat, depth);
+    default:
+      return V3();
+  }
+}
+
+struct OracleScene {
+  Scene s;
+  std::string err;
+  uint64_t nodes = 0, tris = 0, segments = 0;
+};
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+void* oracle_scene_create(const pr_scene_desc* d, int* status, char* err, int errlen) {
+  auto* o = new OracleScene();
+  int st = build_scene(d, o->s, o->err);
+  if (status) *status = st;
+  if (st != PR_OK) {
+    if (err && errlen > 0) snprintf(err, errlen, "%s", o->err.c_str());
+    delete o;
+    return nullptr;
+  }
+  return o;
+}
+
+void oracle_scene_destroy(void* h) { delete static_cast<OracleScene*>(h); }
+
+int oracle_qbvh_info(void* h, int ent, int64_t* nn, int64_t* nl) {
+  auto* o = static_cast<OracleScene*>(h);
+  if (!o || ent < 0 || ent >= (int)o->s.ents.size() || o->s.ents[ent].type != PR_ENT_POLYGON) return PR_E_ARG;
+  *nn = (int64_t)o->s.ents[ent].qbvh.nodes.size();
+  *nl = (int64_t)o->s.ents[ent].qbvh.leaf.size();
+  return PR_OK;
+}
+
+int oracle_qbvh_export(void* h, int ent, float* boxes, int64_t* children, int32_t* axes, int32_t* leaf) {
+  auto* o = static_cast<OracleScene*>(h);
+  if (!o || ent < 0 || ent >= (int)o->s.ents.size() || o->s.ents[ent].type != PR_ENT_POLYGON) return PR_E_ARG;
+  const QBVH& q = o->s.ents[ent].qbvh;
+  for (size_t i = 0; i < q.nodes.size(); i++) {
+    memcpy(boxes + 24 * i, q.nodes[i].bboxes, 24 * sizeof(float));
+    for (int c = 0; c < 4; c++) children[4 * i + c] = q.nodes[i].children[c];
+    axes[3 * i] = q.nodes[i].axis_top;
+    axes[3 * i + 1] = q.nodes[i].axis_left;
+    axes[3 * i + 2] = q.nodes[i].axis_right;
+  }
+  for (size_t i = 0; i < q.leaf.size(); i++) {
+    const int t = q.leaf[i];
+    leaf[i] = t < 0 ? -1 : o->s.ents[ent].tris[t].face;
+  }
+  return PR_OK;
+}
+
+// intersect_scene_ per ray; also reports the QBVH face id, hit position and normal
+int oracle_first_hit(void* h, const double* rays, int64_t n, int32_t* ent, int32_t* prim, double* t,
+                     double* pos, double* nrm, uint64_t* nodes_visited, uint64_t* tri_tests) {
+  auto* o = static_cast<OracleScene*>(h);
+  if (!o || !rays || n < 0) return PR_E_ARG;
+  tl_nodes = tl_tris = 0;
+  for (int64_t k = 0; k < n; k++) {
+    const double* r = rays + 6 * k;
+    Hit hit;
+    const bool got = intersect(o->s, V3(r[0], r[1], r[2]), V3(r[3], r[4], r[5]), hit);
+    ent[k] = got ? hit.object_id : -1;
+    prim[k] = got ? hit.prim : -1;
+    t[k] = got ? hit.distance : -1.0;
+    if (pos) { pos[3 * k] = hit.position.x; pos[3 * k + 1] = hit.position.y; pos[3 * k + 2] = hit.position.z; }
+    if (nrm) { nrm[3 * k] = hit.normal.x; nrm[3 * k + 1] = hit.normal.y; nrm[3 * k + 2] = hit.normal.z; }
+  }
+  if (nodes_visited) *nodes_visited = tl_nodes;
+  if (tri_tests) *tri_tests = tl_tris;
+  return PR_OK;
+}
+
+// radiance() roots from one MT19937-64 stream (the reference harness' 'radiance' command)
+int oracle_radiance(void* h, const double* rays, int64_t n, uint64_t seed, const pr_render_params* prm, double* out) {
+  auto* o = static_cast<OracleScene*>(h);
+  if (!o || !rays || !prm || n < 0) return PR_E_ARG;
+  MT64 rnd(seed);
+  Ctx c{o->s, rnd, prm->nee, prm->media && o->s.media_on, prm->depth, prm->depth_limit, (prm->flags & PR_FLAG_HG_CORRECT) != 0};
+  for (int64_t k = 0; k < n; k++) {
+    const double* r = rays + 6 * k;
+    const V3 v = radiance(c, V3(r[0], r[1], r[2]), V3(r[3], r[4], r[5]), 0);
+    out[3 * k] = v.x; out[3 * k + 1] = v.y; out[3 * k + 2] = v.z;
+  }
+  return PR_OK;
+}
+
+// Render::Run (render.h:1125-1455) over rows [row0, row1): per-thread MT
+// streams seeded thread_id+1, OpenMP dynamic rows, tent filter, luminance
+// cutoff and sensor response.  image: W*H*3 doubles (reference row order).
+// With threads == 1 the result equals the reference bit for bit.
+int oracle_render(void* h, const pr_camera* cam, const pr_render_params* prm, int threads, int row0, int row1,
+                  double* image, double* seconds, uint64_t* segments) {
+  auto* o = static_cast<OracleScene*>(h);
+  if (!o || !cam || !prm || !image || threads < 1) return PR_E_ARG;
+  const Scene& s = o->s;
+  const int W = cam->width, H = cam->height;
+  if (row0 < 0) row0 = 0;
+  if (row1 <= 0 || row1 > H) row1 = H;
+  // CameraScreenPram (render.h:105-150)
+  V3 cpos(cam->position[0], cam->position[1], cam->position[2]);
+  V3 cdir(cam->dir[0], cam->dir[1], cam->dir[2]);
+  const V3 cup(cam->up[0], cam->up[1], cam->up[2]);
+  double cam_phi = std::atan2(cdir.y, cdir.x);
+  if (cam_phi < 0.0) cam_phi += 2.0 * PI;
+  if (std::fabs(cam_phi - PI) < 1.0e-6 || cam_phi < 1.0e-6 || std::fabs(cam_phi - 2.0 * PI) < 1.0e-6) {
+    cdir.y += 1.0e-6;
+    const double len = std::sqrt(cdir.x * cdir.x + cdir.y * cdir.y + cdir.z * cdir.z);
+    cdir.x /= len; cdir.y /= len; cdir.z /= len;
+  }
+  const double sw = cam->screen_width * W / H;
+  const double sh = cam->screen_height;
+  const V3 sx = normalize(cross(cdir, cup)) * sw;
+  const V3 sy = normalize(cross(sx, cdir)) * sh;
+  const V3 center = cpos + cdir * cam->screen_dist;
+  const double iw = 1.0 / W, ih = 1.0 / H;
+  int samples = prm->samples, ss = prm->supersamples;
+  double rate = (1.0 / ss);
+  if (prm->tent_filter) { samples = samples * (ss * ss); ss = 1; rate = 0.5; }
+  const double smp = 1.0 / samples / (ss * ss);
+  const float cutoff = (float)prm->luminance_cutoff;
+  std::vector<V3> img((size_t)W * H);
+  std::vector<std::unique_ptr<MT64>> rnd;
+  for (int i = 0; i < threads; i++) rnd.emplace_back(new MT64((uint64_t)(unsigned)(i + 1)));
+  std::atomic<uint64_t> seg_total(0);
+  const auto t0 = std::chrono::steady_clock::now();
+  for (int sidx = 0; sidx < samples; sidx++) {
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
+    for (int y = row0; y < row1; y++) {
+      const int tid = omp_get_thread_num();
+      tl_segments = 0;
+      Ctx c{s, *rnd[tid], prm->nee, prm->media && s.media_on, prm->depth, prm->depth_limit,
+            (prm->flags & PR_FLAG_HG_CORRECT) != 0};
+      for (int x = 0; x < W; x++) {
+        const int idx = (H - y - 1) * W + x;
+        for (int syy = 0; syy < ss; syy++) {
+          for (int sxx = 0; sxx < ss; sxx++) {
+            V3 acc;
+            double dx = 0, dy = 0;
+            if (prm->tent_filter) {
+              const double rr1 = 2.0 * c.rnd.next01();
+              const double rr2 = 2.0 * c.rnd.next01();
+              dx = rr1 < 1.0 ? std::sqrt(rr1) - 1.0 : 1.0 - std::sqrt(2.0 - rr1);
+              dy = rr2 < 1.0 ? std::sqrt(rr2) - 1.0 : 1.0 - std::sqrt(2.0 - rr2);
+            }
+            const double r1 = (sxx + 0.5 + dx) * rate;
+            const double r2 = (syy + 0.5 + dy) * rate;
+            const V3 sp = center + sx * ((r1 + x) * iw - 0.5) + sy * ((r2 + y) * ih - 0.5);
+            const V3 dir = normalize(sp - cpos);
+            const V3 v = radiance(c, cpos, dir, 0) * smp;
+            acc = acc + v * 1.0;
+            if (cutoff > 0.0) {  // render.h:1375-1384
+              const float lum = (float)dot(V3(0.2126, 0.7152, 0.0722), acc);
+              if (lum > cutoff) {
+                const float xs = cutoff / lum;
+                acc = acc * (double)xs;
+              }
+            }
+            img[idx] = img[idx] + acc;
+          }
+        }
+      }
+      seg_total += tl_segments;
+    }
+  }
+  for (size_t i = 0; i < img.size(); i++) img[i] = img[i] * prm->sensor_response;
+  const auto t1 = std::chrono::steady_clock::now();
+  if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+  if (segments) *segments = seg_total.load();
+  for (size_t i = 0; i < img.size(); i++) {
+    image[3 * i] = img[i].x; image[3 * i + 1] = img[i].y; image[3 * i + 2] = img[i].z;
+  }
+  return PR_OK;
+}
+
+int oracle_light_count(void* h) {
+  auto* o = static_cast<OracleScene*>(h);
+  return o ? (int)o->s.lights.size() : -1;
+}
+
+}  // extern "C"

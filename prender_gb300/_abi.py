@@ -1,0 +1,159 @@
+"""ctypes mirror of include/prender_gpu.h (the C ABI).
+
+Field order and types must match the header exactly; tests check the sizes
+against the shared library's own sizeof report.
+"""
+import ctypes as C
+
+PR_OK = 0
+PR_E_ARG = -1
+PR_E_CUDA = -2
+PR_E_SCENE = -3
+PR_E_BUILD = -4
+PR_E_DEVICE = -5
+PR_E_NOMEM = -6
+PR_E_UNSUPPORTED = -7
+
+# material.h:19-29 ReflectionType
+PR_MAT_DIFFUSE = 0
+PR_MAT_SPECULAR = 1
+PR_MAT_REFRACTION = 2
+PR_MAT_WARD = 3
+PR_MAT_PHONG = 4
+PR_MAT_SSS_REFRACTION = 5
+PR_MAT_SSS_DIFFUSE = 6
+PR_MAT_SSS_WARD = 7
+PR_MAT_REFRACTION_FRESNEL = 8
+
+# entity.h:18-25 EntityType
+PR_ENT_SPHERE = 1
+PR_ENT_UVPLANE = 3
+PR_ENT_CIRCLE = 4
+PR_ENT_POLYGON = 5
+
+PR_MODE_MEGAKERNEL = 0
+PR_MODE_WAVEFRONT = 1
+
+PR_FLAG_HG_CORRECT = 1
+PR_FLAG_EXACT_HITS = 2
+
+D3 = C.c_double * 3
+
+
+class pr_medium(C.Structure):
+    _fields_ = [
+        ("sigma_s_rgb", D3),
+        ("sigma_a_rgb", D3),
+        ("phase_g", D3),
+        ("eta", C.c_double),
+        ("scale", C.c_double),
+        ("r_max", C.c_double),
+        ("level", C.c_int32),
+        ("use_bssrdf", C.c_int32),
+    ]
+
+
+class pr_material(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32),
+        ("pad0", C.c_int32),
+        ("color", D3),
+        ("emission", D3),
+        ("specular", D3),
+        ("roughness", C.c_double),
+        ("refractive_index", C.c_double),
+        ("medium", pr_medium),
+    ]
+
+
+class pr_entity(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32),
+        ("material", C.c_int32),
+        ("normal_inverse", C.c_int32),
+        ("mesh", C.c_int32),
+        ("p", D3),
+        ("radius", C.c_double),
+        ("u", D3),
+        ("v", D3),
+        ("normal", D3),
+        ("radius_inner", C.c_double),
+    ]
+
+
+class pr_mesh(C.Structure):
+    _fields_ = [
+        ("n_vertices", C.c_int32),
+        ("n_faces", C.c_int32),
+        ("vertices", C.POINTER(C.c_float)),
+        ("faces", C.POINTER(C.c_int32)),
+        ("face_normals", C.POINTER(C.c_float)),
+    ]
+
+
+class pr_kerr(C.Structure):
+    _fields_ = [
+        ("enabled", C.c_int32),
+        ("max_steps", C.c_int32),
+        ("position", D3),
+        ("a", C.c_double),
+        ("map_coef", C.c_double * 4),
+        ("escape_radius", C.c_double),
+    ]
+
+
+class pr_scene_desc(C.Structure):
+    _fields_ = [
+        ("n_materials", C.c_int32),
+        ("n_entities", C.c_int32),
+        ("n_meshes", C.c_int32),
+        ("participating_media", C.c_int32),
+        ("materials", C.POINTER(pr_material)),
+        ("entities", C.POINTER(pr_entity)),
+        ("meshes", C.POINTER(pr_mesh)),
+        ("background", D3),
+        ("environment_light", D3),
+        ("medium", pr_medium),
+        ("kerr", pr_kerr),
+    ]
+
+
+class pr_camera(C.Structure):
+    _fields_ = [
+        ("position", D3),
+        ("dir", D3),
+        ("up", D3),
+        ("screen_width", C.c_double),
+        ("screen_height", C.c_double),
+        ("screen_dist", C.c_double),
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+    ]
+
+
+class pr_render_params(C.Structure):
+    _fields_ = [
+        ("samples", C.c_int32),
+        ("supersamples", C.c_int32),
+        ("tent_filter", C.c_int32),
+        ("depth", C.c_int32),
+        ("depth_limit", C.c_int32),
+        ("nee", C.c_int32),
+        ("media", C.c_int32),
+        ("mode", C.c_int32),
+        ("seed", C.c_uint64),
+        ("luminance_cutoff", C.c_double),
+        ("sensor_response", C.c_double),
+        ("max_path_vertices", C.c_int32),
+        ("flags", C.c_int32),
+    ]
+
+
+class pr_render_stats(C.Structure):
+    _fields_ = [
+        ("paths", C.c_uint64),
+        ("segments", C.c_uint64),
+        ("nodes_visited", C.c_uint64),
+        ("tri_tests", C.c_uint64),
+        ("device_ms", C.c_double),
+    ]

@@ -1,0 +1,358 @@
+"""Scene description with the semantics of prender's SceneEnv.
+
+Mirrors the OBJECT / global keywords of the reference's scene format
+(scene_env.h:357-2160): materials follow the reference's defaults (diffuse
+type with roughness 0 unless 'reflection diffuse' sets 1, glass IOR 1.5),
+lights are entities whose material passes Material::isLight (material.h),
+and the camera follows CameraScreenPram (render.h:105-150) with the
+CAMERA_ANGLE rule (scene_env.h:1881-1886).
+
+A Scene can be handed to the GPU library (``to_desc``) and written out in
+the reference's own text format (``write_reference``), so that the same
+bytes drive both.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _abi as A
+
+
+@dataclass
+class Medium:
+    """Homogeneous medium (ParticipatingMediaPrm.h:85-131)."""
+    sigma_s_rgb: Sequence[float] = (0.0, 0.0, 0.0)
+    sigma_a_rgb: Sequence[float] = (0.0, 0.0, 0.0)
+    phase_g: Sequence[float] = (0.0, 0.0, 0.0)
+    eta: float = 0.0
+    scale: float = 1.0
+    r_max: float = 1.0
+    level: int = -1
+    use_bssrdf: int = 1
+
+    def to_c(self) -> A.pr_medium:
+        m = A.pr_medium()
+        m.sigma_s_rgb[:] = [float(x) for x in self.sigma_s_rgb]
+        m.sigma_a_rgb[:] = [float(x) for x in self.sigma_a_rgb]
+        m.phase_g[:] = [float(x) for x in self.phase_g]
+        m.eta, m.scale, m.r_max = float(self.eta), float(self.scale), float(self.r_max)
+        m.level, m.use_bssrdf = int(self.level), int(self.use_bssrdf)
+        return m
+
+
+@dataclass
+class Material:
+    """Material (material.h:54-240); defaults are the reference's."""
+    type: int = A.PR_MAT_DIFFUSE
+    color: Sequence[float] = (0.0, 0.0, 0.0)
+    emission: Sequence[float] = (0.0, 0.0, 0.0)
+    specular: Sequence[float] = (0.0, 0.0, 0.0)
+    roughness: float = 0.0
+    refractive_index: float = 1.5
+    medium: Medium = field(default_factory=Medium)
+
+    @staticmethod
+    def diffuse(color, emission=(0.0, 0.0, 0.0)) -> "Material":
+        """'reflection diffuse' (scene_env.h:1444-1448): roughness 1."""
+        return Material(A.PR_MAT_DIFFUSE, tuple(color), tuple(emission), roughness=1.0)
+
+    @staticmethod
+    def mirror(color) -> "Material":
+        """'reflection specular' (scene_env.h:1486-1490): roughness 0."""
+        return Material(A.PR_MAT_SPECULAR, tuple(color), roughness=0.0)
+
+    @staticmethod
+    def glass(color, ior: float = 1.5) -> "Material":
+        """'reflection reflection' (scene_env.h:1450-1458)."""
+        return Material(A.PR_MAT_REFRACTION, tuple(color), refractive_index=ior)
+
+    def is_light(self) -> bool:
+        """Material::isLight (material.h)."""
+        return (self.type == A.PR_MAT_DIFFUSE and math.sqrt(sum(c * c for c in self.color)) < 0.001
+                and math.sqrt(sum(e * e for e in self.emission)) > 0.001)
+
+    def to_c(self) -> A.pr_material:
+        m = A.pr_material()
+        m.type = int(self.type)
+        m.color[:] = [float(x) for x in self.color]
+        m.emission[:] = [float(x) for x in self.emission]
+        m.specular[:] = [float(x) for x in self.specular]
+        m.roughness = float(self.roughness)
+        m.refractive_index = float(self.refractive_index)
+        m.medium = self.medium.to_c()
+        return m
+
+
+@dataclass
+class Entity:
+    type: int
+    material: int
+    normal_inverse: int = 1
+    mesh: int = -1
+    p: Sequence[float] = (0.0, 0.0, 0.0)
+    radius: float = 0.0
+    u: Sequence[float] = (0.0, 0.0, 0.0)
+    v: Sequence[float] = (0.0, 0.0, 0.0)
+    normal: Sequence[float] = (0.0, 0.0, 1.0)
+    radius_inner: float = 0.0
+
+    def to_c(self) -> A.pr_entity:
+        e = A.pr_entity()
+        e.type, e.material, e.normal_inverse, e.mesh = self.type, self.material, self.normal_inverse, self.mesh
+        e.p[:] = [float(x) for x in self.p]
+        e.radius = float(self.radius)
+        e.u[:] = [float(x) for x in self.u]
+        e.v[:] = [float(x) for x in self.v]
+        e.normal[:] = [float(x) for x in self.normal]
+        e.radius_inner = float(self.radius_inner)
+        return e
+
+
+@dataclass
+class Mesh:
+    vertices: np.ndarray  # (n, 3) float32
+    faces: np.ndarray     # (m, 3) int32, 0-based
+
+    def __post_init__(self):
+        self.vertices = np.ascontiguousarray(self.vertices, dtype=np.float32)
+        self.faces = np.ascontiguousarray(self.faces, dtype=np.int32)
+
+
+@dataclass
+class Camera:
+    """SceneEnv camera fields (scene_env.h:170-178) with the reference defaults."""
+    position: Sequence[float] = (50.0, 52.0, 220.0)
+    dir: Sequence[float] = (0.0, -0.04, -1.0)
+    up: Sequence[float] = (0.0, 1.0, 0.0)
+    screen: Sequence[float] = (30.0, 30.0, 40.0)  # SCREEN w h dist
+    angle: Optional[float] = None                 # CAMERA_ANGLE (degrees)
+    width: int = 320
+    height: int = 240
+
+    def to_c(self) -> A.pr_camera:
+        c = A.pr_camera()
+        c.position[:] = [float(x) for x in self.position]
+        d = np.asarray(self.dir, dtype=np.float64)
+        # SceneEnv::Load normalises camera_dir at the end (scene_env.h:1920)
+        ln = math.sqrt((d[0] * d[0] + d[2] * d[2]) + d[1] * d[1])
+        c.dir[:] = [float(x * (1.0 / ln)) for x in d]
+        c.up[:] = [float(x) for x in self.up]
+        w, h, dist = (float(x) for x in self.screen)
+        if self.angle is not None:  # scene_env.h:1881-1886
+            w = 2.0 * dist * math.tan(self.angle * (math.pi / 180.0) / 2.0)
+            h = w
+        c.screen_width, c.screen_height, c.screen_dist = w, h, dist
+        c.width, c.height = int(self.width), int(self.height)
+        return c
+
+
+@dataclass
+class RenderSettings:
+    """Render::Run inputs (render.h:1125-1200) with the reference defaults
+    (scene_env.h:262-350; luminance_cutoff 0.025, scene_env.h:221)."""
+    samples: int = 8
+    supersamples: int = 2
+    tent_filter: int = 0
+    depth: int = 8
+    depth_limit: int = 64
+    nee: int = 0
+    media: int = 0
+    mode: int = A.PR_MODE_MEGAKERNEL
+    seed: int = 0
+    luminance_cutoff: float = 0.025
+    sensor_response: float = 1.0
+    max_path_vertices: int = 0
+    flags: int = 0
+
+    def to_c(self) -> A.pr_render_params:
+        p = A.pr_render_params()
+        for k in ("samples", "supersamples", "tent_filter", "depth", "depth_limit", "nee", "media", "mode",
+                  "max_path_vertices", "flags"):
+            setattr(p, k, int(getattr(self, k)))
+        p.seed = int(self.seed)
+        p.luminance_cutoff = float(self.luminance_cutoff)
+        p.sensor_response = float(self.sensor_response)
+        return p
+
+    @property
+    def spp(self) -> int:
+        return self.samples * self.supersamples * self.supersamples
+
+
+class SceneDesc:
+    """Holds a pr_scene_desc and every buffer it points to."""
+
+    def __init__(self, scene: "Scene"):
+        self._mats = (A.pr_material * max(1, len(scene.materials)))(*[m.to_c() for m in scene.materials])
+        self._ents = (A.pr_entity * max(1, len(scene.entities)))(*[e.to_c() for e in scene.entities])
+        self._mesh_arrays = []
+        meshes = []
+        for m in scene.meshes:
+            v = np.ascontiguousarray(m.vertices, dtype=np.float32)
+            f = np.ascontiguousarray(m.faces, dtype=np.int32)
+            self._mesh_arrays += [v, f]
+            pm = A.pr_mesh()
+            pm.n_vertices, pm.n_faces = v.shape[0], f.shape[0]
+            pm.vertices = v.ctypes.data_as(C.POINTER(C.c_float))
+            pm.faces = f.ctypes.data_as(C.POINTER(C.c_int32))
+            pm.face_normals = None
+            meshes.append(pm)
+        self._meshes = (A.pr_mesh * max(1, len(meshes)))(*meshes)
+        d = A.pr_scene_desc()
+        d.n_materials, d.n_entities, d.n_meshes = len(scene.materials), len(scene.entities), len(scene.meshes)
+        d.participating_media = int(scene.participating_media)
+        d.materials = C.cast(self._mats, C.POINTER(A.pr_material))
+        d.entities = C.cast(self._ents, C.POINTER(A.pr_entity))
+        d.meshes = C.cast(self._meshes, C.POINTER(A.pr_mesh))
+        d.background[:] = [float(x) for x in scene.background]
+        d.environment_light[:] = [float(x) for x in scene.environment_light]
+        d.medium = scene.medium.to_c()
+        k = A.pr_kerr()
+        if scene.kerr is not None:
+            k.enabled = 1
+            k.max_steps = int(scene.kerr["max_steps"])
+            k.position[:] = [float(x) for x in scene.kerr["position"]]
+            k.a = float(scene.kerr["a"])
+            k.map_coef[:] = [float(x) for x in scene.kerr.get("map_coef", (1.0, 0.0, 1.0, 0.0))]
+            k.escape_radius = float(scene.kerr.get("escape_radius", 0.0))
+        d.kerr = k
+        self.desc = d
+
+    def ptr(self):
+        return C.byref(self.desc)
+
+
+@dataclass
+class Scene:
+    materials: List[Material] = field(default_factory=list)
+    entities: List[Entity] = field(default_factory=list)
+    meshes: List[Mesh] = field(default_factory=list)
+    background: Sequence[float] = (0.0, 0.0, 0.0)
+    environment_light: Sequence[float] = (0.0, 0.0, 0.0)
+    participating_media: int = 0
+    medium: Medium = field(default_factory=Medium)
+    kerr: Optional[dict] = None
+    camera: Camera = field(default_factory=Camera)
+    settings: RenderSettings = field(default_factory=RenderSettings)
+
+    # ---- building (one OBJECT block each) ----
+    def _mat(self, m: Material) -> int:
+        self.materials.append(m)
+        return len(self.materials) - 1
+
+    def add_sphere(self, center, radius, material: Material, normal_inverse: int = 1) -> int:
+        self.entities.append(Entity(A.PR_ENT_SPHERE, self._mat(material), normal_inverse, p=tuple(center),
+                                    radius=float(radius)))
+        return len(self.entities) - 1
+
+    def add_uvplane(self, org, U, V, material: Material, normal_inverse: int = 1) -> int:
+        self.entities.append(Entity(A.PR_ENT_UVPLANE, self._mat(material), normal_inverse, p=tuple(org),
+                                    u=tuple(U), v=tuple(V)))
+        return len(self.entities) - 1
+
+    def add_mesh(self, vertices, faces, material: Material, normal_inverse: int = 1) -> int:
+        self.meshes.append(Mesh(vertices, faces))
+        self.entities.append(Entity(A.PR_ENT_POLYGON, self._mat(material), normal_inverse,
+                                    mesh=len(self.meshes) - 1))
+        return len(self.entities) - 1
+
+    def to_desc(self) -> SceneDesc:
+        return SceneDesc(self)
+
+    # ---- reference text format ----
+    def write_reference(self, directory: str, name: str = "scene.txt", threads: int = 1) -> str:
+        """Writes the scene in the reference's text format (scene_env.h
+        keywords) plus one OBJ per mesh; returns the scene file path."""
+        os.makedirs(directory, exist_ok=True)
+        cam, st = self.camera, self.settings
+
+        def f3(v):
+            return " ".join(_fmt(x) for x in v)
+
+        out = [
+            "IMAGE", f"{cam.width} {cam.height}", "",
+            "THREAD", str(threads), "",
+            "OUTPUT", "out.bmp", "",
+            "SCREEN", f3(cam.screen), "",
+            "SAMPLING", str(st.samples), "",
+            "SUPERSAMPLING", str(st.supersamples), "",
+            "tentfilter", str(st.tent_filter), "",
+            "DEPTH", str(st.depth), "",
+            "DEPTH_LIMIT", str(st.depth_limit), "",
+            "luminance_cutoff", _fmt(st.luminance_cutoff), "",
+            "sensor_response", _fmt(st.sensor_response), "",
+            "nextEventEstimation", str(st.nee), "",
+            "participatingMedia", str(int(self.participating_media and st.media)), "",
+            "CAMERA_POS", f3(cam.position), "",
+            "CAMERA_DIR", f3(cam.dir), "",
+            "CAMERA_UPVEC", f3(cam.up), "",
+            "BACKGROUND", f3(self.background), "",
+            "ENVLIGHT", f3(self.environment_light), "",
+        ]
+        if cam.angle is not None:
+            out += ["CAMERA_ANGLE", _fmt(cam.angle), ""]
+        md = self.medium
+        out += ["SCATTERING", "0", f3(md.sigma_s_rgb), "",
+                "ABSORBING", "0", f3(md.sigma_a_rgb), "",
+                f"PAHASE {f3(md.phase_g)}", ""]
+        refl = {A.PR_MAT_DIFFUSE: "reflection diffuse", A.PR_MAT_SPECULAR: "reflection specular",
+                A.PR_MAT_REFRACTION: "reflection reflection"}
+        for ei, e in enumerate(self.entities):
+            m = self.materials[e.material]
+            out.append("OBJECT")
+            if e.type == A.PR_ENT_SPHERE:
+                out.append(f"sphere {f3(e.p)} {_fmt(e.radius)}")
+            elif e.type == A.PR_ENT_UVPLANE:
+                out += [f"uvplane {f3(e.p)}", f"U {f3(e.u)}", f"V {f3(e.v)}"]
+            elif e.type == A.PR_ENT_POLYGON:
+                objname = f"mesh{e.mesh}.obj"
+                _write_obj(os.path.join(directory, objname), self.meshes[e.mesh])
+                out.append(f"objfile {os.path.join(directory, objname)}")
+            else:
+                raise ValueError("entity type has no reference writer")
+            if m.type == A.PR_MAT_REFRACTION and m.refractive_index != 1.5:
+                out.append(f"refractive_index {_fmt(m.refractive_index)}")
+            out += [f"emission {f3(m.emission)}", f"color {f3(m.color)}"]
+            if e.normal_inverse < 0:
+                out.append("normal -1")
+            if m.type in refl:
+                # 'reflection diffuse' forces roughness 1 and 'specular' 0; an
+                # explicit roughness line written after keeps other values
+                out.append(refl[m.type])
+                default_r = {A.PR_MAT_DIFFUSE: 1.0, A.PR_MAT_SPECULAR: 0.0}.get(m.type)
+                if default_r is not None and float(m.roughness) != default_r:
+                    out.append(f"roughness {_fmt(m.roughness)}")
+            else:
+                raise ValueError("material type has no reference writer")
+            out.append("")
+        path = os.path.join(directory, name)
+        with open(path, "w", newline="\n") as fh:
+            fh.write("\n".join(out) + "\n")
+        return path
+
+
+def _fmt(x) -> str:
+    """Positional decimal that the reference's expression reader (Expr.h:210-280)
+    turns into the same double: at most 15 significant digits, so that its
+    digit accumulation is exact and the single division correctly rounded."""
+    x = float(x)
+    s = np.format_float_positional(x, unique=True, trim="-")
+    digits = s.lstrip("-").replace(".", "").lstrip("0")
+    if len(digits) > 15:
+        raise ValueError(f"{x!r} needs more than 15 significant digits in the reference scene format")
+    return s
+
+
+def _write_obj(path: str, mesh: Mesh) -> None:
+    # %.9g round-trips float32 exactly through sscanf("%f")
+    with open(path, "w", newline="\n") as fh:
+        for v in mesh.vertices:
+            fh.write("v %.9g %.9g %.9g\n" % (float(v[0]), float(v[1]), float(v[2])))
+        for f in mesh.faces:
+            fh.write("f %d %d %d\n" % (int(f[0]) + 1, int(f[1]) + 1, int(f[2]) + 1))

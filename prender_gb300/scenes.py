@@ -1,0 +1,194 @@
+"""Seeded synthetic scenes with the shapes of the benchmark configurations.
+
+No reference meshes or textures ship with prender's test scenes, so every
+input here is generated from a seed: the edupt-style sphere Cornell box,
+the triangle-mesh Cornell box with a Perlin-displaced icosphere, and the
+media / Kerr variants.  Each builder returns a :class:`Scene` that can be
+rendered by the GPU library and written in the reference's scene format.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _abi as A
+from .scene import Camera, Material, Medium, RenderSettings, Scene
+
+
+def cornell_spheres(width: int = 256, height: int = 192, samples: int = 4, supersamples: int = 2,
+                    depth: int = 5, seed: int = 0) -> Scene:
+    """Sphere Cornell box: five radius-1e5 walls (proj/test/CornellBox.txt
+    minus its black front wall), a diffuse, a mirror and a glass sphere, and
+    a radius-5 emissive sphere light inside the box under the ceiling."""
+    s = Scene()
+    s.add_sphere((100001, 40.8, 81.6), 100000, Material.diffuse((0.75, 0.25, 0.25)))   # left
+    s.add_sphere((-99901, 40.8, 81.6), 100000, Material.diffuse((0.25, 0.25, 0.75)))   # right
+    s.add_sphere((50, 40.8, 100000), 100000, Material.diffuse((0.75, 0.75, 0.75)))     # back
+    s.add_sphere((50, 100000, 81.6), 100000, Material.diffuse((0.75, 0.75, 0.75)))     # floor
+    s.add_sphere((50, -99918.4, 81.6), 100000, Material.diffuse((0.75, 0.75, 0.75)))   # ceiling
+    s.add_sphere((65, 20, 20), 20, Material.diffuse((0.25, 0.75, 0.25)))
+    s.add_sphere((27, 16.5, 47), 16.5, Material.mirror((0.99, 0.99, 0.99)))
+    s.add_sphere((77, 16.5, 78), 16.5, Material.glass((0.99, 0.99, 0.99)))
+    s.add_sphere((50, 76, 81.6), 5, Material.diffuse((0, 0, 0), (36, 36, 36)))         # light
+    s.camera = Camera(position=(50, 52, 220), dir=(0, -0.04, -1), angle=30, width=width, height=height)
+    s.settings = RenderSettings(samples=samples, supersamples=supersamples, tent_filter=1, depth=depth,
+                                nee=0, seed=seed)
+    return s
+
+
+# ---------------------------------------------------------------- meshes
+def box_mesh(lo, hi):
+    """Closed axis-aligned box, 12 triangles."""
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    v = np.array([[x0, y0, z0], [x1, y0, z0], [x1, y1, z0], [x0, y1, z0],
+                  [x0, y0, z1], [x1, y0, z1], [x1, y1, z1], [x0, y1, z1]], dtype=np.float32)
+    f = np.array([[0, 1, 2], [0, 2, 3],      # z0
+                  [4, 6, 5], [4, 7, 6],      # z1
+                  [0, 4, 5], [0, 5, 1],      # y0
+                  [3, 2, 6], [3, 6, 7],      # y1
+                  [0, 3, 7], [0, 7, 4],      # x0
+                  [1, 5, 6], [1, 6, 2]],     # x1
+                 dtype=np.int32)
+    return v, f
+
+
+def icosphere(subdiv: int):
+    """Unit icosphere: 20*4^subdiv faces, 10*4^subdiv+2 vertices."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+             (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    v = np.array(verts, dtype=np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array(faces, dtype=np.int64)
+    for _ in range(subdiv):
+        nv = v.shape[0]
+        edges = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]], axis=0)
+        key = np.minimum(edges[:, 0], edges[:, 1]) * (nv + 1) + np.maximum(edges[:, 0], edges[:, 1])
+        uniq, inv = np.unique(key, return_inverse=True)
+        a = uniq // (nv + 1)
+        b = uniq % (nv + 1)
+        mid = v[a] + v[b]
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        v = np.concatenate([v, mid], axis=0)
+        m = inv.reshape(3, -1).T + nv  # midpoints of edges (01, 12, 20) per face
+        f0, f1, f2 = f[:, 0], f[:, 1], f[:, 2]
+        m01, m12, m20 = m[:, 0], m[:, 1], m[:, 2]
+        f = np.concatenate([np.stack([f0, m01, m20], 1), np.stack([f1, m12, m01], 1),
+                            np.stack([f2, m20, m12], 1), np.stack([m01, m12, m20], 1)], axis=0)
+    return v, f.astype(np.int32)
+
+
+def _perlin3(p: np.ndarray, seed: int) -> np.ndarray:
+    """Improved gradient noise (Perlin 2002) with a seeded permutation."""
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(256)
+    perm = np.concatenate([perm, perm])
+    grads = np.array([[1, 1, 0], [-1, 1, 0], [1, -1, 0], [-1, -1, 0], [1, 0, 1], [-1, 0, 1], [1, 0, -1],
+                      [-1, 0, -1], [0, 1, 1], [0, -1, 1], [0, 1, -1], [0, -1, -1], [1, 1, 0], [-1, 1, 0],
+                      [0, -1, 1], [0, -1, -1]], dtype=np.float64)
+    pi = np.floor(p).astype(np.int64)
+    pf = p - pi
+    pi &= 255
+    fade = pf * pf * pf * (pf * (pf * 6 - 15) + 10)
+
+    def h(ix, iy, iz):
+        return perm[perm[perm[ix] + iy] + iz] & 15
+
+    out = np.zeros(p.shape[0])
+    acc = []
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                g = grads[h((pi[:, 0] + dx) & 255, (pi[:, 1] + dy) & 255, (pi[:, 2] + dz) & 255)]
+                d = pf - np.array([dx, dy, dz], dtype=np.float64)
+                acc.append((g * d).sum(1))
+    u, v, w = fade[:, 0], fade[:, 1], fade[:, 2]
+    lerp = lambda a, b, t: a + t * (b - a)  # noqa: E731
+    x00 = lerp(acc[0], acc[1], u)
+    x10 = lerp(acc[2], acc[3], u)
+    x01 = lerp(acc[4], acc[5], u)
+    x11 = lerp(acc[6], acc[7], u)
+    out = lerp(lerp(x00, x10, v), lerp(x01, x11, v), w)
+    return out
+
+
+def displaced_icosphere(subdiv: int, center, radius: float, amp: float = 0.05, freq: float = 4.0,
+                        seed: int = 0):
+    v, f = icosphere(subdiv)
+    n = _perlin3(v * freq + 17.0, seed)
+    r = radius * (1.0 + amp * n)
+    verts = (v * r[:, None] + np.asarray(center, dtype=np.float64)).astype(np.float32)
+    return verts, f
+
+
+def mesh_cornell(width: int = 1024, height: int = 768, samples: int = 16, supersamples: int = 2,
+                 subdiv: int = 7, material: str = "diffuse", depth: int = 5, seed: int = 0) -> Scene:
+    """Triangle-mesh Cornell box: a 12-triangle box, a uvplane area light
+    under the ceiling (U, V of length 5 as in proj/test/CornellBoxMLT2*.txt)
+    and a Perlin-displaced icosphere (subdiv 7 = 327,680 triangles) that is
+    diffuse or glass.  NEE on; 16 x 2^2 tent-filtered samples = 64 spp."""
+    s = Scene()
+    bv, bf = box_mesh((1, 0, 0), (99, 81.6, 250))
+    s.add_mesh(bv, bf, Material.diffuse((0.75, 0.75, 0.75)))
+    s.add_uvplane((47.5, 81.5, 78.5), (5, 0, 0), (0, 0, 5), Material.diffuse((0, 0, 0), (36, 36, 36)))
+    iv, jf = displaced_icosphere(subdiv, (50, 24, 70), 20.0, amp=0.05, seed=seed)
+    mat = Material.glass((0.99, 0.99, 0.99)) if material == "glass" else Material.diffuse((0.25, 0.75, 0.25))
+    s.add_mesh(iv, jf, mat)
+    s.camera = Camera(position=(50, 52, 220), dir=(0, -0.04, -1), angle=30, width=width, height=height)
+    s.settings = RenderSettings(samples=samples, supersamples=supersamples, tent_filter=1, depth=depth,
+                                nee=1, seed=seed)
+    return s
+
+
+def media_cornell(width: int = 128, height: int = 96, samples: int = 4, supersamples: int = 2,
+                  sigma_s: float = 0.05, sigma_a: float = 0.01, g: float = 0.3, subdiv: int = 3,
+                  depth: int = 5, seed: int = 0) -> Scene:
+    """Cornell box filled with a homogeneous medium (global SCATTERING /
+    ABSORBING / PAHASE) around a diffuse icosphere, NEE on."""
+    s = mesh_cornell(width, height, samples, supersamples, subdiv=subdiv, depth=depth, seed=seed)
+    s.participating_media = 1
+    s.medium = Medium(sigma_s_rgb=(sigma_s,) * 3, sigma_a_rgb=(sigma_a,) * 3, phase_g=(g,) * 3)
+    s.settings.media = 1
+    return s
+
+
+def random_rays(scene_bounds_lo, scene_bounds_hi, n: int, seed: int = 0, inside=True) -> np.ndarray:
+    """n rays (org xyz, dir xyz) with origins uniform in the box and
+    directions uniform on the sphere; FP64, 6 per ray."""
+    rng = np.random.default_rng(seed)
+    lo = np.asarray(scene_bounds_lo, dtype=np.float64)
+    hi = np.asarray(scene_bounds_hi, dtype=np.float64)
+    org = lo + (hi - lo) * rng.random((n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.ascontiguousarray(np.concatenate([org, d], axis=1))
+
+
+def camera_rays(scene: Scene, jitter_seed: int = 0) -> np.ndarray:
+    """One primary ray per pixel through the pixel centre of CameraScreenPram
+    (render.h:1261-1269); FP64, 6 per ray, row-major in (y, x)."""
+    c = scene.camera.to_c()
+    W, H = c.width, c.height
+    pos = np.array(c.position[:])
+    d = np.array(c.dir[:])
+    up = np.array(c.up[:])
+    sw = c.screen_width * W / H
+    sx = np.cross(d, up)
+    sx = sx / np.linalg.norm(sx) * sw
+    sy = np.cross(sx, d)
+    sy = sy / np.linalg.norm(sy) * c.screen_height
+    center = pos + d * c.screen_dist
+    rng = np.random.default_rng(jitter_seed)
+    ys, xs = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    jx = rng.random(ys.shape) if jitter_seed else 0.5
+    jy = rng.random(ys.shape) if jitter_seed else 0.5
+    px = ((xs + jx) / W - 0.5)[..., None]
+    py = ((ys + jy) / H - 0.5)[..., None]
+    sp = center + sx * px + sy * py
+    dirs = sp - pos
+    dirs /= np.linalg.norm(dirs, axis=-1, keepdims=True)
+    org = np.broadcast_to(pos, dirs.shape)
+    return np.ascontiguousarray(np.concatenate([org, dirs], axis=-1).reshape(-1, 6))
