@@ -1,0 +1,134 @@
+"""Generates the golden fixtures in tests/golden/ by running the reference
+renderer itself (Sanaxen/prender, compiled by oracle/build_ref.sh).
+
+Run from the repository root in a container where the reference sources are
+mounted:
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+
+Each fixture stores the synthetic inputs (scene parameters, rays) together
+with the reference's outputs, so the tests need neither the reference nor
+its build on the machine that runs them.
+"""
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from prender_gb300 import scenes  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_BIN = os.path.join(ROOT, "oracle", "_ref", "prender_ref")
+
+
+def run_ref(args, cwd, threads=1):
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    r = subprocess.run([REF_BIN] + args, cwd=cwd, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference failed: {args}\n{r.stderr[-2000:]}")
+    return r.stdout
+
+
+def ref_qbvh(path, ent, d):
+    run_ref(["qbvh", path, str(ent), os.path.join(d, "q.bin")], d)
+    b = open(os.path.join(d, "q.bin"), "rb").read()
+    nn, nl = struct.unpack("qq", b[:16])
+    rec = np.dtype([("boxes", "<f4", 24), ("ch", "<u8", 4), ("ax", "<i4", 3)])
+    nodes = np.frombuffer(b[16:16 + nn * rec.itemsize], dtype=rec)
+    leaf = np.frombuffer(b[16 + nn * rec.itemsize:], dtype="<i4").copy()
+    children = nodes["ch"].view(np.int64).copy()
+    boxes = nodes["boxes"].reshape(nn, 6, 4).copy()
+    # slots with an invalid child carry uninitialised boxes in the reference
+    boxes = np.where((children == -1)[:, None, :], np.float32(0), boxes).reshape(nn, 24)
+    return dict(boxes=boxes, children=children, axes=nodes["ax"].copy(), leaf=leaf)
+
+
+def ref_firsthit(path, rays, d):
+    rays.astype(np.float64).tofile(os.path.join(d, "rays.f64"))
+    run_ref(["firsthit", path, os.path.join(d, "rays.f64"), os.path.join(d, "fh.bin")], d)
+    rec = np.dtype([("ent", "<i4"), ("prim", "<i4"), ("t", "<f8"), ("pn", "<f8", 6)])
+    fh = np.fromfile(os.path.join(d, "fh.bin"), dtype=rec)
+    return dict(entity=fh["ent"].copy(), prim=fh["prim"].copy(), t=fh["t"].copy())
+
+
+def ref_radiance(path, rays, seed, d):
+    rays.astype(np.float64).tofile(os.path.join(d, "rays.f64"))
+    run_ref(["radiance", path, os.path.join(d, "rays.f64"), os.path.join(d, "rad.f64"), str(seed)], d)
+    return np.fromfile(os.path.join(d, "rad.f64")).reshape(-1, 3)
+
+
+def ref_render(path, shape, d, threads=1):
+    out = run_ref(["render", path, os.path.join(d, "img.f64")], d, threads)
+    return np.fromfile(os.path.join(d, "img.f64")).reshape(shape[1], shape[0], 3), out.strip().splitlines()[-1]
+
+
+def main():
+    if not os.path.exists(REF_BIN):
+        ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+        subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), ref], check=True)
+    with tempfile.TemporaryDirectory() as d:
+        # -- QBVH structure + first hits on the subdiv-3 mesh Cornell box
+        s = scenes.mesh_cornell(width=32, height=24, samples=1, supersamples=2, subdiv=3)
+        p = s.write_reference(d)
+        q0, q2 = ref_qbvh(p, 0, d), ref_qbvh(p, 2, d)
+        rays = np.concatenate([scenes.random_rays((2, 1, 1), (98, 80, 249), 4096, seed=1), scenes.camera_rays(s)])
+        fh = ref_firsthit(p, rays, d)
+        np.savez_compressed(os.path.join(HERE, "mesh_s3_qbvh_firsthit.npz"), rays=rays,
+                            **{f"box_{k}": v for k, v in q0.items()}, **{f"ico_{k}": v for k, v in q2.items()},
+                            **{f"fh_{k}": v for k, v in fh.items()})
+        # -- per-ray radiance() roots from one MT19937-64 stream
+        cases = {
+            "spheres": scenes.cornell_spheres(width=16, height=12, samples=1, supersamples=1),
+            "mesh_diffuse": scenes.mesh_cornell(width=16, height=12, samples=1, supersamples=1, subdiv=3),
+            "mesh_glass": scenes.mesh_cornell(width=16, height=12, samples=1, supersamples=1, subdiv=3,
+                                              material="glass"),
+            "media_g05": scenes.media_cornell(width=16, height=12, samples=1, supersamples=1, g=0.5),
+        }
+        rad = {}
+        for name, sc in cases.items():
+            dd = os.path.join(d, name)
+            os.makedirs(dd)
+            pp = sc.write_reference(dd)
+            r = scenes.camera_rays(sc)
+            rad[f"{name}_rays"] = r
+            rad[f"{name}_rgb"] = ref_radiance(pp, r, 7, dd)
+        np.savez_compressed(os.path.join(HERE, "radiance_roots.npz"), **rad)
+        # -- whole Render::Run images, one thread (bit-exact) -----------
+        imgs = {}
+        for name, sc in {
+            "spheres": scenes.cornell_spheres(width=24, height=18, samples=2, supersamples=2),
+            "mesh_nee": scenes.mesh_cornell(width=24, height=18, samples=1, supersamples=2, subdiv=3),
+            "media_g05": scenes.media_cornell(width=16, height=12, samples=1, supersamples=2, g=0.5),
+        }.items():
+            dd = os.path.join(d, "r_" + name)
+            os.makedirs(dd)
+            pp = sc.write_reference(dd)
+            img, info = ref_render(pp, (sc.camera.width, sc.camera.height), dd, threads=1)
+            imgs[name] = img
+            print(name, info)
+        np.savez_compressed(os.path.join(HERE, "render_1thread.npz"), **imgs)
+        # -- high-spp reference images for statistical image parity ------
+        hi = {}
+        for name, sc in {
+            "spheres_64x48_1024spp": scenes.cornell_spheres(width=64, height=48, samples=256, supersamples=2),
+            "mesh_64x48_512spp": scenes.mesh_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3),
+            "glass_64x48_512spp": scenes.mesh_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3,
+                                                      material="glass"),
+        }.items():
+            dd = os.path.join(d, "h_" + name)
+            os.makedirs(dd)
+            pp = sc.write_reference(dd, threads=os.cpu_count())
+            img, info = ref_render(pp, (sc.camera.width, sc.camera.height), dd, threads=os.cpu_count())
+            hi[name] = img.astype(np.float32)
+            print(name, info)
+        np.savez_compressed(os.path.join(HERE, "render_highspp.npz"), **hi)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,67 @@
+"""The CPU oracle against golden vectors produced by the reference renderer
+itself (tests/golden/make_golden.py).  Integer and FP64 results are compared
+bit for bit."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from prender_gb300 import scenes
+
+
+@pytest.fixture(scope="module")
+def mesh_s3():
+    s = scenes.mesh_cornell(width=32, height=24, samples=1, supersamples=2, subdiv=3)
+    return s, O.OracleScene(s)
+
+
+@pytest.mark.parametrize("ent,prefix", [(0, "box"), (2, "ico")])
+def test_qbvh_structure_matches_reference(golden, mesh_s3, ent, prefix):
+    g = golden["mesh_s3_qbvh_firsthit"]
+    q = mesh_s3[1].qbvh(ent)
+    valid = (q["children"] != -1)[:, None, :]
+    boxes = np.where(valid, q["boxes"].reshape(-1, 6, 4), np.float32(0)).reshape(-1, 24)
+    assert np.array_equal(q["children"], g[f"{prefix}_children"])
+    assert np.array_equal(q["axes"], g[f"{prefix}_axes"])
+    assert np.array_equal(q["leaf"], g[f"{prefix}_leaf"])
+    assert np.array_equal(boxes, g[f"{prefix}_boxes"])
+
+
+def test_first_hit_bit_exact(golden, mesh_s3):
+    g = golden["mesh_s3_qbvh_firsthit"]
+    h = mesh_s3[1].first_hit(g["rays"])
+    assert np.array_equal(h["entity"], g["fh_entity"])
+    assert np.array_equal(h["prim"], g["fh_prim"])
+    assert np.array_equal(h["t"], g["fh_t"])
+    assert (g["fh_entity"] == 2).sum() > 200  # the rays do reach the icosphere
+
+
+@pytest.mark.parametrize("name,build", [
+    ("spheres", lambda: scenes.cornell_spheres(width=16, height=12, samples=1, supersamples=1)),
+    ("mesh_diffuse", lambda: scenes.mesh_cornell(width=16, height=12, samples=1, supersamples=1, subdiv=3)),
+    ("mesh_glass", lambda: scenes.mesh_cornell(width=16, height=12, samples=1, supersamples=1, subdiv=3,
+                                               material="glass")),
+    ("media_g05", lambda: scenes.media_cornell(width=16, height=12, samples=1, supersamples=1, g=0.5)),
+])
+def test_radiance_roots_bit_exact(golden, name, build):
+    g = golden["radiance_roots"]
+    sc = build()
+    out = O.OracleScene(sc).radiance(g[f"{name}_rays"], 7)
+    assert np.array_equal(out, g[f"{name}_rgb"])
+
+
+@pytest.mark.parametrize("name,build", [
+    ("spheres", lambda: scenes.cornell_spheres(width=24, height=18, samples=2, supersamples=2)),
+    ("mesh_nee", lambda: scenes.mesh_cornell(width=24, height=18, samples=1, supersamples=2, subdiv=3)),
+    ("media_g05", lambda: scenes.media_cornell(width=16, height=12, samples=1, supersamples=2, g=0.5)),
+])
+def test_render_one_thread_bit_exact(golden, name, build):
+    sc = build()
+    img, _, _ = O.OracleScene(sc).render(threads=1)
+    assert np.array_equal(img, golden["render_1thread"][name])
+
+
+def test_high_spp_goldens_are_converged(golden):
+    # sanity of the statistical fixtures: finite, non-negative, lit
+    for k in golden["render_highspp"].files:
+        img = golden["render_highspp"][k]
+        assert np.isfinite(img).all() and (img >= 0).all() and img.mean() > 1e-3
