@@ -1,0 +1,299 @@
+"""Benchmark: Mpaths/s of the radiance estimator on the triangle-mesh Cornell
+box (1024x768, 64 spp tent-filtered, NEE, 327,680-triangle displaced
+icosphere) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+                    [--mode megakernel] [--small]
+
+A step is one full frame (W*H*spp camera paths).  Under torchrun (N>1) each
+rank renders its own disjoint sample range of the same frame (weak scaling,
+no collective on the data path); value = all ranks' paths / max-over-ranks
+time.  Rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpaths/s on 1 GB300 at matched RMSE, wavefront vs plain; adjoint/forward cost"
+
+
+def baseline_metric():
+    try:
+        with open(os.path.join(ROOT, "BASELINE.json")) as f:
+            return json.load(f).get("metric", METRIC)
+    except OSError:
+        return METRIC
+
+
+def workload(small: bool):
+    from prender_gb300 import scenes
+    if small:
+        s = scenes.mesh_cornell(width=256, height=192, samples=4, supersamples=2, subdiv=5)
+        name = "mesh_cornell_256x192_16spp_subdiv5"
+    else:
+        s = scenes.mesh_cornell(width=1024, height=768, samples=16, supersamples=2, subdiv=7)
+        name = "mesh_cornell_1024x768_64spp_subdiv7"
+    return s, name
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+
+        def rd():
+            for line in self.proc.stdout:
+                self.rows.append([x.strip() for x in line.split(",")])
+
+        self.thread = threading.Thread(target=rd, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(scene, rows: int, threads: int):
+    """The oracle port on the host cores over a bounded band of rows."""
+    from oracle import oracle as O
+    o = O.OracleScene(scene)
+    H = scene.camera.height
+    r0 = H // 2 - rows // 2
+    t0 = time.perf_counter()
+    _, secs, _ = o.render(threads=threads, row0=r0, row1=r0 + rows)
+    wall = time.perf_counter() - t0
+    paths = rows * scene.camera.width * scene.settings.spp
+    return paths / secs / 1e6, secs, wall, paths
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    scene, name = workload(args.small)
+    threads = os.cpu_count() or 1
+    rows = max(1, int(args.ref_rows))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, secs, _, paths = cpu_baseline(scene, rows, threads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    sample = f"{rows} middle rows x {scene.camera.width} px x {scene.settings.spp} spp per step"
+    line = {
+        "impl": "reference", "metric": baseline_metric(), "value": round(value, 4), "unit": "Mpaths/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * rows * scene.camera.width * scene.settings.spp / (value * 1e6), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": name, "sample": sample},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__ as g
+    g.build_library()
+    from prender_gb300 import gpu
+    scene, name = workload(args.small)
+    W, H, spp = scene.camera.width, scene.camera.height, scene.settings.spp
+    ctx = gpu.Context(local)
+    t0 = time.perf_counter()
+    ctx.upload(scene)
+    upload_s = time.perf_counter() - t0
+    import ctypes as C
+    cam, prm = scene.camera.to_c(), scene.settings.to_c()
+    out = torch.empty((H, W, 3), dtype=torch.float32, device=f"cuda:{local}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")  # > L2 (129 MB)
+    L = ctx.L
+
+    def step(i):
+        off = (rank + ws * i) * spp  # disjoint sample ranges per rank and step
+        rc = L.pr_render_dev(ctx.h, C.byref(cam), C.byref(prm), C.c_void_p(out.data_ptr()), off, 0)
+        if rc != 0:
+            raise RuntimeError(L.pr_last_error(ctx.h).decode())
+        return ctx.stats()
+
+    for i in range(args.warmup):
+        step(i)
+    clk = ClockSampler(local)
+    clk.start()
+    walls, kern, st = [], [], None
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        st = step(args.warmup + i)
+        torch.cuda.synchronize()
+        walls.append(time.perf_counter() - t0)
+        kern.append(st["device_ms"] / 1e3)
+    clocks = clk.stop()
+    ms = 1e3 * statistics.mean(walls)
+    kern_s = statistics.mean(kern)
+    if dist:
+        t = torch.tensor([ms, kern_s], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, kern_s = float(t[0]), float(t[1])
+    paths = W * H * spp
+    value = ws * paths / (ms / 1e3) / 1e6
+
+    # e2e through the C ABI with a host image buffer (camera + parameters in,
+    # image out, copies inside the timed region)
+    host = np.empty((H, W, 3), np.float32)
+    e2e = []
+    for i in range(max(2, min(args.steps, 4))):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.render(scene, sample_offset=(rank + ws * (1000 + i)) * spp, accumulate=None)
+        e2e.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * statistics.mean(e2e)
+    if dist:
+        t = torch.tensor([e2e_ms], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t[0])
+    e2e_val = ws * paths / (e2e_ms / 1e3) / 1e6
+    del host
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    # roofline: algorithmic bytes of the traversal, B_seg = 144 N_node + 36 N_tri + 64 per segment
+    segs = st["segments"]
+    alg_bytes = 144.0 * st["nodes_visited"] + 36.0 * st["tri_tests"] + 64.0 * segs + 12.0 * st["paths"]
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg_bytes / (st["device_ms"] / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
+            "note": "algorithmic bytes of the megakernel launch; scene (~28 MB) is L2-resident"}
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        try:
+            with open(prof) as f:
+                tr = json.load(f).get(name)
+            if tr:
+                roof["traffic"] = tr
+        except (OSError, ValueError):
+            pass
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        threads = os.cpu_count() or 1
+        rows = max(1, int(args.ref_rows))
+        v, secs, wall, npaths = cpu_baseline(scene, rows, threads)
+        cpu = {"value": round(v, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
+               "sample": f"{rows} middle rows x {W} px x {spp} spp ({npaths} paths, {secs:.1f} s)"}
+    line = {
+        "metric": baseline_metric(), "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": name, "width": W, "height": H, "spp": spp, "triangles": int(scene.meshes[1].faces.shape[0]),
+                   "nee": 1, "mode": "megakernel", "l2": "flushed between steps (256 MB write)",
+                   "paths_per_step": paths, "segments_per_step": segs, "kernel_ms_per_step": round(kern_s * 1e3, 3),
+                   "scene_upload_s": round(upload_s, 3)},
+        "e2e": {"value": round(e2e_val, 3), "unit": "Mpaths/s",
+                "h2d_bytes_per_step": C.sizeof(cam) + C.sizeof(prm), "d2h_bytes_per_step": W * H * 3 * 4},
+        "gpu_launches": 2 * args.steps,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--mode", default="megakernel")
+    ap.add_argument("--small", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-rows", type=int, default=48)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -188,6 +188,11 @@ pr_ctx* pr_create(int device, int* status);
 void pr_destroy(pr_ctx* ctx);
 const char* pr_last_error(const pr_ctx* ctx);
 int pr_abi_version(void);
+/* sizeof of the ABI structs, in the order pr_medium, pr_material,
+ * pr_entity, pr_mesh, pr_kerr, pr_scene_desc, pr_camera,
+ * pr_render_params, pr_render_stats (0..8); 0 for other values.  Lets a
+ * binding check its struct mirrors. */
+size_t pr_abi_sizeof(int which);
 
 /* ---- scene -------------------------------------------------------------- */
 /* Replaces SceneEnv::Load + CreateEntList (scene_env.h:357, scene.cpp:38):
@@ -206,6 +211,14 @@ int pr_qbvh_info(pr_ctx* ctx, int entity, int64_t* n_nodes, int64_t* n_leaf_slot
  * -1 terminators.  Used to check the build against the reference. */
 int pr_qbvh_export(pr_ctx* ctx, int entity, float* boxes, int64_t* children,
                    int32_t* axes, int32_t* leaf_faces);
+
+/* Host-only build of one mesh's QBVH with the reference's rules (SAH
+ * binary tree, BVH.cpp:194-348, flattened by QBVH.cpp:161-302), in the same
+ * export layout as pr_qbvh_export.  Needs no GPU.  Call with null output
+ * arrays to obtain n_nodes / n_leaf_slots, then again to fill them. */
+int pr_qbvh_build_host(const float* vertices, int32_t n_vertices, const int32_t* faces, int32_t n_faces,
+                       int64_t* n_nodes, int64_t* n_leaf_slots, float* boxes, int64_t* children,
+                       int32_t* axes, int32_t* leaf_faces);
 
 /* ---- closest hit ---------------------------------------------------------- */
 /* intersect_scene_ (scene.cpp:83-214) for n rays, including the 1e-6 origin

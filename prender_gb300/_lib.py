@@ -1,0 +1,59 @@
+"""Loads libprender_gpu.so (the C ABI of include/prender_gpu.h) via ctypes.
+
+The library is the product: there is no CPU fallback.  If it is missing the
+import fails loudly with the build command to run.
+"""
+import ctypes as C
+import os
+
+from . import _abi as A
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libprender_gpu.so")
+
+# every entry point declared in include/prender_gpu.h
+EXPORTS = (
+    "pr_create", "pr_destroy", "pr_last_error", "pr_abi_version", "pr_abi_sizeof",
+    "pr_scene_upload", "pr_qbvh_info", "pr_qbvh_export", "pr_qbvh_build_host",
+    "pr_first_hit", "pr_first_hit_dev", "pr_render", "pr_render_dev", "pr_last_render_stats",
+    "pr_kerr_trace", "pr_kerr_trace_dev",
+)
+
+_lib = None
+
+
+class PrenderError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"prender_gpu error {code}: {msg}")
+        self.code = code
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with "
+                          f"`python -c 'import __graft_entry__ as g; g.build()'` (there is no CPU fallback)")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+    L.pr_create.restype = vp
+    L.pr_create.argtypes = [C.c_int, C.POINTER(C.c_int)]
+    L.pr_destroy.argtypes = [vp]
+    L.pr_last_error.restype = C.c_char_p
+    L.pr_last_error.argtypes = [vp]
+    L.pr_abi_sizeof.restype = C.c_size_t
+    L.pr_abi_sizeof.argtypes = [C.c_int]
+    L.pr_scene_upload.argtypes = [vp, vp]
+    L.pr_qbvh_info.argtypes = [vp, C.c_int, vp, vp]
+    L.pr_qbvh_export.argtypes = [vp, C.c_int, vp, vp, vp, vp]
+    L.pr_qbvh_build_host.argtypes = [vp, i32, vp, i32, vp, vp, vp, vp, vp, vp]
+    L.pr_first_hit.argtypes = [vp, vp, i64, vp, vp, vp]
+    L.pr_first_hit_dev.argtypes = [vp, vp, i64, vp, vp, vp]
+    L.pr_render.argtypes = [vp, vp, vp, vp, C.c_uint64, C.c_int]
+    L.pr_render_dev.argtypes = [vp, vp, vp, vp, C.c_uint64, C.c_int]
+    L.pr_last_render_stats.argtypes = [vp, C.POINTER(A.pr_render_stats)]
+    L.pr_kerr_trace.argtypes = [vp, vp, i64, vp, vp, vp, vp, vp, vp]
+    L.pr_kerr_trace_dev.argtypes = [vp, vp, i64, vp, vp, vp, vp, vp, vp]
+    _lib = L
+    return L

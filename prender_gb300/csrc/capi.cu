@@ -1,0 +1,416 @@
+// C ABI (include/prender_gpu.h): context, scene upload, closest-hit hook and
+// the plain renderer.  Host buffers are staged through device copies owned
+// by the context; every error becomes a status code plus pr_last_error().
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/prender_gpu.h"
+#include "pr_internal.h"
+#include "render_kernels.h"
+#include "scene_build.h"
+
+using namespace pr;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e == cudaSuccess) n = bytes;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace
+
+struct pr_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  HostScene host;
+  bool scene_ready = false;
+  DevScene dev{};
+  DevBuf ents, mats, nodes, tris, fnorm;
+  DevBuf errword, counters;  // 4 bytes / 4 x u64
+  DevBuf partial, out, rays, ires, jres, dres;
+  pr_render_stats stats{};
+};
+
+namespace {
+
+int fail(pr_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(pr_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, PR_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define PR_CUDA(ctx, call)                                   \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+int check_device_errors(pr_ctx* c) {
+  uint32_t bits = 0;
+  PR_CUDA(c, cudaMemcpyAsync(&bits, c->errword.p, 4, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (!bits) return PR_OK;
+  std::string m = "device check fired:";
+  if (bits & PR_DEV_STACK_OVERFLOW) m += " traversal-stack-overflow";
+  if (bits & PR_DEV_LOOP_CAP) m += " loop-cap";
+  if (bits & PR_DEV_BAD_INDEX) m += " bad-index";
+  if (bits & PR_DEV_QUEUE_OVERFLOW) m += " queue-overflow";
+  if (bits & PR_DEV_NONFINITE) m += " non-finite-radiance";
+  return fail(c, PR_E_DEVICE, m);
+}
+
+template <class T>
+cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
+  cudaError_t e = b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1));
+  if (e != cudaSuccess || v.empty()) return e;
+  return cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int pr_abi_version(void) { return PR_ABI_VERSION; }
+
+pr_ctx* pr_create(int device, int* status) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0 || device < 0 || device >= n) {
+    if (status) *status = (e != cudaSuccess || n == 0) ? PR_E_CUDA : PR_E_ARG;
+    return nullptr;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) {
+    if (status) *status = PR_E_CUDA;
+    return nullptr;
+  }
+  pr_ctx* c = new pr_ctx();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      c->errword.ensure(16) != cudaSuccess || c->counters.ensure(64) != cudaSuccess) {
+    if (status) *status = PR_E_CUDA;
+    delete c;
+    return nullptr;
+  }
+  if (status) *status = PR_OK;
+  return c;
+}
+
+void pr_destroy(pr_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (DevBuf* b : {&c->ents, &c->mats, &c->nodes, &c->tris, &c->fnorm, &c->errword, &c->counters, &c->partial,
+                    &c->out, &c->rays, &c->ires, &c->jres, &c->dres})
+    b->release();
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* pr_last_error(const pr_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int pr_scene_upload(pr_ctx* c, const pr_scene_desc* d) {
+  if (!c) return PR_E_ARG;
+  PR_CUDA(c, cudaSetDevice(c->device));
+  c->scene_ready = false;
+  std::string err;
+  int st = build_host_scene(d, c->host, err);
+  if (st != PR_OK) return fail(c, st, err);
+  HostScene& h = c->host;
+  PR_CUDA(c, upload(c->ents, h.ents, c->stream));
+  PR_CUDA(c, upload(c->mats, h.mats, c->stream));
+  PR_CUDA(c, upload(c->nodes, h.nodes, c->stream));
+  PR_CUDA(c, upload(c->tris, h.tris, c->stream));
+  PR_CUDA(c, upload(c->fnorm, h.fnorm, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  DevScene& S = c->dev;
+  memset(&S, 0, sizeof(S));
+  S.ents = (const GEntity*)c->ents.p;
+  S.mats = (const GMaterial*)c->mats.p;
+  S.nodes = (const GNode*)c->nodes.p;
+  S.tris = (const float4*)c->tris.p;
+  S.fnorm = (const float*)c->fnorm.p;
+  S.n_ents = (int)h.ents.size();
+  S.n_lights = (int)h.light_ent.size();
+  for (int i = 0; i < S.n_lights; i++) S.light_ent[i] = h.light_ent[i];
+  for (int k = 0; k < 3; k++) {
+    S.background[k] = h.background[k];
+    S.env_light[k] = h.env_light[k];
+  }
+  S.medium = h.medium;
+  S.scene_scale = h.scene_scale;
+  c->scene_ready = true;
+  return PR_OK;
+}
+
+static void export_qbvh(const MeshQbvh& q, float* boxes, int64_t* children, int32_t* axes, int32_t* leaf_faces);
+
+int pr_qbvh_info(pr_ctx* c, int entity, int64_t* n_nodes, int64_t* n_leaf_slots) {
+  if (!c || !c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  for (size_t m = 0; m < c->host.mesh_entity.size(); m++)
+    if (c->host.mesh_entity[m] == entity) {
+      if (n_nodes) *n_nodes = (int64_t)c->host.mesh_qbvh[m].nodes.size();
+      if (n_leaf_slots) *n_leaf_slots = (int64_t)c->host.mesh_qbvh[m].ref_leaf.size();
+      return PR_OK;
+    }
+  return fail(c, PR_E_ARG, "entity is not a mesh");
+}
+
+int pr_qbvh_export(pr_ctx* c, int entity, float* boxes, int64_t* children, int32_t* axes, int32_t* leaf_faces) {
+  if (!c || !c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  for (size_t m = 0; m < c->host.mesh_entity.size(); m++)
+    if (c->host.mesh_entity[m] == entity) {
+      export_qbvh(c->host.mesh_qbvh[m], boxes, children, axes, leaf_faces);
+      return PR_OK;
+    }
+  return fail(c, PR_E_ARG, "entity is not a mesh");
+}
+
+static void export_qbvh(const MeshQbvh& q, float* boxes, int64_t* children, int32_t* axes, int32_t* leaf_faces) {
+  for (size_t i = 0; i < q.nodes.size(); i++) {
+    const RefNode& rn = q.nodes[i];
+    if (boxes) memcpy(boxes + 24 * i, rn.box, 24 * sizeof(float));
+    if (children)
+      for (int s = 0; s < 4; s++) children[4 * i + s] = rn.ref_child[s];
+    if (axes) {
+      axes[3 * i] = rn.axis_top;
+      axes[3 * i + 1] = rn.axis_left;
+      axes[3 * i + 2] = rn.axis_right;
+    }
+  }
+  if (leaf_faces) memcpy(leaf_faces, q.ref_leaf.data(), q.ref_leaf.size() * sizeof(int32_t));
+}
+
+int pr_qbvh_build_host(const float* vertices, int32_t n_vertices, const int32_t* faces, int32_t n_faces,
+                       int64_t* n_nodes, int64_t* n_leaf_slots, float* boxes, int64_t* children, int32_t* axes,
+                       int32_t* leaf_faces) {
+  if (!vertices || !faces || n_vertices <= 0 || n_faces <= 0) return PR_E_ARG;
+  for (int64_t f = 0; f < 3 * (int64_t)n_faces; f++)
+    if (faces[f] < 0 || faces[f] >= n_vertices) return PR_E_ARG;
+  MeshQbvh q;
+  std::string err;
+  int st = build_mesh_qbvh(vertices, faces, n_faces, q, err);
+  if (st != PR_OK) return st;
+  if (n_nodes) *n_nodes = (int64_t)q.nodes.size();
+  if (n_leaf_slots) *n_leaf_slots = (int64_t)q.ref_leaf.size();
+  export_qbvh(q, boxes, children, axes, leaf_faces);
+  return PR_OK;
+}
+
+int pr_first_hit_dev(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, int32_t* prim, double* t) {
+  if (!c) return PR_E_ARG;
+  if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  if (n < 0 || (n > 0 && (!rays || !entity || !prim || !t))) return fail(c, PR_E_ARG, "bad first-hit arguments");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  PR_CUDA(c, launch_first_hit(c->dev, rays, n, entity, prim, t, (uint32_t*)c->errword.p,
+                              (unsigned long long*)c->counters.p, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  unsigned long long cnt[4];
+  PR_CUDA(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  int st = check_device_errors(c);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->stats = pr_render_stats{0, (uint64_t)n, cnt[2], cnt[3], ms};
+  return st;
+}
+
+int pr_first_hit(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, int32_t* prim, double* t) {
+  if (!c) return PR_E_ARG;
+  if (n < 0 || (n > 0 && (!rays || !entity || !prim || !t))) return fail(c, PR_E_ARG, "bad first-hit arguments");
+  if (n == 0) return PR_OK;
+  PR_CUDA(c, cudaSetDevice(c->device));
+  PR_CUDA(c, c->rays.ensure(sizeof(double) * 6 * (size_t)n));
+  PR_CUDA(c, c->ires.ensure(sizeof(int32_t) * (size_t)n));
+  PR_CUDA(c, c->jres.ensure(sizeof(int32_t) * (size_t)n));
+  PR_CUDA(c, c->dres.ensure(sizeof(double) * (size_t)n));
+  PR_CUDA(c, cudaMemcpyAsync(c->rays.p, rays, sizeof(double) * 6 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  int st = pr_first_hit_dev(c, (const double*)c->rays.p, n, (int32_t*)c->ires.p, (int32_t*)c->jres.p, (double*)c->dres.p);
+  if (st != PR_OK) return st;
+  PR_CUDA(c, cudaMemcpyAsync(entity, c->ires.p, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaMemcpyAsync(prim, c->jres.p, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaMemcpyAsync(t, c->dres.p, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PR_OK;
+}
+
+// CameraScreenPram (render.h:105-150) and the Run() sample set-up (:1129-1139)
+static int prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, uint64_t sample_offset,
+                          RenderCfg& g) {
+  if (!cam || !p) return fail(c, PR_E_ARG, "null camera or parameters");
+  if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
+    return fail(c, PR_E_ARG, "image size out of range");
+  if (p->samples <= 0 || p->supersamples <= 0) return fail(c, PR_E_ARG, "samples and supersamples must be positive");
+  memset(&g, 0, sizeof(g));
+  double dir[3] = {cam->dir[0], cam->dir[1], cam->dir[2]};
+  double phi = std::atan2(dir[1], dir[0]);
+  const double PI = 3.14159265358979323846264338327950288;
+  if (phi < 0.0) phi += 2.0 * PI;
+  if (std::fabs(phi - PI) < 1.0e-6 || phi < 1.0e-6 || std::fabs(phi - 2.0 * PI) < 1.0e-6) {
+    dir[1] += 1.0e-6;
+    const double len = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+    for (double& x : dir) x /= len;
+  }
+  auto crs = [](const double* a, const double* b, double* o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  auto nrm = [](double* a) {
+    const double l = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    for (int k = 0; k < 3; k++) a[k] /= l;
+  };
+  const double sw = cam->screen_width * cam->width / cam->height, sh = cam->screen_height;
+  double sx[3], sy[3];
+  crs(dir, cam->up, sx);
+  nrm(sx);
+  for (double& x : sx) x *= sw;
+  crs(sx, dir, sy);
+  nrm(sy);
+  for (double& x : sy) x *= sh;
+  double ctr[3];
+  for (int k = 0; k < 3; k++) ctr[k] = cam->position[k] + dir[k] * cam->screen_dist;
+  g.cam_pos = make_float3((float)cam->position[0], (float)cam->position[1], (float)cam->position[2]);
+  g.center = make_float3((float)ctr[0], (float)ctr[1], (float)ctr[2]);
+  g.screen_x = make_float3((float)sx[0], (float)sx[1], (float)sx[2]);
+  g.screen_y = make_float3((float)sy[0], (float)sy[1], (float)sy[2]);
+  g.width = cam->width;
+  g.height = cam->height;
+  g.iw = (float)(1.0 / cam->width);
+  g.ih = (float)(1.0 / cam->height);
+  int samples = p->samples, ss = p->supersamples;
+  double rate = 1.0 / ss;
+  if (p->tent_filter) {
+    samples = samples * ss * ss;
+    ss = 1;
+    rate = 0.5;
+  }
+  g.spp = samples * ss * ss;
+  g.ss = ss;
+  g.rate = (float)rate;
+  g.smp = (float)(1.0 / samples / (ss * ss));
+  g.tent = p->tent_filter ? 1 : 0;
+  g.cutoff = (float)p->luminance_cutoff;
+  g.sensor = (float)p->sensor_response;
+  g.depth = p->depth;
+  g.depth_limit = p->depth_limit;
+  g.nee = p->nee;
+  g.media = p->media;
+  g.flags = p->flags;
+  g.max_vertices = p->max_path_vertices > 0 ? p->max_path_vertices : 512;
+  g.seed = p->seed;
+  g.sample_offset = sample_offset;
+  g.tiles_x = (uint32_t)((cam->width + 7) / 8);
+  g.tiles_y = (uint32_t)((cam->height + 3) / 4);
+  // enough sample chunks to keep ~1.2M threads in flight
+  const double pixels = (double)cam->width * cam->height;
+  int chunks = (int)std::ceil(1.2e6 / pixels);
+  chunks = std::max(1, std::min(chunks, g.spp));
+  g.chunks = chunks;
+  return PR_OK;
+}
+
+int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, float* rgb_dev, uint64_t sample_offset,
+                  int accumulate) {
+  if (!c) return PR_E_ARG;
+  if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  if (!rgb_dev) return fail(c, PR_E_ARG, "null output");
+  if (p && p->mode != PR_MODE_MEGAKERNEL) return fail(c, PR_E_UNSUPPORTED, "only the megakernel mode is built");
+  RenderCfg g;
+  int st = prepare_render(c, cam, p, sample_offset, g);
+  if (st != PR_OK) return st;
+  PR_CUDA(c, cudaSetDevice(c->device));
+  const size_t n3 = (size_t)g.width * g.height * 3;
+  PR_CUDA(c, c->partial.ensure(sizeof(float) * n3 * (size_t)g.chunks));
+  PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  PR_CUDA(c, launch_megakernel(c->dev, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
+                               (unsigned long long*)c->counters.p, c->stream));
+  PR_CUDA(c, launch_reduce((const float*)c->partial.p, rgb_dev, (int)n3, g.chunks, accumulate, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  unsigned long long cnt[4];
+  PR_CUDA(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  st = check_device_errors(c);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->stats = pr_render_stats{cnt[0], cnt[1], cnt[2], cnt[3], ms};
+  return st;
+}
+
+int pr_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, float* rgb, uint64_t sample_offset,
+              int accumulate) {
+  if (!c) return PR_E_ARG;
+  if (!cam || !rgb) return fail(c, PR_E_ARG, "null camera or output");
+  if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
+    return fail(c, PR_E_ARG, "image size out of range");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  const size_t bytes = sizeof(float) * 3 * (size_t)cam->width * cam->height;
+  PR_CUDA(c, c->out.ensure(bytes));
+  if (accumulate) PR_CUDA(c, cudaMemcpyAsync(c->out.p, rgb, bytes, cudaMemcpyHostToDevice, c->stream));
+  int st = pr_render_dev(c, cam, p, (float*)c->out.p, sample_offset, accumulate);
+  if (st != PR_OK) return st;
+  PR_CUDA(c, cudaMemcpyAsync(rgb, c->out.p, bytes, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PR_OK;
+}
+
+int pr_last_render_stats(pr_ctx* c, pr_render_stats* s) {
+  if (!c || !s) return PR_E_ARG;
+  *s = c->stats;
+  return PR_OK;
+}
+
+int pr_kerr_trace(pr_ctx* c, const double*, int64_t, int32_t*, double*, double*, int32_t*, int32_t*, double*) {
+  return fail(c, PR_E_UNSUPPORTED, "Kerr tracer not built yet");
+}
+int pr_kerr_trace_dev(pr_ctx* c, const double*, int64_t, int32_t*, double*, double*, int32_t*, int32_t*, double*) {
+  return fail(c, PR_E_UNSUPPORTED, "Kerr tracer not built yet");
+}
+
+size_t pr_abi_sizeof(int which) {
+  switch (which) {
+    case 0: return sizeof(pr_medium);
+    case 1: return sizeof(pr_material);
+    case 2: return sizeof(pr_entity);
+    case 3: return sizeof(pr_mesh);
+    case 4: return sizeof(pr_kerr);
+    case 5: return sizeof(pr_scene_desc);
+    case 6: return sizeof(pr_camera);
+    case 7: return sizeof(pr_render_params);
+    case 8: return sizeof(pr_render_stats);
+    default: return 0;
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,99 @@
+// Host/device shared layout of the uploaded scene.
+//
+// The GPU scene is a flat set of arrays in HBM:
+//   * entities and materials (a few dozen records, read through the
+//     read-only cache);
+//   * one QBVH per mesh, all meshes' nodes concatenated, 128-byte nodes
+//     (six float4 of child boxes in SoA form, one int4 of children, one int4
+//     of axes and leaf sizes) so that a node is eight 128-bit loads;
+//   * triangles stored in QBVH leaf order, three float4 each (vertex 0, 1, 2
+//     as the mesh keeps them in float, face id in v0.w), so a leaf is a
+//     contiguous run and the FP64 re-test reads the exact float vertices;
+//   * face normals per mesh face (float3, ObjLoader's rule).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/prender_gpu.h"
+
+namespace pr {
+
+constexpr int kMaxEntities = 64;
+constexpr int kMaxLights = 16;
+constexpr int kStackSize = 64;          // QBVH traversal stack (entries)
+constexpr int kSplitStack = 4;          // pending glass branches (depth <= 2 splits)
+constexpr int32_t kChildInvalid = -1;   // QBVH child slot without a child
+// leaf child = kLeafBit | first leaf slot; inner child = node index (>= 0)
+constexpr uint32_t kLeafBit = 0x80000000u;
+
+struct alignas(16) GNode {   // 128 bytes
+  float bmin_x[4], bmax_x[4];
+  float bmin_y[4], bmax_y[4];
+  float bmin_z[4], bmax_z[4];
+  int32_t child[4];
+  int32_t axes;            // axis_top | axis_left << 2 | axis_right << 4
+  uint16_t count[4];       // triangles in each leaf child
+  int32_t pad;
+};
+static_assert(sizeof(GNode) == 128, "GNode must be 128 bytes");
+
+struct GMaterial {
+  int32_t type;
+  float roughness;
+  float ior;
+  float pad;
+  float color[3];
+  float emission[3];
+  double color_d[3];
+  double emission_d[3];
+  double roughness_d;
+  double ior_d;
+};
+
+struct GEntity {
+  int32_t type;
+  int32_t material;
+  int32_t normal_inverse;
+  int32_t is_light;
+  // sphere / disk centre, uvplane origin (FP64: the hit test runs in FP64)
+  double p[3];
+  double radius;
+  // uvplane: unit axes, lengths and normal (plane.h:146-167)
+  double u_axis[3], v_axis[3], normal[3];
+  double u_length, v_length;
+  double area;
+  // mesh
+  int32_t node_base;       // root node index in the concatenated node array
+  int32_t slot_base;       // first leaf slot of this mesh
+  int32_t face_base;       // first face-normal record of this mesh
+  int32_t n_faces;
+  float bmin[3], bmax[3];  // bounds (for scene extents)
+};
+
+struct GMedium {
+  float sigma_s_mean;      // ParticipatingMedia::scattering
+  float sigma_t_mean;      // ParticipatingMedia::transmittance
+  float sigma_s[3];        // scatteringColor
+  float sigma_t[3];        // transmittanceColor
+  float g[3];              // phase_prm
+  int32_t on;
+};
+
+// Everything a kernel needs, passed by value (fits the 4 KB param space).
+struct DevScene {
+  const GEntity* ents;
+  const GMaterial* mats;
+  const GNode* nodes;
+  const float4* tris;      // 3 per leaf slot
+  const float* fnorm;      // 3 per face
+  int32_t n_ents;
+  int32_t n_lights;
+  int32_t light_ent[kMaxLights];
+  double background[3];
+  double env_light[3];
+  GMedium medium;
+  float scene_scale;       // max |coordinate| of the scene bounds (ray offsets)
+};
+
+}  // namespace pr

@@ -1,0 +1,459 @@
+// Host-side scene import: pr_scene_desc -> flat GPU arrays.
+//
+// Restates the reference's scene set-up: entity geometry and areas
+// (plane.h:146-177, sphere.h:23-27), light registration and ordering
+// (scene_env.h:1567-1719, light.h:95-130), medium set-up
+// (ParticipatingMediaPrm.h:133-160), face normals (ObjLoader.cpp:577-700),
+// and the per-mesh QBVH: binary SAH build (BVH.cpp:194-348) flattened two
+// levels at a time into 4-wide nodes (QBVH.cpp:161-302).  The build follows
+// the reference's rules exactly (std::sort on centroids, the same cost
+// bookkeeping, 0.01 box padding) so node and leaf order are identical.
+//
+// Compiled with -ffp-contract=off: the FP64 build must not depend on
+// whether the host CPU fuses multiply-adds.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pr_internal.h"
+#include "scene_build.h"
+
+namespace pr {
+namespace {
+
+constexpr double kInf = 1.0e128;  // constant.h:33
+
+struct D3 {
+  double x, y, z;
+};
+inline D3 add(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline D3 sub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline D3 scale(D3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+// the reference's SSE dot adds the x,z lanes first (vector3d.h dot/sqr)
+inline double dot(D3 a, D3 b) { return (a.x * b.x + a.z * b.z) + a.y * b.y; }
+inline double len(D3 a) { return std::sqrt(dot(a, a)); }
+inline D3 unit(D3 a) { return scale(a, 1.0 / len(a)); }
+inline D3 cross(D3 a, D3 b) {
+  return {(a.y * b.z) - (a.z * b.y), (a.z * b.x) - (a.x * b.z), (a.x * b.y) - (a.y * b.x)};
+}
+inline D3 mk(const double* p) { return {p[0], p[1], p[2]}; }
+
+struct TriBox {
+  double bmin[3], bmax[3], c[3];
+};
+
+struct BNode {
+  double box[2][3];
+  int children[2] = {-1, -1};
+  int axis = 0;
+  std::vector<int> objects;
+};
+
+// BoundingBox::CalcSurfaceArea, member and template forms (BoundingBox.h:29-39)
+inline double area_member(const double* mn, const double* mx) {
+  double dx = mx[0] - mn[0], dy = mx[1] - mn[1], dz = mx[2] - mn[2];
+  return dx * dy + dx * dz + dy * dz;
+}
+inline double area_template(const double* mn, const double* mx) {
+  double d0 = mx[0] - mn[0], d1 = mx[1] - mn[1], d2 = mx[2] - mn[2];
+  return d0 * d1 + d1 * d2 + d0 * d2;
+}
+
+class SahBuilder {
+ public:
+  explicit SahBuilder(const std::vector<TriBox>& t) : tris_(t) {}
+  std::vector<BNode> nodes;
+
+  void run(int n) {
+    nodes.clear();
+    nodes.reserve(2 * (size_t)n);
+    nodes.emplace_back();
+    std::vector<int> all(n);
+    for (int i = 0; i < n; i++) all[i] = i;
+    build(all, 0);
+  }
+
+ private:
+  const std::vector<TriBox>& tris_;
+
+  void bounds(const std::vector<int>& objs, double* mn, double* mx) const {
+    for (int k = 0; k < 3; k++) { mn[k] = tris_[objs[0]].bmin[k]; mx[k] = tris_[objs[0]].bmax[k]; }
+    for (size_t i = 1; i < objs.size(); i++) {
+      const TriBox& a = tris_[objs[i]];
+      for (int k = 0; k < 3; k++) {
+        if (a.bmin[k] < mn[k]) mn[k] = a.bmin[k];
+        if (a.bmax[k] > mx[k]) mx[k] = a.bmax[k];
+      }
+    }
+  }
+  static void merge(double* mn, double* mx, const TriBox& b) {
+    for (int k = 0; k < 3; k++) {
+      mn[k] = std::min(mn[k], b.bmin[k]);
+      mx[k] = std::max(mx[k], b.bmax[k]);
+    }
+  }
+  void sort_axis(std::vector<int>& v, int axis) const {
+    const std::vector<TriBox>& t = tris_;
+    std::sort(v.begin(), v.end(), [&t, axis](int a, int b) { return t[a].c[axis] < t[b].c[axis]; });
+  }
+  void build(const std::vector<int>& targets, int index) {
+    bounds(targets, nodes[index].box[0], nodes[index].box[1]);
+    const double inv_surf = 1.0 / area_template(nodes[index].box[0], nodes[index].box[1]);
+    const size_t n = targets.size();
+    int best_axis = -1, best_index = -1;
+    double best_cost = -1;
+    std::vector<double> left_area(n), right_area(n);
+    for (int axis = 0; axis < 3; axis++) {
+      std::vector<int> L = targets, R;
+      sort_axis(L, axis);
+      right_area[n - 1] = kInf;
+      R.push_back(L.back());
+      L.pop_back();
+      double mn[3], mx[3];
+      bounds(R, mn, mx);
+      for (int i = (int)L.size() - 1; i >= 0; i--) {
+        right_area[i] = area_member(mn, mx);
+        merge(mn, mx, tris_[L[i]]);
+        R.push_back(L.back());
+        L.pop_back();
+      }
+      L.push_back(R.back());
+      R.pop_back();
+      bounds(L, mn, mx);
+      const double leaf_cost = (double)n;
+      for (int i = (int)R.size() - 1, cut = 0; i >= 0; i--, cut++) {
+        left_area[cut] = area_member(mn, mx);
+        merge(mn, mx, tris_[R.back()]);
+        L.push_back(R.back());
+        R.pop_back();
+        // sizes are taken after the move, as the reference does (BVH.cpp:288-292)
+        const double cost = 2.0 + (left_area[cut] * (double)L.size() + right_area[cut] * (double)R.size()) * inv_surf;
+        if ((cost < best_cost || best_cost == -1) && cost < leaf_cost) {
+          best_cost = cost;
+          best_index = cut;
+          best_axis = axis;
+        }
+      }
+    }
+    if (best_axis == -1) {
+      nodes[index].objects = targets;
+      return;
+    }
+    std::vector<int> lefts = targets;
+    sort_axis(lefts, best_axis);
+    std::vector<int> rights(lefts.begin() + best_index + 1, lefts.end());
+    lefts.resize(best_index + 1);
+    const int c0 = (int)nodes.size();
+    nodes[index].axis = best_axis;
+    nodes[index].children[0] = c0;
+    nodes[index].children[1] = c0 + 1;
+    nodes.emplace_back();
+    nodes.emplace_back();
+    build(lefts, c0);
+    build(rights, c0 + 1);
+  }
+};
+
+inline bool is_leaf(const BNode& b) { return b.children[0] == -1; }
+
+// Flattens a binary SAH tree into 4-wide nodes, the reference way
+// (QBVH.cpp:202-302): grandchildren in slots 2i+j, a leaf child in slot 2i
+// with slot 2i+1 invalid, new nodes numbered in depth-first order.
+class Flattener {
+ public:
+  Flattener(const std::vector<BNode>& b, MeshQbvh& out) : bvh_(b), out_(out) {}
+  void run() {
+    out_.nodes.clear();
+    out_.ref_leaf.clear();
+    out_.leaf_tris.clear();
+    out_.nodes.emplace_back();
+    flatten(0, 0);
+  }
+
+ private:
+  const std::vector<BNode>& bvh_;
+  MeshQbvh& out_;
+
+  void make_leaf(size_t index, const BNode& leaf, int slot) {
+    RefNode& rn = out_.nodes[index];
+    rn.ref_child[slot] = (int64_t)(((uint64_t)1 << 63) | (uint64_t)out_.ref_leaf.size());
+    rn.leaf_first[slot] = (int32_t)out_.leaf_tris.size();
+    rn.leaf_count[slot] = (int32_t)leaf.objects.size();
+    for (int o : leaf.objects) {
+      out_.ref_leaf.push_back(o);
+      out_.leaf_tris.push_back(o);
+    }
+    out_.ref_leaf.push_back(-1);
+  }
+  void put_box(size_t index, const BNode& b, int slot) {
+    for (int a = 0; a < 3; a++) {
+      out_.nodes[index].box[0][a][slot] = (float)b.box[0][a];
+      out_.nodes[index].box[1][a][slot] = (float)b.box[1][a];
+    }
+  }
+  void flatten(size_t index, int target) {
+    const BNode& nt = bvh_[target];
+    {
+      RefNode& rn = out_.nodes[index];
+      rn.axis_top = nt.axis;
+      rn.axis_left = is_leaf(bvh_[nt.children[0]]) ? 0 : bvh_[nt.children[0]].axis;
+      rn.axis_right = is_leaf(bvh_[nt.children[1]]) ? 0 : bvh_[nt.children[1]].axis;
+    }
+    for (int i = 0; i < 2; i++) {
+      const BNode& child = bvh_[nt.children[i]];
+      if (is_leaf(child)) {
+        const int slot = 2 * i;
+        make_leaf(index, child, slot);
+        out_.nodes[index].ref_child[slot + 1] = -1;
+        put_box(index, child, slot);
+      } else {
+        for (int j = 0; j < 2; j++) {
+          const int slot = 2 * i + j;
+          const int gci = child.children[j];
+          put_box(index, bvh_[gci], slot);
+          if (is_leaf(bvh_[gci])) {
+            make_leaf(index, bvh_[gci], slot);
+          } else {
+            const size_t nn = out_.nodes.size();
+            out_.nodes.emplace_back();
+            out_.nodes[index].ref_child[slot] = (int64_t)nn;
+            flatten(nn, gci);
+          }
+        }
+      }
+    }
+  }
+};
+
+}  // namespace
+
+int build_mesh_qbvh(const float* vertices, const int32_t* faces, int n_faces, MeshQbvh& out, std::string& err) {
+  // Triangle::CreateBoundingBox (polygon.h:686-703): 0.01 padding
+  std::vector<TriBox> boxes((size_t)n_faces);
+  for (int f = 0; f < n_faces; f++) {
+    double mn[3] = {kInf, kInf, kInf}, mx[3] = {-kInf, -kInf, -kInf};
+    for (int k = 0; k < 3; k++) {
+      const float* v = vertices + 3 * (size_t)faces[3 * (size_t)f + k];
+      for (int a = 0; a < 3; a++) {
+        const double x = v[a];
+        if (mn[a] > x) mn[a] = x;
+        if (mx[a] < x) mx[a] = x;
+      }
+    }
+    for (int a = 0; a < 3; a++) {
+      boxes[f].bmin[a] = mn[a] - 0.01;
+      boxes[f].bmax[a] = mx[a] + 0.01;
+      // BoundingBox centre: (min + max) / 2.0 (BoundingBox.h:14-19)
+      boxes[f].c[a] = (boxes[f].bmin[a] + boxes[f].bmax[a]) / 2.0;
+    }
+  }
+  SahBuilder b(boxes);
+  b.run(n_faces);
+  if (is_leaf(b.nodes[0])) {
+    err = "mesh too small: its SAH root is a leaf, so the reference would fall back to a binary BVH";
+    return PR_E_BUILD;
+  }
+  Flattener fl(b.nodes, out);
+  fl.run();
+  for (const RefNode& rn : out.nodes)
+    for (int s = 0; s < 4; s++)
+      if (rn.leaf_count[s] > 0xFFFF) {
+        err = "QBVH leaf larger than 65535 triangles";
+        return PR_E_BUILD;
+      }
+  return PR_OK;
+}
+
+// Obj::CalcNormalVector for meshes without vertex normals (ObjLoader.cpp:582-598, :686-697)
+void face_normals(const float* V, const int32_t* F, int n_faces, std::vector<float>& out) {
+  out.resize(3 * (size_t)n_faces);
+  for (int f = 0; f < n_faces; f++) {
+    const int32_t* fc = F + 3 * (size_t)f;
+    float dx1 = V[3 * fc[1]] - V[3 * fc[0]], dy1 = V[3 * fc[1] + 1] - V[3 * fc[0] + 1],
+          dz1 = V[3 * fc[1] + 2] - V[3 * fc[0] + 2];
+    float dx2 = V[3 * fc[2]] - V[3 * fc[0]], dy2 = V[3 * fc[2] + 1] - V[3 * fc[0] + 1],
+          dz2 = V[3 * fc[2] + 2] - V[3 * fc[0] + 2];
+    float nx = dy1 * dz2 - dz1 * dy2, ny = dz1 * dx2 - dx1 * dz2, nz = dx1 * dy2 - dy1 * dx2;
+    float a = std::sqrt(nx * nx + ny * ny + nz * nz);
+    if (a != 0.0f) {
+      nx /= a;
+      ny /= a;
+      nz /= a;
+    }
+    out[3 * f] = nx;
+    out[3 * f + 1] = ny;
+    out[3 * f + 2] = nz;
+  }
+}
+
+static bool is_light(const pr_material& m) {  // Material::isLight (material.h)
+  const D3 c = mk(m.color), e = mk(m.emission);
+  return m.type == PR_MAT_DIFFUSE && len(c) < 0.001 && len(e) > 0.001;
+}
+
+int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
+  hs = HostScene();
+  if (!d || d->n_entities < 0 || d->n_materials < 0 || d->n_meshes < 0) { err = "null or negative scene sizes"; return PR_E_ARG; }
+  if (d->n_entities > kMaxEntities) { err = "too many entities"; return PR_E_ARG; }
+  if ((d->n_materials > 0 && !d->materials) || (d->n_entities > 0 && !d->entities) ||
+      (d->n_meshes > 0 && !d->meshes)) { err = "null scene array"; return PR_E_ARG; }
+  for (int i = 0; i < d->n_materials; i++) {
+    const pr_material& pm = d->materials[i];
+    GMaterial g;
+    memset(&g, 0, sizeof(g));
+    g.type = pm.type;
+    g.roughness = (float)pm.roughness;
+    g.ior = (float)pm.refractive_index;
+    for (int k = 0; k < 3; k++) {
+      g.color[k] = (float)pm.color[k];
+      g.emission[k] = (float)pm.emission[k];
+      g.color_d[k] = pm.color[k];
+      g.emission_d[k] = pm.emission[k];
+    }
+    g.roughness_d = pm.roughness;
+    g.ior_d = pm.refractive_index;
+    if (pm.type != PR_MAT_DIFFUSE && pm.type != PR_MAT_SPECULAR && pm.type != PR_MAT_REFRACTION &&
+        pm.type != PR_MAT_REFRACTION_FRESNEL) {
+      err = "material type " + std::to_string(pm.type) + " is not on this path yet";
+      return PR_E_UNSUPPORTED;
+    }
+    hs.mats.push_back(g);
+  }
+  // global medium (scene_env.h:1892-1896 + setup_Scattering)
+  {
+    const pr_medium& m = d->medium;
+    double ss[3], sa[3];
+    for (int k = 0; k < 3; k++) { ss[k] = m.sigma_s_rgb[k]; sa[k] = m.sigma_a_rgb[k]; }
+    double s_mean = (ss[0] + ss[1] + ss[2]) / 3, a_mean = (sa[0] + sa[1] + sa[2]) / 3;
+    double t_mean = s_mean + a_mean;
+    GMedium& g = hs.medium;
+    memset(&g, 0, sizeof(g));
+    if (t_mean < 1.0e-12) {
+      g.on = 0;
+      for (int k = 0; k < 3; k++) { g.sigma_s[k] = 1.0f; g.sigma_t[k] = 2.0f; }
+    } else {
+      g.on = d->participating_media ? 1 : 0;
+      g.sigma_s_mean = (float)s_mean;
+      g.sigma_t_mean = (float)t_mean;
+      for (int k = 0; k < 3; k++) { g.sigma_s[k] = (float)ss[k]; g.sigma_t[k] = (float)(ss[k] + sa[k]); }
+    }
+    for (int k = 0; k < 3; k++) g.g[k] = (float)m.phase_g[k];
+  }
+  for (int k = 0; k < 3; k++) {
+    hs.background[k] = d->background[k];
+    hs.env_light[k] = d->environment_light[k];
+  }
+  double ext = 1.0;
+  auto grow = [&ext](double x) { ext = std::max(ext, std::fabs(x)); };
+  for (int i = 0; i < d->n_entities; i++) {
+    const pr_entity& pe = d->entities[i];
+    if (pe.material < 0 || pe.material >= d->n_materials) { err = "entity material out of range"; return PR_E_SCENE; }
+    GEntity g;
+    memset(&g, 0, sizeof(g));
+    g.type = pe.type;
+    g.material = pe.material;
+    g.normal_inverse = pe.normal_inverse < 0 ? -1 : 1;
+    const pr_material& pm = d->materials[pe.material];
+    if (pe.type == PR_ENT_SPHERE) {
+      for (int k = 0; k < 3; k++) g.p[k] = pe.p[k];
+      g.radius = pe.radius;
+      g.area = 12.5663706143591729538505735331180115 * pe.radius * pe.radius;  // PS_FORPI r^2
+      if (pe.radius < 1.0e4)
+        for (int k = 0; k < 3; k++) { grow(pe.p[k] - pe.radius); grow(pe.p[k] + pe.radius); }
+    } else if (pe.type == PR_ENT_UVPLANE) {  // UVPlane ctor + CalcArea (plane.h:146-177)
+      const D3 U = mk(pe.u), V = mk(pe.v);
+      g.u_length = len(U);
+      g.v_length = len(V);
+      const D3 u = unit(U), v = unit(V), n = unit(cross(u, v));
+      for (int k = 0; k < 3; k++) {
+        g.p[k] = pe.p[k];
+        g.u_axis[k] = (&u.x)[k];
+        g.v_axis[k] = (&v.x)[k];
+        g.normal[k] = (&n.x)[k];
+      }
+      g.area = len(scale(u, g.u_length)) * len(scale(v, g.v_length)) * (1.0 - std::pow(dot(u, v), 2.0));
+      for (int k = 0; k < 3; k++) grow(pe.p[k]);
+    } else if (pe.type == PR_ENT_POLYGON) {
+      if (pe.mesh < 0 || pe.mesh >= d->n_meshes) { err = "entity mesh out of range"; return PR_E_SCENE; }
+      const pr_mesh& pm_ = d->meshes[pe.mesh];
+      if (pm_.n_faces <= 0 || !pm_.vertices || !pm_.faces) { err = "empty mesh"; return PR_E_SCENE; }
+      for (int64_t f = 0; f < 3 * (int64_t)pm_.n_faces; f++)
+        if (pm_.faces[f] < 0 || pm_.faces[f] >= pm_.n_vertices) { err = "face index out of range"; return PR_E_SCENE; }
+      if (is_light(pm)) { err = "mesh lights are not sampled by the reference's next-event estimation"; return PR_E_UNSUPPORTED; }
+      MeshQbvh q;
+      int st = build_mesh_qbvh(pm_.vertices, pm_.faces, pm_.n_faces, q, err);
+      if (st != PR_OK) return st;
+      std::vector<float> fn;
+      if (pm_.face_normals) fn.assign(pm_.face_normals, pm_.face_normals + 3 * (size_t)pm_.n_faces);
+      else face_normals(pm_.vertices, pm_.faces, pm_.n_faces, fn);
+      g.node_base = (int32_t)hs.nodes.size();
+      g.slot_base = (int32_t)(hs.tris.size() / 3);
+      g.face_base = (int32_t)(hs.fnorm.size() / 3);
+      g.n_faces = pm_.n_faces;
+      // GPU nodes
+      for (const RefNode& rn : q.nodes) {
+        GNode gn;
+        memset(&gn, 0, sizeof(gn));
+        for (int s = 0; s < 4; s++) {
+          gn.bmin_x[s] = rn.box[0][0][s]; gn.bmax_x[s] = rn.box[1][0][s];
+          gn.bmin_y[s] = rn.box[0][1][s]; gn.bmax_y[s] = rn.box[1][1][s];
+          gn.bmin_z[s] = rn.box[0][2][s]; gn.bmax_z[s] = rn.box[1][2][s];
+          const int64_t c = rn.ref_child[s];
+          if (c == -1) {
+            gn.child[s] = kChildInvalid;
+          } else if (c < 0) {  // leaf
+            gn.child[s] = (int32_t)(kLeafBit | (uint32_t)(g.slot_base + rn.leaf_first[s]));
+            gn.count[s] = (uint16_t)rn.leaf_count[s];
+          } else {
+            gn.child[s] = (int32_t)(g.node_base + c);
+          }
+        }
+        gn.axes = rn.axis_top | (rn.axis_left << 2) | (rn.axis_right << 4);
+        hs.nodes.push_back(gn);
+      }
+      for (int t : q.leaf_tris) {
+        for (int k = 0; k < 3; k++) {
+          const float* v = pm_.vertices + 3 * (size_t)pm_.faces[3 * (size_t)t + k];
+          float4 f4;
+          f4.x = v[0];
+          f4.y = v[1];
+          f4.z = v[2];
+          int32_t w = (k == 0) ? t : 0;
+          memcpy(&f4.w, &w, 4);
+          hs.tris.push_back(f4);
+          for (int a = 0; a < 3; a++) grow(v[a]);
+        }
+      }
+      hs.fnorm.insert(hs.fnorm.end(), fn.begin(), fn.end());
+      hs.mesh_qbvh.push_back(std::move(q));
+      hs.mesh_entity.push_back(i);
+    } else {
+      err = "entity type " + std::to_string(pe.type) + " is not on this path yet";
+      return PR_E_UNSUPPORTED;
+    }
+    hs.ents.push_back(g);
+  }
+  // lights: registration order, then LightList::random_light_setup's sort
+  // by power, descending (light.h:97; power = area * |emission|)
+  struct L {
+    double power;
+    int ent;
+  };
+  std::vector<L> lights;
+  for (int i = 0; i < (int)hs.ents.size(); i++) {
+    const pr_material& pm = d->materials[hs.ents[i].material];
+    if (is_light(pm)) {
+      hs.ents[i].is_light = 1;
+      lights.push_back({hs.ents[i].area * len(mk(pm.emission)), i});
+    }
+  }
+  std::sort(lights.begin(), lights.end(), [](const L& a, const L& b) { return a.power > b.power; });
+  if ((int)lights.size() > kMaxLights) { err = "too many lights"; return PR_E_ARG; }
+  for (const L& l : lights) hs.light_ent.push_back(l.ent);
+  hs.scene_scale = (float)ext;
+  return PR_OK;
+}
+
+}  // namespace pr

@@ -1,0 +1,48 @@
+// Host scene built from a pr_scene_desc (see scene_build.cpp).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "pr_internal.h"
+
+namespace pr {
+
+// One 4-wide node in the reference's own terms (QBVH.h:53-61), kept on the
+// host for export and for the GPU node encoding.
+struct RefNode {
+  float box[2][3][4] = {};     // [min/max][xyz][child]
+  int64_t ref_child[4] = {0, 0, 0, 0};  // QBVH child word: leaf = top bit | ref leaf start
+  int32_t leaf_first[4] = {0, 0, 0, 0};  // first slot in leaf_tris (leaf children)
+  int32_t leaf_count[4] = {0, 0, 0, 0};
+  int32_t axis_top = 0, axis_left = 0, axis_right = 0;
+};
+
+struct MeshQbvh {
+  std::vector<RefNode> nodes;
+  std::vector<int32_t> ref_leaf;   // face ids with -1 terminators (m_leafObjectArray)
+  std::vector<int32_t> leaf_tris;  // face ids, leaves contiguous, no terminators
+};
+
+struct HostScene {
+  std::vector<GMaterial> mats;
+  std::vector<GEntity> ents;
+  std::vector<GNode> nodes;
+  std::vector<float4> tris;
+  std::vector<float> fnorm;
+  std::vector<int32_t> light_ent;
+  std::vector<MeshQbvh> mesh_qbvh;
+  std::vector<int32_t> mesh_entity;  // entity index of each mesh_qbvh
+  GMedium medium{};
+  double background[3] = {0, 0, 0};
+  double env_light[3] = {0, 0, 0};
+  float scene_scale = 1.0f;
+};
+
+int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err);
+int build_mesh_qbvh(const float* vertices, const int32_t* faces, int n_faces, MeshQbvh& out, std::string& err);
+void face_normals(const float* V, const int32_t* F, int n_faces, std::vector<float>& out);
+
+}  // namespace pr

@@ -1,0 +1,114 @@
+"""Python host side of the GPU renderer: a thin wrapper over the C ABI that
+mirrors the reference's driver sequence (SceneEnv::Load -> CreateEntList ->
+Render::Run, main.cpp:21-229) so user code and tests read like the
+reference's own flow:
+
+    ctx = Context(0)
+    ctx.upload(scene)             # SceneEnv::Load + CreateEntList + QBVH build
+    img = ctx.render(scene)       # Render::Run -> accumulated image (H, W, 3)
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from ._lib import PrenderError, load  # noqa: F401
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def qbvh_build_host(vertices: np.ndarray, faces: np.ndarray) -> dict:
+    """Reference-layout QBVH of one mesh, built on the host (no GPU)."""
+    L = load()
+    v = np.ascontiguousarray(vertices, dtype=np.float32)
+    f = np.ascontiguousarray(faces, dtype=np.int32)
+    nn, nl = C.c_int64(0), C.c_int64(0)
+    rc = L.pr_qbvh_build_host(_p(v), v.shape[0], _p(f), f.shape[0], C.byref(nn), C.byref(nl),
+                              None, None, None, None)
+    if rc != 0:
+        raise PrenderError(rc, "QBVH build rejected the mesh")
+    boxes = np.empty((nn.value, 24), np.float32)
+    children = np.empty((nn.value, 4), np.int64)
+    axes = np.empty((nn.value, 3), np.int32)
+    leaf = np.empty(nl.value, np.int32)
+    rc = L.pr_qbvh_build_host(_p(v), v.shape[0], _p(f), f.shape[0], None, None, _p(boxes), _p(children),
+                              _p(axes), _p(leaf))
+    if rc != 0:
+        raise PrenderError(rc, "QBVH build failed")
+    return dict(boxes=boxes, children=children, axes=axes, leaf=leaf)
+
+
+class Context:
+    """One GPU context (pr_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        st = C.c_int(0)
+        self.h = self.L.pr_create(device, C.byref(st))
+        if not self.h:
+            raise PrenderError(st.value, f"pr_create({device}) failed (no usable CUDA device?)")
+        self._desc = None
+        self.scene = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.pr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise PrenderError(rc, self.L.pr_last_error(self.h).decode())
+
+    # ---- scene ----
+    def upload(self, scene) -> None:
+        self._desc = scene.to_desc()
+        self._check(self.L.pr_scene_upload(self.h, C.byref(self._desc.desc)))
+        self.scene = scene
+
+    def qbvh(self, entity: int) -> dict:
+        nn, nl = C.c_int64(0), C.c_int64(0)
+        self._check(self.L.pr_qbvh_info(self.h, entity, C.byref(nn), C.byref(nl)))
+        boxes = np.empty((nn.value, 24), np.float32)
+        children = np.empty((nn.value, 4), np.int64)
+        axes = np.empty((nn.value, 3), np.int32)
+        leaf = np.empty(nl.value, np.int32)
+        self._check(self.L.pr_qbvh_export(self.h, entity, _p(boxes), _p(children), _p(axes), _p(leaf)))
+        return dict(boxes=boxes, children=children, axes=axes, leaf=leaf)
+
+    # ---- queries ----
+    def first_hit(self, rays: np.ndarray) -> dict:
+        rays = np.ascontiguousarray(rays, dtype=np.float64)
+        n = rays.shape[0]
+        ent = np.empty(n, np.int32)
+        prim = np.empty(n, np.int32)
+        t = np.empty(n, np.float64)
+        self._check(self.L.pr_first_hit(self.h, _p(rays), n, _p(ent), _p(prim), _p(t)))
+        return dict(entity=ent, prim=prim, t=t)
+
+    def render(self, scene=None, settings=None, camera=None, sample_offset: int = 0,
+               accumulate: np.ndarray | None = None) -> np.ndarray:
+        """Render::Run: returns the (H, W, 3) float32 image in the reference's
+        row order (row 0 = image index 0, i.e. the bottom scan line)."""
+        scene = scene or self.scene
+        cam = (camera or scene.camera).to_c()
+        prm = (settings or scene.settings).to_c()
+        if accumulate is not None:
+            out = np.ascontiguousarray(accumulate, dtype=np.float32)
+        else:
+            out = np.empty((cam.height, cam.width, 3), np.float32)
+        self._check(self.L.pr_render(self.h, C.byref(cam), C.byref(prm), _p(out), sample_offset,
+                                     1 if accumulate is not None else 0))
+        return out
+
+    def stats(self) -> dict:
+        s = A.pr_render_stats()
+        self._check(self.L.pr_last_render_stats(self.h, C.byref(s)))
+        return dict(paths=s.paths, segments=s.segments, nodes_visited=s.nodes_visited, tri_tests=s.tri_tests,
+                    device_ms=s.device_ms)

@@ -192,3 +192,16 @@ def camera_rays(scene: Scene, jitter_seed: int = 0) -> np.ndarray:
     dirs /= np.linalg.norm(dirs, axis=-1, keepdims=True)
     org = np.broadcast_to(pos, dirs.shape)
     return np.ascontiguousarray(np.concatenate([org, dirs], axis=-1).reshape(-1, 6))
+
+
+def rays_toward(vertices: np.ndarray, lo, hi, n: int, seed: int = 0) -> np.ndarray:
+    """n rays from random points in the box [lo, hi] aimed at random mesh
+    vertices (jittered), so that most of them reach the mesh; FP64."""
+    rng = np.random.default_rng(seed)
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    org = lo + (hi - lo) * rng.random((n, 3))
+    tgt = vertices[rng.integers(0, vertices.shape[0], n)].astype(np.float64) + rng.normal(scale=0.05, size=(n, 3))
+    d = tgt - org
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.ascontiguousarray(np.concatenate([org, d], axis=1))

@@ -1,0 +1,146 @@
+"""GPU parity tests, through the C ABI (ctypes), against the oracle and the
+reference-generated golden fixtures.
+
+* closest hits: entity, face id and FP64 distance bit-exact;
+* QBVH built by the library equals the reference's;
+* images: the GPU estimate (independent counter-based streams) agrees with
+  the reference's high-spp render within 3 sigma per pixel for all but a
+  small fraction of pixels, and its RMSE is at the noise level.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from prender_gb300 import gpu, scenes
+from prender_gb300 import _abi as A
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import __graft_entry__ as g
+    g.build_library()
+    c = gpu.Context(0)
+    yield c
+    c.close()
+
+
+def test_first_hit_golden_bit_exact(ctx, golden):
+    s = scenes.mesh_cornell(width=32, height=24, samples=1, supersamples=2, subdiv=3)
+    ctx.upload(s)
+    g = golden["mesh_s3_qbvh_firsthit"]
+    h = ctx.first_hit(g["rays"])
+    assert np.array_equal(h["entity"], g["fh_entity"])
+    assert np.array_equal(h["prim"], g["fh_prim"])
+    assert np.array_equal(h["t"], g["fh_t"])
+
+
+def test_qbvh_upload_matches_golden(ctx, golden):
+    s = scenes.mesh_cornell(width=32, height=24, samples=1, supersamples=2, subdiv=3)
+    ctx.upload(s)
+    g = golden["mesh_s3_qbvh_firsthit"]
+    q = ctx.qbvh(2)
+    assert np.array_equal(q["children"], g["ico_children"])
+    assert np.array_equal(q["leaf"], g["ico_leaf"])
+
+
+def test_first_hit_spheres_bit_exact(ctx):
+    s = scenes.cornell_spheres(width=16, height=12)
+    ctx.upload(s)
+    rays = np.concatenate([scenes.random_rays((2, 1, 1), (98, 80, 170), 20000, seed=11), scenes.camera_rays(s)])
+    h = ctx.first_hit(rays)
+    o = O.OracleScene(s).first_hit(rays)
+    assert np.array_equal(h["entity"], o["entity"])
+    assert np.array_equal(h["t"], o["t"])
+
+
+def test_first_hit_full_size_mesh_bit_exact(ctx):
+    """327,680-triangle displaced icosphere (the mesh Cornell box workload)."""
+    s = scenes.mesh_cornell(subdiv=7)
+    ctx.upload(s)
+    ico = s.meshes[1].vertices
+    rays = np.concatenate([scenes.rays_toward(ico, (2, 1, 100), (98, 80, 249), 200000, seed=21),
+                           scenes.random_rays((2, 1, 1), (98, 80, 249), 50000, seed=22)])
+    h = ctx.first_hit(rays)
+    o = O.OracleScene(s).first_hit(rays)
+    assert (o["entity"] == 2).sum() > 150000
+    assert np.array_equal(h["entity"], o["entity"])
+    assert np.array_equal(h["prim"], o["prim"])
+    assert np.array_equal(h["t"], o["t"])
+
+
+def _batches(ctx, scene, nb, spp_per_batch):
+    st = scene.settings
+    # samples per batch after the tent fold = samples * ss^2
+    imgs = []
+    for b in range(nb):
+        imgs.append(ctx.render(scene, sample_offset=b * spp_per_batch).astype(np.float64))
+    return np.stack(imgs)
+
+
+@pytest.mark.parametrize("name,build,tol_frac", [
+    ("spheres_64x48_1024spp", lambda: scenes.cornell_spheres(width=64, height=48, samples=256, supersamples=2), 0.02),
+    ("mesh_64x48_512spp", lambda: scenes.mesh_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3), 0.02),
+    ("glass_64x48_512spp", lambda: scenes.mesh_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3,
+                                                       material="glass"), 0.03),
+])
+def test_image_matches_reference_statistically(ctx, golden, name, build, tol_frac):
+    s = build()
+    ctx.upload(s)
+    ref = golden["render_highspp"][name].astype(np.float64)
+    nb = 16
+    spp = s.settings.spp
+    b = _batches(ctx, s, nb, spp)
+    mean = b.mean(0)
+    sd_batch = b.std(0, ddof=1)                 # spread of one spp-sample estimate
+    sigma = np.sqrt(sd_batch ** 2 / nb + sd_batch ** 2) + 1e-6  # GPU mean + reference (same spp as a batch)
+    z = np.abs(mean - ref) / sigma
+    frac = float((z > 3.0).mean())
+    rmse = float(np.sqrt(((mean - ref) ** 2).mean()))
+    noise = float(np.sqrt((sigma ** 2).mean()))
+    rel_mean = abs(mean.mean() - ref.mean()) / ref.mean()
+    print(f"{name}: >3sigma fraction {frac:.4f}, rmse {rmse:.3e} vs noise {noise:.3e}, mean rel diff {rel_mean:.4f}")
+    assert rel_mean < 0.01
+    assert frac < tol_frac
+    assert rmse < 1.3 * noise
+
+
+def test_render_is_deterministic_and_shards_by_sample_offset(ctx):
+    s = scenes.mesh_cornell(width=48, height=36, samples=8, supersamples=2, subdiv=3)
+    ctx.upload(s)
+    a = ctx.render(s)
+    b = ctx.render(s)
+    assert np.array_equal(a, b)
+    half = scenes.mesh_cornell(width=48, height=36, samples=4, supersamples=2, subdiv=3).settings
+    h0 = ctx.render(s, settings=half, sample_offset=0)
+    h1 = ctx.render(s, settings=half, sample_offset=16)
+    np.testing.assert_allclose((h0 + h1) / 2, a, rtol=1e-5, atol=1e-7)
+
+
+def test_device_loop_cap_reports_an_error(ctx):
+    s = scenes.cornell_spheres(width=16, height=12, samples=1, supersamples=1)
+    ctx.upload(s)
+    st = s.settings
+    st.max_path_vertices = 1
+    with pytest.raises(gpu.PrenderError) as e:
+        ctx.render(s, settings=st)
+    assert e.value.code == A.PR_E_DEVICE and "loop-cap" in str(e.value)
+    st.max_path_vertices = 0
+    img = ctx.render(s, settings=st)  # the context stays usable
+    assert np.isfinite(img).all()
+
+
+def test_bad_arguments_are_errors(ctx):
+    s = scenes.cornell_spheres(width=16, height=12)
+    ctx.upload(s)
+    st = s.settings
+    st.samples = 0
+    with pytest.raises(gpu.PrenderError) as e:
+        ctx.render(s, settings=st)
+    assert e.value.code == A.PR_E_ARG
+    bad = scenes.cornell_spheres()
+    bad.entities[0].material = 99
+    with pytest.raises(gpu.PrenderError) as e:
+        ctx.upload(bad)
+    assert e.value.code == A.PR_E_SCENE
