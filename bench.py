@@ -35,9 +35,12 @@ def baseline_metric():
         return METRIC
 
 
-def workload(small: bool):
+def workload(small: bool, profile: bool = False):
     from prender_gb300 import scenes
-    if small:
+    if profile:
+        s = scenes.mesh_cornell(width=256, height=192, samples=4, supersamples=2, subdiv=7)
+        name = "mesh_cornell_256x192_16spp_subdiv7"
+    elif small:
         s = scenes.mesh_cornell(width=256, height=192, samples=4, supersamples=2, subdiv=5)
         name = "mesh_cornell_256x192_16spp_subdiv5"
     else:
@@ -167,7 +170,7 @@ def run_gpu(args):
     import __graft_entry__ as g
     g.build_library()
     from prender_gb300 import gpu
-    scene, name = workload(args.small)
+    scene, name = workload(args.small, args.profile)
     W, H, spp = scene.camera.width, scene.camera.height, scene.settings.spp
     ctx = gpu.Context(local)
     t0 = time.perf_counter()
@@ -287,6 +290,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--mode", default="megakernel")
     ap.add_argument("--small", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="full scene, 256x192x16spp image (ncu captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-rows", type=int, default=48)
     args = ap.parse_args()

@@ -232,6 +232,12 @@ int pr_first_hit(pr_ctx* ctx, const double* rays, int64_t n, int32_t* entity,
 int pr_first_hit_dev(pr_ctx* ctx, const double* rays, int64_t n, int32_t* entity,
                      int32_t* prim, double* t);
 
+/* The renderer's own FP32 closest-hit query (near-first QBVH traversal with
+ * culling) on the same ray batch, for checking it against pr_first_hit:
+ * rays are converted to FP32 and the origin is used as given (no 1e-6
+ * push).  Outputs as pr_first_hit, t in FP64 holding the FP32 distance. */
+int pr_trace_fast(pr_ctx* ctx, const double* rays, int64_t n, int32_t* entity, int32_t* prim, double* t);
+
 /* ---- rendering -------------------------------------------------------- */
 /* Render::Run (render.h:1125-1455): accumulates samples [sample_offset,
  * sample_offset + samples*supersamples^2) of every pixel into rgb_accum

@@ -264,6 +264,29 @@ int pr_first_hit(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, int3
   return PR_OK;
 }
 
+int pr_trace_fast(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, int32_t* prim, double* t) {
+  if (!c) return PR_E_ARG;
+  if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  if (n < 0 || (n > 0 && (!rays || !entity || !prim || !t))) return fail(c, PR_E_ARG, "bad trace arguments");
+  if (n == 0) return PR_OK;
+  PR_CUDA(c, cudaSetDevice(c->device));
+  PR_CUDA(c, c->rays.ensure(sizeof(double) * 6 * (size_t)n));
+  PR_CUDA(c, c->ires.ensure(sizeof(int32_t) * (size_t)n));
+  PR_CUDA(c, c->jres.ensure(sizeof(int32_t) * (size_t)n));
+  PR_CUDA(c, c->dres.ensure(sizeof(double) * (size_t)n));
+  PR_CUDA(c, cudaMemcpyAsync(c->rays.p, rays, sizeof(double) * 6 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
+  PR_CUDA(c, launch_trace_fast(c->dev, (const double*)c->rays.p, n, (int32_t*)c->ires.p, (int32_t*)c->jres.p,
+                               (double*)c->dres.p, (uint32_t*)c->errword.p, c->stream));
+  int st = check_device_errors(c);
+  if (st != PR_OK) return st;
+  PR_CUDA(c, cudaMemcpyAsync(entity, c->ires.p, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaMemcpyAsync(prim, c->jres.p, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaMemcpyAsync(t, c->dres.p, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PR_OK;
+}
+
 // CameraScreenPram (render.h:105-150) and the Run() sample set-up (:1129-1139)
 static int prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, uint64_t sample_offset,
                           RenderCfg& g) {

@@ -71,14 +71,18 @@ __device__ __forceinline__ void make_vertex(const DevScene& S, float3 o, float3 
     const double il = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);
     v.p = f3((float)px, (float)py, (float)pz);
     v.n = f3((float)(nx * il), (float)(ny * il), (float)(nz * il));
-  } else {
+  } else if (e.type == PR_ENT_UVPLANE) {
     v.p = o + d * h.t;
-    if (e.type == PR_ENT_UVPLANE) {
-      v.n = f3((float)e.normal[0], (float)e.normal[1], (float)e.normal[2]);
-    } else {
-      const int face = __float_as_int(__ldg(S.tris + 3 * (size_t)h.slot).w);
-      v.n = ld3(S.fnorm + 3 * (size_t)(e.face_base + face));
-    }
+    v.n = f3((float)e.normal[0], (float)e.normal[1], (float)e.normal[2]);
+  } else {
+    // the hit point from the barycentrics: its error is a few ulps of the
+    // vertex coordinates, not of the ray length, which the ulp-scaled
+    // origin offset (offset_ray) relies on
+    const float4* T = S.tris + 3 * (size_t)h.slot;
+    const float4 A = __ldg(T), B = __ldg(T + 1), C = __ldg(T + 2);
+    const float w = 1.0f - h.u - h.v;
+    v.p = f3(w * A.x + h.u * B.x + h.v * C.x, w * A.y + h.u * B.y + h.v * C.y, w * A.z + h.u * B.z + h.v * C.z);
+    v.n = ld3(S.fnorm + 3 * (size_t)(e.face_base + __float_as_int(A.w)));
   }
   if (e.normal_inverse < 0) v.n = -v.n;
 }
@@ -135,8 +139,12 @@ __device__ float3 nee_surface(const DevScene& S, const Vertex& v, float3 on, flo
     if (dot0 >= 0.0f && dot1 >= 0.0f) {
       segs++;
       // visible iff nothing is hit closer than the light point - 1e-3
-      // (directLight_radiance.h:136-171)
-      if (!fast_occluded(S, origin, ldir, dist - 1.0e-3f, st, err)) {
+      // (directLight_radiance.h:136-171); the distance is measured from the
+      // shadow ray's own (offset) origin, which can sit ~1e-3 nearer to the
+      // light than the hit point
+      const float3 dlo = lp - origin;
+      const float disto = sqrtf(dot(dlo, dlo));
+      if (!fast_occluded(S, origin, dlo / disto, disto - 1.0e-3f, st, err)) {
         const float G = dot0 * dot1 / dist2;
         const GMaterial& lm = S.mats[le.material];
         float3 em = ld3(lm.emission);

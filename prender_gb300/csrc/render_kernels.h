@@ -30,6 +30,8 @@ struct RenderCfg {
 cudaError_t launch_megakernel(const DevScene& S, const RenderCfg& cfg, float* out, uint32_t* err,
                               unsigned long long* counters, cudaStream_t stream);
 cudaError_t launch_reduce(const float* partial, float* dst, int n3, int chunks, int accumulate, cudaStream_t stream);
+cudaError_t launch_trace_fast(const DevScene& S, const double* rays, int64_t n, int32_t* ent, int32_t* prim, double* t,
+                              uint32_t* err, cudaStream_t stream);
 cudaError_t launch_first_hit(const DevScene& S, const double* rays, int64_t n, int32_t* ent, int32_t* prim, double* t,
                              uint32_t* err, unsigned long long* counters, cudaStream_t stream);
 

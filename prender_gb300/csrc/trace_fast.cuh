@@ -14,7 +14,8 @@ namespace pr {
 struct FastHit {
   float t;
   int ent;
-  int slot;  // leaf slot of the triangle (meshes), -1 otherwise
+  int slot;   // leaf slot of the triangle (meshes), -1 otherwise
+  float u, v; // barycentrics of the triangle hit
 };
 
 struct TraceStats {
@@ -22,7 +23,8 @@ struct TraceStats {
   uint32_t tris;
 };
 
-__device__ __forceinline__ bool fast_tri(const float4* __restrict__ T, float3 o, float3 d, float tmax, float& t) {
+__device__ __forceinline__ bool fast_tri(const float4* __restrict__ T, float3 o, float3 d, float tmax, float& t, float& bu,
+                                         float& bv) {
   const float4 A = __ldg(T), B = __ldg(T + 1), C = __ldg(T + 2);
   const float3 v0 = f3(A.x, A.y, A.z);
   const float3 e1 = f3(B.x, B.y, B.z) - v0, e2 = f3(C.x, C.y, C.z) - v0;
@@ -39,6 +41,8 @@ __device__ __forceinline__ bool fast_tri(const float4* __restrict__ T, float3 o,
   const float tt = dot(e2, q) * inv;
   if (!(tt > 0.0f) || !(tt < tmax)) return false;
   t = tt;
+  bu = u;
+  bv = v;
   return true;
 }
 
@@ -68,7 +72,7 @@ __device__ __forceinline__ int box4(const GNode* __restrict__ node, float3 inv, 
 // QBVH closest hit (ANY = false) or any hit below tmax (ANY = true).
 template <bool ANY>
 __device__ __forceinline__ bool fast_qbvh(const DevScene& S, const GEntity& e, float3 o, float3 d, float3 inv, float& tbest,
-                                          int& slot, TraceStats& st, uint32_t* err) {
+                                          int& slot, float& bu, float& bv, TraceStats& st, uint32_t* err) {
   int32_t stack[kStackSize];
   int sp = 0;
   stack[sp++] = e.node_base;
@@ -104,10 +108,12 @@ __device__ __forceinline__ bool fast_qbvh(const DevScene& S, const GEntity& e, f
       const int32_t first = (int32_t)((uint32_t)child[c] & ~kLeafBit);
       for (int k = 0; k < cnt[c]; k++) {
         st.tris++;
-        float t;
-        if (fast_tri(S.tris + 3 * (size_t)(first + k), o, d, tbest, t)) {
+        float t, uu, vv;
+        if (fast_tri(S.tris + 3 * (size_t)(first + k), o, d, tbest, t, uu, vv)) {
           tbest = t;
           slot = first + k;
+          bu = uu;
+          bv = vv;
           hit = true;
           if (ANY) return true;
         }
@@ -171,19 +177,22 @@ __device__ __forceinline__ bool fast_closest(const DevScene& S, float3 o, float3
   h.t = 3.0e38f;
   h.ent = -1;
   h.slot = -1;
+  h.u = h.v = 0.0f;
   const float3 inv = safe_inv(d);
   for (int i = 0; i < S.n_ents; i++) {
     const GEntity& e = S.ents[i];
-    float t = h.t;
+    float t = h.t, bu = 0.0f, bv = 0.0f;
     int slot = -1;
     bool got = false;
     if (e.type == PR_ENT_SPHERE) got = fast_sphere(e, o, d, h.t, t);
     else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, o, d, h.t, t);
-    else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<false>(S, e, o, d, inv, t, slot, st, err);
+    else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<false>(S, e, o, d, inv, t, slot, bu, bv, st, err);
     if (got && t < h.t) {
       h.t = t;
       h.ent = i;
       h.slot = slot;
+      h.u = bu;
+      h.v = bv;
     }
   }
   return h.ent >= 0;
@@ -195,12 +204,12 @@ __device__ __forceinline__ bool fast_occluded(const DevScene& S, float3 o, float
   const float3 inv = safe_inv(d);
   for (int i = 0; i < S.n_ents; i++) {
     const GEntity& e = S.ents[i];
-    float t = tmax;
+    float t = tmax, bu, bv;
     int slot;
     bool got = false;
     if (e.type == PR_ENT_SPHERE) got = fast_sphere(e, o, d, tmax, t);
     else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, o, d, tmax, t);
-    else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<true>(S, e, o, d, inv, t, slot, st, err);
+    else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<true>(S, e, o, d, inv, t, slot, bu, bv, st, err);
     if (got) return true;
   }
   return false;

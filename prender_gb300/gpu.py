@@ -92,6 +92,16 @@ class Context:
         self._check(self.L.pr_first_hit(self.h, _p(rays), n, _p(ent), _p(prim), _p(t)))
         return dict(entity=ent, prim=prim, t=t)
 
+    def trace_fast(self, rays: np.ndarray) -> dict:
+        """The renderer's FP32 closest-hit query on the same batch."""
+        rays = np.ascontiguousarray(rays, dtype=np.float64)
+        n = rays.shape[0]
+        ent = np.empty(n, np.int32)
+        prim = np.empty(n, np.int32)
+        t = np.empty(n, np.float64)
+        self._check(self.L.pr_trace_fast(self.h, _p(rays), n, _p(ent), _p(prim), _p(t)))
+        return dict(entity=ent, prim=prim, t=t)
+
     def render(self, scene=None, settings=None, camera=None, sample_offset: int = 0,
                accumulate: np.ndarray | None = None) -> np.ndarray:
         """Render::Run: returns the (H, W, 3) float32 image in the reference's
