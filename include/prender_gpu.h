@@ -172,6 +172,12 @@ typedef struct pr_render_params {
   double sensor_response;     /* final image scale (default 1)               */
   int32_t max_path_vertices;  /* device cap on path length (0 = 512)         */
   int32_t flags;              /* PR_FLAG_*                                   */
+  int32_t total_spp;          /* samples of the whole frame when this call
+                                 renders one shard of it; 0 = this call's
+                                 samples*supersamples^2.  Sets the per-sample
+                                 weight 1/total_spp and so the luminance
+                                 clamp (render.h:1139, :1375-1384)          */
+  int32_t pad1;
 } pr_render_params;
 
 enum {

@@ -146,6 +146,8 @@ class pr_render_params(C.Structure):
         ("sensor_response", C.c_double),
         ("max_path_vertices", C.c_int32),
         ("flags", C.c_int32),
+        ("total_spp", C.c_int32),
+        ("pad1", C.c_int32),
     ]
 
 

@@ -3,8 +3,10 @@
 // by the context; every error becomes a status code plus pr_last_error().
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -14,6 +16,7 @@
 #include "pr_internal.h"
 #include "render_kernels.h"
 #include "scene_build.h"
+#include "wavefront.h"
 
 using namespace pr;
 
@@ -52,6 +55,14 @@ struct pr_ctx {
   DevBuf errword, counters;  // 4 bytes / 4 x u64
   DevBuf partial, out, rays, ires, jres, dres;
   pr_render_stats stats{};
+  // wavefront pool
+  DevBuf wf_o, wf_d, wf_beta, wf_dpw, wf_L, wf_sample, wf_hit, wf_hitv, wf_nee, wf_sho, wf_shd, wf_extq, wf_shq;
+  DevBuf wf_spo, wf_spd, wf_spb, wf_spw, wf_sps, wf_samp, wf_live, wf_pix, wf_ctl;
+  unsigned int wf_slots = 0;
+  cudaGraphExec_t wf_graph = nullptr;
+  unsigned int wf_graph_slots = 0;
+  bool wf_graph_failed = false;
+  WfCtl* wf_host_ctl = nullptr;
 };
 
 namespace {
@@ -127,8 +138,13 @@ void pr_destroy(pr_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (DevBuf* b : {&c->ents, &c->mats, &c->nodes, &c->tris, &c->fnorm, &c->errword, &c->counters, &c->partial,
-                    &c->out, &c->rays, &c->ires, &c->jres, &c->dres})
+                    &c->out, &c->rays, &c->ires, &c->jres, &c->dres, &c->wf_o, &c->wf_d, &c->wf_beta, &c->wf_dpw,
+                    &c->wf_L, &c->wf_sample, &c->wf_hit, &c->wf_hitv, &c->wf_nee, &c->wf_sho, &c->wf_shd, &c->wf_extq,
+                    &c->wf_shq, &c->wf_spo, &c->wf_spd, &c->wf_spb, &c->wf_spw, &c->wf_sps, &c->wf_samp, &c->wf_live,
+                    &c->wf_pix, &c->wf_ctl})
     b->release();
+  if (c->wf_graph) cudaGraphExecDestroy(c->wf_graph);
+  if (c->wf_host_ctl) cudaFreeHost(c->wf_host_ctl);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -167,6 +183,30 @@ int pr_scene_upload(pr_ctx* c, const pr_scene_desc* d) {
   }
   S.medium = h.medium;
   S.scene_scale = h.scene_scale;
+  for (int k = 0; k < 3; k++) {
+    S.bg[k] = (float)h.background[k];
+    S.env[k] = (float)h.env_light[k];
+  }
+  for (int i = 0; i < S.n_ents; i++) {
+    const GEntity& e = h.ents[i];
+    GEntF& f = S.entf[i];
+    f.type = e.type;
+    f.material = e.material;
+    f.normal_inverse = e.normal_inverse;
+    f.is_light = e.is_light;
+    for (int k = 0; k < 3; k++) {
+      f.p[k] = (float)e.p[k];
+      f.u[k] = (float)e.u_axis[k];
+      f.v[k] = (float)e.v_axis[k];
+      f.n[k] = (float)e.normal[k];
+    }
+    f.radius_eps = (float)(e.radius + 1.0e-6);
+    f.u_length = (float)e.u_length;
+    f.v_length = (float)e.v_length;
+    f.area = (float)e.area;
+    f.face_base = e.face_base;
+    f.node_base = e.node_base;
+  }
   c->scene_ready = true;
   return PR_OK;
 }
@@ -341,7 +381,9 @@ static int prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_param
   g.spp = samples * ss * ss;
   g.ss = ss;
   g.rate = (float)rate;
-  g.smp = (float)(1.0 / samples / (ss * ss));
+  if (p->total_spp < 0) return fail(c, PR_E_ARG, "total_spp must be >= 0");
+  // smp = 1 / samples / ss^2 (render.h:1139), over the whole frame when sharded
+  g.smp = p->total_spp > 0 ? (float)(1.0 / p->total_spp) : (float)(1.0 / samples / (ss * ss));
   g.tent = p->tent_filter ? 1 : 0;
   g.cutoff = (float)p->luminance_cutoff;
   g.sensor = (float)p->sensor_response;
@@ -363,31 +405,135 @@ static int prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_param
   return PR_OK;
 }
 
+// paths in flight (slots of the wavefront pool); PR_WF_SLOTS overrides
+static unsigned int wavefront_slots() {
+  const char* e = getenv("PR_WF_SLOTS");
+  long v = e ? strtol(e, nullptr, 10) : 0;
+  if (v < 1024 || v > (1L << 24)) v = 1L << 21;
+  return (unsigned int)v;
+}
+
+static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int accumulate) {
+  const unsigned int P = wavefront_slots();
+  const uint64_t wh = (uint64_t)g.width * g.height;
+  const uint64_t max_pass = 64ull << 20;  // camera samples per pass (sample table 28 B each)
+  uint64_t layers = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.spp, max_pass / wh));
+  const uint64_t pass_cap = layers * wh;
+  const size_t f4 = sizeof(float4);
+  PR_CUDA(c, c->wf_o.ensure(f4 * P));
+  PR_CUDA(c, c->wf_d.ensure(f4 * P));
+  PR_CUDA(c, c->wf_beta.ensure(f4 * P));
+  PR_CUDA(c, c->wf_dpw.ensure(f4 * P));
+  PR_CUDA(c, c->wf_L.ensure(f4 * P));
+  PR_CUDA(c, c->wf_sample.ensure(8ull * P));
+  PR_CUDA(c, c->wf_hit.ensure(f4 * P));
+  PR_CUDA(c, c->wf_hitv.ensure(4ull * P));
+  PR_CUDA(c, c->wf_nee.ensure(f4 * 3 * P));
+  PR_CUDA(c, c->wf_sho.ensure(f4 * 3 * P));
+  PR_CUDA(c, c->wf_shd.ensure(f4 * 3 * P));
+  PR_CUDA(c, c->wf_extq.ensure(4ull * P));
+  PR_CUDA(c, c->wf_shq.ensure(4ull * 3 * P));
+  const unsigned int spawn_cap = 2 * P;
+  PR_CUDA(c, c->wf_spo.ensure(f4 * spawn_cap));
+  PR_CUDA(c, c->wf_spd.ensure(f4 * spawn_cap));
+  PR_CUDA(c, c->wf_spb.ensure(f4 * spawn_cap));
+  PR_CUDA(c, c->wf_spw.ensure(f4 * spawn_cap));
+  PR_CUDA(c, c->wf_sps.ensure(8ull * spawn_cap));
+  PR_CUDA(c, c->wf_samp.ensure(24ull * pass_cap));
+  PR_CUDA(c, c->wf_live.ensure(4ull * pass_cap));
+  PR_CUDA(c, c->wf_pix.ensure(24ull * wh));
+  PR_CUDA(c, c->wf_ctl.ensure(sizeof(WfCtl)));
+  if (!c->wf_host_ctl) PR_CUDA(c, cudaMallocHost((void**)&c->wf_host_ctl, sizeof(WfCtl)));
+  WfBufs B{};
+  B.o = (float4*)c->wf_o.p;
+  B.d = (float4*)c->wf_d.p;
+  B.beta = (float4*)c->wf_beta.p;
+  B.dpw = (float4*)c->wf_dpw.p;
+  B.L = (float4*)c->wf_L.p;
+  B.sample = (uint64_t*)c->wf_sample.p;
+  B.hit = (float4*)c->wf_hit.p;
+  B.hitv = (float*)c->wf_hitv.p;
+  B.nee = (float4*)c->wf_nee.p;
+  B.sh_o = (float4*)c->wf_sho.p;
+  B.sh_d = (float4*)c->wf_shd.p;
+  B.extq = (int*)c->wf_extq.p;
+  B.shq = (int*)c->wf_shq.p;
+  B.sp_o = (float4*)c->wf_spo.p;
+  B.sp_d = (float4*)c->wf_spd.p;
+  B.sp_beta = (float4*)c->wf_spb.p;
+  B.sp_dpw = (float4*)c->wf_spw.p;
+  B.sp_sample = (uint64_t*)c->wf_sps.p;
+  B.samp = (long long*)c->wf_samp.p;
+  B.live = (int*)c->wf_live.p;
+  B.pix = (long long*)c->wf_pix.p;
+  B.ctl = (WfCtl*)c->wf_ctl.p;
+  B.err = (uint32_t*)c->errword.p;
+  B.counters = (unsigned long long*)c->counters.p;
+  B.n_slots = P;
+  B.spawn_cap = spawn_cap;
+  B.max_iterations = 100000u;
+  WfLaunch L;
+  L.shade_blocks = (P + 127) / 128;
+  L.trace_blocks = std::min<unsigned int>((P + 127) / 128, 152u * 64u);
+  PR_CUDA(c, cudaMemsetAsync(c->wf_nee.p, 0, f4 * 3 * P, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->wf_pix.p, 0, 24ull * wh, c->stream));
+  if (!c->wf_graph_failed && (!c->wf_graph || c->wf_graph_slots != P)) {
+    if (c->wf_graph) cudaGraphExecDestroy(c->wf_graph);
+    c->wf_graph = nullptr;
+    cudaError_t e = wf_build_graph(L, c->stream, &c->wf_graph);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      c->wf_graph = nullptr;
+      c->wf_graph_failed = true;  // fall back to the host-driven loop
+    } else {
+      c->wf_graph_slots = P;
+    }
+  }
+  for (uint64_t first = 0; first < (uint64_t)g.spp; first += layers) {
+    const uint64_t n_layers = std::min<uint64_t>(layers, (uint64_t)g.spp - first);
+    B.pass_first = first;
+    B.pass_samples = n_layers * wh;
+    PR_CUDA(c, cudaMemsetAsync(c->wf_samp.p, 0, 24ull * B.pass_samples, c->stream));
+    PR_CUDA(c, wf_set_constants(c->dev, g, B, c->stream));
+    PR_CUDA(c, wf_reset_launch(P, c->stream));
+    if (c->wf_graph) PR_CUDA(c, cudaGraphLaunch(c->wf_graph, c->stream));
+    else PR_CUDA(c, wf_run_host_loop(L, c->wf_host_ctl, (const WfCtl*)c->wf_ctl.p, c->stream));
+  }
+  PR_CUDA(c, wf_resolve_launch(rgb_dev, (int)(3 * wh), accumulate, g.sensor, c->stream));
+  return PR_OK;
+}
+
 int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, float* rgb_dev, uint64_t sample_offset,
                   int accumulate) {
   if (!c) return PR_E_ARG;
   if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
   if (!rgb_dev) return fail(c, PR_E_ARG, "null output");
-  if (p && p->mode != PR_MODE_MEGAKERNEL) return fail(c, PR_E_UNSUPPORTED, "only the megakernel mode is built");
+  if (p && p->mode != PR_MODE_MEGAKERNEL && p->mode != PR_MODE_WAVEFRONT) return fail(c, PR_E_ARG, "unknown render mode");
   RenderCfg g;
   int st = prepare_render(c, cam, p, sample_offset, g);
   if (st != PR_OK) return st;
   PR_CUDA(c, cudaSetDevice(c->device));
   const size_t n3 = (size_t)g.width * g.height * 3;
-  PR_CUDA(c, c->partial.ensure(sizeof(float) * n3 * (size_t)g.chunks));
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-  PR_CUDA(c, launch_megakernel(c->dev, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
-                               (unsigned long long*)c->counters.p, c->stream));
-  PR_CUDA(c, launch_reduce((const float*)c->partial.p, rgb_dev, (int)n3, g.chunks, accumulate, c->stream));
+  if (p->mode == PR_MODE_WAVEFRONT) {
+    st = render_wavefront(c, g, rgb_dev, accumulate);
+    if (st != PR_OK) return st;
+  } else {
+    PR_CUDA(c, c->partial.ensure(sizeof(float) * n3 * (size_t)g.chunks));
+    PR_CUDA(c, launch_megakernel(c->dev, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
+                                 (unsigned long long*)c->counters.p, c->stream));
+    PR_CUDA(c, launch_reduce((const float*)c->partial.p, rgb_dev, (int)n3, g.chunks, accumulate, c->stream));
+  }
   PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
-  unsigned long long cnt[4];
+  unsigned long long cnt[8];
   PR_CUDA(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
   st = check_device_errors(c);
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-  c->stats = pr_render_stats{cnt[0], cnt[1], cnt[2], cnt[3], ms};
+  const uint64_t paths = p->mode == PR_MODE_WAVEFRONT ? (uint64_t)g.spp * g.width * g.height : cnt[0];
+  c->stats = pr_render_stats{paths, cnt[1], cnt[2], cnt[3], ms};
   return st;
 }
 

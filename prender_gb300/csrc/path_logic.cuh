@@ -1,0 +1,470 @@
+// Per-vertex shading shared by the two render forms.
+//
+// The reference's recursive radiance() (radiance.h:25-556) becomes a state
+// machine over a PathState: shade() consumes one closest hit, adds the
+// vertex's terms to L, prepares up to three NEE shadow rays (their
+// contributions are final unless the ray is blocked) and either continues
+// the path, ends it, or -- for ideal glass at depth <= 2, where the
+// reference traces both reflection and refraction (brdf.h:899-936) --
+// continues with one branch and hands back the other.
+//
+// The megakernel traces the shadow rays and the next segment in place; the
+// wavefront queues them.  Both call this same function with the same
+// per-branch counter-based streams (branch ids form a binary tree: the
+// children of branch b are 2b+1 (refraction) and 2b+2 (reflection)), so
+// both forms follow identical paths and produce the same image up to float
+// summation order.
+#pragma once
+#include "device_common.cuh"
+#include "render_kernels.h"
+#include "trace_fast.cuh"
+
+namespace pr {
+
+struct PathState {
+  float3 o, d;
+  float3 beta;
+  float3 dpw;      // weight of the pending light-hit term (specular / glass NEE)
+  float3 L;        // radiance gathered by this branch
+  int depth;
+  uint32_t branch;
+  uint32_t draws;  // uniforms drawn so far from this branch's stream
+  int dp;          // 1: the next hit adds dpw * emission if it is a light
+};
+
+struct ShadowReq {
+  float3 o, d;
+  float tmax;
+  float3 contrib;  // added to L if nothing is hit before tmax
+};
+
+enum { SHADE_END = 0, SHADE_CONTINUE = 1, SHADE_SPLIT = 2 };
+
+constexpr uint32_t kCameraStream = 0x80000000u;
+
+// stream positioned at an arbitrary draw index (resumable between launches)
+__device__ __forceinline__ void rng_at(Rng& r, uint64_t seed, uint64_t sample, uint32_t branch, uint32_t draws) {
+  r.init(seed, sample, branch);
+  r.ctr.z = draws >> 2;
+  r.idx = 4;
+  if (draws & 3) {
+    r.buf = philox4x32_10(r.ctr, r.key);
+    r.ctr.z++;
+    r.idx = (int)(draws & 3);
+  }
+}
+__device__ __forceinline__ uint32_t rng_draws(const Rng& r) { return ((r.ctr.z - (r.idx == 4 ? 0u : 1u)) << 2) + (r.idx == 4 ? 0u : (uint32_t)r.idx); }
+
+__device__ __forceinline__ float3 medium_tr(const GMedium& m, float d) {
+  return f3(expf(-m.sigma_t[0] * d), expf(-m.sigma_t[1] * d), expf(-m.sigma_t[2] * d));
+}
+
+// OrthonormalBasis (vector3d.h:244-253)
+__device__ __forceinline__ void onb(float3 w, float3& u, float3& v) {
+  if (fabsf(w.x) > 1.0e-6f) u = normalize(cross(f3(0.0f, 1.0f, 0.0f), w));
+  else u = normalize(cross(f3(1.0f, 0.0f, 0.0f), w));
+  v = normalize(cross(w, u));
+}
+
+struct Vertex {
+  float3 p, n;  // hit point and geometric normal (after the entity's normal inversion)
+  int mat, ent;
+  float t;
+};
+
+__device__ __forceinline__ void make_vertex(const DevScene& S, float3 o, float3 d, const FastHit& h, Vertex& v) {
+  const GEntF& e = S.entf[h.ent];
+  v.ent = h.ent;
+  v.mat = e.material;
+  v.t = h.t;
+  if (e.type == PR_ENT_SPHERE) {
+    // position and normal in FP64 from the FP64 distance (sphere.h:89-95)
+    const GEntity& ed = S.ents[h.ent];
+    const double t = h.t;
+    const double px = (double)o.x + t * (double)d.x, py = (double)o.y + t * (double)d.y, pz = (double)o.z + t * (double)d.z;
+    const double nx = px - ed.p[0], ny = py - ed.p[1], nz = pz - ed.p[2];
+    const double il = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);
+    v.p = f3((float)px, (float)py, (float)pz);
+    v.n = f3((float)(nx * il), (float)(ny * il), (float)(nz * il));
+  } else if (e.type == PR_ENT_UVPLANE) {
+    v.p = o + d * h.t;
+    v.n = f3(e.n[0], e.n[1], e.n[2]);
+  } else {
+    // the hit point from the barycentrics: its error is a few ulps of the
+    // vertex coordinates, not of the ray length, which the ulp-scaled
+    // origin offset (offset_ray) relies on
+    const float4* T = S.tris + 3 * (size_t)h.slot;
+    const float4 A = __ldg(T), B = __ldg(T + 1), C = __ldg(T + 2);
+    const float w = 1.0f - h.u - h.v;
+    v.p = f3(w * A.x + h.u * B.x + h.v * C.x, w * A.y + h.u * B.y + h.v * C.y, w * A.z + h.u * B.z + h.v * C.z);
+    v.n = ld3(S.fnorm + 3 * (size_t)(e.face_base + __float_as_int(A.w)));
+  }
+  if (e.normal_inverse < 0) v.n = -v.n;
+}
+
+// a point on light entity le (direct_radiance_sample, directLight_radiance.h:326-377;
+// the media variant omits the uvplane's normal * PS_EPS lift, ParticipatingMedia.h:213-224)
+__device__ __forceinline__ float3 sample_light(const GEntF& le, Rng& rng, bool lift) {
+  if (le.type == PR_ENT_SPHERE) {
+    const float r1 = 6.28318530717958647692f * rng.next();
+    const float r2 = 1.0f - 2.0f * rng.next();
+    const float sq = sqrtf(fmaxf(0.0f, 1.0f - r2 * r2));
+    float sn, cs;
+    sincosf(r1, &sn, &cs);
+    return f3(le.p[0], le.p[1], le.p[2]) + f3(sq * cs, sq * sn, r2) * le.radius_eps;
+  }
+  const float t = le.v_length * rng.next();  // v first, then u (directLight_radiance.h:359-360)
+  const float s = le.u_length * rng.next();
+  float3 lp = f3(le.p[0], le.p[1], le.p[2]) + f3(le.u[0], le.u[1], le.u[2]) * s + f3(le.v[0], le.v[1], le.v[2]) * t;
+  if (lift) lp = lp + f3(le.n[0], le.n[1], le.n[2]) * 1.0e-6f;
+  return lp;
+}
+
+__device__ __forceinline__ float3 light_normal(const GEntF& le, float3 lp, bool use_inverse) {
+  float3 n;
+  if (le.type == PR_ENT_SPHERE) n = normalize(lp - f3(le.p[0], le.p[1], le.p[2]));
+  else n = f3(le.n[0], le.n[1], le.n[2]);
+  if (use_inverse && le.normal_inverse < 0) n = -n;
+  return n;
+}
+
+__device__ __forceinline__ const GEntF& pick_light(const DevScene& S, Rng& rng) {
+  int idx = (int)(rng.next() * (float)(S.n_lights - 1) + 0.5f);
+  idx = min(max(idx, 0), S.n_lights - 1);
+  return S.entf[S.light_ent[idx]];
+}
+
+// sampleHG (sampler.h:24-93); the reference's cos expression is (g/2)(...)
+__device__ __forceinline__ float3 sample_hg(float3 raydir, float g, Rng& rng, bool correct) {
+  float3 u, v;
+  onb(raydir, u, v);
+  const float r1 = 6.28318530717958647692f * rng.next();
+  const float r2 = rng.next();
+  const float s = (1.0f - g * g) / (1.0f - g + 2.0f * g * r2);
+  const float cost = correct ? (1.0f + g * g - s * s) / (2.0f * g) : 0.5f * g * (1.0f + g * g - s * s);
+  const float sint = sqrtf(fmaxf(0.0f, 1.0f - cost * cost));
+  float sn, cs;
+  sincosf(r1, &sn, &cs);
+  return normalize(u * (sint * cs) + v * (sint * sn) + raydir * cost);
+}
+
+__device__ __forceinline__ float3 sample_sphere_dir(Rng& rng) {
+  const float r1 = 6.28318530717958647692f * rng.next();
+  const float r2 = 1.0f - 2.0f * rng.next();
+  const float sq = sqrtf(fmaxf(0.0f, 1.0f - r2 * r2));
+  float sn, cs;
+  sincosf(r1, &sn, &cs);
+  return normalize(f3(sq * cs, sq * sn, r2));
+}
+
+__device__ __forceinline__ float phase_hg(float g, float c) {
+  const float w = 1.0f + g * g - 2.0f * g * c;
+  if (fabsf(w) < 1.0e-12f) return 0.0f;
+  return 0.0795774715459476679f * (1.0f - g * g) / (w * sqrtf(w));
+}
+
+// camera ray of per-pixel sample kg (render.h:1203-1269); returns the sample id
+__device__ __forceinline__ uint64_t camera_ray(const RenderCfg& cfg, int x, int y, uint64_t kg, float3& o, float3& d) {
+  const int ssq = cfg.ss * cfg.ss;
+  const int sub = (int)(kg % (uint64_t)ssq);
+  const int sxx = sub % cfg.ss, syy = sub / cfg.ss;
+  const uint64_t sample_id = kg * (uint64_t)cfg.width * (uint64_t)cfg.height + (uint64_t)y * cfg.width + x;
+  Rng cam;
+  cam.init(cfg.seed, sample_id, kCameraStream);
+  float dx = 0.0f, dy = 0.0f;
+  if (cfg.tent) {
+    const float rr1 = 2.0f * cam.next(), rr2 = 2.0f * cam.next();
+    dx = rr1 < 1.0f ? sqrtf(rr1) - 1.0f : 1.0f - sqrtf(2.0f - rr1);
+    dy = rr2 < 1.0f ? sqrtf(rr2) - 1.0f : 1.0f - sqrtf(2.0f - rr2);
+  }
+  const float r1 = (sxx + 0.5f + dx) * cfg.rate, r2 = (syy + 0.5f + dy) * cfg.rate;
+  const float3 sp = cfg.center + cfg.screen_x * ((r1 + x) * cfg.iw - 0.5f) + cfg.screen_y * ((r2 + y) * cfg.ih - 0.5f);
+  o = cfg.cam_pos;
+  d = normalize(sp - cfg.cam_pos);
+  return sample_id;
+}
+
+__device__ __forceinline__ void root_path(PathState& ps, float3 o, float3 d) {
+  ps.o = o;
+  ps.d = d;
+  ps.beta = f3(1, 1, 1);
+  ps.dpw = f3(0, 0, 0);
+  ps.L = f3(0, 0, 0);
+  ps.depth = 0;
+  ps.branch = 0;
+  ps.draws = 0;
+  ps.dp = 0;
+}
+
+// Shades the vertex found by the last closest-hit query of ps.
+__device__ int shade(const DevScene& S, const RenderCfg& cfg, PathState& ps, bool hit, const FastHit& h,
+                     uint64_t sample_id, ShadowReq* sh, int& nsh, PathState& child, uint32_t* err) {
+  nsh = 0;
+  const bool nee = cfg.nee != 0;
+  const bool media = cfg.media != 0 && S.medium.on != 0;
+  if (ps.dp) {  // light hit along a specular / refraction direction (directLight_radiance.h:516-556)
+    if (hit && S.entf[h.ent].is_light) {
+      float3 em = ld3(S.mats[S.entf[h.ent].material].emission);
+      if (media) em = em * medium_tr(S.medium, h.t);
+      ps.L += ps.dpw * em;
+    }
+    ps.dp = 0;
+  }
+  if (!hit) {
+    ps.L += ps.beta * f3(S.bg[0], S.bg[1], S.bg[2]);
+    return SHADE_END;
+  }
+  if (ps.depth >= cfg.max_vertices) {
+    atomicOr(err, PR_DEV_LOOP_CAP);
+    return SHADE_END;
+  }
+  Rng rng;
+  rng_at(rng, cfg.seed, sample_id, ps.branch, ps.draws);
+  Vertex v;
+  make_vertex(S, ps.o, ps.d, h, v);
+  const GMaterial& m = S.mats[v.mat];
+  const GEntF& ent = S.entf[v.ent];
+  const float3 E = ld3(m.emission), C = ld3(m.color);
+  const float3 d = ps.d;
+  const float3 on = dot(v.n, d) < 0.0f ? v.n : -v.n;
+  float p_rr = maxc(E + C);  // WARD / PHONG are not on this path
+  if (ps.depth > cfg.depth_limit) p_rr *= exp2f((float)(cfg.depth_limit - ps.depth));
+  const float3 trr = media ? medium_tr(S.medium, v.t) : f3(1, 1, 1);
+  int result = SHADE_CONTINUE;
+  if (ps.depth > cfg.depth) {
+    if (rng.next() >= p_rr) {
+      ps.L += ps.beta * trr * E;
+      ps.draws = rng_draws(rng);
+      return SHADE_END;
+    }
+  } else {
+    p_rr = 1.0f;
+  }
+  const bool entering = dot(on, v.n) > 0.0f;  // Entity::isInsideDir (entity.h:98-114)
+  float p_scat = 0.0f;
+  if (media && entering) {
+    p_scat = fminf(fmaxf(1.0f - expf(-S.medium.sigma_s_mean * v.t), 0.01f), 0.99f);
+    if (rng.next() < p_scat) {
+      // ---- scattering in the medium before the surface (ParticipatingMedia.h:300-461)
+      const GMedium& md = S.medium;
+      const int sel = min(2, (int)(3.0f * rng.next()));
+      const float u = rng.next();
+      const float et = expf(-md.sigma_t_mean * v.t);
+      const float ds = -logf(1.0f + u * (et - 1.0f)) / md.sigma_t_mean;
+      const float pdf = expf(-md.sigma_t_mean * ds) * (-md.sigma_t_mean / (et - 1.0f));
+      const float g = md.g[sel];
+      float3 nd;
+      float phase;
+      if (g == 0.0f || fabsf(g) > 1.0f) {
+        nd = sample_sphere_dir(rng);
+        phase = 0.0795774715459476679f;
+      } else {
+        nd = sample_hg(d, g, rng, (cfg.flags & PR_FLAG_HG_CORRECT) != 0);
+        phase = phase_hg(g, dot(nd, d));
+      }
+      const float3 npos = ps.o + d * ds;
+      const float3 tr = medium_tr(md, ds);
+      // phase / dirPdf == 1 in the reference's weight
+      const float3 f = tr * f3(md.sigma_s[0], md.sigma_s[1], md.sigma_s[2]) * (phase / pdf / phase / p_scat / p_rr);
+      if (!ent.is_light && S.n_lights > 0) {
+        // NEE from the medium point (eval_direct_radiance_media, ParticipatingMedia.h:27-268)
+        for (int i = 0; i < 3; i++) {
+          const GEntF& le = pick_light(S, rng);
+          const float3 lp = sample_light(le, rng, false);
+          const float3 ln = light_normal(le, lp, false);
+          const float3 dl = lp - npos;
+          const float dist2 = dot(dl, dl);
+          const float dist = sqrtf(dist2);
+          const float3 ldir = dl / dist;
+          const float dot1 = -dot(ln, ldir);
+          if (dot1 >= 0.0f) {
+            const float G = dot1 / dist2;
+            const float3 em = ld3(S.mats[le.material].emission);
+            sh[nsh].o = npos;
+            sh[nsh].d = ldir;
+            sh[nsh].tmax = dist - 1.0e-3f;
+            sh[nsh].contrib = ps.beta * f * em * medium_tr(md, dist) * (0.31830988618379067154f * G * le.area * (1.0f / 3.0f));
+            nsh++;
+          }
+        }
+      }
+      ps.draws = rng_draws(rng);
+      if (!(pdf > 0.0f)) { nsh = 0; return SHADE_END; }
+      if (ent.is_light) {
+        if (ps.depth == 0) ps.L += ps.beta * tr * E;
+        return SHADE_END;
+      }
+      ps.beta = ps.beta * f;
+      ps.o = npos;
+      ps.d = nd;
+      ps.depth++;
+      return SHADE_CONTINUE;
+    }
+  }
+  const float inv_rr = 1.0f / p_rr / (1.0f - p_scat);
+  int kind;  // 0 diffuse, 1 specular, 2 glass
+  if (m.type == PR_MAT_DIFFUSE) kind = (rng.next() < m.roughness) ? 0 : 1;
+  else if (m.type == PR_MAT_SPECULAR) kind = (rng.next() < 1.0f - m.roughness) ? 1 : 0;
+  else kind = 2;
+  const float3 tri = (media && entering) ? trr : f3(1, 1, 1);
+  const float3 env = f3(S.env[0], S.env[1], S.env[2]);
+  if (kind == 0) {
+    // ---- BRDF_Diffuse (brdf.h:408-700)
+    if (ent.is_light) {
+      if (!(ent.type == PR_ENT_UVPLANE && dot(v.n, d) >= 0.0f) && (!nee || ps.depth == 0))
+        ps.L += ps.beta * trr * E * inv_rr;
+      ps.draws = rng_draws(rng);
+      return SHADE_END;
+    }
+    float3 u, w2;
+    onb(on, u, w2);
+    const float r1 = 6.28318530717958647692f * rng.next();
+    const float r2 = rng.next();
+    const float r2s = sqrtf(r2);
+    float sn, cs;
+    sincosf(r1, &sn, &cs);
+    const float3 nd = normalize(u * (cs * r2s) + w2 * (sn * r2s) + on * sqrtf(1.0f - r2));
+    const float3 origin = offset_ray(v.p, on);
+    if (S.n_lights > 0) {
+      if (nee) {
+        // eval_direct_radiance (directLight_radiance.h:19-313), 3 samples averaged
+        const float3 w = ps.beta * tri * C * (inv_rr * 0.31830988618379067154f * (1.0f / 3.0f));
+        for (int i = 0; i < 3; i++) {
+          const GEntF& le = pick_light(S, rng);
+          const float3 lp = sample_light(le, rng, true);
+          const float3 ln = light_normal(le, lp, true);
+          const float3 dl = lp - v.p;
+          const float dist2 = dot(dl, dl);
+          const float dist = sqrtf(dist2);
+          const float3 ldir = dl / dist;
+          const float dot0 = dot(on, ldir), dot1 = -dot(ln, ldir);
+          if (dot0 >= 0.0f && dot1 >= 0.0f) {
+            // visible iff nothing is hit closer than the light point - 1e-3
+            // (directLight_radiance.h:136-171), measured from the shadow
+            // ray's own offset origin
+            const float3 dlo = lp - origin;
+            const float disto = sqrtf(dot(dlo, dlo));
+            float3 em = ld3(S.mats[le.material].emission);
+            if (media) em = em * medium_tr(S.medium, dist);
+            sh[nsh].o = origin;
+            sh[nsh].d = dlo / disto;
+            sh[nsh].tmax = disto - 1.0e-3f;
+            sh[nsh].contrib = w * em * (dot0 * dot1 / dist2 * le.area);
+            nsh++;
+          }
+        }
+      } else {
+        for (int i = 0; i < 3; i++) (void)rng.next();  // light picks; only parallel/spot/infinity lights would add
+      }
+    }
+    ps.L += ps.beta * (env + tri * E);
+    ps.beta = ps.beta * C * tri * inv_rr;
+    ps.o = origin;
+    ps.d = nd;
+    ps.depth++;
+    ps.draws = rng_draws(rng);
+    return SHADE_CONTINUE;
+  }
+  if (kind == 1) {
+    // ---- BRDF_Specular (brdf.h:702-761): mirror about the geometric normal
+    const float3 nd = normalize(d - v.n * (2.0f * dot(v.n, d)));
+    ps.L += ps.beta * (env + tri * E);
+    ps.beta = ps.beta * C * tri * inv_rr;
+    ps.dp = nee;
+    ps.dpw = ps.beta;
+    ps.o = offset_ray(v.p, dot(nd, v.n) > 0.0f ? v.n : -v.n);
+    ps.d = nd;
+    ps.depth++;
+    ps.draws = rng_draws(rng);
+    return SHADE_CONTINUE;
+  }
+  // ---- BRDF_Refraction (brdf.h:763-953)
+  const float3 refl = normalize(d - v.n * (2.0f * dot(v.n, d)));
+  const bool into = dot(v.n, on) > 0.0f;
+  const float nt = m.ior;
+  const float nnt = into ? 1.0f / nt : nt;
+  const float ddn = dot(d, on);
+  const float cos2t = 1.0f - nnt * nnt * (1.0f - ddn * ddn);
+  ps.L += ps.beta * (env + tri * E);
+  const float3 base = ps.beta * C * tri;
+  const float3 refl_o = offset_ray(v.p, dot(refl, v.n) > 0.0f ? v.n : -v.n);
+  if (cos2t < 0.0f) {  // total internal reflection
+    ps.beta = base * inv_rr;
+    ps.dp = nee;
+    ps.dpw = ps.beta;
+    ps.o = refl_o;
+    ps.d = refl;
+    ps.depth++;
+    ps.draws = rng_draws(rng);
+    return SHADE_CONTINUE;
+  }
+  const float3 tdir = normalize(d * nnt - v.n * ((into ? 1.0f : -1.0f) * (ddn * nnt + sqrtf(fabsf(cos2t)))));
+  const float a = nt - 1.0f, bb = nt + 1.0f;
+  const float R0 = (a * a) / (bb * bb);
+  const float c = 1.0f - (into ? -ddn : dot(tdir, -on));
+  const float c2 = c * c;
+  float Re = R0 + (1.0f - R0) * (c2 * c2 * c);
+  float Tr = (1.0f - Re) * (nnt * nnt);
+  float P = 0.25f + 0.5f * Re;
+  if (m.type == PR_MAT_REFRACTION_FRESNEL) {
+    if (into) { P = 1.0f; Re = 1.0f; Tr = 0.0f; }
+    else { P = 0.0f; Re = 0.0f; Tr = 1.0f; }
+  }
+  const float3 tdir_o = offset_ray(v.p, dot(tdir, v.n) > 0.0f ? v.n : -v.n);
+  if (ps.depth > 2) {
+    if (rng.next() < P) {
+      const float3 W = base * (1.0f / (P * p_rr) / (1.0f - p_scat));
+      ps.beta = W * Re;
+      ps.dpw = W;
+      ps.o = refl_o;
+      ps.d = refl;
+    } else {
+      const float3 W = base * (1.0f / ((1.0f - P) * p_rr) / (1.0f - p_scat));
+      ps.beta = W * Tr;
+      ps.dpw = W;
+      ps.o = tdir_o;
+      ps.d = tdir;
+    }
+    ps.dp = nee;
+    ps.depth++;
+    ps.draws = rng_draws(rng);
+    return SHADE_CONTINUE;
+  }
+  // depth <= 2: both branches; the refracted one is handed back
+  const float3 W = base * inv_rr;
+  child.o = tdir_o;
+  child.d = tdir;
+  child.beta = W * Tr;
+  child.dpw = W;
+  child.L = f3(0, 0, 0);
+  child.depth = ps.depth + 1;
+  child.branch = 2 * ps.branch + 1;
+  child.draws = 0;
+  child.dp = nee;
+  ps.beta = W * Re;
+  ps.dp = nee;
+  ps.dpw = W;
+  ps.o = refl_o;
+  ps.d = refl;
+  ps.depth++;
+  ps.branch = 2 * ps.branch + 2;
+  ps.draws = 0;
+  result = SHADE_SPLIT;
+  return result;
+}
+
+// per-sample value after the weight 1/spp and the luminance clamp (render.h:1353, :1375-1384)
+__device__ __forceinline__ float3 finish_sample(const RenderCfg& cfg, float3 L, uint32_t* err) {
+  float3 v = L * cfg.smp;
+  if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z))) {
+    atomicOr(err, PR_DEV_NONFINITE);
+    v = f3(0, 0, 0);
+  }
+  if (cfg.cutoff > 0.0f) {
+    const float lum = 0.2126f * v.x + 0.7152f * v.y + 0.0722f * v.z;
+    if (lum > cfg.cutoff) v = v * (cfg.cutoff / lum);
+  }
+  return v;
+}
+
+}  // namespace pr

@@ -19,7 +19,7 @@
 
 namespace pr {
 
-constexpr int kMaxEntities = 64;
+constexpr int kMaxEntities = 48;
 constexpr int kMaxLights = 16;
 constexpr int kStackSize = 64;          // QBVH traversal stack (entries)
 constexpr int kSplitStack = 4;          // pending glass branches (depth <= 2 splits)
@@ -71,6 +71,21 @@ struct GEntity {
   float bmin[3], bmax[3];  // bounds (for scene extents)
 };
 
+// FP32 copy of an entity for the render path (no FP64 conversions in the
+// inner loops); lives inside DevScene, i.e. in the kernel parameter space.
+struct GEntF {
+  int32_t type, material, normal_inverse, is_light;
+  float p[3];
+  float radius_eps;  // sphere radius + PS_EPS (light sampling, directLight_radiance.h:346)
+  float u[3];
+  float u_length;
+  float v[3];
+  float v_length;
+  float n[3];
+  float area;
+  int32_t face_base, node_base, pad0, pad1;
+};
+
 struct GMedium {
   float sigma_s_mean;      // ParticipatingMedia::scattering
   float sigma_t_mean;      // ParticipatingMedia::transmittance
@@ -92,8 +107,11 @@ struct DevScene {
   int32_t light_ent[kMaxLights];
   double background[3];
   double env_light[3];
+  float bg[3];
+  float env[3];
   GMedium medium;
-  float scene_scale;       // max |coordinate| of the scene bounds (ray offsets)
+  float scene_scale;       // max |coordinate| of the scene bounds
+  GEntF entf[kMaxEntities];
 };
 
 }  // namespace pr

@@ -71,7 +71,7 @@ __device__ __forceinline__ int box4(const GNode* __restrict__ node, float3 inv, 
 
 // QBVH closest hit (ANY = false) or any hit below tmax (ANY = true).
 template <bool ANY>
-__device__ __forceinline__ bool fast_qbvh(const DevScene& S, const GEntity& e, float3 o, float3 d, float3 inv, float& tbest,
+__device__ __forceinline__ bool fast_qbvh(const DevScene& S, const GEntF& e, float3 o, float3 d, float3 inv, float& tbest,
                                           int& slot, float& bu, float& bv, TraceStats& st, uint32_t* err) {
   int32_t stack[kStackSize];
   int sp = 0;
@@ -148,18 +148,18 @@ __device__ __forceinline__ bool fast_sphere(const GEntity& e, float3 o, float3 d
 
 // UVPlane::intersect semantics in FP32 (plane.h:86-110, :220-239): the
 // extent check compares u / |U| against |U| (the reference's own rule).
-__device__ __forceinline__ bool fast_uvplane(const GEntity& e, float3 o, float3 d, float tmax, float& t) {
+__device__ __forceinline__ bool fast_uvplane(const GEntF& e, float3 o, float3 d, float tmax, float& t) {
   const float s = e.normal_inverse < 0 ? -1.0f : 1.0f;
-  const float3 n = f3((float)e.normal[0] * s, (float)e.normal[1] * s, (float)e.normal[2] * s);
+  const float3 n = f3(e.n[0] * s, e.n[1] * s, e.n[2] * s);
   const float dd = dot(d, n);
   if (fabsf(dd) < 1.0e-14f) return false;
-  const float3 org = f3((float)e.p[0], (float)e.p[1], (float)e.p[2]);
+  const float3 org = f3(e.p[0], e.p[1], e.p[2]);
   const float tt = dot(org - o, n) / dd;
   if (!(tt > 0.0f) || !(tt < tmax)) return false;
   const float3 rel = (o + d * tt) - org;
-  const float ul = (float)e.u_length, vl = (float)e.v_length;
-  const float u = dot(rel, f3((float)e.u_axis[0], (float)e.u_axis[1], (float)e.u_axis[2])) / ul;
-  const float v = dot(rel, f3((float)e.v_axis[0], (float)e.v_axis[1], (float)e.v_axis[2])) / vl;
+  const float ul = e.u_length, vl = e.v_length;
+  const float u = dot(rel, f3(e.u[0], e.u[1], e.u[2])) / ul;
+  const float v = dot(rel, f3(e.v[0], e.v[1], e.v[2])) / vl;
   if (u < 0.0f || u > ul || v < 0.0f || v > vl) return false;
   t = tt;
   return true;
@@ -180,11 +180,11 @@ __device__ __forceinline__ bool fast_closest(const DevScene& S, float3 o, float3
   h.u = h.v = 0.0f;
   const float3 inv = safe_inv(d);
   for (int i = 0; i < S.n_ents; i++) {
-    const GEntity& e = S.ents[i];
+    const GEntF& e = S.entf[i];
     float t = h.t, bu = 0.0f, bv = 0.0f;
     int slot = -1;
     bool got = false;
-    if (e.type == PR_ENT_SPHERE) got = fast_sphere(e, o, d, h.t, t);
+    if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], o, d, h.t, t);
     else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, o, d, h.t, t);
     else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<false>(S, e, o, d, inv, t, slot, bu, bv, st, err);
     if (got && t < h.t) {
@@ -203,11 +203,11 @@ __device__ __forceinline__ bool fast_occluded(const DevScene& S, float3 o, float
                                               uint32_t* err) {
   const float3 inv = safe_inv(d);
   for (int i = 0; i < S.n_ents; i++) {
-    const GEntity& e = S.ents[i];
+    const GEntF& e = S.entf[i];
     float t = tmax, bu, bv;
     int slot;
     bool got = false;
-    if (e.type == PR_ENT_SPHERE) got = fast_sphere(e, o, d, tmax, t);
+    if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], o, d, tmax, t);
     else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, o, d, tmax, t);
     else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<true>(S, e, o, d, inv, t, slot, bu, bv, st, err);
     if (got) return true;

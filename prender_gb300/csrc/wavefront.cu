@@ -1,0 +1,410 @@
+// Wavefront renderer: the same estimator as the megakernel (path_logic.cuh),
+// scheduled as a loop of small kernels over a pool of P path slots held in
+// HBM as structure-of-arrays:
+//
+//   wf_shade    one thread per slot: shade the last hit of a live path
+//               (queue its shadow rays and its next segment, or end it), or
+//               refill a free slot -- first with a glass branch waiting in
+//               the spawn ring, else with the next camera sample
+//   wf_extend   closest hit for every queued segment (compacted queue)
+//   wf_shadow   any hit for every queued shadow ray (compacted queue)
+//   wf_control  one thread: swap the per-iteration counters and decide
+//               whether another iteration is needed
+//
+// The loop runs on the device: the four kernels are the body of a CUDA-graph
+// 'while' node whose condition wf_control sets, so a whole frame is one
+// graph launch with no host round trips.  Paths of very uneven length
+// (glass, media, roulette) no longer hold a warp hostage: every launch works
+// on compacted queues of identical work.
+//
+// Accumulation is in 64-bit fixed point: a path adds its radiance to its
+// camera sample's slot (only samples whose glass split into branches need
+// the slot), the last branch to finish applies the per-sample weight and
+// luminance clamp (render.h:1353-1384) and adds the sample to its pixel.
+// Integer sums are associative, so the image does not depend on the order
+// in which paths finish.
+#include <cuda_runtime.h>
+
+#include "path_logic.cuh"
+#include "wavefront.h"
+
+namespace pr {
+
+__constant__ DevScene c_scene;
+__constant__ RenderCfg c_cfg;
+__constant__ WfBufs c_buf;
+
+constexpr float kSampleScale = 4294967296.0f;        // 2^32
+constexpr double kSampleInv = 1.0 / 4294967296.0;
+constexpr double kPixelScale = 1099511627776.0;      // 2^40
+constexpr double kPixelInv = 1.0 / 1099511627776.0;
+
+enum : int { SLOT_FREE = 0, SLOT_RAY = 1, SLOT_HIT = 2 };
+
+__device__ __forceinline__ void store_state(const WfBufs& B, int i, const PathState& ps, int slot_state) {
+  B.o[i] = make_float4(ps.o.x, ps.o.y, ps.o.z, __int_as_float(ps.depth));
+  B.d[i] = make_float4(ps.d.x, ps.d.y, ps.d.z, __int_as_float(ps.dp | (slot_state << 1)));
+  B.beta[i] = make_float4(ps.beta.x, ps.beta.y, ps.beta.z, __uint_as_float(ps.branch));
+  B.dpw[i] = make_float4(ps.dpw.x, ps.dpw.y, ps.dpw.z, __uint_as_float(ps.draws));
+  B.L[i] = make_float4(ps.L.x, ps.L.y, ps.L.z, 0.0f);
+}
+
+__device__ __forceinline__ void load_state(const WfBufs& B, int i, PathState& ps) {
+  const float4 o = B.o[i], d = B.d[i], b = B.beta[i], w = B.dpw[i], l = B.L[i];
+  ps.o = f3(o.x, o.y, o.z);
+  ps.depth = __float_as_int(o.w);
+  ps.d = f3(d.x, d.y, d.z);
+  ps.dp = __float_as_int(d.w) & 1;
+  ps.beta = f3(b.x, b.y, b.z);
+  ps.branch = __float_as_uint(b.w);
+  ps.dpw = f3(w.x, w.y, w.z);
+  ps.draws = __float_as_uint(w.w);
+  ps.L = f3(l.x, l.y, l.z);
+}
+
+// warp-aggregated append to a counter; returns this lane's slot
+__device__ __forceinline__ unsigned int append(unsigned int* counter, bool want) {
+  const unsigned int mask = __ballot_sync(__activemask(), want);
+  if (!want) return 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(mask) - 1;
+  unsigned int base = 0;
+  if (lane == leader) base = atomicAdd(counter, (unsigned int)__popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  return base + (unsigned int)__popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void pixel_of(const RenderCfg& cfg, uint64_t g, int& x, int& y, uint64_t& kg) {
+  const uint64_t wh = (uint64_t)cfg.width * cfg.height;
+  const uint64_t k = g / wh;
+  const uint32_t pix = (uint32_t)(g - k * wh);
+  x = (int)(pix % (uint32_t)cfg.width);
+  y = (int)(pix / (uint32_t)cfg.width);
+  kg = cfg.sample_offset + c_buf.pass_first + k;
+}
+
+__device__ void add_to_pixel(const WfBufs& B, const RenderCfg& cfg, uint64_t g, float3 L) {
+  int x, y;
+  uint64_t kg;
+  pixel_of(cfg, g, x, y, kg);
+  const float3 v = finish_sample(cfg, L, B.err);
+  long long* px = B.pix + 3 * ((size_t)(cfg.height - y - 1) * cfg.width + x);
+  atomicAdd(reinterpret_cast<unsigned long long*>(px + 0), (unsigned long long)llrint((double)v.x * kPixelScale));
+  atomicAdd(reinterpret_cast<unsigned long long*>(px + 1), (unsigned long long)llrint((double)v.y * kPixelScale));
+  atomicAdd(reinterpret_cast<unsigned long long*>(px + 2), (unsigned long long)llrint((double)v.z * kPixelScale));
+}
+
+// a branch is done: a sample that never split finishes at once; otherwise
+// the branch adds to the sample slot and the last one finishes the sample
+__device__ void end_path(const WfBufs& B, const RenderCfg& cfg, const PathState& ps, uint64_t g) {
+  if (ps.branch == 0) {
+    add_to_pixel(B, cfg, g, ps.L);
+    return;
+  }
+  long long* s = B.samp + 3 * g;
+  atomicAdd(reinterpret_cast<unsigned long long*>(s + 0), (unsigned long long)__float2ll_rn(ps.L.x * kSampleScale));
+  atomicAdd(reinterpret_cast<unsigned long long*>(s + 1), (unsigned long long)__float2ll_rn(ps.L.y * kSampleScale));
+  atomicAdd(reinterpret_cast<unsigned long long*>(s + 2), (unsigned long long)__float2ll_rn(ps.L.z * kSampleScale));
+  __threadfence();
+  if (atomicSub(B.live + g, 1) == 1) {
+    __threadfence();
+    const volatile long long* vs = s;
+    const float3 L = f3((float)((double)vs[0] * kSampleInv), (float)((double)vs[1] * kSampleInv),
+                        (float)((double)vs[2] * kSampleInv));
+    add_to_pixel(B, cfg, g, L);
+  }
+}
+
+__global__ void __launch_bounds__(256) wf_reset(unsigned int n_slots) {
+  const WfBufs& B = c_buf;
+  const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_slots) B.d[i] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(SLOT_FREE << 1));
+  if (i == 0) {
+    WfCtl* c = B.ctl;
+    c->ext_count = 0;
+    c->sh_count = 0;
+    c->spawn_head = 0;
+    c->spawn_tail = 0;
+    c->spawn_ready = 0;
+    c->next_sample = 0;
+    c->iterations = 0;
+    c->work = 1;
+  }
+}
+
+__global__ void __launch_bounds__(128) wf_shade() {
+  const DevScene& S = c_scene;
+  const RenderCfg& cfg = c_cfg;
+  const WfBufs& B = c_buf;
+  WfCtl* ctl = B.ctl;
+  const unsigned int stride = gridDim.x * blockDim.x;
+  const unsigned int ready = ctl->spawn_ready;  // spawns written in earlier iterations
+  for (unsigned int base = blockIdx.x * blockDim.x; base < B.n_slots; base += stride) {
+    const unsigned int i = base + threadIdx.x;
+    int state = SLOT_FREE;
+    PathState ps;
+    uint64_t g = 0;
+    bool has_ray = false;
+    if (i < B.n_slots) {
+      state = __float_as_int(B.d[i].w) >> 1;
+      if (state == SLOT_HIT) {
+        load_state(B, i, ps);
+        g = B.sample[i];
+        // shadow rays of the previous vertex that were not blocked
+        for (int k = 0; k < 3; k++) {
+          const float4 c = B.nee[3 * i + k];
+          ps.L += f3(c.x, c.y, c.z);
+        }
+        const float4 h4 = B.hit[i];
+        FastHit h;
+        h.t = h4.x;
+        h.ent = __float_as_int(h4.y);
+        h.slot = __float_as_int(h4.z);
+        h.u = h4.w;
+        h.v = B.hitv[i];
+        int kg_x, kg_y;
+        uint64_t kg;
+        pixel_of(cfg, g, kg_x, kg_y, kg);
+        const uint64_t sample_id = kg * (uint64_t)cfg.width * (uint64_t)cfg.height + (uint64_t)kg_y * cfg.width + kg_x;
+        ShadowReq sh[3];
+        int nsh = 0;
+        PathState child;
+        const int r = shade(S, cfg, ps, h.ent >= 0, h, sample_id, sh, nsh, child, B.err);
+        for (int k = 0; k < 3; k++) {
+          if (k < nsh) {
+            B.nee[3 * i + k] = make_float4(sh[k].contrib.x, sh[k].contrib.y, sh[k].contrib.z, 0.0f);
+            B.sh_o[3 * i + k] = make_float4(sh[k].o.x, sh[k].o.y, sh[k].o.z, sh[k].tmax);
+            B.sh_d[3 * i + k] = make_float4(sh[k].d.x, sh[k].d.y, sh[k].d.z, 0.0f);
+          } else {
+            B.nee[3 * i + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          }
+        }
+        if (r == SHADE_SPLIT) {
+          atomicAdd(B.live + g, 1);
+          const unsigned int t = atomicAdd(&ctl->spawn_tail, 1u);
+          if (t - ctl->spawn_head >= B.spawn_cap) {
+            atomicOr(B.err, PR_DEV_QUEUE_OVERFLOW);
+          } else {
+            const unsigned int q = t % B.spawn_cap;
+            B.sp_o[q] = make_float4(child.o.x, child.o.y, child.o.z, __int_as_float(child.depth));
+            B.sp_d[q] = make_float4(child.d.x, child.d.y, child.d.z, __int_as_float(child.dp));
+            B.sp_beta[q] = make_float4(child.beta.x, child.beta.y, child.beta.z, __uint_as_float(child.branch));
+            B.sp_dpw[q] = make_float4(child.dpw.x, child.dpw.y, child.dpw.z, __uint_as_float(child.draws));
+            B.sp_sample[q] = g;
+          }
+        }
+        if (r == SHADE_END) {
+          end_path(B, cfg, ps, g);
+          state = SLOT_FREE;
+        } else {
+          has_ray = true;
+        }
+        // shadow rays go to the shadow queue
+        for (int k = 0; k < 3; k++) {
+          const unsigned int q = append(&ctl->sh_count, k < nsh);
+          if (k < nsh) B.shq[q] = 3 * i + k;
+        }
+      }
+      if (state == SLOT_FREE) {
+        // refill: a waiting glass branch first, else the next camera sample
+        const unsigned int t = atomicAdd(&ctl->spawn_head, 1u);
+        if (t < ready) {
+          const unsigned int q = t % B.spawn_cap;
+          const float4 o = B.sp_o[q], d = B.sp_d[q], b = B.sp_beta[q], w = B.sp_dpw[q];
+          ps.o = f3(o.x, o.y, o.z);
+          ps.depth = __float_as_int(o.w);
+          ps.d = f3(d.x, d.y, d.z);
+          ps.dp = __float_as_int(d.w);
+          ps.beta = f3(b.x, b.y, b.z);
+          ps.branch = __float_as_uint(b.w);
+          ps.dpw = f3(w.x, w.y, w.z);
+          ps.draws = __float_as_uint(w.w);
+          ps.L = f3(0, 0, 0);
+          g = B.sp_sample[q];
+          has_ray = true;
+        } else {
+          const unsigned long long s = atomicAdd(&ctl->next_sample, 1ull);
+          if (s < B.pass_samples) {
+            g = s;
+            int x, y;
+            uint64_t kg;
+            pixel_of(cfg, g, x, y, kg);
+            float3 o, d;
+            camera_ray(cfg, x, y, kg, o, d);
+            root_path(ps, o, d);
+            B.live[g] = 1;
+            has_ray = true;
+          }
+        }
+      }
+      if (has_ray) {
+        store_state(B, i, ps, SLOT_RAY);
+        B.sample[i] = g;
+      } else if (state == SLOT_FREE) {
+        B.d[i] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(SLOT_FREE << 1));
+      }
+    }
+    const unsigned int q = append(&ctl->ext_count, has_ray);
+    if (has_ray) B.extq[q] = i;
+  }
+}
+
+__global__ void __launch_bounds__(128) wf_extend() {
+  const DevScene& S = c_scene;
+  const WfBufs& B = c_buf;
+  const unsigned int n = B.ctl->ext_count;
+  TraceStats st{0, 0};
+  unsigned int segs = 0;
+  for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int i = B.extq[j];
+    const float4 o4 = B.o[i], d4 = B.d[i];
+    FastHit h;
+    const bool hit = fast_closest(S, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), h, st, B.err);
+    B.hit[i] = make_float4(h.t, __int_as_float(hit ? h.ent : -1), __int_as_float(h.slot), h.u);
+    B.hitv[i] = h.v;
+    B.d[i].w = __int_as_float((__float_as_int(d4.w) & 1) | (SLOT_HIT << 1));
+    segs++;
+  }
+  if (B.counters) {
+    unsigned long long a = segs, c = st.nodes, dd = st.tris;
+    for (int off = 16; off > 0; off >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, off);
+      c += __shfl_down_sync(0xffffffffu, c, off);
+      dd += __shfl_down_sync(0xffffffffu, dd, off);
+    }
+    if ((threadIdx.x & 31) == 0 && a) {
+      atomicAdd(B.counters + 1, a);
+      atomicAdd(B.counters + 2, c);
+      atomicAdd(B.counters + 3, dd);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) wf_shadow() {
+  const DevScene& S = c_scene;
+  const WfBufs& B = c_buf;
+  const unsigned int n = B.ctl->sh_count;
+  TraceStats st{0, 0};
+  unsigned int segs = 0;
+  for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int k = B.shq[j];
+    const float4 o4 = B.sh_o[k], d4 = B.sh_d[k];
+    if (fast_occluded(S, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), o4.w, st, B.err))
+      B.nee[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    segs++;
+  }
+  if (B.counters) {
+    unsigned long long a = segs, c = st.nodes, dd = st.tris;
+    for (int off = 16; off > 0; off >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, off);
+      c += __shfl_down_sync(0xffffffffu, c, off);
+      dd += __shfl_down_sync(0xffffffffu, dd, off);
+    }
+    if ((threadIdx.x & 31) == 0 && a) {
+      atomicAdd(B.counters + 1, a);
+      atomicAdd(B.counters + 2, c);
+      atomicAdd(B.counters + 3, dd);
+    }
+  }
+}
+
+__global__ void wf_control(cudaGraphConditionalHandle handle, int use_graph) {
+  const WfBufs& B = c_buf;
+  WfCtl* c = B.ctl;
+  // tickets past the ready spawns took nothing
+  if (c->spawn_head > c->spawn_ready) c->spawn_head = c->spawn_ready;
+  const bool pending_spawns = c->spawn_tail > c->spawn_head;
+  c->spawn_ready = c->spawn_tail;
+  const bool more_samples = c->next_sample < B.pass_samples;
+  if (c->next_sample > B.pass_samples) c->next_sample = B.pass_samples;
+  unsigned int work = (c->ext_count > 0 || pending_spawns || more_samples) ? 1u : 0u;
+  c->iterations++;
+  if (c->iterations >= B.max_iterations) {
+    atomicOr(B.err, PR_DEV_LOOP_CAP);
+    work = 0;
+  }
+  if (B.counters) B.counters[4] += c->ext_count;
+  c->ext_count = 0;
+  c->sh_count = 0;
+  c->work = work;
+  if (use_graph) cudaGraphSetConditional(handle, work);
+}
+
+// fixed-point pixel sums -> float image (reference row order), times the
+// sensor response (render.h:1405-1409); accumulate adds to the output
+__global__ void wf_resolve(float* __restrict__ out, int n3, int accumulate, float sensor) {
+  const WfBufs& B = c_buf;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  const float v = (float)((double)B.pix[i] * kPixelInv) * sensor;
+  out[i] = accumulate ? out[i] + v : v;
+}
+
+// ------------------------------------------------------------------ host
+cudaError_t wf_set_constants(const DevScene& S, const RenderCfg& cfg, const WfBufs& B, cudaStream_t s) {
+  cudaError_t e = cudaMemcpyToSymbolAsync(c_scene, &S, sizeof(DevScene), 0, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_cfg, &cfg, sizeof(RenderCfg), 0, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_buf, &B, sizeof(WfBufs), 0, cudaMemcpyHostToDevice, s);
+  return e;
+}
+
+static void launch_body(const WfLaunch& L, cudaGraphConditionalHandle handle, int use_graph, cudaStream_t s) {
+  wf_shade<<<L.shade_blocks, 128, 0, s>>>();
+  wf_extend<<<L.trace_blocks, 128, 0, s>>>();
+  wf_shadow<<<L.trace_blocks, 128, 0, s>>>();
+  wf_control<<<1, 1, 0, s>>>(handle, use_graph);
+}
+
+cudaError_t wf_reset_launch(unsigned int n_slots, cudaStream_t s) {
+  wf_reset<<<(n_slots + 255) / 256, 256, 0, s>>>(n_slots);
+  return cudaGetLastError();
+}
+
+// builds the graph  [while work { shade; extend; shadow; control }]
+cudaError_t wf_build_graph(const WfLaunch& L, cudaStream_t s, cudaGraphExec_t* exec) {
+  cudaGraph_t graph;
+  cudaError_t e = cudaGraphCreate(&graph, 0);
+  if (e != cudaSuccess) return e;
+  cudaGraphConditionalHandle handle;
+  e = cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) { cudaGraphDestroy(graph); return e; }
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = handle;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &p);
+  if (e != cudaSuccess) { cudaGraphDestroy(graph); return e; }
+  cudaGraph_t body = p.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) { cudaGraphDestroy(graph); return e; }
+  launch_body(L, handle, 1, s);
+  cudaError_t e2 = cudaGetLastError();
+  e = cudaStreamEndCapture(s, &body);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  return e;
+}
+
+// host-driven loop: launches iterations and checks the work flag every
+// 'check' iterations (used when graph conditionals are unavailable)
+cudaError_t wf_run_host_loop(const WfLaunch& L, WfCtl* host_ctl_pinned, const WfCtl* dev_ctl, cudaStream_t s) {
+  const int check = 8;
+  for (int it = 0; it < (1 << 20); it += check) {
+    for (int k = 0; k < check; k++) launch_body(L, 0, 0, s);
+    cudaError_t e = cudaMemcpyAsync(host_ctl_pinned, dev_ctl, sizeof(WfCtl), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    if (!host_ctl_pinned->work) break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t wf_resolve_launch(float* out, int n3, int accumulate, float sensor, cudaStream_t s) {
+  wf_resolve<<<(n3 + 255) / 256, 256, 0, s>>>(out, n3, accumulate, sensor);
+  return cudaGetLastError();
+}
+
+}  // namespace pr

@@ -169,11 +169,12 @@ class RenderSettings:
     sensor_response: float = 1.0
     max_path_vertices: int = 0
     flags: int = 0
+    total_spp: int = 0
 
     def to_c(self) -> A.pr_render_params:
         p = A.pr_render_params()
         for k in ("samples", "supersamples", "tent_filter", "depth", "depth_limit", "nee", "media", "mode",
-                  "max_path_vertices", "flags"):
+                  "max_path_vertices", "flags", "total_spp"):
             setattr(p, k, int(getattr(self, k)))
         p.seed = int(self.seed)
         p.luminance_cutoff = float(self.luminance_cutoff)
