@@ -197,7 +197,7 @@ __device__ __forceinline__ void root_path(PathState& ps, float3 o, float3 d) {
 }
 
 // Shades the vertex found by the last closest-hit query of ps.
-__device__ int shade(const DevScene& S, const RenderCfg& cfg, PathState& ps, bool hit, const FastHit& h,
+__device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& ps, bool hit, const FastHit& h,
                      uint64_t sample_id, ShadowReq* sh, int& nsh, PathState& child, uint32_t* err) {
   nsh = 0;
   const bool nee = cfg.nee != 0;
