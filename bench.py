@@ -177,6 +177,8 @@ def run_gpu(args):
     ctx.upload(scene)
     upload_s = time.perf_counter() - t0
     import ctypes as C
+    from prender_gb300 import _abi as A
+    scene.settings.mode = A.PR_MODE_WAVEFRONT if args.mode == "wavefront" else A.PR_MODE_MEGAKERNEL
     cam, prm = scene.camera.to_c(), scene.settings.to_c()
     out = torch.empty((H, W, 3), dtype=torch.float32, device=f"cuda:{local}")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")  # > L2 (129 MB)
@@ -189,24 +191,41 @@ def run_gpu(args):
             raise RuntimeError(L.pr_last_error(ctx.h).decode())
         return ctx.stats()
 
+    def timed(nsteps, first):
+        walls, kern, st = [], [], None
+        for i in range(nsteps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            if dist:
+                dist.barrier()
+            t0 = time.perf_counter()
+            st = step(first + i)
+            torch.cuda.synchronize()
+            walls.append(time.perf_counter() - t0)
+            kern.append(st["device_ms"] / 1e3)
+        return walls, kern, st
+
     for i in range(args.warmup):
         step(i)
     clk = ClockSampler(local)
     clk.start()
-    walls, kern, st = [], [], None
-    for i in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
-        t0 = time.perf_counter()
-        st = step(args.warmup + i)
-        torch.cuda.synchronize()
-        walls.append(time.perf_counter() - t0)
-        kern.append(st["device_ms"] / 1e3)
+    walls, kern, st = timed(args.steps, args.warmup)
     clocks = clk.stop()
     ms = 1e3 * statistics.mean(walls)
     kern_s = statistics.mean(kern)
+    # the other form on the same frames, for the wavefront-vs-plain ratio
+    other = None
+    if not args.single_mode:
+        prm_main = prm
+        prm = scene.settings.to_c()
+        prm.mode = A.PR_MODE_MEGAKERNEL if prm_main.mode == A.PR_MODE_WAVEFRONT else A.PR_MODE_WAVEFRONT
+        for i in range(1):
+            step(i)
+        w2, k2, st2 = timed(max(1, min(args.steps, 3)), args.warmup)
+        other = {"mode": "megakernel" if prm.mode == A.PR_MODE_MEGAKERNEL else "wavefront",
+                 "mpaths_per_s": round(W * H * spp / statistics.mean(w2) / 1e6, 3),
+                 "ms_per_step": round(1e3 * statistics.mean(w2), 3), "segments_per_step": st2["segments"]}
+        prm = prm_main
     if dist:
         t = torch.tensor([ms, kern_s], device=f"cuda:{local}", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -243,7 +262,7 @@ def run_gpu(args):
     achieved = alg_bytes / (st["device_ms"] / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
-            "note": "algorithmic bytes of the megakernel launch; scene (~28 MB) is L2-resident"}
+            "note": "algorithmic traversal bytes of the frame's kernels; scene (~28 MB) is L2-resident"}
     prof = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(prof):
         try:
@@ -265,12 +284,12 @@ def run_gpu(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": name, "width": W, "height": H, "spp": spp, "triangles": int(scene.meshes[1].faces.shape[0]),
-                   "nee": 1, "mode": "megakernel", "l2": "flushed between steps (256 MB write)",
+                   "nee": 1, "mode": args.mode, "other_form": other, "l2": "flushed between steps (256 MB write)",
                    "paths_per_step": paths, "segments_per_step": segs, "kernel_ms_per_step": round(kern_s * 1e3, 3),
                    "scene_upload_s": round(upload_s, 3)},
         "e2e": {"value": round(e2e_val, 3), "unit": "Mpaths/s",
                 "h2d_bytes_per_step": C.sizeof(cam) + C.sizeof(prm), "d2h_bytes_per_step": W * H * 3 * 4},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": int(st["kernel_launches"]) * args.steps,
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clocks,
@@ -288,7 +307,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--mode", default="megakernel")
+    ap.add_argument("--mode", default="wavefront", choices=["wavefront", "megakernel"])
+    ap.add_argument("--single-mode", action="store_true", help="do not also time the other render form")
     ap.add_argument("--small", action="store_true")
     ap.add_argument("--profile", action="store_true", help="full scene, 256x192x16spp image (ncu captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -263,6 +263,7 @@ typedef struct pr_render_stats {
   uint64_t nodes_visited;
   uint64_t tri_tests;
   double device_ms;
+  uint64_t kernel_launches;  /* kernels of this library launched by the call */
 } pr_render_stats;
 int pr_last_render_stats(pr_ctx* ctx, pr_render_stats* stats);
 

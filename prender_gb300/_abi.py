@@ -158,4 +158,5 @@ class pr_render_stats(C.Structure):
         ("nodes_visited", C.c_uint64),
         ("tri_tests", C.c_uint64),
         ("device_ms", C.c_double),
+        ("kernel_launches", C.c_uint64),
     ]

@@ -63,6 +63,7 @@ struct pr_ctx {
   unsigned int wf_graph_slots = 0;
   bool wf_graph_failed = false;
   WfCtl* wf_host_ctl = nullptr;
+  uint64_t wf_passes = 0;
 };
 
 namespace {
@@ -281,7 +282,7 @@ int pr_first_hit_dev(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, 
   int st = check_device_errors(c);
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-  c->stats = pr_render_stats{0, (uint64_t)n, cnt[2], cnt[3], ms};
+  c->stats = pr_render_stats{0, (uint64_t)n, cnt[2], cnt[3], ms, 1};
   return st;
 }
 
@@ -471,7 +472,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   B.counters = (unsigned long long*)c->counters.p;
   B.n_slots = P;
   B.spawn_cap = spawn_cap;
-  B.max_iterations = 100000u;
+  B.max_iterations = 20000u;  // bounded device loop; a frame needs a few hundred
   WfLaunch L;
   L.shade_blocks = (P + 127) / 128;
   L.trace_blocks = std::min<unsigned int>((P + 127) / 128, 152u * 64u);
@@ -489,7 +490,9 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
       c->wf_graph_slots = P;
     }
   }
+  c->wf_passes = 0;
   for (uint64_t first = 0; first < (uint64_t)g.spp; first += layers) {
+    c->wf_passes++;
     const uint64_t n_layers = std::min<uint64_t>(layers, (uint64_t)g.spp - first);
     B.pass_first = first;
     B.pass_samples = n_layers * wh;
@@ -532,8 +535,11 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   st = check_device_errors(c);
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-  const uint64_t paths = p->mode == PR_MODE_WAVEFRONT ? (uint64_t)g.spp * g.width * g.height : cnt[0];
-  c->stats = pr_render_stats{paths, cnt[1], cnt[2], cnt[3], ms};
+  const bool wf = p->mode == PR_MODE_WAVEFRONT;
+  const uint64_t paths = wf ? (uint64_t)g.spp * g.width * g.height : cnt[0];
+  // wavefront: reset per pass + 4 per iteration + resolve; megakernel: kernel + reduce
+  const uint64_t launches = wf ? 4 * cnt[5] + c->wf_passes + 1 : 2;
+  c->stats = pr_render_stats{paths, cnt[1], cnt[2], cnt[3], ms, launches};
   return st;
 }
 

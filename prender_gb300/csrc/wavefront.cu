@@ -323,7 +323,10 @@ __global__ void wf_control(cudaGraphConditionalHandle handle, int use_graph) {
     atomicOr(B.err, PR_DEV_LOOP_CAP);
     work = 0;
   }
-  if (B.counters) B.counters[4] += c->ext_count;
+  if (B.counters) {
+    B.counters[4] += c->ext_count;
+    B.counters[5] += 1;  // iterations
+  }
   c->ext_count = 0;
   c->sh_count = 0;
   c->work = work;

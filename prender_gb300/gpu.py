@@ -121,4 +121,4 @@ class Context:
         s = A.pr_render_stats()
         self._check(self.L.pr_last_render_stats(self.h, C.byref(s)))
         return dict(paths=s.paths, segments=s.segments, nodes_visited=s.nodes_visited, tri_tests=s.tri_tests,
-                    device_ms=s.device_ms)
+                    device_ms=s.device_ms, kernel_launches=s.kernel_launches)
