@@ -129,6 +129,7 @@ __global__ void __launch_bounds__(256) wf_reset(unsigned int n_slots) {
     c->next_sample = 0;
     c->iterations = 0;
     c->work = 1;
+    c->head_start = 0;
   }
 }
 
@@ -139,6 +140,8 @@ __global__ void __launch_bounds__(128) wf_shade() {
   WfCtl* ctl = B.ctl;
   const unsigned int stride = gridDim.x * blockDim.x;
   const unsigned int ready = ctl->spawn_ready;  // spawns written in earlier iterations
+  const unsigned int head_start = ctl->head_start;
+  const bool samples_left = ctl->next_sample < B.pass_samples;
   for (unsigned int base = blockIdx.x * blockDim.x; base < B.n_slots; base += stride) {
     const unsigned int i = base + threadIdx.x;
     int state = SLOT_FREE;
@@ -182,7 +185,8 @@ __global__ void __launch_bounds__(128) wf_shade() {
         if (r == SHADE_SPLIT) {
           atomicAdd(B.live + g, 1);
           const unsigned int t = atomicAdd(&ctl->spawn_tail, 1u);
-          if (t - ctl->spawn_head >= B.spawn_cap) {
+          // entries from head_start on may still be unread this iteration
+          if (t - head_start >= B.spawn_cap) {
             atomicOr(B.err, PR_DEV_QUEUE_OVERFLOW);
           } else {
             const unsigned int q = t % B.spawn_cap;
@@ -207,7 +211,7 @@ __global__ void __launch_bounds__(128) wf_shade() {
       }
       if (state == SLOT_FREE) {
         // refill: a waiting glass branch first, else the next camera sample
-        const unsigned int t = atomicAdd(&ctl->spawn_head, 1u);
+        const unsigned int t = (head_start < ready) ? atomicAdd(&ctl->spawn_head, 1u) : ready;
         if (t < ready) {
           const unsigned int q = t % B.spawn_cap;
           const float4 o = B.sp_o[q], d = B.sp_d[q], b = B.sp_beta[q], w = B.sp_dpw[q];
@@ -222,7 +226,7 @@ __global__ void __launch_bounds__(128) wf_shade() {
           ps.L = f3(0, 0, 0);
           g = B.sp_sample[q];
           has_ray = true;
-        } else {
+        } else if (samples_left) {
           const unsigned long long s = atomicAdd(&ctl->next_sample, 1ull);
           if (s < B.pass_samples) {
             g = s;
@@ -314,7 +318,9 @@ __global__ void wf_control(cudaGraphConditionalHandle handle, int use_graph) {
   // tickets past the ready spawns took nothing
   if (c->spawn_head > c->spawn_ready) c->spawn_head = c->spawn_ready;
   const bool pending_spawns = c->spawn_tail > c->spawn_head;
+  if (c->spawn_tail - c->spawn_head > B.spawn_cap) atomicOr(B.err, PR_DEV_QUEUE_OVERFLOW);
   c->spawn_ready = c->spawn_tail;
+  c->head_start = c->spawn_head;
   const bool more_samples = c->next_sample < B.pass_samples;
   if (c->next_sample > B.pass_samples) c->next_sample = B.pass_samples;
   unsigned int work = (c->ext_count > 0 || pending_spawns || more_samples) ? 1u : 0u;

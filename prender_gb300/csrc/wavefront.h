@@ -18,7 +18,7 @@ struct WfCtl {
   unsigned int spawn_ready;  // branches written before this iteration
   unsigned int iterations;
   unsigned int work;         // 1 while another iteration is needed
-  unsigned int pad;
+  unsigned int head_start;   // spawn_head when this iteration began (after correction)
   unsigned long long next_sample;
 };
 
