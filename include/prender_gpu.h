@@ -255,6 +255,21 @@ int pr_render(pr_ctx* ctx, const pr_camera* cam, const pr_render_params* prm,
 int pr_render_dev(pr_ctx* ctx, const pr_camera* cam, const pr_render_params* prm,
                   float* rgb_accum_dev, uint64_t sample_offset, int accumulate);
 
+/* Allocation-free variant of pr_render_dev for the megakernel form (no
+ * counterpart in the reference, which renders on the CPU).  For callers that
+ * must not allocate device memory while rendering: a caller in the middle of
+ * a CUDA stream capture, a frame loop that cannot absorb cudaMalloc's
+ * implicit synchronisation, or a host whose device memory belongs to its own
+ * pool allocator.  It calls no cudaMalloc / cudaFree; its scratch is a 16 MiB
+ * static device array that every GPU loading this library keeps until exit,
+ * so images of at most 1,398,080 pixels are accepted (larger ones return
+ * PR_E_ARG).  The first call on a device looks up that array's address and
+ * should be made before any stream capture starts.  Calls that overlap on
+ * the GPU share the array and race.  The scene must already be uploaded with
+ * pr_scene_upload (which allocates, at set-up).  Result as pr_render_dev. */
+int pr_render_dev_noalloc(pr_ctx* ctx, const pr_camera* cam, const pr_render_params* prm, float* rgb_accum_dev,
+                          uint64_t sample_offset, int accumulate);
+
 /* Per-launch statistics of the last render: paths, path segments (extension
  * plus shadow rays), QBVH nodes visited, triangle tests, device milliseconds. */
 typedef struct pr_render_stats {

@@ -20,51 +20,7 @@
 
 using namespace pr;
 
-namespace {
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t n = 0;
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= n && p) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
-    if (e == cudaSuccess) n = bytes;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-};
-
-}  // namespace
-
-struct pr_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  std::string err;
-  HostScene host;
-  bool scene_ready = false;
-  DevScene dev{};
-  DevBuf ents, mats, nodes, tris, fnorm;
-  DevBuf errword, counters;  // 4 bytes / 4 x u64
-  DevBuf partial, out, rays, ires, jres, dres;
-  pr_render_stats stats{};
-  // wavefront pool
-  DevBuf wf_o, wf_d, wf_beta, wf_dpw, wf_L, wf_sample, wf_hit, wf_hitv, wf_nee, wf_sho, wf_shd, wf_extq, wf_shq;
-  DevBuf wf_spo, wf_spd, wf_spb, wf_spw, wf_sps, wf_samp, wf_live, wf_pix, wf_ctl;
-  unsigned int wf_slots = 0;
-  cudaGraphExec_t wf_graph = nullptr;
-  unsigned int wf_graph_slots = 0;
-  bool wf_graph_failed = false;
-  WfCtl* wf_host_ctl = nullptr;
-  uint64_t wf_passes = 0;
-};
+#include "ctx_internal.h"
 
 namespace {
 
@@ -105,6 +61,8 @@ cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
 }
 
 }  // namespace
+
+int pr::ctx_fail(pr_ctx* c, int code, const std::string& msg) { return fail(c, code, msg); }
 
 extern "C" {
 
@@ -328,8 +286,10 @@ int pr_trace_fast(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, int
   return PR_OK;
 }
 
+}  // extern "C"
+
 // CameraScreenPram (render.h:105-150) and the Run() sample set-up (:1129-1139)
-static int prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, uint64_t sample_offset,
+int pr::prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, uint64_t sample_offset,
                           RenderCfg& g) {
   if (!cam || !p) return fail(c, PR_E_ARG, "null camera or parameters");
   if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
@@ -405,6 +365,8 @@ static int prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_param
   g.chunks = chunks;
   return PR_OK;
 }
+
+extern "C" {
 
 // paths in flight (slots of the wavefront pool); PR_WF_SLOTS overrides
 static unsigned int wavefront_slots() {

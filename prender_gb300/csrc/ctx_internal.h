@@ -1,0 +1,64 @@
+// Context object behind pr_ctx* (internal to the library).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/prender_gpu.h"
+#include "pr_internal.h"
+#include "render_kernels.h"
+#include "scene_build.h"
+#include "wavefront.h"
+
+namespace pr {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e == cudaSuccess) n = bytes;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace pr
+
+struct pr_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  pr::HostScene host;
+  bool scene_ready = false;
+  pr::DevScene dev{};
+  pr::DevBuf ents, mats, nodes, tris, fnorm;
+  pr::DevBuf errword, counters;  // 4 bytes / 4 x u64
+  pr::DevBuf partial, out, rays, ires, jres, dres;
+  pr_render_stats stats{};
+  // wavefront pool
+  pr::DevBuf wf_o, wf_d, wf_beta, wf_dpw, wf_L, wf_sample, wf_hit, wf_hitv, wf_nee, wf_sho, wf_shd, wf_extq, wf_shq;
+  pr::DevBuf wf_spo, wf_spd, wf_spb, wf_spw, wf_sps, wf_samp, wf_live, wf_pix, wf_ctl;
+  unsigned int wf_slots = 0;
+  cudaGraphExec_t wf_graph = nullptr;
+  unsigned int wf_graph_slots = 0;
+  bool wf_graph_failed = false;
+  pr::WfCtl* wf_host_ctl = nullptr;
+  uint64_t wf_passes = 0;
+};
+
+
+namespace pr {
+// CameraScreenPram + Run() set-up for one render call (capi.cu)
+int prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, uint64_t sample_offset, RenderCfg& g);
+int ctx_fail(pr_ctx* c, int code, const std::string& msg);
+}  // namespace pr
