@@ -127,6 +127,11 @@ typedef struct pr_kerr {
   double a;                   /* angular_momentum (spin, M = 1)              */
   double map_coef[4];         /* background (theta, phi) affine coefficients */
   double escape_radius;       /* 0 = reference behaviour (no escape test)    */
+  double texture_coef;        /* background texture scale ('coef', default 1) */
+  const uint8_t* texture;     /* background texture, RGB8, row y of W pixels as
+                                 Bitmap::cell(y, x) returns it; NULL = none   */
+  int32_t texture_width;
+  int32_t texture_height;
 } pr_kerr;
 
 typedef struct pr_scene_desc {

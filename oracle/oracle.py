@@ -24,7 +24,7 @@ def build(force: bool = False) -> str:
 
 def _stale() -> bool:
     t = os.path.getmtime(LIB)
-    for f in ("prender_oracle.cpp", "oracle_math.h", "kerr_oracle.cpp"):
+    for f in ("prender_oracle.cpp", "oracle_math.h"):
         p = os.path.join(HERE, f)
         if os.path.exists(p) and os.path.getmtime(p) > t:
             return True
@@ -46,8 +46,7 @@ def lib():
         L.oracle_radiance.argtypes = [vp, vp, C.c_int64, C.c_uint64, vp, vp]
         L.oracle_render.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
         L.oracle_light_count.argtypes = [vp]
-        if hasattr(L, "oracle_kerr_trace"):
-            L.oracle_kerr_trace.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp]
+        L.oracle_kerr_trace.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -112,6 +111,20 @@ class OracleScene:
         prm = (settings or self.scene.settings).to_c()
         out = np.empty((rays.shape[0], 3), np.float64)
         assert lib().oracle_radiance(self.h, _p(rays), rays.shape[0], seed, C.byref(prm), _p(out)) == 0
+        return out
+
+    def kerr_trace(self, rays: np.ndarray):
+        """Kerr branch of intersect_scene per ray; status 0 background,
+        1 entity hit, 2 event horizon, 4 step underflow, 5 entity ahead of the
+        last step."""
+        rays = np.ascontiguousarray(rays, dtype=np.float64)
+        n = rays.shape[0]
+        out = dict(status=np.empty(n, np.int32), final_bl=np.empty((n, 3)), exit_dir=np.empty((n, 3)),
+                   steps=np.empty(n, np.int32), hit_entity=np.empty(n, np.int32), hit_t=np.empty(n))
+        rc = lib().oracle_kerr_trace(self.h, _p(rays), n, _p(out["status"]), _p(out["final_bl"]),
+                                     _p(out["exit_dir"]), _p(out["steps"]), _p(out["hit_entity"]),
+                                     _p(out["hit_t"]))
+        assert rc == 0, rc
         return out
 
 

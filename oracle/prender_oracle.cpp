@@ -116,8 +116,9 @@ struct Entity {
   // uvplane (plane.h:129-167)
   V3 org, u_axis, v_axis, normal;
   double u_length = 0, v_length = 0;
-  // circle
+  // circle (disk): its base UVPlane keeps normal_vector_inverse 1 (circle.h:117-130)
   double radius_inner = 0;
+  V3 base_normal;
   // mesh
   int mesh = -1;
   std::vector<Tri> tris;
@@ -132,7 +133,20 @@ struct Light {  // light.h:13-74 (area lights only)
   int entity = -1;
 };
 
+struct KerrBH {  // KerrBlackHole (KerrBlackHole.h:86-151) with M = 1, initial_condition 0
+  bool on = false;
+  V3 position;
+  double a = 0, a2 = 0, M = 1.0, Rhor = 0;
+  int max_steps = 10000;
+  double map_coef[4] = {1, 0, 1, 0};
+  double escape_radius = 0;  // 0: the reference's exit by step count only
+  std::vector<unsigned char> texture;  // background map, RGB8, cell(y, x) = texture[3 (y W + x)]
+  int tex_w = 0, tex_h = 0;
+  double texture_coef = 1.0;
+};
+
 struct Scene {
+  KerrBH kerr;
   std::vector<Material> mats;
   std::vector<Entity> ents;
   std::vector<Mesh> meshes;
@@ -182,6 +196,22 @@ bool uvplane_hit(const Entity& e, V3 org, V3 dir, Hit& h) {
 
 inline V3 vtx(const Mesh& m, int id) {
   return V3(m.vert[3 * id], m.vert[3 * id + 1], m.vert[3 * id + 2]);
+}
+
+// Circle::intersect (circle.h:177-337) without textures: the base UVPlane's
+// plane test with no u/v extent (circle = true), then the annulus
+bool circle_hit(const Entity& e, V3 org, V3 dir, Hit& h) {
+  const V3 normal2 = e.base_normal;
+  const double d = dot(dir, normal2);
+  if (std::fabs(d) < EPS14) return false;
+  h.distance = dot((e.org - org), normal2) / d;
+  h.normal = normal2;
+  h.position = dir * h.distance + org;
+  h.material = e.material;
+  if (h.distance < EPS) return false;
+  if (dot(h.position - e.org, h.position - e.org) > e.radius * e.radius) return false;
+  if (dot(h.position - e.org, h.position - e.org) < e.radius_inner * e.radius_inner) return false;
+  return true;
 }
 
 // Triangle::CheckIntersection2 (polygon.h:78-129) + Triangle::intersect (:131-173)
@@ -482,6 +512,7 @@ bool intersect(const Scene& s, V3 org, V3 dir, Hit& isect) {
     switch (e.type) {
       case PR_ENT_SPHERE: got = sphere_hit(e, o2, dir, h); break;
       case PR_ENT_UVPLANE: got = uvplane_hit(e, o2, dir, h); break;
+      case PR_ENT_CIRCLE: got = circle_hit(e, o2, dir, h); break;
       case PR_ENT_POLYGON: got = qbvh_hit(s, e, o2, dir, h); break;
       default: break;
     }
@@ -563,6 +594,15 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
       // UVPlane::CalcArea (plane.h:174-177)
       e.area = length(e.u_axis * e.u_length) * length(e.v_axis * e.v_length) *
                (1.0 - std::pow(dot(e.u_axis, e.v_axis), 2.0));
+    } else if (pe.type == PR_ENT_CIRCLE) {  // Circle ctor (circle.h:117-130)
+      e.org = V3(pe.p[0], pe.p[1], pe.p[2]);
+      e.radius = pe.radius;
+      e.radius_inner = pe.radius_inner;
+      V3 w, u, v;
+      onb(V3(pe.normal[0], pe.normal[1], pe.normal[2]), w, u, v);
+      const V3 U = u * pe.radius, V = v * pe.radius;  // base = UVPlane(o, r*u, r*v)
+      e.base_normal = normalize(cross(normalize(U), normalize(V)));
+      e.area = e.radius * e.radius * PI;  // Circle::CalcArea
     } else if (pe.type == PR_ENT_POLYGON) {
       if (pe.mesh < 0 || pe.mesh >= (int)s.meshes.size()) { err = "entity mesh out of range"; return PR_E_SCENE; }
       e.mesh = pe.mesh;
@@ -606,6 +646,23 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
       return PR_E_UNSUPPORTED;
     }
     s.ents.push_back(std::move(e));
+  }
+  if (d->kerr.enabled) {
+    s.kerr.on = true;
+    s.kerr.position = V3(d->kerr.position[0], d->kerr.position[1], d->kerr.position[2]);
+    s.kerr.a = d->kerr.a;
+    s.kerr.a2 = s.kerr.a * s.kerr.a;
+    s.kerr.M = 1.0;
+    s.kerr.Rhor = s.kerr.M + std::sqrt(s.kerr.M * s.kerr.M - s.kerr.a2) + 1e-10;  // KerrBlackHole.h:116
+    s.kerr.max_steps = d->kerr.max_steps;
+    for (int k = 0; k < 4; k++) s.kerr.map_coef[k] = d->kerr.map_coef[k];
+    s.kerr.escape_radius = d->kerr.escape_radius;
+    s.kerr.texture_coef = d->kerr.texture_coef;
+    if (d->kerr.texture && d->kerr.texture_width > 0 && d->kerr.texture_height > 0) {
+      s.kerr.tex_w = d->kerr.texture_width;
+      s.kerr.tex_h = d->kerr.texture_height;
+      s.kerr.texture.assign(d->kerr.texture, d->kerr.texture + 3 * (size_t)s.kerr.tex_w * s.kerr.tex_h);
+    }
   }
   // light registration (scene_env.h:1567-1586, :1692-1719) + random_light_setup sort (light.h:97)
   for (int i = 0; i < (int)s.ents.size(); i++) {
@@ -960,11 +1017,20 @@ V3 media_radiance(Ctx& c, V3 org, V3 raydir, const Hit& hp, int ent, double p_rr
   return L;
 }
 
+// Kerr branch of intersect_scene (defined with the Kerr restatement below);
+// on a miss, miss_color is what radiance() returns for it (radiance.h:30-43)
+bool kerr_query(const Scene& s, V3 org, V3 dir, Hit& hit, V3& miss_color);
+
 // radiance() (radiance.h:25-556): diffuse / specular / refraction / media
 V3 radiance(Ctx& c, V3 org, V3 dir, int depth) {
   const Scene& s = c.s;
   Hit hp;
-  if (!intersect(s, org, dir, hp)) return s.background;
+  if (s.kerr.on) {
+    V3 miss;
+    if (!kerr_query(s, org, dir, hp, miss)) return miss;
+  } else if (!intersect(s, org, dir, hp)) {
+    return s.background;
+  }
   const Material& mat = s.mats[hp.material];
   const V3 on = dot(hp.normal, dir) < 0.0 ? hp.normal : (-1.0 * hp.normal);
   V3 rw = mat.emission;
@@ -1186,6 +1252,381 @@ int oracle_render(void* h, const pr_camera* cam, const pr_render_params* prm, in
 int oracle_light_count(void* h) {
   auto* o = static_cast<OracleScene*>(h);
   return o ? (int)o->s.lights.size() : -1;
+}
+
+}  // extern "C"
+
+// ======================================================================
+// Kerr geodesics: the Kerr branch of intersect_scene (scene.cpp:448-732)
+// with KerrBlackHole's set-up, initial conditions and Cash-Karp RK45
+// (KerrBlackHole.h:86-151, :310-440, :660-852, :1239-1431), FP64 in the
+// reference's operation order.
+// ======================================================================
+namespace {
+
+inline double clampd(double v, double lo, double hi) {  // Clamp (vector3d.h:236)
+  if (v < lo) return lo;
+  else if (v > hi) return hi;
+  else return v;
+}
+
+// Cartesian::ToBoyerLindquist (vector3d.h:941-951)
+inline void cart_to_bl(double x, double y, double z, double a, double& r, double& th, double& ph) {
+  double r0 = x * x + y * y + z * z;
+  const double u = r0 - a * a;
+  const double zz = 2. * a * z;
+  r0 = std::sqrt((u + std::sqrt(u * u + zz * zz)) / 2.);
+  th = std::acos(clampd(z / r0, -1.0, 1.0));
+  double phi = std::atan2(y / r0, x / r0);
+  if (phi < 0.0) phi += TWOPI;
+  if (phi >= TWOPI) phi = 0.0;
+  r = r0;
+  ph = phi;
+}
+
+// Spherical::ToBoyerLindquist (vector3d.h:888-898): BL (r, th, ph) -> Cartesian
+inline V3 bl_to_cart(double r, double th, double ph, double a) {
+  const double rr = std::sqrt(r * r + a * a);
+  const double sint = std::sin(th);
+  return V3(rr * std::cos(ph) * sint, rr * std::sin(ph) * sint, r * std::cos(th));
+}
+
+// Cartesian::ToSpherical (vector3d.h:900-918)
+inline void cart_to_sph(double x, double y, double z, double& r, double& th, double& ph) {
+  r = std::sqrt(x * x + y * y + z * z);
+  double xx = 0, yy = 0, zz = 0;
+  if (r > 1.0e-16) {
+    xx = x / r;
+    yy = y / r;
+    zz = z / r;
+  } else {
+    th = 0;
+    ph = 0;
+    return;
+  }
+  th = std::acos(clampd(zz, -1.0, 1.0));
+  double phi;
+  if (std::fabs(xx) < 1.0e-6 && std::fabs(yy) < 1.0e-6) phi = 0.0;
+  else phi = std::atan2(yy, xx);
+  if (phi < 0.0) phi += 2.0 * PI;
+  if (phi >= 2.0 * PI) phi = 0.0;
+  ph = phi;
+}
+
+struct KerrRay {
+  const KerrBH& k;
+  double L = 0, kappa = 0;
+  double traceDir = 1.0;
+  explicit KerrRay(const KerrBH& kk) : k(kk) {}
+
+  // KerrBlackHole::geodesic (KerrBlackHole.h:1239-1281)
+  void geodesic(const double* y, double* dydx) const {
+    const double r = y[0];
+    const double theta = y[1];
+    const double pr = y[4];
+    const double ptheta = y[5];
+    const double r2 = r * r;
+    const double twor = 2.0 * k.M * r;
+    const double sintheta = std::sin(theta);
+    double sin2 = sintheta * sintheta;
+    const double costheta = std::cos(theta);
+    const double cos2 = costheta * costheta;
+    const double sigma = r2 + k.a2 * cos2;
+    const double delta = r2 - twor + k.a2;
+    const double sd = sigma * delta;
+    const double siginv = 1.0 / sigma;
+    const double bot = 1.0 / sd;
+    if (std::fabs(sin2) < 1.0e-16) {
+      if (sin2 < 0.0) sin2 = -1.0e-16;
+      else sin2 = 1.0e-16;
+    }
+    dydx[0] = -pr * delta * siginv;
+    dydx[1] = -ptheta * siginv;
+    dydx[2] = -(twor * k.a + (sigma - twor) * L / sin2) * bot;
+    dydx[3] = -(1.0 + (twor * (r2 + k.a2) - twor * k.a * L) * bot);
+    dydx[4] = -(((r - 1.0) * (-kappa) + twor * (r2 + k.a2) - 2.0 * k.a * L) * bot - 2.0 * pr * pr * (r - 1.0) * siginv);
+    dydx[5] = -sintheta * costheta * (L * L / (sin2 * sin2) - k.a2) * siginv;
+  }
+
+  // rkstep (KerrBlackHole.h:1288-1361)
+  void rkstep(const double* y, const double* dydx, double h, double* yout, double* yerr) const {
+    double ak[6], t1[6], t2[6], t3[6], t4[6], t5[6];
+    h *= traceDir;
+    for (int i = 0; i < 6; i++) {
+      const double hdydx = h * dydx[i];
+      const double yi = y[i];
+      t1[i] = yi + 0.2 * hdydx;
+      t2[i] = yi + (3.0 / 40.0) * hdydx;
+      t3[i] = yi + 0.3 * hdydx;
+      t4[i] = yi - (11.0 / 54.0) * hdydx;
+      t5[i] = yi + (1631.0 / 55296.0) * hdydx;
+      yout[i] = yi + (37.0 / 378.0) * hdydx;
+      yerr[i] = ((37.0 / 378.0) - (2825.0 / 27648.0)) * hdydx;
+    }
+    geodesic(t1, ak);
+    for (int i = 0; i < 6; i++) {
+      const double yt = h * ak[i];
+      t2[i] += (9.0 / 40.0) * yt;
+      t3[i] -= 0.9 * yt;
+      t4[i] += 2.5 * yt;
+      t5[i] += (175.0 / 512.0) * yt;
+    }
+    geodesic(t2, ak);
+    for (int i = 0; i < 6; i++) {
+      const double yt = h * ak[i];
+      t3[i] += 1.2 * yt;
+      t4[i] -= (70.0 / 27.0) * yt;
+      t5[i] += (575.0 / 13824.0) * yt;
+      yout[i] += (250.0 / 621.0) * yt;
+      yerr[i] += ((250.0 / 621.0) - (18575.0 / 48384.0)) * yt;
+    }
+    geodesic(t3, ak);
+    for (int i = 0; i < 6; i++) {
+      const double yt = h * ak[i];
+      t4[i] += (35.0 / 27.0) * yt;
+      t5[i] += (44275.0 / 110592.0) * yt;
+      yout[i] += (125.0 / 594.0) * yt;
+      yerr[i] += ((125.0 / 594.0) - (13525.0 / 55296.0)) * yt;
+    }
+    geodesic(t4, ak);
+    for (int i = 0; i < 6; i++) {
+      const double yt = h * ak[i];
+      t5[i] += (253.0 / 4096.0) * yt;
+      yerr[i] -= (277.0 / 14336.0) * yt;
+    }
+    geodesic(t5, ak);
+    for (int i = 0; i < 6; i++) {
+      const double yt = h * ak[i];
+      yout[i] += (512.0 / 1771.0) * yt;
+      yerr[i] += ((512.0 / 1771.0) - 0.25) * yt;
+    }
+  }
+
+  // rkqs (KerrBlackHole.h:1366-1431); returns hnext, updates y
+  double rkqs(double* y, const double* dydx, double htry, double escal, const double* yscal, int& attempts) const {
+    double errmax = 0.0, h = htry, htemp;
+    double yerr[6], ytemp[6];
+    const int loopMax = 40;
+    int loopCnt = 0;
+    while (loopCnt < loopMax) {
+      rkstep(y, dydx, h, ytemp, yerr);
+      attempts++;
+      errmax = 0.0;
+      for (int i = 0; i < 6; i++) {
+        const double temp = std::fabs(yerr[i] / yscal[i]);
+        if (temp > errmax) errmax = temp;
+      }
+      errmax *= escal;
+      if (errmax <= 1.0) break;
+      htemp = 0.9 * h / std::sqrt(std::sqrt(errmax));
+      h *= 0.1;
+      if (h >= 0.0) {
+        if (htemp > h) h = htemp;
+      } else {
+        if (htemp < h) h = htemp;
+      }
+      loopCnt++;
+    }
+    double hnext;
+    if (errmax > 1.89e-4) hnext = 0.9 * h * std::pow(errmax, -0.2);
+    else hnext = 5.0 * h;
+    for (int i = 0; i < 6; i++) y[i] = ytemp[i];
+    return hnext;
+  }
+
+  // NextPosition (KerrBlackHole.h:471-522)
+  double next_position(double* y, const double* dydx, double htry, int& attempts) const {
+    const double escal = 1e11;
+    double yscal[6];
+    for (int i = 0; i < 6; i++) yscal[i] = std::fabs(y[i]) + std::fabs(dydx[i] * htry) + 1.0e-3;
+    return rkqs(y, dydx, htry, escal, yscal, attempts);
+  }
+
+  // initial2 (KerrBlackHole.h:310-440) for theta0 = y[1]
+  void initial2(double* y0, double* ydot0, double r0, double theta0) {
+    y0[3] = 0;
+    y0[4] = 0;
+    y0[5] = 0;
+    double sintheta = std::sin(theta0), costheta = std::cos(theta0);
+    const double cos2 = costheta * costheta;
+    double sin2 = sintheta * sintheta;
+    const double POLE_THRESHOLD = 1e-8;
+    const bool near_pole = (sin2 < POLE_THRESHOLD * POLE_THRESHOLD);
+    if (near_pole) {
+      const double sigma = r0 * r0 + k.a2;
+      const double delta = r0 * r0 - 2.0 * k.M * r0 + k.a2;
+      const double vphi_sin = ydot0[2] * sintheta;
+      const double rdot0 = ydot0[0];
+      const double thetadot0 = ydot0[1];
+      const double energy2 = (sigma - 2.0 * r0) * (rdot0 * rdot0 / delta + thetadot0 * thetadot0) + delta * vphi_sin * vphi_sin;
+      const double energy = std::sqrt(std::fabs(energy2)) + 1e-10;
+      y0[4] = rdot0 * sigma / delta / energy;
+      y0[5] = thetadot0 * sigma / energy;
+      L = 0.0;
+      kappa = y0[5] * y0[5] + k.a2 * sin2;
+    } else {
+      if (sin2 < 1e-16) {
+        sintheta = 1e-16;
+        sin2 = 1e-32;
+      }
+      const double rdot0 = ydot0[0];
+      const double thetadot0 = ydot0[1];
+      const double r2 = r0 * r0;
+      const double sigma = r2 + k.a2 * cos2;
+      const double delta = r2 - 2.0 * k.M * r0 + k.a2;
+      const double s1 = sigma - 2.0 * r0;
+      y0[4] = rdot0 * sigma / delta;
+      y0[5] = thetadot0 * sigma;
+      const double phidot0 = ydot0[2];
+      const double energy2 = s1 * (rdot0 * rdot0 / delta + thetadot0 * thetadot0) + delta * sin2 * phidot0 * phidot0;
+      const double energy = std::sqrt(std::fabs(energy2)) + 1.0e-10;
+      y0[4] = y0[4] / energy;
+      y0[5] = y0[5] / energy;
+      L = ((sigma * delta * phidot0 - 2.0 * k.a * r0 * energy) * sin2 / s1) / energy;
+      kappa = y0[5] * y0[5] + k.a2 * sin2 + L * L / sin2;
+    }
+    geodesic(y0, ydot0);
+  }
+
+  // RayToOrdinaryDifferentialEquationInitial, initial_condition 0 (KerrBlackHole.h:660-852)
+  void initial(const V3& dir, double* y, double* dydx, double r0, double theta0) {
+    y[3] = 0;
+    y[4] = 0;
+    y[5] = 0;
+    const double r = y[0], theta = y[1], phi = y[2];
+    double rs, theta_obs, phi_obs;
+    cart_to_sph(dir.x, dir.y, dir.z, rs, theta_obs, phi_obs);
+    const double Phi = phi - phi_obs;
+    const double cost = std::cos(theta);
+    const double sintobs = std::sin(theta_obs);
+    const double rr = r * r;
+    const double sigma = rr + (k.a * cost) * (k.a * cost);
+    const double R = std::sqrt(k.a2 + rr);
+    const double v = -sintobs * std::cos(Phi);
+    const double zdot = 1.;
+    const double inv_sigma = 1.0 / sigma;
+    const double sint = std::sin(theta);
+    const double rdot0 = zdot * (r * R * v * sint - R * R * std::cos(theta_obs) * cost) * inv_sigma;
+    const double thetadot0 = zdot * (r * sint * std::cos(theta_obs) + R * v * cost) * inv_sigma;
+    double phidot0;
+    const double POLE_THRESHOLD = 1e-8;
+    if (std::fabs(sint) < POLE_THRESHOLD) phidot0 = 0.0;
+    else phidot0 = zdot * sintobs * std::sin(Phi) / (R * sint);
+    dydx[0] = rdot0;
+    dydx[1] = thetadot0;
+    dydx[2] = phidot0;
+    initial2(y, dydx, r0, theta0);
+  }
+};
+
+}  // namespace
+
+namespace {
+
+// The Kerr branch of intersect_scene for one ray (scene.cpp:448-732).
+// Returns the status (0 background, 1 entity hit, 2 event horizon, 4 step
+// underflow, 5 entity ahead of the last step); y is the final state, dir2
+// the last polyline direction, cnt the steps taken, hit the accepted hit.
+int kerr_trace_one(const Scene& s, V3 org, V3 dir, Hit& hit, double* y, V3& dir2, int& cnt) {
+  const KerrBH& kb = s.kerr;
+  KerrRay K(kb);
+  double dydx[6];
+  const V3 rel = org - kb.position;  // Setup (KerrBlackHole.h:153-166)
+  double r0, th0, ph0;
+  cart_to_bl(rel.x, rel.y, rel.z, kb.a, r0, th0, ph0);
+  cnt = 0;
+  V3 org2 = org, org1 = org;
+  dir2 = dir;
+  y[0] = r0; y[1] = th0; y[2] = ph0; y[3] = 0; y[4] = 0; y[5] = 0;
+  if (r0 < kb.Rhor) return 2;
+  K.traceDir = 1.0;
+  K.initial(1.0 * dir, y, dydx, r0, th0);
+  const double h_dist = 2.0;
+  double h_step = h_dist;
+  int attempts = 0;
+  while ((kb.max_steps < 0) ? 1 : (cnt < kb.max_steps)) {
+    if (intersect(s, org1, dir2, hit)) {
+      if (hit.distance < h_dist) {
+        const V3 c = hit.position - kb.position;
+        double sr, sth, sph;
+        cart_to_bl(c.x, c.y, c.z, kb.a, sr, sth, sph);
+        return (sr < kb.Rhor) ? 2 : 1;
+      }
+    }
+    K.geodesic(y, dydx);
+    if (std::fabs(h_step) < 1.0e-10) return 4;
+    const double r_before = y[0];
+    h_step = K.next_position(y, dydx, h_step, attempts);
+    if (h_step > h_dist) h_step = h_dist;
+    if (y[0] < kb.Rhor) return 2;
+    org1 = org2;
+    const V3 c = bl_to_cart(y[0], y[1], y[2], kb.a);
+    org2 = c + kb.position;
+    dir2 = normalize(org2 - org1);
+    cnt++;
+    // optional early exit (not in the reference): far out and receding
+    if (kb.escape_radius > 0.0 && y[0] > kb.escape_radius && y[0] > r_before) break;
+  }
+  if (intersect(s, org2, dir2, hit)) return 5;
+  return 0;
+}
+
+// background colour of an escaped ray (scene.cpp:711-727 + SphericalMapping::Map, circle.h:92-105)
+V3 kerr_background(const KerrBH& kb, const double* yy, const V3& bg) {
+  if (kb.texture.empty()) return bg;
+  double y1 = yy[1] * kb.map_coef[0] + kb.map_coef[1];
+  double y2 = yy[2] * kb.map_coef[2] + kb.map_coef[3];
+  y1 = std::fmod(y1, PI);
+  y2 = std::fmod(y2, 2.0 * PI);
+  double phi = y2, theta = y1;
+  if (phi < 0.0) phi += 2.0 * PI;
+  if (theta < 0.0) theta = -theta;
+  int x = (int)(phi / (2.0 * PI) * kb.tex_w);
+  x = x % kb.tex_w;
+  const int y1i = (int)(theta / PI * kb.tex_h);
+  const int yv = y1i % kb.tex_h;
+  const unsigned char* t = &kb.texture[3 * ((size_t)yv * kb.tex_w + x)];
+  return V3(kb.texture_coef * t[0] / 255.0, kb.texture_coef * t[1] / 255.0, kb.texture_coef * t[2] / 255.0);
+}
+
+bool kerr_query(const Scene& s, V3 org, V3 dir, Hit& hit, V3& miss_color) {
+  double y[6];
+  V3 dir2;
+  int cnt;
+  const int st = kerr_trace_one(s, org, dir, hit, y, dir2, cnt);
+  if (st == 1) return true;
+  if (st == 2) miss_color = V3();
+  else if (st == 0) miss_color = kerr_background(s.kerr, y, s.background);
+  else miss_color = s.background;
+  return false;
+}
+
+}  // namespace
+
+extern "C" {
+
+// One Kerr trace per ray (intersect_scene's Kerr branch, scene.cpp:448-732).
+int oracle_kerr_trace(void* h, const double* rays, int64_t n, int32_t* status, double* final_bl, double* exit_dir,
+                      int32_t* steps, int32_t* hit_entity, double* hit_t) {
+  auto* o = static_cast<OracleScene*>(h);
+  if (!o || !rays || n < 0 || !o->s.kerr.on) return PR_E_ARG;
+  for (int64_t q = 0; q < n; q++) {
+    const double* rr = rays + 6 * q;
+    Hit hit;
+    double y[6];
+    V3 dir2;
+    int cnt = 0;
+    const int st = kerr_trace_one(o->s, V3(rr[0], rr[1], rr[2]), V3(rr[3], rr[4], rr[5]), hit, y, dir2, cnt);
+    status[q] = st;
+    steps[q] = cnt;
+    for (int k = 0; k < 3; k++) final_bl[3 * q + k] = y[k];
+    exit_dir[3 * q] = dir2.x;
+    exit_dir[3 * q + 1] = dir2.y;
+    exit_dir[3 * q + 2] = dir2.z;
+    hit_entity[q] = (st == 1 || st == 5) ? hit.object_id : -1;
+    hit_t[q] = (st == 1 || st == 5) ? hit.distance : -1.0;
+  }
+  return PR_OK;
 }
 
 }  // extern "C"

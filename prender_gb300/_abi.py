@@ -99,6 +99,10 @@ class pr_kerr(C.Structure):
         ("a", C.c_double),
         ("map_coef", C.c_double * 4),
         ("escape_radius", C.c_double),
+        ("texture_coef", C.c_double),
+        ("texture", C.c_void_p),
+        ("texture_width", C.c_int32),
+        ("texture_height", C.c_int32),
     ]
 
 

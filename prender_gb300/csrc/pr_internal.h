@@ -59,6 +59,7 @@ struct GEntity {
   // sphere / disk centre, uvplane origin (FP64: the hit test runs in FP64)
   double p[3];
   double radius;
+  double radius_inner;     // disk (annulus) inner radius
   // uvplane: unit axes, lengths and normal (plane.h:146-167)
   double u_axis[3], v_axis[3], normal[3];
   double u_length, v_length;
@@ -84,6 +85,7 @@ struct GEntF {
   float n[3];
   float area;
   int32_t face_base, node_base, pad0, pad1;
+  // disk: u_length = radius, v_length = inner radius, n = the plane normal
 };
 
 struct GMedium {
@@ -93,6 +95,20 @@ struct GMedium {
   float sigma_t[3];        // transmittanceColor
   float g[3];              // phase_prm
   int32_t on;
+};
+
+// KerrBlackHole state shared by every ray of a scene (KerrBlackHole.h:86-151;
+// M = 1 as SceneEnv constructs it, scene_env.h:2067)
+struct GKerr {
+  int32_t enabled;
+  int32_t max_steps;       // geodesics_max_length
+  double pos[3];           // black hole centre (world)
+  double a, a2, M, Rhor;   // spin, spin^2, mass, horizon radius + 1e-10
+  double map_coef[4];      // background (theta, phi) affine map
+  double escape_radius;    // 0: integrate to max_steps as the reference does
+  double texture_coef;     // background texture scale (background_texture_coef)
+  const unsigned char* texture;  // background texture, RGB8 rows as cell(y, x) reads them
+  int32_t tex_w, tex_h;
 };
 
 // Everything a kernel needs, passed by value (fits the 4 KB param space).

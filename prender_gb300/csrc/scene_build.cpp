@@ -375,6 +375,29 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
       }
       g.area = len(scale(u, g.u_length)) * len(scale(v, g.v_length)) * (1.0 - std::pow(dot(u, v), 2.0));
       for (int k = 0; k < 3; k++) grow(pe.p[k]);
+    } else if (pe.type == PR_ENT_CIRCLE) {
+      // Circle ctor (circle.h:117-134): a UVPlane(o, r u, r v) with u, v from
+      // OrthonormalBasis(n); its plane normal is never inverted (the base
+      // UVPlane keeps the default normal_vector_inverse) and CalcArea = pi r^2
+      if (!(pe.radius > 0.0) || pe.radius_inner < 0.0) { err = "disk radius must be positive"; return PR_E_SCENE; }
+      const D3 w = mk(pe.normal);
+      const D3 u = std::fabs(w.x) > 1.0e-6 ? unit(cross(D3{0.0, 1.0, 0.0}, w)) : unit(cross(D3{1.0, 0.0, 0.0}, w));
+      const D3 v = unit(cross(w, u));
+      const D3 U = scale(u, pe.radius), V = scale(v, pe.radius);
+      const D3 n = unit(cross(unit(U), unit(V)));
+      g.normal_inverse = 1;
+      for (int k = 0; k < 3; k++) {
+        g.p[k] = pe.p[k];
+        g.u_axis[k] = (&u.x)[k];
+        g.v_axis[k] = (&v.x)[k];
+        g.normal[k] = (&n.x)[k];
+      }
+      g.radius = pe.radius;
+      g.radius_inner = pe.radius_inner;
+      g.u_length = pe.radius;
+      g.v_length = pe.radius_inner;
+      g.area = pe.radius * pe.radius * 3.14159265358979323846;
+      for (int k = 0; k < 3; k++) { grow(pe.p[k] - pe.radius); grow(pe.p[k] + pe.radius); }
     } else if (pe.type == PR_ENT_POLYGON) {
       if (pe.mesh < 0 || pe.mesh >= d->n_meshes) { err = "entity mesh out of range"; return PR_E_SCENE; }
       const pr_mesh& pm_ = d->meshes[pe.mesh];
@@ -446,6 +469,7 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
     const pr_material& pm = d->materials[hs.ents[i].material];
     if (is_light(pm)) {
       hs.ents[i].is_light = 1;
+      if (hs.ents[i].type == PR_ENT_CIRCLE) hs.disk_light = true;
       lights.push_back({hs.ents[i].area * len(mk(pm.emission)), i});
     }
   }
@@ -453,6 +477,35 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
   if ((int)lights.size() > kMaxLights) { err = "too many lights"; return PR_E_ARG; }
   for (const L& l : lights) hs.light_ent.push_back(l.ent);
   hs.scene_scale = (float)ext;
+  // black hole (scene_env.h:701-766, :2056-2098; KerrBlackHole ctor :86-151)
+  hs.kerr = GKerr{};
+  hs.kerr_texture.clear();
+  const pr_kerr& pk = d->kerr;
+  if (pk.enabled) {
+    if (!(pk.a * pk.a < 1.0)) { err = "Kerr spin must satisfy |a| < M = 1"; return PR_E_SCENE; }
+    if (pk.max_steps <= 0 || pk.max_steps > 10000000) {
+      err = "geodesics_max_length must be in 1..1e7 (an unbounded trace is not run on the GPU)";
+      return PR_E_ARG;
+    }
+    if (pk.escape_radius < 0.0) { err = "escape_radius must be >= 0"; return PR_E_ARG; }
+    GKerr& k = hs.kerr;
+    k.enabled = 1;
+    k.max_steps = pk.max_steps;
+    for (int q = 0; q < 3; q++) k.pos[q] = pk.position[q];
+    k.a = pk.a;
+    k.a2 = pk.a * pk.a;
+    k.M = 1.0;
+    k.Rhor = k.M + std::sqrt(k.M * k.M - k.a2) + 1e-10;
+    for (int q = 0; q < 4; q++) k.map_coef[q] = pk.map_coef[q];
+    k.escape_radius = pk.escape_radius;
+    k.texture_coef = pk.texture_coef;
+    if (pk.texture) {
+      if (pk.texture_width <= 0 || pk.texture_height <= 0) { err = "background texture size must be positive"; return PR_E_ARG; }
+      hs.kerr_texture.assign(pk.texture, pk.texture + 3 * (size_t)pk.texture_width * pk.texture_height);
+      k.tex_w = pk.texture_width;
+      k.tex_h = pk.texture_height;
+    }
+  }
   return PR_OK;
 }
 

@@ -39,6 +39,9 @@ struct HostScene {
   double background[3] = {0, 0, 0};
   double env_light[3] = {0, 0, 0};
   float scene_scale = 1.0f;
+  GKerr kerr{};
+  std::vector<unsigned char> kerr_texture;
+  bool disk_light = false;  // an emitting disk is registered as a light
 };
 
 int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err);

@@ -215,6 +215,8 @@ class SceneDesc:
         d.environment_light[:] = [float(x) for x in scene.environment_light]
         d.medium = scene.medium.to_c()
         k = A.pr_kerr()
+        k.texture_coef = 1.0
+        self._keep = []
         if scene.kerr is not None:
             k.enabled = 1
             k.max_steps = int(scene.kerr["max_steps"])
@@ -222,6 +224,15 @@ class SceneDesc:
             k.a = float(scene.kerr["a"])
             k.map_coef[:] = [float(x) for x in scene.kerr.get("map_coef", (1.0, 0.0, 1.0, 0.0))]
             k.escape_radius = float(scene.kerr.get("escape_radius", 0.0))
+            k.texture_coef = float(scene.kerr.get("texture_coef", 1.0))
+            tex = scene.kerr.get("texture")
+            if tex is not None:
+                tex = np.ascontiguousarray(tex, dtype=np.uint8)
+                if tex.ndim != 3 or tex.shape[2] != 3:
+                    raise ValueError("background texture must be (H, W, 3) uint8")
+                self._keep.append(tex)
+                k.texture = tex.ctypes.data
+                k.texture_height, k.texture_width = tex.shape[0], tex.shape[1]
         d.kerr = k
         self.desc = d
 
@@ -256,6 +267,23 @@ class Scene:
         self.entities.append(Entity(A.PR_ENT_UVPLANE, self._mat(material), normal_inverse, p=tuple(org),
                                     u=tuple(U), v=tuple(V)))
         return len(self.entities) - 1
+
+    def add_disk(self, center, normal, radius, material: Material, radius_inner: float = 0.0,
+                 normal_inverse: int = 1) -> int:
+        """An annulus ('disk2 x y z r r_inner' + 'normal nx ny nz'; circle.h)."""
+        self.entities.append(Entity(A.PR_ENT_CIRCLE, self._mat(material), normal_inverse, p=tuple(center),
+                                    radius=float(radius), normal=tuple(normal), radius_inner=float(radius_inner)))
+        return len(self.entities) - 1
+
+    def set_black_hole(self, position, a: float, max_steps: int = 10000,
+                       map_coef=(1.0, 0.0, 1.0, 0.0), escape_radius: float = 0.0,
+                       texture=None, texture_coef: float = 1.0) -> None:
+        """A Kerr black hole of mass 1 ('BLACKHOLE x y z' block, scene_env.h:701-766);
+        texture is the background map as an (H, W, 3) uint8 array indexed
+        [y, x] the way the reference's Bitmap::cell(y, x) reads its image."""
+        self.kerr = {"position": tuple(float(x) for x in position), "a": float(a), "max_steps": int(max_steps),
+                     "map_coef": tuple(float(x) for x in map_coef), "escape_radius": float(escape_radius),
+                     "texture": texture, "texture_coef": float(texture_coef)}
 
     def add_mesh(self, vertices, faces, material: Material, normal_inverse: int = 1) -> int:
         self.meshes.append(Mesh(vertices, faces))
@@ -298,6 +326,20 @@ class Scene:
         ]
         if cam.angle is not None:
             out += ["CAMERA_ANGLE", _fmt(cam.angle), ""]
+        if self.kerr is not None:
+            k = self.kerr
+            if k.get("escape_radius", 0.0):
+                raise ValueError("escape_radius has no reference counterpart")
+            out += [f"BLACKHOLE {f3(k['position'])}",
+                    f"geodesics_max_length {int(k['max_steps'])}",
+                    f"angular_momentum {_fmt(k['a'])}",
+                    "initial_condition 0",
+                    f"map_coef {f3(k.get('map_coef', (1.0, 0.0, 1.0, 0.0)))}"]
+            if k.get("texture") is not None:
+                tex_path = os.path.join(directory, "background.bmp")
+                _write_bmp24(tex_path, np.asarray(k["texture"], dtype=np.uint8))
+                out += [f"background_texture {tex_path}", f"coef {_fmt(k.get('texture_coef', 1.0))}"]
+            out.append("")
         md = self.medium
         out += ["SCATTERING", "0", f3(md.sigma_s_rgb), "",
                 "ABSORBING", "0", f3(md.sigma_a_rgb), "",
@@ -311,6 +353,8 @@ class Scene:
                 out.append(f"sphere {f3(e.p)} {_fmt(e.radius)}")
             elif e.type == A.PR_ENT_UVPLANE:
                 out += [f"uvplane {f3(e.p)}", f"U {f3(e.u)}", f"V {f3(e.v)}"]
+            elif e.type == A.PR_ENT_CIRCLE:
+                out += [f"disk2 {f3(e.p)} {_fmt(e.radius)} {_fmt(e.radius_inner)}", f"normal {f3(e.normal)}"]
             elif e.type == A.PR_ENT_POLYGON:
                 objname = f"mesh{e.mesh}.obj"
                 _write_obj(os.path.join(directory, objname), self.meshes[e.mesh])
@@ -348,6 +392,30 @@ def _fmt(x) -> str:
     if len(digits) > 15:
         raise ValueError(f"{x!r} needs more than 15 significant digits in the reference scene format")
     return s
+
+
+def _write_bmp24(path: str, tex: np.ndarray) -> None:
+    """24-bit BMP whose decoded image, read back through the reference's
+    BitMap::cell(y, x) (bitmap.h:187-190: row H-1-y of the top-down decode),
+    is tex[y, x]: the file's bottom row is tex[0]."""
+    h, w, _ = tex.shape
+    row = w * 3
+    pad = (4 - row % 4) % 4
+    size = 54 + (row + pad) * h
+    hdr = bytearray(54)
+    hdr[0:2] = b"BM"
+    hdr[2:6] = size.to_bytes(4, "little")
+    hdr[10:14] = (54).to_bytes(4, "little")
+    hdr[14:18] = (40).to_bytes(4, "little")
+    hdr[18:22] = w.to_bytes(4, "little")
+    hdr[22:26] = h.to_bytes(4, "little")  # positive height: rows stored bottom-up
+    hdr[26:28] = (1).to_bytes(2, "little")
+    hdr[28:30] = (24).to_bytes(2, "little")
+    hdr[34:38] = ((row + pad) * h).to_bytes(4, "little")
+    with open(path, "wb") as fh:
+        fh.write(bytes(hdr))
+        for y in range(h):  # stored bottom row first = tex[0]
+            fh.write(tex[y, :, ::-1].tobytes() + b"\0" * pad)
 
 
 def _write_obj(path: str, mesh: Mesh) -> None:

@@ -8,6 +8,8 @@ rendered by the GPU library and written in the reference's scene format.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 from . import _abi as A
@@ -152,6 +154,46 @@ def media_cornell(width: int = 128, height: int = 96, samples: int = 4, supersam
     s.participating_media = 1
     s.medium = Medium(sigma_s_rgb=(sigma_s,) * 3, sigma_a_rgb=(sigma_a,) * 3, phase_g=(g,) * 3)
     s.settings.media = 1
+    return s
+
+
+def celestial_texture(width: int = 1024, height: int = 512, stars: int = 10000, seed: int = 0,
+                      cells=(24, 12)) -> np.ndarray:
+    """Procedural celestial sphere for the Kerr background map: a seeded
+    two-tone checker in (phi, theta) plus point stars; (H, W, 3) uint8
+    indexed [y, x] as the background lookup's cell(y, x)."""
+    rng = np.random.default_rng(seed)
+    ys, xs = np.meshgrid(np.arange(height), np.arange(width), indexing="ij")
+    cx = (xs * cells[0]) // width
+    cy = (ys * cells[1]) // height
+    even = ((cx + cy) % 2 == 0)[..., None]
+    tex = np.where(even, np.array([38, 44, 70], np.uint8), np.array([16, 14, 30], np.uint8)).astype(np.uint8)
+    sx = rng.integers(0, width, stars)
+    sy = rng.integers(0, height, stars)
+    b = rng.integers(120, 256, stars)
+    tint = rng.integers(0, 3, stars)
+    col = np.stack([b, b, b], 1)
+    col[np.arange(stars), tint] = np.minimum(255, col[np.arange(stars), tint] + 40)
+    tex[sy, sx] = col.astype(np.uint8)
+    return np.ascontiguousarray(tex)
+
+
+def kerr_disk(width: int = 256, height: int = 192, a: float = 0.9, max_steps: int = 400,
+              samples: int = 1, supersamples: int = 1, escape_radius: float = 0.0, texture=None) -> Scene:
+    """A spinning black hole of mass 1 at the origin (spin axis z) with a thin
+    emitting annulus in its equatorial plane (r 3..12), a diffuse sphere behind
+    it that the hole lenses, and a camera 30 M away, 8 degrees above the disk
+    plane; the scene of the reference's BLACKHOLE examples at test scale."""
+    s = Scene()
+    s.add_disk((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 12.0,
+               Material.diffuse((0.75, 0.75, 0.75), emission=(4.0, 2.5, 1.0)), radius_inner=3.0)
+    s.add_sphere((6.0, 40.0, 6.0), 6.0, Material.diffuse((0.25, 0.55, 0.85), emission=(0.4, 0.8, 1.2)))
+    s.set_black_hole((0.0, 0.0, 0.0), a, max_steps=max_steps, escape_radius=escape_radius, texture=texture)
+    el = math.radians(8.0)
+    c, sn = round(math.cos(el), 12), round(math.sin(el), 12)  # decimal-exact in the scene text
+    s.camera = Camera(position=(0.0, round(-30.0 * c, 10), round(30.0 * sn, 10)), dir=(0.0, c, -sn), up=(0.0, 0.0, 1.0),
+                      width=width, height=height, angle=40.0)
+    s.settings = RenderSettings(samples=samples, supersamples=supersamples, depth=1, depth_limit=1, nee=0)
     return s
 
 

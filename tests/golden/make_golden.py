@@ -68,11 +68,48 @@ def ref_render(path, shape, d, threads=1):
     return np.fromfile(os.path.join(d, "img.f64")).reshape(shape[1], shape[0], 3), out.strip().splitlines()[-1]
 
 
+def ref_kerr(path, rays, d):
+    """harness record per ray: object id, hit flag, 16 doubles (loop ended,
+    steps, y[6], org2, dir2, hit distance, 0), hit colour"""
+    rays.astype(np.float64).tofile(os.path.join(d, "rays.f64"))
+    run_ref(["kerr", path, os.path.join(d, "rays.f64"), os.path.join(d, "k.bin")], d)
+    rec = np.dtype([("obj", "<i4"), ("hit", "<i4"), ("rec", "<f8", 16), ("col", "<f8", 3)])
+    k = np.fromfile(os.path.join(d, "k.bin"), dtype=rec)
+    return dict(obj=k["obj"].copy(), hit=k["hit"].copy(), rec=k["rec"].copy())
+
+
+def kerr_golden(d):
+    sys.path.insert(0, os.path.dirname(HERE))
+    import kerr_cases
+    out = {}
+    for name, (sc, rays) in kerr_cases.trace_cases().items():
+        dd = os.path.join(d, "k_" + name)
+        os.makedirs(dd)
+        r = ref_kerr(sc.write_reference(dd), rays, dd)
+        out[f"{name}_rays"] = rays
+        out.update({f"{name}_{k}": v for k, v in r.items()})
+    np.savez_compressed(os.path.join(HERE, "kerr_trace.npz"), **out)
+    imgs = {}
+    for name, sc in kerr_cases.render_cases().items():
+        dd = os.path.join(d, "kr_" + name)
+        os.makedirs(dd)
+        img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+        imgs[name] = img
+        print("kerr", name, info)
+    np.savez_compressed(os.path.join(HERE, "kerr_render.npz"), **imgs)
+
+
 def main():
     if not os.path.exists(REF_BIN):
-        ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+        args = [a for a in sys.argv[1:] if not a.startswith("--")]
+        ref = args[0] if args else "/root/reference"
         subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), ref], check=True)
+    if "--kerr-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            kerr_golden(d)
+        return
     with tempfile.TemporaryDirectory() as d:
+        kerr_golden(d)
         # -- QBVH structure + first hits on the subdiv-3 mesh Cornell box
         s = scenes.mesh_cornell(width=32, height=24, samples=1, supersamples=2, subdiv=3)
         p = s.write_reference(d)
