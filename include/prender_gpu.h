@@ -287,6 +287,24 @@ typedef struct pr_render_stats {
 } pr_render_stats;
 int pr_last_render_stats(pr_ctx* ctx, pr_render_stats* stats);
 
+/* ---- Differentiation ------------------------------------------------- */
+/* Adjoint of pr_render by path replay (no reference counterpart: the
+ * reference renders only).  Given dL_drgb = dLoss/d(image) for the image that
+ * pr_render produced with the same camera, parameters and sample_offset
+ * (3 floats per pixel, same row order), ADDS dLoss/d(material colour) to
+ * d_color and dLoss/d(material emission) to d_emission (3 doubles per
+ * material each, in pr_scene_desc material order; either may be NULL), and
+ * writes dLoss/d(s) for a common scale s of every emission at s = 1 to
+ * *d_emission_scale (may be NULL).  Sampling decisions are held fixed;
+ * scenes with participating media or more than 16 materials are rejected
+ * (PR_E_UNSUPPORTED).  pr_render_adjoint takes host buffers. */
+int pr_render_adjoint(pr_ctx* ctx, const pr_camera* camera, const pr_render_params* params,
+                      const float* dl_drgb, uint64_t sample_offset, double* d_color,
+                      double* d_emission, double* d_emission_scale);
+int pr_render_adjoint_dev(pr_ctx* ctx, const pr_camera* camera, const pr_render_params* params,
+                          const float* dl_drgb_dev, uint64_t sample_offset, double* d_color_dev,
+                          double* d_emission_dev);
+
 /* ---- Kerr geodesics --------------------------------------------------- */
 /* The Kerr branch of intersect_scene (scene.cpp:448-732) for n camera rays
  * (FP64, 6 per ray).  Per ray: status (0 reached background, 1 hit an

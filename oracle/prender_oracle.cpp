@@ -1581,6 +1581,7 @@ V3 kerr_background(const KerrBH& kb, const double* yy, const V3& bg) {
   double phi = y2, theta = y1;
   if (phi < 0.0) phi += 2.0 * PI;
   if (theta < 0.0) theta = -theta;
+  if (!(phi == phi) || !(theta == theta)) return V3();  // non-finite state: no texel (the reference reads out of range)
   int x = (int)(phi / (2.0 * PI) * kb.tex_w);
   x = x % kb.tex_w;
   const int y1i = (int)(theta / PI * kb.tex_h);

@@ -16,7 +16,7 @@ EXPORTS = (
     "pr_create", "pr_destroy", "pr_last_error", "pr_abi_version", "pr_abi_sizeof",
     "pr_scene_upload", "pr_qbvh_info", "pr_qbvh_export", "pr_qbvh_build_host",
     "pr_first_hit", "pr_first_hit_dev", "pr_trace_fast", "pr_render", "pr_render_dev", "pr_render_dev_noalloc", "pr_last_render_stats",
-    "pr_kerr_trace", "pr_kerr_trace_dev",
+    "pr_kerr_trace", "pr_kerr_trace_dev", "pr_render_adjoint", "pr_render_adjoint_dev",
 )
 
 _lib = None
@@ -57,5 +57,7 @@ def load():
     L.pr_last_render_stats.argtypes = [vp, C.POINTER(A.pr_render_stats)]
     L.pr_kerr_trace.argtypes = [vp, vp, i64, vp, vp, vp, vp, vp, vp]
     L.pr_kerr_trace_dev.argtypes = [vp, vp, i64, vp, vp, vp, vp, vp, vp]
+    L.pr_render_adjoint.argtypes = [vp, vp, vp, vp, C.c_uint64, vp, vp, vp]
+    L.pr_render_adjoint_dev.argtypes = [vp, vp, vp, vp, C.c_uint64, vp, vp]
     _lib = L
     return L

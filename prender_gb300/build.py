@@ -15,6 +15,9 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libprender_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# per-file flags: the Kerr tracer keeps every FP64 multiply and add rounded
+# on its own (no FMA contraction), the operation order of the reference
+EXTRA = {"kerr.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -46,10 +49,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
-        cmd = [cc] + flags + ["-c", src, "-o", obj]
+        cmd = [cc] + flags + EXTRA.get(os.path.basename(src), []) + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr[-6000:]}")
+        with open(obj + ".ptxas.txt", "w") as fh:  # registers / spills per kernel
+            fh.write(r.stderr)
         if verbose:
             print(r.stderr)
         return obj

@@ -13,6 +13,8 @@
 #include <vector>
 
 #include "../../include/prender_gpu.h"
+#include "adjoint.h"
+#include "kerr.h"
 #include "pr_internal.h"
 #include "render_kernels.h"
 #include "scene_build.h"
@@ -96,6 +98,9 @@ void pr_destroy(pr_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  for (DevBuf* b : {&c->kerr_tex, &c->k_status, &c->k_bl, &c->k_dir, &c->k_steps, &c->k_ent, &c->k_t,
+                    &c->adj_scratch, &c->adj_grad})
+    b->release();
   for (DevBuf* b : {&c->ents, &c->mats, &c->nodes, &c->tris, &c->fnorm, &c->errword, &c->counters, &c->partial,
                     &c->out, &c->rays, &c->ires, &c->jres, &c->dres, &c->wf_o, &c->wf_d, &c->wf_beta, &c->wf_dpw,
                     &c->wf_L, &c->wf_sample, &c->wf_hit, &c->wf_hitv, &c->wf_nee, &c->wf_sho, &c->wf_shd, &c->wf_extq,
@@ -125,7 +130,10 @@ int pr_scene_upload(pr_ctx* c, const pr_scene_desc* d) {
   PR_CUDA(c, upload(c->nodes, h.nodes, c->stream));
   PR_CUDA(c, upload(c->tris, h.tris, c->stream));
   PR_CUDA(c, upload(c->fnorm, h.fnorm, c->stream));
+  PR_CUDA(c, upload(c->kerr_tex, h.kerr_texture, c->stream));
   PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->kerr = h.kerr;
+  c->kerr.texture = h.kerr_texture.empty() ? nullptr : (const unsigned char*)c->kerr_tex.p;
   DevScene& S = c->dev;
   memset(&S, 0, sizeof(S));
   S.ents = (const GEntity*)c->ents.p;
@@ -295,6 +303,12 @@ int pr::prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* 
   if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
     return fail(c, PR_E_ARG, "image size out of range");
   if (p->samples <= 0 || p->supersamples <= 0) return fail(c, PR_E_ARG, "samples and supersamples must be positive");
+  if (p->nee && c->host.disk_light)
+    return fail(c, PR_E_UNSUPPORTED,
+                "an emitting disk is a light whose sampling the reference leaves undefined (Circle does not set the "
+                "UVPlane axes randomPoint reads, circle.h:110-134); render it without next-event estimation");
+  if (c->kerr.enabled && (p->nee || (p->media && c->host.medium.on)))
+    return fail(c, PR_E_UNSUPPORTED, "Kerr scenes render without next-event estimation and media");
   memset(&g, 0, sizeof(g));
   double dir[3] = {cam->dir[0], cam->dir[1], cam->dir[2]};
   double phi = std::atan2(dir[1], dir[0]);
@@ -440,7 +454,12 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   L.trace_blocks = std::min<unsigned int>((P + 127) / 128, 152u * 64u);
   PR_CUDA(c, cudaMemsetAsync(c->wf_nee.p, 0, f4 * 3 * P, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->wf_pix.p, 0, 24ull * wh, c->stream));
-  if (!c->wf_graph_failed && (!c->wf_graph || c->wf_graph_slots != P)) {
+  // PR_WF_HOST_LOOP=1 drives the iterations from the host instead of the
+  // graph's device-side while loop: profilers that cannot see kernels inside
+  // conditional graph nodes see every launch this way (same kernels, same work)
+  const char* host_loop = getenv("PR_WF_HOST_LOOP");
+  const bool use_graph = !(host_loop && host_loop[0] == '1');
+  if (use_graph && !c->wf_graph_failed && (!c->wf_graph || c->wf_graph_slots != P)) {
     if (c->wf_graph) cudaGraphExecDestroy(c->wf_graph);
     c->wf_graph = nullptr;
     cudaError_t e = wf_build_graph(L, c->stream, &c->wf_graph);
@@ -461,7 +480,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
     PR_CUDA(c, cudaMemsetAsync(c->wf_samp.p, 0, 24ull * B.pass_samples, c->stream));
     PR_CUDA(c, wf_set_constants(c->dev, g, B, c->stream));
     PR_CUDA(c, wf_reset_launch(P, c->stream));
-    if (c->wf_graph) PR_CUDA(c, cudaGraphLaunch(c->wf_graph, c->stream));
+    if (use_graph && c->wf_graph) PR_CUDA(c, cudaGraphLaunch(c->wf_graph, c->stream));
     else PR_CUDA(c, wf_run_host_loop(L, c->wf_host_ctl, (const WfCtl*)c->wf_ctl.p, c->stream));
   }
   PR_CUDA(c, wf_resolve_launch(rgb_dev, (int)(3 * wh), accumulate, g.sensor, c->stream));
@@ -482,7 +501,14 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-  if (p->mode == PR_MODE_WAVEFRONT) {
+  const bool kerr = c->kerr.enabled != 0;
+  if (kerr) {
+    // every scene query of a Kerr scene is a geodesic trace: one form only
+    PR_CUDA(c, c->partial.ensure(sizeof(float) * n3 * (size_t)g.chunks));
+    PR_CUDA(c, launch_kerr_render(c->dev, c->kerr, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
+                                  (unsigned long long*)c->counters.p, c->stream));
+    PR_CUDA(c, launch_reduce((const float*)c->partial.p, rgb_dev, (int)n3, g.chunks, accumulate, c->stream));
+  } else if (p->mode == PR_MODE_WAVEFRONT) {
     st = render_wavefront(c, g, rgb_dev, accumulate);
     if (st != PR_OK) return st;
   } else {
@@ -497,7 +523,7 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   st = check_device_errors(c);
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-  const bool wf = p->mode == PR_MODE_WAVEFRONT;
+  const bool wf = p->mode == PR_MODE_WAVEFRONT && !kerr;
   const uint64_t paths = wf ? (uint64_t)g.spp * g.width * g.height : cnt[0];
   // wavefront: reset per pass + 4 per iteration + resolve; megakernel: kernel + reduce
   const uint64_t launches = wf ? 4 * cnt[5] + c->wf_passes + 1 : 2;
@@ -522,17 +548,144 @@ int pr_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, float*
   return PR_OK;
 }
 
+static int adjoint_checks(pr_ctx* c, const pr_render_params* p) {
+  if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  if (c->kerr.enabled) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass traces straight rays only");
+  if (p && p->media && c->host.medium.on) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover media");
+  if ((int)c->host.mats.size() > kAdjMaterials)
+    return fail(c, PR_E_UNSUPPORTED, "the adjoint pass tracks at most " + std::to_string(kAdjMaterials) + " materials");
+  return PR_OK;
+}
+
+int pr_render_adjoint_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, const float* dl_drgb,
+                          uint64_t sample_offset, double* d_color, double* d_emission) {
+  if (!c) return PR_E_ARG;
+  int st = adjoint_checks(c, p);
+  if (st != PR_OK) return st;
+  if (!dl_drgb) return fail(c, PR_E_ARG, "null dL/d(image)");
+  RenderCfg g;
+  st = prepare_render(c, cam, p, sample_offset, g);
+  if (st != PR_OK) return st;
+  PR_CUDA(c, cudaSetDevice(c->device));
+  const int n_mat = (int)c->host.mats.size();
+  // scratch for outputs the caller does not want
+  PR_CUDA(c, c->adj_scratch.ensure(2 * 3 * sizeof(double) * (size_t)std::max(n_mat, 1)));
+  double* dc = d_color ? d_color : (double*)c->adj_scratch.p;
+  double* de = d_emission ? d_emission : (double*)c->adj_scratch.p + 3 * std::max(n_mat, 1);
+  if (!d_color) PR_CUDA(c, cudaMemsetAsync(dc, 0, 3 * sizeof(double) * n_mat, c->stream));
+  if (!d_emission) PR_CUDA(c, cudaMemsetAsync(de, 0, 3 * sizeof(double) * n_mat, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  PR_CUDA(c, launch_adjoint(c->dev, g, dl_drgb, n_mat, dc, de, (uint32_t*)c->errword.p,
+                            (unsigned long long*)c->counters.p, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  unsigned long long cnt[8];
+  PR_CUDA(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  st = check_device_errors(c);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->stats = pr_render_stats{cnt[0], cnt[1], cnt[2], cnt[3], ms, 1};
+  return st;
+}
+
+int pr_render_adjoint(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, const float* dl_drgb,
+                      uint64_t sample_offset, double* d_color, double* d_emission, double* d_emission_scale) {
+  if (!c) return PR_E_ARG;
+  int st = adjoint_checks(c, p);
+  if (st != PR_OK) return st;
+  if (!cam || !dl_drgb) return fail(c, PR_E_ARG, "null camera or dL/d(image)");
+  if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
+    return fail(c, PR_E_ARG, "image size out of range");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  const size_t bytes = sizeof(float) * 3 * (size_t)cam->width * cam->height;
+  const int n_mat = (int)c->host.mats.size();
+  const size_t gb = 3 * sizeof(double) * (size_t)std::max(n_mat, 1);
+  PR_CUDA(c, c->out.ensure(bytes));
+  PR_CUDA(c, c->adj_grad.ensure(2 * gb));
+  PR_CUDA(c, cudaMemcpyAsync(c->out.p, dl_drgb, bytes, cudaMemcpyHostToDevice, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->adj_grad.p, 0, 2 * gb, c->stream));
+  double* dc = (double*)c->adj_grad.p;
+  double* de = dc + 3 * std::max(n_mat, 1);
+  st = pr_render_adjoint_dev(c, cam, p, (const float*)c->out.p, sample_offset, dc, de);
+  if (st != PR_OK) return st;
+  std::vector<double> h(6 * (size_t)std::max(n_mat, 1));
+  PR_CUDA(c, cudaMemcpyAsync(h.data(), c->adj_grad.p, 2 * gb, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  const double* hc = h.data();
+  const double* he = h.data() + 3 * std::max(n_mat, 1);
+  double scale = 0.0;
+  for (int m = 0; m < n_mat; m++)
+    for (int k = 0; k < 3; k++) {
+      if (d_color) d_color[3 * m + k] += hc[3 * m + k];
+      if (d_emission) d_emission[3 * m + k] += he[3 * m + k];
+      scale += he[3 * m + k] * c->host.mats[m].emission_d[k];
+    }
+  if (d_emission_scale) *d_emission_scale = scale;
+  return PR_OK;
+}
+
 int pr_last_render_stats(pr_ctx* c, pr_render_stats* s) {
   if (!c || !s) return PR_E_ARG;
   *s = c->stats;
   return PR_OK;
 }
 
-int pr_kerr_trace(pr_ctx* c, const double*, int64_t, int32_t*, double*, double*, int32_t*, int32_t*, double*) {
-  return fail(c, PR_E_UNSUPPORTED, "Kerr tracer not built yet");
+int pr_kerr_trace_dev(pr_ctx* c, const double* rays, int64_t n, int32_t* status, double* final_bl, double* exit_dir,
+                      int32_t* steps, int32_t* hit_entity, double* hit_t) {
+  if (!c) return PR_E_ARG;
+  if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  if (!c->kerr.enabled) return fail(c, PR_E_SCENE, "the scene has no black hole");
+  if (n < 0 || (n > 0 && !rays)) return fail(c, PR_E_ARG, "bad ray buffer");
+  if (n > (int64_t)1 << 31) return fail(c, PR_E_ARG, "at most 2^31 rays per call");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  KerrOut o{status, final_bl, exit_dir, steps, hit_entity, hit_t};
+  PR_CUDA(c, launch_kerr_trace(c->dev, c->kerr, rays, n, o, (uint32_t*)c->errword.p,
+                               (unsigned long long*)c->counters.p, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  unsigned long long cnt[8];
+  PR_CUDA(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  int st = check_device_errors(c);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  // paths = rays, segments = segment scene tests, nodes_visited = accepted
+  // steps, tri_tests = RK45 attempts (5 geodesic evaluations each)
+  c->stats = pr_render_stats{cnt[0], cnt[3], cnt[1], cnt[2], ms, n > 0 ? 1ull : 0ull};
+  return st;
 }
-int pr_kerr_trace_dev(pr_ctx* c, const double*, int64_t, int32_t*, double*, double*, int32_t*, int32_t*, double*) {
-  return fail(c, PR_E_UNSUPPORTED, "Kerr tracer not built yet");
+
+int pr_kerr_trace(pr_ctx* c, const double* rays, int64_t n, int32_t* status, double* final_bl, double* exit_dir,
+                  int32_t* steps, int32_t* hit_entity, double* hit_t) {
+  if (!c) return PR_E_ARG;
+  if (n < 0 || (n > 0 && !rays)) return fail(c, PR_E_ARG, "bad ray buffer");
+  if (n > (int64_t)1 << 31) return fail(c, PR_E_ARG, "at most 2^31 rays per call");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  const size_t un = (size_t)std::max<int64_t>(n, 1);
+  PR_CUDA(c, c->rays.ensure(48 * un));
+  PR_CUDA(c, c->k_status.ensure(4 * un));
+  PR_CUDA(c, c->k_bl.ensure(24 * un));
+  PR_CUDA(c, c->k_dir.ensure(24 * un));
+  PR_CUDA(c, c->k_steps.ensure(4 * un));
+  PR_CUDA(c, c->k_ent.ensure(4 * un));
+  PR_CUDA(c, c->k_t.ensure(8 * un));
+  if (n > 0) PR_CUDA(c, cudaMemcpyAsync(c->rays.p, rays, 48 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  int st = pr_kerr_trace_dev(c, (const double*)c->rays.p, n, status ? (int32_t*)c->k_status.p : nullptr,
+                             final_bl ? (double*)c->k_bl.p : nullptr, exit_dir ? (double*)c->k_dir.p : nullptr,
+                             steps ? (int32_t*)c->k_steps.p : nullptr, hit_entity ? (int32_t*)c->k_ent.p : nullptr,
+                             hit_t ? (double*)c->k_t.p : nullptr);
+  if (st != PR_OK || n == 0) return st;
+  const size_t sn = (size_t)n;
+  if (status) PR_CUDA(c, cudaMemcpyAsync(status, c->k_status.p, 4 * sn, cudaMemcpyDeviceToHost, c->stream));
+  if (final_bl) PR_CUDA(c, cudaMemcpyAsync(final_bl, c->k_bl.p, 24 * sn, cudaMemcpyDeviceToHost, c->stream));
+  if (exit_dir) PR_CUDA(c, cudaMemcpyAsync(exit_dir, c->k_dir.p, 24 * sn, cudaMemcpyDeviceToHost, c->stream));
+  if (steps) PR_CUDA(c, cudaMemcpyAsync(steps, c->k_steps.p, 4 * sn, cudaMemcpyDeviceToHost, c->stream));
+  if (hit_entity) PR_CUDA(c, cudaMemcpyAsync(hit_entity, c->k_ent.p, 4 * sn, cudaMemcpyDeviceToHost, c->stream));
+  if (hit_t) PR_CUDA(c, cudaMemcpyAsync(hit_t, c->k_t.p, 8 * sn, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PR_OK;
 }
 
 size_t pr_abi_sizeof(int which) {

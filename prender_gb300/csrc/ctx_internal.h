@@ -41,9 +41,12 @@ struct pr_ctx {
   pr::HostScene host;
   bool scene_ready = false;
   pr::DevScene dev{};
-  pr::DevBuf ents, mats, nodes, tris, fnorm;
+  pr::DevBuf ents, mats, nodes, tris, fnorm, kerr_tex;
+  pr::GKerr kerr{};  // device copy of the black hole (texture pointer on the device)
   pr::DevBuf errword, counters;  // 4 bytes / 4 x u64
   pr::DevBuf partial, out, rays, ires, jres, dres;
+  pr::DevBuf k_status, k_bl, k_dir, k_steps, k_ent, k_t;  // pr_kerr_trace staging
+  pr::DevBuf adj_scratch, adj_grad;                         // adjoint outputs
   pr_render_stats stats{};
   // wavefront pool
   pr::DevBuf wf_o, wf_d, wf_beta, wf_dpw, wf_L, wf_sample, wf_hit, wf_hitv, wf_nee, wf_sho, wf_shd, wf_extq, wf_shq;

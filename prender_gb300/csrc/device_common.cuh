@@ -145,6 +145,23 @@ __device__ __forceinline__ bool exact_uvplane(const GEntity& e, dv3 o, dv3 d, do
   return true;
 }
 
+// Circle::intersect (circle.h:177-200): the base UVPlane's plane test with
+// no extent (its normal never inverted), then the annulus r_in <= |p - o| <= r
+__device__ __forceinline__ bool exact_circle(const GEntity& e, dv3 o, dv3 d, double& t) {
+  const dv3 n2 = ldd3(e.normal);
+  const double dd = ddot(d, n2);
+  if (fabs(dd) < 1.0e-14) return false;
+  const double tt = __ddiv_rn(ddot(dsub3(ldd3(e.p), o), n2), dd);
+  const dv3 pos = {da(dm(d.x, tt), o.x), da(dm(d.y, tt), o.y), da(dm(d.z, tt), o.z)};
+  if (tt < kEps) return false;
+  const dv3 rel = dsub3(pos, ldd3(e.p));
+  const double r2 = ddot(rel, rel);
+  if (r2 > dm(e.radius, e.radius)) return false;
+  if (r2 < dm(e.radius_inner, e.radius_inner)) return false;
+  t = tt;
+  return true;
+}
+
 // Triangle::CheckIntersection2 + Triangle::intersect's t > PS_EPS (polygon.h:78-173)
 __device__ __forceinline__ bool exact_triangle(float4 a, float4 b, float4 c, dv3 o, dv3 d, double& t) {
   const dv3 v0 = {a.x, a.y, a.z};
@@ -330,6 +347,8 @@ __device__ inline bool exact_closest(const DevScene& S, dv3 org, dv3 dir, double
       got = exact_sphere(e, o2, dir, t);
     } else if (e.type == PR_ENT_UVPLANE) {
       got = exact_uvplane(e, o2, dir, t);
+    } else if (e.type == PR_ENT_CIRCLE) {
+      got = exact_circle(e, o2, dir, t);
     } else if (e.type == PR_ENT_POLYGON) {
       if (!ray_ready) {
         r = make_exact_ray(o2, dir);

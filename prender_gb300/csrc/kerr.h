@@ -1,0 +1,31 @@
+// Launch interface of the Kerr geodesic tracer (kerr.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "pr_internal.h"
+#include "render_kernels.h"
+
+namespace pr {
+
+// per-ray results of pr_kerr_trace (device buffers; any may be null)
+struct KerrOut {
+  int32_t* status;
+  double* final_bl;  // 3 per ray
+  double* exit_dir;  // 3 per ray
+  int32_t* steps;
+  int32_t* hit_entity;
+  double* hit_t;
+};
+
+// counters[0] rays, [1] accepted steps, [2] RK45 attempts, [3] segment tests
+cudaError_t launch_kerr_trace(const DevScene& S, const GKerr& K, const double* rays, int64_t n, KerrOut out,
+                              uint32_t* err, unsigned long long* counters, cudaStream_t stream);
+
+// the renderer with every scene query traced along a geodesic; same output
+// layout as launch_megakernel (per-chunk partial images)
+cudaError_t launch_kerr_render(const DevScene& S, const GKerr& K, const RenderCfg& cfg, float* partial, uint32_t* err,
+                               unsigned long long* counters, cudaStream_t stream);
+
+}  // namespace pr

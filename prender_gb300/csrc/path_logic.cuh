@@ -36,6 +36,18 @@ struct ShadowReq {
   float3 o, d;
   float tmax;
   float3 contrib;  // added to L if nothing is hit before tmax
+  float3 ew;       // contrib / emission of the light's material (adjoint)
+  int lmat;        // the light's material
+};
+
+// d L / d emission: shade() reports every term it adds to L as
+// weight * emission(material m) here (adjoint renders only; null otherwise)
+struct EmissionTap {
+  float3* g;  // one entry per material
+  int n;
+  __device__ __forceinline__ void em(int m, float3 w) {
+    if (m >= 0 && m < n) g[m] += w;
+  }
 };
 
 enum { SHADE_END = 0, SHADE_CONTINUE = 1, SHADE_SPLIT = 2 };
@@ -86,7 +98,7 @@ __device__ __forceinline__ void make_vertex(const DevScene& S, float3 o, float3 
     const double il = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);
     v.p = f3((float)px, (float)py, (float)pz);
     v.n = f3((float)(nx * il), (float)(ny * il), (float)(nz * il));
-  } else if (e.type == PR_ENT_UVPLANE) {
+  } else if (e.type == PR_ENT_UVPLANE || e.type == PR_ENT_CIRCLE) {
     v.p = o + d * h.t;
     v.n = f3(e.n[0], e.n[1], e.n[2]);
   } else {
@@ -196,22 +208,27 @@ __device__ __forceinline__ void root_path(PathState& ps, float3 o, float3 d) {
   ps.dp = 0;
 }
 
-// Shades the vertex found by the last closest-hit query of ps.
+// Shades the vertex found by the last closest-hit query of ps.  A tracer
+// that builds the vertex itself (the Kerr geodesic tracer) passes it as pre,
+// and the colour a miss returns as miss (radiance.h:30-43); straight-ray
+// callers leave both null.
 __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& ps, bool hit, const FastHit& h,
-                     uint64_t sample_id, ShadowReq* sh, int& nsh, PathState& child, uint32_t* err) {
+                     uint64_t sample_id, ShadowReq* sh, int& nsh, PathState& child, uint32_t* err,
+                     const Vertex* pre = nullptr, const float3* miss = nullptr, EmissionTap* tap = nullptr) {
   nsh = 0;
   const bool nee = cfg.nee != 0;
   const bool media = cfg.media != 0 && S.medium.on != 0;
   if (ps.dp) {  // light hit along a specular / refraction direction (directLight_radiance.h:516-556)
     if (hit && S.entf[h.ent].is_light) {
       float3 em = ld3(S.mats[S.entf[h.ent].material].emission);
-      if (media) em = em * medium_tr(S.medium, h.t);
-      ps.L += ps.dpw * em;
+      const float3 tr = media ? medium_tr(S.medium, h.t) : f3(1, 1, 1);
+      ps.L += ps.dpw * (em * tr);
+      if (tap) tap->em(S.entf[h.ent].material, ps.dpw * tr);
     }
     ps.dp = 0;
   }
   if (!hit) {
-    ps.L += ps.beta * f3(S.bg[0], S.bg[1], S.bg[2]);
+    ps.L += ps.beta * (miss ? *miss : f3(S.bg[0], S.bg[1], S.bg[2]));
     return SHADE_END;
   }
   if (ps.depth >= cfg.max_vertices) {
@@ -221,7 +238,8 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   Rng rng;
   rng_at(rng, cfg.seed, sample_id, ps.branch, ps.draws);
   Vertex v;
-  make_vertex(S, ps.o, ps.d, h, v);
+  if (pre) v = *pre;
+  else make_vertex(S, ps.o, ps.d, h, v);
   const GMaterial& m = S.mats[v.mat];
   const GEntF& ent = S.entf[v.ent];
   const float3 E = ld3(m.emission), C = ld3(m.color);
@@ -234,6 +252,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   if (ps.depth > cfg.depth) {
     if (rng.next() >= p_rr) {
       ps.L += ps.beta * trr * E;
+      if (tap) tap->em(v.mat, ps.beta * trr);
       ps.draws = rng_draws(rng);
       return SHADE_END;
     }
@@ -283,7 +302,9 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
             sh[nsh].o = npos;
             sh[nsh].d = ldir;
             sh[nsh].tmax = dist - 1.0e-3f;
-            sh[nsh].contrib = ps.beta * f * em * medium_tr(md, dist) * (0.31830988618379067154f * G * le.area * (1.0f / 3.0f));
+            sh[nsh].ew = ps.beta * f * medium_tr(md, dist) * (0.31830988618379067154f * G * le.area * (1.0f / 3.0f));
+            sh[nsh].contrib = sh[nsh].ew * em;
+            sh[nsh].lmat = le.material;
             nsh++;
           }
         }
@@ -291,7 +312,10 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
       ps.draws = rng_draws(rng);
       if (!(pdf > 0.0f)) { nsh = 0; return SHADE_END; }
       if (ent.is_light) {
-        if (ps.depth == 0) ps.L += ps.beta * tr * E;
+        if (ps.depth == 0) {
+          ps.L += ps.beta * tr * E;
+          if (tap) tap->em(v.mat, ps.beta * tr);
+        }
         return SHADE_END;
       }
       ps.beta = ps.beta * f;
@@ -311,8 +335,10 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   if (kind == 0) {
     // ---- BRDF_Diffuse (brdf.h:408-700)
     if (ent.is_light) {
-      if (!(ent.type == PR_ENT_UVPLANE && dot(v.n, d) >= 0.0f) && (!nee || ps.depth == 0))
+      if (!(ent.type == PR_ENT_UVPLANE && dot(v.n, d) >= 0.0f) && (!nee || ps.depth == 0)) {
         ps.L += ps.beta * trr * E * inv_rr;
+        if (tap) tap->em(v.mat, ps.beta * trr * inv_rr);
+      }
       ps.draws = rng_draws(rng);
       return SHADE_END;
     }
@@ -349,7 +375,10 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
             sh[nsh].o = origin;
             sh[nsh].d = dlo / disto;
             sh[nsh].tmax = disto - 1.0e-3f;
-            sh[nsh].contrib = w * em * (dot0 * dot1 / dist2 * le.area);
+            const float3 ew = w * (dot0 * dot1 / dist2 * le.area);
+            sh[nsh].contrib = ew * em;
+            sh[nsh].ew = media ? ew * medium_tr(S.medium, dist) : ew;
+            sh[nsh].lmat = le.material;
             nsh++;
           }
         }
@@ -358,6 +387,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
       }
     }
     ps.L += ps.beta * (env + tri * E);
+    if (tap) tap->em(v.mat, ps.beta * tri);
     ps.beta = ps.beta * C * tri * inv_rr;
     ps.o = origin;
     ps.d = nd;
@@ -369,6 +399,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     // ---- BRDF_Specular (brdf.h:702-761): mirror about the geometric normal
     const float3 nd = normalize(d - v.n * (2.0f * dot(v.n, d)));
     ps.L += ps.beta * (env + tri * E);
+    if (tap) tap->em(v.mat, ps.beta * tri);
     ps.beta = ps.beta * C * tri * inv_rr;
     ps.dp = nee;
     ps.dpw = ps.beta;
@@ -386,6 +417,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   const float ddn = dot(d, on);
   const float cos2t = 1.0f - nnt * nnt * (1.0f - ddn * ddn);
   ps.L += ps.beta * (env + tri * E);
+  if (tap) tap->em(v.mat, ps.beta * tri);
   const float3 base = ps.beta * C * tri;
   const float3 refl_o = offset_ray(v.p, dot(refl, v.n) > 0.0f ? v.n : -v.n);
   if (cos2t < 0.0f) {  // total internal reflection

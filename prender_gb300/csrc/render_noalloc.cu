@@ -63,6 +63,7 @@ extern "C" int pr_render_dev_noalloc(pr_ctx* c, const pr_camera* cam, const pr_r
   if (!rgb_dev) return ctx_fail(c, PR_E_ARG, "null output");
   if (!p || p->mode != PR_MODE_MEGAKERNEL)
     return ctx_fail(c, PR_E_UNSUPPORTED, "pr_render_dev_noalloc renders the megakernel form only");
+  if (c->kerr.enabled) return ctx_fail(c, PR_E_UNSUPPORTED, "pr_render_dev_noalloc renders straight-ray scenes only");
   RenderCfg g;
   int st = prepare_render(c, cam, p, sample_offset, g);
   if (st != PR_OK) return st;

@@ -165,6 +165,22 @@ __device__ __forceinline__ bool fast_uvplane(const GEntF& e, float3 o, float3 d,
   return true;
 }
 
+// Circle::intersect in FP32 (circle.h:177-200): plane test, then the annulus
+// (u_length = radius, v_length = inner radius)
+__device__ __forceinline__ bool fast_circle(const GEntF& e, float3 o, float3 d, float tmax, float& t) {
+  const float3 n = f3(e.n[0], e.n[1], e.n[2]);
+  const float dd = dot(d, n);
+  if (fabsf(dd) < 1.0e-14f) return false;
+  const float3 org = f3(e.p[0], e.p[1], e.p[2]);
+  const float tt = dot(org - o, n) / dd;
+  if (!(tt > 0.0f) || !(tt < tmax)) return false;
+  const float3 rel = (o + d * tt) - org;
+  const float r2 = dot(rel, rel);
+  if (r2 > e.u_length * e.u_length || r2 < e.v_length * e.v_length) return false;
+  t = tt;
+  return true;
+}
+
 __device__ __forceinline__ float3 safe_inv(float3 d) {
   const float big = 1.0e30f;
   return f3(d.x != 0.0f ? 1.0f / d.x : copysignf(big, d.x), d.y != 0.0f ? 1.0f / d.y : copysignf(big, d.y),
@@ -186,6 +202,7 @@ __device__ __forceinline__ bool fast_closest(const DevScene& S, float3 o, float3
     bool got = false;
     if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], o, d, h.t, t);
     else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, o, d, h.t, t);
+    else if (e.type == PR_ENT_CIRCLE) got = fast_circle(e, o, d, h.t, t);
     else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<false>(S, e, o, d, inv, t, slot, bu, bv, st, err);
     if (got && t < h.t) {
       h.t = t;
@@ -209,6 +226,7 @@ __device__ __forceinline__ bool fast_occluded(const DevScene& S, float3 o, float
     bool got = false;
     if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], o, d, tmax, t);
     else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, o, d, tmax, t);
+    else if (e.type == PR_ENT_CIRCLE) got = fast_circle(e, o, d, tmax, t);
     else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<true>(S, e, o, d, inv, t, slot, bu, bv, st, err);
     if (got) return true;
   }

@@ -102,6 +102,39 @@ class Context:
         self._check(self.L.pr_trace_fast(self.h, _p(rays), n, _p(ent), _p(prim), _p(t)))
         return dict(entity=ent, prim=prim, t=t)
 
+    def render_adjoint(self, dl_drgb: np.ndarray, scene=None, settings=None, camera=None,
+                       sample_offset: int = 0) -> dict:
+        """Path-replay adjoint of render(): dLoss/d(material colour) and
+        dLoss/d(material emission), (n_materials, 3) each, and dLoss/d(scale)
+        of all emission, for dl_drgb = dLoss/d(image) of the image render()
+        returned with the same scene, settings, camera and sample_offset."""
+        scene = scene or self.scene
+        cam = (camera or scene.camera).to_c()
+        prm = (settings or scene.settings).to_c()
+        g = np.ascontiguousarray(dl_drgb, dtype=np.float32)
+        if g.shape != (cam.height, cam.width, 3):
+            raise ValueError("dl_drgb must have the image's shape (H, W, 3)")
+        n = len(scene.materials)
+        d_color = np.zeros((n, 3))
+        d_em = np.zeros((n, 3))
+        d_scale = C.c_double(0.0)
+        self._check(self.L.pr_render_adjoint(self.h, C.byref(cam), C.byref(prm), _p(g), sample_offset,
+                                             _p(d_color), _p(d_em), C.byref(d_scale)))
+        return dict(color=d_color, emission=d_em, emission_scale=d_scale.value)
+
+    def kerr_trace(self, rays: np.ndarray) -> dict:
+        """The Kerr branch of intersect_scene per ray (FP64 geodesics);
+        status 0 background, 1 entity hit, 2 event horizon, 4 step underflow,
+        5 entity ahead of the last step."""
+        rays = np.ascontiguousarray(rays, dtype=np.float64)
+        n = rays.shape[0]
+        out = dict(status=np.empty(n, np.int32), final_bl=np.empty((n, 3)), exit_dir=np.empty((n, 3)),
+                   steps=np.empty(n, np.int32), hit_entity=np.empty(n, np.int32), hit_t=np.empty(n))
+        self._check(self.L.pr_kerr_trace(self.h, _p(rays), n, _p(out["status"]), _p(out["final_bl"]),
+                                         _p(out["exit_dir"]), _p(out["steps"]), _p(out["hit_entity"]),
+                                         _p(out["hit_t"])))
+        return out
+
     def render(self, scene=None, settings=None, camera=None, sample_offset: int = 0,
                accumulate: np.ndarray | None = None) -> np.ndarray:
         """Render::Run: returns the (H, W, 3) float32 image in the reference's

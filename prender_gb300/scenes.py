@@ -145,6 +145,37 @@ def mesh_cornell(width: int = 1024, height: int = 768, samples: int = 16, supers
     return s
 
 
+def diff_cornell(width: int = 512, height: int = 512, samples: int = 16, supersamples: int = 2, subdiv: int = 5,
+                 albedo=None, emission_scale: float = 1.0, depth: int = 5, seed: int = 0) -> Scene:
+    """Cornell box for differentiable rendering: eight Lambertian materials
+    (five walls as uv-planes, a displaced icosphere and two boxes) with RGB
+    albedo drawn U(0.1, 0.9) from the seed (or given as an (8, 3) array), and
+    the ceiling light whose emission is scaled by emission_scale.  NEE on;
+    16 x 2^2 tent-filtered samples = 64 spp."""
+    rng = np.random.default_rng(seed)
+    alb = rng.uniform(0.1, 0.9, (8, 3)) if albedo is None else np.asarray(albedo, dtype=np.float64)
+    s = Scene()
+    X0, X1, Y1, Z0, Z1 = 1.0, 99.0, 81.6, 0.0, 250.0
+    # walls facing into the box (normal = normalize(U x V))
+    s.add_uvplane((X0, 0.0, Z0), (0.0, 0.0, Z1), (X1 - X0, 0.0, 0.0), Material.diffuse(alb[0]))   # floor, +y
+    s.add_uvplane((X0, Y1, Z0), (X1 - X0, 0.0, 0.0), (0.0, 0.0, Z1), Material.diffuse(alb[1]))    # ceiling, -y
+    s.add_uvplane((X0, 0.0, Z0), (X1 - X0, 0.0, 0.0), (0.0, Y1, 0.0), Material.diffuse(alb[2]))   # back, +z
+    s.add_uvplane((X0, 0.0, Z0), (0.0, Y1, 0.0), (0.0, 0.0, Z1), Material.diffuse(alb[3]))        # left, +x
+    s.add_uvplane((X1, 0.0, Z0), (0.0, 0.0, Z1), (0.0, Y1, 0.0), Material.diffuse(alb[4]))        # right, -x
+    iv, jf = displaced_icosphere(subdiv, (50, 20, 70), 16.0, amp=0.05, seed=seed)
+    s.add_mesh(iv, jf, Material.diffuse(alb[5]))
+    bv, bf = box_mesh((14, 0, 30), (34, 30, 50))
+    s.add_mesh(bv, bf, Material.diffuse(alb[6]))
+    bv, bf = box_mesh((66, 0, 95), (86, 18, 115))
+    s.add_mesh(bv, bf, Material.diffuse(alb[7]))
+    e = 36.0 * float(emission_scale)
+    s.add_uvplane((47.5, 81.5, 78.5), (5, 0, 0), (0, 0, 5), Material.diffuse((0, 0, 0), (e, e, e)))
+    s.camera = Camera(position=(50, 52, 220), dir=(0, -0.04, -1), angle=30, width=width, height=height)
+    s.settings = RenderSettings(samples=samples, supersamples=supersamples, tent_filter=1, depth=depth,
+                                nee=1, seed=seed)
+    return s
+
+
 def media_cornell(width: int = 128, height: int = 96, samples: int = 4, supersamples: int = 2,
                   sigma_s: float = 0.05, sigma_a: float = 0.01, g: float = 0.3, subdiv: int = 3,
                   depth: int = 5, seed: int = 0) -> Scene:
@@ -194,6 +225,25 @@ def kerr_disk(width: int = 256, height: int = 192, a: float = 0.9, max_steps: in
     s.camera = Camera(position=(0.0, round(-30.0 * c, 10), round(30.0 * sn, 10)), dir=(0.0, c, -sn), up=(0.0, 0.0, 1.0),
                       width=width, height=height, angle=40.0)
     s.settings = RenderSettings(samples=samples, supersamples=supersamples, depth=1, depth_limit=1, nee=0)
+    return s
+
+
+def kerr_lensing(a: float = 0.999, width: int = 2048, height: int = 1024, max_steps: int = 4000,
+                 fov: float = 60.0, texture=None, escape_radius: float = 0.0, r_cam: float = 6.03) -> Scene:
+    """Kerr lensing view: camera at Boyer-Lindquist r = 6.03 M in the
+    equatorial plane (theta = pi/2) looking at the hole, a thin emitting
+    accretion disk r 3..15 M in that plane, and a procedural celestial
+    sphere as the background map (seeded checker + 10k point stars)."""
+    s = Scene()
+    s.add_disk((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 15.0,
+               Material.diffuse((0.0, 0.0, 0.0), emission=(1.6, 0.9, 0.4)), radius_inner=3.0)
+    if texture is None:
+        texture = celestial_texture(1024, 512, stars=10000, seed=0)
+    s.set_black_hole((0.0, 0.0, 0.0), a, max_steps=max_steps, escape_radius=escape_radius, texture=texture)
+    y = round(-math.sqrt(r_cam * r_cam + a * a), 12)  # BL (r, pi/2, 3 pi/2) in Cartesian
+    s.camera = Camera(position=(0.0, y, 0.0), dir=(0.0, 1.0, 0.0), up=(0.0, 0.0, 1.0), width=width, height=height,
+                      angle=fov)
+    s.settings = RenderSettings(samples=1, supersamples=1, depth=1, depth_limit=1, nee=0)
     return s
 
 

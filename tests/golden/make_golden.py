@@ -96,6 +96,13 @@ def kerr_golden(d):
         img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
         imgs[name] = img
         print("kerr", name, info)
+    sc = kerr_cases.highspp_case()
+    dd = os.path.join(d, "kr_highspp")
+    os.makedirs(dd)
+    img, info = ref_render(sc.write_reference(dd, threads=os.cpu_count()), (sc.camera.width, sc.camera.height), dd,
+                           threads=os.cpu_count())
+    imgs["texture_highspp"] = img.astype(np.float32)
+    print("kerr texture_highspp", info)
     np.savez_compressed(os.path.join(HERE, "kerr_render.npz"), **imgs)
 
 

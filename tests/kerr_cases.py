@@ -53,3 +53,12 @@ def status_from_reference(obj, hit, rec):
     st[end & (obj >= 0)] = 5
     st[end & (obj < 0)] = 0
     return st
+
+
+def highspp_case():
+    """The textured Kerr render at 256 spp for statistical image parity."""
+    tex = scenes.celestial_texture(64, 32, stars=200, seed=3)
+    s = scenes.kerr_disk(32, 24, a=0.9, max_steps=300, samples=64, supersamples=2, texture=tex)
+    s.kerr["map_coef"] = (1.0, 0.3, 1.0, -0.7)
+    s.kerr["texture_coef"] = 1.5
+    return s

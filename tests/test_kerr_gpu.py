@@ -1,0 +1,140 @@
+"""Kerr geodesic tracer on the GPU (pr_kerr_trace and Kerr renders), through
+the C ABI, against the reference's own outputs (golden vectors) and the FP64
+oracle.
+
+The kernel runs the reference's FP64 arithmetic in the reference's order
+(no FMA contraction); the GPU's sin / cos / acos / atan2 / pow may differ
+from the host libm in the last bit, so a ray whose step control sits on a
+knife edge may take another step sequence.  Bars: status equal on >= 99.5%
+of rays, exit direction within 1e-6 rad on >= 99% of rays (and every ray
+whose status agrees within 1e-3 rad), hit entities equal where both hit.
+"""
+import numpy as np
+import pytest
+
+import kerr_cases
+from oracle import oracle as O
+from prender_gb300 import _abi as A
+from prender_gb300 import gpu, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import __graft_entry__ as g
+    g.build_library()
+    c = gpu.Context(0)
+    yield c
+    c.close()
+
+
+def _angle(a, b):
+    a = a / np.linalg.norm(a, axis=1, keepdims=True)
+    b = b / np.linalg.norm(b, axis=1, keepdims=True)
+    c = np.clip((a * b).sum(1), -1.0, 1.0)
+    # small angles: |a x b| is better conditioned than acos
+    return np.arctan2(np.linalg.norm(np.cross(a, b), axis=1), c)
+
+
+def _compare(k, st_ref, dir_ref, ent_ref, label):
+    same = k["status"] == st_ref
+    # a ray that starts inside the horizon never enters the step loop: the
+    # reference records no direction for it
+    valid = np.linalg.norm(dir_ref, axis=1) > 0
+    assert np.array_equal(valid, np.linalg.norm(k["exit_dir"], axis=1) > 0) or not valid.all()
+    ang = np.zeros(len(st_ref))
+    ang[valid] = _angle(k["exit_dir"][valid], dir_ref[valid])
+    # exit directions of rays that leave (background) or end on an entity;
+    # a ray that stalls at the horizon (step underflow) or crosses it has no
+    # exit direction, only its status
+    out = np.isin(st_ref, (0, 1, 5)) & valid
+    frac_dir = float((ang[out] <= 1e-6).mean()) if out.any() else 1.0
+    worst = ang[same & out].max() if (same & out).any() else 0.0
+    print(f"{label}: status agree {same.mean():.5f}, exit dir <=1e-6 rad {frac_dir:.5f} of {out.sum()}, "
+          f"max angle (same status) {worst:.3e}, median {np.median(ang[out]) if out.any() else 0:.3e}")
+    assert same.mean() >= 0.995
+    assert frac_dir >= 0.99
+    assert worst <= 1e-3
+    both = same & (st_ref == 1)
+    assert np.array_equal(k["hit_entity"][both], ent_ref[both])
+
+
+@pytest.mark.parametrize("name", sorted(kerr_cases.trace_cases()))
+def test_kerr_trace_matches_reference_golden(ctx, golden, name):
+    g = golden["kerr_trace"]
+    sc, rays = kerr_cases.trace_cases()[name]
+    ctx.upload(sc)
+    k = ctx.kerr_trace(g[f"{name}_rays"])
+    obj, hit, rec = g[f"{name}_obj"], g[f"{name}_hit"], g[f"{name}_rec"]
+    st = kerr_cases.status_from_reference(obj, hit, rec)
+    _compare(k, st, rec[:, 11:14], obj, name)
+    # most rays reproduce the reference's step sequence exactly
+    assert (k["steps"] == rec[:, 1].astype(np.int32)).mean() >= 0.99
+    st_stats = ctx.stats()
+    assert st_stats["paths"] == len(rays) and st_stats["kernel_launches"] == 1
+
+
+@pytest.mark.parametrize("a", [0.6, 0.999])
+def test_kerr_lensing_view_matches_oracle(ctx, a):
+    # the lensing configuration (camera at r = 6.03 M in the equatorial plane,
+    # 60 degree field, disk r 3..15 M) at 96 x 48 rays
+    s = scenes.kerr_lensing(a=a, width=96, height=48, max_steps=4000)
+    rays = scenes.camera_rays(s)
+    ctx.upload(s)
+    k = ctx.kerr_trace(rays)
+    o = O.OracleScene(s).kerr_trace(rays)
+    _compare(k, o["status"], o["exit_dir"], o["hit_entity"], f"lensing a={a}")
+    same = k["status"] == o["status"]
+    assert np.abs(k["final_bl"][same & (o["status"] != 2)] - o["final_bl"][same & (o["status"] != 2)]).max() < 1e-6 * 5000
+
+
+def test_kerr_escape_radius_option_matches_oracle(ctx):
+    s = scenes.kerr_disk(32, 24, a=0.9, max_steps=4000, escape_radius=200.0)
+    rays = scenes.camera_rays(s)
+    ctx.upload(s)
+    k = ctx.kerr_trace(rays)
+    o = O.OracleScene(s).kerr_trace(rays)
+    _compare(k, o["status"], o["exit_dir"], o["hit_entity"], "escape_radius 200")
+    esc = o["status"] == 0
+    assert esc.any() and o["steps"][esc].max() < 4000  # the option ends the escaped rays early
+
+
+def test_kerr_trace_errors(ctx):
+    s = scenes.cornell_spheres(width=16, height=12, samples=1, supersamples=1)
+    ctx.upload(s)
+    with pytest.raises(gpu.PrenderError):
+        ctx.kerr_trace(np.zeros((4, 6)))  # no black hole in the scene
+    s = scenes.kerr_disk(8, 6, a=0.9, max_steps=10)
+    s.kerr["a"] = 1.0  # |a| must be below M
+    with pytest.raises(gpu.PrenderError):
+        ctx.upload(s)
+    s = scenes.kerr_disk(8, 6, a=0.9, max_steps=10)
+    s.settings.nee = 1  # next-event estimation along geodesics is not on this path
+    ctx.upload(s)
+    with pytest.raises(gpu.PrenderError):
+        ctx.render(s)
+
+
+def _batches(ctx, scene, nb, spp_per_batch):
+    return np.stack([ctx.render(scene, sample_offset=b * spp_per_batch).astype(np.float64) for b in range(nb)])
+
+
+def test_kerr_render_matches_reference_statistically(ctx, golden):
+    s = kerr_cases.highspp_case()
+    ctx.upload(s)
+    ref = golden["kerr_render"]["texture_highspp"]
+    nb, spp = 16, s.settings.spp
+    b = _batches(ctx, s, nb, spp)
+    mean = b.mean(0)
+    sd = b.std(0, ddof=1)
+    sigma = np.sqrt(sd ** 2 / nb + sd ** 2) + 1e-6
+    z = np.abs(mean - ref) / sigma
+    frac = float((z > 3.0).mean())
+    rmse = float(np.sqrt(((mean - ref) ** 2).mean()))
+    noise = float(np.sqrt((sigma ** 2).mean()))
+    rel = abs(mean.mean() - ref.mean()) / ref.mean()
+    print(f"kerr render: >3 sigma {frac:.4f}, rmse {rmse:.3e} vs noise {noise:.3e}, mean rel diff {rel:.4f}")
+    assert rel < 0.01
+    assert frac < 0.03
+    assert rmse < 1.3 * noise
