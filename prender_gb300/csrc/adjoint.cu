@@ -21,7 +21,7 @@
 // Sampling decisions (Russian roulette, light choice, glass branch choice)
 // are held fixed and their probabilities are treated as constants, the
 // usual estimator of the derivative of the expectation; the luminance clamp
-// of a sample scales its gradient by the same factor.  Scenes with media are
+// of a sample is differentiated exactly.  Scenes with media are
 // not supported by this pass; materials are limited to kAdjMaterials.
 #include <cuda_runtime.h>
 
@@ -133,16 +133,19 @@ __global__ void __launch_bounds__(128) adjoint_kernel(DevScene S, RenderCfg cfg,
       float3 o, d;
       const uint64_t sample_id = camera_ray(cfg, x, y, cfg.sample_offset + (uint64_t)k, o, d);
       const float3 L = adjoint_sample(S, cfg, o, d, sample_id, n_mat, g_col, g_em, st, err, segs);
-      // finish_sample: v = L * smp, scaled down to the luminance cutoff
-      float3 v = L * cfg.smp;
-      float scale = cfg.smp;
+      // finish_sample: v = L * smp, and above the cutoff v_c = c v / lum(v),
+      // whose derivative is (c / lum) (dv - v (W . dv) / lum) with W the
+      // luminance weights: the adjoint of the clamp maps delta to
+      // (c / lum) (delta - (delta . v / lum) W)
+      const float3 v = L * cfg.smp;
+      float3 w = delta * cfg.smp;
       if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z))) {
-        scale = 0.0f;
+        w = f3(0, 0, 0);
       } else if (cfg.cutoff > 0.0f) {
-        const float lum = 0.2126f * v.x + 0.7152f * v.y + 0.0722f * v.z;
-        if (lum > cfg.cutoff) scale *= cfg.cutoff / lum;
+        const float3 W = f3(0.2126f, 0.7152f, 0.0722f);
+        const float lum = dot(W, v);
+        if (lum > cfg.cutoff) w = (delta - W * (dot(delta, v) / lum)) * (cfg.cutoff / lum * cfg.smp);
       }
-      const float3 w = delta * scale;
       for (int m = 0; m < n_mat; m++) {
         G_col[m] += w * g_col[m];
         G_em[m] += w * g_em[m];

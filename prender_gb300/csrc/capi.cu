@@ -451,7 +451,10 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   B.max_iterations = 20000u;  // bounded device loop; a frame needs a few hundred
   WfLaunch L;
   L.shade_blocks = (P + 127) / 128;
-  L.trace_blocks = std::min<unsigned int>((P + 127) / 128, 152u * 64u);
+  // grid-stride traversal over the queues: up to 64 blocks per SM
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || sms <= 0) sms = 152;
+  L.trace_blocks = std::min<unsigned int>((P + 127) / 128, (unsigned int)sms * 64u);
   PR_CUDA(c, cudaMemsetAsync(c->wf_nee.p, 0, f4 * 3 * P, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->wf_pix.p, 0, 24ull * wh, c->stream));
   // PR_WF_HOST_LOOP=1 drives the iterations from the host instead of the

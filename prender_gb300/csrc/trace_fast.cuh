@@ -99,14 +99,26 @@ __device__ __forceinline__ bool fast_qbvh(const DevScene& S, const GEntF& e, flo
     const int lf = (sg[at] == 0) ? 0 : 2, rf = (lf + 2) & 3;
     if (sg[al] == 0) { order[lf] = 0; order[lf + 1] = 1; } else { order[lf] = 1; order[lf + 1] = 0; }
     if (sg[ar] == 0) { order[rf] = 2; order[rf + 1] = 3; } else { order[rf] = 3; order[rf + 1] = 2; }
-    // leaves near to far now; inner nodes pushed far to near
+    // leaves near to far now, inner nodes pushed far to near.  The leaf
+    // triangles are gathered into one run first, so that all lanes of a warp
+    // test their triangles in the same loop (one code path, not one per
+    // child position)
+    int lfirst[4], lcnt[4];
+    float ltn[4];
+    int nl = 0;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
       const int c = order[i];
       if (!((mask >> c) & 1) || child[c] == kChildInvalid || child[c] >= 0) continue;
-      if (tn[c] > tbest) continue;
-      const int32_t first = (int32_t)((uint32_t)child[c] & ~kLeafBit);
-      for (int k = 0; k < cnt[c]; k++) {
+      lfirst[nl] = (int32_t)((uint32_t)child[c] & ~kLeafBit);
+      lcnt[nl] = cnt[c];
+      ltn[nl] = tn[c];
+      nl++;
+    }
+    for (int l = 0; l < nl; l++) {
+      if (ltn[l] > tbest) continue;
+      const int32_t first = lfirst[l];
+      for (int k = 0; k < lcnt[l]; k++) {
         st.tris++;
         float t, uu, vv;
         if (fast_tri(S.tris + 3 * (size_t)(first + k), o, d, tbest, t, uu, vv)) {

@@ -74,6 +74,24 @@ __device__ __forceinline__ unsigned int append(unsigned int* counter, bool want)
   return base + (unsigned int)__popc(mask & ((1u << lane) - 1u));
 }
 
+// warp-aggregated append of n entries per lane (contiguous per lane, in
+// lane order); returns this lane's first slot
+__device__ __forceinline__ unsigned int append_n(unsigned int* counter, unsigned int n) {
+  const unsigned int active = __activemask();
+  if (active != 0xffffffffu) return n ? atomicAdd(counter, n) : 0u;  // partial warp: one atomic per lane
+  const int lane = threadIdx.x & 31;
+  unsigned int incl = n;  // inclusive prefix sum over lanes 0..lane
+  for (int off = 1; off < 32; off <<= 1) {
+    const unsigned int v = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += v;
+  }
+  const unsigned int total = __shfl_sync(0xffffffffu, incl, 31);
+  unsigned int base = 0;
+  if (lane == 0 && total) base = atomicAdd(counter, total);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  return base + incl - n;
+}
+
 __device__ __forceinline__ void pixel_of(const RenderCfg& cfg, uint64_t g, int& x, int& y, uint64_t& kg) {
   const uint64_t wh = (uint64_t)cfg.width * cfg.height;
   const uint64_t k = g / wh;
@@ -148,6 +166,7 @@ __global__ void __launch_bounds__(128) wf_shade() {
     PathState ps;
     uint64_t g = 0;
     bool has_ray = false;
+    int n_shadow = 0;
     if (i < B.n_slots) {
       state = __float_as_int(B.d[i].w) >> 1;
       if (state == SLOT_HIT) {
@@ -203,11 +222,7 @@ __global__ void __launch_bounds__(128) wf_shade() {
         } else {
           has_ray = true;
         }
-        // shadow rays go to the shadow queue
-        for (int k = 0; k < 3; k++) {
-          const unsigned int q = append(&ctl->sh_count, k < nsh);
-          if (k < nsh) B.shq[q] = 3 * i + k;
-        }
+        n_shadow = nsh;
       }
       if (state == SLOT_FREE) {
         // refill: a waiting glass branch first, else the next camera sample
@@ -250,6 +265,10 @@ __global__ void __launch_bounds__(128) wf_shade() {
     }
     const unsigned int q = append(&ctl->ext_count, has_ray);
     if (has_ray) B.extq[q] = i;
+    // shadow rays: a lane's (up to three) rays share origin and light, so
+    // they go to adjacent queue entries and trace side by side in a warp
+    const unsigned int qs = append_n(&ctl->sh_count, (unsigned int)n_shadow);
+    for (int k = 0; k < n_shadow; k++) B.shq[qs + k] = 3 * i + k;
   }
 }
 

@@ -74,7 +74,7 @@ def test_adjoint_matches_finite_differences(ctx):
     fdm = loss(_render(ctx, _scene(alb, emission_scale=1.0 - H)))
     fd = (fdp - fdm) / (2 * H)
     print(f"emission scale: adjoint {g['emission_scale']:+.6e} fd {fd:+.6e}")
-    assert abs(g["emission_scale"] - fd) <= 0.01 * abs(fd)
+    assert abs(g["emission_scale"] - fd) <= 0.001 * abs(fd)
     # per-material emission gradient of the light, channel sum, equals the scale gradient / 36
     assert abs(g["emission"][8].sum() * 36.0 - g["emission_scale"]) <= 1e-6 * abs(g["emission_scale"])
 
