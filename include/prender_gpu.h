@@ -119,6 +119,13 @@ typedef struct pr_mesh {
   const float* face_normals;  /* 3 * n_faces or NULL                         */
 } pr_mesh;
 
+/* Kerr integrator precision: PR_KERR_FP64 runs the reference's FP64
+ * arithmetic in its order (exit directions within 1e-6 rad of it);
+ * PR_KERR_FP32 integrates in FP32 with a float-pair state and its own step
+ * control (about 50x the FP64 rate on GB300; its error against the FP64
+ * form is stated by the tests). */
+enum { PR_KERR_FP64 = 0, PR_KERR_FP32 = 1 };
+
 /* KerrBlackHole constructor inputs (KerrBlackHole.h:86-151, scene_env.h:701-766,2056-2098) */
 typedef struct pr_kerr {
   int32_t enabled;
@@ -132,6 +139,8 @@ typedef struct pr_kerr {
                                  Bitmap::cell(y, x) returns it; NULL = none   */
   int32_t texture_width;
   int32_t texture_height;
+  int32_t precision;          /* PR_KERR_FP64 (default) or PR_KERR_FP32      */
+  int32_t pad0;
 } pr_kerr;
 
 typedef struct pr_scene_desc {
@@ -286,6 +295,12 @@ typedef struct pr_render_stats {
   uint64_t kernel_launches;  /* kernels of this library launched by the call */
 } pr_render_stats;
 int pr_last_render_stats(pr_ctx* ctx, pr_render_stats* stats);
+/* Per-kernel device time of the last wavefront render when it ran with the
+ * host-driven loop (environment PR_WF_HOST_LOOP=1; zeros otherwise): ms[0..3]
+ * = shade, extend, shadow, control (n entries written, at most 4); and
+ * shadow_counts[0..2] = the frame's shadow rays, node visits and triangle
+ * tests (may be NULL).  No reference counterpart (diagnostics). */
+int pr_last_kernel_times(pr_ctx* ctx, double* ms, unsigned long long* shadow_counts, int n);
 
 /* ---- Differentiation ------------------------------------------------- */
 /* Adjoint of pr_render by path replay (no reference counterpart: the

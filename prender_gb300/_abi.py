@@ -29,6 +29,8 @@ PR_MAT_REFRACTION_FRESNEL = 8
 PR_ENT_SPHERE = 1
 PR_ENT_UVPLANE = 3
 PR_ENT_CIRCLE = 4
+PR_KERR_FP64 = 0
+PR_KERR_FP32 = 1
 PR_ENT_POLYGON = 5
 
 PR_MODE_MEGAKERNEL = 0
@@ -103,6 +105,8 @@ class pr_kerr(C.Structure):
         ("texture", C.c_void_p),
         ("texture_width", C.c_int32),
         ("texture_height", C.c_int32),
+        ("precision", C.c_int32),
+        ("pad0", C.c_int32),
     ]
 
 

@@ -85,7 +85,7 @@ pr_ctx* pr_create(int device, int* status) {
   c->device = device;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
-      c->errword.ensure(16) != cudaSuccess || c->counters.ensure(64) != cudaSuccess) {
+      c->errword.ensure(16) != cudaSuccess || c->counters.ensure(128) != cudaSuccess) {
     if (status) *status = PR_E_CUDA;
     delete c;
     return nullptr;
@@ -238,7 +238,7 @@ int pr_first_hit_dev(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, 
   if (n < 0 || (n > 0 && (!rays || !entity || !prim || !t))) return fail(c, PR_E_ARG, "bad first-hit arguments");
   PR_CUDA(c, cudaSetDevice(c->device));
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
-  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
   PR_CUDA(c, launch_first_hit(c->dev, rays, n, entity, prim, t, (uint32_t*)c->errword.p,
                               (unsigned long long*)c->counters.p, c->stream));
@@ -475,6 +475,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
     }
   }
   c->wf_passes = 0;
+  for (double& t : c->kernel_ms) t = 0.0;
   for (uint64_t first = 0; first < (uint64_t)g.spp; first += layers) {
     c->wf_passes++;
     const uint64_t n_layers = std::min<uint64_t>(layers, (uint64_t)g.spp - first);
@@ -484,7 +485,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
     PR_CUDA(c, wf_set_constants(c->dev, g, B, c->stream));
     PR_CUDA(c, wf_reset_launch(P, c->stream));
     if (use_graph && c->wf_graph) PR_CUDA(c, cudaGraphLaunch(c->wf_graph, c->stream));
-    else PR_CUDA(c, wf_run_host_loop(L, c->wf_host_ctl, (const WfCtl*)c->wf_ctl.p, c->stream));
+    else PR_CUDA(c, wf_run_host_loop(L, c->wf_host_ctl, (const WfCtl*)c->wf_ctl.p, c->stream, c->kernel_ms));
   }
   PR_CUDA(c, wf_resolve_launch(rgb_dev, (int)(3 * wh), accumulate, g.sensor, c->stream));
   return PR_OK;
@@ -502,7 +503,7 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   PR_CUDA(c, cudaSetDevice(c->device));
   const size_t n3 = (size_t)g.width * g.height * 3;
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
-  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
   const bool kerr = c->kerr.enabled != 0;
   if (kerr) {
@@ -521,7 +522,7 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
     PR_CUDA(c, launch_reduce((const float*)c->partial.p, rgb_dev, (int)n3, g.chunks, accumulate, c->stream));
   }
   PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
-  unsigned long long cnt[8];
+  unsigned long long cnt[16];
   PR_CUDA(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
   st = check_device_errors(c);
   float ms = 0;
@@ -531,6 +532,7 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   // wavefront: reset per pass + 4 per iteration + resolve; megakernel: kernel + reduce
   const uint64_t launches = wf ? 4 * cnt[5] + c->wf_passes + 1 : 2;
   c->stats = pr_render_stats{paths, cnt[1], cnt[2], cnt[3], ms, launches};
+  for (int k = 0; k < 3; k++) c->shadow_counts[k] = wf ? cnt[6 + k] : 0;
   return st;
 }
 
@@ -578,12 +580,12 @@ int pr_render_adjoint_dev(pr_ctx* c, const pr_camera* cam, const pr_render_param
   if (!d_color) PR_CUDA(c, cudaMemsetAsync(dc, 0, 3 * sizeof(double) * n_mat, c->stream));
   if (!d_emission) PR_CUDA(c, cudaMemsetAsync(de, 0, 3 * sizeof(double) * n_mat, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
-  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
   PR_CUDA(c, launch_adjoint(c->dev, g, dl_drgb, n_mat, dc, de, (uint32_t*)c->errword.p,
                             (unsigned long long*)c->counters.p, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
-  unsigned long long cnt[8];
+  unsigned long long cnt[16];
   PR_CUDA(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
   st = check_device_errors(c);
   float ms = 0;
@@ -628,6 +630,14 @@ int pr_render_adjoint(pr_ctx* c, const pr_camera* cam, const pr_render_params* p
   return PR_OK;
 }
 
+int pr_last_kernel_times(pr_ctx* c, double* ms, unsigned long long* shadow_counts, int n) {
+  if (!c || !ms || n < 0) return PR_E_ARG;
+  for (int k = 0; k < n && k < 4; k++) ms[k] = c->kernel_ms[k];
+  if (shadow_counts)
+    for (int k = 0; k < 3; k++) shadow_counts[k] = c->shadow_counts[k];
+  return PR_OK;
+}
+
 int pr_last_render_stats(pr_ctx* c, pr_render_stats* s) {
   if (!c || !s) return PR_E_ARG;
   *s = c->stats;
@@ -643,13 +653,13 @@ int pr_kerr_trace_dev(pr_ctx* c, const double* rays, int64_t n, int32_t* status,
   if (n > (int64_t)1 << 31) return fail(c, PR_E_ARG, "at most 2^31 rays per call");
   PR_CUDA(c, cudaSetDevice(c->device));
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
-  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
   KerrOut o{status, final_bl, exit_dir, steps, hit_entity, hit_t};
   PR_CUDA(c, launch_kerr_trace(c->dev, c->kerr, rays, n, o, (uint32_t*)c->errword.p,
                                (unsigned long long*)c->counters.p, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
-  unsigned long long cnt[8];
+  unsigned long long cnt[16];
   PR_CUDA(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
   int st = check_device_errors(c);
   float ms = 0;

@@ -47,6 +47,8 @@ struct pr_ctx {
   pr::DevBuf partial, out, rays, ires, jres, dres;
   pr::DevBuf k_status, k_bl, k_dir, k_steps, k_ent, k_t;  // pr_kerr_trace staging
   pr::DevBuf adj_scratch, adj_grad;                         // adjoint outputs
+  double kernel_ms[4] = {0, 0, 0, 0};        // wavefront shade / extend / shadow / control (host-driven loop)
+  unsigned long long shadow_counts[3] = {0, 0, 0};  // shadow rays, nodes, triangles of the last wavefront frame
   pr_render_stats stats{};
   // wavefront pool
   pr::DevBuf wf_o, wf_d, wf_beta, wf_dpw, wf_L, wf_sample, wf_hit, wf_hitv, wf_nee, wf_sho, wf_shd, wf_extq, wf_shq;

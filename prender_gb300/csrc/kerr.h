@@ -6,6 +6,7 @@
 
 #include "pr_internal.h"
 #include "render_kernels.h"
+#include "../../include/prender_gpu.h"
 
 namespace pr {
 
@@ -20,12 +21,27 @@ struct KerrOut {
 };
 
 // counters[0] rays, [1] accepted steps, [2] RK45 attempts, [3] segment tests
-cudaError_t launch_kerr_trace(const DevScene& S, const GKerr& K, const double* rays, int64_t n, KerrOut out,
-                              uint32_t* err, unsigned long long* counters, cudaStream_t stream);
+cudaError_t launch_kerr_trace_fp64(const DevScene& S, const GKerr& K, const double* rays, int64_t n, KerrOut out,
+                                   uint32_t* err, unsigned long long* counters, cudaStream_t stream);
+cudaError_t launch_kerr_trace_fp32(const DevScene& S, const GKerr& K, const double* rays, int64_t n, KerrOut out,
+                                   uint32_t* err, unsigned long long* counters, cudaStream_t stream);
 
 // the renderer with every scene query traced along a geodesic; same output
 // layout as launch_megakernel (per-chunk partial images)
-cudaError_t launch_kerr_render(const DevScene& S, const GKerr& K, const RenderCfg& cfg, float* partial, uint32_t* err,
-                               unsigned long long* counters, cudaStream_t stream);
+cudaError_t launch_kerr_render_fp64(const DevScene& S, const GKerr& K, const RenderCfg& cfg, float* partial,
+                                    uint32_t* err, unsigned long long* counters, cudaStream_t stream);
+cudaError_t launch_kerr_render_fp32(const DevScene& S, const GKerr& K, const RenderCfg& cfg, float* partial,
+                                    uint32_t* err, unsigned long long* counters, cudaStream_t stream);
+
+inline cudaError_t launch_kerr_trace(const DevScene& S, const GKerr& K, const double* rays, int64_t n, KerrOut out,
+                                     uint32_t* err, unsigned long long* counters, cudaStream_t stream) {
+  return K.precision == PR_KERR_FP32 ? launch_kerr_trace_fp32(S, K, rays, n, out, err, counters, stream)
+                                     : launch_kerr_trace_fp64(S, K, rays, n, out, err, counters, stream);
+}
+inline cudaError_t launch_kerr_render(const DevScene& S, const GKerr& K, const RenderCfg& cfg, float* partial,
+                                      uint32_t* err, unsigned long long* counters, cudaStream_t stream) {
+  return K.precision == PR_KERR_FP32 ? launch_kerr_render_fp32(S, K, cfg, partial, err, counters, stream)
+                                     : launch_kerr_render_fp64(S, K, cfg, partial, err, counters, stream);
+}
 
 }  // namespace pr

@@ -109,6 +109,9 @@ struct GKerr {
   double texture_coef;     // background texture scale (background_texture_coef)
   const unsigned char* texture;  // background texture, RGB8 rows as cell(y, x) reads them
   int32_t tex_w, tex_h;
+  int32_t precision;             // PR_KERR_FP64 / PR_KERR_FP32
+  double scene_radius;           // farthest scene geometry from the hole (BL-safe bound)
+  double scene_inner;            // nearest scene geometry to the hole (0: something at the hole)
 };
 
 // Everything a kernel needs, passed by value (fits the 4 KB param space).

@@ -436,6 +436,17 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
         gn.axes = rn.axis_top | (rn.axis_left << 2) | (rn.axis_right << 4);
         hs.nodes.push_back(gn);
       }
+      for (int a = 0; a < 3; a++) {
+        g.bmin[a] = 3.0e38f;
+        g.bmax[a] = -3.0e38f;
+      }
+      for (int64_t f = 0; f < 3 * (int64_t)pm_.n_faces; f++) {
+        const float* v = pm_.vertices + 3 * (size_t)pm_.faces[f];
+        for (int a = 0; a < 3; a++) {
+          g.bmin[a] = std::min(g.bmin[a], v[a]);
+          g.bmax[a] = std::max(g.bmax[a], v[a]);
+        }
+      }
       for (int t : q.leaf_tris) {
         for (int k = 0; k < 3; k++) {
           const float* v = pm_.vertices + 3 * (size_t)pm_.faces[3 * (size_t)t + k];
@@ -498,6 +509,43 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
     k.Rhor = k.M + std::sqrt(k.M * k.M - k.a2) + 1e-10;
     for (int q = 0; q < 4; q++) k.map_coef[q] = pk.map_coef[q];
     k.escape_radius = pk.escape_radius;
+    if (pk.precision != PR_KERR_FP64 && pk.precision != PR_KERR_FP32) { err = "unknown Kerr precision"; return PR_E_ARG; }
+    k.precision = pk.precision;
+    // farthest and nearest scene surface from the hole (Cartesian, conservative)
+    const D3 P = mk(k.pos);
+    double far = 0.0, near = 1.0e300;
+    for (const GEntity& e : hs.ents) {
+      double f = 0.0, n = 0.0;
+      if (e.type == PR_ENT_SPHERE || e.type == PR_ENT_CIRCLE) {
+        const double dc = len(sub(mk(e.p), P));
+        f = dc + e.radius;
+        n = e.type == PR_ENT_SPHERE ? std::fabs(dc - e.radius)                      // a sphere is its surface
+                                    : std::max({0.0, e.radius_inner - dc, dc - e.radius});  // the annulus
+      } else if (e.type == PR_ENT_UVPLANE) {
+        const D3 o = mk(e.p), U = scale(mk(e.u_axis), e.u_length), V = scale(mk(e.v_axis), e.v_length);
+        const D3 corner[4] = {o, add(o, U), add(o, V), add(add(o, U), V)};
+        for (const D3& q : corner) f = std::max(f, len(sub(q, P)));
+        const D3 ctr = add(o, scale(add(U, V), 0.5));
+        n = std::max(0.0, len(sub(ctr, P)) - 0.5 * len(add(U, V)) - 0.5 * len(sub(U, V)));
+      } else {  // mesh: its bounding box
+        double dn2 = 0.0, df2 = 0.0;
+        for (int a = 0; a < 3; a++) {
+          const double pa = (&P.x)[a], lo = e.bmin[a], hi = e.bmax[a];
+          const double dn = pa < lo ? lo - pa : (pa > hi ? pa - hi : 0.0);
+          const double dfa = std::max(std::fabs(pa - lo), std::fabs(pa - hi));
+          dn2 += dn * dn;
+          df2 += dfa * dfa;
+        }
+        f = std::sqrt(df2);
+        n = std::sqrt(dn2);
+      }
+      far = std::max(far, f);
+      near = std::min(near, n);
+    }
+    if (hs.ents.empty()) near = 0.0;
+    k.scene_radius = far;
+    // in Boyer-Lindquist r: a point at Cartesian distance d has r <= d <= sqrt(r^2 + a^2)
+    k.scene_inner = near * near > k.a2 ? std::sqrt(near * near - k.a2) : 0.0;
     k.texture_coef = pk.texture_coef;
     if (pk.texture) {
       if (pk.texture_width <= 0 || pk.texture_height <= 0) { err = "background texture size must be positive"; return PR_E_ARG; }

@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(128) wf_shade() {
   }
 }
 
-__global__ void __launch_bounds__(128) wf_extend() {
+__global__ void __launch_bounds__(128, 10) wf_extend() {
   const DevScene& S = c_scene;
   const WfBufs& B = c_buf;
   const unsigned int n = B.ctl->ext_count;
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(128) wf_extend() {
   }
 }
 
-__global__ void __launch_bounds__(128) wf_shadow() {
+__global__ void __launch_bounds__(128, 10) wf_shadow() {
   const DevScene& S = c_scene;
   const WfBufs& B = c_buf;
   const unsigned int n = B.ctl->sh_count;
@@ -327,6 +327,9 @@ __global__ void __launch_bounds__(128) wf_shadow() {
       atomicAdd(B.counters + 1, a);
       atomicAdd(B.counters + 2, c);
       atomicAdd(B.counters + 3, dd);
+      atomicAdd(B.counters + 6, a);  // the shadow kernel's own share
+      atomicAdd(B.counters + 7, c);
+      atomicAdd(B.counters + 8, dd);
     }
   }
 }
@@ -418,15 +421,42 @@ cudaError_t wf_build_graph(const WfLaunch& L, cudaStream_t s, cudaGraphExec_t* e
 
 // host-driven loop: launches iterations and checks the work flag every
 // 'check' iterations (used when graph conditionals are unavailable)
-cudaError_t wf_run_host_loop(const WfLaunch& L, WfCtl* host_ctl_pinned, const WfCtl* dev_ctl, cudaStream_t s) {
-  const int check = 8;
-  for (int it = 0; it < (1 << 20); it += check) {
-    for (int k = 0; k < check; k++) launch_body(L, 0, 0, s);
-    cudaError_t e = cudaMemcpyAsync(host_ctl_pinned, dev_ctl, sizeof(WfCtl), cudaMemcpyDeviceToHost, s);
+cudaError_t wf_run_host_loop(const WfLaunch& L, WfCtl* host_ctl_pinned, const WfCtl* dev_ctl, cudaStream_t s,
+                             double* kernel_ms) {
+  constexpr int kCheck = 8;
+  cudaEvent_t ev[kCheck][5] = {};
+  cudaError_t e = cudaSuccess;
+  if (kernel_ms)
+    for (int k = 0; k < kCheck && e == cudaSuccess; k++)
+      for (int q = 0; q < 5 && e == cudaSuccess; q++) e = cudaEventCreate(&ev[k][q]);
+  for (int it = 0; it < (1 << 20) && e == cudaSuccess; it += kCheck) {
+    for (int k = 0; k < kCheck; k++) {
+      if (kernel_ms) cudaEventRecord(ev[k][0], s);
+      wf_shade<<<L.shade_blocks, 128, 0, s>>>();
+      if (kernel_ms) cudaEventRecord(ev[k][1], s);
+      wf_extend<<<L.trace_blocks, 128, 0, s>>>();
+      if (kernel_ms) cudaEventRecord(ev[k][2], s);
+      wf_shadow<<<L.trace_blocks, 128, 0, s>>>();
+      if (kernel_ms) cudaEventRecord(ev[k][3], s);
+      wf_control<<<1, 1, 0, s>>>(0, 0);
+      if (kernel_ms) cudaEventRecord(ev[k][4], s);
+    }
+    e = cudaMemcpyAsync(host_ctl_pinned, dev_ctl, sizeof(WfCtl), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess) break;
+    if (kernel_ms)
+      for (int k = 0; k < kCheck; k++)
+        for (int q = 0; q < 4; q++) {
+          float ms = 0.0f;
+          if (cudaEventElapsedTime(&ms, ev[k][q], ev[k][q + 1]) == cudaSuccess) kernel_ms[q] += ms;
+        }
     if (!host_ctl_pinned->work) break;
   }
+  if (kernel_ms)
+    for (int k = 0; k < kCheck; k++)
+      for (int q = 0; q < 5; q++)
+        if (ev[k][q]) cudaEventDestroy(ev[k][q]);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

@@ -37,7 +37,8 @@ struct WfBufs {
   long long* pix;                   // 3 per pixel: fixed-point image
   WfCtl* ctl;
   uint32_t* err;
-  unsigned long long* counters;     // paths, segments, nodes, triangle tests, extension segments
+  unsigned long long* counters;     // paths, segments, nodes, triangle tests, extension segments,
+                                    // iterations, shadow rays, shadow nodes, shadow triangle tests
   unsigned int n_slots;
   unsigned int spawn_cap;
   unsigned int max_iterations;
@@ -54,7 +55,10 @@ struct WfLaunch {
 cudaError_t wf_set_constants(const DevScene& S, const RenderCfg& cfg, const WfBufs& B, cudaStream_t s);
 cudaError_t wf_reset_launch(unsigned int n_slots, cudaStream_t s);
 cudaError_t wf_build_graph(const WfLaunch& L, cudaStream_t s, cudaGraphExec_t* exec);
-cudaError_t wf_run_host_loop(const WfLaunch& L, WfCtl* host_ctl_pinned, const WfCtl* dev_ctl, cudaStream_t s);
+// kernel_ms (4 entries, may be null) accumulates the device time of each
+// kernel (shade, extend, shadow, control), measured with events
+cudaError_t wf_run_host_loop(const WfLaunch& L, WfCtl* host_ctl_pinned, const WfCtl* dev_ctl, cudaStream_t s,
+                             double* kernel_ms);
 cudaError_t wf_resolve_launch(float* out, int n3, int accumulate, float sensor, cudaStream_t s);
 
 }  // namespace pr

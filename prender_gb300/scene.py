@@ -225,6 +225,7 @@ class SceneDesc:
             k.map_coef[:] = [float(x) for x in scene.kerr.get("map_coef", (1.0, 0.0, 1.0, 0.0))]
             k.escape_radius = float(scene.kerr.get("escape_radius", 0.0))
             k.texture_coef = float(scene.kerr.get("texture_coef", 1.0))
+            k.precision = int(scene.kerr.get("precision", A.PR_KERR_FP64))
             tex = scene.kerr.get("texture")
             if tex is not None:
                 tex = np.ascontiguousarray(tex, dtype=np.uint8)
@@ -277,13 +278,13 @@ class Scene:
 
     def set_black_hole(self, position, a: float, max_steps: int = 10000,
                        map_coef=(1.0, 0.0, 1.0, 0.0), escape_radius: float = 0.0,
-                       texture=None, texture_coef: float = 1.0) -> None:
+                       texture=None, texture_coef: float = 1.0, precision: int = A.PR_KERR_FP64) -> None:
         """A Kerr black hole of mass 1 ('BLACKHOLE x y z' block, scene_env.h:701-766);
         texture is the background map as an (H, W, 3) uint8 array indexed
         [y, x] the way the reference's Bitmap::cell(y, x) reads its image."""
         self.kerr = {"position": tuple(float(x) for x in position), "a": float(a), "max_steps": int(max_steps),
                      "map_coef": tuple(float(x) for x in map_coef), "escape_radius": float(escape_radius),
-                     "texture": texture, "texture_coef": float(texture_coef)}
+                     "texture": texture, "texture_coef": float(texture_coef), "precision": int(precision)}
 
     def add_mesh(self, vertices, faces, material: Material, normal_inverse: int = 1) -> int:
         self.meshes.append(Mesh(vertices, faces))
@@ -328,8 +329,8 @@ class Scene:
             out += ["CAMERA_ANGLE", _fmt(cam.angle), ""]
         if self.kerr is not None:
             k = self.kerr
-            if k.get("escape_radius", 0.0):
-                raise ValueError("escape_radius has no reference counterpart")
+            if k.get("escape_radius", 0.0) or k.get("precision", A.PR_KERR_FP64) != A.PR_KERR_FP64:
+                raise ValueError("escape_radius and the FP32 integrator have no reference counterpart")
             out += [f"BLACKHOLE {f3(k['position'])}",
                     f"geodesics_max_length {int(k['max_steps'])}",
                     f"angular_momentum {_fmt(k['a'])}",
