@@ -295,6 +295,8 @@ def run_gpu(args):
                 "kernel_share": round(kernel_ms[dom] / sum(kernel_ms[k] for k in ("shade", "extend", "shadow",
                                                                                    "control")), 4),
                 "kernel_ms_per_frame": {k: round(kernel_ms[k], 3) for k in ("shade", "extend", "shadow", "control")},
+                "kernel_rays_per_frame": int(rays), "kernel_nodes_per_frame": int(nodes),
+                "kernel_tris_per_frame": int(tris),
                 "note": "algorithmic traversal bytes of the dominant kernel over its CUDA-event time; "
                         "the scene (~28 MB) is L2-resident, so DRAM traffic is far below these bytes"}
         prof = os.path.join(ROOT, "profiles", "traffic.json")

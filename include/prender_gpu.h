@@ -333,6 +333,22 @@ int pr_kerr_trace_dev(pr_ctx* ctx, const double* rays, int64_t n, int32_t* statu
                       double* final_bl, double* exit_dir, int32_t* steps,
                       int32_t* hit_entity, double* hit_t);
 
+/* Ray-bundle Jacobian of the Kerr map (no reference counterpart).  The
+ * initial direction d of each ray is perturbed as normalize(d + s e1 + t e2);
+ * basis holds e1, e2 (6 doubles per ray) or is NULL (then e1 = unit(d x z),
+ * or d x x near the z axis, and e2 = e1 x d).  For rays that leave the scene
+ * (status 0) jac_dir gets d(exit direction)/d(s, t), 3 x 2 row-major, and
+ * jac_bl gets d(final theta, phi)/d(s, t), 2 x 2 row-major; other statuses
+ * give NaN.  Forward mode on dual numbers through the FP64 tracer, along the
+ * primal trace's steps.  Host buffers; any output may be NULL. */
+int pr_kerr_sensitivity(pr_ctx* ctx, const double* rays, int64_t n, const double* basis,
+                        int32_t* status, double* jac_dir, double* jac_bl);
+/* Adjoint form: grad (2 per ray) = cotangent^T d(exit direction)/d(s, t)
+ * for a cotangent of 3 doubles per ray (evaluated from the same forward
+ * tangents: two inputs per ray make forward mode the cheaper one). */
+int pr_kerr_sensitivity_adjoint(pr_ctx* ctx, const double* rays, int64_t n, const double* basis,
+                                const double* cotangent, double* grad);
+
 #ifdef __cplusplus
 }
 #endif

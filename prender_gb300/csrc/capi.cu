@@ -99,7 +99,7 @@ void pr_destroy(pr_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (DevBuf* b : {&c->kerr_tex, &c->k_status, &c->k_bl, &c->k_dir, &c->k_steps, &c->k_ent, &c->k_t,
-                    &c->adj_scratch, &c->adj_grad})
+                    &c->adj_scratch, &c->adj_grad, &c->k_sens})
     b->release();
   for (DevBuf* b : {&c->ents, &c->mats, &c->nodes, &c->tris, &c->fnorm, &c->errword, &c->counters, &c->partial,
                     &c->out, &c->rays, &c->ires, &c->jres, &c->dres, &c->wf_o, &c->wf_d, &c->wf_beta, &c->wf_dpw,
@@ -699,6 +699,57 @@ int pr_kerr_trace(pr_ctx* c, const double* rays, int64_t n, int32_t* status, dou
   if (hit_t) PR_CUDA(c, cudaMemcpyAsync(hit_t, c->k_t.p, 8 * sn, cudaMemcpyDeviceToHost, c->stream));
   PR_CUDA(c, cudaStreamSynchronize(c->stream));
   return PR_OK;
+}
+
+static int kerr_sens_common(pr_ctx* c, const double* rays, int64_t n, const double* basis, const double* cot,
+                            int32_t* status, double* jac_dir, double* jac_bl, double* grad) {
+  if (!c) return PR_E_ARG;
+  if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  if (!c->kerr.enabled) return fail(c, PR_E_SCENE, "the scene has no black hole");
+  if (n < 0 || (n > 0 && !rays)) return fail(c, PR_E_ARG, "bad ray buffer");
+  if (n > (int64_t)1 << 28) return fail(c, PR_E_ARG, "at most 2^28 rays per call");
+  if (n == 0) return PR_OK;
+  PR_CUDA(c, cudaSetDevice(c->device));
+  const size_t un = (size_t)n;
+  // one staging buffer: rays 6, basis 6, cotangent 3, jac_dir 6, jac_bl 4, grad 2 doubles + status per ray
+  PR_CUDA(c, c->k_sens.ensure(un * (27 * sizeof(double) + sizeof(int32_t))));
+  double* d_rays = (double*)c->k_sens.p;
+  double* d_basis = d_rays + 6 * un;
+  double* d_cot = d_basis + 6 * un;
+  double* d_jd = d_cot + 3 * un;
+  double* d_jb = d_jd + 6 * un;
+  double* d_g = d_jb + 4 * un;
+  int32_t* d_st = (int32_t*)(d_g + 2 * un);
+  PR_CUDA(c, cudaMemcpyAsync(d_rays, rays, 48 * un, cudaMemcpyHostToDevice, c->stream));
+  if (basis) PR_CUDA(c, cudaMemcpyAsync(d_basis, basis, 48 * un, cudaMemcpyHostToDevice, c->stream));
+  if (cot) PR_CUDA(c, cudaMemcpyAsync(d_cot, cot, 24 * un, cudaMemcpyHostToDevice, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  PR_CUDA(c, launch_kerr_sensitivity(c->dev, c->kerr, d_rays, basis ? d_basis : nullptr, n, cot ? d_cot : nullptr,
+                                     d_st, d_jd, d_jb, grad ? d_g : nullptr, (uint32_t*)c->errword.p, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  int st = check_device_errors(c);
+  if (st != PR_OK) return st;
+  if (status) PR_CUDA(c, cudaMemcpyAsync(status, d_st, 4 * un, cudaMemcpyDeviceToHost, c->stream));
+  if (jac_dir) PR_CUDA(c, cudaMemcpyAsync(jac_dir, d_jd, 48 * un, cudaMemcpyDeviceToHost, c->stream));
+  if (jac_bl) PR_CUDA(c, cudaMemcpyAsync(jac_bl, d_jb, 32 * un, cudaMemcpyDeviceToHost, c->stream));
+  if (grad) PR_CUDA(c, cudaMemcpyAsync(grad, d_g, 16 * un, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->stats = pr_render_stats{(unsigned long long)n, 0, 0, 0, ms, 1};
+  return PR_OK;
+}
+
+int pr_kerr_sensitivity(pr_ctx* c, const double* rays, int64_t n, const double* basis, int32_t* status,
+                        double* jac_dir, double* jac_bl) {
+  return kerr_sens_common(c, rays, n, basis, nullptr, status, jac_dir, jac_bl, nullptr);
+}
+
+int pr_kerr_sensitivity_adjoint(pr_ctx* c, const double* rays, int64_t n, const double* basis,
+                                const double* cotangent, double* grad) {
+  if (c && n > 0 && (!cotangent || !grad)) return fail(c, PR_E_ARG, "null cotangent or gradient");
+  return kerr_sens_common(c, rays, n, basis, cotangent, nullptr, nullptr, nullptr, grad);
 }
 
 size_t pr_abi_sizeof(int which) {

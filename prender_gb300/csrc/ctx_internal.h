@@ -46,6 +46,7 @@ struct pr_ctx {
   pr::DevBuf errword, counters;  // 4 bytes / 4 x u64
   pr::DevBuf partial, out, rays, ires, jres, dres;
   pr::DevBuf k_status, k_bl, k_dir, k_steps, k_ent, k_t;  // pr_kerr_trace staging
+  pr::DevBuf k_sens;                                        // pr_kerr_sensitivity staging
   pr::DevBuf adj_scratch, adj_grad;                         // adjoint outputs
   double kernel_ms[4] = {0, 0, 0, 0};        // wavefront shade / extend / shadow / control (host-driven loop)
   unsigned long long shadow_counts[3] = {0, 0, 0};  // shadow rays, nodes, triangles of the last wavefront frame

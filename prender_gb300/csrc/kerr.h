@@ -33,6 +33,11 @@ cudaError_t launch_kerr_render_fp64(const DevScene& S, const GKerr& K, const Ren
 cudaError_t launch_kerr_render_fp32(const DevScene& S, const GKerr& K, const RenderCfg& cfg, float* partial,
                                     uint32_t* err, unsigned long long* counters, cudaStream_t stream);
 
+// forward-mode ray-bundle Jacobian (kerr_sens.cu); any output may be null
+cudaError_t launch_kerr_sensitivity(const DevScene& S, const GKerr& K, const double* rays, const double* basis,
+                                    int64_t n, const double* cot, int32_t* status, double* jac_dir, double* jac_bl,
+                                    double* grad, uint32_t* err, cudaStream_t stream);
+
 inline cudaError_t launch_kerr_trace(const DevScene& S, const GKerr& K, const double* rays, int64_t n, KerrOut out,
                                      uint32_t* err, unsigned long long* counters, cudaStream_t stream) {
   return K.precision == PR_KERR_FP32 ? launch_kerr_trace_fp32(S, K, rays, n, out, err, counters, stream)

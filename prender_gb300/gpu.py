@@ -135,6 +135,25 @@ class Context:
                                          _p(out["hit_t"])))
         return out
 
+    def kerr_sensitivity(self, rays: np.ndarray, basis: np.ndarray | None = None,
+                         cotangent: np.ndarray | None = None) -> dict:
+        """Ray-bundle Jacobian of the Kerr map: d(exit direction)/d(s, t)
+        (n, 3, 2) and d(final theta, phi)/d(s, t) (n, 2, 2) for rays that
+        leave the scene (NaN otherwise); with a cotangent (n, 3), also the
+        adjoint product grad = w^T J (n, 2)."""
+        rays = np.ascontiguousarray(rays, dtype=np.float64)
+        n = rays.shape[0]
+        b = None if basis is None else np.ascontiguousarray(basis, dtype=np.float64).reshape(n, 6)
+        out = dict(status=np.empty(n, np.int32), jac_dir=np.empty((n, 3, 2)), jac_bl=np.empty((n, 2, 2)))
+        self._check(self.L.pr_kerr_sensitivity(self.h, _p(rays), n, _p(b), _p(out["status"]), _p(out["jac_dir"]),
+                                               _p(out["jac_bl"])))
+        if cotangent is not None:
+            w = np.ascontiguousarray(cotangent, dtype=np.float64).reshape(n, 3)
+            g = np.empty((n, 2))
+            self._check(self.L.pr_kerr_sensitivity_adjoint(self.h, _p(rays), n, _p(b), _p(w), _p(g)))
+            out["grad"] = g
+        return out
+
     def render(self, scene=None, settings=None, camera=None, sample_offset: int = 0,
                accumulate: np.ndarray | None = None) -> np.ndarray:
         """Render::Run: returns the (H, W, 3) float32 image in the reference's

@@ -180,3 +180,43 @@ def test_kerr_mixed_precision_form_against_fp64(ctx, a):
     # near-hole steps run the reference's FP64 formulas, here with FMA contraction
     assert np.abs(k["hit_t"][hit] - o["hit_t"][hit]).max() < 1e-4
     assert (ang <= 1e-6).mean() >= 0.99
+
+
+def test_kerr_ray_bundle_jacobian_against_central_differences(ctx):
+    """d(exit direction)/d(s, t) of the forward-mode dual-number tracer against
+    central differences of the FP64 tracer (perturbed initial directions,
+    h = 1e-6), for rays that leave the scene; the adjoint form equals w^T J."""
+    s = scenes.kerr_disk(24, 18, a=0.9, max_steps=1500)
+    rays = scenes.camera_rays(s)
+    ctx.upload(s)
+    n = rays.shape[0]
+    rng = np.random.default_rng(4)
+    w = rng.normal(size=(n, 3))
+    J = ctx.kerr_sensitivity(rays, cotangent=w)
+    d = rays[:, 3:] / np.linalg.norm(rays[:, 3:], axis=1, keepdims=True)
+    up = np.where(np.abs(d[:, 2:3]) < 0.9, [[0.0, 0.0, 1.0]], [[1.0, 0.0, 0.0]])
+    e1 = np.cross(d, up)
+    e1 /= np.linalg.norm(e1, axis=1, keepdims=True)
+    e2 = np.cross(e1, d)
+    h = 1e-6
+    fd = np.empty((n, 3, 2))
+    base = ctx.kerr_trace(rays)
+    same = base["status"] == 0
+    for col, e in enumerate((e1, e2)):
+        outs = []
+        for sgn in (1.0, -1.0):
+            r = rays.copy()
+            dd = d + sgn * h * e
+            r[:, 3:] = dd / np.linalg.norm(dd, axis=1, keepdims=True)
+            outs.append(ctx.kerr_trace(r))
+        fd[:, :, col] = (outs[0]["exit_dir"] - outs[1]["exit_dir"]) / (2 * h)
+        same &= (outs[0]["status"] == 0) & (outs[1]["status"] == 0)
+    ok = (J["status"] == 0) & same
+    assert ok.sum() > 100
+    rel = np.linalg.norm((J["jac_dir"] - fd)[ok], axis=(1, 2)) / np.linalg.norm(fd[ok], axis=(1, 2))
+    print(f"Kerr Jacobian vs central differences over {ok.sum()} rays: median rel {np.median(rel):.2e}, "
+          f"p95 {np.quantile(rel, 0.95):.2e}")
+    assert np.median(rel) < 1e-4
+    assert np.quantile(rel, 0.95) < 1e-2
+    assert np.isnan(J["jac_dir"][J["status"] != 0]).all()
+    np.testing.assert_allclose(J["grad"][ok], np.einsum("ni,nij->nj", w[ok], J["jac_dir"][ok]), rtol=1e-12, atol=1e-14)
