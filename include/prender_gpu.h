@@ -295,12 +295,44 @@ typedef struct pr_render_stats {
   uint64_t kernel_launches;  /* kernels of this library launched by the call */
 } pr_render_stats;
 int pr_last_render_stats(pr_ctx* ctx, pr_render_stats* stats);
+/* Autotuner (no reference counterpart): times one short wavefront frame
+ * (one camera sample per pixel, the caller's camera and parameters) for each
+ * candidate path-pool size {2^19 .. 2^22} and traversal grid {16, 32, 64}
+ * blocks per SM, and keeps the fastest for later pr_render calls on this
+ * context.  Images do not depend on either choice.  Outputs may be NULL. */
+int pr_autotune_wavefront(pr_ctx* ctx, const pr_camera* camera, const pr_render_params* params,
+                          int32_t* slots, int32_t* trace_blocks_per_sm, double* frame_ms);
+
 /* Per-kernel device time of the last wavefront render when it ran with the
  * host-driven loop (environment PR_WF_HOST_LOOP=1; zeros otherwise): ms[0..3]
  * = shade, extend, shadow, control (n entries written, at most 4); and
  * shadow_counts[0..2] = the frame's shadow rays, node visits and triangle
  * tests (may be NULL).  No reference counterpart (diagnostics). */
 int pr_last_kernel_times(pr_ctx* ctx, double* ms, unsigned long long* shadow_counts, int n);
+
+/* ---- Batches ---------------------------------------------------------- */
+/* A scene object: an uploaded scene owned by the context, independent of the
+ * one pr_scene_upload sets (SceneEnv::Load + CreateEntList per object). */
+typedef struct pr_scene_obj pr_scene_obj;
+pr_scene_obj* pr_scene_create(pr_ctx* ctx, const pr_scene_desc* desc, int* status);
+void pr_scene_release(pr_ctx* ctx, pr_scene_obj* scene);
+
+typedef struct pr_job {
+  const pr_scene_obj* scene;
+  pr_camera camera;
+  pr_render_params params;    /* each job renders the plain (megakernel) form */
+  float* rgb_dev;             /* W*H*3 floats on the device, image row order  */
+  uint64_t sample_offset;
+  int32_t accumulate;
+  int32_t pad;
+} pr_job;
+
+/* Renders n jobs as one captured CUDA graph (no reference counterpart: the
+ * reference renders one scene per process).  Jobs run on parallel branches
+ * of the graph; each job's image equals pr_render_dev of the same inputs up
+ * to float summation order (a batch uses fewer sample chunks per pixel).
+ * Scene objects must stay alive until the call returns. */
+int pr_render_batch(pr_ctx* ctx, int n, const pr_job* jobs);
 
 /* ---- Differentiation ------------------------------------------------- */
 /* Adjoint of pr_render by path replay (no reference counterpart: the

@@ -168,3 +168,15 @@ class pr_render_stats(C.Structure):
         ("device_ms", C.c_double),
         ("kernel_launches", C.c_uint64),
     ]
+
+
+class pr_job(C.Structure):
+    _fields_ = [
+        ("scene", C.c_void_p),
+        ("camera", pr_camera),
+        ("params", pr_render_params),
+        ("rgb_dev", C.c_void_p),
+        ("sample_offset", C.c_uint64),
+        ("accumulate", C.c_int32),
+        ("pad", C.c_int32),
+    ]

@@ -98,49 +98,55 @@ void pr_destroy(pr_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  for (DevBuf* b : {&c->kerr_tex, &c->k_status, &c->k_bl, &c->k_dir, &c->k_steps, &c->k_ent, &c->k_t,
+  c->cur.release();
+  for (DevBuf* b : {&c->k_status, &c->k_bl, &c->k_dir, &c->k_steps, &c->k_ent, &c->k_t,
                     &c->adj_scratch, &c->adj_grad, &c->k_sens})
     b->release();
-  for (DevBuf* b : {&c->ents, &c->mats, &c->nodes, &c->tris, &c->fnorm, &c->errword, &c->counters, &c->partial,
+  for (DevBuf* b : {&c->errword, &c->counters, &c->partial,
                     &c->out, &c->rays, &c->ires, &c->jres, &c->dres, &c->wf_o, &c->wf_d, &c->wf_beta, &c->wf_dpw,
                     &c->wf_L, &c->wf_sample, &c->wf_hit, &c->wf_hitv, &c->wf_nee, &c->wf_sho, &c->wf_shd, &c->wf_extq,
                     &c->wf_shq, &c->wf_spo, &c->wf_spd, &c->wf_spb, &c->wf_spw, &c->wf_sps, &c->wf_samp, &c->wf_live,
                     &c->wf_pix, &c->wf_ctl})
     b->release();
   if (c->wf_graph) cudaGraphExecDestroy(c->wf_graph);
+  if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
+  for (cudaStream_t st : c->batch_streams) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : c->batch_events) cudaEventDestroy(ev);
+  c->batch_partial.release();
   if (c->wf_host_ctl) cudaFreeHost(c->wf_host_ctl);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
+  cudaGetLastError();  // teardown errors are not reported to later calls
   delete c;
 }
 
 const char* pr_last_error(const pr_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
-int pr_scene_upload(pr_ctx* c, const pr_scene_desc* d) {
-  if (!c) return PR_E_ARG;
+// host build + device copies of one scene (SceneEnv::Load + CreateEntList)
+static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o) {
   PR_CUDA(c, cudaSetDevice(c->device));
-  c->scene_ready = false;
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   std::string err;
-  int st = build_host_scene(d, c->host, err);
+  int st = build_host_scene(d, o.host, err);
   if (st != PR_OK) return fail(c, st, err);
-  HostScene& h = c->host;
-  PR_CUDA(c, upload(c->ents, h.ents, c->stream));
-  PR_CUDA(c, upload(c->mats, h.mats, c->stream));
-  PR_CUDA(c, upload(c->nodes, h.nodes, c->stream));
-  PR_CUDA(c, upload(c->tris, h.tris, c->stream));
-  PR_CUDA(c, upload(c->fnorm, h.fnorm, c->stream));
-  PR_CUDA(c, upload(c->kerr_tex, h.kerr_texture, c->stream));
+  HostScene& h = o.host;
+  PR_CUDA(c, upload(o.ents, h.ents, c->stream));
+  PR_CUDA(c, upload(o.mats, h.mats, c->stream));
+  PR_CUDA(c, upload(o.nodes, h.nodes, c->stream));
+  PR_CUDA(c, upload(o.tris, h.tris, c->stream));
+  PR_CUDA(c, upload(o.fnorm, h.fnorm, c->stream));
+  PR_CUDA(c, upload(o.kerr_tex, h.kerr_texture, c->stream));
   PR_CUDA(c, cudaStreamSynchronize(c->stream));
-  c->kerr = h.kerr;
-  c->kerr.texture = h.kerr_texture.empty() ? nullptr : (const unsigned char*)c->kerr_tex.p;
-  DevScene& S = c->dev;
+  o.kerr = h.kerr;
+  o.kerr.texture = h.kerr_texture.empty() ? nullptr : (const unsigned char*)o.kerr_tex.p;
+  DevScene& S = o.dev;
   memset(&S, 0, sizeof(S));
-  S.ents = (const GEntity*)c->ents.p;
-  S.mats = (const GMaterial*)c->mats.p;
-  S.nodes = (const GNode*)c->nodes.p;
-  S.tris = (const float4*)c->tris.p;
-  S.fnorm = (const float*)c->fnorm.p;
+  S.ents = (const GEntity*)o.ents.p;
+  S.mats = (const GMaterial*)o.mats.p;
+  S.nodes = (const GNode*)o.nodes.p;
+  S.tris = (const float4*)o.tris.p;
+  S.fnorm = (const float*)o.fnorm.p;
   S.n_ents = (int)h.ents.size();
   S.n_lights = (int)h.light_ent.size();
   for (int i = 0; i < S.n_lights; i++) S.light_ent[i] = h.light_ent[i];
@@ -174,18 +180,52 @@ int pr_scene_upload(pr_ctx* c, const pr_scene_desc* d) {
     f.face_base = e.face_base;
     f.node_base = e.node_base;
   }
+  return PR_OK;
+}
+
+int pr_scene_upload(pr_ctx* c, const pr_scene_desc* d) {
+  if (!c) return PR_E_ARG;
+  c->scene_ready = false;
+  int st = build_device_scene(c, d, c->cur);
+  if (st != PR_OK) return st;
   c->scene_ready = true;
   return PR_OK;
+}
+
+pr_scene_obj* pr_scene_create(pr_ctx* c, const pr_scene_desc* d, int* status) {
+  if (!c) {
+    if (status) *status = PR_E_ARG;
+    return nullptr;
+  }
+  pr_scene_obj* o = new pr_scene_obj();
+  int st = build_device_scene(c, d, o->data);
+  if (status) *status = st;
+  if (st != PR_OK) {
+    o->data.release();
+    delete o;
+    return nullptr;
+  }
+  return o;
+}
+
+void pr_scene_release(pr_ctx* c, pr_scene_obj* o) {
+  if (!o) return;
+  if (c) {
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+  }
+  o->data.release();
+  delete o;
 }
 
 static void export_qbvh(const MeshQbvh& q, float* boxes, int64_t* children, int32_t* axes, int32_t* leaf_faces);
 
 int pr_qbvh_info(pr_ctx* c, int entity, int64_t* n_nodes, int64_t* n_leaf_slots) {
   if (!c || !c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
-  for (size_t m = 0; m < c->host.mesh_entity.size(); m++)
-    if (c->host.mesh_entity[m] == entity) {
-      if (n_nodes) *n_nodes = (int64_t)c->host.mesh_qbvh[m].nodes.size();
-      if (n_leaf_slots) *n_leaf_slots = (int64_t)c->host.mesh_qbvh[m].ref_leaf.size();
+  for (size_t m = 0; m < c->cur.host.mesh_entity.size(); m++)
+    if (c->cur.host.mesh_entity[m] == entity) {
+      if (n_nodes) *n_nodes = (int64_t)c->cur.host.mesh_qbvh[m].nodes.size();
+      if (n_leaf_slots) *n_leaf_slots = (int64_t)c->cur.host.mesh_qbvh[m].ref_leaf.size();
       return PR_OK;
     }
   return fail(c, PR_E_ARG, "entity is not a mesh");
@@ -193,9 +233,9 @@ int pr_qbvh_info(pr_ctx* c, int entity, int64_t* n_nodes, int64_t* n_leaf_slots)
 
 int pr_qbvh_export(pr_ctx* c, int entity, float* boxes, int64_t* children, int32_t* axes, int32_t* leaf_faces) {
   if (!c || !c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
-  for (size_t m = 0; m < c->host.mesh_entity.size(); m++)
-    if (c->host.mesh_entity[m] == entity) {
-      export_qbvh(c->host.mesh_qbvh[m], boxes, children, axes, leaf_faces);
+  for (size_t m = 0; m < c->cur.host.mesh_entity.size(); m++)
+    if (c->cur.host.mesh_entity[m] == entity) {
+      export_qbvh(c->cur.host.mesh_qbvh[m], boxes, children, axes, leaf_faces);
       return PR_OK;
     }
   return fail(c, PR_E_ARG, "entity is not a mesh");
@@ -237,10 +277,11 @@ int pr_first_hit_dev(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, 
   if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
   if (n < 0 || (n > 0 && (!rays || !entity || !prim || !t))) return fail(c, PR_E_ARG, "bad first-hit arguments");
   PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-  PR_CUDA(c, launch_first_hit(c->dev, rays, n, entity, prim, t, (uint32_t*)c->errword.p,
+  PR_CUDA(c, launch_first_hit(c->cur.dev, rays, n, entity, prim, t, (uint32_t*)c->errword.p,
                               (unsigned long long*)c->counters.p, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
   unsigned long long cnt[4];
@@ -257,6 +298,7 @@ int pr_first_hit(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, int3
   if (n < 0 || (n > 0 && (!rays || !entity || !prim || !t))) return fail(c, PR_E_ARG, "bad first-hit arguments");
   if (n == 0) return PR_OK;
   PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   PR_CUDA(c, c->rays.ensure(sizeof(double) * 6 * (size_t)n));
   PR_CUDA(c, c->ires.ensure(sizeof(int32_t) * (size_t)n));
   PR_CUDA(c, c->jres.ensure(sizeof(int32_t) * (size_t)n));
@@ -277,13 +319,14 @@ int pr_trace_fast(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, int
   if (n < 0 || (n > 0 && (!rays || !entity || !prim || !t))) return fail(c, PR_E_ARG, "bad trace arguments");
   if (n == 0) return PR_OK;
   PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   PR_CUDA(c, c->rays.ensure(sizeof(double) * 6 * (size_t)n));
   PR_CUDA(c, c->ires.ensure(sizeof(int32_t) * (size_t)n));
   PR_CUDA(c, c->jres.ensure(sizeof(int32_t) * (size_t)n));
   PR_CUDA(c, c->dres.ensure(sizeof(double) * (size_t)n));
   PR_CUDA(c, cudaMemcpyAsync(c->rays.p, rays, sizeof(double) * 6 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
-  PR_CUDA(c, launch_trace_fast(c->dev, (const double*)c->rays.p, n, (int32_t*)c->ires.p, (int32_t*)c->jres.p,
+  PR_CUDA(c, launch_trace_fast(c->cur.dev, (const double*)c->rays.p, n, (int32_t*)c->ires.p, (int32_t*)c->jres.p,
                                (double*)c->dres.p, (uint32_t*)c->errword.p, c->stream));
   int st = check_device_errors(c);
   if (st != PR_OK) return st;
@@ -298,16 +341,17 @@ int pr_trace_fast(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, int
 
 // CameraScreenPram (render.h:105-150) and the Run() sample set-up (:1129-1139)
 int pr::prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, uint64_t sample_offset,
-                          RenderCfg& g) {
+                          RenderCfg& g, const SceneObjData* scene) {
+  const SceneObjData& sc = scene ? *scene : c->cur;
   if (!cam || !p) return fail(c, PR_E_ARG, "null camera or parameters");
   if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
     return fail(c, PR_E_ARG, "image size out of range");
   if (p->samples <= 0 || p->supersamples <= 0) return fail(c, PR_E_ARG, "samples and supersamples must be positive");
-  if (p->nee && c->host.disk_light)
+  if (p->nee && sc.host.disk_light)
     return fail(c, PR_E_UNSUPPORTED,
                 "an emitting disk is a light whose sampling the reference leaves undefined (Circle does not set the "
                 "UVPlane axes randomPoint reads, circle.h:110-134); render it without next-event estimation");
-  if (c->kerr.enabled && (p->nee || (p->media && c->host.medium.on)))
+  if (sc.kerr.enabled && (p->nee || (p->media && sc.host.medium.on)))
     return fail(c, PR_E_UNSUPPORTED, "Kerr scenes render without next-event estimation and media");
   memset(&g, 0, sizeof(g));
   double dir[3] = {cam->dir[0], cam->dir[1], cam->dir[2]};
@@ -391,7 +435,7 @@ static unsigned int wavefront_slots() {
 }
 
 static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int accumulate) {
-  const unsigned int P = wavefront_slots();
+  const unsigned int P = c->tuned_slots ? c->tuned_slots : wavefront_slots();
   const uint64_t wh = (uint64_t)g.width * g.height;
   const uint64_t max_pass = 64ull << 20;  // camera samples per pass (sample table 28 B each)
   uint64_t layers = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.spp, max_pass / wh));
@@ -454,7 +498,8 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   // grid-stride traversal over the queues: up to 64 blocks per SM
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || sms <= 0) sms = 152;
-  L.trace_blocks = std::min<unsigned int>((P + 127) / 128, (unsigned int)sms * 64u);
+  const unsigned int bps = c->tuned_trace_bps ? c->tuned_trace_bps : 64u;
+  L.trace_blocks = std::min<unsigned int>((P + 127) / 128, (unsigned int)sms * bps);
   PR_CUDA(c, cudaMemsetAsync(c->wf_nee.p, 0, f4 * 3 * P, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->wf_pix.p, 0, 24ull * wh, c->stream));
   // PR_WF_HOST_LOOP=1 drives the iterations from the host instead of the
@@ -462,8 +507,13 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   // conditional graph nodes see every launch this way (same kernels, same work)
   const char* host_loop = getenv("PR_WF_HOST_LOOP");
   const bool use_graph = !(host_loop && host_loop[0] == '1');
-  if (use_graph && !c->wf_graph_failed && (!c->wf_graph || c->wf_graph_slots != P)) {
+  if (use_graph && !c->wf_graph_failed &&
+      (!c->wf_graph || c->wf_graph_slots != P || c->wf_graph_trace_blocks != L.trace_blocks)) {
     if (c->wf_graph) cudaGraphExecDestroy(c->wf_graph);
+  if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
+  for (cudaStream_t st : c->batch_streams) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : c->batch_events) cudaEventDestroy(ev);
+  c->batch_partial.release();
     c->wf_graph = nullptr;
     cudaError_t e = wf_build_graph(L, c->stream, &c->wf_graph);
     if (e != cudaSuccess) {
@@ -472,6 +522,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
       c->wf_graph_failed = true;  // fall back to the host-driven loop
     } else {
       c->wf_graph_slots = P;
+      c->wf_graph_trace_blocks = L.trace_blocks;
     }
   }
   c->wf_passes = 0;
@@ -482,7 +533,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
     B.pass_first = first;
     B.pass_samples = n_layers * wh;
     PR_CUDA(c, cudaMemsetAsync(c->wf_samp.p, 0, 24ull * B.pass_samples, c->stream));
-    PR_CUDA(c, wf_set_constants(c->dev, g, B, c->stream));
+    PR_CUDA(c, wf_set_constants(c->cur.dev, g, B, c->stream));
     PR_CUDA(c, wf_reset_launch(P, c->stream));
     if (use_graph && c->wf_graph) PR_CUDA(c, cudaGraphLaunch(c->wf_graph, c->stream));
     else PR_CUDA(c, wf_run_host_loop(L, c->wf_host_ctl, (const WfCtl*)c->wf_ctl.p, c->stream, c->kernel_ms));
@@ -501,15 +552,16 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   int st = prepare_render(c, cam, p, sample_offset, g);
   if (st != PR_OK) return st;
   PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   const size_t n3 = (size_t)g.width * g.height * 3;
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-  const bool kerr = c->kerr.enabled != 0;
+  const bool kerr = c->cur.kerr.enabled != 0;
   if (kerr) {
     // every scene query of a Kerr scene is a geodesic trace: one form only
     PR_CUDA(c, c->partial.ensure(sizeof(float) * n3 * (size_t)g.chunks));
-    PR_CUDA(c, launch_kerr_render(c->dev, c->kerr, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
+    PR_CUDA(c, launch_kerr_render(c->cur.dev, c->cur.kerr, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
                                   (unsigned long long*)c->counters.p, c->stream));
     PR_CUDA(c, launch_reduce((const float*)c->partial.p, rgb_dev, (int)n3, g.chunks, accumulate, c->stream));
   } else if (p->mode == PR_MODE_WAVEFRONT) {
@@ -517,7 +569,7 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
     if (st != PR_OK) return st;
   } else {
     PR_CUDA(c, c->partial.ensure(sizeof(float) * n3 * (size_t)g.chunks));
-    PR_CUDA(c, launch_megakernel(c->dev, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
+    PR_CUDA(c, launch_megakernel(c->cur.dev, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
                                  (unsigned long long*)c->counters.p, c->stream));
     PR_CUDA(c, launch_reduce((const float*)c->partial.p, rgb_dev, (int)n3, g.chunks, accumulate, c->stream));
   }
@@ -543,6 +595,7 @@ int pr_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, float*
   if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
     return fail(c, PR_E_ARG, "image size out of range");
   PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   const size_t bytes = sizeof(float) * 3 * (size_t)cam->width * cam->height;
   PR_CUDA(c, c->out.ensure(bytes));
   if (accumulate) PR_CUDA(c, cudaMemcpyAsync(c->out.p, rgb, bytes, cudaMemcpyHostToDevice, c->stream));
@@ -555,9 +608,9 @@ int pr_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, float*
 
 static int adjoint_checks(pr_ctx* c, const pr_render_params* p) {
   if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
-  if (c->kerr.enabled) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass traces straight rays only");
-  if (p && p->media && c->host.medium.on) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover media");
-  if ((int)c->host.mats.size() > kAdjMaterials)
+  if (c->cur.kerr.enabled) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass traces straight rays only");
+  if (p && p->media && c->cur.host.medium.on) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover media");
+  if ((int)c->cur.host.mats.size() > kAdjMaterials)
     return fail(c, PR_E_UNSUPPORTED, "the adjoint pass tracks at most " + std::to_string(kAdjMaterials) + " materials");
   return PR_OK;
 }
@@ -572,7 +625,8 @@ int pr_render_adjoint_dev(pr_ctx* c, const pr_camera* cam, const pr_render_param
   st = prepare_render(c, cam, p, sample_offset, g);
   if (st != PR_OK) return st;
   PR_CUDA(c, cudaSetDevice(c->device));
-  const int n_mat = (int)c->host.mats.size();
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
+  const int n_mat = (int)c->cur.host.mats.size();
   // scratch for outputs the caller does not want
   PR_CUDA(c, c->adj_scratch.ensure(2 * 3 * sizeof(double) * (size_t)std::max(n_mat, 1)));
   double* dc = d_color ? d_color : (double*)c->adj_scratch.p;
@@ -582,7 +636,7 @@ int pr_render_adjoint_dev(pr_ctx* c, const pr_camera* cam, const pr_render_param
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-  PR_CUDA(c, launch_adjoint(c->dev, g, dl_drgb, n_mat, dc, de, (uint32_t*)c->errword.p,
+  PR_CUDA(c, launch_adjoint(c->cur.dev, g, dl_drgb, n_mat, dc, de, (uint32_t*)c->errword.p,
                             (unsigned long long*)c->counters.p, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
   unsigned long long cnt[16];
@@ -603,8 +657,9 @@ int pr_render_adjoint(pr_ctx* c, const pr_camera* cam, const pr_render_params* p
   if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
     return fail(c, PR_E_ARG, "image size out of range");
   PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   const size_t bytes = sizeof(float) * 3 * (size_t)cam->width * cam->height;
-  const int n_mat = (int)c->host.mats.size();
+  const int n_mat = (int)c->cur.host.mats.size();
   const size_t gb = 3 * sizeof(double) * (size_t)std::max(n_mat, 1);
   PR_CUDA(c, c->out.ensure(bytes));
   PR_CUDA(c, c->adj_grad.ensure(2 * gb));
@@ -624,9 +679,61 @@ int pr_render_adjoint(pr_ctx* c, const pr_camera* cam, const pr_render_params* p
     for (int k = 0; k < 3; k++) {
       if (d_color) d_color[3 * m + k] += hc[3 * m + k];
       if (d_emission) d_emission[3 * m + k] += he[3 * m + k];
-      scale += he[3 * m + k] * c->host.mats[m].emission_d[k];
+      scale += he[3 * m + k] * c->cur.host.mats[m].emission_d[k];
     }
   if (d_emission_scale) *d_emission_scale = scale;
+  return PR_OK;
+}
+
+// Autotuner: times one short frame (the caller's camera and parameters,
+// one camera sample per pixel) for each candidate wavefront pool size and
+// traversal grid, keeps the fastest for this context.  The image does not
+// depend on either (per-branch streams, order-independent fixed-point sums).
+int pr_autotune_wavefront(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, int32_t* slots_out,
+                          int32_t* trace_blocks_per_sm_out, double* ms_out) {
+  if (!c) return PR_E_ARG;
+  if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  if (!cam || !p) return fail(c, PR_E_ARG, "null camera or parameters");
+  if (c->cur.kerr.enabled) return fail(c, PR_E_UNSUPPORTED, "Kerr scenes do not use the wavefront form");
+  pr_render_params q = *p;
+  q.mode = PR_MODE_WAVEFRONT;
+  q.samples = 1;
+  q.supersamples = 1;
+  q.tent_filter = 0;
+  const size_t bytes = sizeof(float) * 3 * (size_t)cam->width * cam->height;
+  PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
+  PR_CUDA(c, c->out.ensure(bytes));
+  const unsigned int cand_slots[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22};
+  const unsigned int cand_bps[] = {16u, 32u, 64u};
+  double best = 1e300;
+  unsigned int best_s = 0, best_b = 0;
+  for (unsigned int sl : cand_slots) {
+    for (unsigned int b : cand_bps) {
+      c->tuned_slots = sl;
+      c->tuned_trace_bps = b;
+      double t = 0.0;
+      for (int rep = 0; rep < 2; rep++) {  // the first run builds the graph and grows the pool
+        int st = pr_render_dev(c, cam, &q, (float*)c->out.p, 0, 0);
+        if (st != PR_OK) {
+          c->tuned_slots = best_s;
+          c->tuned_trace_bps = best_b;
+          return st;
+        }
+        t = c->stats.device_ms;
+      }
+      if (t < best) {
+        best = t;
+        best_s = sl;
+        best_b = b;
+      }
+    }
+  }
+  c->tuned_slots = best_s;
+  c->tuned_trace_bps = best_b;
+  if (slots_out) *slots_out = (int32_t)best_s;
+  if (trace_blocks_per_sm_out) *trace_blocks_per_sm_out = (int32_t)best_b;
+  if (ms_out) *ms_out = best;
   return PR_OK;
 }
 
@@ -648,15 +755,16 @@ int pr_kerr_trace_dev(pr_ctx* c, const double* rays, int64_t n, int32_t* status,
                       int32_t* steps, int32_t* hit_entity, double* hit_t) {
   if (!c) return PR_E_ARG;
   if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
-  if (!c->kerr.enabled) return fail(c, PR_E_SCENE, "the scene has no black hole");
+  if (!c->cur.kerr.enabled) return fail(c, PR_E_SCENE, "the scene has no black hole");
   if (n < 0 || (n > 0 && !rays)) return fail(c, PR_E_ARG, "bad ray buffer");
   if (n > (int64_t)1 << 31) return fail(c, PR_E_ARG, "at most 2^31 rays per call");
   PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
   KerrOut o{status, final_bl, exit_dir, steps, hit_entity, hit_t};
-  PR_CUDA(c, launch_kerr_trace(c->dev, c->kerr, rays, n, o, (uint32_t*)c->errword.p,
+  PR_CUDA(c, launch_kerr_trace(c->cur.dev, c->cur.kerr, rays, n, o, (uint32_t*)c->errword.p,
                                (unsigned long long*)c->counters.p, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
   unsigned long long cnt[16];
@@ -676,6 +784,7 @@ int pr_kerr_trace(pr_ctx* c, const double* rays, int64_t n, int32_t* status, dou
   if (n < 0 || (n > 0 && !rays)) return fail(c, PR_E_ARG, "bad ray buffer");
   if (n > (int64_t)1 << 31) return fail(c, PR_E_ARG, "at most 2^31 rays per call");
   PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   const size_t un = (size_t)std::max<int64_t>(n, 1);
   PR_CUDA(c, c->rays.ensure(48 * un));
   PR_CUDA(c, c->k_status.ensure(4 * un));
@@ -705,11 +814,12 @@ static int kerr_sens_common(pr_ctx* c, const double* rays, int64_t n, const doub
                             int32_t* status, double* jac_dir, double* jac_bl, double* grad) {
   if (!c) return PR_E_ARG;
   if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
-  if (!c->kerr.enabled) return fail(c, PR_E_SCENE, "the scene has no black hole");
+  if (!c->cur.kerr.enabled) return fail(c, PR_E_SCENE, "the scene has no black hole");
   if (n < 0 || (n > 0 && !rays)) return fail(c, PR_E_ARG, "bad ray buffer");
   if (n > (int64_t)1 << 28) return fail(c, PR_E_ARG, "at most 2^28 rays per call");
   if (n == 0) return PR_OK;
   PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   const size_t un = (size_t)n;
   // one staging buffer: rays 6, basis 6, cotangent 3, jac_dir 6, jac_bl 4, grad 2 doubles + status per ray
   PR_CUDA(c, c->k_sens.ensure(un * (27 * sizeof(double) + sizeof(int32_t))));
@@ -725,7 +835,7 @@ static int kerr_sens_common(pr_ctx* c, const double* rays, int64_t n, const doub
   if (cot) PR_CUDA(c, cudaMemcpyAsync(d_cot, cot, 24 * un, cudaMemcpyHostToDevice, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-  PR_CUDA(c, launch_kerr_sensitivity(c->dev, c->kerr, d_rays, basis ? d_basis : nullptr, n, cot ? d_cot : nullptr,
+  PR_CUDA(c, launch_kerr_sensitivity(c->cur.dev, c->cur.kerr, d_rays, basis ? d_basis : nullptr, n, cot ? d_cot : nullptr,
                                      d_st, d_jd, d_jb, grad ? d_g : nullptr, (uint32_t*)c->errword.p, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
   int st = check_device_errors(c);
@@ -752,6 +862,106 @@ int pr_kerr_sensitivity_adjoint(pr_ctx* c, const double* rays, int64_t n, const 
   return kerr_sens_common(c, rays, n, basis, cotangent, nullptr, nullptr, nullptr, grad);
 }
 
+// Many jobs (scene object, camera, parameters, output) as one captured CUDA
+// graph: each job is the megakernel form (one render kernel + the ordered
+// chunk reduction) on its own branch of the graph, so small and large
+// frames overlap on the GPU; the graph is re-captured per call and updated
+// in place when its shape is unchanged.
+int pr_render_batch(pr_ctx* c, int n, const pr_job* jobs) {
+  if (!c) return PR_E_ARG;
+  if (n <= 0 || !jobs) return fail(c, PR_E_ARG, "empty batch");
+  if (n > 4096) return fail(c, PR_E_ARG, "at most 4096 jobs per batch");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
+  std::vector<RenderCfg> cfg((size_t)n);
+  std::vector<size_t> off((size_t)n + 1, 0);
+  uint64_t paths = 0;
+  for (int j = 0; j < n; j++) {
+    const pr_job& J = jobs[j];
+    if (!J.scene) return fail(c, PR_E_ARG, "job " + std::to_string(j) + ": null scene");
+    if (!J.rgb_dev) return fail(c, PR_E_ARG, "job " + std::to_string(j) + ": null output");
+    int st = prepare_render(c, &J.camera, &J.params, J.sample_offset, cfg[j], &J.scene->data);
+    if (st != PR_OK) return fail(c, st, "job " + std::to_string(j) + ": " + c->err);
+    // the batch fills the GPU with many jobs: fewer sample chunks per job
+    cfg[j].chunks = std::max(1, std::min(cfg[j].chunks, (int)std::ceil(2.0e5 / ((double)cfg[j].width * cfg[j].height))));
+    cfg[j].chunks = std::min(cfg[j].chunks, cfg[j].spp);
+    off[j + 1] = off[j] + (size_t)cfg[j].width * cfg[j].height * 3 * (size_t)cfg[j].chunks;
+    paths += (uint64_t)cfg[j].spp * cfg[j].width * cfg[j].height;
+  }
+  PR_CUDA(c, c->batch_partial.ensure(sizeof(float) * std::max<size_t>(off[n], 1)));
+  const int n_streams = std::min(n, 16);
+  while ((int)c->batch_streams.size() < n_streams) {
+    cudaStream_t st;
+    PR_CUDA(c, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    c->batch_streams.push_back(st);
+  }
+  while ((int)c->batch_events.size() < n_streams + 1) {
+    cudaEvent_t ev;
+    PR_CUDA(c, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    c->batch_events.push_back(ev);
+  }
+  PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
+  // capture: fork to the branch streams, one megakernel + reduce per job, join
+  cudaGraph_t graph = nullptr;
+  PR_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaEventRecord(c->batch_events[n_streams], c->stream);
+  for (int k = 0; k < n_streams && e == cudaSuccess; k++)
+    e = cudaStreamWaitEvent(c->batch_streams[k], c->batch_events[n_streams], 0);
+  float* part = (float*)c->batch_partial.p;
+  for (int j = 0; j < n && e == cudaSuccess; j++) {
+    const pr_job& J = jobs[j];
+    cudaStream_t st = c->batch_streams[j % n_streams];
+    const SceneObjData& sc = J.scene->data;
+    const int n3 = cfg[j].width * cfg[j].height * 3;
+    if (sc.kerr.enabled)
+      e = launch_kerr_render(sc.dev, sc.kerr, cfg[j], part + off[j], (uint32_t*)c->errword.p,
+                             (unsigned long long*)c->counters.p, st);
+    else
+      e = launch_megakernel(sc.dev, cfg[j], part + off[j], (uint32_t*)c->errword.p,
+                            (unsigned long long*)c->counters.p, st);
+    if (e == cudaSuccess) e = launch_reduce(part + off[j], J.rgb_dev, n3, cfg[j].chunks, J.accumulate, st);
+  }
+  for (int k = 0; k < n_streams && e == cudaSuccess; k++) {
+    e = cudaEventRecord(c->batch_events[k], c->batch_streams[k]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->batch_events[k], 0);
+  }
+  cudaError_t e2 = cudaStreamEndCapture(c->stream, &graph);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return cuda_fail(c, e != cudaSuccess ? e : e2, "batch capture");
+  }
+  bool updated = false;
+  if (c->batch_exec) {
+    cudaGraphExecUpdateResultInfo info;
+    updated = cudaGraphExecUpdate(c->batch_exec, graph, &info) == cudaSuccess;
+    if (!updated) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(c->batch_exec);
+      c->batch_exec = nullptr;
+    }
+  }
+  if (!updated) {
+    e = cudaGraphInstantiate(&c->batch_exec, graph, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      c->batch_exec = nullptr;
+      return cuda_fail(c, e, "batch graph instantiate");
+    }
+  }
+  cudaGraphDestroy(graph);
+  PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  PR_CUDA(c, cudaGraphLaunch(c->batch_exec, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  unsigned long long cnt[16];
+  PR_CUDA(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  int st = check_device_errors(c);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->stats = pr_render_stats{paths, cnt[1], cnt[2], cnt[3], ms, 2ull * (unsigned long long)n};
+  return st;
+}
+
 size_t pr_abi_sizeof(int which) {
   switch (which) {
     case 0: return sizeof(pr_medium);
@@ -760,6 +970,7 @@ size_t pr_abi_sizeof(int which) {
     case 3: return sizeof(pr_mesh);
     case 4: return sizeof(pr_kerr);
     case 5: return sizeof(pr_scene_desc);
+    case 9: return sizeof(pr_job);
     case 6: return sizeof(pr_camera);
     case 7: return sizeof(pr_render_params);
     case 8: return sizeof(pr_render_stats);

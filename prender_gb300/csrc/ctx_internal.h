@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/prender_gpu.h"
 #include "pr_internal.h"
@@ -31,18 +32,30 @@ struct DevBuf {
   }
 };
 
+// one uploaded scene: host build, device copies, device view
+struct SceneObjData {
+  HostScene host;
+  DevBuf ents, mats, nodes, tris, fnorm, kerr_tex;
+  DevScene dev{};
+  GKerr kerr{};
+  void release() {
+    for (DevBuf* b : {&ents, &mats, &nodes, &tris, &fnorm, &kerr_tex}) b->release();
+  }
+};
+
 }  // namespace pr
+
+struct pr_scene_obj {
+  pr::SceneObjData data;
+};
 
 struct pr_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;
-  pr::HostScene host;
+  pr::SceneObjData cur;  // the scene of pr_scene_upload
   bool scene_ready = false;
-  pr::DevScene dev{};
-  pr::DevBuf ents, mats, nodes, tris, fnorm, kerr_tex;
-  pr::GKerr kerr{};  // device copy of the black hole (texture pointer on the device)
   pr::DevBuf errword, counters;  // 4 bytes / 4 x u64
   pr::DevBuf partial, out, rays, ires, jres, dres;
   pr::DevBuf k_status, k_bl, k_dir, k_steps, k_ent, k_t;  // pr_kerr_trace staging
@@ -57,6 +70,14 @@ struct pr_ctx {
   unsigned int wf_slots = 0;
   cudaGraphExec_t wf_graph = nullptr;
   unsigned int wf_graph_slots = 0;
+  unsigned int wf_graph_trace_blocks = 0;
+  unsigned int tuned_slots = 0;      // autotuner's wavefront pool size (0: default)
+  unsigned int tuned_trace_bps = 0;  // autotuner's traversal blocks per SM (0: default)
+  // pr_render_batch
+  cudaGraphExec_t batch_exec = nullptr;
+  std::vector<cudaStream_t> batch_streams;
+  std::vector<cudaEvent_t> batch_events;
+  pr::DevBuf batch_partial;
   bool wf_graph_failed = false;
   pr::WfCtl* wf_host_ctl = nullptr;
   uint64_t wf_passes = 0;
@@ -65,6 +86,7 @@ struct pr_ctx {
 
 namespace pr {
 // CameraScreenPram + Run() set-up for one render call (capi.cu)
-int prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, uint64_t sample_offset, RenderCfg& g);
+int prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, uint64_t sample_offset, RenderCfg& g,
+                   const SceneObjData* scene = nullptr);
 int ctx_fail(pr_ctx* c, int code, const std::string& msg);
 }  // namespace pr

@@ -63,7 +63,7 @@ extern "C" int pr_render_dev_noalloc(pr_ctx* c, const pr_camera* cam, const pr_r
   if (!rgb_dev) return ctx_fail(c, PR_E_ARG, "null output");
   if (!p || p->mode != PR_MODE_MEGAKERNEL)
     return ctx_fail(c, PR_E_UNSUPPORTED, "pr_render_dev_noalloc renders the megakernel form only");
-  if (c->kerr.enabled) return ctx_fail(c, PR_E_UNSUPPORTED, "pr_render_dev_noalloc renders straight-ray scenes only");
+  if (c->cur.kerr.enabled) return ctx_fail(c, PR_E_UNSUPPORTED, "pr_render_dev_noalloc renders straight-ray scenes only");
   RenderCfg g;
   int st = prepare_render(c, cam, p, sample_offset, g);
   if (st != PR_OK) return st;
@@ -79,6 +79,7 @@ extern "C" int pr_render_dev_noalloc(pr_ctx* c, const pr_camera* cam, const pr_r
   g.chunks = std::max(1, std::min(g.chunks, (int)(room / (n3 * sizeof(float)))));
   cudaError_t e = cudaSetDevice(c->device);
   if (e != cudaSuccess) return ctx_fail(c, PR_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   unsigned char* base = nullptr;
   e = scratch_for_device(c->device, &base);
   if (e != cudaSuccess)
@@ -93,7 +94,7 @@ extern "C" int pr_render_dev_noalloc(pr_ctx* c, const pr_camera* cam, const pr_r
   } while (0)
   NA_CUDA(cudaMemsetAsync(base, 0, kNoAllocHeader, c->stream));
   NA_CUDA(cudaEventRecord(c->ev0, c->stream));
-  NA_CUDA(launch_megakernel(c->dev, g, partial, err, counters, c->stream));
+  NA_CUDA(launch_megakernel(c->cur.dev, g, partial, err, counters, c->stream));
   NA_CUDA(launch_reduce(partial, rgb_dev, (int)n3, g.chunks, accumulate, c->stream));
   NA_CUDA(cudaEventRecord(c->ev1, c->stream));
   uint32_t bits = 0;

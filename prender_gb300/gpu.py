@@ -122,6 +122,38 @@ class Context:
                                              _p(d_color), _p(d_em), C.byref(d_scale)))
         return dict(color=d_color, emission=d_em, emission_scale=d_scale.value)
 
+    def scene_object(self, scene) -> "SceneObject":
+        """An uploaded scene independent of upload() (for render_batch)."""
+        return SceneObject(self, scene)
+
+    def render_batch(self, jobs) -> None:
+        """Renders (scene_object, out_tensor, settings, camera, sample_offset)
+        jobs as one captured CUDA graph; out_tensor is a CUDA float32 tensor
+        (H, W, 3) per job (any object with data_ptr())."""
+        arr = (A.pr_job * len(jobs))()
+        for j, job in enumerate(jobs):
+            so, out = job[0], job[1]
+            settings = job[2] if len(job) > 2 and job[2] is not None else so.scene.settings
+            camera = job[3] if len(job) > 3 and job[3] is not None else so.scene.camera
+            arr[j].scene = so.h
+            arr[j].camera = camera.to_c()
+            arr[j].params = settings.to_c()
+            arr[j].rgb_dev = out.data_ptr()
+            arr[j].sample_offset = job[4] if len(job) > 4 else 0
+            arr[j].accumulate = 0
+        self._check(self.L.pr_render_batch(self.h, len(jobs), arr))
+
+    def autotune(self, scene=None, settings=None, camera=None) -> dict:
+        """Picks the wavefront pool size and traversal grid for this context
+        by timing one-sample frames (pr_autotune_wavefront)."""
+        scene = scene or self.scene
+        cam = (camera or scene.camera).to_c()
+        prm = (settings or scene.settings).to_c()
+        sl, bps, ms = C.c_int32(0), C.c_int32(0), C.c_double(0.0)
+        self._check(self.L.pr_autotune_wavefront(self.h, C.byref(cam), C.byref(prm), C.byref(sl), C.byref(bps),
+                                                 C.byref(ms)))
+        return dict(slots=sl.value, trace_blocks_per_sm=bps.value, frame_ms=ms.value)
+
     def kerr_trace(self, rays: np.ndarray) -> dict:
         """The Kerr branch of intersect_scene per ray (FP64 geodesics);
         status 0 background, 1 entity hit, 2 event horizon, 4 step underflow,
@@ -174,3 +206,21 @@ class Context:
         self._check(self.L.pr_last_render_stats(self.h, C.byref(s)))
         return dict(paths=s.paths, segments=s.segments, nodes_visited=s.nodes_visited, tri_tests=s.tri_tests,
                     device_ms=s.device_ms, kernel_launches=s.kernel_launches)
+
+
+class SceneObject:
+    """A scene uploaded as its own object (pr_scene_create)."""
+
+    def __init__(self, ctx: "Context", scene):
+        self.ctx = ctx
+        self.scene = scene
+        self._desc = scene.to_desc()
+        st = C.c_int(0)
+        self.h = ctx.L.pr_scene_create(ctx.h, self._desc.ptr(), C.byref(st))
+        if not self.h:
+            raise PrenderError(st.value, f"pr_scene_create failed: {ctx.L.pr_last_error(ctx.h).decode()}")
+
+    def release(self):
+        if self.h:
+            self.ctx.L.pr_scene_release(self.ctx.h, self.h)
+            self.h = None

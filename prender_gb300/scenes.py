@@ -188,6 +188,23 @@ def media_cornell(width: int = 128, height: int = 96, samples: int = 4, supersam
     return s
 
 
+def media_batch(n: int = 32, seed: int = 0, sizes=(128, 256, 384, 512, 768, 1024), samples: int = 16,
+                supersamples: int = 2, subdiv: int = 5):
+    """n Cornell variants for one batched launch: a homogeneous medium with
+    sigma_s U(0.05, 0.5), sigma_a 0.01 and HG g U(-0.6, 0.8) around a
+    20k-triangle displaced icosphere (subdiv 5), square images of uneven
+    sizes (128^2 .. 1024^2), 16 x 2^2 tent-filtered samples (64 spp)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        side = int(rng.choice(sizes))
+        s = media_cornell(side, side, samples, supersamples, sigma_s=float(rng.uniform(0.05, 0.5)), sigma_a=0.01,
+                          g=float(rng.uniform(-0.6, 0.8)), subdiv=subdiv, seed=seed)
+        s.settings.seed = seed + i
+        out.append(s)
+    return out
+
+
 def celestial_texture(width: int = 1024, height: int = 512, stars: int = 10000, seed: int = 0,
                       cells=(24, 12)) -> np.ndarray:
     """Procedural celestial sphere for the Kerr background map: a seeded

@@ -45,6 +45,7 @@ def test_struct_layouts_match(lib):
                A.pr_render_params, A.pr_render_stats]
     for i, s in enumerate(structs):
         assert lib.pr_abi_sizeof(i) == C.sizeof(s), s.__name__
+    assert lib.pr_abi_sizeof(9) == C.sizeof(A.pr_job)
     assert lib.pr_abi_version() == 1
 
 
