@@ -93,6 +93,8 @@ typedef struct pr_material {
   double roughness;        /* 'reflection diffuse' sets 1, 'specular' sets 0  */
   double refractive_index; /* default 1.5 (REFRACTIVE_INDEX_OF_GLASS)         */
   pr_medium medium;        /* used by the SSS material types                 */
+  double r_refractive_index; /* 'r_refractive_index' (relative index of the
+                                subsurface medium, default 1.0)               */
 } pr_material;
 
 /* One OBJECT block (scene_env.h:854-1851) after its transforms. */

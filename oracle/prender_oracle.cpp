@@ -61,6 +61,7 @@ struct Material {  // material.h:54-240
   V3 color, emission, specular;
   double roughness = 0.0;
   double refractive_index = 1.5;
+  double r_refractive_index = 1.0;  // relative index of the subsurface medium (material.h:81)
   Medium medium;
   // Material::isLight (material.h): diffuse, dark, emissive
   bool isLight() const {
@@ -126,6 +127,7 @@ struct Entity {
   double area = INF;
   bool light = false;
   int light_id = -1;
+  V3 bb_min, bb_max;  // Entity::boundingBox (CreateBoundingBox of the entity type)
 };
 
 struct Light {  // light.h:13-74 (area lights only)
@@ -536,6 +538,25 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
     m.specular = V3(pm.specular[0], pm.specular[1], pm.specular[2]);
     m.roughness = pm.roughness;
     m.refractive_index = pm.refractive_index;
+    m.r_refractive_index = pm.r_refractive_index;
+    if (m.type == PR_MAT_SSS_REFRACTION || m.type == PR_MAT_SSS_DIFFUSE || m.type == PR_MAT_SSS_WARD) {
+      // the material's own participatingMediaParam (scene_env.h:1305-1362); the
+      // entity set-up calls setup_Scattering when the SCATTERING line is > PS_EPS
+      Medium& md = m.medium;
+      md.scatteringColor = V3(pm.medium.sigma_s_rgb[0], pm.medium.sigma_s_rgb[1], pm.medium.sigma_s_rgb[2]);
+      md.absorbingColor = V3(pm.medium.sigma_a_rgb[0], pm.medium.sigma_a_rgb[1], pm.medium.sigma_a_rgb[2]);
+      for (int k = 0; k < 3; k++) md.phase[k] = pm.medium.phase_g[k];
+      md.r_max = pm.medium.r_max;
+      md.level = pm.medium.level;
+      md.use_bssrdf = pm.medium.use_bssrdf;
+      const double sc = (md.scatteringColor.x + md.scatteringColor.y + md.scatteringColor.z) / 3;
+      if (sc > EPS) md.setup(pm.medium.scale > 0.0 ? pm.medium.scale : 1.0);
+      if (m.type != PR_MAT_SSS_REFRACTION || md.level != -2 || !md.use_bssrdf) {
+        err = "subsurface scattering: only the directional-dipole form (reflection reflection + "
+              "Subsurface_Scattering, level -2) is on this path";
+        return PR_E_UNSUPPORTED;
+      }
+    }
     s.mats.push_back(m);
   }
   for (int i = 0; i < d->n_meshes; i++) {
@@ -583,6 +604,9 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
       e.position = V3(pe.p[0], pe.p[1], pe.p[2]);
       e.radius = pe.radius;
       e.area = FORPI * e.radius * e.radius;  // Sphere::CalcArea (sphere.h:23-27)
+      const V3 ext(e.radius, e.radius, e.radius), eps(0.01, 0.01, 0.01);  // sphere.h:58-63
+      e.bb_min = e.position - ext - eps;
+      e.bb_max = e.position + ext + eps;
     } else if (pe.type == PR_ENT_UVPLANE) {  // UVPlane ctor (plane.h:146-167)
       e.org = V3(pe.p[0], pe.p[1], pe.p[2]);
       V3 U(pe.u[0], pe.u[1], pe.u[2]), V(pe.v[0], pe.v[1], pe.v[2]);
@@ -594,6 +618,21 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
       // UVPlane::CalcArea (plane.h:174-177)
       e.area = length(e.u_axis * e.u_length) * length(e.v_axis * e.v_length) *
                (1.0 - std::pow(dot(e.u_axis, e.v_axis), 2.0));
+      {  // UVPlane::CreateBoundingBox (plane.h:191-215)
+        const V3 q[4] = {e.org, e.org + e.v_length * 1.0 * e.v_axis, e.org + e.u_length * 1.0 * e.u_axis,
+                         e.org + e.u_length * 1.0 * e.u_axis + e.v_length * 1.0 * e.v_axis};
+        V3 mn = q[0], mx = q[0];
+        for (int k = 1; k < 4; k++) {
+          if (mn.x > q[k].x) mn.x = q[k].x;
+          if (mn.y > q[k].y) mn.y = q[k].y;
+          if (mn.z > q[k].z) mn.z = q[k].z;
+          if (mx.x < q[k].x) mx.x = q[k].x;
+          if (mx.y < q[k].y) mx.y = q[k].y;
+          if (mx.z < q[k].z) mx.z = q[k].z;
+        }
+        e.bb_min = mn;
+        e.bb_max = mx;
+      }
     } else if (pe.type == PR_ENT_CIRCLE) {  // Circle ctor (circle.h:117-130)
       e.org = V3(pe.p[0], pe.p[1], pe.p[2]);
       e.radius = pe.radius;
@@ -630,6 +669,21 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
         e.tris.push_back(t);
       }
       if (nf == 0) { err = "empty mesh"; return PR_E_SCENE; }
+      {  // Polygon::CreateBoundingBox over the mesh vertices (polygon.h:875-889)
+        V3 mn(INF, INF, INF), mx(-INF, -INF, -INF);
+        for (size_t k = 0; k + 2 < mesh.vert.size(); k += 3) {
+          const V3 v(mesh.vert[k], mesh.vert[k + 1], mesh.vert[k + 2]);
+          if (mn.x > v.x) mn.x = v.x;
+          if (mn.y > v.y) mn.y = v.y;
+          if (mn.z > v.z) mn.z = v.z;
+          if (mx.x < v.x) mx.x = v.x;
+          if (mx.y < v.y) mx.y = v.y;
+          if (mx.z < v.z) mx.z = v.z;
+        }
+        const V3 eps(0.01, 0.01, 0.01);
+        e.bb_min = mn - eps;
+        e.bb_max = mx + eps;
+      }
       // QBVH::Construct (QBVH.cpp:161-186)
       Builder b(e.tris);
       b.nodes.emplace_back();
@@ -1017,6 +1071,241 @@ V3 media_radiance(Ctx& c, V3 org, V3 raydir, const Hit& hp, int ent, double p_rr
   return L;
 }
 
+// ---------------------------------------------------------------- BSSRDF
+// Directional dipole of Frisvad, Hachisuka and Kjeldsen, "Directional
+// Dipole Model for Subsurface Scattering" (ACM TOG 2014), as the reference
+// evaluates it (bssrdf.h:48-248), and the dipole branch of BRDF_SSS2_
+// (Subsurface_Scattering.h:630-1181) for level -2 materials.
+double dd_C1(double n) {  // 2 C1 / 2 of the paper's moment polynomials (bssrdf.h:48-61)
+  double r;
+  if (n > 1.0) r = -9.23372 + n * (22.2272 + n * (-20.9292 + n * (10.2291 + n * (-2.54396 + 0.254913 * n))));
+  else r = 0.919317 + n * (-3.4793 + n * (6.75335 + n * (-7.80989 + n * (4.98554 - 1.36881 * n))));
+  return r / 2.0;
+}
+double dd_C2(double n) {  // bssrdf.h:63-67
+  double r = -1641.1 + n * (1213.67 + n * (-568.556 + n * (164.798 + n * (-27.0181 + 1.91826 * n))));
+  r += (((135.926 / n) - 656.175) / n + 1376.53) / n;
+  return r / 3.0;
+}
+inline V3 vsqrt(V3 a) { return V3(std::sqrt(a.x), std::sqrt(a.y), std::sqrt(a.z)); }
+inline V3 vdiv(V3 a, V3 b) { return V3(a.x / b.x, a.y / b.y, a.z / b.z); }
+inline double vmin(V3 a) {  // Vector3d::Min
+  double m = a.x;
+  if (m > a.y) m = a.y;
+  if (m > a.z) m = a.z;
+  return m;
+}
+inline double comp(V3 a, int j) { return j == 0 ? a.x : (j == 1 ? a.y : a.z); }
+
+struct Dipole {  // DirectionalDipole (bssrdf.h:75-128)
+  V3 sigma_s, sigma_a, sigma_t, sigma_sp, sigma_tp, albedo_p, D, sigma_tr, de;
+  double Cp, Ce, A, eta;
+  Dipole(const Material& m, double eta_) {
+    eta = eta_;
+    sigma_a = m.medium.absorbingColor;
+    sigma_s = m.medium.scatteringColor;
+    sigma_t = sigma_s + sigma_a;
+    sigma_sp = sigma_s * (V3(1.0, 1.0, 1.0) - V3(m.medium.phase[0], m.medium.phase[1], m.medium.phase[2]));
+    sigma_tp = sigma_sp + sigma_a;
+    albedo_p = vdiv(sigma_sp, sigma_tp);
+    D = vdiv(V3(1.0, 1.0, 1.0), 3.0 * sigma_tp);
+    sigma_tr = vsqrt(vdiv(sigma_a, D));
+    de = vdiv(2.131 * D, vsqrt(albedo_p));
+    Cp = (1.0 - 2.0 * dd_C1(eta)) / 4.0;
+    Ce = (1.0 - 3.0 * dd_C2(eta)) / 2.0;
+    A = (1.0 - Ce) / (2.0 * Cp);
+  }
+};
+
+// Sp_d (bssrdf.h:131-172)
+double dd_sp(const Dipole& dd, V3 x, V3 w, double r, V3 n0, int j) {
+  const double s_tr_r = comp(dd.sigma_tr, j) * r;
+  const double s_tr_r_one = 1.0 + s_tr_r;
+  const double x_dot_w = dot(x, w);
+  const double r_sqr = r * r;
+  const double exp_tr = std::exp(-s_tr_r);
+  const double t0 = 1.0 / (4.0 * dd.Cp) * (0.02533029591058444286096986580243191) * exp_tr / (r * r_sqr);
+  const double t1 = r_sqr / comp(dd.D, j) + 3.0 * s_tr_r_one * x_dot_w;
+  const double t2 = 3.0 * comp(dd.D, j) * s_tr_r_one * dot(w, n0);
+  const double t3 = (s_tr_r_one + 3.0 * comp(dd.D, j) * (3.0 * s_tr_r_one + s_tr_r * s_tr_r) / r_sqr * x_dot_w) * dot(x, n0);
+  return t0 * (dd.Cp * t1 - dd.Ce * (t2 - t3));
+}
+
+// bssrdf (bssrdf.h:188-236)
+double dd_bssrdf(const Dipole& dd, V3 xi, V3 ni, V3 wi, V3 xo, V3 no, V3 wo, int j) {
+  (void)wo;
+  const V3 xoxi = xo - xi;
+  const double r = length(xoxi);
+  V3 ni_s = cross(normalize(xoxi), normalize(cross(ni, xoxi)));
+  if (r < 1.0e-8) ni_s = ni;
+  const double nnt = 1.0 / dd.eta, ddn = -dot(wi, ni);
+  const V3 w12 = normalize(wi * -nnt - ni * (ddn * nnt + std::sqrt(1.0 - nnt * nnt * (1.0 - ddn * ddn))));
+  const V3 wv = w12 - ni_s * (2.0 * dot(w12, ni_s));
+  const double dej = comp(dd.de, j), Dj = comp(dd.D, j);
+  const double cos_beta = -std::sqrt((r * r - dot(xoxi, w12) * dot(xoxi, w12)) / (r * r + dej * dej));
+  double dr;
+  const double mu0 = -dot(no, w12);
+  if (mu0 > 0.0) {
+    double tmp = (Dj * mu0) * ((Dj * mu0) - dej * cos_beta * 2.0) + r * r;
+    if (tmp < 0) tmp = 0.0;
+    dr = std::sqrt(tmp);
+  } else {
+    const double st = comp(dd.sigma_t, j);
+    double tmp = 1.0 / (3.0 * st * 3.0 * st) + r * r;
+    if (tmp < 0) tmp = 0.0;
+    dr = std::sqrt(tmp);
+  }
+  const V3 xoxv = xo - (xi + ni_s * (2.0 * dd.A * dej));
+  const double dv = length(xoxv);
+  const double result = dd_sp(dd, xoxi, w12, dr, no, j) - dd_sp(dd, xoxv, wv, dv, no, j);
+  return (result < 0.0) ? 0.0 : result;
+}
+
+// fresnel (bssrdf.h:239-247)
+double dd_fresnel(double cos_theta, double eta) {
+  const double sin_theta_t_sqr = 1.0 / (eta * eta) * (1.0 - cos_theta * cos_theta);
+  if (sin_theta_t_sqr >= 1.0) return 1.0;
+  const double cos_theta_t = std::sqrt(1.0 - sin_theta_t_sqr);
+  const double r_s = (cos_theta - eta * cos_theta_t) / (cos_theta + eta * cos_theta_t);
+  const double r_p = (eta * cos_theta - cos_theta_t) / (eta * cos_theta + cos_theta_t);
+  return (r_s * r_s + r_p * r_p) * 0.5;
+}
+
+// gaussianSample2D / gaussianSample2DPdf (Subsurface_Scattering.h:612-628)
+V3 gauss_sample_2d(double u1, double u2, double falloff, double rmax) {
+  const double r = std::sqrt(std::log(1.0 - u1 * (1.0 - std::exp(-falloff * rmax * rmax))) / -falloff);
+  const double theta = TWOPI * u2;
+  return V3(r * std::cos(theta), r * std::sin(theta), 0);
+}
+double gauss_pdf_2d(V3 pc, V3 ps, V3 N, double falloff, double rmax) {
+  const V3 d = ps - pc;
+  const V3 projected = d - N * dot(d, N);
+  const double pdf = falloff * std::exp(-falloff * sqr(projected)) / PI;
+  return pdf / (1.0f - std::exp(-falloff * rmax * rmax));
+}
+
+V3 radiance(Ctx& c, V3 org, V3 dir, int depth);
+V3 direct_sample(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, int depth);
+V3 brdf_refraction(Ctx& c, V3 raydir, const Hit& hp, int mat_type, V3 on, double p_rr, double p_scat, int depth);
+const Light& random_light(Ctx& c);
+bool inside_dir(V3 normal, V3 raydir);
+
+// BRDF_SSS2_ (Subsurface_Scattering.h:630-1181) for level -2: Gaussian-disk
+// probe rays for the exit point, the directional dipole, NEE at the exit,
+// or (accept 0.5) the Fresnel-surface refraction; raydir is the refracted
+// direction radiance() passes in
+V3 brdf_sss2(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, double p_scat, int depth) {
+  const Scene& s = c.s;
+  const Material& hm = s.mats[hp.material];
+  const bool ins = inside_dir(hp.normal, raydir);
+  V3 emission = hm.emission;
+  V3 trr(1, 1, 1);
+  if (c.media) trr = s.medium.tr(hp.distance);
+  const double eta = hm.r_refractive_index;
+  const Dipole dd(hm, eta);
+  const Entity& obj = s.ents[ent];
+  const Medium& pm = s.mats[obj.material].medium;
+  V3 incoming, weight(1, 1, 1), direct;
+  Hit out = hp;
+  out.object_id = ent;
+  double samplePDF = 1.0, sampleDir = 1.0;
+  const int sampleN = 40;
+  int err = 1;
+  // samplingType 2 (Gaussian disk), rmax heuristic (:701-714)
+  double sigmaTr = vmin(dd.sigma_tp);
+  const double sigmaTrCoef = 0.001;
+  double rmax;
+  {
+    const double skipRatio = 1.0e-4;
+    const double x = vmin(pm.scatteringColor);
+    double y = 2.0 - 1.0 / (1.0 + std::exp(-4.0 * (x - 1.6)));
+    if (pm.absorbing < 0.001) y *= 1.3 - std::exp(vmin(pm.absorbingColor) * 1000.0);
+    rmax = 1.25 * std::sqrt(std::log(skipRatio) / -sigmaTr) * y * pm.r_max;
+  }
+  const double ln = length(obj.bb_max - obj.bb_min);
+  if (rmax > ln) rmax = ln * 0.3;
+  const double step = 0.5 * rmax / sampleN;
+  V3 on2, dir;
+  for (int i = sampleN; i >= 1; i--) {
+    err = 1;
+    V3 ww, u, v;
+    onb(on, ww, u, v);
+    // g++ evaluates 'gaussianSample2D(rnd->next01(), rnd->next01(), ...)'
+    // right to left: the second argument draws first
+    const double u2 = c.rnd.next01();
+    const double u1 = c.rnd.next01();
+    const V3 pSample = gauss_sample_2d(u1, u2, sigmaTr * sigmaTrCoef, rmax);
+    const V3 p = hp.position + pSample.x * u + pSample.y * v;
+    const double halfProbeLength = i * step;
+    // intersect_scene ignores its target id: the probe takes the closest hit
+    if (!intersect(s, p - on * halfProbeLength, on, out)) continue;
+    on2 = out.normal;
+    samplePDF = gauss_pdf_2d(V3(0, 0, 0), pSample, V3(0, 0, 1), sigmaTr * sigmaTrCoef, rmax);
+    if (dot(hp.normal, on) < 0) on2 = -1.0 * on2;
+    onb(on2, ww, u, v);
+    const double r1 = TWOPI * c.rnd.next01();
+    const double r2 = c.rnd.next01(), r2s = std::sqrt(r2);
+    dir = normalize((u * std::cos(r1) * r2s + v * std::sin(r1) * r2s + ww * std::sqrt(1.0 - r2)));
+    sampleDir = dot(on2, dir) * INV_PI;
+    if (sampleDir > 0) {
+      err = 0;
+      break;
+    }
+  }
+  if (err) return V3();
+  const V3 w = -1.0 * raydir, x = hp.position, n = on;
+  const V3 sw = dir, sp = out.position, sn = on2;
+  const double cos_wi_n = dot(sn, sw);
+  if (cos_wi_n < 0.0) return V3();
+  const double T21 = std::max(1.0 - dd_fresnel(dot(w, n), eta), 0.0);
+  const double T12 = std::max(1.0 - dd_fresnel(cos_wi_n, eta), 0.0);
+  double accept_prob = 0.5;
+  const bool into = dot(hp.normal, on) > 0.0;
+  if (!into) accept_prob = 0;
+  if (c.rnd.next01() < accept_prob) {
+    double pms = 0.5;
+    if (pm.level == -2) pms = 1;
+    if (c.rnd.next01() < pms) {
+      V3 result;
+      result.x = dd_bssrdf(dd, sp, sn, sw, x, n, w, 0);
+      result.y = dd_bssrdf(dd, sp, sn, sw, x, n, w, 1);
+      result.z = dd_bssrdf(dd, sp, sn, sw, x, n, w, 2);
+      weight = hm.color * T12 * result * cos_wi_n * T21 / samplePDF / sampleDir / accept_prob / p_rr /
+               (1.0 - p_scat) / pms;
+      incoming = radiance(c, sp, sw, depth + 1);
+      if (c.nee && !s.lights.empty()) {
+        for (int k = 0; k < 3; k++) {
+          const Light& l = random_light(c);
+          direct = direct + direct_sample(c, l, out, on2, depth) / 1.0;
+        }
+        direct = direct / 3;
+        direct = direct * T12 * result * cos_wi_n * T21 / samplePDF / sampleDir / accept_prob / p_rr /
+                 (1.0 - p_scat);
+      }
+      if (!c.nee && !s.lights.empty()) {
+        for (int k = 0; k < 3; k++) (void)random_light(c);
+        direct = direct / 3;
+        direct = direct * T12 * result * cos_wi_n * T21 / samplePDF / sampleDir / accept_prob / p_rr /
+                 (1.0 - p_scat);
+      }
+      if (length(incoming * weight) > 100) return V3();  // OVER_RADIANCE_CUT2
+    }
+  } else {
+    V3 Tr(1, 1, 1);
+    if (!into) Tr = pm.tr(hp.distance);
+    weight = Tr / (1.0 - accept_prob);
+    incoming = brdf_refraction(c, raydir, hp, PR_MAT_REFRACTION, on, p_rr, p_scat, depth);
+    if (length(incoming * weight) > 200) return V3();  // OVER_RADIANCE_CUT3
+    direct = V3();
+  }
+  if (c.media && ins) {
+    direct = trr * direct;
+    emission = trr * emission;
+    incoming = trr * incoming;
+  }
+  return s.env_light + emission + direct + weight * incoming;
+}
+
 // Kerr branch of intersect_scene (defined with the Kerr restatement below);
 // on a miss, miss_color is what radiance() returns for it (radiance.h:30-43)
 bool kerr_query(const Scene& s, V3 org, V3 dir, Hit& hit, V3& miss_color);
@@ -1070,6 +1359,23 @@ V3 radiance(Ctx& c, V3 org, V3 dir, int depth) {
     case PR_MAT_REFRACTION:
     case PR_MAT_REFRACTION_FRESNEL:
       return brdf_refraction(c, dir, hp, mat.type, on, p_rr, p_scat, depth);
+    case PR_MAT_SSS_REFRACTION: {
+      // radiance.h:154-224 (use_brssdf, level -2): refract into the object,
+      // then the dipole (BRDF_SSS2) with the refracted direction
+      const bool into = dot(hp.normal, on) > 0.0;
+      const double nc = 1.0;
+      const double nt = mat.refractive_index;
+      const double nnt = into ? nc / nt : nt / nc;
+      const double ddn = dot(dir, on);
+      const double cos2t = 1.0 - nnt * nnt * (1.0 - ddn * ddn);
+      V3 tdir = normalize(dir * nnt - hp.normal * (into ? 1.0 : -1.0) * (ddn * nnt + std::sqrt(std::fabs(cos2t))));
+      if (cos2t < 0) tdir = normalize(dir - on * 2.0 * dot(on, dir));
+      V3 tr(1, 1, 1);
+      if (!into) tr = mat.medium.tr(hp.distance);
+      const double probability = 1;
+      (void)c.rnd.next01();  // 'if (rnd->next01() < probability)' with probability 1
+      return tr * brdf_sss2(c, tdir, hp, hp.object_id, on, p_rr, p_scat, depth) / probability;
+    }
     default:
       return V3();
   }

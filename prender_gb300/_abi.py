@@ -65,6 +65,7 @@ class pr_material(C.Structure):
         ("roughness", C.c_double),
         ("refractive_index", C.c_double),
         ("medium", pr_medium),
+        ("r_refractive_index", C.c_double),
     ]
 
 

@@ -156,6 +156,8 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   }
   S.medium = h.medium;
   S.scene_scale = h.scene_scale;
+  S.has_sss = 0;
+  for (const GMaterial& gm : h.mats) S.has_sss |= gm.sss;
   for (int k = 0; k < 3; k++) {
     S.bg[k] = (float)h.background[k];
     S.env[k] = (float)h.env_light[k];
@@ -179,6 +181,7 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
     f.area = (float)e.area;
     f.face_base = e.face_base;
     f.node_base = e.node_base;
+    f.sss_rmax = (float)e.sss_rmax;
   }
   return PR_OK;
 }
@@ -353,6 +356,9 @@ int pr::prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* 
                 "UVPlane axes randomPoint reads, circle.h:110-134); render it without next-event estimation");
   if (sc.kerr.enabled && (p->nee || (p->media && sc.host.medium.on)))
     return fail(c, PR_E_UNSUPPORTED, "Kerr scenes render without next-event estimation and media");
+  if (sc.dev.has_sss && (p->mode == PR_MODE_WAVEFRONT || sc.kerr.enabled))
+    return fail(c, PR_E_UNSUPPORTED,
+                "subsurface (dipole) materials render in the plain form (PR_MODE_MEGAKERNEL) of straight-ray scenes");
   memset(&g, 0, sizeof(g));
   double dir[3] = {cam->dir[0], cam->dir[1], cam->dir[2]};
   double phi = std::atan2(dir[1], dir[0]);
@@ -610,6 +616,7 @@ static int adjoint_checks(pr_ctx* c, const pr_render_params* p) {
   if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
   if (c->cur.kerr.enabled) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass traces straight rays only");
   if (p && p->media && c->cur.host.medium.on) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover media");
+  if (c->cur.dev.has_sss) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover subsurface materials");
   if ((int)c->cur.host.mats.size() > kAdjMaterials)
     return fail(c, PR_E_UNSUPPORTED, "the adjoint pass tracks at most " + std::to_string(kAdjMaterials) + " materials");
   return PR_OK;

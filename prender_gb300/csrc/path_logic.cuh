@@ -208,13 +208,70 @@ __device__ __forceinline__ void root_path(PathState& ps, float3 o, float3 d) {
   ps.dp = 0;
 }
 
-// Shades the vertex found by the last closest-hit query of ps.  A tracer
+// A subsurface vertex whose continuation the reference drops when
+// |weight * incoming| exceeds a bound (OVER_RADIANCE_CUT2 / 3,
+// Subsurface_Scattering.h:19-22): the caller accumulates the continuation
+// and applies the bound when the continuation (all its branches) is done.
+struct SssFrameOut {
+  int open;
+  float3 scale;  // path contributions = scale * (weight * incoming)
+  float thr;
+};
+
+// fresnel (bssrdf.h:239-247)
+__device__ __forceinline__ float dd_fresnel(float cos_theta, float eta) {
+  const float s2 = 1.0f / (eta * eta) * (1.0f - cos_theta * cos_theta);
+  if (s2 >= 1.0f) return 1.0f;
+  const float ct = sqrtf(1.0f - s2);
+  const float rs = (cos_theta - eta * ct) / (cos_theta + eta * ct);
+  const float rp = (eta * cos_theta - ct) / (eta * cos_theta + ct);
+  return (rs * rs + rp * rp) * 0.5f;
+}
+
+// Sp_d (bssrdf.h:131-172), channel j
+__device__ __forceinline__ float dd_sp(const GMaterial& m, float3 x, float3 w, float r, float3 n0, int j) {
+  const float str = m.sss_sigma_tr[j] * r, one = 1.0f + str, xw = dot(x, w), r2 = r * r, D = m.sss_D[j];
+  const float t0 = 1.0f / (4.0f * m.sss_Cp) * 0.025330295910584444f * expf(-str) / (r * r2);
+  const float t1 = r2 / D + 3.0f * one * xw;
+  const float t2 = 3.0f * D * one * dot(w, n0);
+  const float t3 = (one + 3.0f * D * (3.0f * one + str * str) / r2 * xw) * dot(x, n0);
+  return t0 * (m.sss_Cp * t1 - m.sss_Ce * (t2 - t3));
+}
+
+// bssrdf (bssrdf.h:188-236) of the directional dipole (Frisvad, Hachisuka and
+// Kjeldsen, ACM TOG 2014), entry (xi, ni, wi), exit (xo, no), channel j
+__device__ __forceinline__ float dd_bssrdf(const GMaterial& m, float3 xi, float3 ni, float3 wi, float3 xo, float3 no,
+                                           int j) {
+  const float3 xoxi = xo - xi;
+  const float r = sqrtf(dot(xoxi, xoxi));
+  float3 ni_s = r < 1.0e-8f ? ni : cross(xoxi / r, normalize(cross(ni, xoxi)));
+  const float nnt = 1.0f / m.sss_eta, ddn = -dot(wi, ni);
+  const float3 w12 = normalize(wi * -nnt - ni * (ddn * nnt + sqrtf(fmaxf(0.0f, 1.0f - nnt * nnt * (1.0f - ddn * ddn)))));
+  const float3 wv = w12 - ni_s * (2.0f * dot(w12, ni_s));
+  const float de = m.sss_de[j], D = m.sss_D[j];
+  const float xw = dot(xoxi, w12);
+  const float cos_beta = -sqrtf(fmaxf(0.0f, (r * r - xw * xw) / (r * r + de * de)));
+  const float mu0 = -dot(no, w12);
+  float dr;
+  if (mu0 > 0.0f) dr = sqrtf(fmaxf(0.0f, (D * mu0) * ((D * mu0) - de * cos_beta * 2.0f) + r * r));
+  else dr = sqrtf(fmaxf(0.0f, 1.0f / (3.0f * m.sss_sigma_t[j] * 3.0f * m.sss_sigma_t[j]) + r * r));
+  const float3 xoxv = xo - (xi + ni_s * (2.0f * m.sss_A * de));
+  const float dv = sqrtf(dot(xoxv, xoxv));
+  const float res = dd_sp(m, xoxi, w12, dr, no, j) - dd_sp(m, xoxv, wv, dv, no, j);
+  return res < 0.0f ? 0.0f : res;
+}
+
+// Shades the vertex found by the last closest-hit query of ps (SSS: with the
+// subsurface material case compiled in; scenes without it use the leaner
+// instantiation).  A tracer
 // that builds the vertex itself (the Kerr geodesic tracer) passes it as pre,
 // and the colour a miss returns as miss (radiance.h:30-43); straight-ray
 // callers leave both null.
+template <bool SSS = false>
 __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& ps, bool hit, const FastHit& h,
                      uint64_t sample_id, ShadowReq* sh, int& nsh, PathState& child, uint32_t* err,
-                     const Vertex* pre = nullptr, const float3* miss = nullptr, EmissionTap* tap = nullptr) {
+                     const Vertex* pre = nullptr, const float3* miss = nullptr, EmissionTap* tap = nullptr,
+                     SssFrameOut* frame = nullptr) {
   nsh = 0;
   const bool nee = cfg.nee != 0;
   const bool media = cfg.media != 0 && S.medium.on != 0;
@@ -326,8 +383,9 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     }
   }
   const float inv_rr = 1.0f / p_rr / (1.0f - p_scat);
-  int kind;  // 0 diffuse, 1 specular, 2 glass
-  if (m.type == PR_MAT_DIFFUSE) kind = (rng.next() < m.roughness) ? 0 : 1;
+  int kind;  // 0 diffuse, 1 specular, 2 glass, 3 subsurface (directional dipole)
+  if (SSS && m.sss) kind = 3;
+  else if (m.type == PR_MAT_DIFFUSE) kind = (rng.next() < m.roughness) ? 0 : 1;
   else if (m.type == PR_MAT_SPECULAR) kind = (rng.next() < 1.0f - m.roughness) ? 1 : 0;
   else kind = 2;
   const float3 tri = (media && entering) ? trr : f3(1, 1, 1);
@@ -409,12 +467,133 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     ps.draws = rng_draws(rng);
     return SHADE_CONTINUE;
   }
+  float3 dg = d;  // the direction BRDF_Refraction sees (the subsurface branch passes the refracted one)
+  if (SSS && kind == 3) {
+    // ---- subsurface scattering, level -2 (radiance.h:154-224): refract into
+    // the object, then BRDF_SSS2_ (Subsurface_Scattering.h:630-1181) with the
+    // refracted direction
+    const bool into_s = dot(v.n, on) > 0.0f;
+    const float nts = m.ior, nnts = into_s ? 1.0f / nts : nts;
+    const float ddns = dot(d, on);
+    const float cos2ts = 1.0f - nnts * nnts * (1.0f - ddns * ddns);
+    const float3 ts = cos2ts < 0.0f
+                          ? normalize(d - on * (2.0f * dot(on, d)))
+                          : normalize(d * nnts - v.n * ((into_s ? 1.0f : -1.0f) * (ddns * nnts + sqrtf(fabsf(cos2ts)))));
+    const float3 mtr = f3(expf(-m.sss_tr[0] * v.t), expf(-m.sss_tr[1] * v.t), expf(-m.sss_tr[2] * v.t));
+    if (!into_s) ps.beta = ps.beta * mtr;  // leaving: attenuated over the segment inside
+    // exit point: Gaussian-disk probes along the orienting normal, at most 40 (:729-806)
+    float3 tu, tv;
+    onb(on, tu, tv);
+    const float rmax = ent.sss_rmax, fall = m.sss_falloff;
+    const float norm = 1.0f - expf(-fall * rmax * rmax);
+    const float step = 0.5f * rmax / 40.0f;
+    bool found = false;
+    float3 sp = v.p, on2 = on, sw = on;
+    float pdf_s = 1.0f, pdf_d = 1.0f;
+    int exit_mat = v.mat;
+    for (int i = 40; i >= 1 && !found; i--) {
+      const float u1 = rng.next(), u2 = rng.next();
+      const float r = sqrtf(logf(1.0f - u1 * norm) / -fall);
+      float sn, cs;
+      sincosf(6.28318530717958647692f * u2, &sn, &cs);
+      const float px = r * cs, py = r * sn;
+      const float3 po = v.p + tu * px + tv * py - on * ((float)i * step);
+      FastHit ph;
+      TraceStats pst{0, 0};
+      if (!fast_closest(S, po, on, ph, pst, err)) continue;
+      Vertex pv;
+      make_vertex(S, po, on, ph, pv);
+      float3 n2 = pv.n;
+      if (dot(v.n, on) < 0.0f) n2 = -n2;
+      float3 a2, b2;
+      onb(n2, a2, b2);
+      const float r1 = 6.28318530717958647692f * rng.next();
+      const float r2 = rng.next(), r2s = sqrtf(r2);
+      float sn1, cs1;
+      sincosf(r1, &sn1, &cs1);
+      const float3 dir = normalize(a2 * (cs1 * r2s) + b2 * (sn1 * r2s) + n2 * sqrtf(1.0f - r2));
+      const float sd = dot(n2, dir) * 0.31830988618379067154f;
+      if (sd > 0.0f) {
+        found = true;
+        sp = pv.p;
+        on2 = n2;
+        sw = dir;
+        exit_mat = pv.mat;
+        pdf_s = fall * expf(-fall * (px * px + py * py)) * 0.31830988618379067154f / norm;
+        pdf_d = sd;
+      }
+    }
+    const float cos_wi_n = dot(on2, sw);
+    if (!found || cos_wi_n < 0.0f) {  // BRDF_SSS2_ returns zero
+      ps.draws = rng_draws(rng);
+      return SHADE_END;
+    }
+    const float3 wi = -ts;
+    const float T21 = fmaxf(1.0f - dd_fresnel(dot(wi, on), m.sss_eta), 0.0f);
+    const float T12 = fmaxf(1.0f - dd_fresnel(cos_wi_n, m.sss_eta), 0.0f);
+    const float accept = into_s ? 0.5f : 0.0f;
+    ps.L += ps.beta * (env + tri * E);
+    if (rng.next() < accept) {
+      // multiple scattering through the dipole, exit at sp towards sw
+      const float3 res = f3(dd_bssrdf(m, sp, on2, sw, v.p, on, 0), dd_bssrdf(m, sp, on2, sw, v.p, on, 1),
+                            dd_bssrdf(m, sp, on2, sw, v.p, on, 2));
+      const float k = T12 * cos_wi_n * T21 / pdf_s / pdf_d / accept / p_rr / (1.0f - p_scat);
+      const float3 origin_s = offset_ray(sp, on2);
+      if (S.n_lights > 0 && nee) {
+        // direct_radiance_sample at the exit point (the exit object's colour / pi), 3 samples averaged
+        const float3 wn = ps.beta * tri * res * (k * (1.0f / 3.0f)) * ld3(S.mats[exit_mat].color) *
+                          0.31830988618379067154f;
+        for (int i = 0; i < 3; i++) {
+          const GEntF& le = pick_light(S, rng);
+          const float3 lp = sample_light(le, rng, true);
+          const float3 ln = light_normal(le, lp, true);
+          const float3 dl = lp - sp;
+          const float dist2 = dot(dl, dl);
+          const float3 ldir = dl / sqrtf(dist2);
+          const float dot0 = dot(on2, ldir), dot1 = -dot(ln, ldir);
+          if (dot0 >= 0.0f && dot1 >= 0.0f) {
+            const float3 dlo = lp - origin_s;
+            const float disto = sqrtf(dot(dlo, dlo));
+            const float3 em = ld3(S.mats[le.material].emission);
+            const float3 ew = wn * (dot0 * dot1 / dist2 * le.area);
+            sh[nsh].o = origin_s;
+            sh[nsh].d = dlo / disto;
+            sh[nsh].tmax = disto - 1.0e-3f;
+            sh[nsh].contrib = ew * em;
+            sh[nsh].ew = ew;
+            sh[nsh].lmat = le.material;
+            nsh++;
+          }
+        }
+      }
+      if (frame) {
+        frame->open = 1;
+        frame->scale = ps.beta * tri;
+        frame->thr = 100.0f;  // OVER_RADIANCE_CUT2
+      }
+      ps.beta = ps.beta * tri * C * res * k;
+      ps.o = origin_s;
+      ps.d = sw;
+      ps.depth++;
+      ps.draws = rng_draws(rng);
+      return SHADE_CONTINUE;
+    }
+    // Fresnel-surface refraction at the same point along the refracted
+    // direction (:1080-1160): BRDF_Refraction weighted Tr / (1 - accept)
+    if (frame) {
+      frame->open = 1;
+      frame->scale = ps.beta * tri;
+      frame->thr = 200.0f;  // OVER_RADIANCE_CUT3
+    }
+    ps.beta = ps.beta * tri * (into_s ? f3(1, 1, 1) : mtr) * (1.0f / (1.0f - accept));
+    dg = ts;
+  }
   // ---- BRDF_Refraction (brdf.h:763-953)
-  const float3 refl = normalize(d - v.n * (2.0f * dot(v.n, d)));
+  const float3 refl = normalize(dg - v.n * (2.0f * dot(v.n, dg)));
   const bool into = dot(v.n, on) > 0.0f;
   const float nt = m.ior;
   const float nnt = into ? 1.0f / nt : nt;
-  const float ddn = dot(d, on);
+  const float ddn = dot(dg, on);
   const float cos2t = 1.0f - nnt * nnt * (1.0f - ddn * ddn);
   ps.L += ps.beta * (env + tri * E);
   if (tap) tap->em(v.mat, ps.beta * tri);
@@ -430,7 +609,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     ps.draws = rng_draws(rng);
     return SHADE_CONTINUE;
   }
-  const float3 tdir = normalize(d * nnt - v.n * ((into ? 1.0f : -1.0f) * (ddn * nnt + sqrtf(fabsf(cos2t)))));
+  const float3 tdir = normalize(dg * nnt - v.n * ((into ? 1.0f : -1.0f) * (ddn * nnt + sqrtf(fabsf(cos2t)))));
   const float a = nt - 1.0f, bb = nt + 1.0f;
   const float R0 = (a * a) / (bb * bb);
   const float c = 1.0f - (into ? -ddn : dot(tdir, -on));

@@ -49,6 +49,15 @@ struct GMaterial {
   double emission_d[3];
   double roughness_d;
   double ior_d;
+  // directional dipole of a level -2 subsurface material (bssrdf.h:75-128),
+  // from the material's own medium after setup_Scattering
+  int32_t sss;             // 1: PR_MAT_SSS_REFRACTION with the dipole
+  float sss_eta;           // r_refractive_index
+  float sss_Cp, sss_Ce, sss_A;
+  float sss_sigma_tr[3], sss_D[3], sss_de[3], sss_sigma_t[3];
+  float sss_falloff;       // Gaussian-disk falloff: min(sigma_t') * 0.001
+  float sss_rmax0;         // probe-disk radius before the object-size clamp
+  float sss_tr[3];         // the medium's transmittanceColor (exit attenuation)
 };
 
 struct GEntity {
@@ -70,6 +79,8 @@ struct GEntity {
   int32_t face_base;       // first face-normal record of this mesh
   int32_t n_faces;
   float bmin[3], bmax[3];  // bounds (for scene extents)
+  double bb_min[3], bb_max[3];  // Entity::boundingBox of the reference (sphere / mesh / uvplane)
+  double sss_rmax;
 };
 
 // FP32 copy of an entity for the render path (no FP64 conversions in the
@@ -84,7 +95,9 @@ struct GEntF {
   float v_length;
   float n[3];
   float area;
-  int32_t face_base, node_base, pad0, pad1;
+  int32_t face_base, node_base;
+  float sss_rmax;  // subsurface probe-disk radius for this object (its bounding-box clamp applied)
+  int32_t pad1;
   // disk: u_length = radius, v_length = inner radius, n = the plane normal
 };
 
@@ -130,6 +143,7 @@ struct DevScene {
   float env[3];
   GMedium medium;
   float scene_scale;       // max |coordinate| of the scene bounds
+  int32_t has_sss;         // a subsurface (dipole) material is present
   GEntF entf[kMaxEntities];
 };
 

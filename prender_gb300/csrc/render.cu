@@ -14,15 +14,54 @@
 
 namespace pr {
 
+// Subsurface continuations whose radiance the reference bounds
+// (OVER_RADIANCE_CUT2 / 3): frame f collects its continuation's
+// contributions C over all branches inside it; when its last branch ends,
+// C (and the vertex's own emission and direct terms E) go to the parent
+// unless |C / scale| exceeds the bound, in which case the vertex gave zero.
+constexpr int kMaxSssFrames = 16;
+struct SssFrames {
+  float3 C[kMaxSssFrames], E[kMaxSssFrames], scale[kMaxSssFrames];
+  float thr[kMaxSssFrames];
+  int parent[kMaxSssFrames], open[kMaxSssFrames];
+  int n;
+};
+
+__device__ __forceinline__ void frame_add(SssFrames& F, float3& root, int f, float3 x) {
+  if (f < 0) root += x;
+  else F.C[f] += x;
+}
+
+// a branch inside frame f ended (or a child frame closed): close every frame
+// that has nothing open left
+__device__ __forceinline__ void frame_release(SssFrames& F, float3& root, int f) {
+  while (f >= 0) {
+    if (--F.open[f] > 0) return;
+    const float3 s = F.scale[f], c = F.C[f];
+    const float3 q = f3(s.x != 0.0f ? c.x / s.x : 0.0f, s.y != 0.0f ? c.y / s.y : 0.0f, s.z != 0.0f ? c.z / s.z : 0.0f);
+    const bool cut = sqrtf(dot(q, q)) > F.thr[f];
+    const int p = F.parent[f];
+    if (!cut) frame_add(F, root, p, c + F.E[f]);
+    f = p;
+  }
+}
+
 // One camera sample: the whole branch tree of radiance() for one root ray.
+template <bool SSS>
 __device__ float3 trace_sample(const DevScene& S, const RenderCfg& cfg, float3 o0, float3 d0, uint64_t sample_id,
                                TraceStats& st, uint32_t* err, uint32_t& segs) {
   PathState stack[kSplitStack];
+  int sframe[kSplitStack];
   int sp = 0;
-  root_path(stack[sp++], o0, d0);
+  root_path(stack[sp], o0, d0);
+  sframe[sp++] = -1;
   float3 L = f3(0, 0, 0);
+  SssFrames F;
+  F.n = 0;
   while (sp > 0) {
-    PathState ps = stack[--sp];
+    --sp;
+    PathState ps = stack[sp];
+    int fr = sframe[sp];
     for (;;) {
       FastHit h;
       segs++;
@@ -30,22 +69,50 @@ __device__ float3 trace_sample(const DevScene& S, const RenderCfg& cfg, float3 o
       ShadowReq sh[3];
       int nsh = 0;
       PathState child;
-      const int r = shade(S, cfg, ps, hit, h, sample_id, sh, nsh, child, err);
+      SssFrameOut fo;
+      fo.open = 0;
+      const float3 Lb = ps.L;
+      const int r = shade<SSS>(S, cfg, ps, hit, h, sample_id, sh, nsh, child, err, nullptr, nullptr, nullptr,
+                               SSS ? &fo : nullptr);
       for (int k = 0; k < nsh; k++) {
         segs++;
         if (!fast_occluded(S, sh[k].o, sh[k].d, sh[k].tmax, st, err)) ps.L += sh[k].contrib;
       }
+      if (SSS && fo.open && F.n < kMaxSssFrames) {
+        // the branch moves into a new frame: what it gathered so far belongs outside
+        const int f = F.n++;
+        F.E[f] = ps.L - Lb;
+        F.C[f] = f3(0, 0, 0);
+        F.scale[f] = fo.scale;
+        F.thr[f] = fo.thr;
+        F.parent[f] = fr;
+        F.open[f] = 1;
+        frame_add(F, L, fr, Lb);
+        ps.L = f3(0, 0, 0);
+        fr = f;  // the parent keeps its count: the branch left, the child frame came
+      }
       if (r == SHADE_SPLIT) {
-        if (sp < kSplitStack) stack[sp++] = child;
-        else atomicOr(err, PR_DEV_LOOP_CAP);
+        if (sp < kSplitStack) {
+          stack[sp] = child;
+          sframe[sp++] = fr;
+          if (SSS && fr >= 0) F.open[fr]++;
+        } else {
+          atomicOr(err, PR_DEV_LOOP_CAP);
+        }
       }
       if (r == SHADE_END) break;
     }
-    L += ps.L;
+    if (SSS) {
+      frame_add(F, L, fr, ps.L);
+      frame_release(F, L, fr);
+    } else {
+      L += ps.L;
+    }
   }
   return L;
 }
 
+template <bool SSS>
 __global__ void __launch_bounds__(128) pt_megakernel(DevScene S, RenderCfg cfg, float* __restrict__ out,
                                                      uint32_t* __restrict__ err, unsigned long long* __restrict__ counters) {
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -65,7 +132,7 @@ __global__ void __launch_bounds__(128) pt_megakernel(DevScene S, RenderCfg cfg, 
     for (int k = k0; k < k1; k++) {
       float3 o, d;
       const uint64_t sample_id = camera_ray(cfg, x, y, cfg.sample_offset + (uint64_t)k, o, d);
-      acc += finish_sample(cfg, trace_sample(S, cfg, o, d, sample_id, st, err, segs), err);
+      acc += finish_sample(cfg, trace_sample<SSS>(S, cfg, o, d, sample_id, st, err, segs), err);
       paths++;
     }
     acc = acc * cfg.sensor;
@@ -107,7 +174,8 @@ cudaError_t launch_megakernel(const DevScene& S, const RenderCfg& cfg, float* ou
                               unsigned long long* counters, cudaStream_t stream) {
   const uint64_t threads = (uint64_t)cfg.tiles_x * cfg.tiles_y * 32ull * (uint64_t)cfg.chunks;
   const uint32_t blocks = (uint32_t)((threads + 127) / 128);
-  pt_megakernel<<<blocks, 128, 0, stream>>>(S, cfg, out, err, counters);
+  if (S.has_sss) pt_megakernel<true><<<blocks, 128, 0, stream>>>(S, cfg, out, err, counters);
+  else pt_megakernel<false><<<blocks, 128, 0, stream>>>(S, cfg, out, err, counters);
   return cudaGetLastError();
 }
 

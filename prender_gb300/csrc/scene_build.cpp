@@ -314,8 +314,68 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
     }
     g.roughness_d = pm.roughness;
     g.ior_d = pm.refractive_index;
-    if (pm.type != PR_MAT_DIFFUSE && pm.type != PR_MAT_SPECULAR && pm.type != PR_MAT_REFRACTION &&
-        pm.type != PR_MAT_REFRACTION_FRESNEL) {
+    if (pm.type == PR_MAT_SSS_REFRACTION || pm.type == PR_MAT_SSS_DIFFUSE || pm.type == PR_MAT_SSS_WARD) {
+      const pr_medium& md = pm.medium;
+      if (pm.type != PR_MAT_SSS_REFRACTION || md.level != -2 || !md.use_bssrdf || pm.roughness != 0.0) {
+        err = "subsurface scattering: only the directional-dipole form (reflection reflection + "
+              "Subsurface_Scattering, level -2, roughness 0) is on this path";
+        return PR_E_UNSUPPORTED;
+      }
+      // setup_Scattering (ParticipatingMediaPrm.h:133-160) when the SCATTERING line is > PS_EPS
+      double ss[3], sa[3], tc[3] = {0, 0, 0};
+      for (int k = 0; k < 3; k++) { ss[k] = md.sigma_s_rgb[k]; sa[k] = md.sigma_a_rgb[k]; }
+      double sc = (ss[0] + ss[1] + ss[2]) / 3, ab = (sa[0] + sa[1] + sa[2]) / 3;
+      if (sc > 1.0e-6) {
+        const double scale = md.scale > 0.0 ? md.scale : 1.0;
+        for (int k = 0; k < 3; k++) { ss[k] *= scale; sa[k] *= scale; }
+        sc = (ss[0] + ss[1] + ss[2]) / 3;
+        ab = (sa[0] + sa[1] + sa[2]) / 3;
+        if (sc + ab < 1.0e-12) {
+          for (int k = 0; k < 3; k++) ss[k] = sa[k] = 1.0;
+          sc = ab = 0.0;
+        } else {
+          for (int k = 0; k < 3; k++) tc[k] = ss[k] + sa[k];
+        }
+      }
+      // DirectionalDipole (bssrdf.h:75-128)
+      auto C1 = [](double n) {
+        const double r = n > 1.0 ? -9.23372 + n * (22.2272 + n * (-20.9292 + n * (10.2291 + n * (-2.54396 + 0.254913 * n))))
+                                 : 0.919317 + n * (-3.4793 + n * (6.75335 + n * (-7.80989 + n * (4.98554 - 1.36881 * n))));
+        return r / 2.0;
+      };
+      auto C2 = [](double n) {
+        double r = -1641.1 + n * (1213.67 + n * (-568.556 + n * (164.798 + n * (-27.0181 + 1.91826 * n))));
+        r += (((135.926 / n) - 656.175) / n + 1376.53) / n;
+        return r / 3.0;
+      };
+      const double eta = pm.r_refractive_index;
+      double stp_min = 1e300;
+      for (int k = 0; k < 3; k++) {
+        const double ssp = ss[k] * (1.0 - md.phase_g[k]);
+        const double stp = ssp + sa[k];
+        const double albedo_p = ssp / stp;
+        const double D = 1.0 / (3.0 * stp);
+        g.sss_D[k] = (float)D;
+        g.sss_sigma_tr[k] = (float)std::sqrt(sa[k] / D);
+        g.sss_de[k] = (float)(2.131 * D / std::sqrt(albedo_p));
+        g.sss_sigma_t[k] = (float)(ss[k] + sa[k]);
+        g.sss_tr[k] = (float)tc[k];
+        stp_min = std::min(stp_min, stp);
+      }
+      const double Cp = (1.0 - 2.0 * C1(eta)) / 4.0, Ce = (1.0 - 3.0 * C2(eta)) / 2.0;
+      g.sss = 1;
+      g.sss_eta = (float)eta;
+      g.sss_Cp = (float)Cp;
+      g.sss_Ce = (float)Ce;
+      g.sss_A = (float)((1.0 - Ce) / (2.0 * Cp));
+      g.sss_falloff = (float)(stp_min * 0.001);
+      // probe-disk radius heuristic (Subsurface_Scattering.h:701-714)
+      const double x = std::min({ss[0], ss[1], ss[2]});
+      double y = 2.0 - 1.0 / (1.0 + std::exp(-4.0 * (x - 1.6)));
+      if (ab < 0.001) y *= 1.3 - std::exp(std::min({sa[0], sa[1], sa[2]}) * 1000.0);
+      g.sss_rmax0 = (float)(1.25 * std::sqrt(std::log(1.0e-4) / -stp_min) * y * md.r_max);
+    } else if (pm.type != PR_MAT_DIFFUSE && pm.type != PR_MAT_SPECULAR && pm.type != PR_MAT_REFRACTION &&
+               pm.type != PR_MAT_REFRACTION_FRESNEL) {
       err = "material type " + std::to_string(pm.type) + " is not on this path yet";
       return PR_E_UNSUPPORTED;
     }
@@ -360,6 +420,10 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
       for (int k = 0; k < 3; k++) g.p[k] = pe.p[k];
       g.radius = pe.radius;
       g.area = 12.5663706143591729538505735331180115 * pe.radius * pe.radius;  // PS_FORPI r^2
+      for (int k = 0; k < 3; k++) {  // Sphere::CreateBoundingBox (sphere.h:58-63)
+        g.bb_min[k] = pe.p[k] - pe.radius - 0.01;
+        g.bb_max[k] = pe.p[k] + pe.radius + 0.01;
+      }
       if (pe.radius < 1.0e4)
         for (int k = 0; k < 3; k++) { grow(pe.p[k] - pe.radius); grow(pe.p[k] + pe.radius); }
     } else if (pe.type == PR_ENT_UVPLANE) {  // UVPlane ctor + CalcArea (plane.h:146-177)
@@ -374,6 +438,16 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
         g.normal[k] = (&n.x)[k];
       }
       g.area = len(scale(u, g.u_length)) * len(scale(v, g.v_length)) * (1.0 - std::pow(dot(u, v), 2.0));
+      {  // UVPlane::CreateBoundingBox (plane.h:191-215)
+        const D3 o = mk(pe.p), Uu = scale(u, g.u_length), Vv = scale(v, g.v_length);
+        const D3 q[4] = {o, add(o, Vv), add(o, Uu), add(add(o, Uu), Vv)};
+        for (int k = 0; k < 3; k++) { g.bb_min[k] = 1e300; g.bb_max[k] = -1e300; }
+        for (const D3& c : q)
+          for (int k = 0; k < 3; k++) {
+            g.bb_min[k] = std::min(g.bb_min[k], (&c.x)[k]);
+            g.bb_max[k] = std::max(g.bb_max[k], (&c.x)[k]);
+          }
+      }
       for (int k = 0; k < 3; k++) grow(pe.p[k]);
     } else if (pe.type == PR_ENT_CIRCLE) {
       // Circle ctor (circle.h:117-134): a UVPlane(o, r u, r v) with u, v from
@@ -447,6 +521,14 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
           g.bmax[a] = std::max(g.bmax[a], v[a]);
         }
       }
+      // Polygon::CreateBoundingBox over every vertex of the mesh (polygon.h:875-889)
+      for (int a = 0; a < 3; a++) { g.bb_min[a] = 1e300; g.bb_max[a] = -1e300; }
+      for (int64_t k = 0; k < (int64_t)pm_.n_vertices; k++)
+        for (int a = 0; a < 3; a++) {
+          g.bb_min[a] = std::min(g.bb_min[a], (double)pm_.vertices[3 * k + a]);
+          g.bb_max[a] = std::max(g.bb_max[a], (double)pm_.vertices[3 * k + a]);
+        }
+      for (int a = 0; a < 3; a++) { g.bb_min[a] -= 0.01; g.bb_max[a] += 0.01; }
       for (int t : q.leaf_tris) {
         for (int k = 0; k < 3; k++) {
           const float* v = pm_.vertices + 3 * (size_t)pm_.faces[3 * (size_t)t + k];
@@ -466,6 +548,14 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
     } else {
       err = "entity type " + std::to_string(pe.type) + " is not on this path yet";
       return PR_E_UNSUPPORTED;
+    }
+    // subsurface probe-disk radius, clamped by the object's size (Subsurface_Scattering.h:716-718)
+    const GMaterial& gm = hs.mats[pe.material];
+    if (gm.sss) {
+      if (pe.type == PR_ENT_CIRCLE) { err = "subsurface scattering on a disk is not on this path"; return PR_E_UNSUPPORTED; }
+      const D3 ext = {g.bb_max[0] - g.bb_min[0], g.bb_max[1] - g.bb_min[1], g.bb_max[2] - g.bb_min[2]};
+      const double ln = len(ext);
+      g.sss_rmax = gm.sss_rmax0 > ln ? ln * 0.3 : gm.sss_rmax0;
     }
     hs.ents.push_back(g);
   }

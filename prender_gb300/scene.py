@@ -56,6 +56,7 @@ class Material:
     roughness: float = 0.0
     refractive_index: float = 1.5
     medium: Medium = field(default_factory=Medium)
+    r_refractive_index: float = 1.0
 
     @staticmethod
     def diffuse(color, emission=(0.0, 0.0, 0.0)) -> "Material":
@@ -72,6 +73,17 @@ class Material:
         """'reflection reflection' (scene_env.h:1450-1458)."""
         return Material(A.PR_MAT_REFRACTION, tuple(color), refractive_index=ior)
 
+    @staticmethod
+    def subsurface(color, sigma_s, sigma_a, g=0.0, eta: float = 1.3, ior: float = 1.5, r_max: float = 1.0,
+                   scale: float = 1.0) -> "Material":
+        """'reflection reflection' + 'reflection Subsurface_Scattering' with the
+        material's SCATTERING / ABSORBING / PAHASE, 'level -2' (directional
+        dipole, scene_env.h:1305-1362) and r_refractive_index eta."""
+        g3 = tuple(g) if hasattr(g, "__len__") else (float(g),) * 3
+        return Material(A.PR_MAT_SSS_REFRACTION, tuple(color), refractive_index=ior, r_refractive_index=eta,
+                        medium=Medium(sigma_s_rgb=tuple(sigma_s), sigma_a_rgb=tuple(sigma_a), phase_g=g3, scale=scale,
+                                      r_max=r_max, level=-2, use_bssrdf=1))
+
     def is_light(self) -> bool:
         """Material::isLight (material.h)."""
         return (self.type == A.PR_MAT_DIFFUSE and math.sqrt(sum(c * c for c in self.color)) < 0.001
@@ -86,6 +98,7 @@ class Material:
         m.roughness = float(self.roughness)
         m.refractive_index = float(self.refractive_index)
         m.medium = self.medium.to_c()
+        m.r_refractive_index = float(self.r_refractive_index)
         return m
 
 
@@ -346,7 +359,8 @@ class Scene:
                 "ABSORBING", "0", f3(md.sigma_a_rgb), "",
                 f"PAHASE {f3(md.phase_g)}", ""]
         refl = {A.PR_MAT_DIFFUSE: "reflection diffuse", A.PR_MAT_SPECULAR: "reflection specular",
-                A.PR_MAT_REFRACTION: "reflection reflection"}
+                A.PR_MAT_REFRACTION: "reflection reflection",
+                A.PR_MAT_SSS_REFRACTION: "reflection reflection\nreflection Subsurface_Scattering"}
         for ei, e in enumerate(self.entities):
             m = self.materials[e.material]
             out.append("OBJECT")
@@ -362,8 +376,22 @@ class Scene:
                 out.append(f"objfile {os.path.join(directory, objname)}")
             else:
                 raise ValueError("entity type has no reference writer")
-            if m.type == A.PR_MAT_REFRACTION and m.refractive_index != 1.5:
+            if m.type in (A.PR_MAT_REFRACTION, A.PR_MAT_SSS_REFRACTION) and m.refractive_index != 1.5:
                 out.append(f"refractive_index {_fmt(m.refractive_index)}")
+            if m.type == A.PR_MAT_SSS_REFRACTION:
+                md = m.medium
+                if len(set(float(x) for x in md.phase_g)) != 1:
+                    raise ValueError("the reference's 'PAHASE x y z' keeps x for y; give one g")
+                mean_s = sum(float(x) for x in md.sigma_s_rgb) / 3.0
+                mean_a = sum(float(x) for x in md.sigma_a_rgb) / 3.0
+                out += ["SCATTERING", _fmt(round(mean_s, 12)), f3(md.sigma_s_rgb),
+                        "ABSORBING", _fmt(round(mean_a, 12)), f3(md.sigma_a_rgb),
+                        "PAHASE", _fmt(md.phase_g[0]),
+                        "level", str(int(md.level)),
+                        "MATERIAL_R_MAX", _fmt(md.r_max),
+                        f"r_refractive_index {_fmt(m.r_refractive_index)}"]
+                if float(md.scale) != 1.0:
+                    out += ["MATERIAL_SCALE", _fmt(md.scale)]
             out += [f"emission {f3(m.emission)}", f"color {f3(m.color)}"]
             if e.normal_inverse < 0:
                 out.append("normal -1")

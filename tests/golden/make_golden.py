@@ -106,6 +106,26 @@ def kerr_golden(d):
     np.savez_compressed(os.path.join(HERE, "kerr_render.npz"), **imgs)
 
 
+def sss_golden(d):
+    """subsurface (directional dipole) renders: one thread bit-exact, and a
+    high-spp image for the GPU's statistical parity"""
+    out = {}
+    sc = scenes.sss_cornell(width=24, height=18, samples=1, supersamples=2, subdiv=3)
+    dd = os.path.join(d, "s_1t")
+    os.makedirs(dd)
+    img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+    out["sss_1thread"] = img
+    print("sss 1thread", info)
+    sc = scenes.sss_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3)
+    dd = os.path.join(d, "s_hi")
+    os.makedirs(dd)
+    img, info = ref_render(sc.write_reference(dd, threads=os.cpu_count()), (sc.camera.width, sc.camera.height), dd,
+                           threads=os.cpu_count())
+    out["sss_64x48_512spp"] = img.astype(np.float32)
+    print("sss highspp", info)
+    np.savez_compressed(os.path.join(HERE, "sss_render.npz"), **out)
+
+
 def main():
     if not os.path.exists(REF_BIN):
         args = [a for a in sys.argv[1:] if not a.startswith("--")]
@@ -115,8 +135,13 @@ def main():
         with tempfile.TemporaryDirectory() as d:
             kerr_golden(d)
         return
+    if "--sss-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            sss_golden(d)
+        return
     with tempfile.TemporaryDirectory() as d:
         kerr_golden(d)
+        sss_golden(d)
         # -- QBVH structure + first hits on the subdiv-3 mesh Cornell box
         s = scenes.mesh_cornell(width=32, height=24, samples=1, supersamples=2, subdiv=3)
         p = s.write_reference(d)

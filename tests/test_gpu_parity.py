@@ -106,6 +106,30 @@ def test_image_matches_reference_statistically(ctx, golden, name, build, tol_fra
     assert rmse < 1.3 * noise
 
 
+def test_subsurface_image_matches_reference_statistically(ctx, golden):
+    # directional-dipole BSSRDF in the plain form against the reference's 512 spp render
+    s = scenes.sss_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3)
+    s.settings.mode = A.PR_MODE_MEGAKERNEL
+    ctx.upload(s)
+    ref = golden["sss_render"]["sss_64x48_512spp"].astype(np.float64)
+    nb, spp = 16, s.settings.spp
+    b = _batches(ctx, s, nb, spp)
+    mean = b.mean(0)
+    sd = b.std(0, ddof=1)
+    sigma = np.sqrt(sd ** 2 / nb + sd ** 2) + 1e-6
+    frac = float((np.abs(mean - ref) / sigma > 3.0).mean())
+    rmse = float(np.sqrt(((mean - ref) ** 2).mean()))
+    noise = float(np.sqrt((sigma ** 2).mean()))
+    rel = abs(mean.mean() - ref.mean()) / ref.mean()
+    print(f"subsurface: >3 sigma {frac:.4f}, rmse {rmse:.3e} vs noise {noise:.3e}, mean rel diff {rel:.4f}")
+    assert rel < 0.01
+    assert frac < 0.03
+    assert rmse < 1.3 * noise
+    s.settings.mode = A.PR_MODE_WAVEFRONT  # the wavefront form refuses subsurface materials
+    with pytest.raises(gpu.PrenderError):
+        ctx.render(s)
+
+
 def test_render_is_deterministic_and_shards_by_sample_offset(ctx):
     s = scenes.mesh_cornell(width=48, height=36, samples=8, supersamples=2, subdiv=3)
     ctx.upload(s)

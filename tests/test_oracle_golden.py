@@ -65,3 +65,13 @@ def test_high_spp_goldens_are_converged(golden):
     for k in golden["render_highspp"].files:
         img = golden["render_highspp"][k]
         assert np.isfinite(img).all() and (img >= 0).all() and img.mean() > 1e-3
+
+
+def test_subsurface_render_one_thread_bit_exact(golden):
+    # directional-dipole BSSRDF (level -2): probe rays, dipole, exit NEE,
+    # the Fresnel-surface branch and the radiance bounds, against the reference
+    sc = scenes.sss_cornell(width=24, height=18, samples=1, supersamples=2, subdiv=3)
+    img, _, _ = O.OracleScene(sc).render(threads=1)
+    ref = golden["sss_render"]["sss_1thread"]
+    assert np.array_equal(img, ref)
+    assert ref.mean() > 0
