@@ -512,14 +512,13 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   // graph's device-side while loop: profilers that cannot see kernels inside
   // conditional graph nodes see every launch this way (same kernels, same work)
   const char* host_loop = getenv("PR_WF_HOST_LOOP");
-  const bool use_graph = !(host_loop && host_loop[0] == '1');
+  const bool use_graph = !(host_loop && host_loop[0] == '1') && !c->force_host_loop;
   if (use_graph && !c->wf_graph_failed &&
       (!c->wf_graph || c->wf_graph_slots != P || c->wf_graph_trace_blocks != L.trace_blocks)) {
-    if (c->wf_graph) cudaGraphExecDestroy(c->wf_graph);
-  if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
-  for (cudaStream_t st : c->batch_streams) cudaStreamDestroy(st);
-  for (cudaEvent_t ev : c->batch_events) cudaEventDestroy(ev);
-  c->batch_partial.release();
+    if (c->wf_graph) {
+      cudaStreamSynchronize(c->stream);  // the previous render's launch has finished with it
+      cudaGraphExecDestroy(c->wf_graph);
+    }
     c->wf_graph = nullptr;
     cudaError_t e = wf_build_graph(L, c->stream, &c->wf_graph);
     if (e != cudaSuccess) {
@@ -715,29 +714,32 @@ int pr_autotune_wavefront(pr_ctx* c, const pr_camera* cam, const pr_render_param
   const unsigned int cand_bps[] = {16u, 32u, 64u};
   double best = 1e300;
   unsigned int best_s = 0, best_b = 0;
+  // candidates run the host-driven loop (no graph is rebuilt per candidate);
+  // the figure compared is the sum of the kernels' own device times
+  c->force_host_loop = true;
+  int st = PR_OK;
   for (unsigned int sl : cand_slots) {
     for (unsigned int b : cand_bps) {
       c->tuned_slots = sl;
       c->tuned_trace_bps = b;
       double t = 0.0;
-      for (int rep = 0; rep < 2; rep++) {  // the first run builds the graph and grows the pool
-        int st = pr_render_dev(c, cam, &q, (float*)c->out.p, 0, 0);
-        if (st != PR_OK) {
-          c->tuned_slots = best_s;
-          c->tuned_trace_bps = best_b;
-          return st;
-        }
-        t = c->stats.device_ms;
+      for (int rep = 0; rep < 2 && st == PR_OK; rep++) {  // the first run grows the pool
+        st = pr_render_dev(c, cam, &q, (float*)c->out.p, 0, 0);
+        t = c->kernel_ms[0] + c->kernel_ms[1] + c->kernel_ms[2] + c->kernel_ms[3];
       }
+      if (st != PR_OK) break;
       if (t < best) {
         best = t;
         best_s = sl;
         best_b = b;
       }
     }
+    if (st != PR_OK) break;
   }
+  c->force_host_loop = false;
   c->tuned_slots = best_s;
   c->tuned_trace_bps = best_b;
+  if (st != PR_OK) return st;
   if (slots_out) *slots_out = (int32_t)best_s;
   if (trace_blocks_per_sm_out) *trace_blocks_per_sm_out = (int32_t)best_b;
   if (ms_out) *ms_out = best;

@@ -73,6 +73,7 @@ struct pr_ctx {
   unsigned int wf_graph_trace_blocks = 0;
   unsigned int tuned_slots = 0;      // autotuner's wavefront pool size (0: default)
   unsigned int tuned_trace_bps = 0;  // autotuner's traversal blocks per SM (0: default)
+  bool force_host_loop = false;      // the autotuner times candidates with the host-driven loop
   // pr_render_batch
   cudaGraphExec_t batch_exec = nullptr;
   std::vector<cudaStream_t> batch_streams;

@@ -9,6 +9,10 @@ mounted:
 Each fixture stores the synthetic inputs (scene parameters, rays) together
 with the reference's outputs, so the tests need neither the reference nor
 its build on the machine that runs them.
+
+    python tests/golden/make_golden.py --sss-oracle
+
+writes sss_oracle.npz from the oracle alone (no reference build needed).
 """
 import os
 import struct
@@ -126,7 +130,28 @@ def sss_golden(d):
     np.savez_compressed(os.path.join(HERE, "sss_render.npz"), **out)
 
 
+def sss_oracle_golden(nb=16):
+    """16 independent 512-spp renders of the 64x48 subsurface scene by the
+    oracle (pinned bit-exact to the reference by the one-thread fixture):
+    per-pixel mean and standard deviation, the symmetric high-spp target for
+    the GPU's statistical parity.  Needs no reference build."""
+    from oracle import oracle as O
+    sc = scenes.sss_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3)
+    imgs = []
+    for k in range(nb):
+        sc.settings.seed = 100 + k
+        img, _, _ = O.OracleScene(sc).render(threads=os.cpu_count())
+        imgs.append(img)
+    b = np.stack(imgs)
+    np.savez_compressed(os.path.join(HERE, "sss_oracle.npz"), mean_64x48_8192spp=b.mean(0).astype(np.float32),
+                        sd_64x48_512spp=b.std(0, ddof=1).astype(np.float32), batches=np.int32(nb))
+    print("sss oracle batches", nb)
+
+
 def main():
+    if "--sss-oracle" in sys.argv:
+        sss_oracle_golden()
+        return
     if not os.path.exists(REF_BIN):
         args = [a for a in sys.argv[1:] if not a.startswith("--")]
         ref = args[0] if args else "/root/reference"

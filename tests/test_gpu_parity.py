@@ -107,23 +107,47 @@ def test_image_matches_reference_statistically(ctx, golden, name, build, tol_fra
 
 
 def test_subsurface_image_matches_reference_statistically(ctx, golden):
-    # directional-dipole BSSRDF in the plain form against the reference's 512 spp render
+    """Directional-dipole BSSRDF in the plain form, 16 x 512 spp.
+
+    Against the oracle's 16 x 512 spp (the oracle is bit-exact with the
+    reference on one thread): both sides are 8192-spp means with measured
+    per-pixel spreads, so the per-pixel test is symmetric; two halves of the
+    oracle's own batches score 0.6-0.7 % beyond 3 sigma.  Against the
+    reference's single 512 spp render the subsurface paths' fireflies sit on
+    one side: the oracle's 8192-spp mean itself scores 3.2 % of pixels beyond
+    3 sigma there (all with the image above the mean), so that comparison is
+    bounded at 5 %, with its mean and RMSE held to the usual bars."""
     s = scenes.sss_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3)
     s.settings.mode = A.PR_MODE_MEGAKERNEL
     ctx.upload(s)
-    ref = golden["sss_render"]["sss_64x48_512spp"].astype(np.float64)
     nb, spp = 16, s.settings.spp
     b = _batches(ctx, s, nb, spp)
     mean = b.mean(0)
     sd = b.std(0, ddof=1)
+    orc = golden["sss_oracle"]
+    o_mean = orc["mean_64x48_8192spp"].astype(np.float64)
+    o_sd = orc["sd_64x48_512spp"].astype(np.float64)
+    o_nb = int(orc["batches"])
+    sigma = np.sqrt(sd ** 2 / nb + o_sd ** 2 / o_nb) + 1e-6
+    frac = float((np.abs(mean - o_mean) / sigma > 3.0).mean())
+    rmse = float(np.sqrt(((mean - o_mean) ** 2).mean()))
+    noise = float(np.sqrt((sigma ** 2).mean()))
+    rel = abs(mean.mean() - o_mean.mean()) / o_mean.mean()
+    print(f"subsurface vs oracle 8192 spp: >3 sigma {frac:.4f}, rmse {rmse:.3e} vs noise {noise:.3e}, "
+          f"mean rel diff {rel:.4f}")
+    assert rel < 0.01
+    assert frac < 0.02
+    assert rmse < 1.3 * noise
+    ref = golden["sss_render"]["sss_64x48_512spp"].astype(np.float64)
     sigma = np.sqrt(sd ** 2 / nb + sd ** 2) + 1e-6
     frac = float((np.abs(mean - ref) / sigma > 3.0).mean())
     rmse = float(np.sqrt(((mean - ref) ** 2).mean()))
     noise = float(np.sqrt((sigma ** 2).mean()))
     rel = abs(mean.mean() - ref.mean()) / ref.mean()
-    print(f"subsurface: >3 sigma {frac:.4f}, rmse {rmse:.3e} vs noise {noise:.3e}, mean rel diff {rel:.4f}")
+    print(f"subsurface vs reference 512 spp: >3 sigma {frac:.4f}, rmse {rmse:.3e} vs noise {noise:.3e}, "
+          f"mean rel diff {rel:.4f}")
     assert rel < 0.01
-    assert frac < 0.03
+    assert frac < 0.05
     assert rmse < 1.3 * noise
     s.settings.mode = A.PR_MODE_WAVEFRONT  # the wavefront form refuses subsurface materials
     with pytest.raises(gpu.PrenderError):

@@ -75,3 +75,17 @@ def test_subsurface_render_one_thread_bit_exact(golden):
     ref = golden["sss_render"]["sss_1thread"]
     assert np.array_equal(img, ref)
     assert ref.mean() > 0
+
+
+def test_subsurface_oracle_fixture_agrees_with_reference_render(golden):
+    # the oracle's 16 x 512 spp subsurface fixture against the reference's own
+    # 512 spp render: same mean, RMSE at the noise level (the per-pixel tail
+    # is one-sided, reference fireflies, so only the aggregate is bounded here)
+    orc = golden["sss_oracle"]
+    mean = orc["mean_64x48_8192spp"].astype(np.float64)
+    sd = orc["sd_64x48_512spp"].astype(np.float64)
+    nb = int(orc["batches"])
+    ref = golden["sss_render"]["sss_64x48_512spp"].astype(np.float64)
+    sigma = np.sqrt(sd ** 2 / nb + sd ** 2) + 1e-6
+    assert abs(mean.mean() - ref.mean()) / ref.mean() < 0.01
+    assert np.sqrt(((mean - ref) ** 2).mean()) < 1.3 * np.sqrt((sigma ** 2).mean())
