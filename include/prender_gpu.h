@@ -86,7 +86,9 @@ typedef struct pr_medium {
 /* material.h:54-240 Material (texture fields out of scope) */
 typedef struct pr_material {
   int32_t type;            /* PR_MAT_*                                       */
-  int32_t pad0;
+  int32_t disk_map;        /* 'disk_map' (scene_env.h:1163-1169): a disk with
+                              this material under a black hole is shaded from
+                              the accretion-disk texture (circle.h:240-335)  */
   double color[3];
   double emission[3];
   double specular[3];
@@ -108,6 +110,10 @@ typedef struct pr_entity {
   double u[3], v[3];       /* uvplane U and V edge vectors (unnormalised)    */
   double normal[3];        /* disk normal                                    */
   double radius_inner;     /* disk2 inner radius                             */
+  int32_t blackhole_disk;  /* 'blackhole_disk' (scene_env.h:1177-1181, :1627):
+                              index of the accretion-disk texture; 0 is the
+                              reference's default, -1 = none                 */
+  int32_t pad0;
 } pr_entity;
 
 /* Triangle mesh as ObjLoader keeps it (ObjLoader.h:153-233): float vertices,
@@ -142,7 +148,18 @@ typedef struct pr_kerr {
   int32_t texture_width;
   int32_t texture_height;
   int32_t precision;          /* PR_KERR_FP64 (default) or PR_KERR_FP32      */
-  int32_t pad0;
+  int32_t use_accretion_disk_temperature;  /* scene_env.h:496-500           */
+  double color_doppler_factor_effect;      /* scene_env.h:502-507           */
+  double observer[3];         /* camera_position the black hole was built with
+                                 (KerrBlackHole::camera_pos, scene_env.h:2067):
+                                 the disk's Doppler factor is taken from it   */
+  const uint8_t* disk_texture;  /* accretion_disk_texture 0, RGBA8 rows as
+                                   Bitmap::cell(y, x) returns them; NULL = none */
+  int32_t disk_texture_width;
+  int32_t disk_texture_height;
+  uint64_t disk_seed;         /* stream of the disk's alpha test (the reference
+                                 draws it from the scene's generator, seeded
+                                 from the clock, scene_env.h:306)             */
 } pr_kerr;
 
 typedef struct pr_scene_desc {
@@ -382,6 +399,16 @@ int pr_kerr_sensitivity(pr_ctx* ctx, const double* rays, int64_t n, const double
  * tangents: two inputs per ray make forward mode the cheaper one). */
 int pr_kerr_sensitivity_adjoint(pr_ctx* ctx, const double* rays, int64_t n, const double* basis,
                                 const double* cotangent, double* grad);
+
+/* Accretion-disk shading test hook: the texture, temperature and Doppler
+ * branch of Circle::intersect under the black hole (circle.h:240-322, no
+ * alpha test) at n world points of disk entity `entity`.  Host buffers:
+ * points 3n in; valid n (0 where the disk is not there: inside the ISCO,
+ * beyond the radius, off the texture), colour 3n, emission 3n, alpha n out.
+ * PR_E_SCENE without a disk texture; the scene's disk_map flag is not
+ * required. */
+int pr_kerr_disk_shade(pr_ctx* ctx, int entity, const double* points, int64_t n, int32_t* valid,
+                       double* color, double* emission, double* alpha);
 
 #ifdef __cplusplus
 }

@@ -46,7 +46,8 @@ def lib():
         L.oracle_radiance.argtypes = [vp, vp, C.c_int64, C.c_uint64, vp, vp]
         L.oracle_render.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
         L.oracle_light_count.argtypes = [vp]
-        L.oracle_kerr_trace.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp, vp, vp]
+        L.oracle_kerr_trace.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.oracle_kerr_disk_shade.argtypes = [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -116,14 +117,30 @@ class OracleScene:
     def kerr_trace(self, rays: np.ndarray):
         """Kerr branch of intersect_scene per ray; status 0 background,
         1 entity hit, 2 event horizon, 4 step underflow, 5 entity ahead of the
-        last step."""
+        last step; with the hit point's colour and emission (the accretion
+        disk rewrites them, drawing its alpha test from the scene stream
+        seeded with the black hole's disk_seed, one stream over the rays)."""
         rays = np.ascontiguousarray(rays, dtype=np.float64)
         n = rays.shape[0]
         out = dict(status=np.empty(n, np.int32), final_bl=np.empty((n, 3)), exit_dir=np.empty((n, 3)),
-                   steps=np.empty(n, np.int32), hit_entity=np.empty(n, np.int32), hit_t=np.empty(n))
+                   steps=np.empty(n, np.int32), hit_entity=np.empty(n, np.int32), hit_t=np.empty(n),
+                   hit_color=np.empty((n, 3)), hit_emission=np.empty((n, 3)))
         rc = lib().oracle_kerr_trace(self.h, _p(rays), n, _p(out["status"]), _p(out["final_bl"]),
                                      _p(out["exit_dir"]), _p(out["steps"]), _p(out["hit_entity"]),
-                                     _p(out["hit_t"]))
+                                     _p(out["hit_t"]), _p(out["hit_color"]), _p(out["hit_emission"]))
+        assert rc == 0, rc
+        return out
+
+    def kerr_disk_shade(self, entity: int, points: np.ndarray):
+        """The accretion disk's texture / temperature / Doppler shading at
+        world points of disk entity (no alpha test): valid, colour,
+        emission, alpha."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        n = pts.shape[0]
+        out = dict(valid=np.empty(n, np.int32), color=np.empty((n, 3)), emission=np.empty((n, 3)),
+                   alpha=np.empty(n))
+        rc = lib().oracle_kerr_disk_shade(self.h, int(entity), _p(pts), n, _p(out["valid"]), _p(out["color"]),
+                                          _p(out["emission"]), _p(out["alpha"]))
         assert rc == 0, rc
         return out
 

@@ -62,6 +62,7 @@ struct Material {  // material.h:54-240
   double roughness = 0.0;
   double refractive_index = 1.5;
   double r_refractive_index = 1.0;  // relative index of the subsurface medium (material.h:81)
+  int disk_map = 0;                 // 'disk_map' (scene_env.h:1163-1169)
   Medium medium;
   // Material::isLight (material.h): diffuse, dark, emissive
   bool isLight() const {
@@ -76,6 +77,10 @@ struct Hit {  // IntersectionPos (intersection.h:11-30) + object_id
   int material = -1;
   int object_id = -1;
   int prim = -1;
+  // the hit point's own copy of the material when the entity rewrote it
+  // (the accretion disk's texture and Doppler shift, circle.h:264-311)
+  bool ov = false;
+  V3 ov_color, ov_emission;
 };
 
 struct Mesh {
@@ -120,6 +125,9 @@ struct Entity {
   // circle (disk): its base UVPlane keeps normal_vector_inverse 1 (circle.h:117-130)
   double radius_inner = 0;
   V3 base_normal;
+  V3 du_axis, dv_axis;          // the base UVPlane's unit axes and lengths (plane.h:146-167)
+  double du_len = 0, dv_len = 0;
+  int blackhole_disk = 0;       // accretion-disk texture index (0 by default, scene_env.h:271)
   // mesh
   int mesh = -1;
   std::vector<Tri> tris;
@@ -145,6 +153,14 @@ struct KerrBH {  // KerrBlackHole (KerrBlackHole.h:86-151) with M = 1, initial_c
   std::vector<unsigned char> texture;  // background map, RGB8, cell(y, x) = texture[3 (y W + x)]
   int tex_w = 0, tex_h = 0;
   double texture_coef = 1.0;
+  // accretion disk (circle.h:240-335)
+  double Rmstable = 0;                  // inner_orbit() (KerrBlackHole.h:215-240)
+  int use_temperature = 0;
+  double doppler_effect = 0;            // color_doppler_factor_effect
+  V3 observer;                          // camera_pos
+  std::vector<unsigned char> disk_tex;  // RGBA8, cell(y, x) = disk_tex[4 (y W + x)]
+  int disk_w = 0, disk_h = 0;
+  uint64_t disk_seed = 0;
 };
 
 struct Scene {
@@ -200,9 +216,19 @@ inline V3 vtx(const Mesh& m, int id) {
   return V3(m.vert[3 * id], m.vert[3 * id + 1], m.vert[3 * id + 2]);
 }
 
-// Circle::intersect (circle.h:177-337) without textures: the base UVPlane's
-// plane test with no u/v extent (circle = true), then the annulus
-bool circle_hit(const Entity& e, V3 org, V3 dir, Hit& h) {
+// the scene-global generator the entities' alpha tests draw from
+// (SceneEnv::rand_, scene_env.h:213, :306); one per thread here
+thread_local MT64* tl_disk_rnd = nullptr;
+
+// the accretion-disk branch of Circle::intersect under a black hole
+// (circle.h:240-335); defined with the Kerr restatement
+bool kerr_disk_texel(const Scene& s, const Entity& e, Hit& h);
+
+// Circle::intersect (circle.h:177-337): the base UVPlane's plane test with no
+// u/v extent (circle = true), the annulus, then, under a black hole, the
+// accretion-disk texture (a disk without a material texture takes no other
+// branch)
+bool circle_hit(const Scene& s, const Entity& e, V3 org, V3 dir, Hit& h) {
   const V3 normal2 = e.base_normal;
   const double d = dot(dir, normal2);
   if (std::fabs(d) < EPS14) return false;
@@ -213,6 +239,8 @@ bool circle_hit(const Entity& e, V3 org, V3 dir, Hit& h) {
   if (h.distance < EPS) return false;
   if (dot(h.position - e.org, h.position - e.org) > e.radius * e.radius) return false;
   if (dot(h.position - e.org, h.position - e.org) < e.radius_inner * e.radius_inner) return false;
+  if (s.kerr.on && e.blackhole_disk >= 0 && s.mats[e.material].disk_map && !s.kerr.disk_tex.empty())
+    return kerr_disk_texel(s, e, h);
   return true;
 }
 
@@ -514,7 +542,7 @@ bool intersect(const Scene& s, V3 org, V3 dir, Hit& isect) {
     switch (e.type) {
       case PR_ENT_SPHERE: got = sphere_hit(e, o2, dir, h); break;
       case PR_ENT_UVPLANE: got = uvplane_hit(e, o2, dir, h); break;
-      case PR_ENT_CIRCLE: got = circle_hit(e, o2, dir, h); break;
+      case PR_ENT_CIRCLE: got = circle_hit(s, e, o2, dir, h); break;
       case PR_ENT_POLYGON: got = qbvh_hit(s, e, o2, dir, h); break;
       default: break;
     }
@@ -539,6 +567,7 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
     m.roughness = pm.roughness;
     m.refractive_index = pm.refractive_index;
     m.r_refractive_index = pm.r_refractive_index;
+    m.disk_map = pm.disk_map;
     if (m.type == PR_MAT_SSS_REFRACTION || m.type == PR_MAT_SSS_DIFFUSE || m.type == PR_MAT_SSS_WARD) {
       // the material's own participatingMediaParam (scene_env.h:1305-1362); the
       // entity set-up calls setup_Scattering when the SCATTERING line is > PS_EPS
@@ -641,6 +670,11 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
       onb(V3(pe.normal[0], pe.normal[1], pe.normal[2]), w, u, v);
       const V3 U = u * pe.radius, V = v * pe.radius;  // base = UVPlane(o, r*u, r*v)
       e.base_normal = normalize(cross(normalize(U), normalize(V)));
+      e.du_len = length(U);  // UVPlane ctor (plane.h:146-157)
+      e.dv_len = length(V);
+      e.du_axis = normalize(U);
+      e.dv_axis = normalize(V);
+      e.blackhole_disk = pe.blackhole_disk;
       e.area = e.radius * e.radius * PI;  // Circle::CalcArea
     } else if (pe.type == PR_ENT_POLYGON) {
       if (pe.mesh < 0 || pe.mesh >= (int)s.meshes.size()) { err = "entity mesh out of range"; return PR_E_SCENE; }
@@ -716,6 +750,32 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
       s.kerr.tex_w = d->kerr.texture_width;
       s.kerr.tex_h = d->kerr.texture_height;
       s.kerr.texture.assign(d->kerr.texture, d->kerr.texture + 3 * (size_t)s.kerr.tex_w * s.kerr.tex_h);
+    }
+    // inner_orbit (KerrBlackHole.h:215-240) with M = 1 and the class's own
+    // cbrt(x) = pow(x, 1/3)
+    {
+      const double M = s.kerr.M, a = s.kerr.a, a2 = s.kerr.a2, m2 = M * M;
+      auto cbrt_r = [](double x) { return std::pow(x, 1.0 / 3.0); };
+      const double z1 = 1 + cbrt_r(1 - a2 / m2) * (cbrt_r(1 + a / M) + cbrt_r(1 - a / M));
+      const double z2 = std::sqrt(3 * a2 / m2 + z1 * z1);
+      s.kerr.Rmstable = M * (3 + z2 - std::sqrt((3 - z1) * (3 + z1 + 2 * z2)));
+    }
+    s.kerr.use_temperature = d->kerr.use_accretion_disk_temperature;
+    s.kerr.doppler_effect = d->kerr.color_doppler_factor_effect;
+    s.kerr.observer = V3(d->kerr.observer[0], d->kerr.observer[1], d->kerr.observer[2]);
+    s.kerr.disk_seed = d->kerr.disk_seed;
+    if (d->kerr.disk_texture && d->kerr.disk_texture_width > 0 && d->kerr.disk_texture_height > 0) {
+      s.kerr.disk_w = d->kerr.disk_texture_width;
+      s.kerr.disk_h = d->kerr.disk_texture_height;
+      s.kerr.disk_tex.assign(d->kerr.disk_texture, d->kerr.disk_texture + 4 * (size_t)s.kerr.disk_w * s.kerr.disk_h);
+    }
+    for (const Entity& e : s.ents) {
+      if (e.type != PR_ENT_CIRCLE || e.blackhole_disk < 0 || !s.mats[e.material].disk_map) continue;
+      // the reference indexes its texture list with blackhole_disk (circle.h:240-242)
+      if (s.kerr.disk_tex.empty() || e.blackhole_disk != 0) {
+        err = "a disk_map disk under the black hole needs accretion-disk texture 0";
+        return PR_E_SCENE;
+      }
     }
   }
   // light registration (scene_env.h:1567-1586, :1692-1719) + random_light_setup sort (light.h:97)
@@ -832,11 +892,21 @@ bool inside_dir(V3 normal, V3 raydir) {
   return dot(on, normal) > 0;
 }
 
+// the material of a hit point: the scene's, or the copy the entity rewrote
+Material hit_mat(const Scene& s, const Hit& h) {
+  Material m = s.mats[h.material];
+  if (h.ov) {
+    m.color = h.ov_color;
+    m.emission = h.ov_emission;
+  }
+  return m;
+}
+
 // BRDF_Diffuse (brdf.h:408-700), no bump / shadow planes / IBL
 V3 brdf_diffuse(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, double p_scat, int depth) {
   const Scene& s = c.s;
   const Entity& obj = s.ents[ent];
-  const Material& mat = s.mats[hp.material];
+  const Material mat = hit_mat(s, hp);
   const bool ins = inside_dir(hp.normal, raydir);
   V3 emission = mat.emission;
   V3 trr(1, 1, 1);
@@ -884,7 +954,7 @@ V3 brdf_diffuse(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, d
 // BRDF_Specular (brdf.h:702-761)
 V3 brdf_specular(Ctx& c, V3 raydir, const Hit& hp, double p_rr, double p_scat, int depth) {
   const Scene& s = c.s;
-  const Material& mat = s.mats[hp.material];
+  const Material mat = hit_mat(s, hp);
   const bool ins = inside_dir(hp.normal, raydir);
   V3 emission = mat.emission;
   V3 trr(1, 1, 1);
@@ -903,7 +973,7 @@ V3 brdf_specular(Ctx& c, V3 raydir, const Hit& hp, double p_rr, double p_scat, i
 // BRDF_Refraction (brdf.h:763-953), no bump
 V3 brdf_refraction(Ctx& c, V3 raydir, const Hit& hp, int mat_type, V3 on, double p_rr, double p_scat, int depth) {
   const Scene& s = c.s;
-  const Material& mat = s.mats[hp.material];
+  const Material mat = hit_mat(s, hp);
   const bool ins = inside_dir(hp.normal, raydir);
   V3 emission = mat.emission;
   V3 trr(1, 1, 1);
@@ -1063,7 +1133,7 @@ V3 media_radiance(Ctx& c, V3 org, V3 raydir, const Hit& hp, int ent, double p_rr
   }
   if (pdf == 0.0) return V3();
   if (obj.light) {
-    if (depth == 0) return trr * s.mats[hp.material].emission;
+    if (depth == 0) return trr * hit_mat(s, hp).emission;
     return V3();
   }
   V3 L = direct + radiance(c, npos, next_dir, depth + 1);
@@ -1320,7 +1390,7 @@ V3 radiance(Ctx& c, V3 org, V3 dir, int depth) {
   } else if (!intersect(s, org, dir, hp)) {
     return s.background;
   }
-  const Material& mat = s.mats[hp.material];
+  const Material mat = hit_mat(s, hp);
   const V3 on = dot(hp.normal, dir) < 0.0 ? hp.normal : (-1.0 * hp.normal);
   V3 rw = mat.emission;
   switch (mat.type) {
@@ -1458,6 +1528,8 @@ int oracle_radiance(void* h, const double* rays, int64_t n, uint64_t seed, const
   auto* o = static_cast<OracleScene*>(h);
   if (!o || !rays || !prm || n < 0) return PR_E_ARG;
   MT64 rnd(seed);
+  MT64 drnd((uint64_t)(unsigned)o->s.kerr.disk_seed);
+  tl_disk_rnd = &drnd;
   Ctx c{o->s, rnd, prm->nee, prm->media && o->s.media_on, prm->depth, prm->depth_limit, (prm->flags & PR_FLAG_HG_CORRECT) != 0};
   for (int64_t k = 0; k < n; k++) {
     const double* r = rays + 6 * k;
@@ -1504,6 +1576,10 @@ int oracle_render(void* h, const pr_camera* cam, const pr_render_params* prm, in
   std::vector<V3> img((size_t)W * H);
   std::vector<std::unique_ptr<MT64>> rnd;
   for (int i = 0; i < threads; i++) rnd.emplace_back(new MT64((uint64_t)(unsigned)(i + 1)));
+  // the entities' alpha-test stream (SceneEnv::rand_): one generator seeded
+  // with the disk seed on one thread, as the reference's shared one is
+  std::vector<std::unique_ptr<MT64>> drnd;
+  for (int i = 0; i < threads; i++) drnd.emplace_back(new MT64((uint64_t)(unsigned)(s.kerr.disk_seed + i)));
   std::atomic<uint64_t> seg_total(0);
   const auto t0 = std::chrono::steady_clock::now();
   for (int sidx = 0; sidx < samples; sidx++) {
@@ -1511,6 +1587,7 @@ int oracle_render(void* h, const pr_camera* cam, const pr_render_params* prm, in
     for (int y = row0; y < row1; y++) {
       const int tid = omp_get_thread_num();
       tl_segments = 0;
+      tl_disk_rnd = drnd[tid].get();
       Ctx c{s, *rnd[tid], prm->nee, prm->media && s.media_on, prm->depth, prm->depth_limit,
             (prm->flags & PR_FLAG_HG_CORRECT) != 0};
       for (int x = 0; x < W; x++) {
@@ -1833,6 +1910,197 @@ namespace {
 // Returns the status (0 background, 1 entity hit, 2 event horizon, 4 step
 // underflow, 5 entity ahead of the last step); y is the final state, dir2
 // the last polyline direction, cnt the steps taken, hit the accepted hit.
+// ---- accretion disk under the black hole (circle.h:240-335) -------------
+// calculateLuminance (color.h:47-49), BT.709 weights in source order
+inline double luminance(V3 c) { return 0.2126 * c.x + 0.7152 * c.y + 0.0722 * c.z; }
+
+// adjustLuminance / adjustToSourceLuminance (color.h:51-74): the target is
+// rescaled to the source's luminance and rounded to 0..255 integer levels
+V3 adjust_to_source_luminance(V3 source, V3 target) {
+  const double want = luminance(source);
+  const double cur = luminance(target);
+  if (cur == 0.0) {
+    const int value = (int)clampd((double)(int)std::round(want / 0.2126), 0, 255);
+    return V3(value, value, value);
+  }
+  const double scale = want / cur;
+  return V3(clampd((double)(int)std::round(target.x * scale), 0, 255),
+            clampd((double)(int)std::round(target.y * scale), 0, 255),
+            clampd((double)(int)std::round(target.z * scale), 0, 255));
+}
+
+// accretionDiskTemperatureGeom (KerrBlackHole.h:1565-1593): thin-disk
+// T^4 ~ (Mdot / r^3)(1 - sqrt(r_in / r)) with Mdot a tenth of Eddington
+double disk_temperature(double r, double M, double r_in) {
+  const double mdot_edd = (4.0 * PI * 1.67262192369e-27) / (0.1 * 6.6524587158e-29);
+  const double mdot = 0.1 * mdot_edd;
+  (void)M;
+  if (r <= r_in) return 0.0;
+  const double factor = mdot / (r * r * r);
+  double inner = 1.0 - std::sqrt(r_in / r);
+  if (inner < 0) inner = 0;
+  return std::pow(factor * inner, 0.25);
+}
+
+// temperatureToRGB (KerrBlackHole.h:1595-1646): the piecewise blackbody fit
+// the reference uses (temperature clamped to 1000..40000 K)
+V3 temperature_rgb(double temp) {
+  temp = clampd(temp, 1000.0, 40000.0);
+  temp /= 100.0;
+  double r, g, b;
+  if (temp <= 66) {
+    r = 255;
+  } else {
+    r = clampd(329.698727446 * std::pow(temp - 60, -0.1332047592), 0.0, 255.0);
+  }
+  if (temp <= 66) {
+    g = clampd(99.4708025861 * std::log(temp) - 161.1195681661, 0.0, 255.0);
+  } else {
+    g = clampd(288.1221695283 * std::pow(temp - 60, -0.0755148492), 0.0, 255.0);
+  }
+  if (temp >= 66) b = 255;
+  else if (temp <= 19) b = 0;
+  else b = clampd(138.5177312231 * std::log(temp - 10) - 305.0447927307, 0.0, 255.0);
+  return V3(r / 255.0, g / 255.0, b / 255.0);
+}
+
+// wavelengthToIntensity (relativistic.h:64-81): a Gaussian of width 100 nm
+// around the channel's wavelength, faded outside 380..750 nm
+double wl_intensity(double wl, double center) {
+  const double width = 100.0;
+  const double diff = wl - center;
+  double it = std::exp(-(diff * diff) / (2.0 * width * width));
+  if (wl < 380.0 || wl > 750.0) {
+    double fade = 1.0;
+    if (wl < 380.0) fade = std::exp(-(380.0 - wl) / 50.0);
+    else fade = std::exp(-(wl - 750.0) / 50.0);
+    it *= fade;
+  }
+  return it;
+}
+
+// applyDopplerShiftWavelength (relativistic.h:84-108): each channel's
+// wavelength (700 / 546.1 / 435.8 nm) divided by the factor, redistributed
+V3 doppler_wavelength(V3 c, double f) {
+  const double R = 700.0, G = 546.1, B = 435.8;
+  const double rw = R / f, gw = G / f, bw = B / f;
+  V3 o;
+  o.x += c.x * wl_intensity(rw, R);
+  o.y += c.x * wl_intensity(rw, G);
+  o.z += c.x * wl_intensity(rw, B);
+  o.x += c.y * wl_intensity(gw, R);
+  o.y += c.y * wl_intensity(gw, G);
+  o.z += c.y * wl_intensity(gw, B);
+  o.x += c.z * wl_intensity(bw, R);
+  o.y += c.z * wl_intensity(bw, G);
+  o.z += c.z * wl_intensity(bw, B);
+  return V3(clampd(o.x, 0, 1), clampd(o.y, 0, 1), clampd(o.z, 0, 1));
+}
+
+// applyDopplerShiftFull (relativistic.h:141-170): beaming D^4 blended with
+// the wavelength shift by the effect strength, clamped to [0, 1]
+V3 doppler_full(V3 c, double d, double effect) {
+  const double it = d * d * d * d;
+  const V3 wl = doppler_wavelength(c, 1.0 + (d - 1.0) * effect);
+  const V3 si = c * it;
+  const V3 sh = wl * effect + si * (1.0 - effect);
+  return V3(clampd(sh.x, 0, 1), clampd(sh.y, 0, 1), clampd(sh.z, 0, 1));
+}
+
+// the deterministic part of the disk branch at hit point pos: false where
+// the disk is not there (inside the ISCO, beyond the radius, off the
+// texture); else its colour, emission and alpha
+bool disk_shade(const Scene& s, const Entity& e, V3 pos, V3& color_out, V3& emission_out, double& alp_out) {
+  const KerrBH& kb = s.kerr;
+  Hit hh;
+  hh.position = pos;
+  Hit& h = hh;
+  const V3 p = h.position - kb.position;  // Coordinate_transformation (KerrBlackHole.h:461-468)
+  double sr, sth, sph;
+  cart_to_bl(p.x, p.y, p.z, kb.a, sr, sth, sph);
+  if (sr < kb.Rhor) return false;
+  if (sr > e.radius) return false;
+  if (!(sr >= kb.Rmstable)) return false;
+  // the base UVPlane's (u, v) of the hit (plane.h:228-229)
+  const double u = dot(h.position - e.org, e.du_axis) / e.du_len;
+  const double v = dot(h.position - e.org, e.dv_axis) / e.dv_len;
+  // DiscMapping::MapUV (circle.h:53-77) with rMin = Rmstable, disk_r = radius
+  const double theta = std::atan2(u / sr, v / sr);
+  const double rn = (sr - kb.Rmstable) / (e.radius - kb.Rmstable);
+  const double fx = kb.disk_w * 0.5 + kb.disk_w * rn * std::cos(theta);
+  const double fy = kb.disk_h * 0.5 + kb.disk_h * rn * std::sin(theta);
+  // int conversion truncates toward zero: in range iff -1 < f < size
+  if (!(fx > -1.0 && fx < kb.disk_w) || !(fy > -1.0 && fy < kb.disk_h)) return false;
+  const int xi = (int)fx, yi = (int)fy;
+  const unsigned char* t = &kb.disk_tex[4 * ((size_t)yi * kb.disk_w + xi)];
+  const double tmp_r = length(h.position - kb.position);
+  V3 color(t[0] / 255.0, t[1] / 255.0, t[2] / 255.0);
+  if (kb.use_temperature) {
+    const double temp = disk_temperature(tmp_r, 1.0, kb.Rmstable);
+    color = adjust_to_source_luminance(color, temperature_rgb(temp));
+  }
+  V3 emission = s.mats[e.material].emission * color;
+  double alp = t[3] / 255.0;
+  const double cl = length(color) / 3.0;
+  alp = (cl < alp) ? cl : alp;  // std::min(alp, |colour| / 3)
+  // getDiskVelocity (KerrBlackHole.h:1507-1531) about +z with sign -1, then
+  // the circular-orbit speed seen by a locally non-rotating observer
+  V3 vel;
+  {
+    const V3 rv = h.position - kb.position;
+    const double r = length(rv);
+    if (r < 1e-6) {
+      vel = V3();
+    } else {
+      const double vm = std::sqrt(1.0 / r);
+      V3 vd(0.0 * rv.z - 1.0 * rv.y, 1.0 * rv.x - 0.0 * rv.z, 0.0 * rv.y - 0.0 * rv.x);
+      vd = normalize(vd);
+      vel = vd * (vm * -1.0);
+    }
+  }
+  const double a = kb.a;
+  const double omg = 1.0 / (std::pow(tmp_r, 3.0 / 2.0) + a);
+  const double delt = tmp_r * tmp_r - 2.0 * tmp_r + a * a;
+  const double A = std::pow(tmp_r, 4.0) + a * a * tmp_r * tmp_r + 2.0 * a * a * tmp_r;
+  const double o = 2.0 * a * tmp_r / A;
+  vel = normalize(vel) * (omg - o) * A / (tmp_r * tmp_r * std::sqrt(delt));
+  // calculateDopplerFactorFromObserver (KerrBlackHole.h:1534-1562)
+  double doppler = 1.0;
+  {
+    const V3 view = normalize(h.position - kb.observer);
+    const double beta = length(vel);
+    if (!(beta < 1e-6)) {
+      const V3 vdir = normalize(vel);
+      const double cos_t = dot(view, vdir);
+      const double gamma = 1.0 / std::sqrt(1.0 - beta * beta);
+      doppler = 1.0 / (gamma * (1.0 - beta * cos_t));
+    }
+  }
+  color_out = doppler_full(color, doppler, kb.doppler_effect);
+  emission_out = doppler_full(emission, doppler, kb.doppler_effect);
+  alp_out = alp;
+  return true;
+}
+
+bool kerr_disk_texel(const Scene& s, const Entity& e, Hit& h) {
+  const KerrBH& kb = s.kerr;
+  V3 color, emission;
+  double alp;
+  if (!disk_shade(s, e, h.position, color, emission, alp)) return false;
+  if (alp == 0.0) return false;
+  if (alp < 0.99) {
+    if (!tl_disk_rnd) {  // an entry point that set no stream (first-hit queries)
+      thread_local MT64 fallback((uint64_t)(unsigned)kb.disk_seed);
+      tl_disk_rnd = &fallback;
+    }
+    if (alp <= tl_disk_rnd->next01()) return false;
+  }
+  h.ov = true;
+  h.ov_color = color;
+  h.ov_emission = emission;
+  return true;
+}
+
 int kerr_trace_one(const Scene& s, V3 org, V3 dir, Hit& hit, double* y, V3& dir2, int& cnt) {
   const KerrBH& kb = s.kerr;
   KerrRay K(kb);
@@ -1914,9 +2182,11 @@ extern "C" {
 
 // One Kerr trace per ray (intersect_scene's Kerr branch, scene.cpp:448-732).
 int oracle_kerr_trace(void* h, const double* rays, int64_t n, int32_t* status, double* final_bl, double* exit_dir,
-                      int32_t* steps, int32_t* hit_entity, double* hit_t) {
+                      int32_t* steps, int32_t* hit_entity, double* hit_t, double* hit_color, double* hit_emission) {
   auto* o = static_cast<OracleScene*>(h);
   if (!o || !rays || n < 0 || !o->s.kerr.on) return PR_E_ARG;
+  MT64 drnd((uint64_t)(unsigned)o->s.kerr.disk_seed);
+  tl_disk_rnd = &drnd;
   for (int64_t q = 0; q < n; q++) {
     const double* rr = rays + 6 * q;
     Hit hit;
@@ -1932,6 +2202,41 @@ int oracle_kerr_trace(void* h, const double* rays, int64_t n, int32_t* status, d
     exit_dir[3 * q + 2] = dir2.z;
     hit_entity[q] = (st == 1 || st == 5) ? hit.object_id : -1;
     hit_t[q] = (st == 1 || st == 5) ? hit.distance : -1.0;
+    // the hit point's material colour and emission (the disk's rewritten copy)
+    if (hit_color && hit_emission) {
+      V3 c, em;
+      if (st == 1 || st == 5) {
+        const Material m = hit_mat(o->s, hit);
+        c = m.color;
+        em = m.emission;
+      }
+      for (int k = 0; k < 3; k++) {
+        hit_color[3 * q + k] = c[k];
+        hit_emission[3 * q + k] = em[k];
+      }
+    }
+  }
+  return PR_OK;
+}
+
+// The accretion disk's shading at given points of disk entity ent
+// (circle.h:240-322 without the alpha test): valid, colour, emission, alpha.
+int oracle_kerr_disk_shade(void* h, int ent, const double* points, int64_t n, int32_t* valid, double* color,
+                           double* emission, double* alpha) {
+  auto* o = static_cast<OracleScene*>(h);
+  if (!o || !points || n < 0 || !o->s.kerr.on || ent < 0 || ent >= (int)o->s.ents.size()) return PR_E_ARG;
+  const Entity& e = o->s.ents[ent];
+  if (e.type != PR_ENT_CIRCLE || o->s.kerr.disk_tex.empty()) return PR_E_ARG;
+  for (int64_t q = 0; q < n; q++) {
+    V3 c, em;
+    double a = 0.0;
+    const bool ok = disk_shade(o->s, e, V3(points[3 * q], points[3 * q + 1], points[3 * q + 2]), c, em, a);
+    valid[q] = ok ? 1 : 0;
+    for (int k = 0; k < 3; k++) {
+      color[3 * q + k] = ok ? c[k] : 0.0;
+      emission[3 * q + k] = ok ? em[k] : 0.0;
+    }
+    alpha[q] = ok ? a : 0.0;
   }
   return PR_OK;
 }

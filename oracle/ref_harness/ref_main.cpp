@@ -9,7 +9,8 @@
 //   prender_ref firsthit <scene.txt> <rays.f64> <out.bin>  intersect_scene_ (scene.cpp:83)
 //                                                          + QBVH::CheckIntersection (QBVH.cpp:17)
 //   prender_ref qbvh     <scene.txt> <entity> <out.bin>    QBVH node + leaf arrays (QBVH.h:53)
-//   prender_ref kerr     <scene.txt> <rays.f64> <out.bin>  intersect_scene Kerr branch (scene.cpp:448)
+//   prender_ref kerr     <scene.txt> <rays.f64> <out.bin>  intersect_scene Kerr branch (scene.cpp:448),
+//                                                          with the hit point's colour and emission
 //   prender_ref radiance <scene.txt> <rays.f64> <out.f64> <seed>
 //                                                          radiance() roots (radiance.h:25)
 //
@@ -48,10 +49,15 @@ static FILE* wopen(const char* path) {
   return f;
 }
 
+// The scene's own generator (SceneEnv::rand_, scene_env.h:213), which the
+// entities' alpha tests draw from (the accretion disk, circle.h:331), is
+// seeded from the clock (scene_env.h:306); PRENDER_SCENE_RAND_SEED reseeds it
+// through its public seed() so that one-thread runs are reproducible.
 static SceneEnv* load(const char* scene) {
   SceneEnv* env = new SceneEnv();
   env->Load(const_cast<char*>(scene));
   CreateEntList(*env);
+  if (const char* sd = getenv("PRENDER_SCENE_RAND_SEED")) env->rand_.seed((unsigned)strtoul(sd, nullptr, 10));
   return env;
 }
 
@@ -155,9 +161,10 @@ int main(int argc, char** argv) {
                         p.org[0], p.org[1], p.org[2], p.dir[0], p.dir[1], p.dir[2],
                         hit ? isect.hitpoint.distance : -1.0, 0.0};
       fwrite(rec, 8, 16, f);
-      double col[3] = {isect.hitpoint.material.color.x, isect.hitpoint.material.color.y,
-                       isect.hitpoint.material.color.z};
-      fwrite(col, 8, 3, f);
+      double col[6] = {isect.hitpoint.material.color.x,    isect.hitpoint.material.color.y,
+                       isect.hitpoint.material.color.z,    isect.hitpoint.material.emission.x,
+                       isect.hitpoint.material.emission.y, isect.hitpoint.material.emission.z};
+      fwrite(col, 8, 6, f);
     }
     fclose(f);
     return 0;

@@ -58,7 +58,7 @@ class pr_medium(C.Structure):
 class pr_material(C.Structure):
     _fields_ = [
         ("type", C.c_int32),
-        ("pad0", C.c_int32),
+        ("disk_map", C.c_int32),
         ("color", D3),
         ("emission", D3),
         ("specular", D3),
@@ -81,6 +81,8 @@ class pr_entity(C.Structure):
         ("v", D3),
         ("normal", D3),
         ("radius_inner", C.c_double),
+        ("blackhole_disk", C.c_int32),
+        ("pad0", C.c_int32),
     ]
 
 
@@ -107,7 +109,13 @@ class pr_kerr(C.Structure):
         ("texture_width", C.c_int32),
         ("texture_height", C.c_int32),
         ("precision", C.c_int32),
-        ("pad0", C.c_int32),
+        ("use_accretion_disk_temperature", C.c_int32),
+        ("color_doppler_factor_effect", C.c_double),
+        ("observer", D3),
+        ("disk_texture", C.c_void_p),
+        ("disk_texture_width", C.c_int32),
+        ("disk_texture_height", C.c_int32),
+        ("disk_seed", C.c_uint64),
     ]
 
 

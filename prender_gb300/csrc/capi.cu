@@ -137,9 +137,11 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   PR_CUDA(c, upload(o.tris, h.tris, c->stream));
   PR_CUDA(c, upload(o.fnorm, h.fnorm, c->stream));
   PR_CUDA(c, upload(o.kerr_tex, h.kerr_texture, c->stream));
+  PR_CUDA(c, upload(o.kerr_disk_tex, h.kerr_disk_texture, c->stream));
   PR_CUDA(c, cudaStreamSynchronize(c->stream));
   o.kerr = h.kerr;
   o.kerr.texture = h.kerr_texture.empty() ? nullptr : (const unsigned char*)o.kerr_tex.p;
+  o.kerr.disk_tex = h.kerr_disk_texture.empty() ? nullptr : (const uchar4*)o.kerr_disk_tex.p;
   DevScene& S = o.dev;
   memset(&S, 0, sizeof(S));
   S.ents = (const GEntity*)o.ents.p;
@@ -819,11 +821,50 @@ int pr_kerr_trace(pr_ctx* c, const double* rays, int64_t n, int32_t* status, dou
   return PR_OK;
 }
 
+// the scene has a disk_map disk under its black hole (shaded from the disk texture)
+static bool has_kerr_disk(const SceneObjData& o) {
+  for (const GEntity& e : o.host.ents)
+    if (e.kerr_disk) return true;
+  return false;
+}
+
+int pr_kerr_disk_shade(pr_ctx* c, int entity, const double* points, int64_t n, int32_t* valid, double* color,
+                       double* emission, double* alpha) {
+  if (!c) return PR_E_ARG;
+  if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  if (!c->cur.kerr.enabled || !c->cur.kerr.disk_tex) return fail(c, PR_E_SCENE, "the scene has no accretion-disk texture");
+  if (entity < 0 || entity >= (int)c->cur.host.ents.size() || c->cur.host.ents[entity].type != PR_ENT_CIRCLE)
+    return fail(c, PR_E_ARG, "entity is not a disk");
+  if (n < 0 || (n > 0 && (!points || !valid || !color || !emission || !alpha))) return fail(c, PR_E_ARG, "bad buffers");
+  if (n > (int64_t)1 << 28) return fail(c, PR_E_ARG, "at most 2^28 points per call");
+  if (n == 0) return PR_OK;
+  PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
+  const size_t un = (size_t)n;
+  // staging: points 3, colour 3, emission 3, alpha 1 doubles + valid per point
+  PR_CUDA(c, c->k_sens.ensure(un * (10 * sizeof(double) + sizeof(int32_t))));
+  double* d_pts = (double*)c->k_sens.p;
+  double* d_col = d_pts + 3 * un;
+  double* d_em = d_col + 3 * un;
+  double* d_a = d_em + 3 * un;
+  int32_t* d_v = (int32_t*)(d_a + un);
+  PR_CUDA(c, cudaMemcpyAsync(d_pts, points, 24 * un, cudaMemcpyHostToDevice, c->stream));
+  PR_CUDA(c, launch_kerr_disk_shade(c->cur.dev, c->cur.kerr, entity, d_pts, n, d_v, d_col, d_em, d_a, c->stream));
+  PR_CUDA(c, cudaMemcpyAsync(valid, d_v, 4 * un, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaMemcpyAsync(color, d_col, 24 * un, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaMemcpyAsync(emission, d_em, 24 * un, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaMemcpyAsync(alpha, d_a, 8 * un, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PR_OK;
+}
+
 static int kerr_sens_common(pr_ctx* c, const double* rays, int64_t n, const double* basis, const double* cot,
                             int32_t* status, double* jac_dir, double* jac_bl, double* grad) {
   if (!c) return PR_E_ARG;
   if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
   if (!c->cur.kerr.enabled) return fail(c, PR_E_SCENE, "the scene has no black hole");
+  if (has_kerr_disk(c->cur))
+    return fail(c, PR_E_UNSUPPORTED, "the ray-bundle Jacobian does not differentiate the accretion disk's alpha test");
   if (n < 0 || (n > 0 && !rays)) return fail(c, PR_E_ARG, "bad ray buffer");
   if (n > (int64_t)1 << 28) return fail(c, PR_E_ARG, "at most 2^28 rays per call");
   if (n == 0) return PR_OK;

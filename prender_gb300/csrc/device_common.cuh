@@ -329,15 +329,27 @@ __device__ inline bool exact_qbvh(const DevScene& S, const GEntity& e, const Exa
   return false;
 }
 
+// The default hit-shading hook of exact_closest: no entity rewrites its hit.
+struct NoHitShading {
+  __device__ __forceinline__ void begin() {}
+  __device__ __forceinline__ bool circle(const GEntity&, dv3) { return true; }
+  __device__ __forceinline__ void best(const GEntity&) {}
+};
+
 // intersect_scene_ (scene.cpp:83-173): push the origin 1e-6 along the
-// direction, loop over entities, keep the strictly closest.
-__device__ inline bool exact_closest(const DevScene& S, dv3 org, dv3 dir, double& t_out, int& ent_out, int& prim_out,
-                              uint32_t* err, uint64_t& nodes, uint64_t& tris) {
+// direction, loop over entities, keep the strictly closest.  hs sees every
+// disk hit (at its hit point) before it competes for the closest, as
+// Circle::intersect's own texture branch does (circle.h:177-335), and is told
+// which entity ends up closest.
+template <class HS>
+__device__ inline bool exact_closest_hs(const DevScene& S, dv3 org, dv3 dir, double& t_out, int& ent_out,
+                                        int& prim_out, uint32_t* err, uint64_t& nodes, uint64_t& tris, HS& hs) {
   const dv3 o2 = dadd3(org, dscale3(dir, 0.000001));
   double best = kInfD;
   int ent = -1, prim = -1;
   ExactRay r;
   bool ray_ready = false;
+  hs.begin();
   for (int i = 0; i < S.n_ents; i++) {
     const GEntity& e = S.ents[i];
     double t;
@@ -349,6 +361,8 @@ __device__ inline bool exact_closest(const DevScene& S, dv3 org, dv3 dir, double
       got = exact_uvplane(e, o2, dir, t);
     } else if (e.type == PR_ENT_CIRCLE) {
       got = exact_circle(e, o2, dir, t);
+      // the hit point exactly as exact_circle forms it
+      if (got) got = hs.circle(e, {da(dm(dir.x, t), o2.x), da(dm(dir.y, t), o2.y), da(dm(dir.z, t), o2.z)});
     } else if (e.type == PR_ENT_POLYGON) {
       if (!ray_ready) {
         r = make_exact_ray(o2, dir);
@@ -360,12 +374,19 @@ __device__ inline bool exact_closest(const DevScene& S, dv3 org, dv3 dir, double
       best = t;
       ent = i;
       prim = face;
+      hs.best(e);
     }
   }
   t_out = best;
   ent_out = ent;
   prim_out = prim;
   return ent >= 0;
+}
+
+__device__ inline bool exact_closest(const DevScene& S, dv3 org, dv3 dir, double& t_out, int& ent_out, int& prim_out,
+                                     uint32_t* err, uint64_t& nodes, uint64_t& tris) {
+  NoHitShading hs;
+  return exact_closest_hs(S, org, dir, t_out, ent_out, prim_out, err, nodes, tris, hs);
 }
 
 }  // namespace pr

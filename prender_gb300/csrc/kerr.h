@@ -38,6 +38,10 @@ cudaError_t launch_kerr_sensitivity(const DevScene& S, const GKerr& K, const dou
                                     int64_t n, const double* cot, int32_t* status, double* jac_dir, double* jac_bl,
                                     double* grad, uint32_t* err, cudaStream_t stream);
 
+// accretion-disk shading at points of disk entity ent (kerr.cu)
+cudaError_t launch_kerr_disk_shade(const DevScene& S, const GKerr& K, int ent, const double* pts, int64_t n,
+                                   int32_t* valid, double* col, double* em, double* alpha, cudaStream_t stream);
+
 inline cudaError_t launch_kerr_trace(const DevScene& S, const GKerr& K, const double* rays, int64_t n, KerrOut out,
                                      uint32_t* err, unsigned long long* counters, cudaStream_t stream) {
   return K.precision == PR_KERR_FP32 ? launch_kerr_trace_fp32(S, K, rays, n, out, err, counters, stream)

@@ -295,6 +295,8 @@ struct KerrHit {
   dv3 seg_o;       // origin of the segment the hit lies on (before the 1e-6 push)
   dv3 dir2;        // last polyline direction
   double y[6];     // final state
+  bool ov;         // status 1 on the accretion disk: its rewritten colour / emission
+  float3 ovc, ove;
 };
 
 struct KerrCount {
@@ -302,9 +304,206 @@ struct KerrCount {
   uint64_t nodes, tris;
 };
 
+// ---- accretion disk under the black hole (circle.h:240-335) --------------
+// calculateLuminance (color.h:47-49)
+__device__ __forceinline__ double disk_lum(double x, double y, double z) {
+  return 0.2126 * x + 0.7152 * y + 0.0722 * z;
+}
+
+// temperatureToRGB (KerrBlackHole.h:1595-1646): the reference's piecewise
+// blackbody fit, temperature clamped to 1000..40000 K
+__device__ inline void disk_temp_rgb(double temp, double c[3]) {
+  temp = kclamp(temp, 1000.0, 40000.0);
+  temp /= 100.0;
+  double r, g, b;
+  if (temp <= 66) r = 255;
+  else r = kclamp(329.698727446 * pow(temp - 60, -0.1332047592), 0.0, 255.0);
+  if (temp <= 66) g = kclamp(99.4708025861 * log(temp) - 161.1195681661, 0.0, 255.0);
+  else g = kclamp(288.1221695283 * pow(temp - 60, -0.0755148492), 0.0, 255.0);
+  if (temp >= 66) b = 255;
+  else if (temp <= 19) b = 0;
+  else b = kclamp(138.5177312231 * log(temp - 10) - 305.0447927307, 0.0, 255.0);
+  c[0] = r / 255.0;
+  c[1] = g / 255.0;
+  c[2] = b / 255.0;
+}
+
+// wavelengthToIntensity (relativistic.h:64-81)
+__device__ __forceinline__ double disk_wl(double wl, double center) {
+  const double diff = wl - center;
+  double it = exp(-(diff * diff) / (2.0 * 100.0 * 100.0));
+  if (wl < 380.0 || wl > 750.0) it *= (wl < 380.0) ? exp(-(380.0 - wl) / 50.0) : exp(-(wl - 750.0) / 50.0);
+  return it;
+}
+
+// applyDopplerShiftFull (relativistic.h:84-170): beaming D^4 blended with a
+// wavelength shift of the three channels by the effect strength, in [0, 1]
+__device__ inline void disk_doppler(double c[3], double d, double effect) {
+  const double lam[3] = {700.0, 546.1, 435.8};
+  const double f = 1.0 + (d - 1.0) * effect;
+  double wl[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int src = 0; src < 3; src++) {
+    const double w = lam[src] / f;
+#pragma unroll
+    for (int dst = 0; dst < 3; dst++) wl[dst] += c[src] * disk_wl(w, lam[dst]);
+  }
+  const double it = d * d * d * d;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double sh = kclamp(wl[k], 0, 1) * effect + (c[k] * it) * (1.0 - effect);
+    c[k] = kclamp(sh, 0, 1);
+  }
+}
+
+// The deterministic part of the disk branch at world point p: false where
+// the disk is not there (inside the horizon or the ISCO, beyond its radius,
+// off the texture); else colour, emission and alpha (circle.h:244-322).
+__device__ inline bool kerr_disk_shade(const GKerr& K, const GEntity& e, dv3 p, double col[3], double em[3],
+                                       double& alp) {
+  const double rx = p.x - K.pos[0], ry = p.y - K.pos[1], rz = p.z - K.pos[2];
+  double sr, sth, sph;
+  cart_to_bl(rx, ry, rz, K.a, sr, sth, sph);
+  if (sr < K.Rhor || sr > e.radius || !(sr >= K.Rmstable)) return false;
+  // the base UVPlane's (u, v) of the hit (plane.h:228-229)
+  const dv3 rel = dsub3(p, ldd3(e.p));
+  const double u = ddot(rel, ldd3(e.du_axis)) / e.du_len;
+  const double v = ddot(rel, ldd3(e.dv_axis)) / e.dv_len;
+  // DiscMapping::MapUV (circle.h:53-77), rMin = ISCO, disk_r = the disk radius
+  const double theta = atan2(u / sr, v / sr);
+  const double rn = (sr - K.Rmstable) / (e.radius - K.Rmstable);
+  const double fx = K.disk_w * 0.5 + K.disk_w * rn * cos(theta);
+  const double fy = K.disk_h * 0.5 + K.disk_h * rn * sin(theta);
+  // the int conversion truncates toward zero: in range iff -1 < f < size
+  if (!(fx > -1.0 && fx < (double)K.disk_w) || !(fy > -1.0 && fy < (double)K.disk_h)) return false;
+  const uchar4 t = K.disk_tex[(size_t)(int)fy * K.disk_w + (int)fx];
+  const double tmp_r = sqrt((rx * rx + rz * rz) + ry * ry);
+  col[0] = t.x / 255.0;
+  col[1] = t.y / 255.0;
+  col[2] = t.z / 255.0;
+  if (K.use_temp) {
+    // accretionDiskTemperatureGeom (KerrBlackHole.h:1565-1593), then
+    // adjustToSourceLuminance (color.h:51-74) to 0..255 integer levels
+    double temp = 0.0;
+    if (tmp_r > K.Rmstable) {
+      const double mdot = 0.1 * ((4.0 * kPi * 1.67262192369e-27) / (0.1 * 6.6524587158e-29));
+      double inner = 1.0 - sqrt(K.Rmstable / tmp_r);
+      if (inner < 0) inner = 0;
+      temp = pow(mdot / (tmp_r * tmp_r * tmp_r) * inner, 0.25);
+    }
+    double tc[3];
+    disk_temp_rgb(temp, tc);
+    const double want = disk_lum(col[0], col[1], col[2]);
+    const double cur = disk_lum(tc[0], tc[1], tc[2]);
+    if (cur == 0.0) {
+      const double v0 = (double)(int)kclamp((double)(int)round(want / 0.2126), 0, 255);
+      col[0] = col[1] = col[2] = v0;
+    } else {
+      const double sc = want / cur;
+#pragma unroll
+      for (int k = 0; k < 3; k++) col[k] = kclamp((double)(int)round(tc[k] * sc), 0, 255);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) em[k] = e.disk_em[k] * col[k];
+  alp = t.w / 255.0;
+  const double cl = sqrt((col[0] * col[0] + col[2] * col[2]) + col[1] * col[1]) / 3.0;
+  if (cl < alp) alp = cl;  // std::min(alpha, |colour| / 3)
+  // the disk's orbital velocity (getDiskVelocity about +z with sign -1,
+  // KerrBlackHole.h:1507-1531) scaled to the circular-orbit speed seen by a
+  // locally non-rotating observer (circle.h:292-302)
+  double vx = 0.0, vy = 0.0, vz = 0.0;
+  if (!(tmp_r < 1e-6)) {
+    const double vm = sqrt(1.0 / tmp_r);
+    double dx = 0.0 * rz - 1.0 * ry, dy = 1.0 * rx - 0.0 * rz, dz = 0.0 * ry - 0.0 * rx;
+    const double il = 1.0 / sqrt((dx * dx + dz * dz) + dy * dy);
+    dx *= il;
+    dy *= il;
+    dz *= il;
+    const double sg = vm * -1.0;
+    vx = dx * sg;
+    vy = dy * sg;
+    vz = dz * sg;
+  }
+  const double a = K.a;
+  const double omg = 1.0 / (pow(tmp_r, 3.0 / 2.0) + a);
+  const double delt = tmp_r * tmp_r - 2.0 * tmp_r + a * a;
+  const double A = pow(tmp_r, 4.0) + a * a * tmp_r * tmp_r + 2.0 * a * a * tmp_r;
+  const double o = 2.0 * a * tmp_r / A;
+  {
+    const double il = 1.0 / sqrt((vx * vx + vz * vz) + vy * vy);
+    const double m = omg - o, den = tmp_r * tmp_r * sqrt(delt);
+    vx = ((vx * il) * m) * A;
+    vy = ((vy * il) * m) * A;
+    vz = ((vz * il) * m) * A;
+    if (den == 0.0) {  // Vector3d::operator/ by zero (vector3d.h:67-75)
+      vx = vy = vz = 1.0;
+    } else {
+      vx /= den;
+      vy /= den;
+      vz /= den;
+    }
+  }
+  // calculateDopplerFactorFromObserver (KerrBlackHole.h:1534-1562)
+  double dop = 1.0;
+  {
+    double wx = p.x - K.observer[0], wy = p.y - K.observer[1], wz = p.z - K.observer[2];
+    const double iw = 1.0 / sqrt((wx * wx + wz * wz) + wy * wy);
+    wx *= iw;
+    wy *= iw;
+    wz *= iw;
+    const double beta = sqrt((vx * vx + vz * vz) + vy * vy);
+    if (!(beta < 1e-6)) {
+      const double ib = 1.0 / beta;
+      const double cos_t = (wx * (vx * ib) + wz * (vz * ib)) + wy * (vy * ib);
+      const double gamma = 1.0 / sqrt(1.0 - beta * beta);
+      dop = 1.0 / (gamma * (1.0 - beta * cos_t));
+    }
+  }
+  disk_doppler(col, dop, K.doppler_effect);
+  disk_doppler(em, dop, K.doppler_effect);
+  return true;
+}
+
+// exact_closest hook of the Kerr tracer: a disk_map disk is there only where
+// its texture is and its alpha test passes; the closest hit on it carries the
+// rewritten colour and emission.  The alpha test draws from its own stream
+// (the reference draws it from the scene's generator, scene_env.h:213, :306).
+struct KerrDiskShading {
+  const GKerr* K;
+  Rng* rng;
+  bool cand, ov;
+  float3 cc, ce, oc, oe;
+  __device__ __forceinline__ void begin() { ov = false; }
+  __device__ __forceinline__ bool circle(const GEntity& e, dv3 p) {
+    cand = false;
+    if (!e.kerr_disk || !K->disk_tex) return true;
+    double col[3], em[3], alp;
+    if (!kerr_disk_shade(*K, e, p, col, em, alp)) return false;
+    if (alp == 0.0) return false;
+    if (alp < 0.99 && alp <= (double)rng->next()) return false;
+    cand = true;
+    cc = f3((float)col[0], (float)col[1], (float)col[2]);
+    ce = f3((float)em[0], (float)em[1], (float)em[2]);
+    return true;
+  }
+  __device__ __forceinline__ void best(const GEntity& e) {
+    ov = e.type == PR_ENT_CIRCLE && cand;
+    oc = cc;
+    oe = ce;
+  }
+};
+
+// the key of the alpha-test stream: the render seed mixed with the disk seed
+__device__ __forceinline__ uint64_t disk_stream_key(uint64_t seed, const GKerr& K) {
+  return seed ^ (K.disk_seed * 0x9E3779B97F4A7C15ull);
+}
+constexpr uint32_t kDiskBranch = 0xFFFFFFFFu;  // counter lane of the alpha-test stream
+
 // the Kerr branch of intersect_scene for one ray (scene.cpp:448-732)
+template <class HS>
 __device__ void kerr_trace_ray(const DevScene& S, const GKerr& K, dv3 org, dv3 dir, KerrHit& out, KerrCount& cnt,
-                               uint32_t* err) {
+                               uint32_t* err, HS& hs) {
   KerrRay k{K.a, K.a2, K.M, 0.0, 0.0};
   double* y = out.y;
   double dydx[6];
@@ -318,6 +517,7 @@ __device__ void kerr_trace_ray(const DevScene& S, const GKerr& K, dv3 org, dv3 d
   y[4] = 0;
   y[5] = 0;
   out.steps = 0;
+  out.ov = false;
   out.ent = -1;
   out.prim = -1;
   out.t = -1.0;
@@ -336,7 +536,7 @@ __device__ void kerr_trace_ray(const DevScene& S, const GKerr& K, dv3 org, dv3 d
     double t;
     int ent, prim;
     cnt.segments++;
-    if (exact_closest(S, org1, dir2, t, ent, prim, err, cnt.nodes, cnt.tris)) {
+    if (exact_closest_hs(S, org1, dir2, t, ent, prim, err, cnt.nodes, cnt.tris, hs)) {
       if (t < h_dist) {
         // hit point of intersect_scene_: (org1 + 1e-6 dir2) + t dir2
         const dv3 o2 = dadd3(org1, dscale3(dir2, 0.000001));
@@ -353,6 +553,9 @@ __device__ void kerr_trace_ray(const DevScene& S, const GKerr& K, dv3 org, dv3 d
           out.ent = ent;
           out.prim = prim;
           out.t = t;
+          out.ov = hs.ov;
+          out.ovc = hs.oc;
+          out.ove = hs.oe;
         }
         return;
       }
@@ -388,7 +591,7 @@ __device__ void kerr_trace_ray(const DevScene& S, const GKerr& K, dv3 org, dv3 d
   double t;
   int ent, prim;
   cnt.segments++;
-  if (exact_closest(S, org2, dir2, t, ent, prim, err, cnt.nodes, cnt.tris)) {
+  if (exact_closest_hs(S, org2, dir2, t, ent, prim, err, cnt.nodes, cnt.tris, hs)) {
     out.status = 5;
     out.ent = ent;
     out.prim = prim;
@@ -552,8 +755,9 @@ __device__ __forceinline__ bool no_turning_point(double r, double rplus, double 
 }
 
 // the Kerr branch of intersect_scene, mixed precision (see above)
+template <class HS>
 __device__ void kerr_trace_ray_fast(const DevScene& S, const GKerr& K, dv3 org, dv3 dir, KerrHit& out, KerrCount& cnt,
-                                    uint32_t* err) {
+                                    uint32_t* err, HS& hs) {
   KerrRay k{K.a, K.a2, K.M, 0.0, 0.0};
   double* y = out.y;
   double dydx[6];
@@ -567,6 +771,7 @@ __device__ void kerr_trace_ray_fast(const DevScene& S, const GKerr& K, dv3 org, 
   y[4] = 0;
   y[5] = 0;
   out.steps = 0;
+  out.ov = false;
   out.ent = -1;
   out.prim = -1;
   out.t = -1.0;
@@ -593,7 +798,7 @@ __device__ void kerr_trace_ray_fast(const DevScene& S, const GKerr& K, dv3 org, 
       double t;
       int ent, prim;
       cnt.segments++;
-      if (exact_closest(S, org1, dir2, t, ent, prim, err, cnt.nodes, cnt.tris)) {
+      if (exact_closest_hs(S, org1, dir2, t, ent, prim, err, cnt.nodes, cnt.tris, hs)) {
         if (t < h_dist) {
           const dv3 o2 = dadd3(org1, dscale3(dir2, 0.000001));
           const dv3 p = {o2.x + t * dir2.x, o2.y + t * dir2.y, o2.z + t * dir2.z};
@@ -609,6 +814,9 @@ __device__ void kerr_trace_ray_fast(const DevScene& S, const GKerr& K, dv3 org, 
             out.ent = ent;
             out.prim = prim;
             out.t = t;
+            out.ov = hs.ov;
+            out.ovc = hs.oc;
+            out.ove = hs.oe;
           }
           return;
         }
@@ -683,7 +891,7 @@ __device__ void kerr_trace_ray_fast(const DevScene& S, const GKerr& K, dv3 org, 
   double t;
   int ent, prim;
   cnt.segments++;
-  if (exact_closest(S, org2, dir2, t, ent, prim, err, cnt.nodes, cnt.tris)) {
+  if (exact_closest_hs(S, org2, dir2, t, ent, prim, err, cnt.nodes, cnt.tris, hs)) {
     out.status = 5;
     out.ent = ent;
     out.prim = prim;
@@ -703,8 +911,11 @@ __global__ void __launch_bounds__(128) kerr_trace_kernel(DevScene S, GKerr K, co
   if (i < n) {
     const double* r = rays + 6 * i;
     KerrHit h;
-    if (FAST) kerr_trace_ray_fast(S, K, {r[0], r[1], r[2]}, {r[3], r[4], r[5]}, h, c, err);
-    else kerr_trace_ray(S, K, {r[0], r[1], r[2]}, {r[3], r[4], r[5]}, h, c, err);
+    Rng drng;
+    drng.init(disk_stream_key(0, K), (uint64_t)i, kDiskBranch);
+    KerrDiskShading hs{&K, &drng};
+    if (FAST) kerr_trace_ray_fast(S, K, {r[0], r[1], r[2]}, {r[3], r[4], r[5]}, h, c, err, hs);
+    else kerr_trace_ray(S, K, {r[0], r[1], r[2]}, {r[3], r[4], r[5]}, h, c, err, hs);
     if (out.status) out.status[i] = h.status;
     if (out.steps) out.steps[i] = h.steps;
     if (out.final_bl) {
@@ -729,10 +940,12 @@ __global__ void __launch_bounds__(128) kerr_trace_kernel(DevScene S, GKerr K, co
 // colour radiance() returns (horizon black, background map or BACKGROUND).
 template <bool FAST>
 __device__ bool kerr_closest(const DevScene& S, const GKerr& K, float3 o, float3 d, FastHit& h, Vertex& v,
-                             float3& miss, KerrCount& c, uint32_t* err) {
+                             float3& miss, float3 ovr[2], bool& has_ovr, KerrCount& c, uint32_t* err, Rng& drng) {
   KerrHit k;
-  if (FAST) kerr_trace_ray_fast(S, K, {o.x, o.y, o.z}, {d.x, d.y, d.z}, k, c, err);
-  else kerr_trace_ray(S, K, {o.x, o.y, o.z}, {d.x, d.y, d.z}, k, c, err);
+  KerrDiskShading hs{&K, &drng};
+  if (FAST) kerr_trace_ray_fast(S, K, {o.x, o.y, o.z}, {d.x, d.y, d.z}, k, c, err, hs);
+  else kerr_trace_ray(S, K, {o.x, o.y, o.z}, {d.x, d.y, d.z}, k, c, err, hs);
+  has_ovr = false;
   if (k.status != 1) {
     if (k.status == 2) miss = f3(0, 0, 0);
     else if (k.status == 0) miss = kerr_background(K, k.y, S.bg);
@@ -756,6 +969,11 @@ __device__ bool kerr_closest(const DevScene& S, const GKerr& K, float3 o, float3
   v.ent = k.ent;
   v.mat = e.material;
   v.t = (float)k.t;
+  if (k.ov) {  // the accretion disk's own colour and emission at this point
+    has_ovr = true;
+    ovr[0] = k.ovc;
+    ovr[1] = k.ove;
+  }
   h.t = (float)k.t;
   h.ent = k.ent;
   h.slot = -1;
@@ -772,17 +990,21 @@ __device__ float3 kerr_trace_sample(const DevScene& S, const GKerr& K, const Ren
   int sp = 0;
   root_path(stack[sp++], o0, d0);
   float3 L = f3(0, 0, 0);
+  Rng drng;  // the accretion disk's alpha tests of this camera sample
+  drng.init(disk_stream_key(cfg.seed, K), sample_id, kDiskBranch);
   while (sp > 0) {
     PathState ps = stack[--sp];
     for (;;) {
       FastHit h;
       Vertex v;
-      float3 miss;
-      const bool hit = kerr_closest<FAST>(S, K, ps.o, ps.d, h, v, miss, c, err);
+      float3 miss, ovr[2];
+      bool has_ovr;
+      const bool hit = kerr_closest<FAST>(S, K, ps.o, ps.d, h, v, miss, ovr, has_ovr, c, err, drng);
       ShadowReq sh[3];
       int nsh = 0;
       PathState child;
-      const int r = shade(S, cfg, ps, hit, h, sample_id, sh, nsh, child, err, &v, &miss);
+      const int r = shade(S, cfg, ps, hit, h, sample_id, sh, nsh, child, err, &v, &miss, nullptr, nullptr,
+                          has_ovr ? ovr : nullptr);
       if (r == SHADE_SPLIT) {
         if (sp < kSplitStack) stack[sp++] = child;
         else atomicOr(err, PR_DEV_LOOP_CAP);

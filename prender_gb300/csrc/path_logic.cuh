@@ -266,12 +266,13 @@ __device__ __forceinline__ float dd_bssrdf(const GMaterial& m, float3 xi, float3
 // instantiation).  A tracer
 // that builds the vertex itself (the Kerr geodesic tracer) passes it as pre,
 // and the colour a miss returns as miss (radiance.h:30-43); straight-ray
-// callers leave both null.
+// callers leave both null.  ovr (colour, emission) replaces the material's
+// where the entity rewrote its hit point's copy (the accretion disk).
 template <bool SSS = false>
 __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& ps, bool hit, const FastHit& h,
                      uint64_t sample_id, ShadowReq* sh, int& nsh, PathState& child, uint32_t* err,
                      const Vertex* pre = nullptr, const float3* miss = nullptr, EmissionTap* tap = nullptr,
-                     SssFrameOut* frame = nullptr) {
+                     SssFrameOut* frame = nullptr, const float3* ovr = nullptr) {
   nsh = 0;
   const bool nee = cfg.nee != 0;
   const bool media = cfg.media != 0 && S.medium.on != 0;
@@ -299,7 +300,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   else make_vertex(S, ps.o, ps.d, h, v);
   const GMaterial& m = S.mats[v.mat];
   const GEntF& ent = S.entf[v.ent];
-  const float3 E = ld3(m.emission), C = ld3(m.color);
+  const float3 E = ovr ? ovr[1] : ld3(m.emission), C = ovr ? ovr[0] : ld3(m.color);
   const float3 d = ps.d;
   const float3 on = dot(v.n, d) < 0.0f ? v.n : -v.n;
   float p_rr = maxc(E + C);  // WARD / PHONG are not on this path

@@ -81,6 +81,13 @@ struct GEntity {
   float bmin[3], bmax[3];  // bounds (for scene extents)
   double bb_min[3], bb_max[3];  // Entity::boundingBox of the reference (sphere / mesh / uvplane)
   double sss_rmax;
+  // accretion disk under the black hole (circle.h:240-335): set when the
+  // disk's material has disk_map and the hole has a disk texture
+  int32_t kerr_disk;
+  int32_t pad1;
+  double du_axis[3], dv_axis[3];  // the base UVPlane's unit axes and lengths (plane.h:146-157)
+  double du_len, dv_len;
+  double disk_em[3];              // the material's emission, FP64
 };
 
 // FP32 copy of an entity for the render path (no FP64 conversions in the
@@ -125,6 +132,15 @@ struct GKerr {
   int32_t precision;             // PR_KERR_FP64 / PR_KERR_FP32
   double scene_radius;           // farthest scene geometry from the hole (BL-safe bound)
   double scene_inner;            // nearest scene geometry to the hole (0: something at the hole)
+  // accretion disk (circle.h:240-335)
+  double Rmstable;               // inner_orbit() (KerrBlackHole.h:215-240)
+  double doppler_effect;         // color_doppler_factor_effect
+  double observer[3];            // camera_pos of the black hole
+  const uchar4* disk_tex;        // RGBA8 rows as cell(y, x) reads them; null = none
+  int32_t disk_w, disk_h;
+  int32_t use_temp;              // use_accretion_disk_temperature
+  int32_t pad0;
+  uint64_t disk_seed;            // key of the alpha-test stream
 };
 
 // Everything a kernel needs, passed by value (fits the 4 KB param space).

@@ -471,6 +471,16 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
       g.u_length = pe.radius;
       g.v_length = pe.radius_inner;
       g.area = pe.radius * pe.radius * 3.14159265358979323846;
+      // the base UVPlane's own axes and lengths (plane.h:146-157): the disk
+      // texture reads its (u, v) through them
+      const D3 Uu = unit(U), Vu = unit(V);
+      for (int k = 0; k < 3; k++) {
+        g.du_axis[k] = (&Uu.x)[k];
+        g.dv_axis[k] = (&Vu.x)[k];
+      }
+      g.du_len = len(U);
+      g.dv_len = len(V);
+      for (int k = 0; k < 3; k++) g.disk_em[k] = pm.emission[k];
       for (int k = 0; k < 3; k++) { grow(pe.p[k] - pe.radius); grow(pe.p[k] + pe.radius); }
     } else if (pe.type == PR_ENT_POLYGON) {
       if (pe.mesh < 0 || pe.mesh >= d->n_meshes) { err = "entity mesh out of range"; return PR_E_SCENE; }
@@ -642,6 +652,43 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
       hs.kerr_texture.assign(pk.texture, pk.texture + 3 * (size_t)pk.texture_width * pk.texture_height);
       k.tex_w = pk.texture_width;
       k.tex_h = pk.texture_height;
+    }
+    // accretion disk: inner_orbit (KerrBlackHole.h:215-240) with M = 1 and
+    // the class's cbrt(x) = pow(x, 1/3)
+    {
+      const double M = k.M, a = k.a, a2 = k.a2, m2 = M * M;
+      auto cbrt_r = [](double x) { return std::pow(x, 1.0 / 3.0); };
+      const double z1 = 1 + cbrt_r(1 - a2 / m2) * (cbrt_r(1 + a / M) + cbrt_r(1 - a / M));
+      const double z2 = std::sqrt(3 * a2 / m2 + z1 * z1);
+      k.Rmstable = M * (3 + z2 - std::sqrt((3 - z1) * (3 + z1 + 2 * z2)));
+    }
+    k.use_temp = pk.use_accretion_disk_temperature ? 1 : 0;
+    k.doppler_effect = pk.color_doppler_factor_effect;
+    for (int q = 0; q < 3; q++) k.observer[q] = pk.observer[q];
+    k.disk_seed = pk.disk_seed;
+    hs.kerr_disk_texture.clear();
+    if (pk.disk_texture) {
+      if (pk.disk_texture_width <= 0 || pk.disk_texture_height <= 0) {
+        err = "accretion disk texture size must be positive";
+        return PR_E_ARG;
+      }
+      hs.kerr_disk_texture.assign(pk.disk_texture,
+                                  pk.disk_texture + 4 * (size_t)pk.disk_texture_width * pk.disk_texture_height);
+      k.disk_w = pk.disk_texture_width;
+      k.disk_h = pk.disk_texture_height;
+    }
+    for (size_t i = 0; i < hs.ents.size(); i++) {
+      GEntity& e = hs.ents[i];
+      const pr_entity& pe = d->entities[i];
+      const pr_material& pm = d->materials[pe.material];
+      if (e.type != PR_ENT_CIRCLE || pe.blackhole_disk < 0 || !pm.disk_map) continue;
+      // the reference indexes its disk-texture list with blackhole_disk (circle.h:240-242)
+      if (hs.kerr_disk_texture.empty() || pe.blackhole_disk != 0) {
+        err = "a disk_map disk under the black hole needs accretion-disk texture 0";
+        return PR_E_SCENE;
+      }
+      if (!(e.radius > k.Rmstable)) { err = "the accretion disk must reach beyond the ISCO"; return PR_E_SCENE; }
+      e.kerr_disk = 1;
     }
   }
   return PR_OK;

@@ -41,6 +41,7 @@ struct HostScene {
   float scene_scale = 1.0f;
   GKerr kerr{};
   std::vector<unsigned char> kerr_texture;
+  std::vector<unsigned char> kerr_disk_texture;  // RGBA8
   bool disk_light = false;  // an emitting disk is registered as a light
 };
 

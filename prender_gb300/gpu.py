@@ -186,6 +186,18 @@ class Context:
             out["grad"] = g
         return out
 
+    def kerr_disk_shade(self, entity: int, points: np.ndarray) -> dict:
+        """The accretion disk's texture / temperature / Doppler shading at
+        world points of disk entity (no alpha test): valid, colour,
+        emission, alpha."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        n = pts.shape[0]
+        out = dict(valid=np.empty(n, np.int32), color=np.empty((n, 3)), emission=np.empty((n, 3)),
+                   alpha=np.empty(n))
+        self._check(self.L.pr_kerr_disk_shade(self.h, int(entity), _p(pts), n, _p(out["valid"]), _p(out["color"]),
+                                              _p(out["emission"]), _p(out["alpha"])))
+        return out
+
     def render(self, scene=None, settings=None, camera=None, sample_offset: int = 0,
                accumulate: np.ndarray | None = None) -> np.ndarray:
         """Render::Run: returns the (H, W, 3) float32 image in the reference's

@@ -57,6 +57,7 @@ class Material:
     refractive_index: float = 1.5
     medium: Medium = field(default_factory=Medium)
     r_refractive_index: float = 1.0
+    disk_map: int = 0
 
     @staticmethod
     def diffuse(color, emission=(0.0, 0.0, 0.0)) -> "Material":
@@ -99,6 +100,7 @@ class Material:
         m.refractive_index = float(self.refractive_index)
         m.medium = self.medium.to_c()
         m.r_refractive_index = float(self.r_refractive_index)
+        m.disk_map = int(self.disk_map)
         return m
 
 
@@ -114,6 +116,7 @@ class Entity:
     v: Sequence[float] = (0.0, 0.0, 0.0)
     normal: Sequence[float] = (0.0, 0.0, 1.0)
     radius_inner: float = 0.0
+    blackhole_disk: int = 0
 
     def to_c(self) -> A.pr_entity:
         e = A.pr_entity()
@@ -124,6 +127,7 @@ class Entity:
         e.v[:] = [float(x) for x in self.v]
         e.normal[:] = [float(x) for x in self.normal]
         e.radius_inner = float(self.radius_inner)
+        e.blackhole_disk = int(self.blackhole_disk)
         return e
 
 
@@ -247,6 +251,17 @@ class SceneDesc:
                 self._keep.append(tex)
                 k.texture = tex.ctypes.data
                 k.texture_height, k.texture_width = tex.shape[0], tex.shape[1]
+            k.use_accretion_disk_temperature = int(bool(scene.kerr.get("disk_temperature", False)))
+            k.color_doppler_factor_effect = float(scene.kerr.get("doppler_effect", 0.0))
+            obs = scene.kerr.get("observer")
+            k.observer[:] = [float(x) for x in (scene.camera.position if obs is None else obs)]
+            k.disk_seed = int(scene.kerr.get("disk_seed", 1)) & 0xFFFFFFFF
+            dt = scene.kerr.get("disk_texture")
+            if dt is not None:
+                dt = _rgba(dt)
+                self._keep.append(dt)
+                k.disk_texture = dt.ctypes.data
+                k.disk_texture_height, k.disk_texture_width = dt.shape[0], dt.shape[1]
         d.kerr = k
         self.desc = d
 
@@ -291,13 +306,27 @@ class Scene:
 
     def set_black_hole(self, position, a: float, max_steps: int = 10000,
                        map_coef=(1.0, 0.0, 1.0, 0.0), escape_radius: float = 0.0,
-                       texture=None, texture_coef: float = 1.0, precision: int = A.PR_KERR_FP64) -> None:
+                       texture=None, texture_coef: float = 1.0, precision: int = A.PR_KERR_FP64,
+                       disk_texture=None, disk_temperature: bool = False, doppler_effect: float = 0.0,
+                       observer=None, disk_seed: int = 1) -> None:
         """A Kerr black hole of mass 1 ('BLACKHOLE x y z' block, scene_env.h:701-766);
         texture is the background map as an (H, W, 3) uint8 array indexed
-        [y, x] the way the reference's Bitmap::cell(y, x) reads its image."""
+        [y, x] the way the reference's Bitmap::cell(y, x) reads its image.
+
+        disk_texture ((H, W, 3) or (H, W, 4) uint8, same indexing) is
+        accretion_disk_texture 0: disks whose material has disk_map set are
+        shaded from it with the ISCO cut, the Doppler shift of the disk's
+        orbital motion seen from observer (default: the camera position) and
+        the texture's alpha test (circle.h:240-335).  disk_temperature and
+        doppler_effect are use_accretion_disk_temperature and
+        color_doppler_factor_effect; disk_seed seeds the alpha-test stream."""
         self.kerr = {"position": tuple(float(x) for x in position), "a": float(a), "max_steps": int(max_steps),
                      "map_coef": tuple(float(x) for x in map_coef), "escape_radius": float(escape_radius),
-                     "texture": texture, "texture_coef": float(texture_coef), "precision": int(precision)}
+                     "texture": texture, "texture_coef": float(texture_coef), "precision": int(precision),
+                     "disk_texture": disk_texture, "disk_temperature": bool(disk_temperature),
+                     "doppler_effect": float(doppler_effect),
+                     "observer": None if observer is None else tuple(float(x) for x in observer),
+                     "disk_seed": int(disk_seed)}
 
     def add_mesh(self, vertices, faces, material: Material, normal_inverse: int = 1) -> int:
         self.meshes.append(Mesh(vertices, faces))
@@ -353,7 +382,21 @@ class Scene:
                 tex_path = os.path.join(directory, "background.bmp")
                 _write_bmp24(tex_path, np.asarray(k["texture"], dtype=np.uint8))
                 out += [f"background_texture {tex_path}", f"coef {_fmt(k.get('texture_coef', 1.0))}"]
+            if k.get("disk_texture") is not None:
+                dt = _rgba(k["disk_texture"])
+                if (dt[:, :, 3] != 255).any():
+                    raise ValueError("the 24-bit BMP writer carries no alpha; give an opaque disk texture")
+                disk_path = os.path.join(directory, "disk.bmp")
+                _write_bmp24(disk_path, np.ascontiguousarray(dt[:, :, :3]))
+                out.append(f"accretion_disk_texture {disk_path}")
             out.append("")
+            obs = k.get("observer")
+            if obs is not None and tuple(float(x) for x in obs) != tuple(float(x) for x in cam.position):
+                raise ValueError("the reference takes the disk's observer from CAMERA_POS")
+            if k.get("disk_temperature"):
+                out += ["use_accretion_disk_temperature", "1", ""]
+            if k.get("doppler_effect", 0.0):
+                out += ["color_doppler_factor_effect", _fmt(k["doppler_effect"]), ""]
         md = self.medium
         out += ["SCATTERING", "0", f3(md.sigma_s_rgb), "",
                 "ABSORBING", "0", f3(md.sigma_a_rgb), "",
@@ -370,6 +413,8 @@ class Scene:
                 out += [f"uvplane {f3(e.p)}", f"U {f3(e.u)}", f"V {f3(e.v)}"]
             elif e.type == A.PR_ENT_CIRCLE:
                 out += [f"disk2 {f3(e.p)} {_fmt(e.radius)} {_fmt(e.radius_inner)}", f"normal {f3(e.normal)}"]
+                # the keyword sets a scene-wide value every later disk inherits (scene_env.h:1177-1181)
+                out.append(f"blackhole_disk {int(e.blackhole_disk)}")
             elif e.type == A.PR_ENT_POLYGON:
                 objname = f"mesh{e.mesh}.obj"
                 _write_obj(os.path.join(directory, objname), self.meshes[e.mesh])
@@ -393,6 +438,8 @@ class Scene:
                 if float(md.scale) != 1.0:
                     out += ["MATERIAL_SCALE", _fmt(md.scale)]
             out += [f"emission {f3(m.emission)}", f"color {f3(m.color)}"]
+            if m.disk_map:
+                out.append(f"disk_map {int(m.disk_map)}")
             if e.normal_inverse < 0:
                 out.append("normal -1")
             if m.type in refl:
@@ -421,6 +468,18 @@ def _fmt(x) -> str:
     if len(digits) > 15:
         raise ValueError(f"{x!r} needs more than 15 significant digits in the reference scene format")
     return s
+
+
+def _rgba(tex) -> np.ndarray:
+    """(H, W, 3) or (H, W, 4) uint8 texture as contiguous RGBA (alpha 255
+    where none is given, as BitMap::Read sets it for 24-bit images,
+    bitmap.cpp:116-123)."""
+    t = np.asarray(tex, dtype=np.uint8)
+    if t.ndim != 3 or t.shape[2] not in (3, 4):
+        raise ValueError("disk texture must be (H, W, 3) or (H, W, 4) uint8")
+    if t.shape[2] == 3:
+        t = np.concatenate([t, np.full(t.shape[:2] + (1,), 255, np.uint8)], axis=2)
+    return np.ascontiguousarray(t)
 
 
 def _write_bmp24(path: str, tex: np.ndarray) -> None:

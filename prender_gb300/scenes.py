@@ -276,6 +276,71 @@ def kerr_lensing(a: float = 0.999, width: int = 2048, height: int = 1024, max_st
     return s
 
 
+def accretion_texture(width: int = 512, height: int = 512, seed: int = 0, arms: int = 7) -> np.ndarray:
+    """Procedural accretion-disk map for DiscMapping::MapUV (circle.h:53-77):
+    the disk's normalised radius rn maps to the distance rn * size from the
+    image centre, so the annulus rn in [0, 0.5] fills the image.  Hot white
+    inner rim cooling to orange and deep red outward, seeded spiral
+    turbulence streaks; (H, W, 3) uint8 indexed [y, x] as cell(y, x)."""
+    rng = np.random.default_rng(seed)
+    ys, xs = np.meshgrid(np.arange(height), np.arange(width), indexing="ij")
+    dx = (xs + 0.5) / width - 0.5
+    dy = (ys + 0.5) / height - 0.5
+    rn = np.sqrt(dx * dx + dy * dy) * 2.0  # 0 at the ISCO, 1 at the image edge
+    th = np.arctan2(dy, dx)
+    phase = rng.uniform(0.0, 2.0 * np.pi, arms)
+    twist = rng.uniform(4.0, 9.0, arms)
+    turb = np.zeros_like(rn)
+    for k in range(arms):
+        turb += np.sin((k + 2) * th + twist[k] * np.log1p(6.0 * rn) + phase[k])
+    turb = 0.5 + 0.5 * turb / arms
+    heat = np.clip(1.0 - rn, 0.0, 1.0)
+    bright = np.clip((0.35 + 0.65 * turb) * (0.25 + 0.75 * heat ** 0.7), 0.0, 1.0)
+    r = np.clip(255.0 * bright * (0.85 + 0.15 * heat), 0, 255)
+    g = np.clip(255.0 * bright * (0.25 + 0.7 * heat ** 1.5), 0, 255)
+    b = np.clip(255.0 * bright * (0.05 + 0.9 * heat ** 3.0), 0, 255)
+    tex = np.stack([r, g, b], axis=-1)
+    tex[rn > 1.0] = 0.0
+    return np.ascontiguousarray(tex.astype(np.uint8))
+
+
+def kerr_accretion(a: float = 0.999, width: int = 2048, height: int = 1024, max_steps: int = 4000,
+                   fov: float = 60.0, texture=None, disk_texture=None, doppler_effect: float = 0.3,
+                   disk_temperature: bool = False, escape_radius: float = 0.0, r_cam: float = 6.03,
+                   samples: int = 1, supersamples: int = 1, precision: int = A.PR_KERR_FP64,
+                   disk_seed: int = 1, elevation: float = 0.0) -> Scene:
+    """The Kerr lensing view with a textured accretion disk: 'disk2 0 0 0 15 3'
+    with 'blackhole_disk 0' and a disk_map material, the procedural disk map
+    as accretion_disk_texture, color_doppler_factor_effect doppler_effect
+    and the celestial sphere behind; camera at Boyer-Lindquist r = r_cam M
+    in the disk plane looking at the hole (elevation > 0 degrees lifts it
+    above the plane at the same Cartesian distance)."""
+    s = Scene()
+    m = Material.diffuse((0.0, 0.0, 0.0), emission=(2.0, 2.0, 2.0))
+    m.disk_map = 1
+    s.add_disk((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 15.0, m, radius_inner=3.0)
+    if texture is None:
+        texture = celestial_texture(1024, 512, stars=10000, seed=0)
+    elif texture is False:  # no background map: escaped rays take BACKGROUND
+        texture = None
+    if disk_texture is None:
+        disk_texture = accretion_texture(512, 512, seed=0)
+    s.set_black_hole((0.0, 0.0, 0.0), a, max_steps=max_steps, escape_radius=escape_radius, texture=texture,
+                     precision=precision, disk_texture=disk_texture, disk_temperature=disk_temperature,
+                     doppler_effect=doppler_effect, disk_seed=disk_seed)
+    dist = math.sqrt(r_cam * r_cam + a * a)  # BL (r, pi/2, 3 pi/2) in Cartesian
+    if elevation == 0.0:
+        s.camera = Camera(position=(0.0, round(-dist, 12), 0.0), dir=(0.0, 1.0, 0.0), up=(0.0, 0.0, 1.0),
+                          width=width, height=height, angle=fov)
+    else:
+        el = math.radians(elevation)
+        c, sn = round(math.cos(el), 12), round(math.sin(el), 12)  # decimal-exact in the scene text
+        s.camera = Camera(position=(0.0, round(-dist * c, 10), round(dist * sn, 10)), dir=(0.0, c, -sn),
+                          up=(0.0, 0.0, 1.0), width=width, height=height, angle=fov)
+    s.settings = RenderSettings(samples=samples, supersamples=supersamples, depth=1, depth_limit=1, nee=0)
+    return s
+
+
 def random_rays(scene_bounds_lo, scene_bounds_hi, n: int, seed: int = 0, inside=True) -> np.ndarray:
     """n rays (org xyz, dir xyz) with origins uniform in the box and
     directions uniform on the sphere; FP64, 6 per ray."""

@@ -12,7 +12,8 @@ its build on the machine that runs them.
 
     python tests/golden/make_golden.py --sss-oracle
 
-writes sss_oracle.npz from the oracle alone (no reference build needed).
+writes sss_oracle.npz from the oracle alone (no reference build needed);
+--disk-oracle writes kerr_disk_oracle.npz the same way.
 """
 import os
 import struct
@@ -31,8 +32,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "prender_ref")
 
 
-def run_ref(args, cwd, threads=1):
-    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+def run_ref(args, cwd, threads=1, scene_seed=1):
+    # PRENDER_SCENE_RAND_SEED: the harness reseeds the scene's own generator
+    # (the accretion disk's alpha test), which the reference seeds from the clock
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads), PRENDER_SCENE_RAND_SEED=str(scene_seed))
     r = subprocess.run([REF_BIN] + args, cwd=cwd, capture_output=True, text=True, env=env)
     if r.returncode != 0:
         raise RuntimeError(f"reference failed: {args}\n{r.stderr[-2000:]}")
@@ -74,12 +77,13 @@ def ref_render(path, shape, d, threads=1):
 
 def ref_kerr(path, rays, d):
     """harness record per ray: object id, hit flag, 16 doubles (loop ended,
-    steps, y[6], org2, dir2, hit distance, 0), hit colour"""
+    steps, y[6], org2, dir2, hit distance, 0), hit colour and emission"""
     rays.astype(np.float64).tofile(os.path.join(d, "rays.f64"))
     run_ref(["kerr", path, os.path.join(d, "rays.f64"), os.path.join(d, "k.bin")], d)
-    rec = np.dtype([("obj", "<i4"), ("hit", "<i4"), ("rec", "<f8", 16), ("col", "<f8", 3)])
+    rec = np.dtype([("obj", "<i4"), ("hit", "<i4"), ("rec", "<f8", 16), ("col", "<f8", 3), ("em", "<f8", 3)])
     k = np.fromfile(os.path.join(d, "k.bin"), dtype=rec)
-    return dict(obj=k["obj"].copy(), hit=k["hit"].copy(), rec=k["rec"].copy())
+    return dict(obj=k["obj"].copy(), hit=k["hit"].copy(), rec=k["rec"].copy(), col=k["col"].copy(),
+                em=k["em"].copy())
 
 
 def kerr_golden(d):
@@ -108,6 +112,48 @@ def kerr_golden(d):
     imgs["texture_highspp"] = img.astype(np.float32)
     print("kerr texture_highspp", info)
     np.savez_compressed(os.path.join(HERE, "kerr_render.npz"), **imgs)
+
+
+def disk_golden(d):
+    """textured accretion disk under the black hole: per-ray traces with the
+    hit point's colour and emission, one-thread renders (the harness seeds
+    the scene's alpha-test generator with the scenes' disk_seed, 1)"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import kerr_cases
+    out = {}
+    for name, (sc, rays) in kerr_cases.disk_trace_cases().items():
+        dd = os.path.join(d, "kd_" + name)
+        os.makedirs(dd)
+        r = ref_kerr(sc.write_reference(dd), rays, dd)
+        out[f"{name}_rays"] = rays
+        out.update({f"{name}_{k}": v for k, v in r.items()})
+    for name, sc in kerr_cases.disk_render_cases().items():
+        dd = os.path.join(d, "kdr_" + name)
+        os.makedirs(dd)
+        img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+        out[f"render_{name}"] = img
+        print("disk", name, info)
+    np.savez_compressed(os.path.join(HERE, "kerr_disk.npz"), **out)
+
+
+def disk_oracle_golden(nb=16):
+    """16 independent renders of the textured-disk high-spp case by the
+    oracle (pinned to the reference by kerr_disk.npz): per-pixel mean and
+    standard deviation for the GPU's statistical parity."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import kerr_cases
+    from oracle import oracle as O
+    sc = kerr_cases.disk_highspp_case()
+    imgs = []
+    for k in range(nb):
+        sc.settings.seed = 100 + k
+        sc.kerr["disk_seed"] = 1000 + k
+        img, _, _ = O.OracleScene(sc).render(threads=os.cpu_count())
+        imgs.append(img)
+    b = np.stack(imgs)
+    np.savez_compressed(os.path.join(HERE, "kerr_disk_oracle.npz"), mean=b.mean(0).astype(np.float32),
+                        sd=b.std(0, ddof=1).astype(np.float32), batches=np.int32(nb))
+    print("disk oracle batches", nb)
 
 
 def sss_golden(d):
@@ -152,6 +198,9 @@ def main():
     if "--sss-oracle" in sys.argv:
         sss_oracle_golden()
         return
+    if "--disk-oracle" in sys.argv:
+        disk_oracle_golden()
+        return
     if not os.path.exists(REF_BIN):
         args = [a for a in sys.argv[1:] if not a.startswith("--")]
         ref = args[0] if args else "/root/reference"
@@ -160,12 +209,17 @@ def main():
         with tempfile.TemporaryDirectory() as d:
             kerr_golden(d)
         return
+    if "--disk-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            disk_golden(d)
+        return
     if "--sss-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             sss_golden(d)
         return
     with tempfile.TemporaryDirectory() as d:
         kerr_golden(d)
+        disk_golden(d)
         sss_golden(d)
         # -- QBVH structure + first hits on the subdiv-3 mesh Cornell box
         s = scenes.mesh_cornell(width=32, height=24, samples=1, supersamples=2, subdiv=3)

@@ -62,3 +62,36 @@ def highspp_case():
     s.kerr["map_coef"] = (1.0, 0.3, 1.0, -0.7)
     s.kerr["texture_coef"] = 1.5
     return s
+
+
+def disk_scene(width: int, height: int, samples: int = 1, supersamples: int = 1, a: float = 0.9,
+               max_steps: int = 600, temperature: bool = False, doppler: float = 0.3, escape: float = 0.0,
+               disk_seed: int = 1):
+    """The textured accretion disk (disk_map, blackhole_disk 0, a 128 x 128
+    procedural disk map, Doppler shift) seen from 30 M, 20 degrees above the
+    disk plane, with a plain background (no map: an escape radius does not
+    change what an escaped ray returns)."""
+    s = scenes.kerr_accretion(a=a, width=width, height=height, max_steps=max_steps, fov=50.0, texture=False,
+                              disk_texture=scenes.accretion_texture(128, 128, seed=0), doppler_effect=doppler,
+                              disk_temperature=temperature, escape_radius=escape, r_cam=30.0, elevation=20.0,
+                              samples=samples, supersamples=supersamples, disk_seed=disk_seed)
+    s.background = (0.02, 0.03, 0.05)
+    return s
+
+
+def disk_trace_cases():
+    """name -> (scene, rays) for the per-ray trace with the disk's shading."""
+    s1 = disk_scene(32, 16)
+    s2 = disk_scene(24, 12, a=0.6, temperature=True, doppler=0.6)
+    return {"tex_a09": (s1, scenes.camera_rays(s1)), "temp_a06": (s2, scenes.camera_rays(s2))}
+
+
+def disk_render_cases():
+    """name -> scene for one-thread textured-disk renders (bit-exact)."""
+    return {"tex": disk_scene(24, 12, samples=2), "temp": disk_scene(16, 8, a=0.6, temperature=True, doppler=0.6)}
+
+
+def disk_highspp_case():
+    """The textured-disk render for statistical image parity (16 batches of
+    64 x 2^2 samples); an escape radius keeps the oracle's batches short."""
+    return disk_scene(48, 24, samples=64, supersamples=2, escape=60.0)

@@ -220,3 +220,63 @@ def test_kerr_ray_bundle_jacobian_against_central_differences(ctx):
     assert np.quantile(rel, 0.95) < 1e-2
     assert np.isnan(J["jac_dir"][J["status"] != 0]).all()
     np.testing.assert_allclose(J["grad"][ok], np.einsum("ni,nij->nj", w[ok], J["jac_dir"][ok]), rtol=1e-12, atol=1e-14)
+
+
+def test_accretion_disk_shading_matches_oracle(ctx):
+    """The textured disk's deterministic branch (circle.h:244-322: ISCO and
+    radius cuts, disk-map texel, temperature colours, Doppler shift of colour
+    and emission, alpha) at 20,000 points of the disk plane, GPU against the
+    oracle: same valid set and texels, values to 1e-9 (CUDA's atan2 / cos /
+    sin / pow / exp may differ from the host libm in the last bit)."""
+    rng = np.random.default_rng(7)
+    r = np.sqrt(rng.uniform(0.0, 16.0 ** 2, 20000))
+    ph = rng.uniform(0.0, 2.0 * np.pi, r.shape)
+    pts = np.stack([r * np.cos(ph), r * np.sin(ph), np.zeros_like(r)], 1)
+    for temperature, doppler, a in ((False, 0.3, 0.9), (True, 0.6, 0.6), (False, 1.0, 0.999)):
+        s = kerr_cases.disk_scene(16, 8, a=a, temperature=temperature, doppler=doppler)
+        ctx.upload(s)
+        g = ctx.kerr_disk_shade(0, pts)
+        o = O.OracleScene(s).kerr_disk_shade(0, pts)
+        v = o["valid"] == 1
+        print(f"disk shade a={a} temperature={temperature}: {v.sum()} valid, max |dcolour| "
+              f"{np.abs(g['color'] - o['color']).max():.2e}, max |demission| {np.abs(g['emission'] - o['emission']).max():.2e}")
+        assert v.sum() > 2000
+        assert np.array_equal(g["valid"], o["valid"])
+        assert np.abs(g["color"] - o["color"]).max() < 1e-9
+        assert np.abs(g["emission"] - o["emission"]).max() < 1e-9
+        assert np.abs(g["alpha"] - o["alpha"]).max() < 1e-9
+
+
+@pytest.mark.parametrize("precision", [A.PR_KERR_FP64, A.PR_KERR_FP32])
+def test_accretion_disk_render_matches_oracle_statistically(ctx, golden, precision):
+    """The textured-disk render (alpha test from the GPU's own counter-based
+    stream) against the oracle's 16 x 256 spp: per-pixel 3 sigma with both
+    sides' spreads, RMSE at the noise level, mean within 1 %."""
+    s = kerr_cases.disk_highspp_case()
+    s.kerr["precision"] = precision
+    ctx.upload(s)
+    orc = golden["kerr_disk_oracle"]
+    o_mean = orc["mean"].astype(np.float64)
+    o_sd = orc["sd"].astype(np.float64)
+    o_nb = int(orc["batches"])
+    nb, spp = 16, s.settings.spp
+    b = _batches(ctx, s, nb, spp)
+    mean = b.mean(0)
+    sd = b.std(0, ddof=1)
+    sigma = np.sqrt(sd ** 2 / nb + o_sd ** 2 / o_nb) + 1e-6
+    frac = float((np.abs(mean - o_mean) / sigma > 3.0).mean())
+    rmse = float(np.sqrt(((mean - o_mean) ** 2).mean()))
+    noise = float(np.sqrt((sigma ** 2).mean()))
+    rel = abs(mean.mean() - o_mean.mean()) / o_mean.mean()
+    print(f"accretion disk render (precision {precision}): >3 sigma {frac:.4f}, rmse {rmse:.3e} vs noise "
+          f"{noise:.3e}, mean rel diff {rel:.4f}")
+    assert rel < 0.01
+    assert frac < 0.02
+    assert rmse < 1.3 * noise
+
+
+def test_accretion_disk_jacobian_is_refused(ctx):
+    s = kerr_cases.disk_scene(8, 4)
+    ctx.upload(s)
+    with pytest.raises(gpu.PrenderError):
+        ctx.kerr_sensitivity(scenes.camera_rays(s))

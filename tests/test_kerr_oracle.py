@@ -47,3 +47,36 @@ def test_kerr_render_one_thread_bit_exact(golden, name):
     ref = golden["kerr_render"][name]
     assert np.array_equal(img, ref)
     assert ref.max() > 0
+
+
+@pytest.mark.parametrize("name", sorted(kerr_cases.disk_trace_cases()))
+def test_accretion_disk_trace_matches_reference(golden, name):
+    # the textured disk (circle.h:240-335): ISCO cut, disk-map texel, Doppler
+    # shift of colour and emission, temperature colours, and the alpha test
+    # drawn from the scene's generator (seeded 1 in the harness, disk_seed 1
+    # here), one stream over the rays in order
+    g = golden["kerr_disk"]
+    sc, rays = kerr_cases.disk_trace_cases()[name]
+    assert np.array_equal(rays, g[f"{name}_rays"])
+    k = O.OracleScene(sc).kerr_trace(rays)
+    st = kerr_cases.status_from_reference(g[f"{name}_obj"], g[f"{name}_hit"], g[f"{name}_rec"])
+    assert np.array_equal(k["status"], st)
+    h = st == 1
+    assert h.sum() >= 20
+    assert np.array_equal(k["hit_color"][h], g[f"{name}_col"][h])
+    assert np.array_equal(k["hit_emission"][h], g[f"{name}_em"][h])
+    assert np.array_equal(k["exit_dir"], g[f"{name}_rec"][:, 11:14])
+
+
+@pytest.mark.parametrize("name", sorted(kerr_cases.disk_render_cases()))
+def test_accretion_disk_render_one_thread_bit_exact(golden, name):
+    sc = kerr_cases.disk_render_cases()[name]
+    img, _, _ = O.OracleScene(sc).render(threads=1)
+    ref = golden["kerr_disk"][f"render_{name}"]
+    assert np.array_equal(img, ref)
+    assert ref.max() > 0.1
+
+
+def test_accretion_disk_oracle_fixture_is_converged(golden):
+    g = golden["kerr_disk_oracle"]
+    assert np.isfinite(g["mean"]).all() and g["mean"].mean() > 0.01 and int(g["batches"]) >= 8
