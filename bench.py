@@ -346,6 +346,103 @@ def run_gpu(args):
     return 0
 
 
+def kerr_jobs(n_jobs: int, width: int, height: int, precision: int):
+    """The Kerr lensing workload: n_jobs scenes alternating spin 0.6 / 0.999,
+    each seen from its own azimuth around the hole (camera at Boyer-Lindquist
+    r = 6.03 M in the disk plane, 60 degree field), textured accretion disk
+    r 3..15 M with Doppler shading, procedural celestial sphere."""
+    import math
+    from prender_gb300 import scenes
+    from prender_gb300.scene import Camera
+    out = []
+    for j in range(n_jobs):
+        a = 0.6 if j % 2 == 0 else 0.999
+        s = scenes.kerr_accretion(a=a, width=width, height=height, max_steps=4000, precision=precision)
+        ph = 2.0 * math.pi * (j // 2) / max(1, n_jobs // 2)
+        d = math.sqrt(6.03 * 6.03 + a * a)
+        s.camera = Camera(position=(round(d * math.sin(ph), 12), round(-d * math.cos(ph), 12), 0.0),
+                          dir=(round(-math.sin(ph), 12), round(math.cos(ph), 12), 0.0), up=(0.0, 0.0, 1.0),
+                          width=width, height=height, angle=60.0)
+        out.append(s)
+    return out
+
+
+def run_kerr(args):
+    """Kerr lensing renders: one step = n_jobs cameras / spins of 2048 x 1024
+    rays, one sample each, as one pr_render_batch launch (the mixed-precision
+    form); the reference-arithmetic FP64 form is timed on one job beside it."""
+    import torch
+    import __graft_entry__ as g
+    g.build_library()
+    from prender_gb300 import gpu
+    from prender_gb300 import _abi as A
+    W, H = (512, 256) if args.small else (2048, 1024)
+    n_jobs = args.kerr_jobs
+    torch.cuda.set_device(0)
+    ctx = gpu.Context(0)
+    jobs_s = kerr_jobs(n_jobs, W, H, A.PR_KERR_FP32)
+    objs = [ctx.scene_object(s) for s in jobs_s]
+    outs = [torch.empty((H, W, 3), dtype=torch.float32, device="cuda:0") for _ in range(n_jobs)]
+
+    def step(i):
+        ctx.render_batch([(objs[j], outs[j], None, None, i) for j in range(n_jobs)])
+        return ctx.stats()
+
+    for i in range(args.warmup):
+        step(i)
+    clk = ClockSampler(0)
+    clk.start()
+    walls, dev, st = [], [], None
+    for i in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = step(args.warmup + i)
+        torch.cuda.synchronize()
+        walls.append(time.perf_counter() - t0)
+        dev.append(st["device_ms"])
+    clocks = clk.stop()
+    paths = n_jobs * W * H
+    ms = 1e3 * statistics.mean(walls)
+    value = paths / (ms / 1e3) / 1e6
+    # the FP64 form (the reference's arithmetic in its order) on job 1 (a = 0.999) and job 0 (a = 0.6)
+    fp64 = {}
+    for j in (0, 1):
+        s = kerr_jobs(2, W, H, A.PR_KERR_FP64)[j]
+        ctx.upload(s)
+        ctx.render(s)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.render(s)
+        wall = time.perf_counter() - t0
+        st64 = ctx.stats()
+        fp64[f"a{s.kerr['a']}"] = {"mpaths_per_s": round(W * H / wall / 1e6, 4), "ms": round(1e3 * wall, 1),
+                                  "rk_attempts": int(st64["tri_tests"]), "device_ms": round(st64["device_ms"], 1)}
+    # FP64 form roofline: about 630 flops per RK45 attempt (Cash-Karp step
+    # with five geodesic evaluations), against GB300's FP64 pipe
+    # (2 DFMA / clock / SM x 152 SMs x 2.07 GHz x 2 flops = 1.26 TFLOP/s)
+    f = fp64["a0.999"]
+    achieved = 630.0 * f["rk_attempts"] / (f["device_ms"] / 1e3) / 1e12
+    line = {
+        "metric": "Mpaths/s, Kerr geodesic renders", "value": round(value, 4), "unit": "Mpaths/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"kerr_lensing_{W}x{H}_x{n_jobs}_accretion_disk", "jobs_per_launch": n_jobs,
+                   "spins": [0.6, 0.999], "max_steps": 4000, "precision": "mixed (PR_KERR_FP32)",
+                   "rk_attempts_per_step": int(st["tri_tests"]), "steps_accepted_per_step": int(st["nodes_visited"]),
+                   "fp64_form_one_job": fp64},
+        "roofline": {"bound": "fp64", "kernel": "kerr_render_kernel (FP64 form, a = 0.999)",
+                     "achieved": round(achieved, 4), "peak": 1.26, "unit": "TFLOP/s",
+                     "frac": round(achieved / 1.26, 4), "peak_kind": "nominal FP64 pipe",
+                     "note": "630 flops per RK45 attempt"},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    for o in objs:
+        o.release()
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -358,7 +455,12 @@ def main():
     ap.add_argument("--profile", action="store_true", help="full scene, 256x192x16spp image (ncu captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-rows", type=int, default=48)
+    ap.add_argument("--workload", default="mesh", choices=["mesh", "kerr"],
+                    help="kerr: the Kerr lensing renders (not the headline workload)")
+    ap.add_argument("--kerr-jobs", type=int, default=16)
     args = ap.parse_args()
+    if args.workload == "kerr":
+        return run_kerr(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -128,10 +128,16 @@ typedef struct pr_mesh {
 } pr_mesh;
 
 /* Kerr integrator precision: PR_KERR_FP64 runs the reference's FP64
- * arithmetic in its order (exit directions within 1e-6 rad of it);
- * PR_KERR_FP32 integrates in FP32 with a float-pair state and its own step
- * control (about 50x the FP64 rate on GB300; its error against the FP64
- * form is stated by the tests). */
+ * arithmetic in its order (exit directions within 1e-6 rad of it).
+ * PR_KERR_FP32 is the mixed form: the reference's FP64 steps near the hole
+ * and among the scene, FP32 fixed h = 2 steps for outbound rays beyond
+ * max(200, scene radius + 2) while the FP64 error estimate stays small, and
+ * an inbound ray inside all scene geometry with no radial turning point
+ * left reported as captured (status 4) at once.  Renders take that
+ * shortcut only on a black BACKGROUND, where a captured ray's colour does
+ * not depend on whether the reference would end it in the horizon (2) or
+ * by step underflow (4).  Its error against the FP64 form is stated by the
+ * tests. */
 enum { PR_KERR_FP64 = 0, PR_KERR_FP32 = 1 };
 
 /* KerrBlackHole constructor inputs (KerrBlackHole.h:86-151, scene_env.h:701-766,2056-2098) */
@@ -304,7 +310,10 @@ int pr_render_dev_noalloc(pr_ctx* ctx, const pr_camera* cam, const pr_render_par
                           uint64_t sample_offset, int accumulate);
 
 /* Per-launch statistics of the last render: paths, path segments (extension
- * plus shadow rays), QBVH nodes visited, triangle tests, device milliseconds. */
+ * plus shadow rays), QBVH nodes visited, triangle tests, device milliseconds.
+ * Kerr renders and pr_kerr_trace report straight-segment scene tests as
+ * segments, accepted RK45 steps as nodes_visited and RK45 attempts as
+ * tri_tests. */
 typedef struct pr_render_stats {
   uint64_t paths;
   uint64_t segments;

@@ -590,7 +590,10 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   const uint64_t paths = wf ? (uint64_t)g.spp * g.width * g.height : cnt[0];
   // wavefront: reset per pass + 4 per iteration + resolve; megakernel: kernel + reduce
   const uint64_t launches = wf ? 4 * cnt[5] + c->wf_passes + 1 : 2;
-  c->stats = pr_render_stats{paths, cnt[1], cnt[2], cnt[3], ms, launches};
+  // Kerr counters: [1] accepted RK steps, [2] RK attempts, [3] segment scene
+  // tests, reported as pr_kerr_trace does (segments, nodes_visited, tri_tests)
+  c->stats = kerr ? pr_render_stats{paths, cnt[3], cnt[1], cnt[2], ms, launches}
+                  : pr_render_stats{paths, cnt[1], cnt[2], cnt[3], ms, launches};
   for (int k = 0; k < 3; k++) c->shadow_counts[k] = wf ? cnt[6 + k] : 0;
   return st;
 }
@@ -926,9 +929,11 @@ int pr_render_batch(pr_ctx* c, int n, const pr_job* jobs) {
   std::vector<RenderCfg> cfg((size_t)n);
   std::vector<size_t> off((size_t)n + 1, 0);
   uint64_t paths = 0;
+  bool all_kerr = true;
   for (int j = 0; j < n; j++) {
     const pr_job& J = jobs[j];
     if (!J.scene) return fail(c, PR_E_ARG, "job " + std::to_string(j) + ": null scene");
+    all_kerr = all_kerr && J.scene->data.kerr.enabled;
     if (!J.rgb_dev) return fail(c, PR_E_ARG, "job " + std::to_string(j) + ": null output");
     int st = prepare_render(c, &J.camera, &J.params, J.sample_offset, cfg[j], &J.scene->data);
     if (st != PR_OK) return fail(c, st, "job " + std::to_string(j) + ": " + c->err);
@@ -1008,7 +1013,9 @@ int pr_render_batch(pr_ctx* c, int n, const pr_job* jobs) {
   int st = check_device_errors(c);
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-  c->stats = pr_render_stats{paths, cnt[1], cnt[2], cnt[3], ms, 2ull * (unsigned long long)n};
+  // Kerr jobs' counters are reported as pr_kerr_trace reports them
+  c->stats = all_kerr ? pr_render_stats{paths, cnt[3], cnt[1], cnt[2], ms, 2ull * (unsigned long long)n}
+                      : pr_render_stats{paths, cnt[1], cnt[2], cnt[3], ms, 2ull * (unsigned long long)n};
   return st;
 }
 

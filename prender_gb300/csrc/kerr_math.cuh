@@ -757,7 +757,7 @@ __device__ __forceinline__ bool no_turning_point(double r, double rplus, double 
 // the Kerr branch of intersect_scene, mixed precision (see above)
 template <class HS>
 __device__ void kerr_trace_ray_fast(const DevScene& S, const GKerr& K, dv3 org, dv3 dir, KerrHit& out, KerrCount& cnt,
-                                    uint32_t* err, HS& hs) {
+                                    uint32_t* err, HS& hs, bool capture_shortcut) {
   KerrRay k{K.a, K.a2, K.M, 0.0, 0.0};
   double* y = out.y;
   double dydx[6];
@@ -836,8 +836,11 @@ __device__ void kerr_trace_ray_fast(const DevScene& S, const GKerr& K, dv3 org, 
       }
     }
     const double r_before = y[0];
-    if (!far_mode && !capture_checked && dydx[0] < 0.0 && y[0] < K.scene_inner) {
-      // inbound inside all scene geometry: captured if no turning point is left
+    if (capture_shortcut && !far_mode && !capture_checked && dydx[0] < 0.0 && y[0] < K.scene_inner) {
+      // inbound inside all scene geometry: captured if no turning point is
+      // left.  The reference ends such a ray with a step underflow (status 4)
+      // or inside the horizon (2); the shortcut reports 4, so it is taken only
+      // where the two look alike
       capture_checked = true;
       if (no_turning_point(y[0], rplus, K.a, k.L, k.kappa)) {
         out.status = 4;
@@ -914,7 +917,7 @@ __global__ void __launch_bounds__(128) kerr_trace_kernel(DevScene S, GKerr K, co
     Rng drng;
     drng.init(disk_stream_key(0, K), (uint64_t)i, kDiskBranch);
     KerrDiskShading hs{&K, &drng};
-    if (FAST) kerr_trace_ray_fast(S, K, {r[0], r[1], r[2]}, {r[3], r[4], r[5]}, h, c, err, hs);
+    if (FAST) kerr_trace_ray_fast(S, K, {r[0], r[1], r[2]}, {r[3], r[4], r[5]}, h, c, err, hs, true);
     else kerr_trace_ray(S, K, {r[0], r[1], r[2]}, {r[3], r[4], r[5]}, h, c, err, hs);
     if (out.status) out.status[i] = h.status;
     if (out.steps) out.steps[i] = h.steps;
@@ -943,7 +946,10 @@ __device__ bool kerr_closest(const DevScene& S, const GKerr& K, float3 o, float3
                              float3& miss, float3 ovr[2], bool& has_ovr, KerrCount& c, uint32_t* err, Rng& drng) {
   KerrHit k;
   KerrDiskShading hs{&K, &drng};
-  if (FAST) kerr_trace_ray_fast(S, K, {o.x, o.y, o.z}, {d.x, d.y, d.z}, k, c, err, hs);
+  // a captured ray's colour: black (horizon) or BACKGROUND (step underflow)
+  // are the same only on a black background
+  const bool black_bg = S.bg[0] == 0.0f && S.bg[1] == 0.0f && S.bg[2] == 0.0f;
+  if (FAST) kerr_trace_ray_fast(S, K, {o.x, o.y, o.z}, {d.x, d.y, d.z}, k, c, err, hs, black_bg);
   else kerr_trace_ray(S, K, {o.x, o.y, o.z}, {d.x, d.y, d.z}, k, c, err, hs);
   has_ovr = false;
   if (k.status != 1) {
