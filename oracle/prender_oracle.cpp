@@ -51,6 +51,51 @@ struct Medium {  // ParticipatingMediaPrm.h:85-131 (fields used on the path)
       albedoColor = V3(scatteringColor.x / transmittanceColor.x, scatteringColor.y / transmittanceColor.y,
                        scatteringColor.z / transmittanceColor.z);
     }
+    // channel-sampling table of the absorbing coefficients (k = 1,
+    // SAMPLE_ABSORBING, the one the subsurface walk samples): the largest
+    // channel, the smallest absorbing channel, one in between (the
+    // reference takes the minimum over absorbingColor for every k)
+    const V3 sa = absorbingColor;
+    double max_s = -9999999.0, min_s = 9999999.0;
+    max_i = -1;
+    min_i = -1;
+    for (int i = 0; i < 3; i++) {
+      if (max_s < sa[i]) { max_s = sa[i]; max_i = i; }
+      if (min_s > absorbingColor[i]) { min_s = absorbingColor[i]; min_i = i; }
+    }
+    mid_i = -1;
+    for (int i = 0; i < 3; i++)
+      if (max_s > sa[i] && min_s < sa[i]) { mid_i = i; break; }
+    if (mid_i == -1) {
+      const double av = (absorbingColor.x + absorbingColor.y + absorbingColor.z) / 3;
+      const double mx = std::max(std::max(sa.x, sa.y), sa.z), mn = std::min(std::min(sa.x, sa.y), sa.z);
+      mid_i = (std::fabs(mx - av) < std::fabs(mn - av)) ? max_i : min_i;
+    }
+    t_sum = sa[0] + sa[1] + sa[2];
+    if (t_sum > 1.0e-14) {
+      t_[0] = sa[min_i] / t_sum;
+      t_[1] = sa[mid_i] / t_sum;
+      t_[2] = sa[max_i] / t_sum;
+    } else {
+      t_[0] = t_[1] = t_[2] = 1.0 / 3.0;
+    }
+  }
+  int max_i = 0, min_i = 0, mid_i = 0;
+  double t_sum = 0, t_[3] = {1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0};
+  // ParticipatingMedia::sample(u, SAMPLE_ABSORBING, inv) (ParticipatingMediaPrm.h:251-279)
+  int sample(double u, int inv) const {
+    if (t_sum < 1.0e-14) return std::min(2, (int)(3.0 * u));
+    int ii = 0;
+    if (inv) ii = min_i;
+    if (u < t_[0]) ii = min_i;
+    else if (u < t_[0] + t_[1]) ii = mid_i;
+    else if (u < t_[0] + t_[1] + t_[2]) ii = max_i;
+    if (inv) {
+      if (-u < -t_[0]) ii = min_i;
+      else if (-u < -t_[0] - t_[1]) ii = mid_i;
+      else if (-u < -t_[0] - t_[1] - t_[2]) ii = max_i;
+    }
+    return ii;
   }
   // transmittanceRatio (ParticipatingMediaPrm.h:336-340)
   V3 tr(double d) const { return vexp(-1.0 * transmittanceColor * d); }
@@ -580,9 +625,9 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
       md.use_bssrdf = pm.medium.use_bssrdf;
       const double sc = (md.scatteringColor.x + md.scatteringColor.y + md.scatteringColor.z) / 3;
       if (sc > EPS) md.setup(pm.medium.scale > 0.0 ? pm.medium.scale : 1.0);
-      if (m.type != PR_MAT_SSS_REFRACTION || md.level != -2 || !md.use_bssrdf) {
-        err = "subsurface scattering: only the directional-dipole form (reflection reflection + "
-              "Subsurface_Scattering, level -2) is on this path";
+      if (m.type != PR_MAT_SSS_REFRACTION || (md.level != -2 && md.level != -1) || !md.use_bssrdf) {
+        err = "subsurface scattering: only the directional-dipole forms (reflection reflection + "
+              "Subsurface_Scattering, level -2 or -1) are on this path";
         return PR_E_UNSUPPORTED;
       }
     }
@@ -1264,6 +1309,118 @@ bool inside_dir(V3 normal, V3 raydir);
 // probe rays for the exit point, the directional dipole, NEE at the exit,
 // or (accept 0.5) the Fresnel-surface refraction; raydir is the refracted
 // direction radiance() passes in
+V3 radiance(Ctx& c, V3 org, V3 dir, int depth);
+
+// radiance_through_media (Subsurface_Scattering.h:31-543): a walk inside the
+// subsurface object in_ent with at most sc_max scattering events.  At
+// sc_depth 0 it always scatters: a distance sampled towards the far side,
+// a phase-function direction retried (up to 145 times) until it leaves the
+// object or enters another; at sc_max it leaves: across the object's
+// surface (refracted, or mirrored under total internal reflection) with
+// the surface colour and three next-event samples there, or into another
+// object.  The Fresnel factors it computes are not applied.
+V3 through_media(Ctx& c, V3 org, V3 dir, int depth, int in_ent, int sc_depth, int sc_max) {
+  const Scene& s = c.s;
+  const Material& im = s.mats[s.ents[in_ent].material];
+  const Medium& pm = im.medium;
+  double dirPdf = 1.0, phase = 1.0;
+  double rr2 = 1.0;
+  if (depth > c.depth_limit * 30) {
+    rr2 *= std::min(std::pow(0.5, depth - c.depth_limit), std::pow(0.5, sc_depth));
+    if (c.rnd.next01() >= rr2) return im.emission;
+  } else {
+    rr2 = 1.0;
+  }
+  Hit out;
+  if (!intersect(s, org, dir, out)) return V3();
+  const double sig0 = pm.transmittanceColor[pm.sample(c.rnd.next01(), 0)];
+  double probability = 1.0 - std::exp(-sig0 * out.distance);
+  if (probability < 0) probability = 0;
+  else if (probability > 1.0) probability = 1.0;
+  if (sc_depth == 0) probability = 1.0;
+  if (sc_depth == sc_max || out.distance < 1.0e-4) probability = 0;
+  bool sss = (c.rnd.next01() < probability);
+  if (sss) {
+    double d = 0.0, pdf = 1.0;
+    const double p_pdf = 1;
+    V3 new_org = org, nd = dir;
+    sss = false;
+    for (int kk = 0; kk < 145; kk++) {
+      (void)pm.sample(c.rnd.next01(), 1);  // an unused channel draw
+      const int ii = pm.sample(c.rnd.next01(), 1);
+      const double st = pm.transmittanceColor[ii];
+      const double b = out.distance;
+      const double t = -std::log(1.0 + c.rnd.next01() * (std::exp(-st * b) - 1.0)) / st;
+      pdf = std::exp(-st * t) * (-st / (std::exp(-st * b) - 1.0));
+      d = t;
+      new_org = org + d * dir;
+      nd = dir;
+      if (sc_depth < 1) {
+        Hit w;
+        if (intersect(s, org, dir, w) && w.distance < length(new_org - org) && w.object_id == in_ent) continue;
+      }
+      const int select = pm.sample(c.rnd.next01(), 0);
+      const double g = pm.phase[select];
+      if (g == 0.0 || std::fabs(g) > 1.0) {
+        nd = sample_sphere(c);
+        phase = INV_FORPI;
+      } else {
+        nd = sample_hg(c, dir, g);
+        phase = phase_hg(g, dot(dir, nd));
+      }
+      dirPdf = phase;
+      Hit w;
+      if (!intersect(s, new_org, nd, w)) continue;
+      const bool insidedir = inside_dir(w.normal, nd);
+      if (w.object_id == in_ent) {
+        if (insidedir) continue;
+        sss = true;
+        break;
+      }
+      if (insidedir) {
+        sss = true;
+        break;
+      }
+    }
+    if (!sss) return V3();
+    const V3 Tr = pm.tr(d);
+    const V3 Ld = through_media(c, new_org, nd, depth + 1, in_ent, sc_depth + 1, sc_max);
+    const V3 Li = Tr * pm.scatteringColor * Ld * phase / pdf / dirPdf / probability / rr2 / p_pdf;
+    if (length(Li) > 100) return V3();  // OVER_RADIANCE_CUT0
+    return Li;
+  }
+  const V3 Tr = pm.tr(out.distance);
+  if (out.object_id != in_ent) return Tr * radiance(c, out.position, dir, depth + 1) / (1.0 - probability) / rr2;
+  // leaving across the object's own surface
+  const V3 out_on = dot(out.normal, dir) < 0.0 ? out.normal : (-1.0 * out.normal);
+  const V3 refl = normalize(dir - out.normal * 2.0 * dot(out.normal, dir));
+  V3 nd = dir;
+  {
+    const double nc = 1.0, nt = s.mats[out.material].refractive_index;
+    const bool into = dot(out.normal, dir) < 0.0;
+    const double nnt = into ? nc / nt : nt / nc;
+    const double ddn = dot(dir, out_on);
+    const double cos2t = 1.0 - nnt * nnt * (1.0 - ddn * ddn);
+    if (cos2t > 0) nd = normalize(dir * nnt - out.normal * (into ? 1.0 : -1.0) * (ddn * nnt + std::sqrt(std::fabs(cos2t))));
+    if (cos2t < 0) nd = refl;
+  }
+  const V3 weight = Tr * s.mats[out.material].color / (1.0 - probability) / rr2;
+  const V3 Li = radiance(c, out.position, nd, depth + 1);
+  V3 direct;
+  if (c.nee && !s.lights.empty()) {
+    for (int i = 0; i < 3; i++) {
+      const Light& l = random_light(c);
+      direct = direct + direct_sample(c, l, out, out.normal, depth) / 1.0;
+    }
+    direct = direct / 3;
+  }
+  if (!c.nee && !s.lights.empty()) {
+    for (int i = 0; i < 3; i++) (void)random_light(c);
+    direct = direct / 3;
+  }
+  return (direct + Li) * weight;
+}
+
 V3 brdf_sss2(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, double p_scat, int depth) {
   const Scene& s = c.s;
   const Material& hm = s.mats[hp.material];
@@ -1358,6 +1515,12 @@ V3 brdf_sss2(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, doub
         direct = direct * T12 * result * cos_wi_n * T21 / samplePDF / sampleDir / accept_prob / p_rr /
                  (1.0 - p_scat);
       }
+      if (length(incoming * weight) > 100) return V3();  // OVER_RADIANCE_CUT2
+    } else {
+      // single scattering (level -1): the walk radiance_through_media takes
+      // from just inside the entry point along the refracted direction
+      weight = hm.color / accept_prob / p_rr / (1.0 - p_scat) / (1.0 - pms);
+      incoming = through_media(c, hp.position - hp.normal * 0.0001, raydir, depth + 1, ent, 0, 1);
       if (length(incoming * weight) > 100) return V3();  // OVER_RADIANCE_CUT2
     }
   } else {

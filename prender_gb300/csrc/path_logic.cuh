@@ -213,10 +213,32 @@ __device__ __forceinline__ void root_path(PathState& ps, float3 o, float3 d) {
 // Subsurface_Scattering.h:19-22): the caller accumulates the continuation
 // and applies the bound when the continuation (all its branches) is done.
 struct SssFrameOut {
-  int open;
-  float3 scale;  // path contributions = scale * (weight * incoming)
+  int open;       // frames opened at this vertex: 0, 1, or 2 nested ones
+  float3 scale;   // path contributions = scale * (weight * incoming)
   float thr;
+  float3 scale2;  // the inner frame (the single-scattering walk's OVER_RADIANCE_CUT0)
+  float thr2;
+  int nee_inner;  // this vertex's next-event terms belong to the innermost frame
+  float3 inner;   // radiance this vertex adds inside the innermost frame (besides those)
 };
+
+// ParticipatingMedia::sample(u, SAMPLE_ABSORBING, inv) (ParticipatingMediaPrm.h:251-279)
+// over the subsurface material's table
+__device__ __forceinline__ int sss_channel(const GMaterial& m, float u, bool inv) {
+  if (m.sss_tsum < 1.0e-14f) return min(2, (int)(3.0f * u));
+  const int mn = m.sss_idx & 15, md = (m.sss_idx >> 4) & 15, mx = (m.sss_idx >> 8) & 15;
+  const float t0 = m.sss_t[0], t1 = m.sss_t[1], t2 = m.sss_t[2];
+  int ii = inv ? mn : 0;
+  if (u < t0) ii = mn;
+  else if (u < t0 + t1) ii = md;
+  else if (u < t0 + t1 + t2) ii = mx;
+  if (inv) {
+    if (-u < -t0) ii = mn;
+    else if (-u < -t0 - t1) ii = md;
+    else if (-u < -t0 - t1 - t2) ii = mx;
+  }
+  return ii;
+}
 
 // fresnel (bssrdf.h:239-247)
 __device__ __forceinline__ float dd_fresnel(float cos_theta, float eta) {
@@ -259,6 +281,69 @@ __device__ __forceinline__ float dd_bssrdf(const GMaterial& m, float3 xi, float3
   const float dv = sqrtf(dot(xoxv, xoxv));
   const float res = dd_sp(m, xoxi, w12, dr, no, j) - dd_sp(m, xoxv, wv, dv, no, j);
   return res < 0.0f ? 0.0f : res;
+}
+
+// Leaving a subsurface object at the end of the single-scattering walk
+// (radiance_through_media at sc_max, Subsurface_Scattering.h:409-541): the
+// path continues from exit hit oh (vertex ov) with the medium's
+// transmittance over the last segment; into another object straight on,
+// across the object's own surface refracted (mirrored under total internal
+// reflection) and weighted by the surface colour, with three next-event
+// samples at the exit point (colour / pi, the unflipped surface normal as
+// orienting normal).  The reference computes Fresnel factors here that it
+// does not apply.
+__device__ inline void sss_exit(const DevScene& S, const RenderCfg& cfg, const GMaterial& m, int in_ent,
+                                const FastHit& oh, const Vertex& ov, float3 dir, float rr2, float3 beta, int depth,
+                                Rng& rng, ShadowReq* sh, int& nsh, PathState& ps) {
+  const float3 Tr = f3(expf(-m.sss_tr[0] * oh.t), expf(-m.sss_tr[1] * oh.t), expf(-m.sss_tr[2] * oh.t));
+  ps.dp = 0;
+  ps.depth = depth;
+  if (oh.ent != in_ent) {
+    ps.beta = beta * Tr * (1.0f / rr2);
+    ps.o = offset_ray(ov.p, dot(dir, ov.n) > 0.0f ? ov.n : -ov.n);
+    ps.d = dir;
+    return;
+  }
+  const float3 n = ov.n;
+  const bool into = dot(n, dir) < 0.0f;
+  const float3 oon = into ? n : -n;
+  const float nnt = into ? 1.0f / m.ior : m.ior;
+  const float ddn = dot(dir, oon);
+  const float cos2t = 1.0f - nnt * nnt * (1.0f - ddn * ddn);
+  float3 nd = dir;
+  if (cos2t > 0.0f) nd = normalize(dir * nnt - n * ((into ? 1.0f : -1.0f) * (ddn * nnt + sqrtf(fabsf(cos2t)))));
+  if (cos2t < 0.0f) nd = normalize(dir - n * (2.0f * dot(n, dir)));
+  const float3 C = ld3(m.color);
+  const float3 bw = beta * Tr * C * (1.0f / rr2);
+  if (S.n_lights > 0 && cfg.nee != 0) {
+    const float3 origin = offset_ray(ov.p, n);
+    const float3 wn = bw * C * (0.31830988618379067154f / 3.0f);
+    for (int i = 0; i < 3; i++) {
+      const GEntF& le = pick_light(S, rng);
+      const float3 lp = sample_light(le, rng, true);
+      const float3 ln = light_normal(le, lp, true);
+      const float3 dl = lp - ov.p;
+      const float dist2 = dot(dl, dl);
+      const float3 ldir = dl / sqrtf(dist2);
+      const float dot0 = dot(n, ldir), dot1 = -dot(ln, ldir);
+      if (dot0 >= 0.0f && dot1 >= 0.0f) {
+        const float3 dlo = lp - origin;
+        const float disto = sqrtf(dot(dlo, dlo));
+        const float3 em = ld3(S.mats[le.material].emission);
+        const float3 ew = wn * (dot0 * dot1 / dist2 * le.area);
+        sh[nsh].o = origin;
+        sh[nsh].d = dlo / disto;
+        sh[nsh].tmax = disto - 1.0e-3f;
+        sh[nsh].contrib = ew * em;
+        sh[nsh].ew = ew;
+        sh[nsh].lmat = le.material;
+        nsh++;
+      }
+    }
+  }
+  ps.beta = bw;
+  ps.o = offset_ray(ov.p, dot(nd, n) > 0.0f ? n : -n);
+  ps.d = nd;
 }
 
 // Shades the vertex found by the last closest-hit query of ps (SSS: with the
@@ -535,7 +620,107 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     const float accept = into_s ? 0.5f : 0.0f;
     ps.L += ps.beta * (env + tri * E);
     if (rng.next() < accept) {
-      // multiple scattering through the dipole, exit at sp towards sw
+      if (m.sss_level == -1 && rng.next() >= 0.5f) {
+        // ---- single scattering (level -1): radiance_through_media
+        // (Subsurface_Scattering.h:31-543) from just inside the entry point
+        // along the refracted direction, at most one scattering event.  Its
+        // result is bounded twice: |Li| <= 100 inside the walk
+        // (OVER_RADIANCE_CUT0) and |weight * Li| <= 100 here (CUT2)
+        const float3 b0 = ps.beta * tri;
+        const float3 bw1 = b0 * C * (1.0f / (accept * p_rr * (1.0f - p_scat) * 0.5f));
+        const int dl30 = cfg.depth_limit * 30;
+        const int dw = ps.depth + 1;
+        if (frame) {
+          frame->open = 2;
+          frame->scale = b0;
+          frame->thr = 100.0f;
+          frame->scale2 = bw1;
+          frame->thr2 = 100.0f;
+          frame->nee_inner = 1;
+          frame->inner = f3(0, 0, 0);
+        }
+        float rr2a = 1.0f;
+        if (dw > dl30) {
+          rr2a = exp2f((float)(cfg.depth_limit - dw));
+          if (rng.next() >= rr2a) {  // the walk returns the object's emission
+            if (frame) {
+              frame->open = 1;
+              frame->inner = bw1 * E;
+            }
+            ps.draws = rng_draws(rng);
+            return SHADE_END;
+          }
+        }
+        const float3 org0 = v.p - v.n * 1.0e-4f;
+        FastHit oh;
+        TraceStats wst{0, 0};
+        Vertex ov;
+        if (!fast_closest(S, org0, ts, oh, wst, err)) {
+          if (frame) frame->open = 0;
+          ps.draws = rng_draws(rng);
+          return SHADE_END;
+        }
+        if (oh.t < 1.0e-4f) {  // too thin to scatter: leave at once (no CUT0 on this result)
+          make_vertex(S, org0, ts, oh, ov);
+          if (frame) frame->open = 1;
+          sss_exit(S, cfg, m, v.ent, oh, ov, ts, rr2a, bw1, ps.depth + 2, rng, sh, nsh, ps);
+          ps.draws = rng_draws(rng);
+          return SHADE_CONTINUE;
+        }
+        // a scattering point towards the far side, and a phase-function
+        // direction that leaves the object or enters another (145 tries)
+        bool ok = false;
+        float t = 0.0f, pdf = 1.0f, phase = 1.0f;
+        float3 nd = ts;
+        FastHit wh;
+        const bool hgc = (cfg.flags & PR_FLAG_HG_CORRECT) != 0;
+        for (int kk = 0; kk < 145 && !ok; kk++) {
+          const float st = m.sss_tr[sss_channel(m, rng.next(), true)];
+          const float eb = expf(-st * oh.t);
+          t = -logf(1.0f + rng.next() * (eb - 1.0f)) / st;
+          pdf = expf(-st * t) * (-st / (eb - 1.0f));
+          if (oh.t < t && oh.ent == v.ent) continue;  // beyond the object's far side
+          const float3 norg = org0 + ts * t;
+          const float g = m.sss_g[sss_channel(m, rng.next(), false)];
+          if (g == 0.0f || fabsf(g) > 1.0f) {
+            nd = sample_sphere_dir(rng);
+            phase = 0.0795774715459476679f;
+          } else {
+            nd = sample_hg(ts, g, rng, hgc);
+            phase = phase_hg(g, dot(ts, nd));
+          }
+          if (!fast_closest(S, norg, nd, wh, wst, err)) continue;
+          make_vertex(S, norg, nd, wh, ov);
+          const bool entering = dot(ov.n, nd) < 0.0f;  // Entity::isInsideDir
+          ok = (wh.ent == v.ent) ? !entering : entering;
+        }
+        if (!ok) {
+          if (frame) frame->open = 0;
+          ps.draws = rng_draws(rng);
+          return SHADE_END;
+        }
+        const float dir_pdf = phase;
+        const float3 bw2 = bw1 * f3(expf(-m.sss_tr[0] * t) * m.sss_ss[0], expf(-m.sss_tr[1] * t) * m.sss_ss[1],
+                                    expf(-m.sss_tr[2] * t) * m.sss_ss[2]) *
+                           (phase / pdf / dir_pdf / rr2a);
+        // scattering depth 1 = sc_max: leave along nd
+        float rr2b = 1.0f;
+        if (dw + 1 > dl30) {
+          rr2b = fminf(exp2f((float)(cfg.depth_limit - dw - 1)), 0.5f);
+          if (rng.next() >= rr2b) {
+            if (frame) frame->inner = bw2 * E;
+            ps.draws = rng_draws(rng);
+            return SHADE_END;
+          }
+        }
+        sss_exit(S, cfg, m, v.ent, wh, ov, nd, rr2b, bw2, ps.depth + 3, rng, sh, nsh, ps);
+        ps.draws = rng_draws(rng);
+        return SHADE_CONTINUE;
+      }
+      // multiple scattering through the dipole, exit at sp towards sw (level
+      // -1 takes it with probability 1/2: the continuation is weighted by 2,
+      // the next-event terms at the exit point are not)
+      const float pms = m.sss_level == -1 ? 0.5f : 1.0f;
       const float3 res = f3(dd_bssrdf(m, sp, on2, sw, v.p, on, 0), dd_bssrdf(m, sp, on2, sw, v.p, on, 1),
                             dd_bssrdf(m, sp, on2, sw, v.p, on, 2));
       const float k = T12 * cos_wi_n * T21 / pdf_s / pdf_d / accept / p_rr / (1.0f - p_scat);
@@ -571,8 +756,10 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
         frame->open = 1;
         frame->scale = ps.beta * tri;
         frame->thr = 100.0f;  // OVER_RADIANCE_CUT2
+        frame->nee_inner = 0;
+        frame->inner = f3(0, 0, 0);
       }
-      ps.beta = ps.beta * tri * C * res * k;
+      ps.beta = ps.beta * tri * C * res * (k / pms);
       ps.o = origin_s;
       ps.d = sw;
       ps.depth++;
@@ -585,6 +772,8 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
       frame->open = 1;
       frame->scale = ps.beta * tri;
       frame->thr = 200.0f;  // OVER_RADIANCE_CUT3
+      frame->nee_inner = 0;
+      frame->inner = f3(0, 0, 0);
     }
     ps.beta = ps.beta * tri * (into_s ? f3(1, 1, 1) : mtr) * (1.0f / (1.0f - accept));
     dg = ts;

@@ -58,6 +58,13 @@ struct GMaterial {
   float sss_falloff;       // Gaussian-disk falloff: min(sigma_t') * 0.001
   float sss_rmax0;         // probe-disk radius before the object-size clamp
   float sss_tr[3];         // the medium's transmittanceColor (exit attenuation)
+  // level -1 adds the single-scattering walk (radiance_through_media)
+  int32_t sss_level;       // -2 or -1
+  float sss_ss[3];         // scatteringColor
+  float sss_g[3];          // phase parameters (PAHASE)
+  float sss_t[3];          // channel-sampling table: absorbing coefficients of the
+  float sss_tsum;          //   smallest / middle / largest channel over their sum
+  int32_t sss_idx;         // those channels: min | mid << 4 | max << 8
 };
 
 struct GEntity {

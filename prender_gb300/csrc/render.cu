@@ -74,22 +74,40 @@ __device__ float3 trace_sample(const DevScene& S, const RenderCfg& cfg, float3 o
       const float3 Lb = ps.L;
       const int r = shade<SSS>(S, cfg, ps, hit, h, sample_id, sh, nsh, child, err, nullptr, nullptr, nullptr,
                                SSS ? &fo : nullptr);
+      const float3 Lown = ps.L - Lb;
+      float3 Lnee = f3(0, 0, 0);
       for (int k = 0; k < nsh; k++) {
         segs++;
-        if (!fast_occluded(S, sh[k].o, sh[k].d, sh[k].tmax, st, err)) ps.L += sh[k].contrib;
+        if (!fast_occluded(S, sh[k].o, sh[k].d, sh[k].tmax, st, err)) Lnee += sh[k].contrib;
       }
-      if (SSS && fo.open && F.n < kMaxSssFrames) {
-        // the branch moves into a new frame: what it gathered so far belongs outside
+      if (SSS && fo.open && F.n + fo.open <= kMaxSssFrames) {
+        // the branch moves into a new frame (or two nested ones): what it
+        // gathered before this vertex belongs outside, the vertex's own terms
+        // to the frame, its continuation inside
         const int f = F.n++;
-        F.E[f] = ps.L - Lb;
+        F.E[f] = Lown + (fo.nee_inner ? f3(0, 0, 0) : Lnee);
         F.C[f] = f3(0, 0, 0);
         F.scale[f] = fo.scale;
         F.thr[f] = fo.thr;
         F.parent[f] = fr;
         F.open[f] = 1;
         frame_add(F, L, fr, Lb);
+        int in = f;
+        if (fo.open == 2) {
+          in = F.n++;
+          F.E[in] = f3(0, 0, 0);
+          F.C[in] = f3(0, 0, 0);
+          F.scale[in] = fo.scale2;
+          F.thr[in] = fo.thr2;
+          F.parent[in] = f;
+          F.open[in] = 1;
+        }
+        F.C[in] += fo.inner + (fo.nee_inner ? Lnee : f3(0, 0, 0));
         ps.L = f3(0, 0, 0);
-        fr = f;  // the parent keeps its count: the branch left, the child frame came
+        fr = in;  // the parents keep their counts: the branch left, the child frame came
+      } else {
+        ps.L += Lnee;
+        if (SSS && fo.open) ps.L += fo.inner;
       }
       if (r == SHADE_SPLIT) {
         if (sp < kSplitStack) {

@@ -316,15 +316,17 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
     g.ior_d = pm.refractive_index;
     if (pm.type == PR_MAT_SSS_REFRACTION || pm.type == PR_MAT_SSS_DIFFUSE || pm.type == PR_MAT_SSS_WARD) {
       const pr_medium& md = pm.medium;
-      if (pm.type != PR_MAT_SSS_REFRACTION || md.level != -2 || !md.use_bssrdf || pm.roughness != 0.0) {
-        err = "subsurface scattering: only the directional-dipole form (reflection reflection + "
-              "Subsurface_Scattering, level -2, roughness 0) is on this path";
+      if (pm.type != PR_MAT_SSS_REFRACTION || (md.level != -2 && md.level != -1) || !md.use_bssrdf ||
+          pm.roughness != 0.0) {
+        err = "subsurface scattering: only the directional-dipole forms (reflection reflection + "
+              "Subsurface_Scattering, level -2 or -1, roughness 0) are on this path";
         return PR_E_UNSUPPORTED;
       }
       // setup_Scattering (ParticipatingMediaPrm.h:133-160) when the SCATTERING line is > PS_EPS
       double ss[3], sa[3], tc[3] = {0, 0, 0};
       for (int k = 0; k < 3; k++) { ss[k] = md.sigma_s_rgb[k]; sa[k] = md.sigma_a_rgb[k]; }
       double sc = (ss[0] + ss[1] + ss[2]) / 3, ab = (sa[0] + sa[1] + sa[2]) / 3;
+      bool tables = false;
       if (sc > 1.0e-6) {
         const double scale = md.scale > 0.0 ? md.scale : 1.0;
         for (int k = 0; k < 3; k++) { ss[k] *= scale; sa[k] *= scale; }
@@ -336,6 +338,41 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
         } else {
           for (int k = 0; k < 3; k++) tc[k] = ss[k] + sa[k];
         }
+        tables = true;
+      }
+      // channel-sampling table of setup_Scattering for SAMPLE_ABSORBING
+      // (ParticipatingMediaPrm.h:161-231): largest channel, smallest (of
+      // absorbingColor, as the reference takes it for every table), middle
+      g.sss_tsum = 0.0f;
+      g.sss_idx = 0;
+      g.sss_t[0] = g.sss_t[1] = g.sss_t[2] = (float)(1.0 / 3.0);
+      if (tables) {
+        double max_s = -9999999.0, min_s = 9999999.0;
+        int max_i = -1, min_i = -1, mid_i = -1;
+        for (int k = 0; k < 3; k++) {
+          if (max_s < sa[k]) { max_s = sa[k]; max_i = k; }
+          if (min_s > sa[k]) { min_s = sa[k]; min_i = k; }
+        }
+        for (int k = 0; k < 3; k++)
+          if (max_s > sa[k] && min_s < sa[k]) { mid_i = k; break; }
+        if (mid_i == -1) {
+          const double av = (sa[0] + sa[1] + sa[2]) / 3;
+          const double mx = std::max(std::max(sa[0], sa[1]), sa[2]), mn = std::min(std::min(sa[0], sa[1]), sa[2]);
+          mid_i = (std::fabs(mx - av) < std::fabs(mn - av)) ? max_i : min_i;
+        }
+        const double sum = sa[0] + sa[1] + sa[2];
+        if (sum > 1.0e-14) {
+          g.sss_tsum = (float)sum;
+          g.sss_t[0] = (float)(sa[min_i] / sum);
+          g.sss_t[1] = (float)(sa[mid_i] / sum);
+          g.sss_t[2] = (float)(sa[max_i] / sum);
+        }
+        g.sss_idx = min_i | (mid_i << 4) | (max_i << 8);
+      }
+      g.sss_level = md.level;
+      for (int k = 0; k < 3; k++) {
+        g.sss_ss[k] = (float)ss[k];
+        g.sss_g[k] = (float)md.phase_g[k];
       }
       // DirectionalDipole (bssrdf.h:75-128)
       auto C1 = [](double n) {

@@ -76,14 +76,15 @@ class Material:
 
     @staticmethod
     def subsurface(color, sigma_s, sigma_a, g=0.0, eta: float = 1.3, ior: float = 1.5, r_max: float = 1.0,
-                   scale: float = 1.0) -> "Material":
+                   scale: float = 1.0, level: int = -2) -> "Material":
         """'reflection reflection' + 'reflection Subsurface_Scattering' with the
-        material's SCATTERING / ABSORBING / PAHASE, 'level -2' (directional
-        dipole, scene_env.h:1305-1362) and r_refractive_index eta."""
+        material's SCATTERING / ABSORBING / PAHASE, 'level' (-2: directional
+        dipole; -1: dipole or a single-scattering walk, half each;
+        scene_env.h:1305-1362) and r_refractive_index eta."""
         g3 = tuple(g) if hasattr(g, "__len__") else (float(g),) * 3
         return Material(A.PR_MAT_SSS_REFRACTION, tuple(color), refractive_index=ior, r_refractive_index=eta,
                         medium=Medium(sigma_s_rgb=tuple(sigma_s), sigma_a_rgb=tuple(sigma_a), phase_g=g3, scale=scale,
-                                      r_max=r_max, level=-2, use_bssrdf=1))
+                                      r_max=r_max, level=int(level), use_bssrdf=1))
 
     def is_light(self) -> bool:
         """Material::isLight (material.h)."""

@@ -178,13 +178,14 @@ def diff_cornell(width: int = 512, height: int = 512, samples: int = 16, supersa
 
 def sss_cornell(width: int = 128, height: int = 96, samples: int = 4, supersamples: int = 2, subdiv: int = 5,
                 sigma_s=(1.0, 0.9, 0.8), sigma_a=(0.01, 0.02, 0.03), g: float = 0.0, eta: float = 1.3,
-                depth: int = 5, seed: int = 0) -> Scene:
+                depth: int = 5, seed: int = 0, level: int = -2) -> Scene:
     """Mesh Cornell box whose displaced icosphere is a subsurface material:
-    directional-dipole BSSRDF (level -2) with sigma_s' ~ 1, sigma_a ~ 0.01 per
-    unit and relative index eta 1.3 inside a Fresnel surface (IOR 1.5)."""
+    directional-dipole BSSRDF (level -2; level -1 adds the single-scattering
+    walk) with sigma_s' ~ 1, sigma_a ~ 0.01 per unit and relative index eta
+    1.3 inside a Fresnel surface (IOR 1.5)."""
     s = mesh_cornell(width, height, samples, supersamples, subdiv=subdiv, depth=depth, seed=seed)
     s.materials[s.entities[2].material] = Material.subsurface((0.9, 0.8, 0.7), sigma_s=sigma_s, sigma_a=sigma_a,
-                                                              g=g, eta=eta)
+                                                              g=g, eta=eta, level=level)
     return s
 
 

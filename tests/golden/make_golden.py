@@ -13,7 +13,8 @@ its build on the machine that runs them.
     python tests/golden/make_golden.py --sss-oracle
 
 writes sss_oracle.npz from the oracle alone (no reference build needed);
---disk-oracle writes kerr_disk_oracle.npz the same way.
+--disk-oracle and --sss-l1-oracle write kerr_disk_oracle.npz and
+sss_l1_oracle.npz the same way.
 """
 import os
 import struct
@@ -176,27 +177,45 @@ def sss_golden(d):
     np.savez_compressed(os.path.join(HERE, "sss_render.npz"), **out)
 
 
-def sss_oracle_golden(nb=16):
+def sss_l1_golden(d):
+    """level -1 subsurface renders by the reference, one thread (bit-exact)"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import sss_cases
+    out = {}
+    for name, sc in sss_cases.l1_cases().items():
+        dd = os.path.join(d, "s_" + name)
+        os.makedirs(dd)
+        img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+        out[name] = img
+        print("sss", name, info)
+    np.savez_compressed(os.path.join(HERE, "sss_l1_render.npz"), **out)
+
+
+def sss_oracle_golden(nb=16, level=-2):
     """16 independent 512-spp renders of the 64x48 subsurface scene by the
-    oracle (pinned bit-exact to the reference by the one-thread fixture):
+    oracle (pinned bit-exact to the reference by the one-thread fixtures):
     per-pixel mean and standard deviation, the symmetric high-spp target for
     the GPU's statistical parity.  Needs no reference build."""
     from oracle import oracle as O
-    sc = scenes.sss_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3)
+    sc = scenes.sss_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3, level=level)
     imgs = []
     for k in range(nb):
         sc.settings.seed = 100 + k
         img, _, _ = O.OracleScene(sc).render(threads=os.cpu_count())
         imgs.append(img)
     b = np.stack(imgs)
-    np.savez_compressed(os.path.join(HERE, "sss_oracle.npz"), mean_64x48_8192spp=b.mean(0).astype(np.float32),
+    name = "sss_oracle.npz" if level == -2 else "sss_l1_oracle.npz"
+    np.savez_compressed(os.path.join(HERE, name), mean_64x48_8192spp=b.mean(0).astype(np.float32),
                         sd_64x48_512spp=b.std(0, ddof=1).astype(np.float32), batches=np.int32(nb))
-    print("sss oracle batches", nb)
+    print("sss oracle batches", nb, "level", level)
 
 
 def main():
     if "--sss-oracle" in sys.argv:
         sss_oracle_golden()
+        return
+    if "--sss-l1-oracle" in sys.argv:
+        sss_oracle_golden(level=-1)
         return
     if "--disk-oracle" in sys.argv:
         disk_oracle_golden()
@@ -217,10 +236,15 @@ def main():
         with tempfile.TemporaryDirectory() as d:
             sss_golden(d)
         return
+    if "--sss-l1-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            sss_l1_golden(d)
+        return
     with tempfile.TemporaryDirectory() as d:
         kerr_golden(d)
         disk_golden(d)
         sss_golden(d)
+        sss_l1_golden(d)
         # -- QBVH structure + first hits on the subdiv-3 mesh Cornell box
         s = scenes.mesh_cornell(width=32, height=24, samples=1, supersamples=2, subdiv=3)
         p = s.write_reference(d)

@@ -216,3 +216,31 @@ def test_wavefront_equals_megakernel(ctx, name, build):
     wf2 = ctx.render(s)
     assert np.array_equal(wf, wf2)  # fixed-point accumulation: order-independent
     np.testing.assert_allclose(wf, mk, rtol=2e-4, atol=2e-6)
+
+
+def test_subsurface_level_minus1_matches_oracle_statistically(ctx, golden):
+    """Level -1 subsurface material (half the accepted entries take the
+    dipole, half the single-scattering walk through the object with its two
+    radiance bounds) in the plain form, 16 x 512 spp, against the oracle's
+    16 x 512 spp (the oracle is bit-exact with the reference on one thread)."""
+    s = scenes.sss_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3, level=-1)
+    s.settings.mode = A.PR_MODE_MEGAKERNEL
+    ctx.upload(s)
+    nb, spp = 16, s.settings.spp
+    b = _batches(ctx, s, nb, spp)
+    mean = b.mean(0)
+    sd = b.std(0, ddof=1)
+    orc = golden["sss_l1_oracle"]
+    o_mean = orc["mean_64x48_8192spp"].astype(np.float64)
+    o_sd = orc["sd_64x48_512spp"].astype(np.float64)
+    o_nb = int(orc["batches"])
+    sigma = np.sqrt(sd ** 2 / nb + o_sd ** 2 / o_nb) + 1e-6
+    frac = float((np.abs(mean - o_mean) / sigma > 3.0).mean())
+    rmse = float(np.sqrt(((mean - o_mean) ** 2).mean()))
+    noise = float(np.sqrt((sigma ** 2).mean()))
+    rel = abs(mean.mean() - o_mean.mean()) / o_mean.mean()
+    print(f"subsurface level -1 vs oracle 8192 spp: >3 sigma {frac:.4f}, rmse {rmse:.3e} vs noise {noise:.3e}, "
+          f"mean rel diff {rel:.4f}")
+    assert rel < 0.01
+    assert frac < 0.02
+    assert rmse < 1.3 * noise

@@ -89,3 +89,16 @@ def test_subsurface_oracle_fixture_agrees_with_reference_render(golden):
     sigma = np.sqrt(sd ** 2 / nb + sd ** 2) + 1e-6
     assert abs(mean.mean() - ref.mean()) / ref.mean() < 0.01
     assert np.sqrt(((mean - ref) ** 2).mean()) < 1.3 * np.sqrt((sigma ** 2).mean())
+
+
+@pytest.mark.parametrize("name", ["l1_g0", "l1_g05", "l1_nonee"])
+def test_subsurface_level_minus1_render_one_thread_bit_exact(golden, name):
+    # level -1: half the accepted entries take the dipole, half the
+    # single-scattering walk radiance_through_media (distance sampling,
+    # phase-function retries, exit refraction with next-event samples)
+    import sss_cases
+    sc = sss_cases.l1_cases()[name]
+    img, _, _ = O.OracleScene(sc).render(threads=1)
+    ref = golden["sss_l1_render"][name]
+    assert np.array_equal(img, ref)
+    assert ref.mean() > 0
