@@ -135,6 +135,8 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   PR_CUDA(c, upload(o.mats, h.mats, c->stream));
   PR_CUDA(c, upload(o.nodes, h.nodes, c->stream));
   PR_CUDA(c, upload(o.tris, h.tris, c->stream));
+  PR_CUDA(c, upload(o.rnodes, h.rnodes, c->stream));
+  PR_CUDA(c, upload(o.rtris, h.rtris, c->stream));
   PR_CUDA(c, upload(o.fnorm, h.fnorm, c->stream));
   PR_CUDA(c, upload(o.kerr_tex, h.kerr_texture, c->stream));
   PR_CUDA(c, upload(o.kerr_disk_tex, h.kerr_disk_texture, c->stream));
@@ -148,6 +150,8 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   S.mats = (const GMaterial*)o.mats.p;
   S.nodes = (const GNode*)o.nodes.p;
   S.tris = (const float4*)o.tris.p;
+  S.rnodes = (const GNode*)o.rnodes.p;
+  S.rtris = (const float4*)o.rtris.p;
   S.fnorm = (const float*)o.fnorm.p;
   S.n_ents = (int)h.ents.size();
   S.n_lights = (int)h.light_ent.size();
@@ -182,7 +186,7 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
     f.v_length = (float)e.v_length;
     f.area = (float)e.area;
     f.face_base = e.face_base;
-    f.node_base = e.node_base;
+    f.node_base = e.rnode_base;
     f.sss_rmax = (float)e.sss_rmax;
   }
   return PR_OK;

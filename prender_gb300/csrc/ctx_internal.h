@@ -35,11 +35,11 @@ struct DevBuf {
 // one uploaded scene: host build, device copies, device view
 struct SceneObjData {
   HostScene host;
-  DevBuf ents, mats, nodes, tris, fnorm, kerr_tex, kerr_disk_tex;
+  DevBuf ents, mats, nodes, tris, rnodes, rtris, fnorm, kerr_tex, kerr_disk_tex;
   DevScene dev{};
   GKerr kerr{};
   void release() {
-    for (DevBuf* b : {&ents, &mats, &nodes, &tris, &fnorm, &kerr_tex, &kerr_disk_tex}) b->release();
+    for (DevBuf* b : {&ents, &mats, &nodes, &tris, &rnodes, &rtris, &fnorm, &kerr_tex, &kerr_disk_tex}) b->release();
   }
 };
 

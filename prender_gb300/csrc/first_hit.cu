@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(128) trace_fast_kernel(DevScene S, const doubl
   TraceStats st{0, 0};
   const bool got = fast_closest(S, o, d, h, st, err);
   ent[i] = got ? h.ent : -1;
-  prim[i] = (got && h.slot >= 0) ? __float_as_int(S.tris[3 * (size_t)h.slot].w) : -1;
+  prim[i] = (got && h.slot >= 0) ? __float_as_int(S.rtris[3 * (size_t)h.slot].w) : -1;
   tout[i] = got ? (double)h.t : -1.0;
 }
 

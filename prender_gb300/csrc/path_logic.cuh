@@ -105,7 +105,7 @@ __device__ __forceinline__ void make_vertex(const DevScene& S, float3 o, float3 
     // the hit point from the barycentrics: its error is a few ulps of the
     // vertex coordinates, not of the ray length, which the ulp-scaled
     // origin offset (offset_ray) relies on
-    const float4* T = S.tris + 3 * (size_t)h.slot;
+    const float4* T = S.rtris + 3 * (size_t)h.slot;
     const float4 A = __ldg(T), B = __ldg(T + 1), C = __ldg(T + 2);
     const float w = 1.0f - h.u - h.v;
     v.p = f3(w * A.x + h.u * B.x + h.v * C.x, w * A.y + h.u * B.y + h.v * C.y, w * A.z + h.u * B.z + h.v * C.z);

@@ -83,6 +83,8 @@ struct GEntity {
   // mesh
   int32_t node_base;       // root node index in the concatenated node array
   int32_t slot_base;       // first leaf slot of this mesh
+  int32_t rnode_base;      // root of the mesh's render-path tree (DevScene::rnodes)
+  int32_t pad2;
   int32_t face_base;       // first face-normal record of this mesh
   int32_t n_faces;
   float bmin[3], bmax[3];  // bounds (for scene extents)
@@ -109,7 +111,7 @@ struct GEntF {
   float v_length;
   float n[3];
   float area;
-  int32_t face_base, node_base;
+  int32_t face_base, node_base;  // node_base: the render-path tree's root (DevScene::rnodes)
   float sss_rmax;  // subsurface probe-disk radius for this object (its bounding-box clamp applied)
   int32_t pad1;
   // disk: u_length = radius, v_length = inner radius, n = the plane normal
@@ -154,8 +156,10 @@ struct GKerr {
 struct DevScene {
   const GEntity* ents;
   const GMaterial* mats;
-  const GNode* nodes;
+  const GNode* nodes;      // the reference's trees (exact first-hit path)
   const float4* tris;      // 3 per leaf slot
+  const GNode* rnodes;     // the render path's trees (render_bvh.h)
+  const float4* rtris;     // 3 per leaf slot of those
   const float* fnorm;      // 3 per face
   int32_t n_ents;
   int32_t n_lights;

@@ -19,6 +19,7 @@
 
 #include "pr_internal.h"
 #include "scene_build.h"
+#include "render_bvh.h"
 
 namespace pr {
 namespace {
@@ -590,6 +591,9 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
         }
       }
       hs.fnorm.insert(hs.fnorm.end(), fn.begin(), fn.end());
+      // the render traversal's own tree (same closest hits, fewer tests)
+      g.rnode_base = (int32_t)hs.rnodes.size();
+      build_render_bvh(pm_.vertices, pm_.faces, pm_.n_faces, hs.rnodes, hs.rtris);
       hs.mesh_qbvh.push_back(std::move(q));
       hs.mesh_entity.push_back(i);
     } else {

@@ -83,7 +83,7 @@ __device__ __forceinline__ bool fast_qbvh(const DevScene& S, const GEntF& e, flo
   while (sp > 0) {
     if (++guard > (1 << 22)) { atomicOr(err, PR_DEV_LOOP_CAP); break; }
     const int32_t ni = stack[--sp];
-    const GNode* node = S.nodes + ni;
+    const GNode* node = S.rnodes + ni;
     st.nodes++;
     float tn[4];
     const int mask = box4(node, inv, oinv, tbest, tn);
@@ -121,7 +121,7 @@ __device__ __forceinline__ bool fast_qbvh(const DevScene& S, const GEntF& e, flo
       for (int k = 0; k < lcnt[l]; k++) {
         st.tris++;
         float t, uu, vv;
-        if (fast_tri(S.tris + 3 * (size_t)(first + k), o, d, tbest, t, uu, vv)) {
+        if (fast_tri(S.rtris + 3 * (size_t)(first + k), o, d, tbest, t, uu, vv)) {
           tbest = t;
           slot = first + k;
           bu = uu;
