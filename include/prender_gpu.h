@@ -409,6 +409,19 @@ int pr_kerr_sensitivity(pr_ctx* ctx, const double* rays, int64_t n, const double
 int pr_kerr_sensitivity_adjoint(pr_ctx* ctx, const double* rays, int64_t n, const double* basis,
                                 const double* cotangent, double* grad);
 
+/* ---- output --------------------------------------------------------- */
+/* 8-bit output of an image (Render::OutputBmp, render.h:1563-1589, with
+ * ppm.h:22-27): per channel int(pow(clamp(x, 0, 1), g) * 255 + 0.5), g =
+ * 1/2.2, or g = gamma_offset when |gamma_offset| > 0.01 (the reference uses
+ * the offset itself as the exponent; negative offsets are refused).  in:
+ * W*H*3 floats in pr_render's row order; out: W*H*3 bytes in the bitmap's
+ * cell(i, j) order (row i = image row H-1-i), R, G, B.  _dev: device
+ * buffers; the plain form takes host buffers. */
+int pr_image_to_rgb8(pr_ctx* ctx, const float* rgb, int32_t width, int32_t height, double gamma_offset,
+                     uint8_t* out);
+int pr_image_to_rgb8_dev(pr_ctx* ctx, const float* rgb_dev, int32_t width, int32_t height, double gamma_offset,
+                         uint8_t* out_dev);
+
 /* Accretion-disk shading test hook: the texture, temperature and Doppler
  * branch of Circle::intersect under the black hole (circle.h:240-322, no
  * alpha test) at n world points of disk entity `entity`.  Host buffers:

@@ -17,7 +17,7 @@ EXPORTS = (
     "pr_scene_upload", "pr_qbvh_info", "pr_qbvh_export", "pr_qbvh_build_host",
     "pr_first_hit", "pr_first_hit_dev", "pr_trace_fast", "pr_render", "pr_render_dev", "pr_render_dev_noalloc", "pr_last_render_stats",
     "pr_kerr_trace", "pr_kerr_trace_dev", "pr_render_adjoint", "pr_render_adjoint_dev",
-    "pr_last_kernel_times", "pr_kerr_sensitivity", "pr_kerr_sensitivity_adjoint", "pr_kerr_disk_shade", "pr_autotune_wavefront",
+    "pr_last_kernel_times", "pr_kerr_sensitivity", "pr_kerr_sensitivity_adjoint", "pr_kerr_disk_shade", "pr_image_to_rgb8", "pr_image_to_rgb8_dev", "pr_autotune_wavefront",
     "pr_scene_create", "pr_scene_release", "pr_render_batch",
 )
 
@@ -65,6 +65,8 @@ def load():
     L.pr_kerr_sensitivity.argtypes = [vp, vp, i64, vp, vp, vp, vp]
     L.pr_kerr_sensitivity_adjoint.argtypes = [vp, vp, i64, vp, vp, vp]
     L.pr_kerr_disk_shade.argtypes = [vp, C.c_int, vp, i64, vp, vp, vp, vp]
+    L.pr_image_to_rgb8.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_double, vp]
+    L.pr_image_to_rgb8_dev.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_double, vp]
     L.pr_autotune_wavefront.argtypes = [vp, vp, vp, vp, vp, vp]
     L.pr_scene_create.restype = vp
     L.pr_scene_create.argtypes = [vp, vp, C.POINTER(C.c_int)]

@@ -828,6 +828,38 @@ int pr_kerr_trace(pr_ctx* c, const double* rays, int64_t n, int32_t* status, dou
   return PR_OK;
 }
 
+int pr_image_to_rgb8_dev(pr_ctx* c, const float* rgb_dev, int32_t width, int32_t height, double gamma_offset,
+                         uint8_t* out_dev) {
+  if (!c) return PR_E_ARG;
+  if (width <= 0 || height <= 0 || (int64_t)width * height > ((int64_t)1 << 30)) return fail(c, PR_E_ARG, "bad image size");
+  if (!rgb_dev || !out_dev) return fail(c, PR_E_ARG, "null image buffer");
+  if (gamma_offset < -0.01) return fail(c, PR_E_ARG, "negative gamma_offset");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
+  PR_CUDA(c, launch_to_rgb8(rgb_dev, width, height, gamma_offset, out_dev, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PR_OK;
+}
+
+int pr_image_to_rgb8(pr_ctx* c, const float* rgb, int32_t width, int32_t height, double gamma_offset, uint8_t* out) {
+  if (!c) return PR_E_ARG;
+  if (width <= 0 || height <= 0 || (int64_t)width * height > ((int64_t)1 << 30)) return fail(c, PR_E_ARG, "bad image size");
+  if (!rgb || !out) return fail(c, PR_E_ARG, "null image buffer");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();
+  const size_t n3 = (size_t)width * height * 3;
+  // staging in the context's ray buffer: the float image, then the bytes
+  PR_CUDA(c, c->rays.ensure(n3 * sizeof(float) + n3));
+  float* d_in = (float*)c->rays.p;
+  uint8_t* d_out = (uint8_t*)(d_in + n3);
+  PR_CUDA(c, cudaMemcpyAsync(d_in, rgb, n3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  const int st = pr_image_to_rgb8_dev(c, d_in, width, height, gamma_offset, d_out);
+  if (st != PR_OK) return st;
+  PR_CUDA(c, cudaMemcpyAsync(out, d_out, n3, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PR_OK;
+}
+
 // the scene has a disk_map disk under its black hole (shaded from the disk texture)
 static bool has_kerr_disk(const SceneObjData& o) {
   for (const GEntity& e : o.host.ents)

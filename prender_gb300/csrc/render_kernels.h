@@ -30,6 +30,9 @@ struct RenderCfg {
 cudaError_t launch_megakernel(const DevScene& S, const RenderCfg& cfg, float* out, uint32_t* err,
                               unsigned long long* counters, cudaStream_t stream);
 cudaError_t launch_reduce(const float* partial, float* dst, int n3, int chunks, int accumulate, cudaStream_t stream);
+// 8-bit bitmap rows of a float image (output.cu)
+cudaError_t launch_to_rgb8(const float* rgb, int width, int height, double gamma_offset, uint8_t* out,
+                           cudaStream_t stream);
 cudaError_t launch_trace_fast(const DevScene& S, const double* rays, int64_t n, int32_t* ent, int32_t* prim, double* t,
                               uint32_t* err, cudaStream_t stream);
 cudaError_t launch_first_hit(const DevScene& S, const double* rays, int64_t n, int32_t* ent, int32_t* prim, double* t,

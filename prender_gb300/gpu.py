@@ -186,6 +186,16 @@ class Context:
             out["grad"] = g
         return out
 
+    def to_rgb8(self, image: np.ndarray, gamma_offset: float = 0.0) -> np.ndarray:
+        """Render::OutputBmp's 8-bit conversion of an (H, W, 3) float image in
+        pr_render's row order; returns (H, W, 3) uint8 rows as the bitmap's
+        cell(i, j) holds them (write with scene.write_bmp)."""
+        img = np.ascontiguousarray(image, dtype=np.float32)
+        h, w = img.shape[0], img.shape[1]
+        out = np.empty((h, w, 3), np.uint8)
+        self._check(self.L.pr_image_to_rgb8(self.h, _p(img), w, h, float(gamma_offset), _p(out)))
+        return out
+
     def kerr_disk_shade(self, entity: int, points: np.ndarray) -> dict:
         """The accretion disk's texture / temperature / Doppler shading at
         world points of disk entity (no alpha test): valid, colour,

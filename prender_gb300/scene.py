@@ -483,6 +483,13 @@ def _rgba(tex) -> np.ndarray:
     return np.ascontiguousarray(t)
 
 
+def write_bmp(path: str, rgb8: np.ndarray) -> None:
+    """Writes a 24-bit BMP from (H, W, 3) uint8 rows in the bitmap's
+    cell(i, j) order (what Context.to_rgb8 returns), as Render::OutputBmp's
+    BitMap::Write would."""
+    _write_bmp24(path, np.ascontiguousarray(rgb8, dtype=np.uint8))
+
+
 def _write_bmp24(path: str, tex: np.ndarray) -> None:
     """24-bit BMP whose decoded image, read back through the reference's
     BitMap::cell(y, x) (bitmap.h:187-190: row H-1-y of the top-down decode),

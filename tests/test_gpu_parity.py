@@ -266,3 +266,28 @@ def test_subsurface_level_minus1_matches_oracle_statistically(ctx, golden):
     assert rel < 0.01
     assert frac < 0.02
     assert rmse < 1.3 * noise
+
+
+def test_eight_bit_output_matches_the_reference_formula(ctx, tmp_path):
+    """Render::OutputBmp (render.h:1563-1589) with ppm.h's to_int: clamp,
+    gamma 1/2.2 (or gamma_offset as the exponent), * 255 + 0.5, truncated;
+    bitmap row i = image row H-1-i.  CUDA's pow may differ from the host's
+    in the last bit, which moves a value across a .5 boundary at most
+    rarely."""
+    from prender_gb300.scene import write_bmp
+    rng = np.random.default_rng(3)
+    img = rng.uniform(-0.2, 1.3, (37, 53, 3)).astype(np.float32)
+    img[0, 0] = (0.0, 1.0, np.nan)
+    for gamma in (0.0, 0.8):
+        g = 1.0 / 2.2 if gamma == 0.0 else gamma
+        x = np.clip(img.astype(np.float64), 0.0, 1.0)
+        ref = np.floor(np.power(x, g) * 255 + 0.5)
+        ref = ref[::-1]
+        out = ctx.to_rgb8(img, gamma).astype(np.float64)
+        fin = np.isfinite(ref)
+        diff = np.abs(out[fin] - ref[fin])
+        assert diff.max() <= 1 and (diff > 0).mean() < 1e-3
+    write_bmp(str(tmp_path / "out.bmp"), ctx.to_rgb8(img))
+    assert (tmp_path / "out.bmp").stat().st_size == 54 + (53 * 3 + 1) * 37
+    with pytest.raises(gpu.PrenderError):
+        ctx.to_rgb8(img, -1.0)
