@@ -296,10 +296,12 @@ int pr_render_dev(pr_ctx* ctx, const pr_camera* cam, const pr_render_params* prm
 
 /* Allocation-free variant of pr_render_dev for the megakernel form (no
  * counterpart in the reference, which renders on the CPU).  For callers that
- * must not allocate device memory while rendering: a caller in the middle of
- * a CUDA stream capture, a frame loop that cannot absorb cudaMalloc's
- * implicit synchronisation, or a host whose device memory belongs to its own
- * pool allocator.  It calls no cudaMalloc / cudaFree; its scratch is a 16 MiB
+ * must not allocate device memory while rendering: a frame loop with a hard
+ * time budget, which cannot absorb the device-wide synchronisation that
+ * cudaMalloc / cudaFree may cause, or a host application whose device memory
+ * is all handed out by its own pool allocator, so that an allocation behind
+ * its back can fail or break its accounting.  It calls no cudaMalloc /
+ * cudaFree; its scratch is a 16 MiB
  * static device array that every GPU loading this library keeps until exit,
  * so images of at most 1,398,080 pixels are accepted (larger ones return
  * PR_E_ARG).  The first call on a device looks up that array's address and

@@ -1,12 +1,12 @@
 // pr_render_dev_noalloc: the plain (megakernel) render for callers that must
 // not allocate device memory while they render.
 //
-// Who needs it: code that enqueues a frame while a CUDA stream capture is in
-// progress (allocating during capture invalidates the capture), frame loops
-// with a hard time budget (cudaMalloc / cudaFree can synchronise the device
-// and stall the frame), and hosts whose device memory is owned by their own
-// pool allocator and that forbid allocations behind its back.  pr_render_dev
-// grows its scratch on demand with cudaMalloc; this entry point never does.
+// Who needs it: frame loops with a hard time budget (cudaMalloc / cudaFree
+// can synchronise the whole device and stall the frame), and host
+// applications whose device memory is all handed out by their own pool
+// allocator, where an allocation behind the pool's back can fail or break
+// its accounting.  pr_render_dev grows its scratch on demand with
+// cudaMalloc; this entry point never does.
 //
 // Its scratch -- the per-chunk partial images of the megakernel and the
 // device error word / counters -- lives in one file-scope __device__ array

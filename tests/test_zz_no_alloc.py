@@ -1,9 +1,8 @@
 """pr_render_dev_noalloc: the allocation-free render entry point.
 
 It exists for callers that may not allocate device memory while they render
-(a stream capture in progress, a frame loop that cannot absorb the implicit
-synchronisation of cudaMalloc, or a host whose device memory is owned by its
-own pool).  Its scratch is a static device array shared by all calls, so
+(a frame loop that cannot absorb the device-wide synchronisation cudaMalloc
+may cause, or a host whose device memory is all owned by its own pool).  Its scratch is a static device array shared by all calls, so
 this file checks, through the C ABI, that two calls in a row each give the
 same image as pr_render_dev, and that a failed call leaves nothing behind
 for the next one.  The file is named to run last, so a failure here comes
