@@ -97,6 +97,9 @@ typedef struct pr_material {
   pr_medium medium;        /* used by the SSS material types                 */
   double r_refractive_index; /* 'r_refractive_index' (relative index of the
                                 subsurface medium, default 1.0)               */
+  double ward_alpha[2];    /* 'ward_brdf lo_d lo_s alp_x alp_y' roughness along
+                              the orienting normal's u and v axes (material.h:42-47) */
+  double phong_exponent;   /* 'phong_brdf lo_d lo_s n' specular exponent     */
 } pr_material;
 
 /* One OBJECT block (scene_env.h:854-1851) after its transforms. */

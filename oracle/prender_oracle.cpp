@@ -108,6 +108,8 @@ struct Material {  // material.h:54-240
   double refractive_index = 1.5;
   double r_refractive_index = 1.0;  // relative index of the subsurface medium (material.h:81)
   int disk_map = 0;                 // 'disk_map' (scene_env.h:1163-1169)
+  double ward_ax = 0, ward_ay = 0;  // brdfParameter.ward_brdf (material.h:42-47)
+  double phong_n = 0;               // brdfParameter.phong_brdf.specular_exponent
   Medium medium;
   // Material::isLight (material.h): diffuse, dark, emissive
   bool isLight() const {
@@ -613,6 +615,9 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
     m.refractive_index = pm.refractive_index;
     m.r_refractive_index = pm.r_refractive_index;
     m.disk_map = pm.disk_map;
+    m.ward_ax = pm.ward_alpha[0];
+    m.ward_ay = pm.ward_alpha[1];
+    m.phong_n = pm.phong_exponent;
     if (m.type == PR_MAT_SSS_REFRACTION || m.type == PR_MAT_SSS_DIFFUSE || m.type == PR_MAT_SSS_WARD) {
       // the material's own participatingMediaParam (scene_env.h:1305-1362); the
       // entity set-up calls setup_Scattering when the SCATTERING line is > PS_EPS
@@ -863,7 +868,14 @@ const Light& random_light(Ctx& c) {
 }
 
 // eval_direct_radiance for area lights and a diffuse receiver (directLight_radiance.h:19-313)
-V3 eval_direct(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, V3 light_pos, int depth) {
+Material hit_mat(const Scene& s, const Hit& h);
+
+// the BRDF direct_radiance_sample evaluates towards the light: the vertex's
+// own reflection type (directLight_radiance.h:211-290)
+enum { NEE_DIFFUSE = 0, NEE_WARD = 1, NEE_PHONG = 2 };
+
+V3 eval_direct(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, V3 light_pos, int depth,
+               int brdf = NEE_DIFFUSE, V3 ray_dir = V3()) {
   const Entity& le = c.s.ents[light.entity];
   V3 light_normal;
   double pdf = 1.0;
@@ -894,7 +906,31 @@ V3 eval_direct(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, V
           const double t = length(v0.position - light_pos);
           emission = emission * c.s.medium.tr(t);
         }
-        rad = (emission * (c.s.mats[v0.material].color * INV_PI)) * G / pdf;
+        const Material vm = hit_mat(c.s, v0);
+        if (brdf == NEE_WARD) {
+          V3 w, u, v;
+          onb(orienting_normal, w, u, v);
+          const V3 in = -1.0 * ray_dir;
+          const V3 halfv = normalize(in + light_dir);
+          const V3 dir = light_dir;
+          const double ww0 = std::pow(dot(halfv, orienting_normal), 2.0);
+          if (std::fabs(ww0) < 1.0e-16) return V3();
+          const double ww1 = (std::pow(dot(halfv, u) / vm.ward_ax, 2.0) + std::pow(dot(halfv, v) / vm.ward_ay, 2.0)) / ww0;
+          const double ww2 = 4.0 * PI * vm.ward_ax * vm.ward_ay * std::sqrt(dot(dir, orienting_normal) * dot(in, orienting_normal));
+          if (std::fabs(ww2) < 1.0e-16) return V3();
+          const double ww = std::exp(-ww1) / ww2;
+          if (ww < 0.0) return V3();
+          rad = (emission * (vm.specular * ww)) * G / pdf;
+        } else if (brdf == NEE_PHONG) {
+          const V3 ref = normalize(ray_dir - orienting_normal * 2.0 * dot(orienting_normal, ray_dir));
+          if (dot(ref, light_dir) < 0.0) return V3();
+          const double ww1 = std::pow(dot(ref, light_dir), vm.phong_n);
+          const double ww = ((vm.phong_n + 2) / TWOPI) * ww1;
+          if (ww < 0.0) return V3();
+          rad = (emission * (vm.specular * ww)) * G / pdf;
+        } else {
+          rad = (emission * (vm.color * INV_PI)) * G / pdf;
+        }
       }
     }
   }
@@ -902,7 +938,8 @@ V3 eval_direct(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, V
 }
 
 // direct_radiance_sample (directLight_radiance.h:318-387), area lights
-V3 direct_sample(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, int depth) {
+V3 direct_sample(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, int depth, int brdf = NEE_DIFFUSE,
+                 V3 ray_dir = V3()) {
   const Entity& le = c.s.ents[light.entity];
   V3 light_pos;
   if (le.type == PR_ENT_SPHERE) {
@@ -915,7 +952,7 @@ V3 direct_sample(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal,
     const double s = le.u_length * c.rnd.next01();
     light_pos = le.org + le.u_axis * s + le.v_axis * t + le.normal * EPS;
   }
-  return eval_direct(c, light, v0, orienting_normal, light_pos, depth);
+  return eval_direct(c, light, v0, orienting_normal, light_pos, depth, brdf, ray_dir);
 }
 
 // direct_light_perfect_refrection (directLight_radiance.h:516-556), no
@@ -985,6 +1022,74 @@ V3 brdf_diffuse(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, d
   }
   if (!c.nee && !s.lights.empty()) {
     for (int i = 0; i < 3; i++) (void)random_light(c);  // only parallel/spot/infinity lights contribute
+    direct = direct / 3;
+    direct = direct / p_rr / (1.0 - p_scat);
+  }
+  if (c.media && ins) {
+    direct = trr * direct;
+    emission = trr * emission;
+    incoming = trr * incoming;
+  }
+  return s.env_light + emission + direct + weight * incoming;
+}
+
+// BRDF_Phong (brdf.h:16-190) and BRDF_Ward (brdf.h:192-319): one direction
+// from the lobe (cos^n about the mirror direction; Ward's anisotropic
+// half-vector sampling about the orienting normal, Walter's "Notes on the
+// Ward BRDF"), its radiance first, then three next-event samples evaluated
+// with the same lobe; a direction below the surface returns zero for the
+// whole vertex
+V3 brdf_glossy(Ctx& c, V3 raydir, const Hit& hp, V3 on, double p_rr, double p_scat, int depth, int brdf) {
+  const Scene& s = c.s;
+  const Material mat = hit_mat(s, hp);
+  const bool ins = inside_dir(hp.normal, raydir);
+  V3 emission = mat.emission;
+  V3 trr(1, 1, 1);
+  if (c.media) trr = s.medium.tr(hp.distance);
+  V3 dir;
+  double ww;
+  if (brdf == NEE_PHONG) {
+    V3 w, u, v;
+    onb(normalize(raydir - on * 2.0 * dot(on, raydir)), w, u, v);
+    const double ph = TWOPI * c.rnd.next01();
+    double cost = std::pow(c.rnd.next01(), 1.0 / (mat.phong_n + 1.0));
+    if (cost > 1.0) cost = 1.0;
+    if (cost < -1.0) cost = -1.0;
+    const double sint = std::sqrt(1.0 - cost * cost);
+    dir = normalize((u * std::cos(ph) * sint + v * std::sin(ph) * sint + w * cost));
+    if (dot(on, dir) < 0.0) return V3();
+    ww = (mat.phong_n + 2) / (mat.phong_n + 1);
+  } else {
+    const double ax = mat.ward_ax, ay = mat.ward_ay;
+    const V3 in = -1.0 * raydir;
+    V3 w, u, v;
+    onb(on, w, u, v);
+    const double u1 = c.rnd.next01();
+    const double u2 = c.rnd.next01();
+    double phi = std::atan(ay / ax * std::tan(TWOPI * u2));
+    if (0.25 <= u2 && u2 <= 0.75) phi += PI;
+    else if (0.75 < u2) phi += TWOPI;
+    const double theta = std::atan(std::sqrt(-std::log(u1) / (std::pow(std::cos(phi), 2) / std::pow(ax, 2) +
+                                                                 std::pow(std::sin(phi), 2) / std::pow(ay, 2))));
+    const V3 halfv = normalize((u * std::cos(phi) * std::sin(theta) + v * std::sin(phi) * std::sin(theta) +
+                                w * std::cos(theta)));
+    dir = normalize(2.0 * dot(in, halfv) * halfv - in);
+    if (dot(on, dir) < 0.0) return V3();
+    ww = dot(halfv, in) * std::pow(dot(halfv, on), 3) * std::sqrt(dot(dir, on) / dot(in, on));
+  }
+  V3 incoming = radiance(c, hp.position, dir, depth + 1);
+  const V3 weight = mat.specular * ww / p_rr / (1.0 - p_scat);
+  V3 direct;
+  if (c.nee && !s.lights.empty()) {
+    for (int i = 0; i < 3; i++) {
+      const Light& l = random_light(c);
+      direct = direct + direct_sample(c, l, hp, on, depth, brdf, raydir) / 1.0;
+    }
+    direct = direct / 3;
+    direct = direct / p_rr / (1.0 - p_scat);
+  }
+  if (!c.nee && !s.lights.empty()) {
+    for (int i = 0; i < 3; i++) (void)random_light(c);
     direct = direct / 3;
     direct = direct / p_rr / (1.0 - p_scat);
   }
@@ -1300,7 +1405,7 @@ double gauss_pdf_2d(V3 pc, V3 ps, V3 N, double falloff, double rmax) {
 }
 
 V3 radiance(Ctx& c, V3 org, V3 dir, int depth);
-V3 direct_sample(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, int depth);
+V3 direct_sample(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, int depth, int brdf, V3 ray_dir);
 V3 brdf_refraction(Ctx& c, V3 raydir, const Hit& hp, int mat_type, V3 on, double p_rr, double p_scat, int depth);
 const Light& random_light(Ctx& c);
 bool inside_dir(V3 normal, V3 raydir);
@@ -1410,7 +1515,7 @@ V3 through_media(Ctx& c, V3 org, V3 dir, int depth, int in_ent, int sc_depth, in
   if (c.nee && !s.lights.empty()) {
     for (int i = 0; i < 3; i++) {
       const Light& l = random_light(c);
-      direct = direct + direct_sample(c, l, out, out.normal, depth) / 1.0;
+      direct = direct + direct_sample(c, l, out, out.normal, depth, NEE_DIFFUSE, V3()) / 1.0;
     }
     direct = direct / 3;
   }
@@ -1503,7 +1608,7 @@ V3 brdf_sss2(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, doub
       if (c.nee && !s.lights.empty()) {
         for (int k = 0; k < 3; k++) {
           const Light& l = random_light(c);
-          direct = direct + direct_sample(c, l, out, on2, depth) / 1.0;
+          direct = direct + direct_sample(c, l, out, on2, depth, NEE_DIFFUSE, V3()) / 1.0;
         }
         direct = direct / 3;
         direct = direct * T12 * result * cos_wi_n * T21 / samplePDF / sampleDir / accept_prob / p_rr /
@@ -1589,6 +1694,17 @@ V3 radiance(Ctx& c, V3 org, V3 dir, int depth) {
     case PR_MAT_SPECULAR:
       if (c.rnd.next01() < 1.0 - mat.roughness) return brdf_specular(c, dir, hp, p_rr, p_scat, depth);
       return brdf_diffuse(c, dir, hp, hp.object_id, on, p_rr, p_scat, depth);
+    case PR_MAT_PHONG:  // radiance.h:470-484: diffuse with probability roughness
+      if (c.rnd.next01() < mat.roughness) return brdf_diffuse(c, dir, hp, hp.object_id, on, p_rr, p_scat, depth);
+      return brdf_glossy(c, dir, hp, on, p_rr, p_scat, depth, NEE_PHONG);
+    case PR_MAT_WARD: {  // radiance.h:493-509: diffuse with probability rd / (rd + rs)
+      const double rd = (mat.color.x + mat.color.y + mat.color.z) / 3.0;
+      const double rs = (mat.specular.x + mat.specular.y + mat.specular.z) / 3.0;
+      const double diffuse_probability = rd / (rs + rd);
+      const double u = c.rnd.next01();
+      if (u < diffuse_probability) return brdf_diffuse(c, dir, hp, hp.object_id, on, p_rr, p_scat, depth);
+      return brdf_glossy(c, dir, hp, on, p_rr, p_scat, depth, NEE_WARD);
+    }
     case PR_MAT_REFRACTION:
     case PR_MAT_REFRACTION_FRESNEL:
       return brdf_refraction(c, dir, hp, mat.type, on, p_rr, p_scat, depth);

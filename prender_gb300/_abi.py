@@ -66,6 +66,8 @@ class pr_material(C.Structure):
         ("refractive_index", C.c_double),
         ("medium", pr_medium),
         ("r_refractive_index", C.c_double),
+        ("ward_alpha", C.c_double * 2),
+        ("phong_exponent", C.c_double),
     ]
 
 

@@ -625,6 +625,10 @@ static int adjoint_checks(pr_ctx* c, const pr_render_params* p) {
   if (c->cur.kerr.enabled) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass traces straight rays only");
   if (p && p->media && c->cur.host.medium.on) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover media");
   if (c->cur.dev.has_sss) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover subsurface materials");
+  for (const GMaterial& m : c->cur.host.mats)
+    if (m.type == PR_MAT_WARD || m.type == PR_MAT_PHONG)
+      return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover Ward or Phong materials (their lobes scale "
+                                       "with the specular colour, not the colour it differentiates)");
   if ((int)c->cur.host.mats.size() > kAdjMaterials)
     return fail(c, PR_E_UNSUPPORTED, "the adjoint pass tracks at most " + std::to_string(kAdjMaterials) + " materials");
   return PR_OK;

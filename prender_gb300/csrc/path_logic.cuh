@@ -388,7 +388,9 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   const float3 E = ovr ? ovr[1] : ld3(m.emission), C = ovr ? ovr[0] : ld3(m.color);
   const float3 d = ps.d;
   const float3 on = dot(v.n, d) < 0.0f ? v.n : -v.n;
-  float p_rr = maxc(E + C);  // WARD / PHONG are not on this path
+  // RR weight: emission + the reflectances the type can scatter with (radiance.h:79-89)
+  const float3 Sp = ld3(m.specular);
+  float p_rr = maxc(m.type == PR_MAT_WARD ? E + C + Sp : m.type == PR_MAT_PHONG ? E + Sp : E + C);
   if (ps.depth > cfg.depth_limit) p_rr *= exp2f((float)(cfg.depth_limit - ps.depth));
   const float3 trr = media ? medium_tr(S.medium, v.t) : f3(1, 1, 1);
   int result = SHADE_CONTINUE;
@@ -469,11 +471,15 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     }
   }
   const float inv_rr = 1.0f / p_rr / (1.0f - p_scat);
-  int kind;  // 0 diffuse, 1 specular, 2 glass, 3 subsurface (directional dipole)
+  int kind;  // 0 diffuse, 1 specular, 2 glass, 3 subsurface (directional dipole), 4 Phong, 5 Ward
   if (SSS && m.sss) kind = 3;
   else if (m.type == PR_MAT_DIFFUSE) kind = (rng.next() < m.roughness) ? 0 : 1;
   else if (m.type == PR_MAT_SPECULAR) kind = (rng.next() < 1.0f - m.roughness) ? 1 : 0;
-  else kind = 2;
+  else if (m.type == PR_MAT_PHONG) kind = (rng.next() < m.roughness) ? 0 : 4;  // radiance.h:470-484
+  else if (m.type == PR_MAT_WARD) {  // radiance.h:493-509: diffuse with probability rd / (rd + rs)
+    const float rd = (C.x + C.y + C.z) * (1.0f / 3.0f), rs = (Sp.x + Sp.y + Sp.z) * (1.0f / 3.0f);
+    kind = (rng.next() < rd / (rs + rd)) ? 0 : 5;
+  } else kind = 2;
   const float3 tri = (media && entering) ? trr : f3(1, 1, 1);
   const float3 env = f3(S.env[0], S.env[1], S.env[2]);
   if (kind == 0) {
@@ -533,6 +539,98 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     ps.L += ps.beta * (env + tri * E);
     if (tap) tap->em(v.mat, ps.beta * tri);
     ps.beta = ps.beta * C * tri * inv_rr;
+    ps.o = origin;
+    ps.d = nd;
+    ps.depth++;
+    ps.draws = rng_draws(rng);
+    return SHADE_CONTINUE;
+  }
+  if (kind == 4 || kind == 5) {
+    // ---- BRDF_Phong (brdf.h:16-190) / BRDF_Ward (brdf.h:192-319): one
+    // direction from the lobe, weighted by the specular colour; a direction
+    // below the surface gives the whole vertex zero.  Next-event samples are
+    // evaluated with the same lobe (directLight_radiance.h:211-256)
+    float3 a, b, nd;
+    float ww;
+    const float3 in = -d;
+    const float3 refl = normalize(d - on * (2.0f * dot(on, d)));
+    if (kind == 4) {
+      onb(refl, a, b);
+      const float ph = 6.28318530717958647692f * rng.next();
+      float cost = powf(rng.next(), 1.0f / (m.phong_n + 1.0f));
+      cost = fminf(1.0f, fmaxf(-1.0f, cost));
+      const float sint = sqrtf(fmaxf(0.0f, 1.0f - cost * cost));
+      float sn, cs;
+      sincosf(ph, &sn, &cs);
+      nd = normalize(a * (cs * sint) + b * (sn * sint) + refl * cost);
+      ww = (m.phong_n + 2.0f) / (m.phong_n + 1.0f);
+    } else {
+      onb(on, a, b);
+      const float ax = m.ward_ax, ay = m.ward_ay;
+      const float u1 = rng.next(), u2 = rng.next();
+      // importance sampling of the half vector (Walter, "Notes on the Ward BRDF", 2005)
+      float phi = atanf(ay / ax * tanf(6.28318530717958647692f * u2));
+      if (0.25f <= u2 && u2 <= 0.75f) phi += 3.14159265358979323846f;
+      else if (0.75f < u2) phi += 6.28318530717958647692f;
+      float sp, cp;
+      sincosf(phi, &sp, &cp);
+      const float theta = atanf(sqrtf(-logf(fmaxf(u1, 1.0e-30f)) / (cp * cp / (ax * ax) + sp * sp / (ay * ay))));
+      float st, ct;
+      sincosf(theta, &st, &ct);
+      const float3 h = normalize(a * (cp * st) + b * (sp * st) + on * ct);
+      nd = normalize(h * (2.0f * dot(in, h)) - in);
+      const float hn = dot(h, on);
+      ww = dot(h, in) * hn * hn * hn * sqrtf(fmaxf(0.0f, dot(nd, on) / dot(in, on)));
+    }
+    if (dot(on, nd) < 0.0f) {  // the reference returns zero for the vertex
+      ps.draws = rng_draws(rng);
+      return SHADE_END;
+    }
+    const float3 origin = offset_ray(v.p, on);
+    if (S.n_lights > 0 && nee) {
+      const float3 w = ps.beta * tri * Sp * (inv_rr * (1.0f / 3.0f));
+      for (int i = 0; i < 3; i++) {
+        const GEntF& le = pick_light(S, rng);
+        const float3 lp = sample_light(le, rng, true);
+        const float3 ln = light_normal(le, lp, true);
+        const float3 dl = lp - v.p;
+        const float dist2 = dot(dl, dl);
+        const float dist = sqrtf(dist2);
+        const float3 ldir = dl / dist;
+        const float dot0 = dot(on, ldir), dot1 = -dot(ln, ldir);
+        if (!(dot0 >= 0.0f && dot1 >= 0.0f)) continue;
+        float f;  // the lobe's value towards the light (times specular, applied in w)
+        if (kind == 4) {
+          const float c = dot(refl, ldir);
+          if (c < 0.0f) continue;
+          f = (m.phong_n + 2.0f) * 0.15915494309189533577f * powf(c, m.phong_n);
+        } else {
+          const float3 h = normalize(in + ldir);
+          const float ww0 = dot(h, on) * dot(h, on);
+          if (fabsf(ww0) < 1.0e-16f) continue;
+          const float hu = dot(h, a) / m.ward_ax, hv = dot(h, b) / m.ward_ay;
+          const float ww2 = 4.0f * 3.14159265358979323846f * m.ward_ax * m.ward_ay * sqrtf(fmaxf(0.0f, dot0 * dot(in, on)));
+          if (fabsf(ww2) < 1.0e-16f) continue;
+          f = expf(-(hu * hu + hv * hv) / ww0) / ww2;
+        }
+        if (!(f > 0.0f)) continue;
+        const float3 dlo = lp - origin;
+        const float disto = sqrtf(dot(dlo, dlo));
+        float3 em = ld3(S.mats[le.material].emission);
+        if (media) em = em * medium_tr(S.medium, dist);
+        sh[nsh].o = origin;
+        sh[nsh].d = dlo / disto;
+        sh[nsh].tmax = disto - 1.0e-3f;
+        const float3 ew = w * (f * dot0 * dot1 / dist2 * le.area);
+        sh[nsh].contrib = ew * em;
+        sh[nsh].ew = media ? ew * medium_tr(S.medium, dist) : ew;
+        sh[nsh].lmat = le.material;
+        nsh++;
+      }
+    }
+    ps.L += ps.beta * (env + tri * E);
+    if (tap) tap->em(v.mat, ps.beta * tri);
+    ps.beta = ps.beta * Sp * (ww * inv_rr) * tri;
     ps.o = origin;
     ps.d = nd;
     ps.depth++;

@@ -65,6 +65,10 @@ struct GMaterial {
   float sss_t[3];          // channel-sampling table: absorbing coefficients of the
   float sss_tsum;          //   smallest / middle / largest channel over their sum
   int32_t sss_idx;         // those channels: min | mid << 4 | max << 8
+  // glossy lobes (brdf.h:16-319)
+  float specular[3];
+  float ward_ax, ward_ay;  // Ward roughness along the orienting normal's u / v axes
+  float phong_n;           // Phong exponent
 };
 
 struct GEntity {

@@ -413,9 +413,21 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
       if (ab < 0.001) y *= 1.3 - std::exp(std::min({sa[0], sa[1], sa[2]}) * 1000.0);
       g.sss_rmax0 = (float)(1.25 * std::sqrt(std::log(1.0e-4) / -stp_min) * y * md.r_max);
     } else if (pm.type != PR_MAT_DIFFUSE && pm.type != PR_MAT_SPECULAR && pm.type != PR_MAT_REFRACTION &&
-               pm.type != PR_MAT_REFRACTION_FRESNEL) {
+               pm.type != PR_MAT_REFRACTION_FRESNEL && pm.type != PR_MAT_WARD && pm.type != PR_MAT_PHONG) {
       err = "material type " + std::to_string(pm.type) + " is not on this path yet";
       return PR_E_UNSUPPORTED;
+    }
+    for (int k = 0; k < 3; k++) g.specular[k] = (float)pm.specular[k];
+    g.ward_ax = (float)pm.ward_alpha[0];
+    g.ward_ay = (float)pm.ward_alpha[1];
+    g.phong_n = (float)pm.phong_exponent;
+    if (pm.type == PR_MAT_WARD && !(pm.ward_alpha[0] > 0.0 && pm.ward_alpha[1] > 0.0)) {
+      err = "Ward roughness alpha_x and alpha_y must be positive";
+      return PR_E_ARG;
+    }
+    if (pm.type == PR_MAT_PHONG && !(pm.phong_exponent > -1.0)) {
+      err = "Phong exponent must be above -1";
+      return PR_E_ARG;
     }
     hs.mats.push_back(g);
   }

@@ -58,6 +58,8 @@ class Material:
     medium: Medium = field(default_factory=Medium)
     r_refractive_index: float = 1.0
     disk_map: int = 0
+    ward_alpha: Sequence[float] = (0.1, 0.1)
+    phong_exponent: float = 1.0
 
     @staticmethod
     def diffuse(color, emission=(0.0, 0.0, 0.0)) -> "Material":
@@ -68,6 +70,24 @@ class Material:
     def mirror(color) -> "Material":
         """'reflection specular' (scene_env.h:1486-1490): roughness 0."""
         return Material(A.PR_MAT_SPECULAR, tuple(color), roughness=0.0)
+
+    @staticmethod
+    def ward(color, specular, alpha_x: float, alpha_y: float, emission=(0.0, 0.0, 0.0)) -> "Material":
+        """'reflection ward_brdf' with 'ward_brdf 1 1 alpha_x alpha_y'
+        (scene_env.h:1417-1425, :1492-1495): diffuse colour with probability
+        rd / (rd + rs) of the mean reflectances, else Ward's anisotropic
+        glossy lobe weighted by specular (brdf.h:192-319)."""
+        return Material(A.PR_MAT_WARD, tuple(color), tuple(emission), tuple(specular),
+                        ward_alpha=(float(alpha_x), float(alpha_y)))
+
+    @staticmethod
+    def phong(color, specular, exponent: float, roughness: float = 0.0, emission=(0.0, 0.0, 0.0)) -> "Material":
+        """'reflection phong_brdf' with 'phong_brdf 1 1 exponent' (scene_env.h
+        :1427-1435, :1497-1500): diffuse with probability roughness, else the
+        cos^n lobe about the mirror direction weighted by specular
+        (brdf.h:16-190, radiance.h:470-484)."""
+        return Material(A.PR_MAT_PHONG, tuple(color), tuple(emission), tuple(specular), roughness=float(roughness),
+                        phong_exponent=float(exponent))
 
     @staticmethod
     def glass(color, ior: float = 1.5) -> "Material":
@@ -102,6 +122,8 @@ class Material:
         m.medium = self.medium.to_c()
         m.r_refractive_index = float(self.r_refractive_index)
         m.disk_map = int(self.disk_map)
+        m.ward_alpha[:] = [float(x) for x in self.ward_alpha]
+        m.phong_exponent = float(self.phong_exponent)
         return m
 
 
@@ -403,7 +425,8 @@ class Scene:
                 "ABSORBING", "0", f3(md.sigma_a_rgb), "",
                 f"PAHASE {f3(md.phase_g)}", ""]
         refl = {A.PR_MAT_DIFFUSE: "reflection diffuse", A.PR_MAT_SPECULAR: "reflection specular",
-                A.PR_MAT_REFRACTION: "reflection reflection",
+                A.PR_MAT_REFRACTION: "reflection reflection", A.PR_MAT_WARD: "reflection ward_brdf",
+                A.PR_MAT_PHONG: "reflection phong_brdf",
                 A.PR_MAT_SSS_REFRACTION: "reflection reflection\nreflection Subsurface_Scattering"}
         for ei, e in enumerate(self.entities):
             m = self.materials[e.material]
@@ -439,6 +462,12 @@ class Scene:
                 if float(md.scale) != 1.0:
                     out += ["MATERIAL_SCALE", _fmt(md.scale)]
             out += [f"emission {f3(m.emission)}", f"color {f3(m.color)}"]
+            if m.type in (A.PR_MAT_WARD, A.PR_MAT_PHONG):
+                out.append(f"specular {f3(m.specular)}")
+                if m.type == A.PR_MAT_WARD:
+                    out.append(f"ward_brdf 1 1 {_fmt(m.ward_alpha[0])} {_fmt(m.ward_alpha[1])}")
+                else:
+                    out.append(f"phong_brdf 1 1 {_fmt(m.phong_exponent)}")
             if m.disk_map:
                 out.append(f"disk_map {int(m.disk_map)}")
             if e.normal_inverse < 0:
@@ -447,7 +476,8 @@ class Scene:
                 # 'reflection diffuse' forces roughness 1 and 'specular' 0; an
                 # explicit roughness line written after keeps other values
                 out.append(refl[m.type])
-                default_r = {A.PR_MAT_DIFFUSE: 1.0, A.PR_MAT_SPECULAR: 0.0}.get(m.type)
+                default_r = {A.PR_MAT_DIFFUSE: 1.0, A.PR_MAT_SPECULAR: 0.0, A.PR_MAT_PHONG: 0.0,
+                             A.PR_MAT_WARD: 0.0}.get(m.type)
                 if default_r is not None and float(m.roughness) != default_r:
                     out.append(f"roughness {_fmt(m.roughness)}")
             else:

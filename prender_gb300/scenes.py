@@ -131,13 +131,20 @@ def mesh_cornell(width: int = 1024, height: int = 768, samples: int = 16, supers
     """Triangle-mesh Cornell box: a 12-triangle box, a uvplane area light
     under the ceiling (U, V of length 5 as in proj/test/CornellBoxMLT2*.txt)
     and a Perlin-displaced icosphere (subdiv 7 = 327,680 triangles) that is
-    diffuse or glass.  NEE on; 16 x 2^2 tent-filtered samples = 64 spp."""
+    diffuse, glass, ward or phong.  NEE on; 16 x 2^2 tent-filtered samples = 64 spp."""
     s = Scene()
     bv, bf = box_mesh((1, 0, 0), (99, 81.6, 250))
     s.add_mesh(bv, bf, Material.diffuse((0.75, 0.75, 0.75)))
     s.add_uvplane((47.5, 81.5, 78.5), (5, 0, 0), (0, 0, 5), Material.diffuse((0, 0, 0), (36, 36, 36)))
     iv, jf = displaced_icosphere(subdiv, (50, 24, 70), 20.0, amp=0.05, seed=seed)
-    mat = Material.glass((0.99, 0.99, 0.99)) if material == "glass" else Material.diffuse((0.25, 0.75, 0.25))
+    if material == "glass":
+        mat = Material.glass((0.99, 0.99, 0.99))
+    elif material == "ward":  # anisotropic brushed-metal lobe over a dark diffuse base
+        mat = Material.ward((0.10, 0.25, 0.10), (0.60, 0.55, 0.45), alpha_x=0.08, alpha_y=0.30)
+    elif material == "phong":  # glossy lobe (n = 40), diffuse on 30 % of hits
+        mat = Material.phong((0.25, 0.60, 0.25), (0.55, 0.55, 0.55), exponent=40.0, roughness=0.3)
+    else:
+        mat = Material.diffuse((0.25, 0.75, 0.25))
     s.add_mesh(iv, jf, mat)
     s.camera = Camera(position=(50, 52, 220), dir=(0, -0.04, -1), angle=30, width=width, height=height)
     s.settings = RenderSettings(samples=samples, supersamples=supersamples, tent_filter=1, depth=depth,

@@ -13,8 +13,8 @@ its build on the machine that runs them.
     python tests/golden/make_golden.py --sss-oracle
 
 writes sss_oracle.npz from the oracle alone (no reference build needed);
---disk-oracle and --sss-l1-oracle write kerr_disk_oracle.npz and
-sss_l1_oracle.npz the same way.
+--disk-oracle, --sss-l1-oracle and --glossy-oracle write
+kerr_disk_oracle.npz, sss_l1_oracle.npz and glossy_oracle.npz the same way.
 """
 import os
 import struct
@@ -191,6 +191,42 @@ def sss_l1_golden(d):
     np.savez_compressed(os.path.join(HERE, "sss_l1_render.npz"), **out)
 
 
+def glossy_golden(d):
+    """Ward and Phong renders by the reference, one thread (bit-exact)"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import glossy_cases
+    out = {}
+    for name, sc in glossy_cases.one_thread_cases().items():
+        dd = os.path.join(d, "g_" + name)
+        os.makedirs(dd)
+        img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+        out[name] = img
+        print("glossy", name, info)
+    np.savez_compressed(os.path.join(HERE, "glossy_render.npz"), **out)
+
+
+def glossy_oracle_golden(nb=16):
+    """16 independent 512-spp renders of each glossy scene by the oracle:
+    per-pixel mean and standard deviation for the GPU's statistical parity"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import glossy_cases
+    from oracle import oracle as O
+    out = {}
+    for mat in ("ward", "phong"):
+        sc = glossy_cases.highspp_case(mat)
+        imgs = []
+        for k in range(nb):
+            sc.settings.seed = 100 + k
+            img, _, _ = O.OracleScene(sc).render(threads=os.cpu_count())
+            imgs.append(img)
+        b = np.stack(imgs)
+        out[f"{mat}_mean"] = b.mean(0).astype(np.float32)
+        out[f"{mat}_sd"] = b.std(0, ddof=1).astype(np.float32)
+    out["batches"] = np.int32(nb)
+    np.savez_compressed(os.path.join(HERE, "glossy_oracle.npz"), **out)
+    print("glossy oracle batches", nb)
+
+
 def sss_oracle_golden(nb=16, level=-2):
     """16 independent 512-spp renders of the 64x48 subsurface scene by the
     oracle (pinned bit-exact to the reference by the one-thread fixtures):
@@ -210,12 +246,22 @@ def sss_oracle_golden(nb=16, level=-2):
     print("sss oracle batches", nb, "level", level)
 
 
+KNOWN_FLAGS = {"--kerr-only", "--disk-only", "--sss-only", "--sss-l1-only", "--glossy-only", "--sss-oracle",
+               "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle"}
+
+
 def main():
+    bad = [a for a in sys.argv[1:] if a.startswith("--") and a not in KNOWN_FLAGS]
+    if bad:
+        sys.exit(f"unknown option(s) {bad}; known: {sorted(KNOWN_FLAGS)}")
     if "--sss-oracle" in sys.argv:
         sss_oracle_golden()
         return
     if "--sss-l1-oracle" in sys.argv:
         sss_oracle_golden(level=-1)
+        return
+    if "--glossy-oracle" in sys.argv:
+        glossy_oracle_golden()
         return
     if "--disk-oracle" in sys.argv:
         disk_oracle_golden()
@@ -236,6 +282,10 @@ def main():
         with tempfile.TemporaryDirectory() as d:
             sss_golden(d)
         return
+    if "--glossy-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            glossy_golden(d)
+        return
     if "--sss-l1-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             sss_l1_golden(d)
@@ -245,6 +295,7 @@ def main():
         disk_golden(d)
         sss_golden(d)
         sss_l1_golden(d)
+        glossy_golden(d)
         # -- QBVH structure + first hits on the subdiv-3 mesh Cornell box
         s = scenes.mesh_cornell(width=32, height=24, samples=1, supersamples=2, subdiv=3)
         p = s.write_reference(d)

@@ -291,3 +291,40 @@ def test_eight_bit_output_matches_the_reference_formula(ctx, tmp_path):
     assert (tmp_path / "out.bmp").stat().st_size == 54 + (53 * 3 + 1) * 37
     with pytest.raises(gpu.PrenderError):
         ctx.to_rgb8(img, -1.0)
+
+
+@pytest.mark.parametrize("mode", [A.PR_MODE_MEGAKERNEL, A.PR_MODE_WAVEFRONT])
+@pytest.mark.parametrize("mat", ["ward", "phong"])
+def test_glossy_image_matches_oracle_statistically(ctx, golden, mat, mode):
+    """Ward (anisotropic) and Phong glossy lobes, 16 x 512 spp, in both forms,
+    against the oracle's 16 x 512 spp (bit-exact with the reference on one
+    thread): per-pixel 3 sigma with both sides' spreads, RMSE at the noise
+    level, image mean within 1 %."""
+    import glossy_cases
+    s = glossy_cases.highspp_case(mat)
+    s.settings.mode = mode
+    ctx.upload(s)
+    nb, spp = 16, s.settings.spp
+    b = _batches(ctx, s, nb, spp)
+    mean = b.mean(0)
+    sd = b.std(0, ddof=1)
+    orc = golden["glossy_oracle"]
+    o_mean = orc[f"{mat}_mean"].astype(np.float64)
+    o_sd = orc[f"{mat}_sd"].astype(np.float64)
+    o_nb = int(orc["batches"])
+    sigma = np.sqrt(sd ** 2 / nb + o_sd ** 2 / o_nb) + 1e-6
+    frac = float((np.abs(mean - o_mean) / sigma > 3.0).mean())
+    rmse = float(np.sqrt(((mean - o_mean) ** 2).mean()))
+    noise = float(np.sqrt((sigma ** 2).mean()))
+    rel = abs(mean.mean() - o_mean.mean()) / o_mean.mean()
+    print(f"{mat} mode {mode}: >3 sigma {frac:.4f}, rmse {rmse:.3e} vs noise {noise:.3e}, mean rel diff {rel:.4f}")
+    assert rel < 0.01
+    assert frac < 0.02
+    assert rmse < 1.3 * noise
+
+
+def test_glossy_materials_are_refused_by_the_adjoint(ctx):
+    s = scenes.mesh_cornell(width=16, height=12, samples=1, supersamples=1, subdiv=3, material="ward")
+    ctx.upload(s)
+    with pytest.raises(gpu.PrenderError):
+        ctx.render_adjoint(np.ones((12, 16, 3), np.float32), s)

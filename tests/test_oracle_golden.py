@@ -102,3 +102,16 @@ def test_subsurface_level_minus1_render_one_thread_bit_exact(golden, name):
     ref = golden["sss_l1_render"][name]
     assert np.array_equal(img, ref)
     assert ref.mean() > 0
+
+
+@pytest.mark.parametrize("name", ["ward_nee1", "ward_nee0", "phong_nee1", "phong_nee0"])
+def test_glossy_render_one_thread_bit_exact(golden, name):
+    # Ward (anisotropic half-vector sampling, weight (h.i)(h.n)^3 sqrt(o.n / i.n))
+    # and Phong (cos^n lobe about the mirror direction, diffuse with
+    # probability roughness) with next-event samples evaluated by the lobe
+    import glossy_cases
+    sc = glossy_cases.one_thread_cases()[name]
+    img, _, _ = O.OracleScene(sc).render(threads=1)
+    ref = golden["glossy_render"][name]
+    assert np.array_equal(img, ref)
+    assert ref.mean() > 0
