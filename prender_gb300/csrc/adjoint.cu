@@ -71,7 +71,7 @@ __device__ float3 adjoint_sample(const DevScene& S, const RenderCfg& cfg, float3
       ShadowReq sh[3];
       int nsh = 0;
       PathState child;
-      const int r = shade(S, cfg, ps, hit, h, sample_id, sh, nsh, child, err, nullptr, nullptr, &tap);
+      const int r = shade<false, false>(S, cfg, ps, hit, h, sample_id, sh, nsh, child, err, nullptr, nullptr, &tap);
       if (r != SHADE_END) {
         // a non-terminal vertex: everything this branch adds from here on scales with its colour
         const int m = S.entf[h.ent].material;

@@ -163,7 +163,11 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   S.medium = h.medium;
   S.scene_scale = h.scene_scale;
   S.has_sss = 0;
-  for (const GMaterial& gm : h.mats) S.has_sss |= gm.sss;
+  S.has_glossy = 0;
+  for (const GMaterial& gm : h.mats) {
+    S.has_sss |= gm.sss;
+    S.has_glossy |= (gm.type == PR_MAT_WARD || gm.type == PR_MAT_PHONG) ? 1 : 0;
+  }
   for (int k = 0; k < 3; k++) {
     S.bg[k] = (float)h.background[k];
     S.env[k] = (float)h.env_light[k];

@@ -347,13 +347,14 @@ __device__ inline void sss_exit(const DevScene& S, const RenderCfg& cfg, const G
 }
 
 // Shades the vertex found by the last closest-hit query of ps (SSS: with the
-// subsurface material case compiled in; scenes without it use the leaner
-// instantiation).  A tracer
+// subsurface material case compiled in; GLOSSY: with the Ward and Phong
+// lobes; the plain form keeps a leaner instantiation for scenes without
+// them).  A tracer
 // that builds the vertex itself (the Kerr geodesic tracer) passes it as pre,
 // and the colour a miss returns as miss (radiance.h:30-43); straight-ray
 // callers leave both null.  ovr (colour, emission) replaces the material's
 // where the entity rewrote its hit point's copy (the accretion disk).
-template <bool SSS = false>
+template <bool SSS = false, bool GLOSSY = true>
 __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& ps, bool hit, const FastHit& h,
                      uint64_t sample_id, ShadowReq* sh, int& nsh, PathState& child, uint32_t* err,
                      const Vertex* pre = nullptr, const float3* miss = nullptr, EmissionTap* tap = nullptr,
@@ -475,8 +476,8 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   if (SSS && m.sss) kind = 3;
   else if (m.type == PR_MAT_DIFFUSE) kind = (rng.next() < m.roughness) ? 0 : 1;
   else if (m.type == PR_MAT_SPECULAR) kind = (rng.next() < 1.0f - m.roughness) ? 1 : 0;
-  else if (m.type == PR_MAT_PHONG) kind = (rng.next() < m.roughness) ? 0 : 4;  // radiance.h:470-484
-  else if (m.type == PR_MAT_WARD) {  // radiance.h:493-509: diffuse with probability rd / (rd + rs)
+  else if (GLOSSY && m.type == PR_MAT_PHONG) kind = (rng.next() < m.roughness) ? 0 : 4;  // radiance.h:470-484
+  else if (GLOSSY && m.type == PR_MAT_WARD) {  // radiance.h:493-509: diffuse with probability rd / (rd + rs)
     const float rd = (C.x + C.y + C.z) * (1.0f / 3.0f), rs = (Sp.x + Sp.y + Sp.z) * (1.0f / 3.0f);
     kind = (rng.next() < rd / (rs + rd)) ? 0 : 5;
   } else kind = 2;
@@ -545,7 +546,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     ps.draws = rng_draws(rng);
     return SHADE_CONTINUE;
   }
-  if (kind == 4 || kind == 5) {
+  if (GLOSSY && (kind == 4 || kind == 5)) {
     // ---- BRDF_Phong (brdf.h:16-190) / BRDF_Ward (brdf.h:192-319): one
     // direction from the lobe, weighted by the specular colour; a direction
     // below the surface gives the whole vertex zero.  Next-event samples are

@@ -175,6 +175,7 @@ struct DevScene {
   GMedium medium;
   float scene_scale;       // max |coordinate| of the scene bounds
   int32_t has_sss;         // a subsurface (dipole) material is present
+  int32_t has_glossy;      // a Ward or Phong material is present
   GEntF entf[kMaxEntities];
 };
 
