@@ -437,6 +437,34 @@ int pr_image_to_rgb8_dev(pr_ctx* ctx, const float* rgb_dev, int32_t width, int32
 int pr_kerr_disk_shade(pr_ctx* ctx, int entity, const double* points, int64_t n, int32_t* valid,
                        double* color, double* emission, double* alpha);
 
+/* ---- scene files ---------------------------------------------------- */
+/* The reference's scene text format read on the host (SceneEnv::Load,
+ * scene_env.h:357-2160, with its expression evaluator Expr.h for every
+ * value it evaluates: VAR variables, arithmetic, functions, %NAME%
+ * environment references; OBJ meshes as Obj::Load reads them, quads and
+ * vertex normals included; rotation / translate / scale of spheres and
+ * meshes; TARGET_POS and CAMERA_MATRIX; BMP textures), replacing the
+ * `prender scene.txt` front end (main.cpp) for callers that render through
+ * this library.  No GPU is touched.  pr_scene_file_load returns NULL on
+ * failure with "file:line: message" in err (errlen bytes): a missing file,
+ * a value the evaluator rejects, or a keyword of a feature this library
+ * does not render (other lights, object textures, transformed uvplanes and
+ * disks, lens, MLT, wormholes, OBJ materials), which is refused rather than
+ * skipped.  Lines that do not change the image are skipped and listed by
+ * pr_scene_file_warnings.  The reference's overrides of settings by
+ * environment variables (SAMPLING, IMAGE_X, ...) are not applied. */
+typedef struct pr_scene_file pr_scene_file;
+pr_scene_file* pr_scene_file_load(const char* path, char* err, int errlen);
+/* The scene, for pr_scene_upload / pr_scene_create; its buffers live until
+ * pr_scene_file_free. */
+const pr_scene_desc* pr_scene_file_desc(const pr_scene_file* file);
+/* Camera (CAMERA_ANGLE rule applied, direction normalised), render
+ * parameters (mode PR_MODE_MEGAKERNEL, seed 0: set them before pr_render)
+ * and gamma_offset (for pr_image_to_rgb8); any pointer may be NULL. */
+int pr_scene_file_camera(const pr_scene_file* file, pr_camera* cam, pr_render_params* prm, double* gamma_offset);
+const char* pr_scene_file_warnings(const pr_scene_file* file);
+void pr_scene_file_free(pr_scene_file* file);
+
 #ifdef __cplusplus
 }
 #endif

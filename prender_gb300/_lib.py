@@ -19,6 +19,7 @@ EXPORTS = (
     "pr_kerr_trace", "pr_kerr_trace_dev", "pr_render_adjoint", "pr_render_adjoint_dev",
     "pr_last_kernel_times", "pr_kerr_sensitivity", "pr_kerr_sensitivity_adjoint", "pr_kerr_disk_shade", "pr_image_to_rgb8", "pr_image_to_rgb8_dev", "pr_autotune_wavefront",
     "pr_scene_create", "pr_scene_release", "pr_render_batch",
+    "pr_scene_file_load", "pr_scene_file_desc", "pr_scene_file_camera", "pr_scene_file_warnings", "pr_scene_file_free",
 )
 
 _lib = None
@@ -72,5 +73,13 @@ def load():
     L.pr_scene_create.argtypes = [vp, vp, C.POINTER(C.c_int)]
     L.pr_scene_release.argtypes = [vp, vp]
     L.pr_render_batch.argtypes = [vp, C.c_int, vp]
+    L.pr_scene_file_load.restype = vp
+    L.pr_scene_file_load.argtypes = [C.c_char_p, C.c_char_p, C.c_int]
+    L.pr_scene_file_desc.restype = vp
+    L.pr_scene_file_desc.argtypes = [vp]
+    L.pr_scene_file_camera.argtypes = [vp, vp, vp, vp]
+    L.pr_scene_file_warnings.restype = C.c_char_p
+    L.pr_scene_file_warnings.argtypes = [vp]
+    L.pr_scene_file_free.argtypes = [vp]
     _lib = L
     return L

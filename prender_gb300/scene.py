@@ -158,10 +158,18 @@ class Entity:
 class Mesh:
     vertices: np.ndarray  # (n, 3) float32
     faces: np.ndarray     # (m, 3) int32, 0-based
+    # (m, 3) float32 shading normals per face, or None for the OBJ loader's
+    # rule from the vertices (an OBJ file with vertex normals, or a mesh
+    # moved by rotation / scale, carries its own)
+    face_normals: Optional[np.ndarray] = None
 
     def __post_init__(self):
         self.vertices = np.ascontiguousarray(self.vertices, dtype=np.float32)
         self.faces = np.ascontiguousarray(self.faces, dtype=np.int32)
+        if self.face_normals is not None:
+            self.face_normals = np.ascontiguousarray(self.face_normals, dtype=np.float32).reshape(-1, 3)
+            if self.face_normals.shape[0] != self.faces.shape[0]:
+                raise ValueError("face_normals needs one normal per face")
 
 
 @dataclass
@@ -243,6 +251,10 @@ class SceneDesc:
             pm.vertices = v.ctypes.data_as(C.POINTER(C.c_float))
             pm.faces = f.ctypes.data_as(C.POINTER(C.c_int32))
             pm.face_normals = None
+            if m.face_normals is not None:
+                fn = np.ascontiguousarray(m.face_normals, dtype=np.float32)
+                self._mesh_arrays.append(fn)
+                pm.face_normals = fn.ctypes.data_as(C.POINTER(C.c_float))
             meshes.append(pm)
         self._meshes = (A.pr_mesh * max(1, len(meshes)))(*meshes)
         d = A.pr_scene_desc()
@@ -440,6 +452,8 @@ class Scene:
                 # the keyword sets a scene-wide value every later disk inherits (scene_env.h:1177-1181)
                 out.append(f"blackhole_disk {int(e.blackhole_disk)}")
             elif e.type == A.PR_ENT_POLYGON:
+                if self.meshes[e.mesh].face_normals is not None:
+                    raise ValueError("a mesh with its own face normals has no reference writer")
                 objname = f"mesh{e.mesh}.obj"
                 _write_obj(os.path.join(directory, objname), self.meshes[e.mesh])
                 out.append(f"objfile {os.path.join(directory, objname)}")

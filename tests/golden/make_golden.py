@@ -15,6 +15,8 @@ its build on the machine that runs them.
 writes sss_oracle.npz from the oracle alone (no reference build needed);
 --disk-oracle, --sss-l1-oracle and --glossy-oracle write
 kerr_disk_oracle.npz, sss_l1_oracle.npz and glossy_oracle.npz the same way.
+--scene-files-only writes the meshes and textures that the scene files in
+scene_files/ name, and scene_files.npz from the reference's renders of them.
 """
 import os
 import struct
@@ -246,8 +248,105 @@ def sss_oracle_golden(nb=16, level=-2):
     print("sss oracle batches", nb, "level", level)
 
 
+SCENE_DIR = os.path.join(HERE, "scene_files")
+SCENE_FILES = ("spheres_expr", "mesh_obj", "media", "sss", "kerr_disk")
+
+
+def _grid(o, u, v, n):
+    """(n+1)^2 vertices of the parallelogram o + s u + t v"""
+    o, u, v = (np.asarray(x, dtype=np.float64) for x in (o, u, v))
+    return [o + u * (i / n) + v * (j / n) for j in range(n + 1) for i in range(n + 1)]
+
+
+def _quads(base, n):
+    """vertex numbers (1-based) of the n x n cells of a grid starting at base"""
+    for j in range(n):
+        for i in range(n):
+            a = base + j * (n + 1) + i
+            yield a, a + 1, a + n + 2, a + n + 1
+
+
+def write_scene_assets():
+    """The OBJ meshes and BMP textures that the scene files in scene_files/
+    name: a room whose walls are quads and triangles, a cube whose faces use
+    every face form of the OBJ reader (v, v/vt, v//vn, v/vt/vn; three and
+    four vertices) with vertex normals, and two small textures."""
+    out = ["# walls of a room: quads (floor, ceiling) and triangles (back, left, right)"]
+    walls = [((0, 0, 170), (100, 0, 0), (0, 0, -170), "q"), ((0, 81.6, 0), (100, 0, 0), (0, 0, 170), "q"),
+             ((0, 0, 0), (100, 0, 0), (0, 81.6, 0), "t"), ((0, 0, 170), (0, 0, -170), (0, 81.6, 0), "t"),
+             ((100, 0, 0), (0, 0, 170), (0, 81.6, 0), "t")]
+    n, faces, nv = 4, [], 0
+    for o, u, v, kind in walls:
+        for p in _grid(o, u, v, n):
+            out.append("v %.6g %.6g %.6g" % tuple(p))
+        for a, b, c, d in _quads(nv + 1, n):
+            faces += [f"f {a} {b} {c} {d}"] if kind == "q" else [f"f {a} {b} {c}", f"f {c} {d} {a}"]
+        nv += (n + 1) ** 2
+    with open(os.path.join(SCENE_DIR, "room.obj"), "w", newline="\n") as fh:
+        fh.write("\n".join(out + faces) + "\n")
+    # a cube [-1, 1]^3; vn 1 is a deliberately odd normal that the faces
+    # without normal numbers fall back on, vn 2..7 the outward normals
+    out = ["# a cube written with every face form", "vt 0 0", "vn 0.6 0.8 0"]
+    sides = [((1, -1, 1), (0, 0, -2), (0, 2, 0), (1, 0, 0), "vn4"), ((-1, -1, -1), (0, 0, 2), (0, 2, 0), (-1, 0, 0), "vn4"),
+             ((-1, 1, 1), (2, 0, 0), (0, 0, -2), (0, 1, 0), "vtn4"), ((-1, -1, -1), (2, 0, 0), (0, 0, 2), (0, -1, 0), "vtn3"),
+             ((-1, -1, 1), (2, 0, 0), (0, 2, 0), (0, 0, 1), "vt4"), ((1, -1, -1), (-2, 0, 0), (0, 2, 0), (0, 0, -1), "v3")]
+    n, faces, nv = 3, [], 0
+    for k, (o, u, v, nrm, kind) in enumerate(sides):
+        out.append("vn %g %g %g" % nrm)
+        for p in _grid(o, u, v, n):
+            out.append("v %.6g %.6g %.6g" % tuple(p))
+        ni = k + 2
+        for a, b, c, d in _quads(nv + 1, n):
+            if kind == "vn4":
+                faces.append(f"f {a}//{ni} {b}//{ni} {c}//{ni} {d}//{ni}")
+            elif kind == "vtn4":
+                faces.append(f"f {a}/1/{ni} {b}/1/{ni} {c}/1/{ni} {d}/1/{ni}")
+            elif kind == "vtn3":
+                faces += [f"f {a}/1/{ni} {b}/1/{ni} {c}/1/{ni}", f"f {c}/1/{ni} {d}/1/{ni} {a}/1/{ni}"]
+            elif kind == "vt4":
+                faces.append(f"f {a}/1 {b}/1 {c}/1 {d}/1")
+            else:
+                faces += [f"f {a} {b} {c}", f"f {c} {d} {a}"]
+        nv += (n + 1) ** 2
+    with open(os.path.join(SCENE_DIR, "cube_vn.obj"), "w", newline="\n") as fh:
+        fh.write("\n".join(out + faces) + "\n")
+    from prender_gb300.scene import write_bmp
+    rng = np.random.default_rng(7)
+    y, x = np.mgrid[0:16, 0:32]
+    sky = np.stack([x * 8, y * 16, (x + y) * 5], axis=2) + rng.integers(0, 8, (16, 32, 3))
+    write_bmp(os.path.join(SCENE_DIR, "sky.bmp"), np.clip(sky, 0, 255).astype(np.uint8))
+    y, x = np.mgrid[0:32, 0:32]
+    disk = np.stack([255 - x * 4, 128 + (y % 8) * 12, x * y // 5], axis=2) + rng.integers(0, 16, (32, 32, 3))
+    write_bmp(os.path.join(SCENE_DIR, "disk.bmp"), np.clip(disk, 0, 255).astype(np.uint8))
+
+
+def scene_files_golden(d):
+    """One-thread renders by the reference of the scene files in
+    scene_files/, read by the reference's own SceneEnv::Load (run from a
+    copy of that folder, so the files they name resolve there)"""
+    import shutil
+    write_scene_assets()
+    work = os.path.join(d, "scene_files")  # the reference writes dumps beside its working folder
+    shutil.copytree(SCENE_DIR, work)
+    out = {}
+    for name in SCENE_FILES:
+        path = os.path.join(work, name + ".txt")
+        img_path = os.path.join(d, name + ".f64")
+        info = run_ref(["render", path, img_path], work, 1).strip().splitlines()[-1]
+        w, h = _image_size(path)
+        out[name] = np.fromfile(img_path).reshape(h, w, 3)
+        print("scene file", name, info)
+    np.savez_compressed(os.path.join(HERE, "scene_files.npz"), **out)
+
+
+def _image_size(path):
+    lines = open(path).read().splitlines()
+    w, h = lines[lines.index("IMAGE") + 1].split()
+    return int(w), int(h)
+
+
 KNOWN_FLAGS = {"--kerr-only", "--disk-only", "--sss-only", "--sss-l1-only", "--glossy-only", "--sss-oracle",
-               "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle"}
+               "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle", "--scene-files-only"}
 
 
 def main():
@@ -270,6 +369,10 @@ def main():
         args = [a for a in sys.argv[1:] if not a.startswith("--")]
         ref = args[0] if args else "/root/reference"
         subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), ref], check=True)
+    if "--scene-files-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            scene_files_golden(d)
+        return
     if "--kerr-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             kerr_golden(d)
@@ -296,6 +399,7 @@ def main():
         sss_golden(d)
         sss_l1_golden(d)
         glossy_golden(d)
+        scene_files_golden(d)
         # -- QBVH structure + first hits on the subdiv-3 mesh Cornell box
         s = scenes.mesh_cornell(width=32, height=24, samples=1, supersamples=2, subdiv=3)
         p = s.write_reference(d)

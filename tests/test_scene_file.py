@@ -1,0 +1,302 @@
+"""The scene-file reader (pr_scene_file_load), on the CPU.
+
+* Scene files in the reference's format, written by hand to cover its
+  reader's rules (expressions over VAR variables, TARGET_POS, CAMERA_MATRIX,
+  transforms, OBJ quads and vertex normals, the global medium, subsurface
+  materials, the black hole with textures), read by this library and
+  rendered by the oracle, equal bit for bit the reference's own renders of
+  the same files (tests/golden/scene_files.npz, made by
+  tests/golden/make_golden.py --scene-files-only).
+* Scenes built in Python and written with Scene.write_reference read back
+  into the same scene description.
+* The expression rules, the OBJ face forms, BMP rows and the refusals.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from prender_gb300 import _abi as A
+from prender_gb300 import scene_file, scenes
+from prender_gb300.scene import write_bmp
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SCENE_DIR = os.path.join(HERE, "golden", "scene_files")
+SCENE_FILES = ("spheres_expr", "mesh_obj", "media", "sss", "kerr_disk")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+    g.build_library()
+    O.build()
+
+
+@pytest.mark.parametrize("name", SCENE_FILES)
+def test_scene_file_renders_like_the_reference(golden, name):
+    s = scene_file.load(os.path.join(SCENE_DIR, name + ".txt"))
+    img, _, _ = O.OracleScene(s).render(threads=1)
+    ref = golden["scene_files"][name]
+    assert ref.mean() > 0
+    assert np.array_equal(img, ref)
+
+
+def _written_cases():
+    import glossy_cases
+    import kerr_cases
+    out = {
+        "spheres": scenes.cornell_spheres(width=24, height=18, samples=2, supersamples=2),
+        "mesh": scenes.mesh_cornell(width=24, height=18, samples=1, supersamples=2, subdiv=3),
+        "media": scenes.media_cornell(width=16, height=12, samples=1, supersamples=2, g=0.5),
+        "sss": scenes.sss_cornell(width=16, height=12, samples=1, supersamples=1),
+        "sss_l1": scenes.sss_cornell(width=16, height=12, samples=1, supersamples=1, level=-1),
+        "kerr_disk": kerr_cases.disk_scene(16, 8, a=0.6, temperature=True, doppler=0.6),
+    }
+    out.update({"glossy_" + k: v for k, v in glossy_cases.one_thread_cases().items()})
+    return out
+
+
+@pytest.mark.parametrize("name", list(_written_cases()))
+def test_written_scene_reads_back_the_same(tmp_path, name):
+    s = _written_cases()[name]
+    back = scene_file.load(s.write_reference(str(tmp_path)))
+    assert back.materials == s.materials
+    assert back.entities == s.entities
+    assert len(back.meshes) == len(s.meshes)
+    for a, b in zip(back.meshes, s.meshes):
+        assert np.array_equal(a.vertices, b.vertices) and np.array_equal(a.faces, b.faces)
+        assert a.face_normals is None
+    assert back.background == tuple(s.background) and back.environment_light == tuple(s.environment_light)
+    assert back.participating_media == int(s.participating_media and s.settings.media)
+    assert back.medium == s.medium
+    c1, c2 = back.camera.to_c(), s.camera.to_c()
+    for f, _ in A.pr_camera._fields_:
+        assert np.array_equal(np.asarray(getattr(c1, f)), np.asarray(getattr(c2, f))), f
+    for f in ("samples", "supersamples", "tent_filter", "depth", "depth_limit", "nee", "sensor_response"):
+        assert getattr(back.settings, f) == getattr(s.settings, f), f
+    # the reference holds the cut-off in a float
+    assert back.settings.luminance_cutoff == float(np.float32(s.settings.luminance_cutoff))
+    if s.kerr is not None:
+        for k in ("position", "a", "max_steps", "map_coef", "texture_coef", "disk_temperature", "doppler_effect"):
+            assert back.kerr[k] == s.kerr[k], k
+        assert back.kerr["observer"] == tuple(s.camera.position)
+        if s.kerr.get("disk_texture") is not None:
+            assert np.array_equal(back.kerr["disk_texture"][:, :, :3], np.asarray(s.kerr["disk_texture"])[:, :, :3])
+
+
+def _scene(tmp_path, body, name="s.txt"):
+    p = tmp_path / name
+    p.write_text(body)
+    return str(p)
+
+
+def _screen(tmp_path, text):
+    return scene_file.load(_scene(tmp_path, f"SCREEN\n{text}\n")).camera.screen
+
+
+def _gamma(tmp_path, text, pre=""):
+    return scene_file.load(_scene(tmp_path, f"{pre}gamma_offset\n{text}\n")).gamma_offset
+
+
+def test_values_split_at_blanks_before_operands(tmp_path):
+    assert _screen(tmp_path, "1 -2 3") == (1.0, -2.0, 3.0)
+    assert _screen(tmp_path, "1 - 2 3") == (1.0, -2.0, 3.0)
+    assert _screen(tmp_path, "1+2 3*4 (5)") == (3.0, 12.0, 5.0)
+
+
+@pytest.mark.parametrize("text,value", [
+    ("010", 8.0), ("0x1f", 31.0), ("0t15", 15.0), ("0b2:101", 5.0), ("0.5", 0.5), ("1.5e2", 150.0),
+    ("2e-1", 0.2), ("2^3^2", 512.0), ("-2^2", 4.0), ("7%4", 3.0), ("-7%4", 1.0), ("10/4*2", 5.0),
+    ("1-2-3", -4.0), ("sqrt(16)+floor(2.7)+ceil(0.2)", 7.0), ("pow(2,10)", 1024.0), ("atan2(0,1)", 0.0),
+    ("sind(90)", 1.0), ("datan2(1,1)", 45.0), ("pi", np.pi), ("e", np.e),
+])
+def test_expression_values(tmp_path, text, value):
+    assert _gamma(tmp_path, text) == pytest.approx(value, rel=1e-15, abs=1e-15)
+
+
+def test_literals_accumulate_digits_and_divide_once(tmp_path):
+    # every digit into one double, one division by 10^(fraction digits)
+    assert _gamma(tmp_path, "0.123456789") == 123456789.0 / 1e9
+    assert _gamma(tmp_path, "12.5e3") == 125.0 / 10.0 * 1000.0
+
+
+def test_variables_first_definition_holds(tmp_path):
+    pre = "VAR A\n2\n\nVAR B\nA*3\n\nVAR A\n100\n\n"
+    assert _gamma(tmp_path, "A+B", pre) == 8.0
+
+
+def test_environment_references(tmp_path, monkeypatch):
+    monkeypatch.setenv("PR_TEST_GAMMA", "1.5*2")
+    assert _gamma(tmp_path, "%PR_TEST_GAMMA%") == 3.0
+    monkeypatch.delenv("PR_TEST_GAMMA")
+    assert _gamma(tmp_path, "%PR_TEST_GAMMA%") == 0.0
+
+
+@pytest.mark.parametrize("body,msg", [
+    ("gamma_offset\n1 2\n", "unexpected text"),
+    ("gamma_offset\nZZ\n", "unknown name"),
+    ("gamma_offset\n(1 + 2)\n", "expected ')'"),
+    ("SCREEN\n1 2\n", "expected a number"),
+    ("OBJECT\nsphere 0 0 0 1\ncolor 1 1\n\n", "expected a number"),
+    ("OBJECT\nsphere 0 0 0 1\nward_brdf 0.75 0.5 0.5\n\n", "expected a number"),
+])
+def test_bad_values_are_errors_with_the_line(tmp_path, body, msg):
+    with pytest.raises(scene_file.SceneFileError) as e:
+        scene_file.load(_scene(tmp_path, body))
+    assert msg in str(e.value) and "s.txt:" in str(e.value)
+
+
+@pytest.mark.parametrize("body", [
+    "OBJECT\nsphere 0 0 0 1\ntexture wood.bmp\n\n",
+    "OBJECT\nsphere 0 0 0 1\nbump_texture b.bmp\n\n",
+    "OBJECT\nsphere 0 0 0 1\nparallel_light 1\n\n",
+    "OBJECT\nsphere 0 0 0 1\nspot_light 1\n\n",
+    "OBJECT\nsphere 0 0 0 1\nsmooth 1\n\n",
+    "OBJECT\nsphere 0 0 0 1\nMATERIAL_SYMBOL\nKetchup\n\n",
+    "OBJECT\nsphere 0 0 0 1\nreflection reflection1\n1 2 3 4 5 6\n\n",
+    "OBJECT\nplane 0 0 0\nnormal 0 1 0\n\n",
+    "OBJECT\nhemisphere 0 0 0 1\n\n",
+    "OBJECT\ninfinity_light 0 -1 0\n\n",
+    "OBJECT\nuvplane 0 0 0\nU 1 0 0\nV 0 1 0\nrotation 0 10 0\n\n",
+    "OBJECT\ndisk 0 0 0 1\nnormal 0 1 0\ntranslate 1 0 0\n\n",
+    "OBJECT\nsphere 0 0 0 1\nreflection reflection\nreflection Subsurface_Scattering\n\n",
+    "LENS\n0.5 100\n",
+    "metropolisTransport\n1\n",
+    "WORMHOLE\n\n",
+    "BLACKHOLE\ninitial_condition 1\n\n",
+])
+def test_features_not_rendered_here_are_refused(tmp_path, body):
+    with pytest.raises(scene_file.SceneFileError):
+        scene_file.load(_scene(tmp_path, body))
+
+
+def test_switched_off_features_are_accepted(tmp_path):
+    s = scene_file.load(_scene(tmp_path, "LENS\n0 100\n\nmetropolisTransport\n0\n\n"
+                                         "OBJECT\nsphere 0 0 0 1\nparallel_light 0\nsmooth 0\nback 0\n\n"))
+    assert len(s.entities) == 1
+
+
+def test_missing_files_are_errors(tmp_path):
+    with pytest.raises(scene_file.SceneFileError, match="cannot open"):
+        scene_file.load(str(tmp_path / "none.txt"))
+    with pytest.raises(scene_file.SceneFileError, match="cannot open"):
+        scene_file.load(_scene(tmp_path, "OBJECT\nobjfile nowhere.obj\n\n"))
+
+
+def test_defaults_and_line_rules(tmp_path):
+    body = ("# one comment line before a keyword is skipped\n"
+            "IMAGE\n#a comment in place of the value is skipped too\n64 32\n\n"
+            "CAMERA_POS\n1 2 3\n\nCAMERA_DIR\n0 0 -2\n\n"
+            "PAHASE 0.1 0.2 0.3\n\n"
+            "SCATTERING\n9\n0.1 0.2 0.3\n\n"
+            "THREAD\n8\n\nOUTPUT\nx.bmp\n\nunknown_keyword\n\n"
+            "OBJECT\nsphere 1 2 3 4\nPAHASE 0.5 0.6 0.7\nnormal -1\n\n"
+            "OBJECT\ndisk2 0 0 0 5 1\nnormal 0 0 1\nblackhole_disk 2\n\n"
+            "OBJECT\ndisk 0 0 0 5\nnormal 0 0 1\n\n")
+    s = scene_file.load(_scene(tmp_path, body.replace("\n", "\r\n")))
+    assert (s.camera.width, s.camera.height) == (64, 32)
+    assert s.camera.dir == (0.0, 0.0, -1.0) and s.camera.position == (1.0, 2.0, 3.0)
+    assert s.medium.phase_g == (0.1, 0.2, 0.3)
+    assert s.medium.sigma_s_rgb == (0.1, 0.2, 0.3)
+    assert s.settings.samples == 8 and s.settings.supersamples == 2 and s.settings.depth == 8
+    assert s.settings.media == 0
+    assert "unknown_keyword" in s.file_warnings
+    m = s.materials[0]
+    assert m.medium.phase_g == (0.5, 0.5, 0.7)  # an OBJECT block keeps x for y
+    assert s.entities[0].p == (0.5, 0.6, 0.7)   # and the line moves the sphere's centre
+    assert s.entities[0].normal_inverse == -1
+    assert s.entities[1].blackhole_disk == 2 and s.entities[2].blackhole_disk == 2
+    assert s.entities[1].radius_inner == 1.0
+
+
+def test_camera_angle_and_target(tmp_path):
+    s = scene_file.load(_scene(tmp_path, "SCREEN\n1 1 40\n\nCAMERA_ANGLE\n30\n\n"
+                                         "CAMERA_POS\n0 0 0\n\nTARGET_POS\n3 0 4\n\n"))
+    w = 2.0 * 40.0 * np.tan(30.0 * (np.pi / 180.0) / 2.0)
+    assert s.camera.screen[0] == w and s.camera.screen[1] == w
+    assert s.camera.dir == pytest.approx((0.6, 0.0, 0.8), abs=1e-15)
+
+
+def test_black_hole_placed_along_the_camera(tmp_path):
+    s = scene_file.load(_scene(tmp_path, "CAMERA_POS\n0 0 10\n\nCAMERA_DIR\n0 0 -1\n\n"
+                                         "BLACKHOLE\ndist 25\nangular_momentum 0.5\ncoef 2\n\n"))
+    assert s.kerr["position"] == (0.0, 0.0, -15.0)
+    assert s.kerr["a"] == 0.5 and s.kerr["texture_coef"] == 2.0 and s.kerr["max_steps"] == 10000
+
+
+def _obj_scene(tmp_path, obj, extra=""):
+    (tmp_path / "m.obj").write_text(obj)
+    return scene_file.load(_scene(tmp_path, f"OBJECT\nobjfile m.obj\n{extra}\n"))
+
+
+def test_obj_quads_split_as_the_reference(tmp_path):
+    obj = "v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\n  v 0 0 1\nf 1 2 3 4\nf 1/1 2/1 5/1\nf 2//1 3//1 5//1\n"
+    s = _obj_scene(tmp_path, obj)
+    m = s.meshes[0]
+    assert m.vertices.shape == (5, 3)
+    assert m.faces.tolist() == [[0, 1, 2], [2, 3, 0], [0, 1, 4], [1, 2, 4]]
+    assert m.face_normals is None  # no vertex normals: the loader's rule at upload
+
+
+def test_obj_vertex_normals_give_the_face_normal(tmp_path):
+    obj = ("v 0 0 0\nv 1 0 0\nv 0 1 0\nv 1 1 0\nvn 1 0 0\nvn 0 1 0\nvn 0 0 1\n"
+           "f 1//1 2//2 3//3\nf 2 4 3\n")
+    fn = _obj_scene(tmp_path, obj).meshes[0].face_normals
+    # the mean in float (sum in float, / 3 in double), then divided by the
+    # length of its float square sum
+    c = np.float32(1.0 / 3.0)
+    sq = np.float32(np.float32(c * c) + np.float32(c * c)) + np.float32(c * c)
+    assert fn[0].tolist() == [float(np.float32(float(c) / np.sqrt(float(sq))))] * 3
+    # a face without normal numbers takes normal 1 for all three (the reference's zeroed ids)
+    assert fn[1].tolist() == [1.0, 0.0, 0.0]
+
+
+def test_obj_materials_are_refused(tmp_path):
+    (tmp_path / "m.mtl").write_text("newmtl red\nKd 1 0 0\n")
+    with pytest.raises(scene_file.SceneFileError, match="mtllib"):
+        _obj_scene(tmp_path, "mtllib m.mtl\nusemtl red\nv 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+
+
+def test_mesh_transforms_move_vertices_in_float_steps(tmp_path):
+    obj = "v 1 0 0\nv 0 1 0\nv 0 0 1\nv 1 1 1\nf 1 2 3\nf 2 3 4\n"
+    m = _obj_scene(tmp_path, obj, "scale 2 3 4\ntranslate 1 1 1\n").meshes[0]
+    assert m.vertices.tolist() == [[3, 1, 1], [1, 4, 1], [1, 1, 5], [3, 4, 5]]
+    assert m.face_normals is not None and np.allclose(np.linalg.norm(m.face_normals, axis=1), 1.0, atol=1e-6)
+
+
+def _bmp_scene(tmp_path, data, name="t.bmp"):
+    (tmp_path / name).write_bytes(data)
+    return scene_file.load(_scene(tmp_path, f"BLACKHOLE\naccretion_disk_texture {name}\nbackground_texture {name}\n\n"))
+
+
+def _bmp32(w, h, px, top_down=False):
+    hdr = bytearray(54)
+    hdr[0:2] = b"BM"
+    hdr[10:14] = (54).to_bytes(4, "little")
+    hdr[14:18] = (40).to_bytes(4, "little")
+    hdr[18:22] = w.to_bytes(4, "little")
+    hdr[22:26] = (-h if top_down else h).to_bytes(4, "little", signed=True)
+    hdr[26:28] = (1).to_bytes(2, "little")
+    hdr[28:30] = (32).to_bytes(2, "little")
+    return bytes(hdr) + bytes(px)
+
+
+def test_bmp_rows_and_alpha(tmp_path):
+    tex = np.arange(2 * 3 * 3, dtype=np.uint8).reshape(2, 3, 3) * 7
+    write_bmp(str(tmp_path / "a.bmp"), tex)
+    s = _bmp_scene(tmp_path, (tmp_path / "a.bmp").read_bytes())
+    assert np.array_equal(s.kerr["texture"], tex)
+    assert np.array_equal(s.kerr["disk_texture"][:, :, :3], tex) and (s.kerr["disk_texture"][:, :, 3] == 255).all()
+    # 32-bit, stored bottom-up: row 0 of the file is cell row 0
+    px = [10, 20, 30, 40, 50, 60, 70, 80]  # B G R A per pixel, 2 x 1
+    s = _bmp_scene(tmp_path, _bmp32(1, 2, px))
+    assert s.kerr["disk_texture"].tolist() == [[[30, 20, 10, 40]], [[70, 60, 50, 80]]]
+    # stored top-down (negative height): the rows reverse
+    s = _bmp_scene(tmp_path, _bmp32(1, 2, px, top_down=True))
+    assert s.kerr["disk_texture"].tolist() == [[[70, 60, 50, 80]], [[30, 20, 10, 40]]]
+    # all-zero alpha reads as opaque
+    s = _bmp_scene(tmp_path, _bmp32(1, 2, [1, 2, 3, 0, 4, 5, 6, 0]))
+    assert (s.kerr["disk_texture"][:, :, 3] == 255).all()
+    with pytest.raises(scene_file.SceneFileError, match="BMP"):
+        _bmp_scene(tmp_path, b"GIF89a" + bytes(100))

@@ -1,0 +1,64 @@
+"""Scenes read from the reference's scene files (pr_scene_file_load),
+uploaded and traced on the GPU: closest hits bit-exact against the oracle
+(transformed meshes, OBJ quads, faces with their own normals), and renders
+that agree with the oracle's statistically."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from prender_gb300 import gpu, scene_file, scenes
+
+pytestmark = pytest.mark.gpu
+
+SCENE_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "scene_files")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import __graft_entry__ as g
+    g.build_library()
+    O.build()
+    c = gpu.Context(0)
+    yield c
+    c.close()
+
+
+def _load(name):
+    return scene_file.load(os.path.join(SCENE_DIR, name + ".txt"))
+
+
+@pytest.mark.parametrize("name", ["spheres_expr", "mesh_obj", "media", "sss"])
+def test_scene_file_closest_hits_bit_exact(ctx, name):
+    s = _load(name)
+    ctx.upload(s)
+    rays = np.concatenate([scenes.random_rays((2, 1, 1), (98, 80, 170), 20000, seed=3), scenes.camera_rays(s)])
+    h = ctx.first_hit(rays)
+    o = O.OracleScene(s).first_hit(rays)
+    assert np.array_equal(h["entity"], o["entity"])
+    assert np.array_equal(h["prim"], o["prim"])
+    assert np.array_equal(h["t"], o["t"])
+
+
+@pytest.mark.parametrize("name", ["spheres_expr", "mesh_obj", "sss"])
+def test_scene_file_render_matches_oracle_statistically(ctx, name):
+    # GPU: 16 batches of 64 spp; oracle: one 1024-spp image.  Both means carry
+    # the spread of a 1024-spp estimate, so |diff| is within 3 sigma of
+    # sqrt(2) * (batch sd / 4) for all but a few pixels.
+    s = _load(name)
+    s.settings.samples, s.settings.supersamples = 16, 2
+    ctx.upload(s)
+    nb, spp = 16, s.settings.spp
+    b = np.stack([ctx.render(s, sample_offset=k * spp).astype(np.float64) for k in range(nb)])
+    mean = b.mean(0)
+    sd = b.std(0, ddof=1)
+    s.settings.samples = 16 * nb
+    ref, _, _ = O.OracleScene(s).render(threads=os.cpu_count())
+    sigma = np.sqrt(2.0 * sd ** 2 / nb) + 1e-6
+    z = np.abs(mean - ref) / sigma
+    frac = float((z > 3.0).mean())
+    rel = abs(mean.mean() - ref.mean()) / ref.mean()
+    print(f"{name}: >3 sigma {frac:.4f}, mean rel diff {rel:.4f}")
+    assert rel < 0.03
+    assert frac < 0.03
