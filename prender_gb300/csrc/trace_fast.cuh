@@ -143,8 +143,8 @@ __device__ __forceinline__ bool fast_qbvh(const DevScene& S, const GEntF& e, flo
   return hit;
 }
 
-// FP64 sphere test from an FP32 ray; threshold PS_EPS as in sphere.h:80-87
-__device__ __forceinline__ bool fast_sphere(const GEntity& e, float3 o, float3 d, float tmax, float& t) {
+// FP64 sphere distance of an FP32 ray; threshold PS_EPS as in sphere.h:80-87
+__device__ __forceinline__ bool sphere_t64(const GEntity& e, float3 o, float3 d, double& tt) {
   const double px = e.p[0] - (double)o.x, py = e.p[1] - (double)o.y, pz = e.p[2] - (double)o.z;
   const double b = px * (double)d.x + py * (double)d.y + pz * (double)d.z;
   const double D4 = b * b - (px * px + py * py + pz * pz) + e.radius * e.radius;
@@ -152,8 +152,13 @@ __device__ __forceinline__ bool fast_sphere(const GEntity& e, float3 o, float3 d
   const double s = sqrt(D4);
   const double t1 = b - s, t2 = b + s;
   if (t1 < kEps && t2 < kEps) return false;
-  const double tt = (t1 > kEps) ? t1 : t2;
-  if (!(tt < (double)tmax)) return false;
+  tt = (t1 > kEps) ? t1 : t2;
+  return true;
+}
+
+__device__ __forceinline__ bool fast_sphere(const GEntity& e, float3 o, float3 d, float tmax, float& t) {
+  double tt;
+  if (!sphere_t64(e, o, d, tt) || !(tt < (double)tmax)) return false;
   t = (float)tt;
   return true;
 }

@@ -284,9 +284,10 @@ def write_scene_assets():
         nv += (n + 1) ** 2
     with open(os.path.join(SCENE_DIR, "room.obj"), "w", newline="\n") as fh:
         fh.write("\n".join(out + faces) + "\n")
-    # a cube [-1, 1]^3; vn 1 is a deliberately odd normal that the faces
-    # without normal numbers fall back on, vn 2..7 the outward normals
-    out = ["# a cube written with every face form", "vt 0 0", "vn 0.6 0.8 0"]
+    # a cube [-1, 1]^3; vn 1 is the normal that the faces without normal
+    # numbers fall back on (outward for +z, inward for -z), vn 2..7 the
+    # outward normals
+    out = ["# a cube written with every face form", "vt 0 0", "vn 0 0 1"]
     sides = [((1, -1, 1), (0, 0, -2), (0, 2, 0), (1, 0, 0), "vn4"), ((-1, -1, -1), (0, 0, 2), (0, 2, 0), (-1, 0, 0), "vn4"),
              ((-1, 1, 1), (2, 0, 0), (0, 0, -2), (0, 1, 0), "vtn4"), ((-1, -1, -1), (2, 0, 0), (0, 0, 2), (0, -1, 0), "vtn3"),
              ((-1, -1, 1), (2, 0, 0), (0, 2, 0), (0, 0, 1), "vt4"), ((1, -1, -1), (-2, 0, 0), (0, 2, 0), (0, 0, -1), "v3")]
