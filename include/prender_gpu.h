@@ -330,7 +330,7 @@ typedef struct pr_render_stats {
 int pr_last_render_stats(pr_ctx* ctx, pr_render_stats* stats);
 /* Autotuner (no reference counterpart): times one short wavefront frame
  * (one camera sample per pixel, the caller's camera and parameters) for each
- * candidate path-pool size {2^19 .. 2^22} and traversal grid {16, 32, 64}
+ * candidate path-pool size {2^19 .. 2^22} and traversal grid {4, 8, 16}
  * blocks per SM, and keeps the fastest for later pr_render calls on this
  * context.  Images do not depend on either choice.  Outputs may be NULL. */
 int pr_autotune_wavefront(pr_ctx* ctx, const pr_camera* camera, const pr_render_params* params,

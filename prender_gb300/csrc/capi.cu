@@ -511,10 +511,11 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   B.max_iterations = 20000u;  // bounded device loop; a frame needs a few hundred
   WfLaunch L;
   L.shade_blocks = (P + 127) / 128;
-  // grid-stride traversal over the queues: up to 64 blocks per SM
+  // persistent traversal: one resident wave of blocks (more waves only queue
+  // behind it and find the rays taken)
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || sms <= 0) sms = 152;
-  const unsigned int bps = c->tuned_trace_bps ? c->tuned_trace_bps : 64u;
+  const unsigned int bps = c->tuned_trace_bps ? c->tuned_trace_bps : kTraceBlocksPerSM;
   L.trace_blocks = std::min<unsigned int>((P + 127) / 128, (unsigned int)sms * bps);
   PR_CUDA(c, cudaMemsetAsync(c->wf_nee.p, 0, f4 * 3 * P, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->wf_pix.p, 0, 24ull * wh, c->stream));
@@ -728,7 +729,7 @@ int pr_autotune_wavefront(pr_ctx* c, const pr_camera* cam, const pr_render_param
   cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   PR_CUDA(c, c->out.ensure(bytes));
   const unsigned int cand_slots[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22};
-  const unsigned int cand_bps[] = {16u, 32u, 64u};
+  const unsigned int cand_bps[] = {kTraceBlocksPerSM / 2, kTraceBlocksPerSM, 2 * kTraceBlocksPerSM};
   double best = 1e300;
   unsigned int best_s = 0, best_b = 0;
   // candidates run the host-driven loop (no graph is rebuilt per candidate);

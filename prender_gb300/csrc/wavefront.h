@@ -10,6 +10,10 @@
 namespace pr {
 
 // device-side counters of one frame
+// blocks of 128 resident per SM for the persistent traversal kernels
+// (__launch_bounds__(128, 8): 64 registers a thread)
+constexpr unsigned int kTraceBlocksPerSM = 8;
+
 struct WfCtl {
   unsigned int ext_count;    // segments queued for wf_extend this iteration
   unsigned int sh_count;     // shadow rays queued for wf_shadow this iteration
@@ -19,6 +23,8 @@ struct WfCtl {
   unsigned int iterations;
   unsigned int work;         // 1 while another iteration is needed
   unsigned int head_start;   // spawn_head when this iteration began (after correction)
+  unsigned int ext_fetch;    // extension rays taken by wf_extend's lanes so far
+  unsigned int sh_fetch;     // shadow rays taken by wf_shadow's lanes so far
   unsigned long long next_sample;
 };
 

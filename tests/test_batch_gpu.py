@@ -55,6 +55,6 @@ def test_autotuner_keeps_the_image(ctx):
     before = ctx.render(s)
     t = ctx.autotune(s)
     print("autotuned:", t)
-    assert t["slots"] in (1 << 19, 1 << 20, 1 << 21, 1 << 22) and t["trace_blocks_per_sm"] in (16, 32, 64)
+    assert t["slots"] in (1 << 19, 1 << 20, 1 << 21, 1 << 22) and t["trace_blocks_per_sm"] in (4, 8, 16)
     after = ctx.render(s)
     assert np.array_equal(before, after)
