@@ -90,13 +90,10 @@ __device__ __forceinline__ void make_vertex(const DevScene& S, float3 o, float3 
   v.mat = e.material;
   v.t = h.t;
   if (e.type == PR_ENT_SPHERE) {
-    // position and normal in FP64 from the FP64 distance (sphere.h:89-95),
-    // recomputed: the FP32 distance of the hit is off by up to half an ulp
-    // of t (1.5e-5 beyond t = 256), as much as the origin offset of the next
-    // ray near a coordinate of zero, which would then start behind the surface
+    // position and normal in FP64 from the FP64 distance (sphere.h:89-95):
+    // the hit's t plus the remainder fast_sphere kept in u
     const GEntity& ed = S.ents[h.ent];
-    double t;
-    if (!sphere_t64(ed, o, d, t)) t = h.t;
+    const double t = (double)h.t + (double)h.u;
     const double px = (double)o.x + t * (double)d.x, py = (double)o.y + t * (double)d.y, pz = (double)o.z + t * (double)d.z;
     const double nx = px - ed.p[0], ny = py - ed.p[1], nz = pz - ed.p[2];
     const double il = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);

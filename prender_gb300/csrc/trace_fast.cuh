@@ -156,10 +156,15 @@ __device__ __forceinline__ bool sphere_t64(const GEntity& e, float3 o, float3 d,
   return true;
 }
 
-__device__ __forceinline__ bool fast_sphere(const GEntity& e, float3 o, float3 d, float tmax, float& t) {
+// t is the FP32 distance, rest what it rounded off (t + rest is the FP64
+// distance to ~2^-48: the hit point is rebuilt from it, since the FP32
+// distance alone is up to half an ulp of t off -- 1.5e-5 beyond t = 256, as
+// much as the origin offset of the next ray near a coordinate of zero)
+__device__ __forceinline__ bool fast_sphere(const GEntity& e, float3 o, float3 d, float tmax, float& t, float& rest) {
   double tt;
   if (!sphere_t64(e, o, d, tt) || !(tt < (double)tmax)) return false;
   t = (float)tt;
+  rest = (float)(tt - (double)t);
   return true;
 }
 
@@ -217,7 +222,7 @@ __device__ __forceinline__ bool fast_closest(const DevScene& S, float3 o, float3
     float t = h.t, bu = 0.0f, bv = 0.0f;
     int slot = -1;
     bool got = false;
-    if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], o, d, h.t, t);
+    if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], o, d, h.t, t, bu);
     else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, o, d, h.t, t);
     else if (e.type == PR_ENT_CIRCLE) got = fast_circle(e, o, d, h.t, t);
     else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<false>(S, e, o, d, inv, t, slot, bu, bv, st, err);
@@ -241,7 +246,7 @@ __device__ __forceinline__ bool fast_occluded(const DevScene& S, float3 o, float
     float t = tmax, bu, bv;
     int slot;
     bool got = false;
-    if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], o, d, tmax, t);
+    if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], o, d, tmax, t, bu);
     else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, o, d, tmax, t);
     else if (e.type == PR_ENT_CIRCLE) got = fast_circle(e, o, d, tmax, t);
     else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<true>(S, e, o, d, inv, t, slot, bu, bv, st, err);

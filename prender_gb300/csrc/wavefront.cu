@@ -326,9 +326,9 @@ __device__ __forceinline__ bool lane_step(const DevScene& S, TraceLane& r, int32
         r.sp = 1;
         break;
       }
-      float t = r.tmax;
+      float t = r.tmax, rest = 0.0f;
       bool got = false;
-      if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], r.o, r.d, r.tmax, t);
+      if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], r.o, r.d, r.tmax, t, rest);
       else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, r.o, r.d, r.tmax, t);
       else if (e.type == PR_ENT_CIRCLE) got = fast_circle(e, r.o, r.d, r.tmax, t);
       r.ent++;
@@ -339,7 +339,8 @@ __device__ __forceinline__ bool lane_step(const DevScene& S, TraceLane& r, int32
       if (got && t < r.tmax) {
         r.h.ent = i;
         r.h.slot = -1;
-        r.h.u = r.h.v = 0.0f;
+        r.h.u = rest;  // a sphere's remainder of t (0 for planes and disks)
+        r.h.v = 0.0f;
         r.tmax = t;
         r.h.t = t;
       }
