@@ -153,7 +153,10 @@ __global__ void __launch_bounds__(256) wf_reset(unsigned int n_slots) {
   }
 }
 
-__global__ void __launch_bounds__(128) wf_shade() {
+// 6 blocks of 128 per SM (80 registers, a few spilled): measured on GB300
+// over 4 / 5 / 6 / 7 / 8 / 10 blocks, mesh Cornell box 1024x768x64 spp,
+// wf_shade 108 / 99 / 94 / 96 / 102 / 110 ms per frame
+__global__ void __launch_bounds__(128, 6) wf_shade() {
   const DevScene& S = c_scene;
   const RenderCfg& cfg = c_cfg;
   const WfBufs& B = c_buf;
