@@ -53,7 +53,9 @@ def test_scene_file_render_matches_oracle_statistically(ctx, name):
     b = np.stack([ctx.render(s, sample_offset=k * spp).astype(np.float64) for k in range(nb)])
     mean = b.mean(0)
     sd = b.std(0, ddof=1)
-    ref, _, _ = O.OracleScene(s).render(threads=os.cpu_count())
+    # one oracle thread: the oracle's rows then draw from fixed streams, so
+    # the comparison is the same on every run
+    ref, _, _ = O.OracleScene(s).render(threads=1)
     sigma = np.sqrt(sd ** 2 / nb + sd ** 2) + 1e-6
     z = np.abs(mean - ref) / sigma
     frac = float((z > 3.0).mean())
