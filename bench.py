@@ -25,6 +25,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Mpaths/s on 1 GB300 at matched RMSE, wavefront vs plain; adjoint/forward cost"
+# bytes a traversal reads per node visit / triangle test / ray (see the roofline below)
+B_NODE, B_TRI, B_RAY = 80.0, 48.0, 64.0
 
 
 def baseline_metric():
@@ -38,8 +40,8 @@ def baseline_metric():
 def workload(small: bool, profile: bool = False):
     from prender_gb300 import scenes
     if profile:
-        s = scenes.mesh_cornell(width=256, height=192, samples=4, supersamples=2, subdiv=7)
-        name = "mesh_cornell_256x192_16spp_subdiv7"
+        s = scenes.mesh_cornell(width=512, height=384, samples=4, supersamples=2, subdiv=7)
+        name = "mesh_cornell_512x384_16spp_subdiv7"
     elif small:
         s = scenes.mesh_cornell(width=256, height=192, samples=4, supersamples=2, subdiv=5)
         name = "mesh_cornell_256x192_16spp_subdiv5"
@@ -118,17 +120,33 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def sample_rows(height: int, rows: int):
+    """rows image rows spread evenly over the frame (every k-th row, the
+    first at k / 2), so the CPU sample sees walls, floor, light and mesh in
+    the frame's own proportions"""
+    rows = max(1, min(rows, height))
+    step = height / rows
+    return [int(step * i + step / 2) for i in range(rows)]
+
+
 def cpu_baseline(scene, rows: int, threads: int):
-    """The oracle port on the host cores over a bounded band of rows."""
+    """The oracle port on the host cores over a bounded sample of rows spread
+    over the whole frame."""
     from oracle import oracle as O
     o = O.OracleScene(scene)
-    H = scene.camera.height
-    r0 = H // 2 - rows // 2
+    rl = sample_rows(scene.camera.height, rows)
     t0 = time.perf_counter()
-    _, secs, _ = o.render(threads=threads, row0=r0, row1=r0 + rows)
+    _, secs, _ = o.render_rows(rl, threads=threads)
     wall = time.perf_counter() - t0
-    paths = rows * scene.camera.width * scene.settings.spp
+    paths = len(rl) * scene.camera.width * scene.settings.spp
     return paths / secs / 1e6, secs, wall, paths
+
+
+def sample_desc(scene, rows: int) -> str:
+    H = scene.camera.height
+    rl = sample_rows(H, rows)
+    return (f"{len(rl)} rows spread over the frame (every {H / len(rl):g}th row of {H}) x "
+            f"{scene.camera.width} px x {scene.settings.spp} spp")
 
 
 def run_reference(args):
@@ -144,7 +162,7 @@ def run_reference(args):
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
-    sample = f"{rows} middle rows x {scene.camera.width} px x {scene.settings.spp} spp per step"
+    sample = sample_desc(scene, rows) + " per step"
     line = {
         "impl": "reference", "metric": baseline_metric(), "value": round(value, 4), "unit": "Mpaths/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -205,6 +223,9 @@ def run_gpu(args):
             kern.append(st["device_ms"] / 1e3)
         return walls, kern, st
 
+    tuned = None
+    if args.autotune and args.mode == "wavefront":
+        tuned = ctx.autotune(scene)  # pool size and traversal grid for this scene, kept by the context
     for i in range(args.warmup):
         step(i)
     clk = ClockSampler(local)
@@ -275,9 +296,10 @@ def run_gpu(args):
             dist.destroy_process_group()
         return 0
     # roofline of the dominant kernel: algorithmic bytes of its traversal,
-    # B = 144 N_node + 36 N_tri + 64 per ray (128-byte node + 16 B of
-    # metadata, three 12-byte vertices, ray record in and hit record out),
-    # over its own device time
+    # B = 80 N_node + 48 N_tri + 64 per ray (one 80-byte compressed 8-wide
+    # node per visit, three 16-byte vertex records per triangle test, ray
+    # record in and hit record out), N_node and N_tri counted by the kernel
+    # itself on this frame, over its own device time
     segs = st["segments"]
     peak, peak_kind = measured_peak_hbm()
     if kernel_ms:
@@ -288,7 +310,7 @@ def run_gpu(args):
             nodes = kernel_ms["nodes"] - kernel_ms["shadow_nodes"]
             tris = kernel_ms["tris"] - kernel_ms["shadow_tris"]
             rays = kernel_ms["segments"] - kernel_ms["shadow_rays"]
-        alg_bytes = 144.0 * nodes + 36.0 * tris + 64.0 * rays
+        alg_bytes = B_NODE * nodes + B_TRI * tris + B_RAY * rays
         achieved = alg_bytes / (kernel_ms[dom] / 1e3) / 1e9
         roof = {"bound": "hbm", "kernel": f"wf_{dom}", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
@@ -297,8 +319,9 @@ def run_gpu(args):
                 "kernel_ms_per_frame": {k: round(kernel_ms[k], 3) for k in ("shade", "extend", "shadow", "control")},
                 "kernel_rays_per_frame": int(rays), "kernel_nodes_per_frame": int(nodes),
                 "kernel_tris_per_frame": int(tris),
-                "note": "algorithmic traversal bytes of the dominant kernel over its CUDA-event time; "
-                        "the scene (~28 MB) is L2-resident, so DRAM traffic is far below these bytes"}
+                "note": "algorithmic traversal bytes of the dominant kernel (80 B per wide-node visit, 48 B per "
+                        "triangle test, 64 B per ray) over its CUDA-event time; the scene (~26 MB) is "
+                        "L2-resident, so DRAM traffic is far below these bytes"}
         prof = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(prof):
             try:
@@ -312,18 +335,21 @@ def run_gpu(args):
             except (OSError, ValueError, KeyError):
                 pass
     else:
-        alg_bytes = 144.0 * st["nodes_visited"] + 36.0 * st["tri_tests"] + 64.0 * segs + 12.0 * st["paths"]
+        alg_bytes = B_NODE * st["nodes_visited"] + B_TRI * st["tri_tests"] + B_RAY * segs + 12.0 * st["paths"]
         achieved = alg_bytes / (st["device_ms"] / 1e3) / 1e9
         roof = {"bound": "hbm", "kernel": "pt_megakernel", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
                 "note": "algorithmic traversal bytes of the frame; scene (~28 MB) is L2-resident"}
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = adjoint_cost(ctx, local, args.small)
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         threads = os.cpu_count() or 1
         rows = max(1, int(args.ref_rows))
         v, secs, wall, npaths = cpu_baseline(scene, rows, threads)
         cpu = {"value": round(v, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
-               "sample": f"{rows} middle rows x {W} px x {spp} spp ({npaths} paths, {secs:.1f} s)"}
+               "sample": sample_desc(scene, rows) + f" ({npaths} paths, {secs:.1f} s)"}
     line = {
         "metric": baseline_metric(), "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
@@ -331,11 +357,12 @@ def run_gpu(args):
         "config": {"workload": name, "width": W, "height": H, "spp": spp, "triangles": int(scene.meshes[1].faces.shape[0]),
                    "nee": 1, "mode": args.mode, "other_form": other, "l2": "flushed between steps (256 MB write)",
                    "paths_per_step": paths, "segments_per_step": segs, "kernel_ms_per_step": round(kern_s * 1e3, 3),
-                   "scene_upload_s": round(upload_s, 3)},
+                   "scene_upload_s": round(upload_s, 3), "autotuned": tuned},
         "e2e": {"value": round(e2e_val, 3), "unit": "Mpaths/s",
                 "h2d_bytes_per_step": C.sizeof(cam) + C.sizeof(prm), "d2h_bytes_per_step": W * H * 3 * 4},
         "gpu_launches": int(st["kernel_launches"]) * args.steps,
         "roofline": roof,
+        "adjoint": adjoint,
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
@@ -344,6 +371,68 @@ def run_gpu(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def adjoint_cost(ctx, device: int, small: bool, reps: int = 3):
+    """The metric's second half on the differentiable-render workload: mesh
+    Cornell box 512^2, 64 spp (16 x 2^2 tent-filtered), eight Lambertian
+    materials with RGB albedo U(0.1, 0.9) plus the light's emission scale as
+    parameters; L2 loss to a target rendered at parameters perturbed by
+    N(0, 0.1^2).  Device time of one forward frame (plain form, which the
+    adjoint replays, and the wavefront form) against one path-replay adjoint
+    pass through pr_render_adjoint_dev."""
+    import ctypes as C
+    import torch
+    from prender_gb300 import _abi as A
+    from prender_gb300 import scenes
+    side = 128 if small else 512
+    s = scenes.diff_cornell(side, side, samples=16, supersamples=2, subdiv=5, seed=0)
+    alb = np.random.default_rng(0).uniform(0.1, 0.9, (8, 3))  # diff_cornell's own draw for seed 0
+    pert = np.random.default_rng(1)
+    tgt = scenes.diff_cornell(side, side, samples=16, supersamples=2, subdiv=5, seed=0,
+                              albedo=np.clip(alb + pert.normal(0.0, 0.1, alb.shape), 0.0, 1.0),
+                              emission_scale=1.0 + float(pert.normal(0.0, 0.1)))
+    dev = f"cuda:{device}"
+    L = ctx.L
+    target = torch.empty((side, side, 3), dtype=torch.float32, device=dev)
+    img = torch.empty_like(target)
+    cam = s.camera.to_c()
+
+    def render(out, mode, off=0):
+        prm = s.settings.to_c()
+        prm.mode = mode
+        rc = L.pr_render_dev(ctx.h, C.byref(cam), C.byref(prm), C.c_void_p(out.data_ptr()), off, 0)
+        if rc != 0:
+            raise RuntimeError(L.pr_last_error(ctx.h).decode())
+        return ctx.stats()["device_ms"]
+
+    ctx.upload(tgt)
+    render(target, A.PR_MODE_MEGAKERNEL, off=1 << 20)
+    ctx.upload(s)
+    fwd = [render(img, A.PR_MODE_MEGAKERNEL) for _ in range(reps + 1)][1:]
+    fwd_wf = [render(img, A.PR_MODE_WAVEFRONT) for _ in range(reps + 1)][1:]
+    render(img, A.PR_MODE_MEGAKERNEL)
+    dl = (2.0 * (img - target)).contiguous()
+    n_mat = len(s.materials)
+    d_color = torch.zeros((n_mat, 3), dtype=torch.float64, device=dev)
+    d_em = torch.zeros((n_mat, 3), dtype=torch.float64, device=dev)
+    prm = s.settings.to_c()
+    adj = []
+    for _ in range(reps + 1):
+        rc = L.pr_render_adjoint_dev(ctx.h, C.byref(cam), C.byref(prm), C.c_void_p(dl.data_ptr()), 0,
+                                     C.c_void_p(d_color.data_ptr()), C.c_void_p(d_em.data_ptr()))
+        if rc != 0:
+            raise RuntimeError(L.pr_last_error(ctx.h).decode())
+        adj.append(ctx.stats()["device_ms"])
+    adj = adj[1:]
+    f, fw, a = statistics.median(fwd), statistics.median(fwd_wf), statistics.median(adj)
+    loss = float(((img - target) ** 2).sum())
+    return {"workload": f"diff_cornell_{side}x{side}_64spp_8materials_subdiv5", "paths": side * side * 64,
+            "forward_ms": round(f, 3), "forward_wavefront_ms": round(fw, 3), "adjoint_ms": round(a, 3),
+            "ratio": round(a / f, 3), "ratio_vs_wavefront": round(a / fw, 3), "loss": loss,
+            "grad_norm": float(torch.linalg.norm(d_color).item()),
+            "note": "device time per pass (CUDA events on the render stream), median of "
+                    f"{reps}; ratio = adjoint / forward of the plain form the adjoint replays"}
 
 
 def kerr_jobs(n_jobs: int, width: int, height: int, precision: int):
@@ -454,6 +543,9 @@ def main():
     ap.add_argument("--small", action="store_true")
     ap.add_argument("--profile", action="store_true", help="full scene, 256x192x16spp image (ncu captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward cost measurement")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default wavefront pool size and traversal grid")
     ap.add_argument("--ref-rows", type=int, default=48)
     ap.add_argument("--workload", default="mesh", choices=["mesh", "kerr"],
                     help="kerr: the Kerr lensing renders (not the headline workload)")

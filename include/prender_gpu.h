@@ -307,10 +307,16 @@ int pr_render_dev(pr_ctx* ctx, const pr_camera* cam, const pr_render_params* prm
  * cudaFree; its scratch is a 16 MiB
  * static device array that every GPU loading this library keeps until exit,
  * so images of at most 1,398,080 pixels are accepted (larger ones return
- * PR_E_ARG).  The first call on a device looks up that array's address and
- * should be made before any stream capture starts.  Calls that overlap on
- * the GPU share the array and race.  The scene must already be uploaded with
- * pr_scene_upload (which allocates, at set-up).  Result as pr_render_dev. */
+ * PR_E_ARG).  The first call on a device looks up that array's address in
+ * the device's primary context and keeps it; make that first call before
+ * any stream capture starts.  The kept address is not valid in a context
+ * made with the driver API, nor after cudaDeviceReset.  Calls that overlap
+ * on the GPU share the array and race.  The scene must already be uploaded
+ * with pr_scene_upload (which allocates, at set-up).  Result as
+ * pr_render_dev, except where pr_render_dev's per-chunk partial images
+ * (min(ceil(1.2e6 / pixels), spp) chunks of W*H*3 floats) would not fit in
+ * the array: there the samples are summed in fewer chunks, so the image
+ * agrees with pr_render_dev's to float rounding rather than bit for bit. */
 int pr_render_dev_noalloc(pr_ctx* ctx, const pr_camera* cam, const pr_render_params* prm, float* rgb_accum_dev,
                           uint64_t sample_offset, int accumulate);
 
@@ -329,10 +335,11 @@ typedef struct pr_render_stats {
 } pr_render_stats;
 int pr_last_render_stats(pr_ctx* ctx, pr_render_stats* stats);
 /* Autotuner (no reference counterpart): times one short wavefront frame
- * (one camera sample per pixel, the caller's camera and parameters) for each
- * candidate path-pool size {2^19 .. 2^22} and traversal grid {4, 8, 16}
- * blocks per SM, and keeps the fastest for later pr_render calls on this
- * context.  Images do not depend on either choice.  Outputs may be NULL. */
+ * (the caller's camera and parameters with enough camera samples per pixel
+ * to fill the largest pool twice over) for each candidate path-pool size
+ * {2^19 .. 2^22} and traversal grid {4, 8, 16} blocks per SM, and keeps the
+ * fastest for later pr_render calls on this context.  Images do not depend
+ * on either choice.  Outputs may be NULL. */
 int pr_autotune_wavefront(pr_ctx* ctx, const pr_camera* camera, const pr_render_params* params,
                           int32_t* slots, int32_t* trace_blocks_per_sm, double* frame_ms);
 

@@ -45,11 +45,21 @@ def lib():
         L.oracle_first_hit.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp]
         L.oracle_radiance.argtypes = [vp, vp, C.c_int64, C.c_uint64, vp, vp]
         L.oracle_render.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
+        L.oracle_render_rows.argtypes = [vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp]
         L.oracle_light_count.argtypes = [vp]
         L.oracle_kerr_trace.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]
         L.oracle_kerr_disk_shade.argtypes = [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp]
+        L.oracle_sample_hg.argtypes = [C.c_double, C.c_int, C.c_uint64, vp, C.c_int64, vp]
         _lib = L
     return _lib
+
+
+def sample_hg(g: float, correct: bool, seed: int, raydir, n: int) -> np.ndarray:
+    """n scattering directions of sampleHG about raydir (n x 3)"""
+    d = np.ascontiguousarray(raydir, dtype=np.float64)
+    out = np.empty((n, 3), np.float64)
+    assert lib().oracle_sample_hg(float(g), int(bool(correct)), int(seed), _p(d), int(n), _p(out)) == 0
+    return out
 
 
 def _p(a):
@@ -104,6 +114,19 @@ class OracleScene:
         segs = C.c_uint64(0)
         rc = lib().oracle_render(self.h, C.byref(cam), C.byref(prm), threads, row0, row1, _p(img),
                                  C.byref(secs), C.byref(segs))
+        assert rc == 0, rc
+        return img, secs.value, segs.value
+
+    def render_rows(self, rows, threads: int = 1, settings=None):
+        """Render::Run over the given image rows only (the rest stays zero)."""
+        cam = self.scene.camera.to_c()
+        prm = (settings or self.scene.settings).to_c()
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        img = np.zeros((cam.height, cam.width, 3), np.float64)
+        secs = C.c_double(0)
+        segs = C.c_uint64(0)
+        rc = lib().oracle_render_rows(self.h, C.byref(cam), C.byref(prm), threads, _p(r), int(r.size), _p(img),
+                                      C.byref(secs), C.byref(segs))
         assert rc == 0, rc
         return img, secs.value, segs.value
 

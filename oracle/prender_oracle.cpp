@@ -1818,18 +1818,58 @@ int oracle_radiance(void* h, const double* rays, int64_t n, uint64_t seed, const
   return PR_OK;
 }
 
+// sampleHG (sampler.h:24-93) about one incoming direction, n draws from one
+// MT19937-64 stream: the reference's (g/2) form, or with correct != 0 the
+// Henyey-Greenstein inverse CDF.  out: n x 3 unit directions.
+int oracle_sample_hg(double g, int correct, uint64_t seed, const double* raydir, int64_t n, double* out) {
+  if (!raydir || !out || n < 0) return PR_E_ARG;
+  static const Scene empty{};
+  MT64 rnd(seed);
+  Ctx c{empty, rnd, 0, 0, 0, 0, correct};
+  const V3 d = normalize(V3(raydir[0], raydir[1], raydir[2]));
+  for (int64_t k = 0; k < n; k++) {
+    const V3 v = sample_hg(c, d, g);
+    out[3 * k] = v.x; out[3 * k + 1] = v.y; out[3 * k + 2] = v.z;
+  }
+  return PR_OK;
+}
+
 // Render::Run (render.h:1125-1455) over rows [row0, row1): per-thread MT
 // streams seeded thread_id+1, OpenMP dynamic rows, tent filter, luminance
 // cutoff and sensor response.  image: W*H*3 doubles (reference row order).
 // With threads == 1 the result equals the reference bit for bit.
+static int render_rows(OracleScene* o, const pr_camera* cam, const pr_render_params* prm, int threads,
+                       const std::vector<int>& rows, double* image, double* seconds, uint64_t* segments);
+
 int oracle_render(void* h, const pr_camera* cam, const pr_render_params* prm, int threads, int row0, int row1,
                   double* image, double* seconds, uint64_t* segments) {
   auto* o = static_cast<OracleScene*>(h);
   if (!o || !cam || !prm || !image || threads < 1) return PR_E_ARG;
-  const Scene& s = o->s;
-  const int W = cam->width, H = cam->height;
+  const int H = cam->height;
   if (row0 < 0) row0 = 0;
   if (row1 <= 0 || row1 > H) row1 = H;
+  std::vector<int> rows;
+  for (int y = row0; y < row1; y++) rows.push_back(y);
+  return render_rows(o, cam, prm, threads, rows, image, seconds, segments);
+}
+
+// The same over an explicit list of rows (each in [0, H)), e.g. every k-th
+// row of the frame for a CPU sample spread over the whole image.
+int oracle_render_rows(void* h, const pr_camera* cam, const pr_render_params* prm, int threads, const int32_t* rows,
+                       int n_rows, double* image, double* seconds, uint64_t* segments) {
+  auto* o = static_cast<OracleScene*>(h);
+  if (!o || !cam || !prm || !image || threads < 1 || n_rows < 0 || (n_rows > 0 && !rows)) return PR_E_ARG;
+  std::vector<int> r(rows, rows + n_rows);
+  for (int y : r)
+    if (y < 0 || y >= cam->height) return PR_E_ARG;
+  return render_rows(o, cam, prm, threads, r, image, seconds, segments);
+}
+
+static int render_rows(OracleScene* o, const pr_camera* cam, const pr_render_params* prm, int threads,
+                       const std::vector<int>& rows, double* image, double* seconds, uint64_t* segments) {
+  const Scene& s = o->s;
+  const int W = cam->width, H = cam->height;
+  const int n_rows = (int)rows.size();
   // CameraScreenPram (render.h:105-150)
   V3 cpos(cam->position[0], cam->position[1], cam->position[2]);
   V3 cdir(cam->dir[0], cam->dir[1], cam->dir[2]);
@@ -1863,7 +1903,8 @@ int oracle_render(void* h, const pr_camera* cam, const pr_render_params* prm, in
   const auto t0 = std::chrono::steady_clock::now();
   for (int sidx = 0; sidx < samples; sidx++) {
 #pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
-    for (int y = row0; y < row1; y++) {
+    for (int ri = 0; ri < n_rows; ri++) {
+      const int y = rows[ri];
       const int tid = omp_get_thread_num();
       tl_segments = 0;
       tl_disk_rnd = drnd[tid].get();

@@ -46,13 +46,7 @@ int check_device_errors(pr_ctx* c) {
   PR_CUDA(c, cudaMemcpyAsync(&bits, c->errword.p, 4, cudaMemcpyDeviceToHost, c->stream));
   PR_CUDA(c, cudaStreamSynchronize(c->stream));
   if (!bits) return PR_OK;
-  std::string m = "device check fired:";
-  if (bits & PR_DEV_STACK_OVERFLOW) m += " traversal-stack-overflow";
-  if (bits & PR_DEV_LOOP_CAP) m += " loop-cap";
-  if (bits & PR_DEV_BAD_INDEX) m += " bad-index";
-  if (bits & PR_DEV_QUEUE_OVERFLOW) m += " queue-overflow";
-  if (bits & PR_DEV_NONFINITE) m += " non-finite-radiance";
-  return fail(c, PR_E_DEVICE, m);
+  return fail(c, PR_E_DEVICE, pr::device_error_message(bits));
 }
 
 template <class T>
@@ -65,6 +59,18 @@ cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
 }  // namespace
 
 int pr::ctx_fail(pr_ctx* c, int code, const std::string& msg) { return fail(c, code, msg); }
+
+std::string pr::device_error_message(uint32_t bits) {
+  std::string m = "device check fired:";
+  if (bits & PR_DEV_STACK_OVERFLOW) m += " traversal-stack-overflow";
+  if (bits & PR_DEV_LOOP_CAP) m += " loop-cap";
+  if (bits & PR_DEV_BAD_INDEX) m += " bad-index";
+  if (bits & PR_DEV_QUEUE_OVERFLOW) m += " queue-overflow";
+  if (bits & PR_DEV_NONFINITE) m += " non-finite-radiance";
+  const uint32_t known = PR_DEV_STACK_OVERFLOW | PR_DEV_LOOP_CAP | PR_DEV_BAD_INDEX | PR_DEV_QUEUE_OVERFLOW | PR_DEV_NONFINITE;
+  if (bits & ~known) m += " other (bits " + std::to_string(bits & ~known) + ")";
+  return m;
+}
 
 extern "C" {
 
@@ -150,7 +156,7 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   S.mats = (const GMaterial*)o.mats.p;
   S.nodes = (const GNode*)o.nodes.p;
   S.tris = (const float4*)o.tris.p;
-  S.rnodes = (const GNode*)o.rnodes.p;
+  S.rnodes = (const WNode*)o.rnodes.p;
   S.rtris = (const float4*)o.rtris.p;
   S.fnorm = (const float*)o.fnorm.p;
   S.n_ents = (int)h.ents.size();
@@ -719,17 +725,21 @@ int pr_autotune_wavefront(pr_ctx* c, const pr_camera* cam, const pr_render_param
   if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
   if (!cam || !p) return fail(c, PR_E_ARG, "null camera or parameters");
   if (c->cur.kerr.enabled) return fail(c, PR_E_UNSUPPORTED, "Kerr scenes do not use the wavefront form");
+  const unsigned int cand_slots[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22};
+  const unsigned int cand_bps[] = {kTraceBlocksPerSM / 2, kTraceBlocksPerSM, 2 * kTraceBlocksPerSM};
+  // a tuning frame of the caller's scene with enough camera samples to keep
+  // the largest pool full for a while (twice its slots, at least one per pixel)
   pr_render_params q = *p;
   q.mode = PR_MODE_WAVEFRONT;
-  q.samples = 1;
+  const double pixels = std::max(1.0, (double)cam->width * (double)cam->height);
+  q.samples = (int32_t)std::max(1.0, std::ceil(2.0 * (double)cand_slots[3] / pixels));
   q.supersamples = 1;
   q.tent_filter = 0;
+  q.total_spp = 0;
   const size_t bytes = sizeof(float) * 3 * (size_t)cam->width * cam->height;
   PR_CUDA(c, cudaSetDevice(c->device));
   cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   PR_CUDA(c, c->out.ensure(bytes));
-  const unsigned int cand_slots[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22};
-  const unsigned int cand_bps[] = {kTraceBlocksPerSM / 2, kTraceBlocksPerSM, 2 * kTraceBlocksPerSM};
   double best = 1e300;
   unsigned int best_s = 0, best_b = 0;
   // candidates run the host-driven loop (no graph is rebuilt per candidate);

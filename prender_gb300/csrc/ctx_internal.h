@@ -90,4 +90,6 @@ namespace pr {
 int prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, uint64_t sample_offset, RenderCfg& g,
                    const SceneObjData* scene = nullptr);
 int ctx_fail(pr_ctx* c, int code, const std::string& msg);
+// names of the set bits of a device error word (PR_DEV_*), for pr_last_error
+std::string device_error_message(uint32_t bits);
 }  // namespace pr

@@ -1,6 +1,10 @@
-// Kerr geodesics, FP32 form (see kerr_math.cuh): FP32 integration with a
-// float-pair state, FP64 only for the set-up, the pole steps and the exit
-// direction.  Compiled with FMA contraction.
+// Kerr geodesics, mixed-precision form (PR_KERR_FP32; the templates are in
+// kerr_math.cuh): the reference's FP64 Cash-Karp steps with its error
+// control near the hole and among the scene geometry; FP32 increments of
+// fixed h = 2 steps, added to the FP64 state, only for outbound rays beyond
+// max(200 M, scene radius + 2) whose last FP64 error estimate is small; and
+// an inbound ray with no radial turning point left reported as captured at
+// once.  Compiled with FMA contraction (the FP64 form, kerr.cu, is not).
 #include "kerr_math.cuh"
 
 namespace pr {

@@ -22,6 +22,7 @@ namespace pr {
 constexpr int kMaxEntities = 48;
 constexpr int kMaxLights = 16;
 constexpr int kStackSize = 64;          // QBVH traversal stack (entries)
+constexpr int kWStack = 32;             // wide-tree traversal stack (node groups); a tree may be this deep
 constexpr int kSplitStack = 4;          // pending glass branches (depth <= 2 splits)
 constexpr int32_t kChildInvalid = -1;   // QBVH child slot without a child
 // leaf child = kLeafBit | first leaf slot; inner child = node index (>= 0)
@@ -37,6 +38,30 @@ struct alignas(16) GNode {   // 128 bytes
   int32_t pad;
 };
 static_assert(sizeof(GNode) == 128, "GNode must be 128 bytes");
+
+// The render path's node: eight children with boxes quantised to 8 bits per
+// plane on a per-node grid (compressed wide BVH node after Ylitie, Karras
+// and Laine, "Efficient Incoherent Ray Traversal on GPUs Through Compressed
+// Wide BVHs", HPG 2017), 80 bytes = five 128-bit loads.  Child box of slot s
+// on axis a: [p_a + qlo_a[s] * 2^ea, p_a + qhi_a[s] * 2^ea].  Inner children
+// are stored contiguously from child_base in slot order (child of slot s =
+// child_base + popcount(imask below s)); the triangles of the leaf children
+// (at most 3 each) contiguously from tri_base in slot order.  meta byte s of
+// a leaf = (1 << count) - 1 << 5 | offset of its first triangle from
+// tri_base; 0 for inner and empty slots.  An empty slot has qlo > qhi.
+// Slots are assigned so that a ray whose direction has sign bits k (bit a
+// set: negative along axis a) meets the children roughly near to far in the
+// order slot = i ^ k, i = 0..7.
+struct alignas(16) WNode {   // 80 bytes
+  float p[3];
+  uint32_t e_imask;        // ex | ey << 8 | ez << 16 (biased float exponents) | imask << 24
+  int32_t child_base;
+  int32_t tri_base;
+  uint32_t meta[2];        // byte s of the pair
+  uint32_t qlo_x[2], qlo_y[2], qlo_z[2];
+  uint32_t qhi_x[2], qhi_y[2], qhi_z[2];
+};
+static_assert(sizeof(WNode) == 80, "WNode must be 80 bytes");
 
 struct GMaterial {
   int32_t type;
@@ -162,8 +187,8 @@ struct DevScene {
   const GMaterial* mats;
   const GNode* nodes;      // the reference's trees (exact first-hit path)
   const float4* tris;      // 3 per leaf slot
-  const GNode* rnodes;     // the render path's trees (render_bvh.h)
-  const float4* rtris;     // 3 per leaf slot of those
+  const WNode* rnodes;     // the render path's trees (render_bvh.h)
+  const float4* rtris;     // 3 per triangle slot of those
   const float* fnorm;      // 3 per face
   int32_t n_ents;
   int32_t n_lights;

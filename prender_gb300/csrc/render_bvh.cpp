@@ -1,11 +1,15 @@
-// Binned-SAH 4-wide BVH for the FP32 render traversal (see render_bvh.h).
+// Binned-SAH BVH collapsed to compressed 8-wide nodes for the FP32 render
+// traversal (see render_bvh.h and WNode in pr_internal.h).
 //
 // A binary tree is built top-down with 16 centroid bins on each axis and
 // the surface-area cost Ct + Ci (A_L N_L + A_R N_R) / A against a leaf's
 // Ci N; nodes of more than kMaxLeaf triangles are always split (at the
-// median when every centroid falls in one bin).  Each binary node and its
-// two children are then emitted as one 4-wide node (grandchildren in slots
-// 0-3), which is the layout and child order the traversal expects.
+// median when every centroid falls in one bin).  Each wide node then takes
+// a binary node's children and keeps opening the child of largest surface
+// area until it holds eight (or only leaves remain).  Children go to slots
+// by the octant of their centroid seen from the node's (greedy assignment
+// of the eight corner directions), and their boxes are quantised outward on
+// a grid of power-of-two spacing anchored at the node's padded minimum.
 #include "render_bvh.h"
 
 #include <algorithm>
@@ -16,11 +20,10 @@ namespace pr {
 namespace {
 
 constexpr int kBins = 16;
-constexpr int kMaxLeaf = 8;
-// a 4-wide node visit against one triangle test: measured on GB300 (mesh
-// Cornell box, wavefront frame) over 1.2 / 3 / 6 / 12 with leaves of at most
-// 8 or 16 triangles; 3 with 8 was fastest
+constexpr int kMaxLeaf = 3;  // a wide node's meta byte holds at most three triangles per leaf
+// a node visit against one triangle test in the binary SAH
 constexpr float kCostNode = 3.0f;
+constexpr int kWidth = 8;
 
 struct Box {
   float mn[3] = {3.0e38f, 3.0e38f, 3.0e38f};
@@ -168,92 +171,188 @@ struct Emitter {
   const std::vector<Tri>& tris;
   const float* vertices;
   const int32_t* faces;
-  std::vector<GNode>& out;
+  std::vector<WNode>& out;
   std::vector<float4>& otris;
 
-  int32_t leaf(const BNode& b, uint16_t& count) {
-    const int32_t slot = (int32_t)(otris.size() / 3);
-    for (int i = b.first; i < b.first + b.count; i++) {
-      const int32_t f = tris[i].face;
-      for (int k = 0; k < 3; k++) {
-        const float* v = vertices + 3 * (size_t)faces[3 * (size_t)f + k];
-        float4 q;
-        q.x = v[0];
-        q.y = v[1];
-        q.z = v[2];
-        int32_t w = (k == 0) ? f : 0;
-        memcpy(&q.w, &w, 4);
-        otris.push_back(q);
-      }
+  // children of binary node n for one wide node: open the largest inner child
+  // until there are kWidth (a leaf root stays a single leaf child)
+  void gather(int n, std::vector<int>& ch) const {
+    ch.clear();
+    if (bn[n].left < 0) {
+      ch.push_back(n);
+      return;
     }
-    count = (uint16_t)b.count;
-    return (int32_t)(kLeafBit | (uint32_t)slot);
+    ch.push_back(bn[n].left);
+    ch.push_back(bn[n].right);
+    while ((int)ch.size() < kWidth) {
+      int best = -1;
+      float ba = -1.0f;
+      for (int i = 0; i < (int)ch.size(); i++) {
+        const BNode& c = bn[ch[i]];
+        if (c.left < 0) continue;
+        const float a = c.box.area();
+        if (a > ba) {
+          ba = a;
+          best = i;
+        }
+      }
+      if (best < 0) break;
+      const int c = ch[best];
+      ch[best] = bn[c].left;
+      ch.push_back(bn[c].right);
+    }
   }
 
-  // one 4-wide node from binary node n (a leaf root becomes a node with one leaf child)
-  int32_t emit(int n) {
-    const int32_t idx = (int32_t)out.size();
-    out.emplace_back();
-    int slots[4] = {-1, -1, -1, -1};
-    int at = 0, al = 0, ar = 0;
-    const BNode& b = bn[n];
-    if (b.left < 0) {
-      slots[0] = n;
-    } else {
-      at = b.axis;
-      const BNode& L = bn[b.left];
-      const BNode& R = bn[b.right];
-      if (L.left < 0) {
-        slots[0] = b.left;
-      } else {
-        slots[0] = L.left;
-        slots[1] = L.right;
-        al = L.axis;
-      }
-      if (R.left < 0) {
-        slots[2] = b.right;
-      } else {
-        slots[2] = R.left;
-        slots[3] = R.right;
-        ar = R.axis;
-      }
+  // slot of each child: greedy assignment of the octant corner directions
+  // (slot s points to -/+ along axis a as bit a of s is 0/1) to the children
+  // whose centroid, seen from the node's centre, lies furthest that way
+  static void assign_slots(const Box& node, const std::vector<Box>& boxes, int slot_of[kWidth]) {
+    const int n = (int)boxes.size();
+    float cost[kWidth][kWidth];
+    float nc[3];
+    for (int a = 0; a < 3; a++) nc[a] = 0.5f * (node.mn[a] + node.mx[a]);
+    for (int i = 0; i < n; i++) {
+      float d[3];
+      for (int a = 0; a < 3; a++) d[a] = 0.5f * (boxes[i].mn[a] + boxes[i].mx[a]) - nc[a];
+      for (int s = 0; s < kWidth; s++)
+        cost[i][s] = -((s & 1 ? d[0] : -d[0]) + (s & 2 ? d[1] : -d[1]) + (s & 4 ? d[2] : -d[2]));
     }
-    GNode g;
-    memset(&g, 0, sizeof(g));
-    for (int s = 0; s < 4; s++) {
-      if (slots[s] < 0) {
-        g.child[s] = kChildInvalid;
-        // an empty box no ray enters
-        g.bmin_x[s] = g.bmin_y[s] = g.bmin_z[s] = 3.0e38f;
-        g.bmax_x[s] = g.bmax_y[s] = g.bmax_z[s] = -3.0e38f;
+    bool child_done[kWidth] = {}, slot_used[kWidth] = {};
+    for (int k = 0; k < n; k++) {
+      int bi = -1, bs = -1;
+      float bc = 3.0e38f;
+      for (int i = 0; i < n; i++) {
+        if (child_done[i]) continue;
+        for (int s = 0; s < kWidth; s++)
+          if (!slot_used[s] && cost[i][s] < bc) {
+            bc = cost[i][s];
+            bi = i;
+            bs = s;
+          }
+      }
+      child_done[bi] = true;
+      slot_used[bs] = true;
+      slot_of[bi] = bs;
+    }
+  }
+
+  int max_depth = 0;
+
+  // fills node idx from binary node n; returns after its subtree is emitted
+  void emit(int idx, int n, int depth) {
+    max_depth = std::max(max_depth, depth);
+    std::vector<int> ch;
+    gather(n, ch);
+    const int nch = (int)ch.size();
+    std::vector<Box> boxes(nch);
+    Box nb;
+    for (int i = 0; i < nch; i++) {
+      boxes[i] = padded(bn[ch[i]].box);
+      nb.grow(boxes[i]);
+    }
+    int slot_of[kWidth];
+    assign_slots(nb, boxes, slot_of);
+    int at_slot[kWidth];
+    for (int s = 0; s < kWidth; s++) at_slot[s] = -1;
+    for (int i = 0; i < nch; i++) at_slot[slot_of[i]] = i;
+
+    WNode w;
+    memset(&w, 0, sizeof(w));
+    // grid of spacing 2^e >= extent / 253 with its origin one step below the
+    // node's padded minimum: every child box keeps a full step of margin on
+    // each side (the traversal's plane distances may be off by half a step)
+    uint32_t ebits[3];
+    float scale[3];
+    for (int a = 0; a < 3; a++) {
+      const double ext = std::max((double)nb.mx[a] - (double)nb.mn[a], 1.0e-30);
+      int e = (int)std::ceil(std::log2(ext / 253.0));
+      e = std::max(-120, std::min(120, e));
+      while (std::ldexp(253.0, e) < ext && e < 120) e++;
+      ebits[a] = (uint32_t)(e + 127);
+      scale[a] = std::ldexp(1.0f, e);
+      w.p[a] = nb.mn[a] - scale[a];
+    }
+    uint8_t qlo[3][kWidth], qhi[3][kWidth], meta[kWidth] = {};
+    uint32_t imask = 0;
+    int n_inner = 0, n_tris = 0;
+    for (int s = 0; s < kWidth; s++) {
+      const int i = at_slot[s];
+      if (i < 0) {  // empty: qlo > qhi, no ray enters
+        for (int a = 0; a < 3; a++) {
+          qlo[a][s] = 1;
+          qhi[a][s] = 0;
+        }
         continue;
       }
-      const BNode& c = bn[slots[s]];
-      const Box pb = padded(c.box);
-      g.bmin_x[s] = pb.mn[0];
-      g.bmax_x[s] = pb.mx[0];
-      g.bmin_y[s] = pb.mn[1];
-      g.bmax_y[s] = pb.mx[1];
-      g.bmin_z[s] = pb.mn[2];
-      g.bmax_z[s] = pb.mx[2];
+      for (int a = 0; a < 3; a++) {
+        // outward to the grid plus one step, checked in float arithmetic
+        int lo = (int)std::floor(((double)boxes[i].mn[a] - (double)w.p[a]) / scale[a]) - 1;
+        int hi = (int)std::ceil(((double)boxes[i].mx[a] - (double)w.p[a]) / scale[a]) + 1;
+        lo = std::max(0, std::min(255, lo));
+        hi = std::max(0, std::min(255, hi));
+        while (lo > 0 && w.p[a] + (float)(lo + 1) * scale[a] > boxes[i].mn[a]) lo--;
+        while (hi < 255 && w.p[a] + (float)(hi - 1) * scale[a] < boxes[i].mx[a]) hi++;
+        qlo[a][s] = (uint8_t)lo;
+        qhi[a][s] = (uint8_t)hi;
+      }
+      const BNode& c = bn[ch[i]];
       if (c.left < 0) {
-        uint16_t cnt = 0;
-        g.child[s] = leaf(c, cnt);
-        g.count[s] = cnt;
+        meta[s] = (uint8_t)((((1u << c.count) - 1u) << 5) | (uint32_t)n_tris);
+        n_tris += c.count;
       } else {
-        g.child[s] = emit(slots[s]);
+        imask |= 1u << s;
+        n_inner++;
       }
     }
-    g.axes = at | (al << 2) | (ar << 4);
-    out[idx] = g;
-    return idx;
+    w.e_imask = ebits[0] | ebits[1] << 8 | ebits[2] << 16 | imask << 24;
+    for (int s = 0; s < kWidth; s++) {
+      const int word = s >> 2, sh = 8 * (s & 3);
+      w.meta[word] |= (uint32_t)meta[s] << sh;
+      w.qlo_x[word] |= (uint32_t)qlo[0][s] << sh;
+      w.qlo_y[word] |= (uint32_t)qlo[1][s] << sh;
+      w.qlo_z[word] |= (uint32_t)qlo[2][s] << sh;
+      w.qhi_x[word] |= (uint32_t)qhi[0][s] << sh;
+      w.qhi_y[word] |= (uint32_t)qhi[1][s] << sh;
+      w.qhi_z[word] |= (uint32_t)qhi[2][s] << sh;
+    }
+    // this node's leaf triangles, contiguous in slot order
+    w.tri_base = (int32_t)(otris.size() / 3);
+    for (int s = 0; s < kWidth; s++) {
+      const int i = at_slot[s];
+      if (i < 0 || bn[ch[i]].left >= 0) continue;
+      const BNode& c = bn[ch[i]];
+      for (int t = c.first; t < c.first + c.count; t++) {
+        const int32_t f = tris[t].face;
+        for (int k = 0; k < 3; k++) {
+          const float* v = vertices + 3 * (size_t)faces[3 * (size_t)f + k];
+          float4 q;
+          q.x = v[0];
+          q.y = v[1];
+          q.z = v[2];
+          int32_t wv = (k == 0) ? f : 0;
+          memcpy(&q.w, &wv, 4);
+          otris.push_back(q);
+        }
+      }
+    }
+    // inner children: a contiguous block, then each subtree
+    w.child_base = (int32_t)out.size();
+    out.resize(out.size() + (size_t)n_inner);
+    out[(size_t)idx] = w;
+    int k = 0;
+    for (int s = 0; s < kWidth; s++) {
+      const int i = at_slot[s];
+      if (i < 0 || bn[ch[i]].left < 0) continue;
+      emit(w.child_base + k, ch[i], depth + 1);
+      k++;
+    }
   }
 };
 
 }  // namespace
 
-void build_render_bvh(const float* vertices, const int32_t* faces, int32_t n_faces, std::vector<GNode>& nodes,
-                      std::vector<float4>& tris) {
+int build_render_bvh(const float* vertices, const int32_t* faces, int32_t n_faces, std::vector<WNode>& nodes,
+                     std::vector<float4>& tris) {
   std::vector<Tri> t((size_t)n_faces);
   for (int32_t f = 0; f < n_faces; f++) {
     Tri& q = t[(size_t)f];
@@ -265,7 +364,10 @@ void build_render_bvh(const float* vertices, const int32_t* faces, int32_t n_fac
   b.nodes.reserve(2 * (size_t)n_faces);
   b.build(0, n_faces);
   Emitter e{b.nodes, t, vertices, faces, nodes, tris};
-  e.emit(0);
+  const int root = (int)nodes.size();
+  nodes.emplace_back();
+  e.emit(root, 0, 1);
+  return e.max_depth;
 }
 
 }  // namespace pr

@@ -16,10 +16,24 @@
 // current); make that first call before any stream capture begins.  The
 // scene still comes from pr_scene_upload, which does allocate, at set-up.
 //
+// The address is looked up once per device number and kept: it is the
+// array's address in that device's primary context, the one the CUDA
+// runtime uses.  It is not valid in a context the caller made itself with
+// the driver API, nor after cudaDeviceReset (the array then has a new
+// address that this library does not look up again).
+//
 // All calls share the one array: two calls whose work overlaps on the GPU
 // (different streams or contexts on the same device) race on it and give
 // wrong images.  Each call clears the error word and counters it uses; the
 // partial images are fully overwritten by every call.
+//
+// Sample chunks: pr_render_dev splits each pixel's samples into
+// min(ceil(1.2e6 / pixels), spp) chunks, each summed by its own thread.
+// This entry point keeps that split while the chunks' partial images fit in
+// the array and otherwise uses as many chunks as fit (for example one
+// instead of two at 1024 x 768).  The samples are the same, only the order
+// of the float sums differs, so such images agree with pr_render_dev's to
+// float rounding, not bit for bit.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -59,9 +73,10 @@ extern "C" int pr_render_dev_noalloc(pr_ctx* c, const pr_camera* cam, const pr_r
                                      uint64_t sample_offset, int accumulate) {
   using namespace pr;
   if (!c) return PR_E_ARG;
+  if (!cam || !p) return ctx_fail(c, PR_E_ARG, "null camera or parameters");
   if (!c->scene_ready) return ctx_fail(c, PR_E_SCENE, "no scene uploaded");
   if (!rgb_dev) return ctx_fail(c, PR_E_ARG, "null output");
-  if (!p || p->mode != PR_MODE_MEGAKERNEL)
+  if (p->mode != PR_MODE_MEGAKERNEL)
     return ctx_fail(c, PR_E_UNSUPPORTED, "pr_render_dev_noalloc renders the megakernel form only");
   if (c->cur.kerr.enabled) return ctx_fail(c, PR_E_UNSUPPORTED, "pr_render_dev_noalloc renders straight-ray scenes only");
   RenderCfg g;
@@ -106,6 +121,6 @@ extern "C" int pr_render_dev_noalloc(pr_ctx* c, const pr_camera* cam, const pr_r
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
   c->stats = pr_render_stats{cnt[0], cnt[1], cnt[2], cnt[3], ms, 2};
-  if (bits) return ctx_fail(c, PR_E_DEVICE, "device check fired (error bits " + std::to_string(bits) + ")");
+  if (bits) return ctx_fail(c, PR_E_DEVICE, device_error_message(bits));
   return PR_OK;
 }

@@ -605,7 +605,12 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
       hs.fnorm.insert(hs.fnorm.end(), fn.begin(), fn.end());
       // the render traversal's own tree (same closest hits, fewer tests)
       g.rnode_base = (int32_t)hs.rnodes.size();
-      build_render_bvh(pm_.vertices, pm_.faces, pm_.n_faces, hs.rnodes, hs.rtris);
+      const int rdepth = build_render_bvh(pm_.vertices, pm_.faces, pm_.n_faces, hs.rnodes, hs.rtris);
+      if (rdepth > kWStack) {
+        err = "mesh " + std::to_string(i) + ": render tree of depth " + std::to_string(rdepth) +
+              " exceeds the traversal stack (" + std::to_string(kWStack) + ")";
+        return PR_E_BUILD;
+      }
       hs.mesh_qbvh.push_back(std::move(q));
       hs.mesh_entity.push_back(i);
     } else {

@@ -31,7 +31,7 @@ struct HostScene {
   std::vector<GEntity> ents;
   std::vector<GNode> nodes;
   std::vector<float4> tris;
-  std::vector<GNode> rnodes;   // render-path trees
+  std::vector<WNode> rnodes;   // render-path trees
   std::vector<float4> rtris;
   std::vector<float> fnorm;
   std::vector<int32_t> light_ent;

@@ -1,9 +1,9 @@
 // FP32 closest-hit and any-hit queries used while rendering.
 //
-// QBVH traversal per thread with a small local stack: children ordered near
-// to far by the node's split axes and the ray signs (the reference's own
-// ordering, QBVH.cpp:80-100, popped nearest-first), each child box culled
-// against the current closest hit, leaves tested as soon as they are met.
+// Traversal of the render path's compressed 8-wide trees (WNode) per thread
+// with a small local stack of node groups: children visited near to far by
+// their octant slots, each child box culled against the current closest hit,
+// leaves tested as soon as their node is visited.
 // Spheres keep the reference's FP64 test (its 1e5-radius walls cancel
 // catastrophically in FP32); planes and triangles are FP32.
 #pragma once
@@ -46,98 +46,169 @@ __device__ __forceinline__ bool fast_tri(const float4* __restrict__ T, float3 o,
   return true;
 }
 
-// 4-wide slab test; returns a mask of children whose box overlaps [0, tmax)
-// and their entry distances.
-__device__ __forceinline__ int box4(const GNode* __restrict__ node, float3 inv, float3 oinv, float tmax, float tn[4]) {
-  const float4* n4 = reinterpret_cast<const float4*>(node);
-  const float4 mnx = __ldg(n4 + 0), mxx = __ldg(n4 + 1), mny = __ldg(n4 + 2), mxy = __ldg(n4 + 3);
-  const float4 mnz = __ldg(n4 + 4), mxz = __ldg(n4 + 5);
-  const float a0[4] = {mnx.x, mnx.y, mnx.z, mnx.w}, a1[4] = {mxx.x, mxx.y, mxx.z, mxx.w};
-  const float b0[4] = {mny.x, mny.y, mny.z, mny.w}, b1[4] = {mxy.x, mxy.y, mxy.z, mxy.w};
-  const float c0[4] = {mnz.x, mnz.y, mnz.z, mnz.w}, c1[4] = {mxz.x, mxz.y, mxz.z, mxz.w};
-  int mask = 0;
-#pragma unroll
-  for (int c = 0; c < 4; c++) {
-    const float tx0 = fmaf(a0[c], inv.x, -oinv.x), tx1 = fmaf(a1[c], inv.x, -oinv.x);
-    const float ty0 = fmaf(b0[c], inv.y, -oinv.y), ty1 = fmaf(b1[c], inv.y, -oinv.y);
-    const float tz0 = fmaf(c0[c], inv.z, -oinv.z), tz1 = fmaf(c1[c], inv.z, -oinv.z);
-    const float tnear = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
-    const float tfar = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
-    tn[c] = tnear;
-    mask |= (tnear <= tfar) ? (1 << c) : 0;
-  }
-  return mask;
+// Ray data of the wide traversal
+struct WRay {
+  float3 o, d, inv;
+  int oct;  // sign bits of d (bit a: negative along axis a)
+};
+
+__device__ __forceinline__ float3 safe_inv(float3 d) {
+  const float big = 1.0e30f;
+  return f3(d.x != 0.0f ? 1.0f / d.x : copysignf(big, d.x), d.y != 0.0f ? 1.0f / d.y : copysignf(big, d.y),
+            d.z != 0.0f ? 1.0f / d.z : copysignf(big, d.z));
 }
 
-// QBVH closest hit (ANY = false) or any hit below tmax (ANY = true).
+__device__ __forceinline__ WRay make_wray(float3 o, float3 d) {
+  WRay r;
+  r.o = o;
+  r.d = d;
+  r.inv = safe_inv(d);
+  r.oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
+  return r;
+}
+
+// byte k of w as the float 2^23 + byte (bit pattern 0x4B0000qq), exact
+__device__ __forceinline__ float qbyte_biased(uint32_t w, int k) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)k));
+}
+
+// three-input minimum / maximum (one instruction on sm_100 and later)
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+// bit i of m moves to bit i ^ x (x in 0..7)
+__device__ __forceinline__ uint32_t permute_xor8(uint32_t m, int x) {
+  if (x & 1) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+  if (x & 2) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+  if (x & 4) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+  return m;
+}
+
+// Node group of the wide traversal: the node index of the first inner child,
+// the node's inner-child mask and the not yet visited inner children that the
+// ray hit, in traversal order (bit i: slot i ^ oct)
+struct WGroup {
+  int base;
+  uint32_t bits;  // hits | imask << 8
+};
+
+// One wide node against the ray (slab test of its eight quantised child
+// boxes against [0, tmax)): the group of its hit inner children and the
+// mask of its hit leaves' triangles (bit k: triangle slot tri_base + k).
+__device__ __forceinline__ void wnode_visit(const WNode* __restrict__ n, const WRay& r, float tmax, WGroup& g,
+                                            uint32_t& tri_mask, int& tri_base) {
+  const float4 a = __ldg(reinterpret_cast<const float4*>(n));
+  const int4 b = __ldg(reinterpret_cast<const int4*>(n) + 1);
+  const uint4 c = __ldg(reinterpret_cast<const uint4*>(n) + 2);  // qlo_x, qlo_y
+  const uint4 d = __ldg(reinterpret_cast<const uint4*>(n) + 3);  // qlo_z, qhi_x
+  const uint4 e = __ldg(reinterpret_cast<const uint4*>(n) + 4);  // qhi_y, qhi_z
+  const uint32_t em = __float_as_uint(a.w);
+  // plane q of axis x at distance (p + q 2^e - o) / d = q sx + bx; the bytes
+  // come biased by 2^23, folded into bx (one rounding, at most half a grid
+  // step: the builder leaves a full step of margin around every child box)
+  const float sx = __uint_as_float((em & 0xFFu) << 23) * r.inv.x;
+  const float sy = __uint_as_float(((em >> 8) & 0xFFu) << 23) * r.inv.y;
+  const float sz = __uint_as_float(((em >> 16) & 0xFFu) << 23) * r.inv.z;
+  const float bx = fmaf(-8388608.0f, sx, (a.x - r.o.x) * r.inv.x);
+  const float by = fmaf(-8388608.0f, sy, (a.y - r.o.y) * r.inv.y);
+  const float bz = fmaf(-8388608.0f, sz, (a.z - r.o.z) * r.inv.z);
+  // near and far planes per axis: the low planes are near for a positive direction
+  const bool nx = r.oct & 1, ny = r.oct & 2, nz = r.oct & 4;
+  const uint32_t nx0 = nx ? d.z : c.x, nx1 = nx ? d.w : c.y, fx0 = nx ? c.x : d.z, fx1 = nx ? c.y : d.w;
+  const uint32_t ny0 = ny ? e.x : c.z, ny1 = ny ? e.y : c.w, fy0 = ny ? c.z : e.x, fy1 = ny ? c.w : e.y;
+  const uint32_t nz0 = nz ? e.z : d.x, nz1 = nz ? e.w : d.y, fz0 = nz ? d.x : e.z, fz1 = nz ? d.y : e.w;
+  uint32_t hits = 0;
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    const int k = s & 3;
+    const float tnx = fmaf(qbyte_biased(s < 4 ? nx0 : nx1, k), sx, bx);
+    const float tfx = fmaf(qbyte_biased(s < 4 ? fx0 : fx1, k), sx, bx);
+    const float tny = fmaf(qbyte_biased(s < 4 ? ny0 : ny1, k), sy, by);
+    const float tfy = fmaf(qbyte_biased(s < 4 ? fy0 : fy1, k), sy, by);
+    const float tnz = fmaf(qbyte_biased(s < 4 ? nz0 : nz1, k), sz, bz);
+    const float tfz = fmaf(qbyte_biased(s < 4 ? fz0 : fz1, k), sz, bz);
+    const float tn = fmax3(tnx, tny, fmaxf(tnz, 0.0f));
+    const float tf = fmin3(tfx, tfy, fminf(tfz, tmax));
+    hits |= (tn <= tf) ? (1u << s) : 0u;
+  }
+  const uint32_t imask = em >> 24;
+  uint32_t tm = 0;
+  if (hits & ~imask) {
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      const uint32_t m = ((s < 4 ? (uint32_t)b.z : (uint32_t)b.w) >> (8 * (s & 3))) & 0xFFu;
+      tm |= ((hits >> s) & 1u) ? ((m >> 5) << (m & 31u)) : 0u;
+    }
+  }
+  g.base = b.x;
+  g.bits = permute_xor8(hits & imask, r.oct) | imask << 8;
+  tri_mask = tm;
+  tri_base = b.y;
+}
+
+// the next child of a group (its lowest pending hit); clears it
+__device__ __forceinline__ int wgroup_next(WGroup& g, int oct) {
+  const int i = __ffs(g.bits & 0xFFu) - 1;
+  g.bits &= ~(1u << i);
+  const int s = i ^ oct;
+  return g.base + __popc((g.bits >> 8) & ((1u << s) - 1u));
+}
+
+// the root of a mesh as a group with one pending child
+__device__ __forceinline__ WGroup wgroup_root(int root, int oct) {
+  WGroup g;
+  g.base = root;
+  g.bits = (1u << oct) | (1u << 8);  // pending bit oct is slot 0, the only inner child
+  return g;
+}
+
+// Wide-BVH closest hit (ANY = false) or any hit below tmax (ANY = true):
+// children are visited near to far by the slot order, each node's leaf
+// triangles tested as soon as the node is visited.
 template <bool ANY>
-__device__ __forceinline__ bool fast_qbvh(const DevScene& S, const GEntF& e, float3 o, float3 d, float3 inv, float& tbest,
-                                          int& slot, float& bu, float& bv, TraceStats& st, uint32_t* err) {
-  int32_t stack[kStackSize];
+__device__ __forceinline__ bool fast_qbvh(const DevScene& S, const GEntF& e, const WRay& r, float& tbest, int& slot,
+                                          float& bu, float& bv, TraceStats& st, uint32_t* err) {
+  WGroup stack[kWStack];
   int sp = 0;
-  stack[sp++] = e.node_base;
-  const float3 oinv = o * inv;
-  const int sx = d.x >= 0.0f ? 0 : 1, sy = d.y >= 0.0f ? 0 : 1, sz = d.z >= 0.0f ? 0 : 1;
+  WGroup g = wgroup_root(e.node_base, r.oct);
   bool hit = false;
   int guard = 0;
-  while (sp > 0) {
+  while (true) {
+    if ((g.bits & 0xFFu) == 0) {
+      if (sp == 0) break;
+      g = stack[--sp];
+    }
     if (++guard > (1 << 22)) { atomicOr(err, PR_DEV_LOOP_CAP); break; }
-    const int32_t ni = stack[--sp];
-    const GNode* node = S.rnodes + ni;
+    const int child = wgroup_next(g, r.oct);
+    if (g.bits & 0xFFu) {
+      if (sp >= kWStack) { atomicOr(err, PR_DEV_STACK_OVERFLOW); return hit; }
+      stack[sp++] = g;
+    }
     st.nodes++;
-    float tn[4];
-    const int mask = box4(node, inv, oinv, tbest, tn);
-    if (!mask) continue;
-    const int4 ch = __ldg(reinterpret_cast<const int4*>(node) + 6);
-    const int4 meta = __ldg(reinterpret_cast<const int4*>(node) + 7);
-    const int axes = meta.x;
-    const int child[4] = {ch.x, ch.y, ch.z, ch.w};
-    const int cnt[4] = {meta.y & 0xFFFF, (int)((uint32_t)meta.y >> 16), meta.z & 0xFFFF, (int)((uint32_t)meta.z >> 16)};
-    const int sg[3] = {sx, sy, sz};
-    const int at = axes & 3, al = (axes >> 2) & 3, ar = (axes >> 4) & 3;
-    int order[4];
-    const int lf = (sg[at] == 0) ? 0 : 2, rf = (lf + 2) & 3;
-    if (sg[al] == 0) { order[lf] = 0; order[lf + 1] = 1; } else { order[lf] = 1; order[lf + 1] = 0; }
-    if (sg[ar] == 0) { order[rf] = 2; order[rf + 1] = 3; } else { order[rf] = 3; order[rf + 1] = 2; }
-    // leaves near to far now, inner nodes pushed far to near.  The leaf
-    // triangles are gathered into one run first, so that all lanes of a warp
-    // test their triangles in the same loop (one code path, not one per
-    // child position)
-    int lfirst[4], lcnt[4];
-    float ltn[4];
-    int nl = 0;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-      const int c = order[i];
-      if (!((mask >> c) & 1) || child[c] == kChildInvalid || child[c] >= 0) continue;
-      lfirst[nl] = (int32_t)((uint32_t)child[c] & ~kLeafBit);
-      lcnt[nl] = cnt[c];
-      ltn[nl] = tn[c];
-      nl++;
-    }
-    for (int l = 0; l < nl; l++) {
-      if (ltn[l] > tbest) continue;
-      const int32_t first = lfirst[l];
-      for (int k = 0; k < lcnt[l]; k++) {
-        st.tris++;
-        float t, uu, vv;
-        if (fast_tri(S.rtris + 3 * (size_t)(first + k), o, d, tbest, t, uu, vv)) {
-          tbest = t;
-          slot = first + k;
-          bu = uu;
-          bv = vv;
-          hit = true;
-          if (ANY) return true;
-        }
+    uint32_t tm;
+    int tb;
+    wnode_visit(S.rnodes + child, r, tbest, g, tm, tb);
+    while (tm) {
+      const int k = __ffs(tm) - 1;
+      tm &= tm - 1u;
+      st.tris++;
+      float t, uu, vv;
+      if (fast_tri(S.rtris + 3 * (size_t)(tb + k), r.o, r.d, tbest, t, uu, vv)) {
+        tbest = t;
+        slot = tb + k;
+        bu = uu;
+        bv = vv;
+        hit = true;
+        if (ANY) return true;
       }
-    }
-#pragma unroll
-    for (int i = 3; i >= 0; i--) {
-      const int c = order[i];
-      if (!((mask >> c) & 1) || child[c] < 0) continue;
-      if (tn[c] > tbest) continue;
-      if (sp >= kStackSize) { atomicOr(err, PR_DEV_STACK_OVERFLOW); return hit; }
-      stack[sp++] = child[c];
     }
   }
   return hit;
@@ -203,12 +274,6 @@ __device__ __forceinline__ bool fast_circle(const GEntF& e, float3 o, float3 d, 
   return true;
 }
 
-__device__ __forceinline__ float3 safe_inv(float3 d) {
-  const float big = 1.0e30f;
-  return f3(d.x != 0.0f ? 1.0f / d.x : copysignf(big, d.x), d.y != 0.0f ? 1.0f / d.y : copysignf(big, d.y),
-            d.z != 0.0f ? 1.0f / d.z : copysignf(big, d.z));
-}
-
 // closest hit over the entity list (strict '<' in list order)
 __device__ __forceinline__ bool fast_closest(const DevScene& S, float3 o, float3 d, FastHit& h, TraceStats& st,
                                              uint32_t* err) {
@@ -216,7 +281,7 @@ __device__ __forceinline__ bool fast_closest(const DevScene& S, float3 o, float3
   h.ent = -1;
   h.slot = -1;
   h.u = h.v = 0.0f;
-  const float3 inv = safe_inv(d);
+  const WRay r = make_wray(o, d);
   for (int i = 0; i < S.n_ents; i++) {
     const GEntF& e = S.entf[i];
     float t = h.t, bu = 0.0f, bv = 0.0f;
@@ -225,7 +290,7 @@ __device__ __forceinline__ bool fast_closest(const DevScene& S, float3 o, float3
     if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], o, d, h.t, t, bu);
     else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, o, d, h.t, t);
     else if (e.type == PR_ENT_CIRCLE) got = fast_circle(e, o, d, h.t, t);
-    else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<false>(S, e, o, d, inv, t, slot, bu, bv, st, err);
+    else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<false>(S, e, r, t, slot, bu, bv, st, err);
     if (got && t < h.t) {
       h.t = t;
       h.ent = i;
@@ -240,7 +305,7 @@ __device__ __forceinline__ bool fast_closest(const DevScene& S, float3 o, float3
 // any hit with t < tmax
 __device__ __forceinline__ bool fast_occluded(const DevScene& S, float3 o, float3 d, float tmax, TraceStats& st,
                                               uint32_t* err) {
-  const float3 inv = safe_inv(d);
+  const WRay r = make_wray(o, d);
   for (int i = 0; i < S.n_ents; i++) {
     const GEntF& e = S.entf[i];
     float t = tmax, bu, bv;
@@ -249,7 +314,7 @@ __device__ __forceinline__ bool fast_occluded(const DevScene& S, float3 o, float
     if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], o, d, tmax, t, bu);
     else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, o, d, tmax, t);
     else if (e.type == PR_ENT_CIRCLE) got = fast_circle(e, o, d, tmax, t);
-    else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<true>(S, e, o, d, inv, t, slot, bu, bv, st, err);
+    else if (e.type == PR_ENT_POLYGON) got = fast_qbvh<true>(S, e, r, t, slot, bu, bv, st, err);
     if (got) return true;
   }
   return false;

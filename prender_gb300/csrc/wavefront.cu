@@ -168,12 +168,14 @@ __global__ void __launch_bounds__(128, 6) wf_shade() {
   for (unsigned int base = blockIdx.x * blockDim.x; base < B.n_slots; base += stride) {
     const unsigned int i = base + threadIdx.x;
     int state = SLOT_FREE;
+    bool was_free = true;  // free before this iteration (its record already says so)
     PathState ps;
     uint64_t g = 0;
     bool has_ray = false;
     int n_shadow = 0;
     if (i < B.n_slots) {
       state = __float_as_int(B.d[i].w) >> 1;
+      was_free = state == SLOT_FREE;
       if (state == SLOT_HIT) {
         load_state(B, i, ps);
         g = B.sample[i];
@@ -264,7 +266,7 @@ __global__ void __launch_bounds__(128, 6) wf_shade() {
       if (has_ray) {
         store_state(B, i, ps, SLOT_RAY);
         B.sample[i] = g;
-      } else if (state == SLOT_FREE) {
+      } else if (!was_free) {  // its path ended and nothing refilled it
         B.d[i] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(SLOT_FREE << 1));
       }
     }
@@ -291,23 +293,23 @@ constexpr int kRefillLanes = 16;
 constexpr unsigned int kWarpStepCap = 1u << 26;
 
 struct TraceLane {
-  float3 o, d, inv, oinv;
+  WRay ray;
   float tmax;        // current closest (closest hit) or the ray's limit (any hit)
-  int sg;            // ray direction signs, bit per axis
-  int ent;           // next entity of the list to test
-  int sp;            // traversal stack depth of the current mesh (0: between entities)
+  int ent;           // next entity of the list to test (the current mesh while in_mesh)
+  int sp;            // node groups on the traversal stack
+  bool in_mesh;      // inside the traversal of mesh 'ent'
+  WGroup g;          // the current node group
   FastHit h;
 };
 
 __device__ __forceinline__ void lane_start(TraceLane& r, float3 o, float3 d, float tmax) {
-  r.o = o;
-  r.d = d;
-  r.inv = safe_inv(d);
-  r.oinv = o * r.inv;
+  r.ray = make_wray(o, d);
   r.tmax = tmax;
-  r.sg = (d.x >= 0.0f ? 0 : 1) | (d.y >= 0.0f ? 0 : 2) | (d.z >= 0.0f ? 0 : 4);
   r.ent = 0;
   r.sp = 0;
+  r.in_mesh = false;
+  r.g.base = 0;
+  r.g.bits = 0;
   r.h.t = tmax;
   r.h.ent = -1;
   r.h.slot = -1;
@@ -317,23 +319,24 @@ __device__ __forceinline__ void lane_start(TraceLane& r, float3 o, float3 d, flo
 // one step of a ray; returns true when the ray is done (ANY: r.h.ent >= 0
 // means occluded)
 template <bool ANY>
-__device__ __forceinline__ bool lane_step(const DevScene& S, TraceLane& r, int32_t* stack, TraceStats& st,
+__device__ __forceinline__ bool lane_step(const DevScene& S, TraceLane& r, WGroup* stack, TraceStats& st,
                                           uint32_t* err) {
-  if (r.sp == 0) {
+  if (!r.in_mesh) {
     // non-mesh entities up to the next mesh, in list order
     while (r.ent < S.n_ents) {
       const int i = r.ent;
       const GEntF& e = S.entf[i];
       if (e.type == PR_ENT_POLYGON) {
-        stack[0] = e.node_base;
-        r.sp = 1;
+        r.g = wgroup_root(e.node_base, r.ray.oct);
+        r.sp = 0;
+        r.in_mesh = true;
         break;
       }
       float t = r.tmax, rest = 0.0f;
       bool got = false;
-      if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], r.o, r.d, r.tmax, t, rest);
-      else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, r.o, r.d, r.tmax, t);
-      else if (e.type == PR_ENT_CIRCLE) got = fast_circle(e, r.o, r.d, r.tmax, t);
+      if (e.type == PR_ENT_SPHERE) got = fast_sphere(S.ents[i], r.ray.o, r.ray.d, r.tmax, t, rest);
+      else if (e.type == PR_ENT_UVPLANE) got = fast_uvplane(e, r.ray.o, r.ray.d, r.tmax, t);
+      else if (e.type == PR_ENT_CIRCLE) got = fast_circle(e, r.ray.o, r.ray.d, r.tmax, t);
       r.ent++;
       if (ANY && got) {  // the test itself keeps t below the limit
         r.h.ent = i;
@@ -348,70 +351,42 @@ __device__ __forceinline__ bool lane_step(const DevScene& S, TraceLane& r, int32
         r.h.t = t;
       }
     }
-    return r.sp == 0;  // past the last entity
+    return !r.in_mesh;  // past the last entity
   }
-  // one node of the current mesh (fast_qbvh's loop body)
-  const int32_t ni = stack[--r.sp];
-  const GNode* node = S.rnodes + ni;
+  // one node of the current mesh with its leaf triangles (fast_qbvh's loop body)
+  if ((r.g.bits & 0xFFu) == 0) r.g = stack[--r.sp];  // stacked groups always hold a pending child
+  const int child = wgroup_next(r.g, r.ray.oct);
+  if (r.g.bits & 0xFFu) {
+    if (r.sp >= kWStack) {
+      atomicOr(err, PR_DEV_STACK_OVERFLOW);
+      r.in_mesh = false;
+      r.ent = S.n_ents;
+      return true;
+    }
+    stack[r.sp++] = r.g;
+  }
   st.nodes++;
-  float tn[4];
-  const int mask = box4(node, r.inv, r.oinv, r.tmax, tn);
-  if (mask) {
-    const int4 ch = __ldg(reinterpret_cast<const int4*>(node) + 6);
-    const int4 meta = __ldg(reinterpret_cast<const int4*>(node) + 7);
-    const int axes = meta.x;
-    const int child[4] = {ch.x, ch.y, ch.z, ch.w};
-    const int cnt[4] = {meta.y & 0xFFFF, (int)((uint32_t)meta.y >> 16), meta.z & 0xFFFF, (int)((uint32_t)meta.z >> 16)};
-    const int at = axes & 3, al = (axes >> 2) & 3, ar = (axes >> 4) & 3;
-    int order[4];
-    const int lf = ((r.sg >> at) & 1) == 0 ? 0 : 2, rf = (lf + 2) & 3;
-    if (((r.sg >> al) & 1) == 0) { order[lf] = 0; order[lf + 1] = 1; } else { order[lf] = 1; order[lf + 1] = 0; }
-    if (((r.sg >> ar) & 1) == 0) { order[rf] = 2; order[rf + 1] = 3; } else { order[rf] = 3; order[rf + 1] = 2; }
-    int lfirst[4], lcnt[4];
-    float ltn[4];
-    int nl = 0;
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const int c = order[q];
-      if (!((mask >> c) & 1) || child[c] == kChildInvalid || child[c] >= 0) continue;
-      lfirst[nl] = (int32_t)((uint32_t)child[c] & ~kLeafBit);
-      lcnt[nl] = cnt[c];
-      ltn[nl] = tn[c];
-      nl++;
-    }
-    for (int l = 0; l < nl; l++) {
-      if (ltn[l] > r.tmax) continue;
-      const int32_t first = lfirst[l];
-      for (int k = 0; k < lcnt[l]; k++) {
-        st.tris++;
-        float t, uu, vv;
-        if (fast_tri(S.rtris + 3 * (size_t)(first + k), r.o, r.d, r.tmax, t, uu, vv)) {
-          r.h.ent = r.ent;
-          r.h.slot = first + k;
-          if (ANY) return true;
-          r.tmax = t;
-          r.h.t = t;
-          r.h.u = uu;
-          r.h.v = vv;
-        }
-      }
-    }
-#pragma unroll
-    for (int q = 3; q >= 0; q--) {
-      const int c = order[q];
-      if (!((mask >> c) & 1) || child[c] < 0) continue;
-      if (tn[c] > r.tmax) continue;
-      if (r.sp >= kStackSize) {
-        atomicOr(err, PR_DEV_STACK_OVERFLOW);
-        r.sp = 0;
-        r.ent = S.n_ents;
-        return true;
-      }
-      stack[r.sp++] = child[c];
+  uint32_t tm;
+  int tb;
+  wnode_visit(S.rnodes + child, r.ray, r.tmax, r.g, tm, tb);
+  while (tm) {
+    const int k = __ffs(tm) - 1;
+    tm &= tm - 1u;
+    st.tris++;
+    float t, uu, vv;
+    if (fast_tri(S.rtris + 3 * (size_t)(tb + k), r.ray.o, r.ray.d, r.tmax, t, uu, vv)) {
+      r.h.ent = r.ent;
+      r.h.slot = tb + k;
+      if (ANY) return true;
+      r.tmax = t;
+      r.h.t = t;
+      r.h.u = uu;
+      r.h.v = vv;
     }
   }
-  if (r.sp == 0) {
-    r.ent++;  // this mesh is done
+  if ((r.g.bits & 0xFFu) == 0 && r.sp == 0) {
+    r.in_mesh = false;  // this mesh is done
+    r.ent++;
     return r.ent >= S.n_ents;
   }
   return false;
@@ -425,7 +400,7 @@ __device__ __forceinline__ void persistent_trace(const DevScene& S, unsigned int
                                                  uint32_t* err) {
   const int lane = threadIdx.x & 31;
   TraceLane r;
-  int32_t stack[kStackSize];
+  WGroup stack[kWStack];
   bool busy = false, exhausted = false;
   for (unsigned int step = 0;; step++) {
     const unsigned int idle = __ballot_sync(0xffffffffu, !busy && !exhausted);

@@ -145,7 +145,7 @@ class Context:
 
     def autotune(self, scene=None, settings=None, camera=None) -> dict:
         """Picks the wavefront pool size and traversal grid for this context
-        by timing one-sample frames (pr_autotune_wavefront)."""
+        by timing short frames of the scene (pr_autotune_wavefront)."""
         scene = scene or self.scene
         cam = (camera or scene.camera).to_c()
         prm = (settings or scene.settings).to_c()

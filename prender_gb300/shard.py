@@ -17,10 +17,22 @@ import numpy as np
 
 
 def shard(rank: int, world: int, spp: int):
-    """(sample_offset, total_spp) of rank's shard of a frame of world * spp samples."""
+    """(sample_offset, total_spp) of rank's shard of a frame of world * spp samples.
+
+    spp counts camera samples per pixel as the renderer draws them:
+    samples * supersamples^2 of pr_render_params (Render::Run folds the
+    supersampling grid and the tent filter into the sample count,
+    render.h:1133-1138) -- not the 'samples' field alone.  shard_settings()
+    derives it from the render parameters."""
     if not (0 <= rank < world) or spp <= 0:
         raise ValueError("bad shard")
     return rank * spp, world * spp
+
+
+def shard_settings(rank: int, world: int, settings):
+    """(sample_offset, total_spp) of rank's shard when every rank renders with
+    these RenderSettings (its samples * supersamples^2 camera samples per pixel)."""
+    return shard(rank, world, settings.samples * settings.supersamples * settings.supersamples)
 
 
 def render_sharded(render: Callable[[int, int], np.ndarray], spp: int, group=None) -> np.ndarray:

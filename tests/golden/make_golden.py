@@ -248,6 +248,72 @@ def sss_oracle_golden(nb=16, level=-2):
     print("sss oracle batches", nb, "level", level)
 
 
+def media_golden(d):
+    """participating-media renders by the reference, one thread (bit-exact),
+    and per-ray radiance() roots, over the media cases' sigma_s, g and NEE"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import media_cases
+    out = {}
+    for name, sc in media_cases.one_thread_cases().items():
+        dd = os.path.join(d, "m_" + name)
+        os.makedirs(dd)
+        img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+        out[f"render_{name}"] = img
+        print("media", name, info)
+    for name, sc in media_cases.root_cases().items():
+        dd = os.path.join(d, "mr_" + name)
+        os.makedirs(dd)
+        r = scenes.camera_rays(sc)
+        out[f"roots_{name}_rays"] = r
+        out[f"roots_{name}_rgb"] = ref_radiance(sc.write_reference(dd), r, 7, dd)
+    np.savez_compressed(os.path.join(HERE, "media_render.npz"), **out)
+
+
+def media_oracle_golden(nb=16):
+    """16 independent 256-spp renders of each media case by the oracle
+    (pinned bit-exact to the reference by media_render.npz; its HG-correct
+    sampler by the HG distribution): per-pixel mean and spread"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import media_cases
+    from oracle import oracle as O
+    out = {}
+    for name in media_cases.CASES:
+        sc = media_cases.highspp_case(name)
+        imgs = []
+        for k in range(nb):
+            sc.settings.seed = 100 + k
+            img, _, _ = O.OracleScene(sc).render(threads=os.cpu_count())
+            imgs.append(img)
+        b = np.stack(imgs)
+        out[f"{name}_mean"] = b.mean(0).astype(np.float32)
+        out[f"{name}_sd"] = b.std(0, ddof=1).astype(np.float32)
+        print("media oracle", name, float(b.mean()))
+    out["batches"] = np.int32(nb)
+    np.savez_compressed(os.path.join(HERE, "media_oracle.npz"), **out)
+
+
+def mesh7_oracle_golden(nb=16):
+    """The benchmarked scene itself (327,680-triangle displaced icosphere,
+    diffuse and glass) at 128 x 96, 16 independent 256-spp renders by the
+    oracle: per-pixel mean and spread"""
+    from oracle import oracle as O
+    out = {}
+    for mat in ("diffuse", "glass"):
+        sc = scenes.mesh_cornell(width=128, height=96, samples=64, supersamples=2, subdiv=7, material=mat)
+        o = O.OracleScene(sc)
+        imgs = []
+        for k in range(nb):
+            sc.settings.seed = 100 + k
+            img, _, _ = o.render(threads=os.cpu_count(), settings=sc.settings)
+            imgs.append(img)
+        b = np.stack(imgs)
+        out[f"{mat}_mean"] = b.mean(0).astype(np.float32)
+        out[f"{mat}_sd"] = b.std(0, ddof=1).astype(np.float32)
+        print("mesh subdiv 7 oracle", mat, float(b.mean()))
+    out["batches"] = np.int32(nb)
+    np.savez_compressed(os.path.join(HERE, "mesh7_oracle.npz"), **out)
+
+
 SCENE_DIR = os.path.join(HERE, "scene_files")
 SCENE_FILES = ("spheres_expr", "mesh_obj", "media", "sss", "kerr_disk")
 
@@ -347,13 +413,20 @@ def _image_size(path):
 
 
 KNOWN_FLAGS = {"--kerr-only", "--disk-only", "--sss-only", "--sss-l1-only", "--glossy-only", "--sss-oracle",
-               "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle", "--scene-files-only"}
+               "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle", "--scene-files-only", "--media-only",
+               "--media-oracle", "--mesh7-oracle"}
 
 
 def main():
     bad = [a for a in sys.argv[1:] if a.startswith("--") and a not in KNOWN_FLAGS]
     if bad:
         sys.exit(f"unknown option(s) {bad}; known: {sorted(KNOWN_FLAGS)}")
+    if "--media-oracle" in sys.argv:
+        media_oracle_golden()
+        return
+    if "--mesh7-oracle" in sys.argv:
+        mesh7_oracle_golden()
+        return
     if "--sss-oracle" in sys.argv:
         sss_oracle_golden()
         return
@@ -377,6 +450,10 @@ def main():
     if "--kerr-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             kerr_golden(d)
+        return
+    if "--media-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            media_golden(d)
         return
     if "--disk-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:

@@ -328,3 +328,33 @@ def test_glossy_materials_are_refused_by_the_adjoint(ctx):
     ctx.upload(s)
     with pytest.raises(gpu.PrenderError):
         ctx.render_adjoint(np.ones((12, 16, 3), np.float32), s)
+
+
+@pytest.mark.parametrize("mode", [A.PR_MODE_MEGAKERNEL, A.PR_MODE_WAVEFRONT])
+@pytest.mark.parametrize("mat", ["diffuse", "glass"])
+def test_benchmarked_scene_matches_oracle_statistically(ctx, golden, mat, mode):
+    """The benchmarked frame's scene itself -- 12-triangle box, area light,
+    327,680-triangle displaced icosphere, diffuse or glass -- at 128 x 96,
+    16 x 256 spp, in both forms, against the oracle's 16 x 256 spp (the
+    oracle renders through the reference's own QBVH of this mesh)."""
+    s = scenes.mesh_cornell(width=128, height=96, samples=64, supersamples=2, subdiv=7, material=mat)
+    s.settings.mode = mode
+    ctx.upload(s)
+    nb, spp = 16, s.settings.spp
+    b = _batches(ctx, s, nb, spp)
+    mean = b.mean(0)
+    sd = b.std(0, ddof=1)
+    orc = golden["mesh7_oracle"]
+    o_mean = orc[f"{mat}_mean"].astype(np.float64)
+    o_sd = orc[f"{mat}_sd"].astype(np.float64)
+    o_nb = int(orc["batches"])
+    sigma = np.sqrt(sd ** 2 / nb + o_sd ** 2 / o_nb) + 1e-6
+    frac = float((np.abs(mean - o_mean) / sigma > 3.0).mean())
+    rmse = float(np.sqrt(((mean - o_mean) ** 2).mean()))
+    noise = float(np.sqrt((sigma ** 2).mean()))
+    rel = abs(mean.mean() - o_mean.mean()) / o_mean.mean()
+    print(f"subdiv-7 {mat} mode {mode}: >3 sigma {frac:.4f}, rmse {rmse:.3e} vs noise {noise:.3e}, "
+          f"mean rel diff {rel:.4f}")
+    assert rel < 0.01
+    assert frac < 0.02
+    assert rmse < 1.3 * noise

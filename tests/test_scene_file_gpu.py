@@ -41,7 +41,7 @@ def test_scene_file_closest_hits_bit_exact(ctx, name):
     assert np.array_equal(h["t"], o["t"])
 
 
-@pytest.mark.parametrize("name", ["spheres_expr", "mesh_obj", "sss"])
+@pytest.mark.parametrize("name", ["spheres_expr", "mesh_obj", "media", "sss"])
 def test_scene_file_render_matches_oracle_statistically(ctx, name):
     # 16 independent 1024-spp GPU frames against one 1024-spp oracle frame:
     # the GPU mean carries sd / 4, the oracle frame sd, where sd is the

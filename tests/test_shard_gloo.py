@@ -44,6 +44,10 @@ def test_shard_ranges():
     assert shard.shard(1, 2, 16) == (16, 32)
     with pytest.raises(ValueError):
         shard.shard(2, 2, 16)
+    # samples 4 on a 2x2 supersampling grid are 16 camera samples per pixel
+    from prender_gb300.scene import RenderSettings
+    st = RenderSettings(samples=4, supersamples=2)
+    assert shard.shard_settings(1, 2, st) == (16, 32)
 
 
 def test_two_gloo_ranks_equal_one_process():
