@@ -259,8 +259,7 @@ struct Emitter {
     WNode w;
     memset(&w, 0, sizeof(w));
     // grid of spacing 2^e >= extent / 253 with its origin one step below the
-    // node's padded minimum: every child box keeps a full step of margin on
-    // each side (the traversal's plane distances may be off by half a step)
+    // node's padded minimum
     uint32_t ebits[3];
     float scale[3];
     for (int a = 0; a < 3; a++) {
@@ -285,13 +284,13 @@ struct Emitter {
         continue;
       }
       for (int a = 0; a < 3; a++) {
-        // outward to the grid plus one step, checked in float arithmetic
-        int lo = (int)std::floor(((double)boxes[i].mn[a] - (double)w.p[a]) / scale[a]) - 1;
-        int hi = (int)std::ceil(((double)boxes[i].mx[a] - (double)w.p[a]) / scale[a]) + 1;
+        // outward to the grid, checked in float arithmetic
+        int lo = (int)std::floor(((double)boxes[i].mn[a] - (double)w.p[a]) / scale[a]);
+        int hi = (int)std::ceil(((double)boxes[i].mx[a] - (double)w.p[a]) / scale[a]);
         lo = std::max(0, std::min(255, lo));
         hi = std::max(0, std::min(255, hi));
-        while (lo > 0 && w.p[a] + (float)(lo + 1) * scale[a] > boxes[i].mn[a]) lo--;
-        while (hi < 255 && w.p[a] + (float)(hi - 1) * scale[a] < boxes[i].mx[a]) hi++;
+        while (lo > 0 && w.p[a] + (float)lo * scale[a] > boxes[i].mn[a]) lo--;
+        while (hi < 255 && w.p[a] + (float)hi * scale[a] < boxes[i].mx[a]) hi++;
         qlo[a][s] = (uint8_t)lo;
         qhi[a][s] = (uint8_t)hi;
       }

@@ -67,9 +67,9 @@ __device__ __forceinline__ WRay make_wray(float3 o, float3 d) {
   return r;
 }
 
-// byte k of w as the float 2^23 + byte (bit pattern 0x4B0000qq), exact
-__device__ __forceinline__ float qbyte_biased(uint32_t w, int k) {
-  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)k));
+// byte k of w as an exact float (0x4B0000qq is 2^23 + qq)
+__device__ __forceinline__ float qbyte(uint32_t w, int k) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)k)) - 8388608.0f;
 }
 
 // three-input minimum / maximum (one instruction on sm_100 and later)
@@ -111,15 +111,16 @@ __device__ __forceinline__ void wnode_visit(const WNode* __restrict__ n, const W
   const uint4 d = __ldg(reinterpret_cast<const uint4*>(n) + 3);  // qlo_z, qhi_x
   const uint4 e = __ldg(reinterpret_cast<const uint4*>(n) + 4);  // qhi_y, qhi_z
   const uint32_t em = __float_as_uint(a.w);
-  // plane q of axis x at distance (p + q 2^e - o) / d = q sx + bx; the bytes
-  // come biased by 2^23, folded into bx (one rounding, at most half a grid
-  // step: the builder leaves a full step of margin around every child box)
+  // plane q of axis x at distance (p + q 2^e - o) / d = q sx + bx.  (Folding
+  // the bytes' 2^23 bias into bx saves the subtraction but rounds bx by up
+  // to half a grid step, which needs a step of margin around every box:
+  // measured on GB300, twice the triangle tests per shadow ray and no gain.)
   const float sx = __uint_as_float((em & 0xFFu) << 23) * r.inv.x;
   const float sy = __uint_as_float(((em >> 8) & 0xFFu) << 23) * r.inv.y;
   const float sz = __uint_as_float(((em >> 16) & 0xFFu) << 23) * r.inv.z;
-  const float bx = fmaf(-8388608.0f, sx, (a.x - r.o.x) * r.inv.x);
-  const float by = fmaf(-8388608.0f, sy, (a.y - r.o.y) * r.inv.y);
-  const float bz = fmaf(-8388608.0f, sz, (a.z - r.o.z) * r.inv.z);
+  const float bx = (a.x - r.o.x) * r.inv.x;
+  const float by = (a.y - r.o.y) * r.inv.y;
+  const float bz = (a.z - r.o.z) * r.inv.z;
   // near and far planes per axis: the low planes are near for a positive direction
   const bool nx = r.oct & 1, ny = r.oct & 2, nz = r.oct & 4;
   const uint32_t nx0 = nx ? d.z : c.x, nx1 = nx ? d.w : c.y, fx0 = nx ? c.x : d.z, fx1 = nx ? c.y : d.w;
@@ -129,12 +130,12 @@ __device__ __forceinline__ void wnode_visit(const WNode* __restrict__ n, const W
 #pragma unroll
   for (int s = 0; s < 8; s++) {
     const int k = s & 3;
-    const float tnx = fmaf(qbyte_biased(s < 4 ? nx0 : nx1, k), sx, bx);
-    const float tfx = fmaf(qbyte_biased(s < 4 ? fx0 : fx1, k), sx, bx);
-    const float tny = fmaf(qbyte_biased(s < 4 ? ny0 : ny1, k), sy, by);
-    const float tfy = fmaf(qbyte_biased(s < 4 ? fy0 : fy1, k), sy, by);
-    const float tnz = fmaf(qbyte_biased(s < 4 ? nz0 : nz1, k), sz, bz);
-    const float tfz = fmaf(qbyte_biased(s < 4 ? fz0 : fz1, k), sz, bz);
+    const float tnx = fmaf(qbyte(s < 4 ? nx0 : nx1, k), sx, bx);
+    const float tfx = fmaf(qbyte(s < 4 ? fx0 : fx1, k), sx, bx);
+    const float tny = fmaf(qbyte(s < 4 ? ny0 : ny1, k), sy, by);
+    const float tfy = fmaf(qbyte(s < 4 ? fy0 : fy1, k), sy, by);
+    const float tnz = fmaf(qbyte(s < 4 ? nz0 : nz1, k), sz, bz);
+    const float tfz = fmaf(qbyte(s < 4 ? fz0 : fz1, k), sz, bz);
     const float tn = fmax3(tnx, tny, fmaxf(tnz, 0.0f));
     const float tf = fmin3(tfx, tfy, fminf(tfz, tmax));
     hits |= (tn <= tf) ? (1u << s) : 0u;
