@@ -268,6 +268,20 @@ int pr_qbvh_build_host(const float* vertices, int32_t n_vertices, const int32_t*
                        int64_t* n_nodes, int64_t* n_leaf_slots, float* boxes, int64_t* children,
                        int32_t* axes, int32_t* leaf_faces);
 
+/* The render path's own tree of one mesh (no reference counterpart; the
+ * reference builds only the QBVH above): a binned-SAH binary tree collapsed
+ * to compressed 8-wide nodes, built on the host (on_gpu = 0) or on the GPU
+ * (on_gpu = 1; pr_scene_upload uses it for meshes of 4096 faces and more).
+ * Both builders make the same split decisions, so the nodes are equal and
+ * only the order of triangles within a leaf may differ.  nodes: 80 bytes per
+ * node (grid origin as 3 floats, x/y/z grid exponents and the inner-child
+ * mask as 4 bytes, first inner child, first triangle slot, 8 leaf bytes,
+ * then the children's lower and upper planes as 6 x 8 bytes), node 0 the
+ * root; tri_faces: the face id of each triangle slot.  Outputs may be NULL
+ * (counts only); PR_E_ARG if a capacity is too small (counts still set). */
+int pr_render_bvh_export(pr_ctx* ctx, const pr_mesh* mesh, int on_gpu, void* nodes, int64_t nodes_cap,
+                         int32_t* tri_faces, int64_t tris_cap, int64_t* n_nodes, int64_t* n_tris);
+
 /* ---- closest hit ---------------------------------------------------------- */
 /* intersect_scene_ (scene.cpp:83-214) for n rays, including the 1e-6 origin
  * push, the linear entity loop and QBVH::CheckIntersection (QBVH.cpp:17-137).

@@ -23,6 +23,7 @@
 using namespace pr;
 
 #include "ctx_internal.h"
+#include "render_bvh.h"
 
 namespace {
 
@@ -109,10 +110,7 @@ void pr_destroy(pr_ctx* c) {
                     &c->adj_scratch, &c->adj_grad, &c->k_sens})
     b->release();
   for (DevBuf* b : {&c->errword, &c->counters, &c->partial,
-                    &c->out, &c->rays, &c->ires, &c->jres, &c->dres, &c->wf_o, &c->wf_d, &c->wf_beta, &c->wf_dpw,
-                    &c->wf_L, &c->wf_sample, &c->wf_hit, &c->wf_hitv, &c->wf_nee, &c->wf_sho, &c->wf_shd, &c->wf_extq,
-                    &c->wf_shq, &c->wf_spo, &c->wf_spd, &c->wf_spb, &c->wf_spw, &c->wf_sps, &c->wf_samp, &c->wf_live,
-                    &c->wf_pix, &c->wf_ctl})
+                    &c->out, &c->rays, &c->ires, &c->jres, &c->dres, &c->wf_arena})
     b->release();
   if (c->wf_graph) cudaGraphExecDestroy(c->wf_graph);
   if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
@@ -129,14 +127,54 @@ void pr_destroy(pr_ctx* c) {
 
 const char* pr_last_error(const pr_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
+// render trees of the large meshes: binary tree on the GPU, wide nodes on the host
+static int build_pending_trees(pr_ctx* c, HostScene& h) {
+  for (const HostScene::PendingTree& pt : h.pending_trees) {
+    std::vector<BinNode> tree;
+    std::vector<int32_t> order;
+    const pr_mesh& m = *pt.mesh;
+    PR_CUDA(c, build_render_bvh_binary_gpu(m.vertices, m.n_vertices, m.faces, m.n_faces, c->stream, tree, order));
+    h.ents[(size_t)pt.entity].rnode_base = (int32_t)h.rnodes.size();
+    const int depth = emit_render_bvh(m.vertices, m.faces, tree, order, h.rnodes, h.rtris);
+    if (depth > kWStack)
+      return fail(c, PR_E_BUILD, "mesh of entity " + std::to_string(pt.entity) + ": render tree of depth " +
+                                     std::to_string(depth) + " exceeds the traversal stack");
+  }
+  h.pending_trees.clear();  // they pointed into the caller's scene description
+  return PR_OK;
+}
+
+// the reference-layout QBVHs that large meshes left for their first use
+// (the exact first-hit path and the QBVH export)
+static int ensure_exact(pr_ctx* c, SceneObjData& o) {
+  if (o.host.deferred_exact.empty()) return PR_OK;
+  std::string err;
+  int st = complete_exact_qbvh(o.host, err);
+  if (st != PR_OK) return fail(c, st, err);
+  PR_CUDA(c, cudaSetDevice(c->device));
+  PR_CUDA(c, upload(o.ents, o.host.ents, c->stream));
+  PR_CUDA(c, upload(o.nodes, o.host.nodes, c->stream));
+  PR_CUDA(c, upload(o.tris, o.host.tris, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  o.dev.ents = (const GEntity*)o.ents.p;
+  o.dev.nodes = (const GNode*)o.nodes.p;
+  o.dev.tris = (const float4*)o.tris.p;
+  return PR_OK;
+}
+
 // host build + device copies of one scene (SceneEnv::Load + CreateEntList)
 static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o) {
   PR_CUDA(c, cudaSetDevice(c->device));
   cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
   std::string err;
-  int st = build_host_scene(d, o.host, err);
+  SceneBuildOptions opt;
+  opt.gpu_render_trees = true;
+  opt.defer_exact = true;
+  int st = build_host_scene(d, o.host, err, opt);
   if (st != PR_OK) return fail(c, st, err);
   HostScene& h = o.host;
+  st = build_pending_trees(c, h);
+  if (st != PR_OK) return st;
   PR_CUDA(c, upload(o.ents, h.ents, c->stream));
   PR_CUDA(c, upload(o.mats, h.mats, c->stream));
   PR_CUDA(c, upload(o.nodes, h.nodes, c->stream));
@@ -239,8 +277,38 @@ void pr_scene_release(pr_ctx* c, pr_scene_obj* o) {
 
 static void export_qbvh(const MeshQbvh& q, float* boxes, int64_t* children, int32_t* axes, int32_t* leaf_faces);
 
+int pr_render_bvh_export(pr_ctx* c, const pr_mesh* m, int on_gpu, void* nodes, int64_t nodes_cap,
+                         int32_t* tri_faces, int64_t tris_cap, int64_t* n_nodes, int64_t* n_tris) {
+  if (!c) return PR_E_ARG;
+  if (!m || m->n_faces <= 0 || m->n_vertices <= 0 || !m->vertices || !m->faces) return fail(c, PR_E_ARG, "empty mesh");
+  for (int64_t f = 0; f < 3 * (int64_t)m->n_faces; f++)
+    if (m->faces[f] < 0 || m->faces[f] >= m->n_vertices) return fail(c, PR_E_ARG, "face index out of range");
+  std::vector<WNode> wn;
+  std::vector<float4> wt;
+  if (on_gpu) {
+    PR_CUDA(c, cudaSetDevice(c->device));
+    cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
+    std::vector<BinNode> tree;
+    std::vector<int32_t> order;
+    PR_CUDA(c, build_render_bvh_binary_gpu(m->vertices, m->n_vertices, m->faces, m->n_faces, c->stream, tree, order));
+    emit_render_bvh(m->vertices, m->faces, tree, order, wn, wt);
+  } else {
+    build_render_bvh(m->vertices, m->faces, m->n_faces, wn, wt);
+  }
+  const int64_t nn = (int64_t)wn.size(), nt = (int64_t)(wt.size() / 3);
+  if (n_nodes) *n_nodes = nn;
+  if (n_tris) *n_tris = nt;
+  if ((nodes && nodes_cap < nn) || (tri_faces && tris_cap < nt)) return fail(c, PR_E_ARG, "output capacity too small");
+  if (nodes) memcpy(nodes, wn.data(), sizeof(WNode) * wn.size());
+  if (tri_faces)
+    for (int64_t i = 0; i < nt; i++) memcpy(&tri_faces[i], &wt[(size_t)(3 * i)].w, 4);
+  return PR_OK;
+}
+
 int pr_qbvh_info(pr_ctx* c, int entity, int64_t* n_nodes, int64_t* n_leaf_slots) {
   if (!c || !c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  const int st = ensure_exact(c, c->cur);
+  if (st != PR_OK) return st;
   for (size_t m = 0; m < c->cur.host.mesh_entity.size(); m++)
     if (c->cur.host.mesh_entity[m] == entity) {
       if (n_nodes) *n_nodes = (int64_t)c->cur.host.mesh_qbvh[m].nodes.size();
@@ -252,6 +320,8 @@ int pr_qbvh_info(pr_ctx* c, int entity, int64_t* n_nodes, int64_t* n_leaf_slots)
 
 int pr_qbvh_export(pr_ctx* c, int entity, float* boxes, int64_t* children, int32_t* axes, int32_t* leaf_faces) {
   if (!c || !c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  const int st = ensure_exact(c, c->cur);
+  if (st != PR_OK) return st;
   for (size_t m = 0; m < c->cur.host.mesh_entity.size(); m++)
     if (c->cur.host.mesh_entity[m] == entity) {
       export_qbvh(c->cur.host.mesh_qbvh[m], boxes, children, axes, leaf_faces);
@@ -297,6 +367,8 @@ int pr_first_hit_dev(pr_ctx* c, const double* rays, int64_t n, int32_t* entity, 
   if (n < 0 || (n > 0 && (!rays || !entity || !prim || !t))) return fail(c, PR_E_ARG, "bad first-hit arguments");
   PR_CUDA(c, cudaSetDevice(c->device));
   cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
+  const int se = ensure_exact(c, c->cur);
+  if (se != PR_OK) return se;
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
@@ -448,6 +520,9 @@ int pr::prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* 
 
 extern "C" {
 
+// byte skew between consecutive arrays of the wavefront pool
+constexpr size_t kArenaSkew = 4352;
+
 // paths in flight (slots of the wavefront pool); PR_WF_SLOTS overrides
 static unsigned int wavefront_slots() {
   const char* e = getenv("PR_WF_SLOTS");
@@ -463,53 +538,51 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   uint64_t layers = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.spp, max_pass / wh));
   const uint64_t pass_cap = layers * wh;
   const size_t f4 = sizeof(float4);
-  PR_CUDA(c, c->wf_o.ensure(f4 * P));
-  PR_CUDA(c, c->wf_d.ensure(f4 * P));
-  PR_CUDA(c, c->wf_beta.ensure(f4 * P));
-  PR_CUDA(c, c->wf_dpw.ensure(f4 * P));
-  PR_CUDA(c, c->wf_L.ensure(f4 * P));
-  PR_CUDA(c, c->wf_sample.ensure(8ull * P));
-  PR_CUDA(c, c->wf_hit.ensure(f4 * P));
-  PR_CUDA(c, c->wf_hitv.ensure(4ull * P));
-  PR_CUDA(c, c->wf_nee.ensure(f4 * 3 * P));
-  PR_CUDA(c, c->wf_sho.ensure(f4 * 3 * P));
-  PR_CUDA(c, c->wf_shd.ensure(f4 * 3 * P));
-  PR_CUDA(c, c->wf_extq.ensure(4ull * P));
-  PR_CUDA(c, c->wf_shq.ensure(4ull * 3 * P));
   const unsigned int spawn_cap = 2 * P;
-  PR_CUDA(c, c->wf_spo.ensure(f4 * spawn_cap));
-  PR_CUDA(c, c->wf_spd.ensure(f4 * spawn_cap));
-  PR_CUDA(c, c->wf_spb.ensure(f4 * spawn_cap));
-  PR_CUDA(c, c->wf_spw.ensure(f4 * spawn_cap));
-  PR_CUDA(c, c->wf_sps.ensure(8ull * spawn_cap));
-  PR_CUDA(c, c->wf_samp.ensure(24ull * pass_cap));
-  PR_CUDA(c, c->wf_live.ensure(4ull * pass_cap));
-  PR_CUDA(c, c->wf_pix.ensure(24ull * wh));
-  PR_CUDA(c, c->wf_ctl.ensure(sizeof(WfCtl)));
+  // the pool in one allocation, its arrays in a fixed order, each start
+  // moved on by a further kArenaSkew bytes so that the records of one slot
+  // in different arrays do not share an address modulo any large power of
+  // two (the layout no longer depends on what was allocated before)
+  const size_t sizes[] = {f4 * P, f4 * P, f4 * P, f4 * P, f4 * P, 8ull * P, f4 * P, 4ull * P,
+                          f4 * 3 * P, f4 * 3 * P, f4 * 3 * P, 4ull * P, 4ull * 3 * P,
+                          f4 * spawn_cap, f4 * spawn_cap, f4 * spawn_cap, f4 * spawn_cap, 8ull * spawn_cap,
+                          24ull * pass_cap, 4ull * pass_cap, 24ull * wh, sizeof(WfCtl)};
+  constexpr int kArrays = (int)(sizeof(sizes) / sizeof(sizes[0]));
+  size_t offs[kArrays];
+  size_t total = 0;
+  for (int k = 0; k < kArrays; k++) {
+    total = (total + 4095) & ~(size_t)4095;
+    offs[k] = total + (size_t)k * kArenaSkew;
+    total = offs[k] + sizes[k];
+  }
+  PR_CUDA(c, c->wf_arena.ensure(total));
+  unsigned char* ab = static_cast<unsigned char*>(c->wf_arena.p);
+  void* arr[kArrays];
+  for (int k = 0; k < kArrays; k++) arr[k] = ab + offs[k];
   if (!c->wf_host_ctl) PR_CUDA(c, cudaMallocHost((void**)&c->wf_host_ctl, sizeof(WfCtl)));
   WfBufs B{};
-  B.o = (float4*)c->wf_o.p;
-  B.d = (float4*)c->wf_d.p;
-  B.beta = (float4*)c->wf_beta.p;
-  B.dpw = (float4*)c->wf_dpw.p;
-  B.L = (float4*)c->wf_L.p;
-  B.sample = (uint64_t*)c->wf_sample.p;
-  B.hit = (float4*)c->wf_hit.p;
-  B.hitv = (float*)c->wf_hitv.p;
-  B.nee = (float4*)c->wf_nee.p;
-  B.sh_o = (float4*)c->wf_sho.p;
-  B.sh_d = (float4*)c->wf_shd.p;
-  B.extq = (int*)c->wf_extq.p;
-  B.shq = (int*)c->wf_shq.p;
-  B.sp_o = (float4*)c->wf_spo.p;
-  B.sp_d = (float4*)c->wf_spd.p;
-  B.sp_beta = (float4*)c->wf_spb.p;
-  B.sp_dpw = (float4*)c->wf_spw.p;
-  B.sp_sample = (uint64_t*)c->wf_sps.p;
-  B.samp = (long long*)c->wf_samp.p;
-  B.live = (int*)c->wf_live.p;
-  B.pix = (long long*)c->wf_pix.p;
-  B.ctl = (WfCtl*)c->wf_ctl.p;
+  B.o = (float4*)arr[0];
+  B.d = (float4*)arr[1];
+  B.beta = (float4*)arr[2];
+  B.dpw = (float4*)arr[3];
+  B.L = (float4*)arr[4];
+  B.sample = (uint64_t*)arr[5];
+  B.hit = (float4*)arr[6];
+  B.hitv = (float*)arr[7];
+  B.nee = (float4*)arr[8];
+  B.sh_o = (float4*)arr[9];
+  B.sh_d = (float4*)arr[10];
+  B.extq = (int*)arr[11];
+  B.shq = (int*)arr[12];
+  B.sp_o = (float4*)arr[13];
+  B.sp_d = (float4*)arr[14];
+  B.sp_beta = (float4*)arr[15];
+  B.sp_dpw = (float4*)arr[16];
+  B.sp_sample = (uint64_t*)arr[17];
+  B.samp = (long long*)arr[18];
+  B.live = (int*)arr[19];
+  B.pix = (long long*)arr[20];
+  B.ctl = (WfCtl*)arr[21];
   B.err = (uint32_t*)c->errword.p;
   B.counters = (unsigned long long*)c->counters.p;
   B.n_slots = P;
@@ -523,8 +596,8 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || sms <= 0) sms = 152;
   const unsigned int bps = c->tuned_trace_bps ? c->tuned_trace_bps : kTraceBlocksPerSM;
   L.trace_blocks = std::min<unsigned int>((P + 127) / 128, (unsigned int)sms * bps);
-  PR_CUDA(c, cudaMemsetAsync(c->wf_nee.p, 0, f4 * 3 * P, c->stream));
-  PR_CUDA(c, cudaMemsetAsync(c->wf_pix.p, 0, 24ull * wh, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(B.nee, 0, f4 * 3 * P, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(B.pix, 0, 24ull * wh, c->stream));
   // PR_WF_HOST_LOOP=1 drives the iterations from the host instead of the
   // graph's device-side while loop: profilers that cannot see kernels inside
   // conditional graph nodes see every launch this way (same kernels, same work)
@@ -554,11 +627,11 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
     const uint64_t n_layers = std::min<uint64_t>(layers, (uint64_t)g.spp - first);
     B.pass_first = first;
     B.pass_samples = n_layers * wh;
-    PR_CUDA(c, cudaMemsetAsync(c->wf_samp.p, 0, 24ull * B.pass_samples, c->stream));
+    PR_CUDA(c, cudaMemsetAsync(B.samp, 0, 24ull * B.pass_samples, c->stream));
     PR_CUDA(c, wf_set_constants(c->cur.dev, g, B, c->stream));
     PR_CUDA(c, wf_reset_launch(P, c->stream));
     if (use_graph && c->wf_graph) PR_CUDA(c, cudaGraphLaunch(c->wf_graph, c->stream));
-    else PR_CUDA(c, wf_run_host_loop(L, c->wf_host_ctl, (const WfCtl*)c->wf_ctl.p, c->stream, c->kernel_ms));
+    else PR_CUDA(c, wf_run_host_loop(L, c->wf_host_ctl, (const WfCtl*)B.ctl, c->stream, c->kernel_ms));
   }
   PR_CUDA(c, wf_resolve_launch(rgb_dev, (int)(3 * wh), accumulate, g.sensor, c->stream));
   return PR_OK;

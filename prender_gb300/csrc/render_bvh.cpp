@@ -369,4 +369,27 @@ int build_render_bvh(const float* vertices, const int32_t* faces, int32_t n_face
   return e.max_depth;
 }
 
+int emit_render_bvh(const float* vertices, const int32_t* faces, const std::vector<BinNode>& tree,
+                    const std::vector<int32_t>& order, std::vector<WNode>& nodes, std::vector<float4>& tris) {
+  std::vector<BNode> bn(tree.size());
+  for (size_t i = 0; i < tree.size(); i++) {
+    const BinNode& q = tree[i];
+    for (int a = 0; a < 3; a++) {
+      bn[i].box.mn[a] = q.mn[a];
+      bn[i].box.mx[a] = q.mx[a];
+    }
+    bn[i].left = q.left;
+    bn[i].right = q.right;
+    bn[i].first = q.first;
+    bn[i].count = q.count;
+  }
+  std::vector<Tri> t(order.size());  // the emitter reads only the face of each position
+  for (size_t i = 0; i < order.size(); i++) t[i].face = order[i];
+  Emitter e{bn, t, vertices, faces, nodes, tris};
+  const int root = (int)nodes.size();
+  nodes.emplace_back();
+  e.emit(root, 0, 1);
+  return e.max_depth;
+}
+
 }  // namespace pr

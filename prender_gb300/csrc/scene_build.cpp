@@ -294,7 +294,66 @@ static bool is_light(const pr_material& m) {  // Material::isLight (material.h)
   return m.type == PR_MAT_DIFFUSE && len(c) < 0.001 && len(e) > 0.001;
 }
 
-int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
+// The reference-layout QBVH of one mesh (QBVH.cpp:161-302) into the exact
+// path's arrays, and the entity's indexes into them.
+static int append_exact_qbvh(HostScene& hs, GEntity& g, int entity, const float* vertices, const int32_t* faces,
+                             int n_faces, std::string& err) {
+  MeshQbvh q;
+  int st = build_mesh_qbvh(vertices, faces, n_faces, q, err);
+  if (st != PR_OK) {
+    err = "mesh of entity " + std::to_string(entity) + ": " + err;
+    return st;
+  }
+  g.node_base = (int32_t)hs.nodes.size();
+  g.slot_base = (int32_t)(hs.tris.size() / 3);
+  for (const RefNode& rn : q.nodes) {
+    GNode gn;
+    memset(&gn, 0, sizeof(gn));
+    for (int s = 0; s < 4; s++) {
+      gn.bmin_x[s] = rn.box[0][0][s]; gn.bmax_x[s] = rn.box[1][0][s];
+      gn.bmin_y[s] = rn.box[0][1][s]; gn.bmax_y[s] = rn.box[1][1][s];
+      gn.bmin_z[s] = rn.box[0][2][s]; gn.bmax_z[s] = rn.box[1][2][s];
+      const int64_t c = rn.ref_child[s];
+      if (c == -1) {
+        gn.child[s] = kChildInvalid;
+      } else if (c < 0) {  // leaf
+        gn.child[s] = (int32_t)(kLeafBit | (uint32_t)(g.slot_base + rn.leaf_first[s]));
+        gn.count[s] = (uint16_t)rn.leaf_count[s];
+      } else {
+        gn.child[s] = (int32_t)(g.node_base + c);
+      }
+    }
+    gn.axes = rn.axis_top | (rn.axis_left << 2) | (rn.axis_right << 4);
+    hs.nodes.push_back(gn);
+  }
+  for (int t : q.leaf_tris) {
+    for (int k = 0; k < 3; k++) {
+      const float* v = vertices + 3 * (size_t)faces[3 * (size_t)t + k];
+      float4 f4;
+      f4.x = v[0];
+      f4.y = v[1];
+      f4.z = v[2];
+      int32_t w = (k == 0) ? t : 0;
+      memcpy(&f4.w, &w, 4);
+      hs.tris.push_back(f4);
+    }
+  }
+  hs.mesh_qbvh.push_back(std::move(q));
+  hs.mesh_entity.push_back(entity);
+  return PR_OK;
+}
+
+int complete_exact_qbvh(HostScene& hs, std::string& err) {
+  for (const HostScene::DeferredMesh& m : hs.deferred_exact) {
+    int st = append_exact_qbvh(hs, hs.ents[(size_t)m.entity], m.entity, m.vertices.data(), m.faces.data(),
+                               (int)(m.faces.size() / 3), err);
+    if (st != PR_OK) return st;
+  }
+  hs.deferred_exact.clear();
+  return PR_OK;
+}
+
+int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, const SceneBuildOptions& opt) {
   hs = HostScene();
   if (!d || d->n_entities < 0 || d->n_materials < 0 || d->n_meshes < 0) { err = "null or negative scene sizes"; return PR_E_ARG; }
   if (d->n_entities > kMaxEntities) { err = "too many entities"; return PR_E_ARG; }
@@ -539,36 +598,23 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
       for (int64_t f = 0; f < 3 * (int64_t)pm_.n_faces; f++)
         if (pm_.faces[f] < 0 || pm_.faces[f] >= pm_.n_vertices) { err = "face index out of range"; return PR_E_SCENE; }
       if (is_light(pm)) { err = "mesh lights are not sampled by the reference's next-event estimation"; return PR_E_UNSUPPORTED; }
-      MeshQbvh q;
-      int st = build_mesh_qbvh(pm_.vertices, pm_.faces, pm_.n_faces, q, err);
-      if (st != PR_OK) return st;
+      const bool big = pm_.n_faces >= kGpuBuildMinFaces;
       std::vector<float> fn;
       if (pm_.face_normals) fn.assign(pm_.face_normals, pm_.face_normals + 3 * (size_t)pm_.n_faces);
       else face_normals(pm_.vertices, pm_.faces, pm_.n_faces, fn);
-      g.node_base = (int32_t)hs.nodes.size();
-      g.slot_base = (int32_t)(hs.tris.size() / 3);
       g.face_base = (int32_t)(hs.fnorm.size() / 3);
       g.n_faces = pm_.n_faces;
-      // GPU nodes
-      for (const RefNode& rn : q.nodes) {
-        GNode gn;
-        memset(&gn, 0, sizeof(gn));
-        for (int s = 0; s < 4; s++) {
-          gn.bmin_x[s] = rn.box[0][0][s]; gn.bmax_x[s] = rn.box[1][0][s];
-          gn.bmin_y[s] = rn.box[0][1][s]; gn.bmax_y[s] = rn.box[1][1][s];
-          gn.bmin_z[s] = rn.box[0][2][s]; gn.bmax_z[s] = rn.box[1][2][s];
-          const int64_t c = rn.ref_child[s];
-          if (c == -1) {
-            gn.child[s] = kChildInvalid;
-          } else if (c < 0) {  // leaf
-            gn.child[s] = (int32_t)(kLeafBit | (uint32_t)(g.slot_base + rn.leaf_first[s]));
-            gn.count[s] = (uint16_t)rn.leaf_count[s];
-          } else {
-            gn.child[s] = (int32_t)(g.node_base + c);
-          }
-        }
-        gn.axes = rn.axis_top | (rn.axis_left << 2) | (rn.axis_right << 4);
-        hs.nodes.push_back(gn);
+      if (big && opt.defer_exact && !d->kerr.enabled) {
+        g.node_base = -1;
+        g.slot_base = -1;
+        HostScene::DeferredMesh dm;
+        dm.entity = i;
+        dm.vertices.assign(pm_.vertices, pm_.vertices + 3 * (size_t)pm_.n_vertices);
+        dm.faces.assign(pm_.faces, pm_.faces + 3 * (size_t)pm_.n_faces);
+        hs.deferred_exact.push_back(std::move(dm));
+      } else {
+        int st = append_exact_qbvh(hs, g, i, pm_.vertices, pm_.faces, pm_.n_faces, err);
+        if (st != PR_OK) return st;
       }
       for (int a = 0; a < 3; a++) {
         g.bmin[a] = 3.0e38f;
@@ -579,6 +625,7 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
         for (int a = 0; a < 3; a++) {
           g.bmin[a] = std::min(g.bmin[a], v[a]);
           g.bmax[a] = std::max(g.bmax[a], v[a]);
+          grow(v[a]);
         }
       }
       // Polygon::CreateBoundingBox over every vertex of the mesh (polygon.h:875-889)
@@ -589,30 +636,20 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err) {
           g.bb_max[a] = std::max(g.bb_max[a], (double)pm_.vertices[3 * k + a]);
         }
       for (int a = 0; a < 3; a++) { g.bb_min[a] -= 0.01; g.bb_max[a] += 0.01; }
-      for (int t : q.leaf_tris) {
-        for (int k = 0; k < 3; k++) {
-          const float* v = pm_.vertices + 3 * (size_t)pm_.faces[3 * (size_t)t + k];
-          float4 f4;
-          f4.x = v[0];
-          f4.y = v[1];
-          f4.z = v[2];
-          int32_t w = (k == 0) ? t : 0;
-          memcpy(&f4.w, &w, 4);
-          hs.tris.push_back(f4);
-          for (int a = 0; a < 3; a++) grow(v[a]);
-        }
-      }
       hs.fnorm.insert(hs.fnorm.end(), fn.begin(), fn.end());
       // the render traversal's own tree (same closest hits, fewer tests)
-      g.rnode_base = (int32_t)hs.rnodes.size();
-      const int rdepth = build_render_bvh(pm_.vertices, pm_.faces, pm_.n_faces, hs.rnodes, hs.rtris);
-      if (rdepth > kWStack) {
-        err = "mesh " + std::to_string(i) + ": render tree of depth " + std::to_string(rdepth) +
-              " exceeds the traversal stack (" + std::to_string(kWStack) + ")";
-        return PR_E_BUILD;
+      if (big && opt.gpu_render_trees) {
+        g.rnode_base = -1;
+        hs.pending_trees.push_back({i, &pm_});
+      } else {
+        g.rnode_base = (int32_t)hs.rnodes.size();
+        const int rdepth = build_render_bvh(pm_.vertices, pm_.faces, pm_.n_faces, hs.rnodes, hs.rtris);
+        if (rdepth > kWStack) {
+          err = "mesh " + std::to_string(i) + ": render tree of depth " + std::to_string(rdepth) +
+                " exceeds the traversal stack (" + std::to_string(kWStack) + ")";
+          return PR_E_BUILD;
+        }
       }
-      hs.mesh_qbvh.push_back(std::move(q));
-      hs.mesh_entity.push_back(i);
     } else {
       err = "entity type " + std::to_string(pe.type) + " is not on this path yet";
       return PR_E_UNSUPPORTED;

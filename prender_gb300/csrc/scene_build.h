@@ -45,9 +45,34 @@ struct HostScene {
   std::vector<unsigned char> kerr_texture;
   std::vector<unsigned char> kerr_disk_texture;  // RGBA8
   bool disk_light = false;  // an emitting disk is registered as a light
+  // meshes whose render tree the caller builds (pointers into the scene
+  // description: valid during the upload call only)
+  struct PendingTree {
+    int entity;
+    const pr_mesh* mesh;
+  };
+  std::vector<PendingTree> pending_trees;
+  // meshes whose reference-layout QBVH is built on first use (copies)
+  struct DeferredMesh {
+    int entity;
+    std::vector<float> vertices;
+    std::vector<int32_t> faces;
+  };
+  std::vector<DeferredMesh> deferred_exact;
 };
 
-int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err);
+// How build_host_scene treats meshes of at least kGpuBuildMinFaces faces.
+struct SceneBuildOptions {
+  bool gpu_render_trees = false;  // leave their render trees to the caller (pending_trees)
+  bool defer_exact = false;       // leave their reference-layout QBVH for later (deferred_exact),
+                                  // except in scenes with a black hole, whose rays use it
+};
+
+int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err,
+                     const SceneBuildOptions& opt = SceneBuildOptions());
+// Builds the deferred reference-layout QBVHs of hs (appending nodes and
+// triangles, setting their entities' node_base / slot_base).
+int complete_exact_qbvh(HostScene& hs, std::string& err);
 int build_mesh_qbvh(const float* vertices, const int32_t* faces, int n_faces, MeshQbvh& out, std::string& err);
 void face_normals(const float* V, const int32_t* F, int n_faces, std::vector<float>& out);
 

@@ -143,6 +143,26 @@ class Context:
             arr[j].accumulate = 0
         self._check(self.L.pr_render_batch(self.h, len(jobs), arr))
 
+    def render_bvh(self, vertices: np.ndarray, faces: np.ndarray, on_gpu: bool) -> dict:
+        """The render path's tree of one mesh from the host or the GPU builder
+        (pr_render_bvh_export): nodes as raw 80-byte records (uint8, n x 80)
+        and the face id of each triangle slot."""
+        v = np.ascontiguousarray(vertices, dtype=np.float32)
+        f = np.ascontiguousarray(faces, dtype=np.int32)
+        m = A.pr_mesh()
+        m.n_vertices, m.n_faces = v.shape[0], f.shape[0]
+        m.vertices = v.ctypes.data_as(C.POINTER(C.c_float))
+        m.faces = f.ctypes.data_as(C.POINTER(C.c_int32))
+        m.face_normals = None
+        nn, nt = C.c_int64(0), C.c_int64(0)
+        self._check(self.L.pr_render_bvh_export(self.h, C.byref(m), int(on_gpu), None, 0, None, 0, C.byref(nn),
+                                                C.byref(nt)))
+        nodes = np.zeros((nn.value, 80), np.uint8)
+        tri = np.zeros(nt.value, np.int32)
+        self._check(self.L.pr_render_bvh_export(self.h, C.byref(m), int(on_gpu), _p(nodes), nn.value, _p(tri),
+                                                nt.value, C.byref(nn), C.byref(nt)))
+        return dict(nodes=nodes, tri_faces=tri)
+
     def autotune(self, scene=None, settings=None, camera=None) -> dict:
         """Picks the wavefront pool size and traversal grid for this context
         by timing short frames of the scene (pr_autotune_wavefront)."""
