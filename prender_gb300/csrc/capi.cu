@@ -110,7 +110,10 @@ void pr_destroy(pr_ctx* c) {
                     &c->adj_scratch, &c->adj_grad, &c->k_sens})
     b->release();
   for (DevBuf* b : {&c->errword, &c->counters, &c->partial,
-                    &c->out, &c->rays, &c->ires, &c->jres, &c->dres, &c->wf_arena})
+                    &c->out, &c->rays, &c->ires, &c->jres, &c->dres, &c->wf_o, &c->wf_d, &c->wf_beta, &c->wf_dpw,
+                    &c->wf_L, &c->wf_sample, &c->wf_hit, &c->wf_hitv, &c->wf_nee, &c->wf_sho, &c->wf_shd, &c->wf_extq,
+                    &c->wf_shq, &c->wf_spo, &c->wf_spd, &c->wf_spb, &c->wf_spw, &c->wf_sps, &c->wf_samp, &c->wf_live,
+                    &c->wf_pix, &c->wf_ctl})
     b->release();
   if (c->wf_graph) cudaGraphExecDestroy(c->wf_graph);
   if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
@@ -177,6 +180,18 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   if (st != PR_OK) return st;
   PR_CUDA(c, upload(o.ents, h.ents, c->stream));
   PR_CUDA(c, upload(o.mats, h.mats, c->stream));
+  // the exact path's arrays get their space now, as an eager build would
+  // take it, and are filled on first use: measured on GB300, letting the
+  // wavefront pool take that space instead slows wf_shade by 15 % (the
+  // pool's placement in memory matters to it; the cause is not known)
+  size_t res_nodes = h.nodes.size(), res_tris = h.tris.size();
+  for (const HostScene::DeferredMesh& m : h.deferred_exact) {
+    const size_t nf = m.faces.size() / 3;
+    res_tris += 3 * nf;
+    res_nodes += (size_t)std::ceil((double)nf / 5.6);  // the reference's SAH: about 5.6 faces per 4-wide node
+  }
+  PR_CUDA(c, o.nodes.ensure(sizeof(GNode) * std::max<size_t>(res_nodes, 1)));
+  PR_CUDA(c, o.tris.ensure(sizeof(float4) * std::max<size_t>(res_tris, 1)));
   PR_CUDA(c, upload(o.nodes, h.nodes, c->stream));
   PR_CUDA(c, upload(o.tris, h.tris, c->stream));
   PR_CUDA(c, upload(o.rnodes, h.rnodes, c->stream));
@@ -520,9 +535,6 @@ int pr::prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* 
 
 extern "C" {
 
-// byte skew between consecutive arrays of the wavefront pool
-constexpr size_t kArenaSkew = 4352;
-
 // paths in flight (slots of the wavefront pool); PR_WF_SLOTS overrides
 static unsigned int wavefront_slots() {
   const char* e = getenv("PR_WF_SLOTS");
@@ -538,51 +550,53 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   uint64_t layers = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.spp, max_pass / wh));
   const uint64_t pass_cap = layers * wh;
   const size_t f4 = sizeof(float4);
+  PR_CUDA(c, c->wf_o.ensure(f4 * P));
+  PR_CUDA(c, c->wf_d.ensure(f4 * P));
+  PR_CUDA(c, c->wf_beta.ensure(f4 * P));
+  PR_CUDA(c, c->wf_dpw.ensure(f4 * P));
+  PR_CUDA(c, c->wf_L.ensure(f4 * P));
+  PR_CUDA(c, c->wf_sample.ensure(8ull * P));
+  PR_CUDA(c, c->wf_hit.ensure(f4 * P));
+  PR_CUDA(c, c->wf_hitv.ensure(4ull * P));
+  PR_CUDA(c, c->wf_nee.ensure(f4 * 3 * P));
+  PR_CUDA(c, c->wf_sho.ensure(f4 * 3 * P));
+  PR_CUDA(c, c->wf_shd.ensure(f4 * 3 * P));
+  PR_CUDA(c, c->wf_extq.ensure(4ull * P));
+  PR_CUDA(c, c->wf_shq.ensure(4ull * 3 * P));
   const unsigned int spawn_cap = 2 * P;
-  // the pool in one allocation, its arrays in a fixed order, each start
-  // moved on by a further kArenaSkew bytes so that the records of one slot
-  // in different arrays do not share an address modulo any large power of
-  // two (the layout no longer depends on what was allocated before)
-  const size_t sizes[] = {f4 * P, f4 * P, f4 * P, f4 * P, f4 * P, 8ull * P, f4 * P, 4ull * P,
-                          f4 * 3 * P, f4 * 3 * P, f4 * 3 * P, 4ull * P, 4ull * 3 * P,
-                          f4 * spawn_cap, f4 * spawn_cap, f4 * spawn_cap, f4 * spawn_cap, 8ull * spawn_cap,
-                          24ull * pass_cap, 4ull * pass_cap, 24ull * wh, sizeof(WfCtl)};
-  constexpr int kArrays = (int)(sizeof(sizes) / sizeof(sizes[0]));
-  size_t offs[kArrays];
-  size_t total = 0;
-  for (int k = 0; k < kArrays; k++) {
-    total = (total + 4095) & ~(size_t)4095;
-    offs[k] = total + (size_t)k * kArenaSkew;
-    total = offs[k] + sizes[k];
-  }
-  PR_CUDA(c, c->wf_arena.ensure(total));
-  unsigned char* ab = static_cast<unsigned char*>(c->wf_arena.p);
-  void* arr[kArrays];
-  for (int k = 0; k < kArrays; k++) arr[k] = ab + offs[k];
+  PR_CUDA(c, c->wf_spo.ensure(f4 * spawn_cap));
+  PR_CUDA(c, c->wf_spd.ensure(f4 * spawn_cap));
+  PR_CUDA(c, c->wf_spb.ensure(f4 * spawn_cap));
+  PR_CUDA(c, c->wf_spw.ensure(f4 * spawn_cap));
+  PR_CUDA(c, c->wf_sps.ensure(8ull * spawn_cap));
+  PR_CUDA(c, c->wf_samp.ensure(24ull * pass_cap));
+  PR_CUDA(c, c->wf_live.ensure(4ull * pass_cap));
+  PR_CUDA(c, c->wf_pix.ensure(24ull * wh));
+  PR_CUDA(c, c->wf_ctl.ensure(sizeof(WfCtl)));
   if (!c->wf_host_ctl) PR_CUDA(c, cudaMallocHost((void**)&c->wf_host_ctl, sizeof(WfCtl)));
   WfBufs B{};
-  B.o = (float4*)arr[0];
-  B.d = (float4*)arr[1];
-  B.beta = (float4*)arr[2];
-  B.dpw = (float4*)arr[3];
-  B.L = (float4*)arr[4];
-  B.sample = (uint64_t*)arr[5];
-  B.hit = (float4*)arr[6];
-  B.hitv = (float*)arr[7];
-  B.nee = (float4*)arr[8];
-  B.sh_o = (float4*)arr[9];
-  B.sh_d = (float4*)arr[10];
-  B.extq = (int*)arr[11];
-  B.shq = (int*)arr[12];
-  B.sp_o = (float4*)arr[13];
-  B.sp_d = (float4*)arr[14];
-  B.sp_beta = (float4*)arr[15];
-  B.sp_dpw = (float4*)arr[16];
-  B.sp_sample = (uint64_t*)arr[17];
-  B.samp = (long long*)arr[18];
-  B.live = (int*)arr[19];
-  B.pix = (long long*)arr[20];
-  B.ctl = (WfCtl*)arr[21];
+  B.o = (float4*)c->wf_o.p;
+  B.d = (float4*)c->wf_d.p;
+  B.beta = (float4*)c->wf_beta.p;
+  B.dpw = (float4*)c->wf_dpw.p;
+  B.L = (float4*)c->wf_L.p;
+  B.sample = (uint64_t*)c->wf_sample.p;
+  B.hit = (float4*)c->wf_hit.p;
+  B.hitv = (float*)c->wf_hitv.p;
+  B.nee = (float4*)c->wf_nee.p;
+  B.sh_o = (float4*)c->wf_sho.p;
+  B.sh_d = (float4*)c->wf_shd.p;
+  B.extq = (int*)c->wf_extq.p;
+  B.shq = (int*)c->wf_shq.p;
+  B.sp_o = (float4*)c->wf_spo.p;
+  B.sp_d = (float4*)c->wf_spd.p;
+  B.sp_beta = (float4*)c->wf_spb.p;
+  B.sp_dpw = (float4*)c->wf_spw.p;
+  B.sp_sample = (uint64_t*)c->wf_sps.p;
+  B.samp = (long long*)c->wf_samp.p;
+  B.live = (int*)c->wf_live.p;
+  B.pix = (long long*)c->wf_pix.p;
+  B.ctl = (WfCtl*)c->wf_ctl.p;
   B.err = (uint32_t*)c->errword.p;
   B.counters = (unsigned long long*)c->counters.p;
   B.n_slots = P;
@@ -596,7 +610,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || sms <= 0) sms = 152;
   const unsigned int bps = c->tuned_trace_bps ? c->tuned_trace_bps : kTraceBlocksPerSM;
   L.trace_blocks = std::min<unsigned int>((P + 127) / 128, (unsigned int)sms * bps);
-  PR_CUDA(c, cudaMemsetAsync(B.nee, 0, f4 * 3 * P, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->wf_nee.p, 0, f4 * 3 * P, c->stream));
   PR_CUDA(c, cudaMemsetAsync(B.pix, 0, 24ull * wh, c->stream));
   // PR_WF_HOST_LOOP=1 drives the iterations from the host instead of the
   // graph's device-side while loop: profilers that cannot see kernels inside

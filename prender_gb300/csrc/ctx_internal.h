@@ -65,7 +65,8 @@ struct pr_ctx {
   unsigned long long shadow_counts[3] = {0, 0, 0};  // shadow rays, nodes, triangles of the last wavefront frame
   pr_render_stats stats{};
   // wavefront pool
-  pr::DevBuf wf_arena;  // every array of the pool, one allocation (render_wavefront)
+  pr::DevBuf wf_o, wf_d, wf_beta, wf_dpw, wf_L, wf_sample, wf_hit, wf_hitv, wf_nee, wf_sho, wf_shd, wf_extq, wf_shq;
+  pr::DevBuf wf_spo, wf_spd, wf_spb, wf_spw, wf_sps, wf_samp, wf_live, wf_pix, wf_ctl;
   unsigned int wf_slots = 0;
   cudaGraphExec_t wf_graph = nullptr;
   unsigned int wf_graph_slots = 0;
