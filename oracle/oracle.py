@@ -48,6 +48,7 @@ def lib():
         L.oracle_render_rows.argtypes = [vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp]
         L.oracle_light_count.argtypes = [vp]
         L.oracle_kerr_trace.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.oracle_kerr_trace_threads.argtypes = [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]
         L.oracle_kerr_disk_shade.argtypes = [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp]
         L.oracle_sample_hg.argtypes = [C.c_double, C.c_int, C.c_uint64, vp, C.c_int64, vp]
         _lib = L
@@ -137,18 +138,19 @@ class OracleScene:
         assert lib().oracle_radiance(self.h, _p(rays), rays.shape[0], seed, C.byref(prm), _p(out)) == 0
         return out
 
-    def kerr_trace(self, rays: np.ndarray):
+    def kerr_trace(self, rays: np.ndarray, threads: int = 1):
         """Kerr branch of intersect_scene per ray; status 0 background,
         1 entity hit, 2 event horizon, 4 step underflow, 5 entity ahead of the
         last step; with the hit point's colour and emission (the accretion
         disk rewrites them, drawing its alpha test from the scene stream
-        seeded with the black hole's disk_seed, one stream over the rays)."""
+        seeded with the black hole's disk_seed, one stream over the rays).
+        threads > 1 traces in parallel where no such disk is in the scene."""
         rays = np.ascontiguousarray(rays, dtype=np.float64)
         n = rays.shape[0]
         out = dict(status=np.empty(n, np.int32), final_bl=np.empty((n, 3)), exit_dir=np.empty((n, 3)),
                    steps=np.empty(n, np.int32), hit_entity=np.empty(n, np.int32), hit_t=np.empty(n),
                    hit_color=np.empty((n, 3)), hit_emission=np.empty((n, 3)))
-        rc = lib().oracle_kerr_trace(self.h, _p(rays), n, _p(out["status"]), _p(out["final_bl"]),
+        rc = lib().oracle_kerr_trace_threads(self.h, int(threads), _p(rays), n, _p(out["status"]), _p(out["final_bl"]),
                                      _p(out["exit_dir"]), _p(out["steps"]), _p(out["hit_entity"]),
                                      _p(out["hit_t"]), _p(out["hit_color"]), _p(out["hit_emission"]))
         assert rc == 0, rc

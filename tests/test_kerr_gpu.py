@@ -6,9 +6,13 @@ The kernel runs the reference's FP64 arithmetic in the reference's order
 (no FMA contraction); the GPU's sin / cos / acos / atan2 / pow may differ
 from the host libm in the last bit, so a ray whose step control sits on a
 knife edge may take another step sequence.  Bars: status equal on >= 99.5%
-of rays, exit direction within 1e-6 rad on >= 99% of rays (and every ray
-whose status agrees within 1e-3 rad), hit entities equal where both hit.
+of rays, exit direction within 1e-6 rad on >= 99.5% of the rays that leave
+or end on an entity (every ray beyond that bar is counted and printed with
+its angle), every ray whose status agrees within 1e-3 rad, hit entities
+equal where both hit.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -51,10 +55,14 @@ def _compare(k, st_ref, dir_ref, ent_ref, label):
     out = np.isin(st_ref, (0, 1, 5)) & valid
     frac_dir = float((ang[out] <= 1e-6).mean()) if out.any() else 1.0
     worst = ang[same & out].max() if (same & out).any() else 0.0
-    print(f"{label}: status agree {same.mean():.5f}, exit dir <=1e-6 rad {frac_dir:.5f} of {out.sum()}, "
-          f"max angle (same status) {worst:.3e}, median {np.median(ang[out]) if out.any() else 0:.3e}")
+    beyond = np.flatnonzero(out & (ang > 1e-6))
+    print(f"{label}: status agree {same.mean():.5f}, exit dir <=1e-6 rad {frac_dir:.5f} of {out.sum()} "
+          f"({len(beyond)} beyond), max angle (same status) {worst:.3e}, "
+          f"median {np.median(ang[out]) if out.any() else 0:.3e}")
+    if len(beyond):
+        print(f"  beyond 1e-6 rad: angles {np.sort(ang[beyond])[-8:]}, statuses {st_ref[beyond][:8]}")
     assert same.mean() >= 0.995
-    assert frac_dir >= 0.99
+    assert frac_dir >= 0.995
     assert worst <= 1e-3
     both = same & (st_ref == 1)
     assert np.array_equal(k["hit_entity"][both], ent_ref[both])
@@ -96,6 +104,19 @@ def test_kerr_lensing_view_matches_oracle(ctx, a):
     assert (np.abs(kb[:, 0] - ob[:, 0]) <= 1e-7 * ob[:, 0]).mean() >= 0.99
     dphi = np.abs((kb[:, 2] - ob[:, 2] + np.pi) % (2 * np.pi) - np.pi)
     assert (np.maximum(np.abs(kb[:, 1] - ob[:, 1]), dphi) <= 1e-6).mean() >= 0.99
+
+
+@pytest.mark.parametrize("a", [0.6, 0.999])
+def test_kerr_lensing_view_512x256_matches_oracle(ctx, a):
+    """The same lensing view at 512 x 256 rays (131,072 geodesics of up to
+    4000 steps each), FP64 form against the FP64 oracle."""
+    s = scenes.kerr_lensing(a=a, width=512, height=256, max_steps=4000)
+    rays = scenes.camera_rays(s)
+    ctx.upload(s)
+    k = ctx.kerr_trace(rays)
+    o = O.OracleScene(s).kerr_trace(rays, threads=os.cpu_count() or 1)
+    _compare(k, o["status"], o["exit_dir"], o["hit_entity"], f"lensing 512x256 a={a}")
+    assert (o["status"] == 1).sum() > 1000  # the disk is in view
 
 
 def test_kerr_escape_radius_option_matches_oracle(ctx):
@@ -220,6 +241,44 @@ def test_kerr_ray_bundle_jacobian_against_central_differences(ctx):
     assert np.quantile(rel, 0.95) < 1e-2
     assert np.isnan(J["jac_dir"][J["status"] != 0]).all()
     np.testing.assert_allclose(J["grad"][ok], np.einsum("ni,nij->nj", w[ok], J["jac_dir"][ok]), rtol=1e-12, atol=1e-14)
+
+
+def test_kerr_ray_bundle_jacobian_against_oracle_differences(ctx):
+    """The GPU's forward-mode Jacobian against central differences of the
+    FP64 oracle (the reference's arithmetic on the CPU) at perturbed initial
+    directions, h = 1e-6, for rays that leave the scene in all three traces:
+    the derivative of the reference's own map, not of the GPU's tracer."""
+    s = scenes.kerr_disk(24, 18, a=0.9, max_steps=1500)
+    rays = scenes.camera_rays(s)
+    ctx.upload(s)
+    n = rays.shape[0]
+    J = ctx.kerr_sensitivity(rays)
+    d = rays[:, 3:] / np.linalg.norm(rays[:, 3:], axis=1, keepdims=True)
+    up = np.where(np.abs(d[:, 2:3]) < 0.9, [[0.0, 0.0, 1.0]], [[1.0, 0.0, 0.0]])
+    e1 = np.cross(d, up)
+    e1 /= np.linalg.norm(e1, axis=1, keepdims=True)
+    e2 = np.cross(e1, d)
+    h = 1e-6
+    orc = O.OracleScene(s)
+    threads = os.cpu_count() or 1
+    fd = np.empty((n, 3, 2))
+    same = orc.kerr_trace(rays, threads=threads)["status"] == 0
+    for col, e in enumerate((e1, e2)):
+        outs = []
+        for sgn in (1.0, -1.0):
+            r = rays.copy()
+            dd = d + sgn * h * e
+            r[:, 3:] = dd / np.linalg.norm(dd, axis=1, keepdims=True)
+            outs.append(orc.kerr_trace(r, threads=threads))
+        fd[:, :, col] = (outs[0]["exit_dir"] - outs[1]["exit_dir"]) / (2 * h)
+        same &= (outs[0]["status"] == 0) & (outs[1]["status"] == 0)
+    ok = (J["status"] == 0) & same
+    assert ok.sum() > 100
+    rel = np.linalg.norm((J["jac_dir"] - fd)[ok], axis=(1, 2)) / np.linalg.norm(fd[ok], axis=(1, 2))
+    print(f"Kerr Jacobian vs oracle central differences over {ok.sum()} rays: median rel {np.median(rel):.2e}, "
+          f"p95 {np.quantile(rel, 0.95):.2e}")
+    assert np.median(rel) < 1e-4
+    assert np.quantile(rel, 0.95) < 1e-2
 
 
 def test_accretion_disk_shading_matches_oracle(ctx):
