@@ -209,17 +209,23 @@ def media_cornell(width: int = 128, height: int = 96, samples: int = 4, supersam
 
 
 def media_batch(n: int = 32, seed: int = 0, sizes=(128, 256, 384, 512, 768, 1024), samples: int = 16,
-                supersamples: int = 2, subdiv: int = 5):
+                supersamples: int = 2, subdiv: int = 5, bssrdf: bool = True):
     """n Cornell variants for one batched launch: a homogeneous medium with
     sigma_s U(0.05, 0.5), sigma_a 0.01 and HG g U(-0.6, 0.8) around a
-    20k-triangle displaced icosphere (subdiv 5), square images of uneven
-    sizes (128^2 .. 1024^2), 16 x 2^2 tent-filtered samples (64 spp)."""
+    20k-triangle displaced icosphere (subdiv 5) that is a directional-dipole
+    BSSRDF material (sigma_s' ~ 1, sigma_a ~ 0.01 per unit, relative index
+    1.3; diffuse with bssrdf=False), square images of uneven sizes
+    (128^2 .. 1024^2), 16 x 2^2 tent-filtered samples (64 spp)."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
         side = int(rng.choice(sizes))
-        s = media_cornell(side, side, samples, supersamples, sigma_s=float(rng.uniform(0.05, 0.5)), sigma_a=0.01,
-                          g=float(rng.uniform(-0.6, 0.8)), subdiv=subdiv, seed=seed)
+        # parameters rounded to 6 decimals, so that the reference's scene format holds them exactly
+        s = media_cornell(side, side, samples, supersamples, sigma_s=round(float(rng.uniform(0.05, 0.5)), 6),
+                          sigma_a=0.01, g=round(float(rng.uniform(-0.6, 0.8)), 6), subdiv=subdiv, seed=seed)
+        if bssrdf:
+            s.materials[s.entities[2].material] = Material.subsurface(
+                (0.9, 0.8, 0.7), sigma_s=(1.0, 0.95, 0.9), sigma_a=(0.01, 0.012, 0.015), eta=1.3, level=-2)
         s.settings.seed = seed + i
         out.append(s)
     return out

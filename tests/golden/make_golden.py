@@ -13,8 +13,11 @@ its build on the machine that runs them.
     python tests/golden/make_golden.py --sss-oracle
 
 writes sss_oracle.npz from the oracle alone (no reference build needed);
---disk-oracle, --sss-l1-oracle and --glossy-oracle write
-kerr_disk_oracle.npz, sss_l1_oracle.npz and glossy_oracle.npz the same way.
+--disk-oracle, --sss-l1-oracle, --glossy-oracle, --media-oracle,
+--mesh7-oracle and --batch-oracle write kerr_disk_oracle.npz,
+sss_l1_oracle.npz, glossy_oracle.npz, media_oracle.npz, mesh7_oracle.npz and
+batch_oracle.npz the same way; --media-only and --batch-only write the
+reference's own one-thread media and batch-variant renders.
 --scene-files-only writes the meshes and textures that the scene files in
 scene_files/ name, and scene_files.npz from the reference's renders of them.
 """
@@ -292,6 +295,42 @@ def media_oracle_golden(nb=16):
     np.savez_compressed(os.path.join(HERE, "media_oracle.npz"), **out)
 
 
+def batch_golden(d):
+    """media + BSSRDF batch variants rendered by the reference, one thread (bit-exact)"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import batch_cases
+    out = {}
+    for name, sc in batch_cases.one_thread_cases().items():
+        dd = os.path.join(d, "b_" + name)
+        os.makedirs(dd)
+        img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+        out[name] = img
+        print("batch", name, info)
+    np.savez_compressed(os.path.join(HERE, "batch_render.npz"), **out)
+
+
+def batch_oracle_golden(nb=16):
+    """16 independent 256-spp renders of each high-spp batch variant by the
+    oracle: per-pixel mean and spread"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import batch_cases
+    from oracle import oracle as O
+    out = {}
+    for i, sc in enumerate(batch_cases.highspp_variants()):
+        o = O.OracleScene(sc)
+        imgs = []
+        for k in range(nb):
+            sc.settings.seed = 100 + k
+            img, _, _ = o.render(threads=os.cpu_count(), settings=sc.settings)
+            imgs.append(img)
+        b = np.stack(imgs)
+        out[f"v{i}_mean"] = b.mean(0).astype(np.float32)
+        out[f"v{i}_sd"] = b.std(0, ddof=1).astype(np.float32)
+        print("batch oracle", i, sc.camera.width, float(b.mean()))
+    out["batches"] = np.int32(nb)
+    np.savez_compressed(os.path.join(HERE, "batch_oracle.npz"), **out)
+
+
 def mesh7_oracle_golden(nb=16):
     """The benchmarked scene itself (327,680-triangle displaced icosphere,
     diffuse and glass) at 128 x 96, 16 independent 256-spp renders by the
@@ -414,7 +453,7 @@ def _image_size(path):
 
 KNOWN_FLAGS = {"--kerr-only", "--disk-only", "--sss-only", "--sss-l1-only", "--glossy-only", "--sss-oracle",
                "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle", "--scene-files-only", "--media-only",
-               "--media-oracle", "--mesh7-oracle"}
+               "--media-oracle", "--mesh7-oracle", "--batch-only", "--batch-oracle"}
 
 
 def main():
@@ -426,6 +465,9 @@ def main():
         return
     if "--mesh7-oracle" in sys.argv:
         mesh7_oracle_golden()
+        return
+    if "--batch-oracle" in sys.argv:
+        batch_oracle_golden()
         return
     if "--sss-oracle" in sys.argv:
         sss_oracle_golden()
@@ -454,6 +496,10 @@ def main():
     if "--media-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             media_golden(d)
+        return
+    if "--batch-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            batch_golden(d)
         return
     if "--disk-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:

@@ -58,3 +58,43 @@ def test_autotuner_keeps_the_image(ctx):
     assert t["slots"] in (1 << 19, 1 << 20, 1 << 21, 1 << 22) and t["trace_blocks_per_sm"] in (4, 8, 16)
     after = ctx.render(s)
     assert np.array_equal(before, after)
+
+
+def test_batch_of_media_bssrdf_variants_matches_oracle_statistically(ctx, golden):
+    """Three variants of the batched workload (global HG medium, 20,480-
+    triangle directional-dipole icosphere) at uneven sizes, rendered together
+    by pr_render_batch, 16 batches of 256 spp, against the oracle's 16 x 256
+    spp per variant (the oracle is bit-exact with the reference on these
+    variants, one thread): per-pixel 3 sigma with both sides' spreads, RMSE at
+    the noise level, mean within 1 %."""
+    import torch
+    import batch_cases
+    variants = batch_cases.highspp_variants()
+    objs = [ctx.scene_object(s) for s in variants]
+    outs = [torch.zeros((s.camera.height, s.camera.width, 3), dtype=torch.float32, device="cuda:0") for s in variants]
+    nb, spp = 16, variants[0].settings.spp
+    acc = [[] for _ in variants]
+    for b in range(nb):
+        ctx.render_batch([(o, out, None, None, b * spp) for o, out in zip(objs, outs)])
+        torch.cuda.synchronize()
+        for i, out in enumerate(outs):
+            acc[i].append(out.cpu().numpy().astype(np.float64))
+    orc = golden["batch_oracle"]
+    o_nb = int(orc["batches"])
+    for i, s in enumerate(variants):
+        bt = np.stack(acc[i])
+        mean, sd = bt.mean(0), bt.std(0, ddof=1)
+        o_mean = orc[f"v{i}_mean"].astype(np.float64)
+        o_sd = orc[f"v{i}_sd"].astype(np.float64)
+        sigma = np.sqrt(sd ** 2 / nb + o_sd ** 2 / o_nb) + 1e-7
+        frac = float((np.abs(mean - o_mean) / sigma > 3.0).mean())
+        rmse = float(np.sqrt(((mean - o_mean) ** 2).mean()))
+        noise = float(np.sqrt((sigma ** 2).mean()))
+        rel = abs(mean.mean() - o_mean.mean()) / o_mean.mean()
+        print(f"batch variant {i} ({s.camera.width}^2): >3 sigma {frac:.4f}, rmse {rmse:.3e} vs noise {noise:.3e}, "
+              f"mean rel diff {rel:.4f}")
+        assert rel < 0.01
+        assert frac < 0.02
+        assert rmse < 1.3 * noise
+    for o in objs:
+        o.release()

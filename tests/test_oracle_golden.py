@@ -167,3 +167,15 @@ def test_hg_sampling_modes(g):
     cos_q = np.sort(O.sample_hg(g, False, 5, d, n) @ d)
     assert np.abs(cos_q).max() <= g * g + 1e-9
     assert np.max(np.abs(emp - _hg_cdf(np.clip(cos_q / (g * g), -1, 1), g))) < crit
+
+
+@pytest.mark.parametrize("name", ["variant0", "variant1"])
+def test_batch_variant_render_one_thread_bit_exact(golden, name):
+    # the batched workload's variants: a global HG medium around a
+    # 20,480-triangle directional-dipole BSSRDF icosphere
+    import batch_cases
+    sc = batch_cases.one_thread_cases()[name]
+    img, _, _ = O.OracleScene(sc).render(threads=1)
+    ref = golden["batch_render"][name]
+    assert np.array_equal(img, ref)
+    assert ref.mean() > 0
