@@ -448,6 +448,15 @@ int pr_image_to_rgb8(pr_ctx* ctx, const float* rgb, int32_t width, int32_t heigh
 int pr_image_to_rgb8_dev(pr_ctx* ctx, const float* rgb_dev, int32_t width, int32_t height, double gamma_offset,
                          uint8_t* out_dev);
 
+/* HDR output of an image (Render::OutputHdr, render.h:1649-1667, with
+ * HDRImage::HDRPixel, hdr.h:30-44): Radiance RGBE bytes, 4 per pixel (R, G, B
+ * mantissas and the exponent + 128; zero where max(R, G, B) <= 1e-32), the
+ * file's scanline order (scanline r = row r of pr_render's order).  in: W*H*3
+ * floats; out: W*H*4 bytes (4-byte aligned for _dev).  The header and the
+ * scanline framing are the writer's (prender_gb300.scene.write_hdr). */
+int pr_image_to_rgbe(pr_ctx* ctx, const float* rgb, int32_t width, int32_t height, uint8_t* out);
+int pr_image_to_rgbe_dev(pr_ctx* ctx, const float* rgb_dev, int32_t width, int32_t height, uint8_t* out_dev);
+
 /* Accretion-disk shading test hook: the texture, temperature and Doppler
  * branch of Circle::intersect under the black hole (circle.h:240-322, no
  * alpha test) at n world points of disk entity `entity`.  Host buffers:

@@ -13,6 +13,8 @@
 //                                                          with the hit point's colour and emission
 //   prender_ref radiance <scene.txt> <rays.f64> <out.f64> <seed>
 //                                                          radiance() roots (radiance.h:25)
+//   prender_ref hdr      <scene.txt> <image.f64> <out.hdr>  Render::OutputHdr (render.h:1649) of a given
+//                                                          image (the scene's size, W*H*3 doubles)
 //
 // The reference keeps members private; the harness opens them up for reading.
 #include <omp.h>
@@ -186,6 +188,20 @@ int main(int argc, char** argv) {
       fwrite(c, 8, 3, f);
     }
     fclose(f);
+    return 0;
+  }
+  if (cmd == "hdr" && argc >= 5) {
+    SceneEnv* env = load(argv[2]);
+    Render r(*env);
+    std::vector<double> img = read_f64(argv[3]);
+    const int w = env->image_width, h = env->image_height;
+    if ((int64_t)img.size() != (int64_t)w * h * 3) { fprintf(stderr, "image size mismatch\n"); return 3; }
+    // Run() allocates the image (render.h:1142); here it is given
+    struct RenderView { SceneEnv* env_p; Color* image; };
+    Color* image = new Color[(size_t)w * h];
+    for (int i = 0; i < w * h; i++) image[i] = Color(img[3 * i], img[3 * i + 1], img[3 * i + 2]);
+    reinterpret_cast<RenderView*>(&r)->image = image;
+    r.OutputHdr(argv[4]);
     return 0;
   }
   fprintf(stderr, "bad command\n");

@@ -966,6 +966,37 @@ int pr_image_to_rgb8(pr_ctx* c, const float* rgb, int32_t width, int32_t height,
   return PR_OK;
 }
 
+int pr_image_to_rgbe_dev(pr_ctx* c, const float* rgb_dev, int32_t width, int32_t height, uint8_t* out_dev) {
+  if (!c) return PR_E_ARG;
+  if (width <= 0 || height <= 0 || (int64_t)width * height > ((int64_t)1 << 30)) return fail(c, PR_E_ARG, "bad image size");
+  if (!rgb_dev || !out_dev) return fail(c, PR_E_ARG, "null image buffer");
+  if (((uintptr_t)out_dev & 3) != 0) return fail(c, PR_E_ARG, "the RGBE buffer must be 4-byte aligned");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
+  PR_CUDA(c, launch_to_rgbe(rgb_dev, width, height, out_dev, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PR_OK;
+}
+
+int pr_image_to_rgbe(pr_ctx* c, const float* rgb, int32_t width, int32_t height, uint8_t* out) {
+  if (!c) return PR_E_ARG;
+  if (width <= 0 || height <= 0 || (int64_t)width * height > ((int64_t)1 << 30)) return fail(c, PR_E_ARG, "bad image size");
+  if (!rgb || !out) return fail(c, PR_E_ARG, "null image buffer");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();
+  const size_t n = (size_t)width * height;
+  // staging in the context's ray buffer: the float image, then the RGBE pixels
+  PR_CUDA(c, c->rays.ensure(n * 3 * sizeof(float) + n * 4));
+  float* d_in = (float*)c->rays.p;
+  uint8_t* d_out = (uint8_t*)(d_in + 3 * n);
+  PR_CUDA(c, cudaMemcpyAsync(d_in, rgb, n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  const int st = pr_image_to_rgbe_dev(c, d_in, width, height, d_out);
+  if (st != PR_OK) return st;
+  PR_CUDA(c, cudaMemcpyAsync(out, d_out, n * 4, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PR_OK;
+}
+
 // the scene has a disk_map disk under its black hole (shaded from the disk texture)
 static bool has_kerr_disk(const SceneObjData& o) {
   for (const GEntity& e : o.host.ents)

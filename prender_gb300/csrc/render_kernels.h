@@ -33,6 +33,8 @@ cudaError_t launch_reduce(const float* partial, float* dst, int n3, int chunks, 
 // 8-bit bitmap rows of a float image (output.cu)
 cudaError_t launch_to_rgb8(const float* rgb, int width, int height, double gamma_offset, uint8_t* out,
                            cudaStream_t stream);
+// Radiance RGBE pixels for the HDR writer (output.cu)
+cudaError_t launch_to_rgbe(const float* rgb, int width, int height, uint8_t* out, cudaStream_t stream);
 cudaError_t launch_trace_fast(const DevScene& S, const double* rays, int64_t n, int32_t* ent, int32_t* prim, double* t,
                               uint32_t* err, cudaStream_t stream);
 cudaError_t launch_first_hit(const DevScene& S, const double* rays, int64_t n, int32_t* ent, int32_t* prim, double* t,

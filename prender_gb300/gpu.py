@@ -216,6 +216,16 @@ class Context:
         self._check(self.L.pr_image_to_rgb8(self.h, _p(img), w, h, float(gamma_offset), _p(out)))
         return out
 
+    def to_rgbe(self, image: np.ndarray) -> np.ndarray:
+        """Render::OutputHdr's Radiance RGBE pixels of an (H, W, 3) float image
+        in pr_render's row order; returns (H, W, 4) uint8, scanline r = image
+        row r (write with scene.write_hdr)."""
+        img = np.ascontiguousarray(image, dtype=np.float32)
+        h, w = img.shape[0], img.shape[1]
+        out = np.empty((h, w, 4), np.uint8)
+        self._check(self.L.pr_image_to_rgbe(self.h, _p(img), w, h, _p(out)))
+        return out
+
     def kerr_disk_shade(self, entity: int, points: np.ndarray) -> dict:
         """The accretion disk's texture / temperature / Doppler shading at
         world points of disk entity (no alpha test): valid, colour,

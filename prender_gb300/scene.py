@@ -527,6 +527,29 @@ def _rgba(tex) -> np.ndarray:
     return np.ascontiguousarray(t)
 
 
+def write_hdr(path: str, rgbe: np.ndarray) -> None:
+    """Writes a Radiance .hdr file from (H, W, 4) RGBE bytes in scanline order
+    (what Context.to_rgbe returns) as HDRImage::save does (hdr.h:213-246):
+    the same header lines, '-Y H +X W', then per scanline the new-style
+    marker 2 2 and the width, and each of the four byte planes as literal
+    runs of at most 127 bytes."""
+    q = np.ascontiguousarray(rgbe, dtype=np.uint8)
+    h, w = q.shape[0], q.shape[1]
+    out = bytearray()
+    out += b"#?RADIANCE\n# Made with 100% pure HDR Shop\nFORMAT=32-bit_rle_rgbe\nEXPOSURE=1.0000000000000\n\n"
+    out += f"-Y {h} +X {w}\n".encode()
+    for r in range(h):
+        out += bytes((2, 2, (w >> 8) & 0xFF, w & 0xFF))
+        for c in range(4):
+            plane = q[r, :, c].tobytes()
+            for k in range(0, w, 127):
+                chunk = plane[k:k + 127]
+                out.append(len(chunk))
+                out += chunk
+    with open(path, "wb") as f:
+        f.write(bytes(out))
+
+
 def write_bmp(path: str, rgb8: np.ndarray) -> None:
     """Writes a 24-bit BMP from (H, W, 3) uint8 rows in the bitmap's
     cell(i, j) order (what Context.to_rgb8 returns), as Render::OutputBmp's

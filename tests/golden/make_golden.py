@@ -17,7 +17,8 @@ writes sss_oracle.npz from the oracle alone (no reference build needed);
 --mesh7-oracle and --batch-oracle write kerr_disk_oracle.npz,
 sss_l1_oracle.npz, glossy_oracle.npz, media_oracle.npz, mesh7_oracle.npz and
 batch_oracle.npz the same way; --media-only and --batch-only write the
-reference's own one-thread media and batch-variant renders.
+reference's own one-thread media and batch-variant renders, --hdr-only its
+Render::OutputHdr file of a seeded image.
 --scene-files-only writes the meshes and textures that the scene files in
 scene_files/ name, and scene_files.npz from the reference's renders of them.
 """
@@ -295,6 +296,25 @@ def media_oracle_golden(nb=16):
     np.savez_compressed(os.path.join(HERE, "media_oracle.npz"), **out)
 
 
+def hdr_golden(d):
+    """Render::OutputHdr of a seeded image by the reference: the image (float32,
+    as pr_render returns it) and the file's bytes"""
+    rng = np.random.default_rng(11)
+    w, h = 300, 23  # wider than one 127-byte literal run, two bytes of width
+    img = np.exp(rng.uniform(np.log(1e-6), np.log(50.0), (h, w, 3))).astype(np.float32)
+    img[0, :5] = 0.0                   # black
+    img[1, :3] = (1e-33, 0.0, 0.0)     # below the 1e-32 cut
+    img[2, :4] = (1.0, 0.5, 0.25)      # exact powers of two
+    img[3, :2] = (255.9, 1.0, 0.001)
+    sc = scenes.cornell_spheres(width=w, height=h, samples=1, supersamples=1)
+    p = sc.write_reference(d)
+    img.astype(np.float64).reshape(-1, 3).tofile(os.path.join(d, "img.f64"))
+    run_ref(["hdr", p, os.path.join(d, "img.f64"), os.path.join(d, "out.hdr")], d)
+    data = np.frombuffer(open(os.path.join(d, "out.hdr"), "rb").read(), np.uint8)
+    np.savez_compressed(os.path.join(HERE, "hdr_output.npz"), image=img, hdr=data)
+    print("hdr bytes", data.size)
+
+
 def batch_golden(d):
     """media + BSSRDF batch variants rendered by the reference, one thread (bit-exact)"""
     sys.path.insert(0, os.path.dirname(HERE))
@@ -453,7 +473,7 @@ def _image_size(path):
 
 KNOWN_FLAGS = {"--kerr-only", "--disk-only", "--sss-only", "--sss-l1-only", "--glossy-only", "--sss-oracle",
                "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle", "--scene-files-only", "--media-only",
-               "--media-oracle", "--mesh7-oracle", "--batch-only", "--batch-oracle"}
+               "--media-oracle", "--mesh7-oracle", "--batch-only", "--batch-oracle", "--hdr-only"}
 
 
 def main():
@@ -496,6 +516,10 @@ def main():
     if "--media-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             media_golden(d)
+        return
+    if "--hdr-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            hdr_golden(d)
         return
     if "--batch-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
