@@ -113,7 +113,8 @@ void pr_destroy(pr_ctx* c) {
                     &c->out, &c->rays, &c->ires, &c->jres, &c->dres, &c->wf_o, &c->wf_d, &c->wf_beta, &c->wf_dpw,
                     &c->wf_L, &c->wf_sample, &c->wf_hit, &c->wf_hitv, &c->wf_nee, &c->wf_sho, &c->wf_shd, &c->wf_extq,
                     &c->wf_shq, &c->wf_spo, &c->wf_spd, &c->wf_spb, &c->wf_spw, &c->wf_sps, &c->wf_samp, &c->wf_live,
-                    &c->wf_pix, &c->wf_ctl})
+                    &c->wf_pix, &c->wf_ctl, &c->wf_frc, &c->wf_fre, &c->wf_frs, &c->wf_frl, &c->wf_spf,
+                    &c->wf_neef})
     b->release();
   if (c->wf_graph) cudaGraphExecDestroy(c->wf_graph);
   if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
@@ -459,9 +460,8 @@ int pr::prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* 
                 "UVPlane axes randomPoint reads, circle.h:110-134); render it without next-event estimation");
   if (sc.kerr.enabled && (p->nee || (p->media && sc.host.medium.on)))
     return fail(c, PR_E_UNSUPPORTED, "Kerr scenes render without next-event estimation and media");
-  if (sc.dev.has_sss && (p->mode == PR_MODE_WAVEFRONT || sc.kerr.enabled))
-    return fail(c, PR_E_UNSUPPORTED,
-                "subsurface (dipole) materials render in the plain form (PR_MODE_MEGAKERNEL) of straight-ray scenes");
+  if (sc.dev.has_sss && sc.kerr.enabled)
+    return fail(c, PR_E_UNSUPPORTED, "subsurface (dipole) materials render in straight-ray scenes only");
   memset(&g, 0, sizeof(g));
   double dir[3] = {cam->dir[0], cam->dir[1], cam->dir[2]};
   double phi = std::atan2(dir[1], dir[0]);
@@ -546,9 +546,13 @@ static unsigned int wavefront_slots() {
 static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int accumulate) {
   const unsigned int P = c->tuned_slots ? c->tuned_slots : wavefront_slots();
   const uint64_t wh = (uint64_t)g.width * g.height;
-  const uint64_t max_pass = 64ull << 20;  // camera samples per pass (sample table 28 B each)
+  // camera samples per pass (sample table 28 B each); subsurface scenes take
+  // smaller passes, whose frames (72 B each) come from a per-pass pool
+  const bool sss = c->cur.dev.has_sss != 0;
+  const uint64_t max_pass = sss ? (4ull << 20) : (64ull << 20);
   uint64_t layers = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.spp, max_pass / wh));
   const uint64_t pass_cap = layers * wh;
+  const uint64_t frame_cap = sss ? std::min<uint64_t>(8 * pass_cap, 1ull << 30) : 0;
   const size_t f4 = sizeof(float4);
   PR_CUDA(c, c->wf_o.ensure(f4 * P));
   PR_CUDA(c, c->wf_d.ensure(f4 * P));
@@ -573,6 +577,14 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   PR_CUDA(c, c->wf_live.ensure(4ull * pass_cap));
   PR_CUDA(c, c->wf_pix.ensure(24ull * wh));
   PR_CUDA(c, c->wf_ctl.ensure(sizeof(WfCtl)));
+  if (sss) {
+    PR_CUDA(c, c->wf_frc.ensure(24ull * frame_cap));
+    PR_CUDA(c, c->wf_fre.ensure(24ull * frame_cap));
+    PR_CUDA(c, c->wf_frs.ensure(f4 * frame_cap));
+    PR_CUDA(c, c->wf_frl.ensure(8ull * frame_cap));
+    PR_CUDA(c, c->wf_spf.ensure(4ull * spawn_cap));
+    PR_CUDA(c, c->wf_neef.ensure(4ull * P));
+  }
   if (!c->wf_host_ctl) PR_CUDA(c, cudaMallocHost((void**)&c->wf_host_ctl, sizeof(WfCtl)));
   WfBufs B{};
   B.o = (float4*)c->wf_o.p;
@@ -597,6 +609,13 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   B.live = (int*)c->wf_live.p;
   B.pix = (long long*)c->wf_pix.p;
   B.ctl = (WfCtl*)c->wf_ctl.p;
+  B.fr_c = sss ? (long long*)c->wf_frc.p : nullptr;
+  B.fr_e = sss ? (long long*)c->wf_fre.p : nullptr;
+  B.fr_scale = sss ? (float4*)c->wf_frs.p : nullptr;
+  B.fr_link = sss ? (int2*)c->wf_frl.p : nullptr;
+  B.sp_frame = sss ? (int*)c->wf_spf.p : nullptr;
+  B.neef = sss ? (int*)c->wf_neef.p : nullptr;
+  B.frame_cap = (unsigned int)frame_cap;
   B.err = (uint32_t*)c->errword.p;
   B.counters = (unsigned long long*)c->counters.p;
   B.n_slots = P;
@@ -604,6 +623,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   B.max_iterations = 20000u;  // bounded device loop; a frame needs a few hundred
   WfLaunch L;
   L.shade_blocks = (P + 127) / 128;
+  L.sss = sss ? 1 : 0;
   // persistent traversal: one resident wave of blocks (more waves only queue
   // behind it and find the rays taken)
   int sms = 0;
@@ -612,13 +632,18 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   L.trace_blocks = std::min<unsigned int>((P + 127) / 128, (unsigned int)sms * bps);
   PR_CUDA(c, cudaMemsetAsync(c->wf_nee.p, 0, f4 * 3 * P, c->stream));
   PR_CUDA(c, cudaMemsetAsync(B.pix, 0, 24ull * wh, c->stream));
+  if (sss) {
+    PR_CUDA(c, cudaMemsetAsync(B.neef, 0xFF, 4ull * P, c->stream));  // -1: no frame takes shadow terms
+    PR_CUDA(c, cudaMemsetAsync(c->wf_L.p, 0, f4 * P, c->stream));   // the frame lane of every slot: none
+  }
   // PR_WF_HOST_LOOP=1 drives the iterations from the host instead of the
   // graph's device-side while loop: profilers that cannot see kernels inside
   // conditional graph nodes see every launch this way (same kernels, same work)
   const char* host_loop = getenv("PR_WF_HOST_LOOP");
   const bool use_graph = !(host_loop && host_loop[0] == '1') && !c->force_host_loop;
   if (use_graph && !c->wf_graph_failed &&
-      (!c->wf_graph || c->wf_graph_slots != P || c->wf_graph_trace_blocks != L.trace_blocks)) {
+      (!c->wf_graph || c->wf_graph_slots != P || c->wf_graph_trace_blocks != L.trace_blocks ||
+       c->wf_graph_sss != L.sss)) {
     if (c->wf_graph) {
       cudaStreamSynchronize(c->stream);  // the previous render's launch has finished with it
       cudaGraphExecDestroy(c->wf_graph);
@@ -632,6 +657,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
     } else {
       c->wf_graph_slots = P;
       c->wf_graph_trace_blocks = L.trace_blocks;
+      c->wf_graph_sss = L.sss;
     }
   }
   c->wf_passes = 0;

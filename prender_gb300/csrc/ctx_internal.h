@@ -67,10 +67,12 @@ struct pr_ctx {
   // wavefront pool
   pr::DevBuf wf_o, wf_d, wf_beta, wf_dpw, wf_L, wf_sample, wf_hit, wf_hitv, wf_nee, wf_sho, wf_shd, wf_extq, wf_shq;
   pr::DevBuf wf_spo, wf_spd, wf_spb, wf_spw, wf_sps, wf_samp, wf_live, wf_pix, wf_ctl;
+  pr::DevBuf wf_frc, wf_fre, wf_frs, wf_frl, wf_spf, wf_neef;  // subsurface frames (wavefront form)
   unsigned int wf_slots = 0;
   cudaGraphExec_t wf_graph = nullptr;
   unsigned int wf_graph_slots = 0;
   unsigned int wf_graph_trace_blocks = 0;
+  int wf_graph_sss = 0;              // the graph launches the subsurface shading kernel
   unsigned int tuned_slots = 0;      // autotuner's wavefront pool size (0: default)
   unsigned int tuned_trace_bps = 0;  // autotuner's traversal blocks per SM (0: default)
   bool force_host_loop = false;      // the autotuner times candidates with the host-driven loop

@@ -133,6 +133,76 @@ __device__ void end_path(const WfBufs& B, const RenderCfg& cfg, const PathState&
   }
 }
 
+// ---- subsurface frames of the wavefront form -------------------------------
+// The plain form keeps a sample's frames in registers (render.cu); here the
+// branches of one camera sample run in different slots at the same time, so
+// the frames live in the pool: fixed-point sums (the cut decision then does
+// not depend on the order in which branches end) and a count of open
+// branches and inner frames, the last of which closes the frame.
+
+__device__ __forceinline__ void fx_add3(long long* p, float3 v) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(p + 0), (unsigned long long)__float2ll_rn(v.x * kSampleScale));
+  atomicAdd(reinterpret_cast<unsigned long long*>(p + 1), (unsigned long long)__float2ll_rn(v.y * kSampleScale));
+  atomicAdd(reinterpret_cast<unsigned long long*>(p + 2), (unsigned long long)__float2ll_rn(v.z * kSampleScale));
+}
+
+__device__ __forceinline__ float3 fx_read3(const long long* p) {
+  const volatile long long* v = p;
+  return f3((float)((double)v[0] * kSampleInv), (float)((double)v[1] * kSampleInv), (float)((double)v[2] * kSampleInv));
+}
+
+// radiance x of a branch (or of a closing frame) goes to frame f, or to the camera sample
+__device__ __forceinline__ void frame_add(const WfBufs& B, int f, uint64_t g, float3 x) {
+  if (x.x == 0.0f && x.y == 0.0f && x.z == 0.0f) return;
+  fx_add3(f >= 0 ? B.fr_c + 3 * (size_t)f : B.samp + 3 * g, x);
+}
+
+// a new frame inside parent with one open item (the branch that opens it)
+__device__ int frame_alloc(const WfBufs& B, int parent, float3 scale, float thr, float3 e, float3 c) {
+  const unsigned int f = atomicAdd(&B.ctl->frame_next, 1u);
+  if (f >= B.frame_cap) {
+    atomicOr(B.err, PR_DEV_QUEUE_OVERFLOW);
+    return -2;
+  }
+  long long* pc = B.fr_c + 3 * (size_t)f;
+  long long* pe = B.fr_e + 3 * (size_t)f;
+  pc[0] = __float2ll_rn(c.x * kSampleScale);
+  pc[1] = __float2ll_rn(c.y * kSampleScale);
+  pc[2] = __float2ll_rn(c.z * kSampleScale);
+  pe[0] = __float2ll_rn(e.x * kSampleScale);
+  pe[1] = __float2ll_rn(e.y * kSampleScale);
+  pe[2] = __float2ll_rn(e.z * kSampleScale);
+  B.fr_scale[f] = make_float4(scale.x, scale.y, scale.z, thr);
+  B.fr_link[f] = make_int2(parent, 1);
+  return (int)f;
+}
+
+// one open item of frame f (-1: of the camera sample g) ended: close every
+// frame that has nothing open left (its C + E to its parent unless
+// |C / scale| exceeds its bound), and finish the sample when its last item ends
+__device__ void frame_release(const WfBufs& B, const RenderCfg& cfg, int f, uint64_t g) {
+  for (int level = 0; level < 64; level++) {
+    __threadfence();  // this item's sums before its count
+    if (f < 0) {
+      if (atomicSub(B.live + g, 1) == 1) {
+        __threadfence();
+        add_to_pixel(B, cfg, g, fx_read3(B.samp + 3 * g));
+      }
+      return;
+    }
+    if (atomicSub(&B.fr_link[f].y, 1) != 1) return;
+    __threadfence();
+    const float3 c = fx_read3(B.fr_c + 3 * (size_t)f), e = fx_read3(B.fr_e + 3 * (size_t)f);
+    const float4 sc = B.fr_scale[f];
+    const float3 q = f3(sc.x != 0.0f ? c.x / sc.x : 0.0f, sc.y != 0.0f ? c.y / sc.y : 0.0f,
+                        sc.z != 0.0f ? c.z / sc.z : 0.0f);
+    const int parent = B.fr_link[f].x;
+    if (!(sqrtf(dot(q, q)) > sc.w)) frame_add(B, parent, g, c + e);
+    f = parent;
+  }
+  atomicOr(B.err, PR_DEV_LOOP_CAP);
+}
+
 __global__ void __launch_bounds__(256) wf_reset(unsigned int n_slots) {
   const WfBufs& B = c_buf;
   const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -150,13 +220,16 @@ __global__ void __launch_bounds__(256) wf_reset(unsigned int n_slots) {
     c->iterations = 0;
     c->work = 1;
     c->head_start = 0;
+    c->frame_next = 0;
   }
 }
 
-// 6 blocks of 128 per SM (80 registers, a few spilled): measured on GB300
-// over 4 / 5 / 6 / 7 / 8 / 10 blocks, mesh Cornell box 1024x768x64 spp,
-// wf_shade 108 / 99 / 94 / 96 / 102 / 110 ms per frame
-__global__ void __launch_bounds__(128, 6) wf_shade() {
+// One iteration's shading of every slot.  SSS: scenes with subsurface
+// materials (the fuller shade() with the dipole and the single-scattering
+// walk, and the frames above); every camera sample then ends through its
+// sample slot, since frames may take radiance from any of its branches.
+template <bool SSS>
+__device__ __forceinline__ void wf_shade_impl() {
   const DevScene& S = c_scene;
   const RenderCfg& cfg = c_cfg;
   const WfBufs& B = c_buf;
@@ -173,6 +246,8 @@ __global__ void __launch_bounds__(128, 6) wf_shade() {
     uint64_t g = 0;
     bool has_ray = false;
     int n_shadow = 0;
+    int fr = -1;      // the slot's innermost subsurface frame (SSS)
+    int nee_to = -1;  // where this vertex's shadow terms go (SSS: a frame's E, or the path)
     if (i < B.n_slots) {
       state = __float_as_int(B.d[i].w) >> 1;
       was_free = state == SLOT_FREE;
@@ -180,9 +255,18 @@ __global__ void __launch_bounds__(128, 6) wf_shade() {
         load_state(B, i, ps);
         g = B.sample[i];
         // shadow rays of the previous vertex that were not blocked
+        float3 nee = f3(0, 0, 0);
         for (int k = 0; k < 3; k++) {
           const float4 c = B.nee[3 * i + k];
-          ps.L += f3(c.x, c.y, c.z);
+          nee += f3(c.x, c.y, c.z);
+        }
+        if (SSS) {
+          fr = __float_as_int(B.L[i].w) - 1;
+          const int nf = B.neef[i];
+          if (nf >= 0) frame_add(B, nf, g, nee);  // the frame-opening vertex's own terms
+          else ps.L += nee;
+        } else {
+          ps.L += nee;
         }
         const float4 h4 = B.hit[i];
         FastHit h;
@@ -198,7 +282,37 @@ __global__ void __launch_bounds__(128, 6) wf_shade() {
         ShadowReq sh[3];
         int nsh = 0;
         PathState child;
-        const int r = shade(S, cfg, ps, h.ent >= 0, h, sample_id, sh, nsh, child, B.err);
+        int r;
+        if (SSS) {
+          const float3 Lb = ps.L;
+          SssFrameOut fo;
+          fo.open = 0;
+          r = shade<true, true>(S, cfg, ps, h.ent >= 0, h, sample_id, sh, nsh, child, B.err, nullptr, nullptr,
+                                nullptr, &fo);
+          if (fo.open) {
+            // the branch moves into a new frame (or two nested ones): what it
+            // gathered before this vertex belongs outside, the vertex's own
+            // terms to the frame, its continuation inside (render.cu does the same)
+            frame_add(B, fr, g, Lb);
+            const int f = frame_alloc(B, fr, fo.scale, fo.thr, ps.L - Lb, fo.open == 1 ? fo.inner : f3(0, 0, 0));
+            int in = f;
+            if (f >= 0 && fo.open == 2) in = frame_alloc(B, f, fo.scale2, fo.thr2, f3(0, 0, 0), fo.inner);
+            if (f >= 0 && in >= 0) {
+              nee_to = fo.nee_inner ? -1 : f;
+              ps.L = f3(0, 0, 0);
+              fr = in;
+            } else {
+              r = SHADE_END;  // frames exhausted (reported): the branch ends
+              nsh = 0;
+            }
+          }
+          if (r == SHADE_END && nsh > 0) {  // shadow terms are only queued for continuing paths
+            atomicOr(B.err, PR_DEV_BAD_INDEX);
+            nsh = 0;
+          }
+        } else {
+          r = shade(S, cfg, ps, h.ent >= 0, h, sample_id, sh, nsh, child, B.err);
+        }
         for (int k = 0; k < 3; k++) {
           if (k < nsh) {
             B.nee[3 * i + k] = make_float4(sh[k].contrib.x, sh[k].contrib.y, sh[k].contrib.z, 0.0f);
@@ -209,7 +323,8 @@ __global__ void __launch_bounds__(128, 6) wf_shade() {
           }
         }
         if (r == SHADE_SPLIT) {
-          atomicAdd(B.live + g, 1);
+          if (SSS && fr >= 0) atomicAdd(&B.fr_link[fr].y, 1);
+          else atomicAdd(B.live + g, 1);
           const unsigned int t = atomicAdd(&ctl->spawn_tail, 1u);
           // entries from head_start on may still be unread this iteration
           if (t - head_start >= B.spawn_cap) {
@@ -221,10 +336,16 @@ __global__ void __launch_bounds__(128, 6) wf_shade() {
             B.sp_beta[q] = make_float4(child.beta.x, child.beta.y, child.beta.z, __uint_as_float(child.branch));
             B.sp_dpw[q] = make_float4(child.dpw.x, child.dpw.y, child.dpw.z, __uint_as_float(child.draws));
             B.sp_sample[q] = g;
+            if (SSS) B.sp_frame[q] = fr;
           }
         }
         if (r == SHADE_END) {
-          end_path(B, cfg, ps, g);
+          if (SSS) {
+            frame_add(B, fr, g, ps.L);
+            frame_release(B, cfg, fr, g);
+          } else {
+            end_path(B, cfg, ps, g);
+          }
           state = SLOT_FREE;
         } else {
           has_ray = true;
@@ -247,6 +368,7 @@ __global__ void __launch_bounds__(128, 6) wf_shade() {
           ps.draws = __float_as_uint(w.w);
           ps.L = f3(0, 0, 0);
           g = B.sp_sample[q];
+          if (SSS) fr = B.sp_frame[q];
           has_ray = true;
         } else if (samples_left) {
           const unsigned long long s = atomicAdd(&ctl->next_sample, 1ull);
@@ -259,6 +381,7 @@ __global__ void __launch_bounds__(128, 6) wf_shade() {
             camera_ray(cfg, x, y, kg, o, d);
             root_path(ps, o, d);
             B.live[g] = 1;
+            fr = -1;
             has_ray = true;
           }
         }
@@ -266,6 +389,10 @@ __global__ void __launch_bounds__(128, 6) wf_shade() {
       if (has_ray) {
         store_state(B, i, ps, SLOT_RAY);
         B.sample[i] = g;
+        if (SSS) {
+          B.L[i].w = __int_as_float(fr + 1);
+          B.neef[i] = nee_to;
+        }
       } else if (!was_free) {  // its path ended and nothing refilled it
         B.d[i] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(SLOT_FREE << 1));
       }
@@ -278,6 +405,12 @@ __global__ void __launch_bounds__(128, 6) wf_shade() {
     for (int k = 0; k < n_shadow; k++) B.shq[qs + k] = 3 * i + k;
   }
 }
+
+// 6 blocks of 128 per SM (80 registers, a few spilled): measured on GB300
+// over 4 / 5 / 6 / 7 / 8 / 10 blocks, mesh Cornell box 1024x768x64 spp,
+// wf_shade 108 / 99 / 94 / 96 / 102 / 110 ms per frame
+__global__ void __launch_bounds__(128, 6) wf_shade() { wf_shade_impl<false>(); }
+__global__ void __launch_bounds__(128, 3) wf_shade_sss() { wf_shade_impl<true>(); }
 
 // Persistent traversal with ray replacement (Aila & Laine 2009, "Understanding
 // the efficiency of ray traversal on GPUs", dynamic ray fetch): the lanes of a
@@ -544,8 +677,13 @@ cudaError_t wf_set_constants(const DevScene& S, const RenderCfg& cfg, const WfBu
   return e;
 }
 
+static void launch_shade(const WfLaunch& L, cudaStream_t s) {
+  if (L.sss) wf_shade_sss<<<L.shade_blocks, 128, 0, s>>>();
+  else wf_shade<<<L.shade_blocks, 128, 0, s>>>();
+}
+
 static void launch_body(const WfLaunch& L, cudaGraphConditionalHandle handle, int use_graph, cudaStream_t s) {
-  wf_shade<<<L.shade_blocks, 128, 0, s>>>();
+  launch_shade(L, s);
   wf_extend<<<L.trace_blocks, 128, 0, s>>>();
   wf_shadow<<<L.trace_blocks, 128, 0, s>>>();
   wf_control<<<1, 1, 0, s>>>(handle, use_graph);
@@ -597,7 +735,7 @@ cudaError_t wf_run_host_loop(const WfLaunch& L, WfCtl* host_ctl_pinned, const Wf
   for (int it = 0; it < (1 << 20) && e == cudaSuccess; it += kCheck) {
     for (int k = 0; k < kCheck; k++) {
       if (kernel_ms) cudaEventRecord(ev[k][0], s);
-      wf_shade<<<L.shade_blocks, 128, 0, s>>>();
+      launch_shade(L, s);
       if (kernel_ms) cudaEventRecord(ev[k][1], s);
       wf_extend<<<L.trace_blocks, 128, 0, s>>>();
       if (kernel_ms) cudaEventRecord(ev[k][2], s);

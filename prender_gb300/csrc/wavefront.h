@@ -26,6 +26,8 @@ struct WfCtl {
   unsigned int ext_fetch;    // extension rays taken by wf_extend's lanes so far
   unsigned int sh_fetch;     // shadow rays taken by wf_shadow's lanes so far
   unsigned long long next_sample;
+  unsigned int frame_next;   // subsurface frames handed out this pass
+  unsigned int pad;
 };
 
 // structure-of-arrays path pool (P slots) and queues
@@ -42,6 +44,19 @@ struct WfBufs {
   int* live;                        // branches still running per camera sample
   long long* pix;                   // 3 per pixel: fixed-point image
   WfCtl* ctl;
+  // subsurface frames (scenes with dipole materials): a vertex whose radiance
+  // the reference bounds (OVER_RADIANCE_CUT2 / 3 / 0) opens a frame; the
+  // radiance of everything inside it collects in fr_c (fixed point), its own
+  // terms in fr_e, and when its last branch or inner frame ends the frame
+  // passes C + E to its parent unless |C / scale| > thr
+  long long* fr_c;                  // 3 per frame
+  long long* fr_e;                  // 3 per frame
+  float4* fr_scale;                 // scale, thr
+  int2* fr_link;                    // parent (-1: the camera sample), open branches and frames
+  int* sp_frame;                    // frame of each waiting glass branch (-1: none)
+  int* neef;                        // per slot: the frame whose E takes the pending shadow terms (-1: the path)
+  unsigned int frame_cap;
+  unsigned int frame_pad;
   uint32_t* err;
   unsigned long long* counters;     // paths, segments, nodes, triangle tests, extension segments,
                                     // iterations, shadow rays, shadow nodes, shadow triangle tests
@@ -56,6 +71,7 @@ struct WfBufs {
 struct WfLaunch {
   unsigned int shade_blocks;
   unsigned int trace_blocks;
+  int sss;  // the scene has subsurface materials: the fuller shading kernel with frames
 };
 
 cudaError_t wf_set_constants(const DevScene& S, const RenderCfg& cfg, const WfBufs& B, cudaStream_t s);

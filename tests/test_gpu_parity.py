@@ -128,8 +128,9 @@ def test_image_matches_reference_statistically(ctx, golden, name, build, tol_fra
     assert rmse < 1.3 * noise
 
 
-def test_subsurface_image_matches_reference_statistically(ctx, golden):
-    """Directional-dipole BSSRDF in the plain form, 16 x 512 spp.
+@pytest.mark.parametrize("mode", [A.PR_MODE_MEGAKERNEL, A.PR_MODE_WAVEFRONT])
+def test_subsurface_image_matches_reference_statistically(ctx, golden, mode):
+    """Directional-dipole BSSRDF in both forms, 16 x 512 spp.
 
     Against the oracle's 16 x 512 spp (the oracle is bit-exact with the
     reference on one thread): both sides are 8192-spp means with measured
@@ -140,7 +141,7 @@ def test_subsurface_image_matches_reference_statistically(ctx, golden):
     3 sigma there (all with the image above the mean), so that comparison is
     bounded at 5 %, with its mean and RMSE held to the usual bars."""
     s = scenes.sss_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3)
-    s.settings.mode = A.PR_MODE_MEGAKERNEL
+    s.settings.mode = mode
     ctx.upload(s)
     nb, spp = 16, s.settings.spp
     b = _batches(ctx, s, nb, spp)
@@ -171,9 +172,6 @@ def test_subsurface_image_matches_reference_statistically(ctx, golden):
     assert rel < 0.01
     assert frac < 0.05
     assert rmse < 1.3 * noise
-    s.settings.mode = A.PR_MODE_WAVEFRONT  # the wavefront form refuses subsurface materials
-    with pytest.raises(gpu.PrenderError):
-        ctx.render(s)
 
 
 def test_render_is_deterministic_and_shards_by_sample_offset(ctx):
@@ -225,6 +223,10 @@ def test_bad_arguments_are_errors(ctx):
     ("mesh_glass", lambda: scenes.mesh_cornell(width=48, height=36, samples=4, supersamples=2, subdiv=4,
                                                material="glass")),
     ("media_hg", lambda: scenes.media_cornell(width=48, height=36, samples=4, supersamples=2, g=0.5)),
+    ("sss_dipole", lambda: scenes.sss_cornell(width=48, height=36, samples=4, supersamples=2, subdiv=3)),
+    ("sss_level_minus1", lambda: scenes.sss_cornell(width=48, height=36, samples=4, supersamples=2, subdiv=3,
+                                                    level=-1)),
+    ("media_bssrdf", lambda: scenes.media_batch(n=1, seed=3, sizes=(48,), samples=4, supersamples=2, subdiv=4)[0]),
 ])
 def test_wavefront_equals_megakernel(ctx, name, build):
     """Both forms shade with the same code and the same per-branch streams, so
@@ -240,13 +242,14 @@ def test_wavefront_equals_megakernel(ctx, name, build):
     np.testing.assert_allclose(wf, mk, rtol=2e-4, atol=2e-6)
 
 
-def test_subsurface_level_minus1_matches_oracle_statistically(ctx, golden):
+@pytest.mark.parametrize("mode", [A.PR_MODE_MEGAKERNEL, A.PR_MODE_WAVEFRONT])
+def test_subsurface_level_minus1_matches_oracle_statistically(ctx, golden, mode):
     """Level -1 subsurface material (half the accepted entries take the
     dipole, half the single-scattering walk through the object with its two
-    radiance bounds) in the plain form, 16 x 512 spp, against the oracle's
+    radiance bounds) in both forms, 16 x 512 spp, against the oracle's
     16 x 512 spp (the oracle is bit-exact with the reference on one thread)."""
     s = scenes.sss_cornell(width=64, height=48, samples=128, supersamples=2, subdiv=3, level=-1)
-    s.settings.mode = A.PR_MODE_MEGAKERNEL
+    s.settings.mode = mode
     ctx.upload(s)
     nb, spp = 16, s.settings.spp
     b = _batches(ctx, s, nb, spp)
