@@ -374,18 +374,21 @@ void pr_scene_release(pr_ctx* ctx, pr_scene_obj* scene);
 typedef struct pr_job {
   const pr_scene_obj* scene;
   pr_camera camera;
-  pr_render_params params;    /* each job renders the plain (megakernel) form */
+  pr_render_params params;    /* params.mode: plain (megakernel) or wavefront form */
   float* rgb_dev;             /* W*H*3 floats on the device, image row order  */
   uint64_t sample_offset;
   int32_t accumulate;
   int32_t pad;
 } pr_job;
 
-/* Renders n jobs as one captured CUDA graph (no reference counterpart: the
- * reference renders one scene per process).  Jobs run on parallel branches
- * of the graph; each job's image equals pr_render_dev of the same inputs up
- * to float summation order (a batch uses fewer sample chunks per pixel).
- * Scene objects must stay alive until the call returns. */
+/* Renders n jobs (no reference counterpart: the reference renders one scene
+ * per process).  Plain-form jobs (and Kerr scenes) run as one captured CUDA
+ * graph, on parallel branches; each such image equals pr_render_dev of the
+ * same inputs up to float summation order (a batch uses fewer sample chunks
+ * per pixel).  Wavefront-form jobs share the context's path pool and run one
+ * after another after that graph, each as pr_render_dev would run it (one
+ * graph launch per pass), with the same image.  Scene objects must stay
+ * alive until the call returns. */
 int pr_render_batch(pr_ctx* ctx, int n, const pr_job* jobs);
 
 /* ---- Differentiation ------------------------------------------------- */

@@ -543,12 +543,14 @@ static unsigned int wavefront_slots() {
   return (unsigned int)v;
 }
 
-static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int accumulate) {
+static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int accumulate,
+                            const SceneObjData* scene = nullptr) {
+  const SceneObjData& sc = scene ? *scene : c->cur;
   const unsigned int P = c->tuned_slots ? c->tuned_slots : wavefront_slots();
   const uint64_t wh = (uint64_t)g.width * g.height;
   // camera samples per pass (sample table 28 B each); subsurface scenes take
   // smaller passes, whose frames (72 B each) come from a per-pass pool
-  const bool sss = c->cur.dev.has_sss != 0;
+  const bool sss = sc.dev.has_sss != 0;
   const uint64_t max_pass = sss ? (4ull << 20) : (64ull << 20);
   uint64_t layers = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.spp, max_pass / wh));
   const uint64_t pass_cap = layers * wh;
@@ -668,7 +670,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
     B.pass_first = first;
     B.pass_samples = n_layers * wh;
     PR_CUDA(c, cudaMemsetAsync(B.samp, 0, 24ull * B.pass_samples, c->stream));
-    PR_CUDA(c, wf_set_constants(c->cur.dev, g, B, c->stream));
+    PR_CUDA(c, wf_set_constants(sc.dev, g, B, c->stream));
     PR_CUDA(c, wf_reset_launch(P, c->stream));
     if (use_graph && c->wf_graph) PR_CUDA(c, cudaGraphLaunch(c->wf_graph, c->stream));
     else PR_CUDA(c, wf_run_host_loop(L, c->wf_host_ctl, (const WfCtl*)B.ctl, c->stream, c->kernel_ms));
@@ -1142,6 +1144,11 @@ int pr_render_batch(pr_ctx* c, int n, const pr_job* jobs) {
     off[j + 1] = off[j] + (size_t)cfg[j].width * cfg[j].height * 3 * (size_t)cfg[j].chunks;
     paths += (uint64_t)cfg[j].spp * cfg[j].width * cfg[j].height;
   }
+  // jobs in the wavefront form share the context's path pool: they run one
+  // after another on the context's stream, after the graph of the others
+  std::vector<char> wf_job((size_t)n, 0);
+  for (int j = 0; j < n; j++)
+    wf_job[j] = jobs[j].params.mode == PR_MODE_WAVEFRONT && !jobs[j].scene->data.kerr.enabled;
   PR_CUDA(c, c->batch_partial.ensure(sizeof(float) * std::max<size_t>(off[n], 1)));
   const int n_streams = std::min(n, 16);
   while ((int)c->batch_streams.size() < n_streams) {
@@ -1164,6 +1171,7 @@ int pr_render_batch(pr_ctx* c, int n, const pr_job* jobs) {
     e = cudaStreamWaitEvent(c->batch_streams[k], c->batch_events[n_streams], 0);
   float* part = (float*)c->batch_partial.p;
   for (int j = 0; j < n && e == cudaSuccess; j++) {
+    if (wf_job[j]) continue;
     const pr_job& J = jobs[j];
     cudaStream_t st = c->batch_streams[j % n_streams];
     const SceneObjData& sc = J.scene->data;
@@ -1206,15 +1214,29 @@ int pr_render_batch(pr_ctx* c, int n, const pr_job* jobs) {
   cudaGraphDestroy(graph);
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
   PR_CUDA(c, cudaGraphLaunch(c->batch_exec, c->stream));
+  uint64_t launches = 0, wf_passes = 0;
+  for (int j = 0; j < n; j++) {
+    if (!wf_job[j]) {
+      launches += 2;
+      continue;
+    }
+    const int stw = render_wavefront(c, cfg[j], jobs[j].rgb_dev, jobs[j].accumulate, &jobs[j].scene->data);
+    if (stw != PR_OK) return fail(c, stw, "job " + std::to_string(j) + ": " + c->err);
+    wf_passes += c->wf_passes;
+  }
   PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
   unsigned long long cnt[16];
   PR_CUDA(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
   int st = check_device_errors(c);
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  // wavefront jobs: 4 launches per iteration, a reset per pass and a resolve per job
+  for (int j = 0; j < n; j++)
+    if (wf_job[j]) launches += 1;
+  launches += 4 * cnt[5] + wf_passes;
   // Kerr jobs' counters are reported as pr_kerr_trace reports them
-  c->stats = all_kerr ? pr_render_stats{paths, cnt[3], cnt[1], cnt[2], ms, 2ull * (unsigned long long)n}
-                      : pr_render_stats{paths, cnt[1], cnt[2], cnt[3], ms, 2ull * (unsigned long long)n};
+  c->stats = all_kerr ? pr_render_stats{paths, cnt[3], cnt[1], cnt[2], ms, launches}
+                      : pr_render_stats{paths, cnt[1], cnt[2], cnt[3], ms, launches};
   return st;
 }
 

@@ -48,6 +48,35 @@ def test_batch_matches_single_renders(ctx):
         o.release()
 
 
+def test_batch_wavefront_jobs_equal_single_wavefront_renders(ctx):
+    """Jobs in the wavefront form (one after another on the shared path pool)
+    beside plain-form jobs in the same call: each wavefront image equals
+    pr_render_dev's wavefront image of the same inputs exactly (fixed-point
+    accumulation), subsurface and media scenes included."""
+    import torch
+    variants = scenes.media_batch(n=4, seed=7, sizes=(40, 56), samples=2, supersamples=2, subdiv=4)
+    variants[1].settings.mode = A.PR_MODE_MEGAKERNEL
+    for k in (0, 2, 3):
+        variants[k].settings.mode = A.PR_MODE_WAVEFRONT
+    variants[3] = scenes.mesh_cornell(width=48, height=36, samples=2, supersamples=2, subdiv=4, material="glass")
+    variants[3].settings.mode = A.PR_MODE_WAVEFRONT
+    objs = [ctx.scene_object(s) for s in variants]
+    outs = [torch.zeros((s.camera.height, s.camera.width, 3), dtype=torch.float32, device="cuda:0") for s in variants]
+    ctx.render_batch([(o, out, None, None, 4) for o, out in zip(objs, outs)])
+    torch.cuda.synchronize()
+    for s, out in zip(variants, outs):
+        ctx.upload(s)
+        ref = ctx.render(s, sample_offset=4)
+        got = out.cpu().numpy()
+        assert np.isfinite(got).all() and got.mean() > 0
+        if s.settings.mode == A.PR_MODE_WAVEFRONT:
+            assert np.array_equal(got, ref)
+        else:
+            np.testing.assert_allclose(got, ref, rtol=1e-4, atol=1e-6)
+    for o in objs:
+        o.release()
+
+
 def test_autotuner_keeps_the_image(ctx):
     s = scenes.mesh_cornell(width=96, height=72, samples=2, supersamples=2, subdiv=5)
     s.settings.mode = A.PR_MODE_WAVEFRONT
