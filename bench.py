@@ -291,6 +291,34 @@ def run_gpu(args):
         finally:
             del os.environ["PR_WF_HOST_LOOP"]
 
+    # the same frame with the glass icosphere (the workload names diffuse and
+    # glass), both forms, after the headline measurement
+    glass = None
+    if not args.small and not args.profile and not args.no_glass:
+        from prender_gb300 import scenes as SC
+        gs = SC.mesh_cornell(width=W, height=H, samples=16, supersamples=2, subdiv=7, material="glass")
+        ctx.upload(gs)
+        glass = {}
+        for mname, mval in (("wavefront", A.PR_MODE_WAVEFRONT), ("megakernel", A.PR_MODE_MEGAKERNEL)):
+            gp = gs.settings.to_c()
+            gp.mode = mval
+            gcam = gs.camera.to_c()
+            ts = []
+            for i in range(3 if mval == A.PR_MODE_WAVEFRONT else 2):
+                flush.zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                rc = L.pr_render_dev(ctx.h, C.byref(gcam), C.byref(gp), C.c_void_p(out.data_ptr()),
+                                     (rank + ws * (2000 + i)) * spp, 0)
+                torch.cuda.synchronize()
+                if rc != 0:
+                    raise RuntimeError(L.pr_last_error(ctx.h).decode())
+                ts.append(time.perf_counter() - t0)
+            gst = ctx.stats()
+            t = statistics.mean(ts[1:])  # the first frame builds the glass scene's pool and graph
+            glass[mname] = {"mpaths_per_s": round(paths / t / 1e6, 3), "ms_per_step": round(1e3 * t, 3),
+                            "segments_per_step": int(gst["segments"])}
+
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -357,7 +385,7 @@ def run_gpu(args):
         "config": {"workload": name, "width": W, "height": H, "spp": spp, "triangles": int(scene.meshes[1].faces.shape[0]),
                    "nee": 1, "mode": args.mode, "other_form": other, "l2": "flushed between steps (256 MB write)",
                    "paths_per_step": paths, "segments_per_step": segs, "kernel_ms_per_step": round(kern_s * 1e3, 3),
-                   "scene_upload_s": round(upload_s, 3), "autotuned": tuned},
+                   "scene_upload_s": round(upload_s, 3), "autotuned": tuned, "glass_icosphere": glass},
         "e2e": {"value": round(e2e_val, 3), "unit": "Mpaths/s",
                 "h2d_bytes_per_step": C.sizeof(cam) + C.sizeof(prm), "d2h_bytes_per_step": W * H * 3 * 4},
         "gpu_launches": int(st["kernel_launches"]) * args.steps,
@@ -611,6 +639,7 @@ def main():
     ap.add_argument("--profile", action="store_true", help="full scene, 256x192x16spp image (ncu captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward cost measurement")
+    ap.add_argument("--no-glass", action="store_true", help="skip the glass-icosphere frames")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default wavefront pool size and traversal grid")
     ap.add_argument("--ref-rows", type=int, default=48)
