@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define PR_ABI_VERSION 1
+#define PR_ABI_VERSION 2
 
 /* ---- status codes --------------------------------------------------- */
 enum {
@@ -61,8 +61,13 @@ enum {
   PR_MAT_REFRACTION_FRESNEL = 8
 };
 
-/* entity.h:18-25 EntityType, same numbering */
+/* entity.h:18-25 EntityType, same numbering.  PR_ENT_INF_LIGHT is an
+ * 'infinity_light x y z' OBJECT (scene_env.h:891-894, :1525-1541): no
+ * geometry, a directional light at infinity whose emission is its
+ * material's; it counts as an entity here (the reference keeps it out of
+ * its entity list, so later entity indices are one higher than its). */
 enum {
+  PR_ENT_INF_LIGHT = 0,
   PR_ENT_SPHERE = 1,
   PR_ENT_UVPLANE = 3,
   PR_ENT_CIRCLE = 4,
@@ -116,7 +121,27 @@ typedef struct pr_entity {
   int32_t blackhole_disk;  /* 'blackhole_disk' (scene_env.h:1177-1181, :1627):
                               index of the accretion-disk texture; 0 is the
                               reference's default, -1 = none                 */
+  /* light kinds of an emitting entity (light.h:13-74, scene_env.h:1210-1252).
+   * Only meaningful when the material is a light (diffuse, |colour| < 1e-3,
+   * |emission| > 1e-3).  parallel_light: a uvplane or sphere whose light
+   * arrives along -light_dir from wherever the entity is seen (a uvplane
+   * with light_dir zero takes its own normal * normal_inverse).
+   * spot_light: a sphere whose intensity |emission| falls off outside the
+   * cone around light_dir (SpotLightFalloff) and with distance
+   * (spot_attenuation).  Next-event estimation samples both kinds even when
+   * it is off for area lights (brdf.h:590-605). */
+  int32_t parallel_light;  /* 'parallel_light 1'                              */
+  int32_t spot_light;      /* 'spot_light 1' (spheres only)                  */
   int32_t pad0;
+  double light_dir[3];     /* parallel_light_dir / spot_light_dir, unit length
+                              as the parser leaves them; PR_ENT_INF_LIGHT: the
+                              'infinity_light' direction as given (its length
+                              scales the light, as in the reference)         */
+  double spot_angle[2];    /* spot_light_angle: cone and falloff widths in
+                              degrees (cos(a0), cos(a0 - a1) bound the falloff) */
+  double spot_falloff;     /* spot_light_falloff exponent (parser default 0) */
+  double spot_attenuation[3]; /* spot_attenuation a0 a1 a2: intensity divided by
+                              a0 + d (a1 + a2 d) (parser default 0 0 1)      */
 } pr_entity;
 
 /* Triangle mesh as ObjLoader keeps it (ObjLoader.h:153-233): float vertices,
@@ -248,6 +273,13 @@ size_t pr_abi_sizeof(int which);
  * LightList::random_light_setup, light.h:95) and builds one QBVH per mesh
  * with the reference's SAH rules (BVH.cpp:194-348, QBVH.cpp:161-302). */
 int pr_scene_upload(pr_ctx* ctx, const pr_scene_desc* scene);
+
+/* The checks pr_scene_upload makes of a scene description (sizes, indices,
+ * materials, light kinds, the black hole), on the host, with no device and
+ * no tree build.  Returns the status pr_scene_upload would; on an error
+ * the reason goes to msg (msg_len bytes, NUL-terminated) when msg is not
+ * null. */
+int pr_scene_check(const pr_scene_desc* scene, char* msg, int msg_len);
 
 /* QBVH statistics of a mesh entity: node count and leaf-array length.
  * Replaces QBVH::Construct bookkeeping (QBVH.cpp:161-186). */

@@ -20,6 +20,7 @@ constexpr double TWOPI = 6.28318530717958647692528676655900576;    // constant.h
 constexpr double INV_PI = 0.31830988618379067153776752674502872;   // constant.h:9
 constexpr double FORPI = 12.5663706143591729538505735331180115;    // constant.h:24
 constexpr double INV_FORPI = 0.07957747154594766788444188168625718;// constant.h:26
+constexpr double RAD = PI / 180.0;                                 // constant.h:31 (PS_RAD)
 constexpr double INF = 1.0e128;                                    // constant.h:33
 constexpr double EPS = 1.0e-6;                                     // constant.h:36
 constexpr double EPS14 = 1.0e-14;                                  // constant.h:39

@@ -185,9 +185,33 @@ struct Entity {
   V3 bb_min, bb_max;  // Entity::boundingBox (CreateBoundingBox of the entity type)
 };
 
-struct Light {  // light.h:13-74 (area lights only)
+struct Light {  // light.h:13-74
   double power = 0;
-  int entity = -1;
+  int entity = -1;   // Light::light; an infinity light has none
+  int parallel = 0, spot = 0, infinity = 0;
+  V3 dir;            // parallel / spot direction; infinity light: as given
+  // spot light (light.h:36-46 defaults): cosTotalWidth, cosFalloffStart
+  double cos_total = 0, cos_start = 0;
+  double falloff = 2.0;
+  double att[3] = {1.0, 0.0, 0.0};
+  V3 inf_emission;   // infinity_light_emitssin
+  V3 center;         // spot: the sphere's centre
+  // SpotLightFalloff (light.h:52-63)
+  double spot_falloff(V3 w) const {
+    const double costheta = dot(dir, w);
+    if (costheta < cos_total) return 0.0;
+    if (costheta > cos_start) return 1.0;
+    const double delta = (costheta - cos_total) / (cos_start - cos_total);
+    return std::pow(delta, falloff);
+  }
+  // SpotLightEmission (light.h:64-73)
+  V3 spot_emission(V3 intensity, V3 light_pos, V3 p) const {
+    const V3 wi = normalize(light_pos - p);
+    const double dist = length(light_pos - p);
+    double inv_a = att[0] + dist * (att[1] + att[2] * dist);
+    if (inv_a < 1.0e-3) inv_a = 1.0;
+    return intensity * spot_falloff(wi * -1.0) / inv_a;
+  }
 };
 
 struct KerrBH {  // KerrBlackHole (KerrBlackHole.h:86-151) with M = 1, initial_condition 0
@@ -779,6 +803,8 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
       Flattener fl(b.nodes, e.qbvh);
       fl.flatten(0, 0);
       if (m.isLight()) { err = "mesh lights are not sampled by the reference's NEE"; return PR_E_UNSUPPORTED; }
+    } else if (pe.type == PR_ENT_INF_LIGHT) {
+      // 'infinity_light': no geometry (scene_env.h:1525-1541)
     } else {
       err = "entity type not supported by the oracle";
       return PR_E_UNSUPPORTED;
@@ -828,21 +854,47 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
       }
     }
   }
-  // light registration (scene_env.h:1567-1586, :1692-1719) + random_light_setup sort (light.h:97)
+  // light registration in entity order (scene_env.h:1525-1541, :1567-1586,
+  // :1645-1663, :1692-1719) + random_light_setup's sort (light.h:97).
+  // Entity::light_id stays the registration index, which the reference
+  // later uses to index the sorted list (directLight_radiance.h:541).
   for (int i = 0; i < (int)s.ents.size(); i++) {
     Entity& e = s.ents[i];
+    const pr_entity& pe = d->entities[i];
     const Material& m = s.mats[e.material];
-    if (m.isLight()) {
-      e.light = true;
-      Light l;
-      l.entity = i;
-      l.power = e.area * length(m.emission);
-      e.light_id = (int)s.lights.size();
+    if (!m.isLight()) continue;
+    Light l;
+    const V3 dir(pe.light_dir[0], pe.light_dir[1], pe.light_dir[2]);
+    if (e.type == PR_ENT_INF_LIGHT) {
+      l.infinity = 1;
+      l.dir = dir;
+      l.inf_emission = m.emission;
+      l.power = length(m.emission);
       s.lights.push_back(l);
+      continue;
     }
+    e.light = true;
+    l.entity = i;
+    l.parallel = pe.parallel_light;
+    l.spot = pe.spot_light;
+    l.dir = dir;
+    if (e.type == PR_ENT_UVPLANE && l.parallel && length(dir) < 1.0e-16) l.dir = e.normal * (double)e.normal_inverse;
+    e.light_id = (int)s.lights.size();
+    l.power = e.area * length(m.emission);
+    if (l.spot) {
+      // SpotLightPower of the default cone, before the entity's own angles are set
+      l.cos_total = std::cos(30.0 * RAD);
+      l.cos_start = std::cos(25.0 * RAD);
+      l.power = length(m.emission) * 2.0 * PI * (1.0 - .5 * (l.cos_start + l.cos_total));
+      l.cos_total = std::cos(pe.spot_angle[0] * RAD);
+      l.cos_start = std::cos((pe.spot_angle[0] - pe.spot_angle[1]) * RAD);
+      l.falloff = pe.spot_falloff;
+      for (int k = 0; k < 3; k++) l.att[k] = pe.spot_attenuation[k];
+      l.center = e.position;
+    }
+    s.lights.push_back(l);
   }
   std::sort(s.lights.begin(), s.lights.end(), [](const Light& a, const Light& b) { return a.power > b.power; });
-  for (int k = 0; k < (int)s.lights.size(); k++) s.ents[s.lights[k].entity].light_id = k;
   return PR_OK;
 }
 
@@ -876,34 +928,60 @@ enum { NEE_DIFFUSE = 0, NEE_WARD = 1, NEE_PHONG = 2 };
 
 V3 eval_direct(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, V3 light_pos, int depth,
                int brdf = NEE_DIFFUSE, V3 ray_dir = V3()) {
-  const Entity& le = c.s.ents[light.entity];
   V3 light_normal;
   double pdf = 1.0;
-  if (le.type == PR_ENT_SPHERE) {
-    light_normal = normalize(light_pos - le.position);
-    if (le.normal_inverse < 0) light_normal = light_normal * -1.0;
-    pdf = 1.0 / le.area;
-  } else if (le.type == PR_ENT_UVPLANE) {
-    light_normal = le.normal;
-    if (le.normal_inverse < 0) light_normal = light_normal * -1.0;
-    pdf = 1.0 / le.area;
+  V3 emission;
+  if (!light.infinity) {
+    const Entity& le = c.s.ents[light.entity];
+    if (le.type == PR_ENT_SPHERE) {
+      light_normal = normalize(light_pos - le.position);
+      if (le.normal_inverse < 0) light_normal = light_normal * -1.0;
+      pdf = 1.0 / le.area;
+    } else if (le.type == PR_ENT_UVPLANE) {
+      light_normal = le.normal;
+      if (le.normal_inverse < 0) light_normal = light_normal * -1.0;
+      pdf = 1.0 / le.area;
+    }
+    emission = c.s.mats[le.material].emission;
+  } else {
+    light_normal = light.dir;
+    pdf = 1.0;
+    emission = light.inf_emission;
   }
-  V3 emission = c.s.mats[le.material].emission;
-  const V3 light_dir = normalize(light_pos - v0.position);
-  const double dist2 = sqr(light_pos - v0.position);
-  const double dot0 = dot(orienting_normal, light_dir);
-  const double dot1 = dot(light_normal, -1.0 * light_dir);
+  V3 light_dir = normalize(light_pos - v0.position);
+  double dist2 = sqr(light_pos - v0.position);
+  double dot0 = dot(orienting_normal, light_dir);
+  double dot1 = dot(light_normal, -1.0 * light_dir);
+  // directional kinds: fixed direction, no distance or light-side cosine
+  // (directLight_radiance.h:84-122); a spot light keeps the cosine of the
+  // sampled point at the receiver
+  if (light.infinity || light.parallel) {
+    light_dir = light.dir * -1.0;
+    pdf = 1.0;
+    dot1 = 1.0;
+    dist2 = 1.0;
+    dot0 = dot(orienting_normal, light_dir);
+  }
+  if (light.spot) {
+    light_dir = normalize(light.center - v0.position);
+    pdf = 1.0;
+    dot1 = 1.0;
+    dist2 = 1.0;
+  }
+  const bool point = light.infinity || light.parallel || light.spot;
   V3 rad;
   if (dot0 >= 0 && dot1 >= 0) {
     const double G = dot0 * dot1 / dist2;
     Hit is;
     const bool isect = intersect(c.s, v0.position, light_dir, is);
-    if (isect) {
-      const bool cond = std::fabs(std::sqrt(dist2) - is.distance) < 1e-3;
+    if (isect || light.infinity) {
+      const bool cond = point || std::fabs(std::sqrt(dist2) - is.distance) < 1e-3;
       if (cond) {
         if (is.object_id >= 0 && is.object_id != light.entity) return V3();
-        if (c.media) {  // env->participatingMedia (directLight_radiance.h:188-204)
-          const double t = length(v0.position - light_pos);
+        if (light.spot) emission = light.spot_emission(emission, light.center, v0.position);
+        if (light.infinity) emission = light.inf_emission;
+        if (c.media && !light.infinity) {  // env->participatingMedia (directLight_radiance.h:188-204)
+          const double t = light.spot ? length(v0.position - light.center) : length(v0.position - light_pos);
           emission = emission * c.s.medium.tr(t);
         }
         const Material vm = hit_mat(c.s, v0);
@@ -928,6 +1006,8 @@ V3 eval_direct(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, V
           const double ww = ((vm.phong_n + 2) / TWOPI) * ww1;
           if (ww < 0.0) return V3();
           rad = (emission * (vm.specular * ww)) * G / pdf;
+        } else if (point) {  // not a diffuse surface light: BRDF = colour (directLight_radiance.h:260-283)
+          rad = (emission * vm.color) * G / pdf;
         } else {
           rad = (emission * (vm.color * INV_PI)) * G / pdf;
         }
@@ -940,8 +1020,9 @@ V3 eval_direct(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, V
 // direct_radiance_sample (directLight_radiance.h:318-387), area lights
 V3 direct_sample(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, int depth, int brdf = NEE_DIFFUSE,
                  V3 ray_dir = V3()) {
+  V3 light_pos;  // an infinity light draws no point (light_pos stays zero)
+  if (light.infinity) return eval_direct(c, light, v0, orienting_normal, light_pos, depth, brdf, ray_dir);
   const Entity& le = c.s.ents[light.entity];
-  V3 light_pos;
   if (le.type == PR_ENT_SPHERE) {
     const double r1 = TWOPI * c.rnd.next01();
     const double r2 = 1.0 - 2.0 * c.rnd.next01();
@@ -955,14 +1036,39 @@ V3 direct_sample(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal,
   return eval_direct(c, light, v0, orienting_normal, light_pos, depth, brdf, ray_dir);
 }
 
-// direct_light_perfect_refrection (directLight_radiance.h:516-556), no
-// parallel/spot/infinity lights
+// direct_light_perfect_refrection (directLight_radiance.h:516-556): the
+// infinity light met by a miss (infinity_light_direct + InfinityLight,
+// light.h:157-173), else a light entity's emission, for a parallel or spot
+// light (the kind of the light the entity's registration index points to in
+// the sorted list) times the cosine to its direction and the spot's
+// emission (parallel_light_direct / spot_light_direct, :406-477); org is the
+// specular vertex
 V3 direct_perfect(Ctx& c, V3 org, V3 dir, int depth) {
   Hit lid;
   const bool isect = intersect(c.s, org, dir, lid);
   V3 d;
-  if (isect && c.s.ents[lid.object_id].light) {
-    d = c.s.mats[lid.material].emission;
+  int exist_infinity_light = 0;
+  if (!isect) {
+    for (const Light& l : c.s.lights)
+      if (l.infinity && std::fabs(dot(l.dir, dir * -1.0) - 1.0) < 1.0e-3) {
+        exist_infinity_light++;
+        d = l.inf_emission;
+        break;
+      }
+  }
+  if (isect && c.s.ents[lid.object_id].light && !exist_infinity_light) {
+    const V3 em = c.s.mats[lid.material].emission;
+    d = em;
+    const Light& light = c.s.lights[c.s.ents[lid.object_id].light_id];
+    if (light.parallel) {
+      const double dot0 = dot(dir, light.dir * -1.0);
+      d = dot0 >= 0.0 ? em * dot0 : V3();
+    }
+    if (light.spot) {
+      const V3 intensity = light.spot_emission(em, light.center, org);
+      const double dot0 = dot(dir, normalize(light.center - org));
+      d = dot0 >= 0.0 ? intensity * dot0 : V3();
+    }
     if (c.media) d = c.s.medium.tr(lid.distance) * d;
   }
   return d;
@@ -1020,8 +1126,11 @@ V3 brdf_diffuse(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, d
     direct = direct / 3;
     direct = direct / p_rr / (1.0 - p_scat);
   }
-  if (!c.nee && !s.lights.empty()) {
-    for (int i = 0; i < 3; i++) (void)random_light(c);  // only parallel/spot/infinity lights contribute
+  if (!c.nee && !s.lights.empty()) {  // parallel, spot and infinity lights only (brdf.h:590-605)
+    for (int i = 0; i < 3; i++) {
+      const Light& l = random_light(c);
+      if (l.parallel || l.spot || l.infinity) direct = direct + direct_sample(c, l, hp, on, depth) / 1.0;
+    }
     direct = direct / 3;
     direct = direct / p_rr / (1.0 - p_scat);
   }
@@ -1088,8 +1197,11 @@ V3 brdf_glossy(Ctx& c, V3 raydir, const Hit& hp, V3 on, double p_rr, double p_sc
     direct = direct / 3;
     direct = direct / p_rr / (1.0 - p_scat);
   }
-  if (!c.nee && !s.lights.empty()) {
-    for (int i = 0; i < 3; i++) (void)random_light(c);
+  if (!c.nee && !s.lights.empty()) {  // parallel, spot and infinity lights only (brdf.h:128-146)
+    for (int i = 0; i < 3; i++) {
+      const Light& l = random_light(c);
+      if (l.parallel || l.spot || l.infinity) direct = direct + direct_sample(c, l, hp, on, depth, brdf, raydir) / 1.0;
+    }
     direct = direct / 3;
     direct = direct / p_rr / (1.0 - p_scat);
   }
@@ -1211,38 +1323,69 @@ double phase_hg(double g, double costheta) {
 
 // eval_direct_radiance_media / direct_radiance_sample_media (ParticipatingMedia.h:27-268)
 V3 direct_media(Ctx& c, const Light& light, V3 pos, int depth) {
-  const Entity& le = c.s.ents[light.entity];
   V3 light_pos, light_normal;
   double pdf = 1.0;
-  if (le.type == PR_ENT_SPHERE) {
-    const double r1 = 2 * PI * c.rnd.next01();
-    const double r2 = 1.0 - 2.0 * c.rnd.next01();
-    light_pos = le.position + ((le.radius + EPS) * V3(std::sqrt(1.0 - r2 * r2) * std::cos(r1), std::sqrt(1.0 - r2 * r2) * std::sin(r1), r2));
-  } else if (le.type == PR_ENT_UVPLANE) {
-    const double t = le.v_length * c.rnd.next01();
-    const double s = le.u_length * c.rnd.next01();
-    light_pos = le.org + le.u_axis * s + le.v_axis * t;
+  V3 emission;
+  if (!light.infinity) {
+    const Entity& le = c.s.ents[light.entity];
+    if (le.type == PR_ENT_SPHERE) {
+      const double r1 = 2 * PI * c.rnd.next01();
+      const double r2 = 1.0 - 2.0 * c.rnd.next01();
+      light_pos = le.position + ((le.radius + EPS) * V3(std::sqrt(1.0 - r2 * r2) * std::cos(r1), std::sqrt(1.0 - r2 * r2) * std::sin(r1), r2));
+    } else if (le.type == PR_ENT_UVPLANE) {
+      const double t = le.v_length * c.rnd.next01();
+      const double s = le.u_length * c.rnd.next01();
+      light_pos = le.org + le.u_axis * s + le.v_axis * t;
+    }
   }
-  const V3 trr = c.s.medium.tr(length(pos - light_pos));
+  // transmittance over the distance to the point (spot: the centre; infinity: none)
+  double tt = length(pos - light_pos);
+  if (light.spot) tt = length(pos - light.center);
+  if (light.infinity) tt = 0.0;
+  const V3 trr = c.s.medium.tr(tt);
   // eval_direct_radiance_media
-  if (le.type == PR_ENT_SPHERE) {
-    light_normal = normalize(light_pos - le.position);
-    pdf = 1.0 / le.area;
+  if (!light.infinity) {
+    const Entity& le = c.s.ents[light.entity];
+    if (le.type == PR_ENT_SPHERE) {
+      light_normal = normalize(light_pos - le.position);
+      pdf = 1.0 / le.area;
+    } else {
+      light_normal = le.normal;
+      pdf = 1.0 / le.area;
+    }
+    emission = c.s.mats[le.material].emission;
   } else {
-    light_normal = le.normal;
-    pdf = 1.0 / le.area;
+    light_normal = light.dir;
+    pdf = 1.0;
+    emission = light.inf_emission;
   }
-  const V3 emission = c.s.mats[le.material].emission;
-  const V3 light_dir = normalize(light_pos - pos);
-  const double dist2 = sqr(light_pos - pos);
-  const double dot1 = dot(light_normal, -1.0 * light_dir);
+  V3 light_dir = normalize(light_pos - pos);
+  double dist2 = sqr(light_pos - pos);
+  double dot1 = dot(light_normal, -1.0 * light_dir);
+  if (light.infinity || light.parallel) {
+    light_dir = light.dir * -1.0;
+    pdf = 1.0;
+    dot1 = 1.0;
+    dist2 = 1.0;
+  }
+  if (light.spot) {
+    light_dir = normalize(light.center - pos);
+    pdf = 1.0;
+    dot1 = 1.0;
+    dist2 = 1.0;
+  }
+  const bool point = light.infinity || light.parallel || light.spot;
   V3 rad;
   if (dot1 >= 0) {
     const double G = dot1 / dist2;
     Hit is;
-    if (intersect(c.s, pos, light_dir, is)) {
-      if (std::fabs(std::sqrt(dist2) - is.distance) < 1e-3) {
-        if (!(is.object_id >= 0 && is.object_id != light.entity)) rad = emission * (1.0 / PI) * G / pdf;
+    const bool isect = intersect(c.s, pos, light_dir, is);
+    if (isect || light.infinity) {
+      if (point || std::fabs(std::sqrt(dist2) - is.distance) < 1e-3) {
+        if (!(is.object_id >= 0 && is.object_id != light.entity)) {
+          if (light.spot) emission = light.spot_emission(emission, light.center, pos);
+          rad = point ? emission * G / pdf : emission * (1.0 / PI) * G / pdf;
+        }
       }
     }
   }
@@ -1519,8 +1662,12 @@ V3 through_media(Ctx& c, V3 org, V3 dir, int depth, int in_ent, int sc_depth, in
     }
     direct = direct / 3;
   }
-  if (!c.nee && !s.lights.empty()) {
-    for (int i = 0; i < 3; i++) (void)random_light(c);
+  if (!c.nee && !s.lights.empty()) {  // parallel, spot and infinity lights only (Subsurface_Scattering.h:519-535)
+    for (int i = 0; i < 3; i++) {
+      const Light& l = random_light(c);
+      if (l.parallel || l.spot || l.infinity)
+        direct = direct + direct_sample(c, l, out, out.normal, depth, NEE_DIFFUSE, V3()) / 1.0;
+    }
     direct = direct / 3;
   }
   return (direct + Li) * weight;
@@ -1615,7 +1762,14 @@ V3 brdf_sss2(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, doub
                  (1.0 - p_scat);
       }
       if (!c.nee && !s.lights.empty()) {
-        for (int k = 0; k < 3; k++) (void)random_light(c);
+        // parallel, spot and infinity lights only, sampled at the ENTRY point
+        // with its orienting normal (Subsurface_Scattering.h:989-1010; the
+        // NEE branch above takes the exit point)
+        for (int k = 0; k < 3; k++) {
+          const Light& l = random_light(c);
+          if (l.parallel || l.spot || l.infinity)
+            direct = direct + direct_sample(c, l, hp, on, depth, NEE_DIFFUSE, V3()) / 1.0;
+        }
         direct = direct / 3;
         direct = direct * T12 * result * cos_wi_n * T21 / samplePDF / sampleDir / accept_prob / p_rr /
                  (1.0 - p_scat);

@@ -26,6 +26,7 @@ PR_MAT_SSS_WARD = 7
 PR_MAT_REFRACTION_FRESNEL = 8
 
 # entity.h:18-25 EntityType
+PR_ENT_INF_LIGHT = 0
 PR_ENT_SPHERE = 1
 PR_ENT_UVPLANE = 3
 PR_ENT_CIRCLE = 4
@@ -84,7 +85,13 @@ class pr_entity(C.Structure):
         ("normal", D3),
         ("radius_inner", C.c_double),
         ("blackhole_disk", C.c_int32),
+        ("parallel_light", C.c_int32),
+        ("spot_light", C.c_int32),
         ("pad0", C.c_int32),
+        ("light_dir", D3),
+        ("spot_angle", C.c_double * 2),
+        ("spot_falloff", C.c_double),
+        ("spot_attenuation", D3),
     ]
 
 

@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libprender_gpu.so")
 # every entry point declared in include/prender_gpu.h
 EXPORTS = (
     "pr_create", "pr_destroy", "pr_last_error", "pr_abi_version", "pr_abi_sizeof",
-    "pr_scene_upload", "pr_qbvh_info", "pr_qbvh_export", "pr_qbvh_build_host", "pr_render_bvh_export",
+    "pr_scene_upload", "pr_scene_check", "pr_qbvh_info", "pr_qbvh_export", "pr_qbvh_build_host", "pr_render_bvh_export",
     "pr_first_hit", "pr_first_hit_dev", "pr_trace_fast", "pr_render", "pr_render_dev", "pr_render_dev_noalloc", "pr_last_render_stats",
     "pr_kerr_trace", "pr_kerr_trace_dev", "pr_render_adjoint", "pr_render_adjoint_dev",
     "pr_last_kernel_times", "pr_kerr_sensitivity", "pr_kerr_sensitivity_adjoint", "pr_kerr_disk_shade", "pr_image_to_rgb8", "pr_image_to_rgb8_dev", "pr_image_to_rgbe", "pr_image_to_rgbe_dev", "pr_autotune_wavefront",
@@ -48,6 +48,7 @@ def load():
     L.pr_abi_sizeof.restype = C.c_size_t
     L.pr_abi_sizeof.argtypes = [C.c_int]
     L.pr_scene_upload.argtypes = [vp, vp]
+    L.pr_scene_check.argtypes = [vp, vp, C.c_int]
     L.pr_qbvh_info.argtypes = [vp, C.c_int, vp, vp]
     L.pr_qbvh_export.argtypes = [vp, C.c_int, vp, vp, vp, vp]
     L.pr_qbvh_build_host.argtypes = [vp, i32, vp, i32, vp, vp, vp, vp, vp, vp]

@@ -214,8 +214,12 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   S.rtris = (const float4*)o.rtris.p;
   S.fnorm = (const float*)o.fnorm.p;
   S.n_ents = (int)h.ents.size();
-  S.n_lights = (int)h.light_ent.size();
-  for (int i = 0; i < S.n_lights; i++) S.light_ent[i] = h.light_ent[i];
+  S.n_lights = (int)h.lights.size();
+  S.n_point_lights = 0;
+  for (int i = 0; i < S.n_lights; i++) {
+    S.lights[i] = h.lights[i];
+    S.n_point_lights += h.lights[i].kind != PR_LIGHT_AREA ? 1 : 0;
+  }
   for (int k = 0; k < 3; k++) {
     S.background[k] = h.background[k];
     S.env_light[k] = h.env_light[k];
@@ -239,6 +243,7 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
     f.material = e.material;
     f.normal_inverse = e.normal_inverse;
     f.is_light = e.is_light;
+    f.light_id = i < (int)h.light_id.size() ? h.light_id[i] : -1;
     for (int k = 0; k < 3; k++) {
       f.p[k] = (float)e.p[k];
       f.u[k] = (float)e.u_axis[k];
@@ -263,6 +268,25 @@ int pr_scene_upload(pr_ctx* c, const pr_scene_desc* d) {
   if (st != PR_OK) return st;
   c->scene_ready = true;
   return PR_OK;
+}
+
+int pr_scene_check(const pr_scene_desc* d, char* msg, int msg_len) {
+  HostScene hs;
+  std::string err;
+  SceneBuildOptions opt;
+  opt.gpu_render_trees = true;  // big meshes' trees are left pending (not built here)
+  opt.defer_exact = true;
+  int st = PR_E_NOMEM;
+  try {
+    st = build_host_scene(d, hs, err, opt);
+  } catch (const std::exception& ex) {  // allocation failures of the host build
+    err = ex.what();
+  }
+  if (st != PR_OK && msg && msg_len > 0) {
+    strncpy(msg, err.c_str(), (size_t)msg_len - 1);
+    msg[msg_len - 1] = 0;
+  }
+  return st;
 }
 
 pr_scene_obj* pr_scene_create(pr_ctx* c, const pr_scene_desc* d, int* status) {
@@ -626,6 +650,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   WfLaunch L;
   L.shade_blocks = (P + 127) / 128;
   L.sss = sss ? 1 : 0;
+  L.point = sc.dev.n_point_lights > 0 ? 1 : 0;
   // persistent traversal: one resident wave of blocks (more waves only queue
   // behind it and find the rays taken)
   int sms = 0;
@@ -645,7 +670,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   const bool use_graph = !(host_loop && host_loop[0] == '1') && !c->force_host_loop;
   if (use_graph && !c->wf_graph_failed &&
       (!c->wf_graph || c->wf_graph_slots != P || c->wf_graph_trace_blocks != L.trace_blocks ||
-       c->wf_graph_sss != L.sss)) {
+       c->wf_graph_variant != L.sss + 2 * L.point)) {
     if (c->wf_graph) {
       cudaStreamSynchronize(c->stream);  // the previous render's launch has finished with it
       cudaGraphExecDestroy(c->wf_graph);
@@ -659,7 +684,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
     } else {
       c->wf_graph_slots = P;
       c->wf_graph_trace_blocks = L.trace_blocks;
-      c->wf_graph_sss = L.sss;
+      c->wf_graph_variant = L.sss + 2 * L.point;
     }
   }
   c->wf_passes = 0;
@@ -751,6 +776,8 @@ static int adjoint_checks(pr_ctx* c, const pr_render_params* p) {
   if (c->cur.kerr.enabled) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass traces straight rays only");
   if (p && p->media && c->cur.host.medium.on) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover media");
   if (c->cur.dev.has_sss) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover subsurface materials");
+  if (c->cur.dev.n_point_lights > 0)
+    return fail(c, PR_E_UNSUPPORTED, "the adjoint pass covers area lights only (no parallel, spot or infinity lights)");
   for (const GMaterial& m : c->cur.host.mats)
     if (m.type == PR_MAT_WARD || m.type == PR_MAT_PHONG)
       return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover Ward or Phong materials (their lobes scale "

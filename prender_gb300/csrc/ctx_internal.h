@@ -72,7 +72,7 @@ struct pr_ctx {
   cudaGraphExec_t wf_graph = nullptr;
   unsigned int wf_graph_slots = 0;
   unsigned int wf_graph_trace_blocks = 0;
-  int wf_graph_sss = 0;              // the graph launches the subsurface shading kernel
+  int wf_graph_variant = 0;          // shading kernel the graph launches: sss + 2 * point
   unsigned int tuned_slots = 0;      // autotuner's wavefront pool size (0: default)
   unsigned int tuned_trace_bps = 0;  // autotuner's traversal blocks per SM (0: default)
   bool force_host_loop = false;      // the autotuner times candidates with the host-driven loop

@@ -141,11 +141,151 @@ __device__ __forceinline__ float3 light_normal(const GEntF& le, float3 lp, bool 
   return n;
 }
 
-__device__ __forceinline__ const GEntF& pick_light(const DevScene& S, Rng& rng) {
+// LightList::randomLight (light.h:132-155): rounded index, probability 1
+__device__ __forceinline__ const GLight& pick_light(const DevScene& S, Rng& rng) {
   int idx = (int)(rng.next() * (float)(S.n_lights - 1) + 0.5f);
   idx = min(max(idx, 0), S.n_lights - 1);
-  return S.entf[S.light_ent[idx]];
+  return S.lights[idx];
 }
+
+// SpotLightEmission / |emission| (light.h:47-73): the cone falloff of the
+// direction from the light's centre to p, over the distance attenuation
+__device__ __forceinline__ float spot_factor(const GLight& L, float3 p) {
+  const float3 dl = f3(L.center[0], L.center[1], L.center[2]) - p;
+  const float dist = sqrtf(dot(dl, dl));
+  const float3 wi = dl / dist;
+  float inv_a = L.att[0] + dist * (L.att[1] + L.att[2] * dist);
+  if (inv_a < 1.0e-3f) inv_a = 1.0f;
+  const float ct = -dot(f3(L.dir[0], L.dir[1], L.dir[2]), wi);
+  float f;
+  if (ct < L.cos_total) f = 0.0f;
+  else if (ct > L.cos_start) f = 1.0f;
+  else f = powf((ct - L.cos_total) / (L.cos_start - L.cos_total), L.falloff);
+  return f / inv_a;
+}
+
+// One next-event sample of light L seen from point p (direct_radiance_sample
+// + eval_direct_radiance, directLight_radiance.h:19-387; a medium point,
+// surface = false, has no cosine at the receiver, samples uvplanes without
+// the normal * PS_EPS lift and ignores normal inversion,
+// ParticipatingMedia.h:27-268).  Area lights: a point on the light, G =
+// cos0 cos1 / d^2 over pdf = 1 / area, visible iff nothing is hit before
+// the point.  Parallel lights: direction -dir, G = cos0, visible iff the
+// first thing hit along it is the light itself.  Spot lights: direction to
+// the centre, G = cos0 of the sampled surface point (the reference keeps
+// that cosine), the emission scaled by the cone falloff and attenuation,
+// visible iff the light is the first thing hit.  Infinity lights: direction
+// -dir as given, G = cos0 with that vector, visible iff nothing is hit; no
+// medium attenuation (the reference has no light entity to measure to).
+struct LightSample {
+  float3 ldir;  // light_dir of eval_direct_radiance (the BRDF is evaluated towards it)
+  float3 k;     // G / pdf, times the spot factor and the medium's transmittance
+  float3 so, sd;  // shadow ray
+  float tmax;
+  bool area;    // area light: a diffuse receiver takes colour / pi, the other kinds colour
+};
+
+// parallel, spot and infinity lights (compiled into the shading
+// instantiations for scenes that have them)
+__device__ __forceinline__ bool point_light_sample(const DevScene& S, const GLight& L, float3 p, float3 on,
+                                                   float3 origin, bool surface, bool media, Rng& rng,
+                                                   LightSample& ls) {
+  ls.area = false;
+  ls.so = origin;
+  if (L.kind == PR_LIGHT_INFINITY) {  // draws nothing
+    ls.ldir = -f3(L.dir[0], L.dir[1], L.dir[2]);
+    const float dot0 = surface ? dot(on, ls.ldir) : 1.0f;
+    if (!(dot0 >= 0.0f)) return false;
+    ls.k = f3(dot0, dot0, dot0);
+    ls.sd = ls.ldir / L.dir_len;
+    ls.tmax = 1.0e30f;
+    return true;
+  }
+  const GEntF& le = S.entf[L.ent];
+  const float3 lp = sample_light(le, rng, surface);
+  float trd;  // path length through the medium
+  float g;
+  if (L.kind == PR_LIGHT_PARALLEL) {
+    ls.ldir = -f3(L.dir[0], L.dir[1], L.dir[2]);
+    g = surface ? dot(on, ls.ldir) : 1.0f;
+    ls.sd = ls.ldir;
+    const float3 dl = lp - p;
+    trd = sqrtf(dot(dl, dl));
+  } else {
+    const float3 c = f3(L.center[0], L.center[1], L.center[2]);
+    const float3 dc = c - p;
+    trd = sqrtf(dot(dc, dc));
+    ls.ldir = dc / trd;
+    const float3 dl = lp - p;
+    g = surface ? dot(on, dl / sqrtf(dot(dl, dl))) : 1.0f;
+    const float3 dco = c - origin;
+    ls.sd = dco / sqrtf(dot(dco, dco));
+  }
+  if (!(g >= 0.0f)) return false;
+  if (L.kind == PR_LIGHT_SPOT) g *= spot_factor(L, p);
+  // the light must be the first thing the shadow ray meets
+  float tl = 3.0e38f, rest;
+  bool on_light;
+  if (le.type == PR_ENT_SPHERE) on_light = fast_sphere(S.ents[L.ent], origin, ls.sd, 3.0e38f, tl, rest);
+  else on_light = fast_uvplane(le, origin, ls.sd, 3.0e38f, tl);
+  if (!on_light) return false;
+  ls.k = f3(g, g, g);
+  if (media) ls.k = ls.k * medium_tr(S.medium, trd);
+  ls.tmax = tl - 1.0e-3f;
+  return true;
+}
+
+__device__ __forceinline__ void push_shadow(const DevScene& S, const LightSample& ls, float3 ew, int lmat,
+                                            ShadowReq* sh, int& nsh) {
+  sh[nsh].o = ls.so;
+  sh[nsh].d = ls.sd;
+  sh[nsh].tmax = ls.tmax;
+  sh[nsh].ew = ew;
+  sh[nsh].contrib = ew * ld3(S.mats[lmat].emission);
+  sh[nsh].lmat = lmat;
+  nsh++;
+}
+
+// direct_light_perfect_refrection (directLight_radiance.h:516-556): what a
+// specular or glass vertex at o sees of the lights straight along d, as a
+// factor on the emission of material mat (-1: nothing).  A miss meets an
+// infinity light within |dir . -d - 1| < 1e-3 (LightList::InfinityLight,
+// light.h:157-173); a light entity gives its emission, scaled for a
+// parallel or spot light by the cosine to the light direction and the spot
+// factor (parallel_light_direct / spot_light_direct, :406-477), where the
+// reference takes the light kind from its sorted list at the entity's
+// registration index.
+template <bool POINT>
+__device__ __forceinline__ float perfect_direct(const DevScene& S, float3 o, float3 d, bool hit, const FastHit& h,
+                                                int& mat) {
+  mat = -1;
+  if (!POINT) {
+    if (hit && S.entf[h.ent].is_light) mat = S.entf[h.ent].material;
+    return 1.0f;
+  }
+  if (!hit) {
+    for (int i = 0; i < S.n_lights; i++) {
+      const GLight& L = S.lights[i];
+      if (L.kind == PR_LIGHT_INFINITY && fabsf(-dot(f3(L.dir[0], L.dir[1], L.dir[2]), d) - 1.0f) < 1.0e-3f) {
+        mat = L.mat;
+        return 1.0f;
+      }
+    }
+    return 0.0f;
+  }
+  const GEntF& e = S.entf[h.ent];
+  if (!e.is_light) return 0.0f;
+  mat = e.material;
+  const GLight& L = S.lights[e.light_id];
+  if (L.kind == PR_LIGHT_PARALLEL) return fmaxf(-dot(d, f3(L.dir[0], L.dir[1], L.dir[2])), 0.0f);
+  if (L.kind == PR_LIGHT_SPOT) {
+    const float3 dc = f3(L.center[0], L.center[1], L.center[2]) - o;
+    const float c = dot(d, dc / sqrtf(dot(dc, dc)));
+    return c >= 0.0f ? c * spot_factor(L, o) : 0.0f;
+  }
+  return 1.0f;
+}
+
 
 // sampleHG (sampler.h:24-93); the reference's cos expression is (g/2)(...)
 __device__ __forceinline__ float3 sample_hg(float3 raydir, float g, Rng& rng, bool correct) {
@@ -293,6 +433,7 @@ __device__ __forceinline__ float dd_bssrdf(const GMaterial& m, float3 xi, float3
 // samples at the exit point (colour / pi, the unflipped surface normal as
 // orienting normal).  The reference computes Fresnel factors here that it
 // does not apply.
+template <bool POINT>
 __device__ inline void sss_exit(const DevScene& S, const RenderCfg& cfg, const GMaterial& m, int in_ent,
                                 const FastHit& oh, const Vertex& ov, float3 dir, float rr2, float3 beta, int depth,
                                 Rng& rng, ShadowReq* sh, int& nsh, PathState& ps) {
@@ -316,11 +457,21 @@ __device__ inline void sss_exit(const DevScene& S, const RenderCfg& cfg, const G
   if (cos2t < 0.0f) nd = normalize(dir - n * (2.0f * dot(n, dir)));
   const float3 C = ld3(m.color);
   const float3 bw = beta * Tr * C * (1.0f / rr2);
-  if (S.n_lights > 0 && cfg.nee != 0) {
+  const bool nee = cfg.nee != 0;
+  if (S.n_lights > 0 && (nee || POINT)) {
+    // without NEE only parallel, spot and infinity lights are sampled (:519-535)
     const float3 origin = offset_ray(ov.p, n);
     const float3 wn = bw * C * (0.31830988618379067154f / 3.0f);
     for (int i = 0; i < 3; i++) {
-      const GEntF& le = pick_light(S, rng);
+      const GLight& L = pick_light(S, rng);
+      if (POINT && L.kind != PR_LIGHT_AREA) {  // colour, not colour / pi
+        LightSample ls;
+        if (point_light_sample(S, L, ov.p, n, origin, true, cfg.media != 0 && S.medium.on != 0, rng, ls))
+          push_shadow(S, ls, wn * ls.k * 3.14159265358979323846f, L.mat, sh, nsh);
+        continue;
+      }
+      if (!nee) continue;
+      const GEntF& le = S.entf[L.ent];
       const float3 lp = sample_light(le, rng, true);
       const float3 ln = light_normal(le, lp, true);
       const float3 dl = lp - ov.p;
@@ -331,7 +482,8 @@ __device__ inline void sss_exit(const DevScene& S, const RenderCfg& cfg, const G
         const float3 dlo = lp - origin;
         const float disto = sqrtf(dot(dlo, dlo));
         const float3 em = ld3(S.mats[le.material].emission);
-        const float3 ew = wn * (dot0 * dot1 / dist2 * le.area);
+        float3 ew = wn * (dot0 * dot1 / dist2 * le.area);
+        if (cfg.media != 0 && S.medium.on != 0) ew = ew * medium_tr(S.medium, sqrtf(dist2));
         sh[nsh].o = origin;
         sh[nsh].d = dlo / disto;
         sh[nsh].tmax = disto - 1.0e-3f;
@@ -347,15 +499,34 @@ __device__ inline void sss_exit(const DevScene& S, const RenderCfg& cfg, const G
   ps.d = nd;
 }
 
+// the Phong (kind 4) or Ward (kind 5) lobe towards ldir as the reference's
+// next-event samples evaluate it (directLight_radiance.h:211-256), with the
+// specular colour left to the caller; 0 where it gives nothing
+__device__ __forceinline__ float glossy_lobe(int kind, const GMaterial& m, float3 refl, float3 in, float3 on, float3 a,
+                                             float3 b, float3 ldir) {
+  if (kind == 4) {
+    const float c = dot(refl, ldir);
+    if (c < 0.0f) return 0.0f;
+    return (m.phong_n + 2.0f) * 0.15915494309189533577f * powf(c, m.phong_n);
+  }
+  const float3 h = normalize(in + ldir);
+  const float ww0 = dot(h, on) * dot(h, on);
+  if (fabsf(ww0) < 1.0e-16f) return 0.0f;
+  const float hu = dot(h, a) / m.ward_ax, hv = dot(h, b) / m.ward_ay;
+  const float ww2 = 4.0f * 3.14159265358979323846f * m.ward_ax * m.ward_ay * sqrtf(fmaxf(0.0f, dot(ldir, on) * dot(in, on)));
+  if (fabsf(ww2) < 1.0e-16f) return 0.0f;
+  return expf(-(hu * hu + hv * hv) / ww0) / ww2;
+}
+
 // Shades the vertex found by the last closest-hit query of ps (SSS: with the
 // subsurface material case compiled in; GLOSSY: with the Ward and Phong
-// lobes; the plain form keeps a leaner instantiation for scenes without
-// them).  A tracer
+// lobes; POINT: with parallel, spot and infinity lights; the plain form
+// keeps a leaner instantiation for scenes without them).  A tracer
 // that builds the vertex itself (the Kerr geodesic tracer) passes it as pre,
 // and the colour a miss returns as miss (radiance.h:30-43); straight-ray
 // callers leave both null.  ovr (colour, emission) replaces the material's
 // where the entity rewrote its hit point's copy (the accretion disk).
-template <bool SSS = false, bool GLOSSY = true>
+template <bool SSS = false, bool GLOSSY = true, bool POINT = false>
 __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& ps, bool hit, const FastHit& h,
                      uint64_t sample_id, ShadowReq* sh, int& nsh, PathState& child, uint32_t* err,
                      const Vertex* pre = nullptr, const float3* miss = nullptr, EmissionTap* tap = nullptr,
@@ -363,8 +534,17 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   nsh = 0;
   const bool nee = cfg.nee != 0;
   const bool media = cfg.media != 0 && S.medium.on != 0;
-  if (ps.dp) {  // light hit along a specular / refraction direction (directLight_radiance.h:516-556)
-    if (hit && S.entf[h.ent].is_light) {
+  if (ps.dp) {  // light along a specular / refraction direction (directLight_radiance.h:516-556)
+    if (POINT) {
+      int lm;
+      const float fl = perfect_direct<POINT>(S, ps.o, ps.d, hit, h, lm);
+      if (lm >= 0 && fl > 0.0f) {
+        // the medium attenuates a light entity's term over the hit distance (:549-552)
+        const float3 w = ps.dpw * ((hit && media) ? medium_tr(S.medium, h.t) : f3(1, 1, 1)) * fl;
+        ps.L += w * ld3(S.mats[lm].emission);
+        if (tap) tap->em(lm, w);
+      }
+    } else if (hit && S.entf[h.ent].is_light) {
       float3 em = ld3(S.mats[S.entf[h.ent].material].emission);
       const float3 tr = media ? medium_tr(S.medium, h.t) : f3(1, 1, 1);
       ps.L += ps.dpw * (em * tr);
@@ -433,9 +613,17 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
       // phase / dirPdf == 1 in the reference's weight
       const float3 f = tr * f3(md.sigma_s[0], md.sigma_s[1], md.sigma_s[2]) * (phase / pdf / phase / p_scat / p_rr);
       if (!ent.is_light && S.n_lights > 0) {
-        // NEE from the medium point (eval_direct_radiance_media, ParticipatingMedia.h:27-268)
+        // NEE from the medium point (eval_direct_radiance_media, ParticipatingMedia.h:27-268):
+        // emission / pi for area lights, emission for the other kinds
         for (int i = 0; i < 3; i++) {
-          const GEntF& le = pick_light(S, rng);
+          const GLight& L = pick_light(S, rng);
+          if (POINT && L.kind != PR_LIGHT_AREA) {
+            LightSample ls;
+            if (point_light_sample(S, L, npos, f3(0, 0, 0), npos, false, true, rng, ls))
+              push_shadow(S, ls, ps.beta * f * ls.k * (1.0f / 3.0f), L.mat, sh, nsh);
+            continue;
+          }
+          const GEntF& le = S.entf[L.ent];
           const float3 lp = sample_light(le, rng, false);
           const float3 ln = light_normal(le, lp, false);
           const float3 dl = lp - npos;
@@ -504,11 +692,21 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     const float3 nd = normalize(u * (cs * r2s) + w2 * (sn * r2s) + on * sqrtf(1.0f - r2));
     const float3 origin = offset_ray(v.p, on);
     if (S.n_lights > 0) {
-      if (nee) {
-        // eval_direct_radiance (directLight_radiance.h:19-313), 3 samples averaged
+      if (nee || POINT) {
+        // eval_direct_radiance (directLight_radiance.h:19-313), 3 samples
+        // averaged; without NEE only parallel, spot and infinity lights
+        // (brdf.h:590-605), which take the colour, not colour / pi
         const float3 w = ps.beta * tri * C * (inv_rr * 0.31830988618379067154f * (1.0f / 3.0f));
         for (int i = 0; i < 3; i++) {
-          const GEntF& le = pick_light(S, rng);
+          const GLight& L = pick_light(S, rng);
+          if (POINT && L.kind != PR_LIGHT_AREA) {
+            LightSample ls;
+            if (point_light_sample(S, L, v.p, on, origin, true, media, rng, ls))
+              push_shadow(S, ls, w * ls.k * 3.14159265358979323846f, L.mat, sh, nsh);
+            continue;
+          }
+          if (!nee) continue;
+          const GEntF& le = S.entf[L.ent];
           const float3 lp = sample_light(le, rng, true);
           const float3 ln = light_normal(le, lp, true);
           const float3 dl = lp - v.p;
@@ -589,10 +787,20 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
       return SHADE_END;
     }
     const float3 origin = offset_ray(v.p, on);
-    if (S.n_lights > 0 && nee) {
+    if (S.n_lights > 0 && (nee || POINT)) {
+      // without NEE only parallel, spot and infinity lights (brdf.h:128-146)
       const float3 w = ps.beta * tri * Sp * (inv_rr * (1.0f / 3.0f));
       for (int i = 0; i < 3; i++) {
-        const GEntF& le = pick_light(S, rng);
+        const GLight& L = pick_light(S, rng);
+        if (POINT && L.kind != PR_LIGHT_AREA) {
+          LightSample ls;
+          if (!point_light_sample(S, L, v.p, on, origin, true, media, rng, ls)) continue;
+          const float f = glossy_lobe(kind, m, refl, in, on, a, b, ls.ldir);
+          if (f > 0.0f) push_shadow(S, ls, w * ls.k * f, L.mat, sh, nsh);
+          continue;
+        }
+        if (!nee) continue;
+        const GEntF& le = S.entf[L.ent];
         const float3 lp = sample_light(le, rng, true);
         const float3 ln = light_normal(le, lp, true);
         const float3 dl = lp - v.p;
@@ -763,7 +971,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
         if (oh.t < 1.0e-4f) {  // too thin to scatter: leave at once (no CUT0 on this result)
           make_vertex(S, org0, ts, oh, ov);
           if (frame) frame->open = 1;
-          sss_exit(S, cfg, m, v.ent, oh, ov, ts, rr2a, bw1, ps.depth + 2, rng, sh, nsh, ps);
+          sss_exit<POINT>(S, cfg, m, v.ent, oh, ov, ts, rr2a, bw1, ps.depth + 2, rng, sh, nsh, ps);
           ps.draws = rng_draws(rng);
           return SHADE_CONTINUE;
         }
@@ -813,7 +1021,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
             return SHADE_END;
           }
         }
-        sss_exit(S, cfg, m, v.ent, wh, ov, nd, rr2b, bw2, ps.depth + 3, rng, sh, nsh, ps);
+        sss_exit<POINT>(S, cfg, m, v.ent, wh, ov, nd, rr2b, bw2, ps.depth + 3, rng, sh, nsh, ps);
         ps.draws = rng_draws(rng);
         return SHADE_CONTINUE;
       }
@@ -825,12 +1033,25 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
                             dd_bssrdf(m, sp, on2, sw, v.p, on, 2));
       const float k = T12 * cos_wi_n * T21 / pdf_s / pdf_d / accept / p_rr / (1.0f - p_scat);
       const float3 origin_s = offset_ray(sp, on2);
-      if (S.n_lights > 0 && nee) {
-        // direct_radiance_sample at the exit point (the exit object's colour / pi), 3 samples averaged
+      if (S.n_lights > 0 && (nee || POINT)) {
+        // direct_radiance_sample, 3 samples averaged: with NEE at the exit
+        // point (the exit object's colour / pi); without it only parallel,
+        // spot and infinity lights, at the ENTRY point with its own colour
+        // (Subsurface_Scattering.h:961-1010)
         const float3 wn = ps.beta * tri * res * (k * (1.0f / 3.0f)) * ld3(S.mats[exit_mat].color) *
                           0.31830988618379067154f;
         for (int i = 0; i < 3; i++) {
-          const GEntF& le = pick_light(S, rng);
+          const GLight& L = pick_light(S, rng);
+          if (POINT && L.kind != PR_LIGHT_AREA) {
+            const float3 rp = nee ? sp : v.p, rn = nee ? on2 : on;
+            const float3 ro = nee ? origin_s : offset_ray(v.p, on);
+            const float3 wp = ps.beta * tri * res * (k * (1.0f / 3.0f)) * ld3(S.mats[nee ? exit_mat : v.mat].color);
+            LightSample ls;
+            if (point_light_sample(S, L, rp, rn, ro, true, media, rng, ls)) push_shadow(S, ls, wp * ls.k, L.mat, sh, nsh);
+            continue;
+          }
+          if (!nee) continue;
+          const GEntF& le = S.entf[L.ent];
           const float3 lp = sample_light(le, rng, true);
           const float3 ln = light_normal(le, lp, true);
           const float3 dl = lp - sp;
@@ -841,7 +1062,8 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
             const float3 dlo = lp - origin_s;
             const float disto = sqrtf(dot(dlo, dlo));
             const float3 em = ld3(S.mats[le.material].emission);
-            const float3 ew = wn * (dot0 * dot1 / dist2 * le.area);
+            float3 ew = wn * (dot0 * dot1 / dist2 * le.area);
+            if (media) ew = ew * medium_tr(S.medium, sqrtf(dist2));
             sh[nsh].o = origin_s;
             sh[nsh].d = dlo / disto;
             sh[nsh].tmax = disto - 1.0e-3f;

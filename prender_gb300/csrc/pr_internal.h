@@ -142,8 +142,27 @@ struct GEntF {
   float area;
   int32_t face_base, node_base;  // node_base: the render-path tree's root (DevScene::rnodes)
   float sss_rmax;  // subsurface probe-disk radius for this object (its bounding-box clamp applied)
-  int32_t pad1;
+  int32_t light_id;  // lights: registration index (Entity::light_id), which the reference
+                     // uses as an index into the sorted list (directLight_radiance.h:541)
   // disk: u_length = radius, v_length = inner radius, n = the plane normal
+};
+
+// One entry of the light list in LightList::random_light_setup's order
+// (sorted by power, light.h:97): what next-event estimation needs of each
+// light kind (light.h:13-74, directLight_radiance.h:19-133).
+enum { PR_LIGHT_AREA = 0, PR_LIGHT_PARALLEL = 1, PR_LIGHT_SPOT = 2, PR_LIGHT_INFINITY = 3 };
+struct GLight {
+  int32_t ent;        // the emitting entity (an infinity light's own type-0 entity)
+  int32_t kind;       // PR_LIGHT_*
+  int32_t mat;        // material whose emission the light gives off
+  float falloff;      // spot: SpotLightFalloff exponent
+  float dir[3];       // parallel: unit direction the light travels; spot: cone axis;
+                      // infinity: the direction as given (not normalised)
+  float cos_total;    // spot: cos(cone width), spot_light_cos_angle[0]
+  float center[3];    // spot: sphere centre
+  float cos_start;    // spot: cos(cone - falloff width), spot_light_cos_angle[1]
+  float att[3];       // spot: attenuation a0 + d (a1 + a2 d)
+  float dir_len;      // |dir| (infinity lights: the shadow ray runs along -dir / |dir|)
 };
 
 struct GMedium {
@@ -192,7 +211,8 @@ struct DevScene {
   const float* fnorm;      // 3 per face
   int32_t n_ents;
   int32_t n_lights;
-  int32_t light_ent[kMaxLights];
+  int32_t n_point_lights;  // parallel, spot and infinity lights (sampled even without NEE)
+  GLight lights[kMaxLights];
   double background[3];
   double env_light[3];
   float bg[3];

@@ -72,8 +72,8 @@ __device__ float3 trace_sample(const DevScene& S, const RenderCfg& cfg, float3 o
       SssFrameOut fo;
       fo.open = 0;
       const float3 Lb = ps.L;
-      const int r = shade<SSS, SSS>(S, cfg, ps, hit, h, sample_id, sh, nsh, child, err, nullptr, nullptr, nullptr,
-                               SSS ? &fo : nullptr);
+      const int r = shade<SSS, SSS, SSS>(S, cfg, ps, hit, h, sample_id, sh, nsh, child, err, nullptr, nullptr,
+                                         nullptr, SSS ? &fo : nullptr);
       const float3 Lown = ps.L - Lb;
       float3 Lnee = f3(0, 0, 0);
       for (int k = 0; k < nsh; k++) {
@@ -195,8 +195,10 @@ cudaError_t launch_megakernel(const DevScene& S, const RenderCfg& cfg, float* ou
                               unsigned long long* counters, cudaStream_t stream) {
   const uint64_t threads = (uint64_t)cfg.tiles_x * cfg.tiles_y * 32ull * (uint64_t)cfg.chunks;
   const uint32_t blocks = (uint32_t)((threads + 127) / 128);
-  // the fuller instantiation (subsurface frames, glossy lobes) only where needed
-  if (S.has_sss || S.has_glossy) pt_megakernel<true><<<blocks, 128, 0, stream>>>(S, cfg, out, err, counters);
+  // the fuller instantiation (subsurface frames, glossy lobes, parallel /
+  // spot / infinity lights) only where needed
+  if (S.has_sss || S.has_glossy || S.n_point_lights > 0)
+    pt_megakernel<true><<<blocks, 128, 0, stream>>>(S, cfg, out, err, counters);
   else pt_megakernel<false><<<blocks, 128, 0, stream>>>(S, cfg, out, err, counters);
   return cudaGetLastError();
 }

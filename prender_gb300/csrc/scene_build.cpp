@@ -650,6 +650,9 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
           return PR_E_BUILD;
         }
       }
+    } else if (pe.type == PR_ENT_INF_LIGHT) {
+      // no geometry: the traversals skip type 0, only the light list keeps it
+      // (scene_env.h:1525-1541)
     } else {
       err = "entity type " + std::to_string(pe.type) + " is not on this path yet";
       return PR_E_UNSUPPORTED;
@@ -664,24 +667,87 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
     }
     hs.ents.push_back(g);
   }
-  // lights: registration order, then LightList::random_light_setup's sort
-  // by power, descending (light.h:97; power = area * |emission|)
+  // lights: registration order (scene_env.h:1525-1541, :1567-1586,
+  // :1645-1663, :1692-1719), then LightList::random_light_setup's sort by
+  // power, descending (light.h:97).  Power: area * |emission|; a spot light
+  // SpotLightPower(|emission|) of the default cone (the reference computes
+  // it before it sets the entity's angles); an infinity light |emission|.
   struct L {
     double power;
-    int ent;
+    GLight g;
   };
   std::vector<L> lights;
+  hs.light_id.assign(hs.ents.size(), -1);
+  const double PI = 3.14159265358979323846, RAD = PI / 180.0;
   for (int i = 0; i < (int)hs.ents.size(); i++) {
+    const pr_entity& pe = d->entities[i];
     const pr_material& pm = d->materials[hs.ents[i].material];
-    if (is_light(pm)) {
-      hs.ents[i].is_light = 1;
-      if (hs.ents[i].type == PR_ENT_CIRCLE) hs.disk_light = true;
-      lights.push_back({hs.ents[i].area * len(mk(pm.emission)), i});
+    const int ty = hs.ents[i].type;
+    if (pe.parallel_light && pe.spot_light) {
+      err = "an entity is either a parallel or a spot light";
+      return PR_E_UNSUPPORTED;
     }
+    if ((pe.parallel_light || pe.spot_light) && (ty == PR_ENT_INF_LIGHT || ty == PR_ENT_POLYGON)) {
+      err = "parallel and spot lights are uvplanes or spheres";
+      return PR_E_UNSUPPORTED;
+    }
+    if (!is_light(pm)) continue;
+    const double elen = len(mk(pm.emission));
+    L l;
+    memset(&l.g, 0, sizeof(l.g));
+    l.g.ent = i;
+    l.g.mat = hs.ents[i].material;
+    l.g.kind = PR_LIGHT_AREA;
+    l.g.att[2] = 1.0f;
+    l.power = hs.ents[i].area * elen;
+    D3 dir = mk(pe.light_dir);
+    if (ty == PR_ENT_INF_LIGHT) {
+      if (!(len(dir) > 0.0)) { err = "an infinity light needs a direction"; return PR_E_SCENE; }
+      l.g.kind = PR_LIGHT_INFINITY;
+      l.power = elen;
+    } else if (pe.parallel_light) {
+      if (ty == PR_ENT_CIRCLE) {
+        err = "a parallel disk light samples the disk the way the reference leaves undefined (circle.h:110-134)";
+        return PR_E_UNSUPPORTED;
+      }
+      if (ty == PR_ENT_UVPLANE && len(dir) < 1.0e-16) {  // the plane's own normal (scene_env.h:1575-1578)
+        const GEntity& g = hs.ents[i];
+        dir = D3{g.normal[0] * g.normal_inverse, g.normal[1] * g.normal_inverse, g.normal[2] * g.normal_inverse};
+      }
+      if (!(len(dir) > 0.0)) { err = "a parallel sphere light needs parallel_light_dir"; return PR_E_SCENE; }
+      l.g.kind = PR_LIGHT_PARALLEL;
+    } else if (pe.spot_light) {
+      if (ty != PR_ENT_SPHERE) {
+        err = "spot lights are spheres (the reference reads every spot light's centre as a sphere's)";
+        return PR_E_UNSUPPORTED;
+      }
+      l.g.kind = PR_LIGHT_SPOT;
+      const double c0 = std::cos(30.0 * RAD), c1 = std::cos(25.0 * RAD);  // Light() defaults (light.h:41-43)
+      l.power = elen * 2.0 * PI * (1.0 - .5 * (c1 + c0));
+      l.g.cos_total = (float)std::cos(pe.spot_angle[0] * RAD);
+      l.g.cos_start = (float)std::cos((pe.spot_angle[0] - pe.spot_angle[1]) * RAD);
+      l.g.falloff = (float)pe.spot_falloff;
+      for (int k = 0; k < 3; k++) {
+        l.g.att[k] = (float)pe.spot_attenuation[k];
+        l.g.center[k] = (float)pe.p[k];
+      }
+    }
+    for (int k = 0; k < 3; k++) l.g.dir[k] = (float)(&dir.x)[k];
+    l.g.dir_len = (float)len(dir);
+    hs.ents[i].is_light = 1;
+    if (ty == PR_ENT_CIRCLE) hs.disk_light = true;
+    hs.light_id[i] = (int32_t)lights.size();
+    lights.push_back(l);
   }
   std::sort(lights.begin(), lights.end(), [](const L& a, const L& b) { return a.power > b.power; });
   if ((int)lights.size() > kMaxLights) { err = "too many lights"; return PR_E_ARG; }
-  for (const L& l : lights) hs.light_ent.push_back(l.ent);
+  for (const L& l : lights) hs.lights.push_back(l.g);
+  if (d->kerr.enabled)
+    for (const GLight& g : hs.lights)
+      if (g.kind != PR_LIGHT_AREA) {
+        err = "parallel, spot and infinity lights are sampled along straight rays only (no black hole)";
+        return PR_E_UNSUPPORTED;
+      }
   hs.scene_scale = (float)ext;
   // black hole (scene_env.h:701-766, :2056-2098; KerrBlackHole ctor :86-151)
   hs.kerr = GKerr{};

@@ -34,7 +34,8 @@ struct HostScene {
   std::vector<WNode> rnodes;   // render-path trees
   std::vector<float4> rtris;
   std::vector<float> fnorm;
-  std::vector<int32_t> light_ent;
+  std::vector<GLight> lights;           // in the reference's sorted order
+  std::vector<int32_t> light_id;        // per entity: registration index (-1: not a light)
   std::vector<MeshQbvh> mesh_qbvh;
   std::vector<int32_t> mesh_entity;  // entity index of each mesh_qbvh
   GMedium medium{};

@@ -679,8 +679,13 @@ class Loader {
     e.normal_inverse = 1;
     e.mesh = -1;
     e.normal[2] = 1.0;
+    e.spot_attenuation[2] = 1.0;  // the parser's defaults (scene_env.h:877-884)
     ObjMesh mesh;
-    if (starts(g, "sphere ")) {
+    if (starts(g, "infinity_light ")) {  // a direction, used as given (scene_env.h:891-894)
+      const std::vector<double> v = num_.many(after_key(g), 3);
+      e.type = PR_ENT_INF_LIGHT;
+      for (int i = 0; i < 3; i++) e.light_dir[i] = v[i];
+    } else if (starts(g, "sphere ")) {
       const std::vector<double> v = num_.many(after_key(g), 4);
       e.type = PR_ENT_SPHERE;
       for (int i = 0; i < 3; i++) e.p[i] = v[i];
@@ -872,7 +877,25 @@ class Loader {
       scan(b, "disk_map %d", m.disk_map);
     } else if (k == "blackhole_disk") {
       scan(b, "blackhole_disk %d", blackhole_disk_);
-    } else if (among(k, {"background", "smooth", "shadow", "parallel_light", "spot_light"})) {
+    } else if (k == "parallel_light") {
+      scan(b, "parallel_light %d", e.parallel_light);
+    } else if (k == "spot_light") {
+      scan(b, "spot_light %d", e.spot_light);
+    } else if (k == "parallel_light_dir" || k == "spot_light_dir") {
+      // one direction for both keywords, normalised as read (scene_env.h:1216-1234)
+      const std::vector<double> v = num_.many(after_key(b), 3);
+      const double inv = 1.0 / std::sqrt((v[0] * v[0] + v[2] * v[2]) + v[1] * v[1]);
+      for (int i = 0; i < 3; i++) e.light_dir[i] = v[i] * inv;
+    } else if (k == "spot_light_angle") {
+      const std::vector<double> v = num_.many(after_key(b), 2);
+      e.spot_angle[0] = v[0];
+      e.spot_angle[1] = v[1];
+    } else if (k == "spot_light_falloff") {
+      e.spot_falloff = num_.many(after_key(b), 1)[0];
+    } else if (k == "spot_attenuation") {
+      const std::vector<double> v = num_.many(after_key(b), 3);
+      for (int i = 0; i < 3; i++) e.spot_attenuation[i] = v[i];
+    } else if (among(k, {"background", "smooth", "shadow"})) {
       int on = 0;
       scan(after_key(b), "%d", on);
       if (on != 0) refuse(b);
@@ -881,8 +904,7 @@ class Loader {
     } else if (among(k, {"texture", "bump_texture", "ibl_texture", "equirectangular_map", "hemisphere_map",
                          "angular_map", "panoramic_map"})) {
       refuse(b);
-    } else if (among(k, {"back", "repeat", "ibl_texture_coef", "parallel_light_dir", "spot_light_dir",
-                         "spot_light_angle", "spot_light_falloff", "spot_attenuation"})) {
+    } else if (among(k, {"back", "repeat", "ibl_texture_coef"})) {
       // not read by anything rendered here
     } else {
       S_.warnings += "skipped in OBJECT: " + b + "\n";

@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(256) wf_reset(unsigned int n_slots) {
 // materials (the fuller shade() with the dipole and the single-scattering
 // walk, and the frames above); every camera sample then ends through its
 // sample slot, since frames may take radiance from any of its branches.
-template <bool SSS>
+template <bool SSS, bool POINT>
 __device__ __forceinline__ void wf_shade_impl() {
   const DevScene& S = c_scene;
   const RenderCfg& cfg = c_cfg;
@@ -263,7 +263,10 @@ __device__ __forceinline__ void wf_shade_impl() {
         if (SSS) {
           fr = __float_as_int(B.L[i].w) - 1;
           const int nf = B.neef[i];
-          if (nf >= 0) frame_add(B, nf, g, nee);  // the frame-opening vertex's own terms
+          // the frame-opening vertex's own terms join the frame's E, outside
+          // its bound (as the megakernel's F.E; the reference bounds only
+          // weight * incoming, Subsurface_Scattering.h:1061-1066)
+          if (nf >= 0) fx_add3(B.fr_e + 3 * (size_t)nf, nee);
           else ps.L += nee;
         } else {
           ps.L += nee;
@@ -287,8 +290,8 @@ __device__ __forceinline__ void wf_shade_impl() {
           const float3 Lb = ps.L;
           SssFrameOut fo;
           fo.open = 0;
-          r = shade<true, true>(S, cfg, ps, h.ent >= 0, h, sample_id, sh, nsh, child, B.err, nullptr, nullptr,
-                                nullptr, &fo);
+          r = shade<true, true, true>(S, cfg, ps, h.ent >= 0, h, sample_id, sh, nsh, child, B.err, nullptr,
+                                      nullptr, nullptr, &fo);
           if (fo.open) {
             // the branch moves into a new frame (or two nested ones): what it
             // gathered before this vertex belongs outside, the vertex's own
@@ -311,7 +314,7 @@ __device__ __forceinline__ void wf_shade_impl() {
             nsh = 0;
           }
         } else {
-          r = shade(S, cfg, ps, h.ent >= 0, h, sample_id, sh, nsh, child, B.err);
+          r = shade<false, true, POINT>(S, cfg, ps, h.ent >= 0, h, sample_id, sh, nsh, child, B.err);
         }
         for (int k = 0; k < 3; k++) {
           if (k < nsh) {
@@ -409,8 +412,11 @@ __device__ __forceinline__ void wf_shade_impl() {
 // 6 blocks of 128 per SM (80 registers, a few spilled): measured on GB300
 // over 4 / 5 / 6 / 7 / 8 / 10 blocks, mesh Cornell box 1024x768x64 spp,
 // wf_shade 108 / 99 / 94 / 96 / 102 / 110 ms per frame
-__global__ void __launch_bounds__(128, 6) wf_shade() { wf_shade_impl<false>(); }
-__global__ void __launch_bounds__(128, 3) wf_shade_sss() { wf_shade_impl<true>(); }
+__global__ void __launch_bounds__(128, 6) wf_shade() { wf_shade_impl<false, false>(); }
+// scenes with parallel, spot or infinity lights
+__global__ void __launch_bounds__(128, 4) wf_shade_point() { wf_shade_impl<false, true>(); }
+// scenes with subsurface materials (any light kind)
+__global__ void __launch_bounds__(128, 3) wf_shade_sss() { wf_shade_impl<true, true>(); }
 
 // Persistent traversal with ray replacement (Aila & Laine 2009, "Understanding
 // the efficiency of ray traversal on GPUs", dynamic ray fetch): the lanes of a
@@ -679,6 +685,7 @@ cudaError_t wf_set_constants(const DevScene& S, const RenderCfg& cfg, const WfBu
 
 static void launch_shade(const WfLaunch& L, cudaStream_t s) {
   if (L.sss) wf_shade_sss<<<L.shade_blocks, 128, 0, s>>>();
+  else if (L.point) wf_shade_point<<<L.shade_blocks, 128, 0, s>>>();
   else wf_shade<<<L.shade_blocks, 128, 0, s>>>();
 }
 

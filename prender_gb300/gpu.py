@@ -42,6 +42,17 @@ def qbvh_build_host(vertices: np.ndarray, faces: np.ndarray) -> dict:
     return dict(boxes=boxes, children=children, axes=axes, leaf=leaf)
 
 
+def check_scene(scene) -> None:
+    """The checks of a scene upload, on the host (no GPU): raises
+    PrenderError with pr_scene_upload's status and reason."""
+    L = load()
+    desc = scene.to_desc()
+    msg = C.create_string_buffer(512)
+    rc = L.pr_scene_check(desc.ptr(), msg, 512)
+    if rc != 0:
+        raise PrenderError(rc, msg.value.decode(errors="replace"))
+
+
 class Context:
     """One GPU context (pr_ctx)."""
 

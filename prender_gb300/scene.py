@@ -140,6 +140,19 @@ class Entity:
     normal: Sequence[float] = (0.0, 0.0, 1.0)
     radius_inner: float = 0.0
     blackhole_disk: int = 0
+    # light kinds (light.h:13-74): parallel / spot flags, the direction as
+    # the C ABI takes it (parallel_light_dir / spot_light_dir normalised the
+    # way the reference's parser does; an infinity light's as given), the
+    # spot cone in degrees, falloff exponent and distance attenuation (the
+    # parser's defaults).  light_dir_text keeps the unnormalised direction a
+    # scene file gives, for the file writer.
+    parallel_light: int = 0
+    spot_light: int = 0
+    light_dir: Sequence[float] = (0.0, 0.0, 0.0)
+    spot_angle: Sequence[float] = (0.0, 0.0)
+    spot_falloff: float = 0.0
+    spot_attenuation: Sequence[float] = (0.0, 0.0, 1.0)
+    light_dir_text: Optional[Sequence[float]] = field(default=None, compare=False, repr=False)
 
     def to_c(self) -> A.pr_entity:
         e = A.pr_entity()
@@ -151,7 +164,21 @@ class Entity:
         e.normal[:] = [float(x) for x in self.normal]
         e.radius_inner = float(self.radius_inner)
         e.blackhole_disk = int(self.blackhole_disk)
+        e.parallel_light = int(self.parallel_light)
+        e.spot_light = int(self.spot_light)
+        e.light_dir[:] = [float(x) for x in self.light_dir]
+        e.spot_angle[:] = [float(x) for x in self.spot_angle]
+        e.spot_falloff = float(self.spot_falloff)
+        e.spot_attenuation[:] = [float(x) for x in self.spot_attenuation]
         return e
+
+
+def _normalize_ref(v):
+    """normalize (vector3d.h:162-165): v * (1 / length), the squared length
+    summed as (x x + z z) + y y (Vector3d::sqr's SSE2 pairing,
+    vector3d.h:99-117), so that the result is the reference parser's double"""
+    inv = 1.0 / math.sqrt((v[0] * v[0] + v[2] * v[2]) + v[1] * v[1])
+    return [v[0] * inv, v[1] * inv, v[2] * inv]
 
 
 @dataclass
@@ -363,6 +390,39 @@ class Scene:
                      "observer": None if observer is None else tuple(float(x) for x in observer),
                      "disk_seed": int(disk_seed)}
 
+    def add_infinity_light(self, direction, emission) -> int:
+        """'infinity_light x y z' (scene_env.h:891-894, :1525-1541): light from
+        infinitely far along direction (as given; its length scales the
+        light the way the reference's unnormalised vector does)"""
+        self.entities.append(Entity(A.PR_ENT_INF_LIGHT, self._mat(Material.diffuse((0.0, 0.0, 0.0), emission)),
+                                    light_dir=tuple(float(x) for x in direction)))
+        return len(self.entities) - 1
+
+    def add_spot_light(self, center, radius, emission, direction, angle, falloff: float = 0.0,
+                       attenuation=(0.0, 0.0, 1.0)) -> int:
+        """A spot light: an emitting sphere with 'spot_light 1',
+        spot_light_dir, spot_light_angle (cone, falloff widths in degrees),
+        spot_light_falloff and spot_attenuation (scene_env.h:1223-1252)"""
+        i = self.add_sphere(center, radius, Material.diffuse((0.0, 0.0, 0.0), emission))
+        e = self.entities[i]
+        e.spot_light = 1
+        e.light_dir_text = tuple(float(x) for x in direction)
+        e.light_dir = tuple(_normalize_ref(e.light_dir_text))
+        e.spot_angle = tuple(float(x) for x in angle)
+        e.spot_falloff = float(falloff)
+        e.spot_attenuation = tuple(float(x) for x in attenuation)
+        return i
+
+    def make_parallel_light(self, index: int, direction=None) -> None:
+        """'parallel_light 1' (+ parallel_light_dir) on emitting entity index:
+        its light arrives along -direction (a uvplane without one takes its
+        own normal, scene_env.h:1572-1578)"""
+        e = self.entities[index]
+        e.parallel_light = 1
+        if direction is not None:
+            e.light_dir_text = tuple(float(x) for x in direction)
+            e.light_dir = tuple(_normalize_ref(e.light_dir_text))
+
     def add_mesh(self, vertices, faces, material: Material, normal_inverse: int = 1) -> int:
         self.meshes.append(Mesh(vertices, faces))
         self.entities.append(Entity(A.PR_ENT_POLYGON, self._mat(material), normal_inverse,
@@ -451,6 +511,8 @@ class Scene:
                 out += [f"disk2 {f3(e.p)} {_fmt(e.radius)} {_fmt(e.radius_inner)}", f"normal {f3(e.normal)}"]
                 # the keyword sets a scene-wide value every later disk inherits (scene_env.h:1177-1181)
                 out.append(f"blackhole_disk {int(e.blackhole_disk)}")
+            elif e.type == A.PR_ENT_INF_LIGHT:
+                out.append(f"infinity_light {f3(e.light_dir)}")
             elif e.type == A.PR_ENT_POLYGON:
                 if self.meshes[e.mesh].face_normals is not None:
                     raise ValueError("a mesh with its own face normals has no reference writer")
@@ -484,6 +546,16 @@ class Scene:
                     out.append(f"phong_brdf 1 1 {_fmt(m.phong_exponent)}")
             if m.disk_map:
                 out.append(f"disk_map {int(m.disk_map)}")
+            ldir = e.light_dir_text if e.light_dir_text is not None else e.light_dir
+            if e.parallel_light:
+                out.append("parallel_light 1")
+                if any(float(x) for x in ldir):
+                    out.append(f"parallel_light_dir {f3(ldir)}")
+            if e.spot_light:
+                out += ["spot_light 1", f"spot_light_dir {f3(ldir)}",
+                        f"spot_light_angle {_fmt(e.spot_angle[0])} {_fmt(e.spot_angle[1])}",
+                        f"spot_light_falloff {_fmt(e.spot_falloff)}",
+                        f"spot_attenuation {f3(e.spot_attenuation)}"]
             if e.normal_inverse < 0:
                 out.append("normal -1")
             if m.type in refl:

@@ -88,7 +88,10 @@ def load(path: str) -> Scene:
             s.entities.append(Entity(
                 type=int(e.type), material=int(e.material), normal_inverse=int(e.normal_inverse), mesh=int(e.mesh),
                 p=_v(e.p), radius=float(e.radius), u=_v(e.u), v=_v(e.v), normal=_v(e.normal),
-                radius_inner=float(e.radius_inner), blackhole_disk=int(e.blackhole_disk)))
+                radius_inner=float(e.radius_inner), blackhole_disk=int(e.blackhole_disk),
+                parallel_light=int(e.parallel_light), spot_light=int(e.spot_light), light_dir=_v(e.light_dir),
+                spot_angle=_v(e.spot_angle, 2), spot_falloff=float(e.spot_falloff),
+                spot_attenuation=_v(e.spot_attenuation)))
         for i in range(d.n_meshes):
             pm = d.meshes[i]
             v = np.ctypeslib.as_array(pm.vertices, shape=(pm.n_vertices * 3,)).reshape(-1, 3).copy()

@@ -14,11 +14,12 @@ its build on the machine that runs them.
 
 writes sss_oracle.npz from the oracle alone (no reference build needed);
 --disk-oracle, --sss-l1-oracle, --glossy-oracle, --media-oracle,
---mesh7-oracle and --batch-oracle write kerr_disk_oracle.npz,
-sss_l1_oracle.npz, glossy_oracle.npz, media_oracle.npz, mesh7_oracle.npz and
-batch_oracle.npz the same way; --media-only and --batch-only write the
-reference's own one-thread media and batch-variant renders, --hdr-only its
-Render::OutputHdr file of a seeded image.
+--mesh7-oracle, --batch-oracle and --lights-oracle write kerr_disk_oracle.npz,
+sss_l1_oracle.npz, glossy_oracle.npz, media_oracle.npz, mesh7_oracle.npz,
+batch_oracle.npz and lights_oracle.npz the same way; --media-only,
+--batch-only and --lights-only write the reference's own one-thread media,
+batch-variant and light-kind renders, --hdr-only its Render::OutputHdr file
+of a seeded image.
 --scene-files-only writes the meshes and textures that the scene files in
 scene_files/ name, and scene_files.npz from the reference's renders of them.
 """
@@ -351,6 +352,44 @@ def batch_oracle_golden(nb=16):
     np.savez_compressed(os.path.join(HERE, "batch_oracle.npz"), **out)
 
 
+def lights_golden(d):
+    """spot / parallel / infinity light scenes rendered by the reference, one thread (bit-exact)"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import lights_cases
+    out = {}
+    for name, sc in lights_cases.one_thread_cases().items():
+        dd = os.path.join(d, "l_" + name)
+        os.makedirs(dd)
+        img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+        out[name] = img
+        print("lights", name, info, float(img.mean()))
+    np.savez_compressed(os.path.join(HERE, "lights_render.npz"), **out)
+
+
+def lights_oracle_golden(nb=16):
+    """16 independent 256-spp renders of each light-kind scene by the
+    oracle (pinned bit-exact to the reference by lights_render.npz):
+    per-pixel mean and spread"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import lights_cases
+    from oracle import oracle as O
+    out = {}
+    for name in lights_cases.CASES:
+        sc = lights_cases.highspp_case(name)
+        o = O.OracleScene(sc)
+        imgs = []
+        for k in range(nb):
+            sc.settings.seed = 100 + k
+            img, _, _ = o.render(threads=os.cpu_count(), settings=sc.settings)
+            imgs.append(img)
+        b = np.stack(imgs)
+        out[f"{name}_mean"] = b.mean(0).astype(np.float32)
+        out[f"{name}_sd"] = b.std(0, ddof=1).astype(np.float32)
+        print("lights oracle", name, float(b.mean()))
+    out["batches"] = np.int32(nb)
+    np.savez_compressed(os.path.join(HERE, "lights_oracle.npz"), **out)
+
+
 def mesh7_oracle_golden(nb=16):
     """The benchmarked scene itself (327,680-triangle displaced icosphere,
     diffuse and glass) at 128 x 96, 16 independent 256-spp renders by the
@@ -473,7 +512,8 @@ def _image_size(path):
 
 KNOWN_FLAGS = {"--kerr-only", "--disk-only", "--sss-only", "--sss-l1-only", "--glossy-only", "--sss-oracle",
                "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle", "--scene-files-only", "--media-only",
-               "--media-oracle", "--mesh7-oracle", "--batch-only", "--batch-oracle", "--hdr-only"}
+               "--media-oracle", "--mesh7-oracle", "--batch-only", "--batch-oracle", "--hdr-only",
+               "--lights-only", "--lights-oracle"}
 
 
 def main():
@@ -482,6 +522,9 @@ def main():
         sys.exit(f"unknown option(s) {bad}; known: {sorted(KNOWN_FLAGS)}")
     if "--media-oracle" in sys.argv:
         media_oracle_golden()
+        return
+    if "--lights-oracle" in sys.argv:
+        lights_oracle_golden()
         return
     if "--mesh7-oracle" in sys.argv:
         mesh7_oracle_golden()
@@ -516,6 +559,10 @@ def main():
     if "--media-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             media_golden(d)
+        return
+    if "--lights-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            lights_golden(d)
         return
     if "--hdr-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:

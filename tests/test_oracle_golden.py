@@ -117,6 +117,24 @@ def test_glossy_render_one_thread_bit_exact(golden, name):
     assert ref.mean() > 0
 
 
+@pytest.mark.parametrize("name", ["spot", "spot_media", "parallel", "parallel_nonee", "infinity", "sss_spot",
+                                  "infinity_raw"])
+def test_light_kinds_render_one_thread_bit_exact(golden, name):
+    # spot (cone falloff, attenuation, the sampled point's cosine), parallel
+    # (uvplane and sphere emitters, the plane's own normal by default) and
+    # infinity lights (no point drawn, visible iff nothing is hit, a
+    # direction used as given), in NEE, the no-NEE sampling of those kinds,
+    # media NEE, the perfect-direction term of mirrors and glass through the
+    # entity's registration index into the sorted list, and both subsurface
+    # exits (the dipole's no-NEE samples at its entry point)
+    import lights_cases
+    sc = lights_cases.one_thread_cases()[name]
+    img, _, _ = O.OracleScene(sc).render(threads=1)
+    ref = golden["lights_render"][name]
+    assert np.array_equal(img, ref)
+    assert ref.mean() > 0
+
+
 def _media_cases():
     import media_cases
     return media_cases

@@ -54,6 +54,8 @@ def _written_cases():
         "kerr_disk": kerr_cases.disk_scene(16, 8, a=0.6, temperature=True, doppler=0.6),
     }
     out.update({"glossy_" + k: v for k, v in glossy_cases.one_thread_cases().items()})
+    import lights_cases
+    out.update({"lights_" + k: v for k, v in lights_cases.one_thread_cases().items()})
     return out
 
 
@@ -83,6 +85,59 @@ def test_written_scene_reads_back_the_same(tmp_path, name):
         assert back.kerr["observer"] == tuple(s.camera.position)
         if s.kerr.get("disk_texture") is not None:
             assert np.array_equal(back.kerr["disk_texture"][:, :, :3], np.asarray(s.kerr["disk_texture"])[:, :, :3])
+
+
+@pytest.mark.parametrize("name", ["spot", "spot_media", "parallel", "parallel_nonee", "infinity", "sss_spot",
+                                  "infinity_raw"])
+def test_light_kind_files_render_like_the_reference(tmp_path, golden, name):
+    # the files the reference rendered for lights_render.npz, read by this
+    # library's reader (infinity_light, parallel_light(_dir), spot_light,
+    # spot_light_dir / _angle / _falloff, spot_attenuation) and rendered by
+    # the oracle
+    import lights_cases
+    sc = lights_cases.one_thread_cases()[name]
+    s = scene_file.load(sc.write_reference(str(tmp_path)))
+    img, _, _ = O.OracleScene(s).render(threads=1)
+    assert np.array_equal(img, golden["lights_render"][name])
+
+
+@pytest.mark.parametrize("body,code,msg", [
+    ("uvplane 0 10 0\nU 1 0 0\nV 0 0 1\nspot_light 1\n", A.PR_E_UNSUPPORTED, "spot lights are spheres"),
+    ("sphere 0 10 0 1\nparallel_light 1\nspot_light 1\n", A.PR_E_UNSUPPORTED, "either a parallel or a spot"),
+    ("sphere 0 10 0 1\nparallel_light 1\n", A.PR_E_SCENE, "parallel_light_dir"),
+    ("disk 0 10 0 1\nnormal 0 -1 0\nparallel_light 1\nparallel_light_dir 0 -1 0\n", A.PR_E_UNSUPPORTED,
+     "parallel disk"),
+    ("infinity_light 0 0 0\n", A.PR_E_SCENE, "infinity light needs a direction"),
+])
+def test_light_kinds_refused_where_the_reference_reads_garbage(tmp_path, body, code, msg):
+    """A spot light's centre is read as a sphere's whatever its shape, a
+    parallel sphere without a direction shoots zero-length shadow rays, a
+    disk's sampling is undefined (circle.h:110-134): pr_scene_check refuses
+    them on the host, as an upload would"""
+    from prender_gb300 import gpu
+    text = ("IMAGE\n8 6\n\nOBJECT\n" + body + "emission 1 1 1\ncolor 0 0 0\nreflection diffuse\n\n"
+            "OBJECT\nsphere 0 0 0 1\ncolor 0.5 0.5 0.5\nreflection diffuse\n\n")
+    s = scene_file.load(_scene(tmp_path, text))
+    with pytest.raises(gpu.PrenderError) as e:
+        gpu.check_scene(s)
+    assert str(code) in str(e.value) and msg in str(e.value)
+
+
+def test_light_kind_fields_read_from_the_file(tmp_path):
+    text = ("IMAGE\n8 6\n\nOBJECT\ninfinity_light 1 -1.5 -0.4\nemission 1 1 1\ncolor 0 0 0\n"
+            "reflection diffuse\n\nOBJECT\nsphere 40 81 70 1\nemission 50 50 50\ncolor 0 0 0\n"
+            "reflection diffuse\nspot_light 1\nspot_light_angle 20 10\nspot_light_dir 0 -2 0\n"
+            "spot_light_falloff 0.5\nspot_attenuation 0 1 0\n\nOBJECT\nuvplane 0 10 0\nU 5 0 0\nV 0 0 5\n"
+            "emission 5 5 5\ncolor 0 0 0\nreflection diffuse\nparallel_light 1\n\n")
+    s = scene_file.load(_scene(tmp_path, text))
+    inf, spot, par = s.entities
+    assert inf.type == A.PR_ENT_INF_LIGHT and inf.light_dir == (1.0, -1.5, -0.4)  # as given
+    assert spot.spot_light == 1 and spot.light_dir == (0.0, -1.0, 0.0)  # normalised
+    assert spot.spot_angle == (20.0, 10.0) and spot.spot_falloff == 0.5 and spot.spot_attenuation == (0.0, 1.0, 0.0)
+    assert par.parallel_light == 1 and par.light_dir == (0.0, 0.0, 0.0)  # the plane's normal, taken at upload
+    assert par.spot_attenuation == (0.0, 0.0, 1.0)  # the parser's default
+    from prender_gb300 import gpu
+    gpu.check_scene(s)
 
 
 def _scene(tmp_path, body, name="s.txt"):
@@ -150,14 +205,11 @@ def test_bad_values_are_errors_with_the_line(tmp_path, body, msg):
 @pytest.mark.parametrize("body", [
     "OBJECT\nsphere 0 0 0 1\ntexture wood.bmp\n\n",
     "OBJECT\nsphere 0 0 0 1\nbump_texture b.bmp\n\n",
-    "OBJECT\nsphere 0 0 0 1\nparallel_light 1\n\n",
-    "OBJECT\nsphere 0 0 0 1\nspot_light 1\n\n",
     "OBJECT\nsphere 0 0 0 1\nsmooth 1\n\n",
     "OBJECT\nsphere 0 0 0 1\nMATERIAL_SYMBOL\nKetchup\n\n",
     "OBJECT\nsphere 0 0 0 1\nreflection reflection1\n1 2 3 4 5 6\n\n",
     "OBJECT\nplane 0 0 0\nnormal 0 1 0\n\n",
     "OBJECT\nhemisphere 0 0 0 1\n\n",
-    "OBJECT\ninfinity_light 0 -1 0\n\n",
     "OBJECT\nuvplane 0 0 0\nU 1 0 0\nV 0 1 0\nrotation 0 10 0\n\n",
     "OBJECT\ndisk 0 0 0 1\nnormal 0 1 0\ntranslate 1 0 0\n\n",
     "OBJECT\nsphere 0 0 0 1\nreflection reflection\nreflection Subsurface_Scattering\n\n",
