@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define PR_ABI_VERSION 2
+#define PR_ABI_VERSION 3
 
 /* ---- status codes --------------------------------------------------- */
 enum {
@@ -105,7 +105,32 @@ typedef struct pr_material {
   double ward_alpha[2];    /* 'ward_brdf lo_d lo_s alp_x alp_y' roughness along
                               the orienting normal's u and v axes (material.h:42-47) */
   double phong_exponent;   /* 'phong_brdf lo_d lo_s n' specular exponent     */
+  /* Textures on spheres, hemispheres and uvplanes (sphere.h:117-240,
+   * plane.h:241-273).  texture: 'texture file.bmp', RGB8 rows as
+   * BitMap::cell(y, x) reads them; a hit takes its colour and specular from
+   * the texel.  ibl_*: 'ibl_texture file.bmp|.hdr': a hit takes its colour
+   * from the texel and its emission from ibl_coef times the texel
+   * (ibl_texture_coef); give the image as RGB8 (ibl_rgb8, a BMP) or as float
+   * RGB (ibl_rgbf, a Radiance HDR as HDRImage holds it), not both.  NULL
+   * pointers: no texture.  map_flags: PR_MAP_* (several may be set, applied
+   * in the reference's order). */
+  const uint8_t* texture;
+  int32_t texture_width, texture_height;
+  const uint8_t* ibl_rgb8;
+  const float* ibl_rgbf;
+  int32_t ibl_width, ibl_height;
+  double ibl_coef;         /* ibl_texture_coef (default 1)                   */
+  int32_t repeat;          /* 'repeat' (default 1; 0 is taken as 1)          */
+  int32_t map_flags;
 } pr_material;
+
+/* texture mappings of spheres (material.h:188-192) */
+enum {
+  PR_MAP_HEMISPHERE = 1,     /* hemisphere_map    */
+  PR_MAP_ANGULAR = 2,        /* angular_map       */
+  PR_MAP_PANORAMIC = 4,      /* panoramic_map     */
+  PR_MAP_EQUIRECTANGULAR = 8 /* equirectangular_map */
+};
 
 /* One OBJECT block (scene_env.h:854-1851) after its transforms. */
 typedef struct pr_entity {
@@ -132,7 +157,8 @@ typedef struct pr_entity {
    * it is off for area lights (brdf.h:590-605). */
   int32_t parallel_light;  /* 'parallel_light 1'                              */
   int32_t spot_light;      /* 'spot_light 1' (spheres only)                  */
-  int32_t pad0;
+  int32_t hemisphere;      /* PR_ENT_SPHERE: 'hemisphere x y z r', the half
+                              with y >= 0 about the centre (sphere.h:98-103) */
   double light_dir[3];     /* parallel_light_dir / spot_light_dir, unit length
                               as the parser leaves them; PR_ENT_INF_LIGHT: the
                               'infinity_light' direction as given (its length

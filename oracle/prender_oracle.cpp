@@ -111,6 +111,15 @@ struct Material {  // material.h:54-240
   double ward_ax = 0, ward_ay = 0;  // brdfParameter.ward_brdf (material.h:42-47)
   double phong_n = 0;               // brdfParameter.phong_brdf.specular_exponent
   Medium medium;
+  // texture (BitMap cell(i, j) RGB) and IBL image (IBL_Color(i, j) as doubles)
+  // (shared: hit_mat copies the material per hit)
+  std::shared_ptr<const std::vector<unsigned char>> tex;
+  int tex_w = 0, tex_h = 0;
+  std::shared_ptr<const std::vector<double>> ibl;
+  int ibl_w = 0, ibl_h = 0;
+  double ibl_coef = 1.0;
+  int repeat = 1;
+  int map_flags = 0;
   // Material::isLight (material.h): diffuse, dark, emissive
   bool isLight() const {
     return type == PR_MAT_DIFFUSE && length(color) < 0.001 && length(emission) > 0.001;
@@ -128,6 +137,8 @@ struct Hit {  // IntersectionPos (intersection.h:11-30) + object_id
   // (the accretion disk's texture and Doppler shift, circle.h:264-311)
   bool ov = false;
   V3 ov_color, ov_emission;
+  bool ov_spec = false;  // a texture also rewrote the specular colour
+  V3 ov_specular;
 };
 
 struct Mesh {
@@ -166,6 +177,7 @@ struct Entity {
   // sphere
   V3 position;
   double radius = 0;
+  int hemisphere = 0;  // 'hemisphere': the half with y >= 0 about the centre
   // uvplane (plane.h:129-167)
   V3 org, u_axis, v_axis, normal;
   double u_length = 0, v_length = 0;
@@ -249,7 +261,88 @@ thread_local uint64_t tl_nodes = 0, tl_tris = 0, tl_segments = 0;
 
 // -------------------------------------------------------------- primitives
 // Sphere::intersect core (sphere.h:68-96)
-bool sphere_hit(const Entity& e, V3 org, V3 dir, Hit& h) {
+// (int) of a double as x86-64's cvttsd2si gives it: NaN and values out of
+// range become INT_MIN (the reference's texel indices take NaN at the poles)
+inline int trunc_int(double x) {
+  if (!(x > -2147483649.0 && x < 2147483648.0)) return INT32_MIN;
+  return (int)x;
+}
+
+// the repeat wrap of a texture coordinate (sphere.h:189-196, plane.h:241-248)
+inline double wrap01(double x) {
+  double dmy;
+  if (x < 0 || x > 1) x = std::modf(x, &dmy);
+  if (x < 0) x = 1.0 - std::fabs(x);
+  return x;
+}
+
+inline void texel_rgb(const Material& m, int i, int j, V3& c) {
+  const unsigned char* t = &(*m.tex)[3 * ((size_t)i * m.tex_w + j)];
+  c = V3((double)t[0] / 255.0, (double)t[1] / 255.0, (double)t[2] / 255.0);
+}
+
+inline V3 ibl_rgb(const Material& m, int i, int j) {
+  const double* t = &(*m.ibl)[3 * ((size_t)i * m.ibl_w + j)];
+  return V3(t[0], t[1], t[2]);
+}
+
+// the sphere's (u, v) of one mapping (sphere.h:117-180, :245-300): the
+// spherical angles, then equirectangular, angular and panoramic, each
+// replacing the last where set; swap_uv: the IBL block's (theta, phi) order
+void sphere_uv(const Material& m, V3 vv, bool swap_uv, bool clamp_angular, double& u, double& v) {
+  const double th = std::acos(std::max(-1.0, std::min(1.0, vv.z)));  // SphericalTheta (vector3d.h:259-261)
+  double ph = std::atan2(vv.y, vv.x);                                 // SphericalPhi (:262-267)
+  if (ph < 0.0) ph += TWOPI;
+  if (ph >= TWOPI) ph = 0.0;
+  u = swap_uv ? th / PI : ph / TWOPI;
+  v = swap_uv ? ph / TWOPI : th / PI;
+  if (m.map_flags & PR_MAP_EQUIRECTANGULAR) {
+    const double len = std::sqrt(vv.x * vv.x + vv.y * vv.y + vv.z * vv.z);
+    if (len == 0.0) {
+      u = 0.0;
+      v = 0.5;
+    } else {
+      const double x = vv.x / len, y = vv.y / len, z = vv.z / len;
+      const double lambda = std::atan2(z, x);
+      const double phi = std::asin(std::fmax(-1.0, std::fmin(1.0, y)));
+      double uu = (lambda + PI) / (2.0 * PI);
+      double vv2 = (0.5 * PI - phi) / PI;
+      uu = uu - std::floor(uu);
+      if (vv2 < 0.0) vv2 = 0.0;
+      else if (vv2 > 1.0) vv2 = 1.0;
+      u = uu;
+      v = vv2;
+    }
+  }
+  if (m.map_flags & PR_MAP_ANGULAR) {
+    double s = vv.z;
+    if (clamp_angular) {
+      if (vv.z < -1.0) s = -1.0;
+      if (vv.z > 1.0) s = 1.0;
+    }
+    double r = (1.0 / PI) * std::acos(s);
+    r /= std::sqrt(vv.x * vv.x + vv.y * vv.y);
+    u = vv.x * r;
+    v = vv.y * r;
+    u = 0.5 * u + 0.5;
+    v = 0.5 * v + 0.5;
+  }
+  if (m.map_flags & PR_MAP_PANORAMIC) {
+    double s = vv.y;
+    if (vv.y < -1.0) s = -1.0;
+    if (vv.y > 1.0) s = 1.0;
+    u = 1.0 + std::atan2(vv.x, -vv.z) / PI;
+    v = std::acos(s) / PI;
+    const double a = u, b = v;
+    u = 0.5 * a;
+    v = 1.0 - b;
+  }
+}
+
+// Sphere::intersect (sphere.h:68-103) with its texture and IBL parts
+// (sphere.h:104-240): the hit point's colour and specular from the texture,
+// its colour and emission from the IBL image
+bool sphere_hit(const Scene& s, const Entity& e, V3 org, V3 dir, Hit& h) {
   const V3 p_o = e.position - org;
   const double b = dot(p_o, dir);
   const double D4 = b * b - dot(p_o, p_o) + e.radius * e.radius;
@@ -262,11 +355,70 @@ bool sphere_hit(const Entity& e, V3 org, V3 dir, Hit& h) {
   h.normal = normalize(h.position - e.position);
   if (e.normal_inverse < 0) h.normal = h.normal * -1.0;
   h.material = e.material;
+  const V3 p = h.position - e.position;
+  if (e.hemisphere && p.y < 0.0) return false;
+  const Material& m = s.mats[e.material];
+  if (!m.tex && !m.ibl) return true;
+  const double pp[3] = {p.x, p.y, p.z};
+  int X = 0, Y = 1, Z = 2;
+  if (m.map_flags & PR_MAP_HEMISPHERE) {
+    X = 2;
+    Y = 0;
+    Z = 1;
+  }
+  const V3 vv(pp[X] / e.radius, pp[Y] / e.radius, pp[Z] / e.radius);
+  const bool pole = !(std::fabs(pp[Z] - e.radius) > EPS16);
+  V3 color = m.color, emission = m.emission, specular = m.specular;
+  bool rewrote = false;
+  if (m.tex && !pole) {
+    double u, v;
+    sphere_uv(m, vv, false, false, u, v);
+    if (e.hemisphere) u *= 2.0;
+    const double uu = wrap01(u * (double)m.repeat), vw = wrap01(v * (double)m.repeat);
+    int j = trunc_int((m.tex_w - 1) * uu);
+    int i = trunc_int((m.tex_h - 1) * vw);
+    if (m.map_flags & PR_MAP_HEMISPHERE) {
+      j = trunc_int((m.tex_w - 1) / 2 + (m.tex_w - 1) * 0.5 * pp[X] / e.radius);
+      i = trunc_int((m.tex_h - 1) / 2 + (m.tex_h - 1) * 0.5 * pp[Y] / e.radius);
+    }
+    if (i < 0) i = 0;
+    if (i >= m.tex_h - 1) i = m.tex_h - 1;
+    if (j < 0) j = 0;
+    if (j >= m.tex_w - 1) j = m.tex_w - 1;
+    texel_rgb(m, i, j, color);
+    specular = color;
+    h.ov_spec = true;
+    rewrote = true;
+  }
+  if (m.ibl && !pole) {
+    double u, v;
+    sphere_uv(m, vv, true, true, u, v);
+    if (e.hemisphere) u *= 2.0;
+    int j = trunc_int((m.ibl_w - 1) * u);
+    int i = trunc_int((m.ibl_h - 1) * v);
+    if (m.map_flags & PR_MAP_HEMISPHERE) {
+      j = trunc_int((m.ibl_w - 1) / 2 + (m.ibl_w - 1) * 0.5 * pp[X] / e.radius);
+      i = trunc_int((m.ibl_h - 1) / 2 + (m.ibl_h - 1) * 0.5 * pp[Y] / e.radius);
+    }
+    if (i < 0) i = 0;
+    if (i >= m.ibl_h - 1) i = m.ibl_h - 1;
+    if (j < 0) j = 0;
+    if (j >= m.ibl_w - 1) j = m.ibl_w - 1;
+    color = ibl_rgb(m, i, j);
+    emission = m.ibl_coef * color;
+    rewrote = true;
+  }
+  if (rewrote) {
+    h.ov = true;
+    h.ov_color = color;
+    h.ov_emission = emission;
+    h.ov_specular = specular;
+  }
   return true;
 }
 
 // UVPlane::intersect (plane.h:220-239) over Plane::intersect (plane.h:86-110)
-bool uvplane_hit(const Entity& e, V3 org, V3 dir, Hit& h) {
+bool uvplane_hit(const Scene& s, const Entity& e, V3 org, V3 dir, Hit& h) {
   V3 normal2 = e.normal;
   if (e.normal_inverse < 0) normal2 = e.normal * -1.0;
   const double d = dot(dir, normal2);
@@ -280,6 +432,24 @@ bool uvplane_hit(const Entity& e, V3 org, V3 dir, Hit& h) {
   const double v = dot(V3(h.position - e.org), e.v_axis) / e.v_length;
   if (u < 0 || u > e.u_length) return false;
   if (v < 0 || v > e.v_length) return false;
+  // the texture and IBL parts (plane.h:241-273)
+  const Material& m = s.mats[e.material];
+  if (!m.tex && !m.ibl) return true;
+  const double uu = wrap01(u * (double)m.repeat), vw = wrap01(v * (double)m.repeat);
+  V3 color = m.color, emission = m.emission, specular = m.specular;
+  if (m.tex) {
+    texel_rgb(m, trunc_int((m.tex_h - 1) * vw), trunc_int((m.tex_w - 1) * uu), color);
+    specular = color;
+    h.ov_spec = true;
+  }
+  if (m.ibl) {
+    color = ibl_rgb(m, trunc_int((m.ibl_h - 1) * vw), trunc_int((m.ibl_w - 1) * uu));
+    emission = m.ibl_coef * color;
+  }
+  h.ov = true;
+  h.ov_color = color;
+  h.ov_emission = emission;
+  h.ov_specular = specular;
   return true;
 }
 
@@ -611,8 +781,8 @@ bool intersect(const Scene& s, V3 org, V3 dir, Hit& isect) {
     Hit h;
     bool got = false;
     switch (e.type) {
-      case PR_ENT_SPHERE: got = sphere_hit(e, o2, dir, h); break;
-      case PR_ENT_UVPLANE: got = uvplane_hit(e, o2, dir, h); break;
+      case PR_ENT_SPHERE: got = sphere_hit(s, e, o2, dir, h); break;
+      case PR_ENT_UVPLANE: got = uvplane_hit(s, e, o2, dir, h); break;
       case PR_ENT_CIRCLE: got = circle_hit(s, e, o2, dir, h); break;
       case PR_ENT_POLYGON: got = qbvh_hit(s, e, o2, dir, h); break;
       default: break;
@@ -642,6 +812,23 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
     m.ward_ax = pm.ward_alpha[0];
     m.ward_ay = pm.ward_alpha[1];
     m.phong_n = pm.phong_exponent;
+    if (pm.texture && pm.texture_width > 0 && pm.texture_height > 0) {
+      m.tex_w = pm.texture_width;
+      m.tex_h = pm.texture_height;
+      m.tex = std::make_shared<const std::vector<unsigned char>>(pm.texture, pm.texture + 3 * (size_t)m.tex_w * m.tex_h);
+    }
+    if ((pm.ibl_rgb8 || pm.ibl_rgbf) && pm.ibl_width > 0 && pm.ibl_height > 0) {
+      // IBL_Color (material.h:230-236): a bitmap's bytes / 255, an HDR image's values
+      m.ibl_w = pm.ibl_width;
+      m.ibl_h = pm.ibl_height;
+      const size_t n = 3 * (size_t)m.ibl_w * m.ibl_h;
+      auto v = std::make_shared<std::vector<double>>(n);
+      for (size_t k = 0; k < n; k++) (*v)[k] = pm.ibl_rgb8 ? (double)pm.ibl_rgb8[k] / 255.0 : (double)pm.ibl_rgbf[k];
+      m.ibl = v;
+    }
+    m.ibl_coef = pm.ibl_coef;
+    m.repeat = pm.repeat;
+    m.map_flags = pm.map_flags;
     if (m.type == PR_MAT_SSS_REFRACTION || m.type == PR_MAT_SSS_DIFFUSE || m.type == PR_MAT_SSS_WARD) {
       // the material's own participatingMediaParam (scene_env.h:1305-1362); the
       // entity set-up calls setup_Scattering when the SCATTERING line is > PS_EPS
@@ -706,7 +893,12 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
     if (pe.type == PR_ENT_SPHERE) {
       e.position = V3(pe.p[0], pe.p[1], pe.p[2]);
       e.radius = pe.radius;
+      e.hemisphere = pe.hemisphere ? 1 : 0;
       e.area = FORPI * e.radius * e.radius;  // Sphere::CalcArea (sphere.h:23-27)
+      if (e.hemisphere) {
+        e.area = 0.5 * e.area;
+        if (m.isLight()) { err = "hemisphere lights are not sampled here"; return PR_E_UNSUPPORTED; }
+      }
       const V3 ext(e.radius, e.radius, e.radius), eps(0.01, 0.01, 0.01);  // sphere.h:58-63
       e.bb_min = e.position - ext - eps;
       e.bb_max = e.position + ext + eps;
@@ -1087,6 +1279,7 @@ Material hit_mat(const Scene& s, const Hit& h) {
     m.color = h.ov_color;
     m.emission = h.ov_emission;
   }
+  if (h.ov_spec) m.specular = h.ov_specular;
   return m;
 }
 
@@ -1813,6 +2006,9 @@ V3 radiance(Ctx& c, V3 org, V3 dir, int depth) {
     return s.background;
   }
   const Material mat = hit_mat(s, hp);
+  // an object with an IBL image gives its hit point's emission and nothing
+  // else (radiance.h:45-50, IBL_LIGHT 0)
+  if (mat.ibl) return mat.emission;
   const V3 on = dot(hp.normal, dir) < 0.0 ? hp.normal : (-1.0 * hp.normal);
   V3 rw = mat.emission;
   switch (mat.type) {

@@ -33,6 +33,10 @@ PR_ENT_CIRCLE = 4
 PR_KERR_FP64 = 0
 PR_KERR_FP32 = 1
 PR_ENT_POLYGON = 5
+PR_MAP_HEMISPHERE = 1
+PR_MAP_ANGULAR = 2
+PR_MAP_PANORAMIC = 4
+PR_MAP_EQUIRECTANGULAR = 8
 
 PR_MODE_MEGAKERNEL = 0
 PR_MODE_WAVEFRONT = 1
@@ -69,6 +73,16 @@ class pr_material(C.Structure):
         ("r_refractive_index", C.c_double),
         ("ward_alpha", C.c_double * 2),
         ("phong_exponent", C.c_double),
+        ("texture", C.POINTER(C.c_uint8)),
+        ("texture_width", C.c_int32),
+        ("texture_height", C.c_int32),
+        ("ibl_rgb8", C.POINTER(C.c_uint8)),
+        ("ibl_rgbf", C.POINTER(C.c_float)),
+        ("ibl_width", C.c_int32),
+        ("ibl_height", C.c_int32),
+        ("ibl_coef", C.c_double),
+        ("repeat", C.c_int32),
+        ("map_flags", C.c_int32),
     ]
 
 
@@ -87,7 +101,7 @@ class pr_entity(C.Structure):
         ("blackhole_disk", C.c_int32),
         ("parallel_light", C.c_int32),
         ("spot_light", C.c_int32),
-        ("pad0", C.c_int32),
+        ("hemisphere", C.c_int32),
         ("light_dir", D3),
         ("spot_angle", C.c_double * 2),
         ("spot_falloff", C.c_double),

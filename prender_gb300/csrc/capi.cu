@@ -198,6 +198,10 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   PR_CUDA(c, upload(o.rnodes, h.rnodes, c->stream));
   PR_CUDA(c, upload(o.rtris, h.rtris, c->stream));
   PR_CUDA(c, upload(o.fnorm, h.fnorm, c->stream));
+  // texel pools only for scenes with images (an allocation more or less
+  // moves the wavefront pool, whose placement wf_shade is sensitive to)
+  if (!h.texels.empty()) PR_CUDA(c, upload(o.texels, h.texels, c->stream));
+  if (!h.ibl_texels.empty()) PR_CUDA(c, upload(o.ibl_texels, h.ibl_texels, c->stream));
   PR_CUDA(c, upload(o.kerr_tex, h.kerr_texture, c->stream));
   PR_CUDA(c, upload(o.kerr_disk_tex, h.kerr_disk_texture, c->stream));
   PR_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -213,6 +217,8 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   S.rnodes = (const WNode*)o.rnodes.p;
   S.rtris = (const float4*)o.rtris.p;
   S.fnorm = (const float*)o.fnorm.p;
+  S.texels = (const float4*)o.texels.p;
+  S.ibl_texels = (const float4*)o.ibl_texels.p;
   S.n_ents = (int)h.ents.size();
   S.n_lights = (int)h.lights.size();
   S.n_point_lights = 0;
@@ -228,9 +234,11 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   S.scene_scale = h.scene_scale;
   S.has_sss = 0;
   S.has_glossy = 0;
+  S.has_tex = 0;
   for (const GMaterial& gm : h.mats) {
     S.has_sss |= gm.sss;
     S.has_glossy |= (gm.type == PR_MAT_WARD || gm.type == PR_MAT_PHONG) ? 1 : 0;
+    S.has_tex |= (gm.tex_off >= 0 || gm.ibl_off >= 0) ? 1 : 0;
   }
   for (int k = 0; k < 3; k++) {
     S.bg[k] = (float)h.background[k];
@@ -650,7 +658,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   WfLaunch L;
   L.shade_blocks = (P + 127) / 128;
   L.sss = sss ? 1 : 0;
-  L.point = sc.dev.n_point_lights > 0 ? 1 : 0;
+  L.ext = (sc.dev.n_point_lights > 0 || sc.dev.has_tex) ? 1 : 0;
   // persistent traversal: one resident wave of blocks (more waves only queue
   // behind it and find the rays taken)
   int sms = 0;
@@ -670,7 +678,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
   const bool use_graph = !(host_loop && host_loop[0] == '1') && !c->force_host_loop;
   if (use_graph && !c->wf_graph_failed &&
       (!c->wf_graph || c->wf_graph_slots != P || c->wf_graph_trace_blocks != L.trace_blocks ||
-       c->wf_graph_variant != L.sss + 2 * L.point)) {
+       c->wf_graph_variant != L.sss + 2 * L.ext)) {
     if (c->wf_graph) {
       cudaStreamSynchronize(c->stream);  // the previous render's launch has finished with it
       cudaGraphExecDestroy(c->wf_graph);
@@ -684,7 +692,7 @@ static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int a
     } else {
       c->wf_graph_slots = P;
       c->wf_graph_trace_blocks = L.trace_blocks;
-      c->wf_graph_variant = L.sss + 2 * L.point;
+      c->wf_graph_variant = L.sss + 2 * L.ext;
     }
   }
   c->wf_passes = 0;
@@ -778,6 +786,8 @@ static int adjoint_checks(pr_ctx* c, const pr_render_params* p) {
   if (c->cur.dev.has_sss) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover subsurface materials");
   if (c->cur.dev.n_point_lights > 0)
     return fail(c, PR_E_UNSUPPORTED, "the adjoint pass covers area lights only (no parallel, spot or infinity lights)");
+  if (c->cur.dev.has_tex)
+    return fail(c, PR_E_UNSUPPORTED, "the adjoint pass differentiates material colours, not textures");
   for (const GMaterial& m : c->cur.host.mats)
     if (m.type == PR_MAT_WARD || m.type == PR_MAT_PHONG)
       return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover Ward or Phong materials (their lobes scale "

@@ -35,11 +35,12 @@ struct DevBuf {
 // one uploaded scene: host build, device copies, device view
 struct SceneObjData {
   HostScene host;
-  DevBuf ents, mats, nodes, tris, rnodes, rtris, fnorm, kerr_tex, kerr_disk_tex;
+  DevBuf ents, mats, nodes, tris, rnodes, rtris, fnorm, kerr_tex, kerr_disk_tex, texels, ibl_texels;
   DevScene dev{};
   GKerr kerr{};
   void release() {
-    for (DevBuf* b : {&ents, &mats, &nodes, &tris, &rnodes, &rtris, &fnorm, &kerr_tex, &kerr_disk_tex}) b->release();
+    for (DevBuf* b : {&ents, &mats, &nodes, &tris, &rnodes, &rtris, &fnorm, &kerr_tex, &kerr_disk_tex, &texels, &ibl_texels})
+      b->release();
   }
 };
 
@@ -72,7 +73,7 @@ struct pr_ctx {
   cudaGraphExec_t wf_graph = nullptr;
   unsigned int wf_graph_slots = 0;
   unsigned int wf_graph_trace_blocks = 0;
-  int wf_graph_variant = 0;          // shading kernel the graph launches: sss + 2 * point
+  int wf_graph_variant = 0;          // shading kernel the graph launches: sss + 2 * ext
   unsigned int tuned_slots = 0;      // autotuner's wavefront pool size (0: default)
   unsigned int tuned_trace_bps = 0;  // autotuner's traversal blocks per SM (0: default)
   bool force_host_loop = false;      // the autotuner times candidates with the host-driven loop

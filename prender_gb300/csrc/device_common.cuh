@@ -124,6 +124,8 @@ __device__ __forceinline__ bool exact_sphere(const GEntity& e, dv3 o, dv3 d, dou
   const double t1 = ds(b, s), t2 = da(b, s);
   if (t1 < kEps && t2 < kEps) return false;
   t = (t1 > kEps) ? t1 : t2;
+  // a hemisphere keeps the hit only on its y >= y_centre half (sphere.h:98-103)
+  if (e.hemisphere && ds(da(o.y, dm(t, d.y)), e.p[1]) < 0.0) return false;
   return true;
 }
 

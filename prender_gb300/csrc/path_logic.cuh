@@ -255,11 +255,11 @@ __device__ __forceinline__ void push_shadow(const DevScene& S, const LightSample
 // factor (parallel_light_direct / spot_light_direct, :406-477), where the
 // reference takes the light kind from its sorted list at the entity's
 // registration index.
-template <bool POINT>
+template <bool EXT>
 __device__ __forceinline__ float perfect_direct(const DevScene& S, float3 o, float3 d, bool hit, const FastHit& h,
                                                 int& mat) {
   mat = -1;
-  if (!POINT) {
+  if (!EXT) {
     if (hit && S.entf[h.ent].is_light) mat = S.entf[h.ent].material;
     return 1.0f;
   }
@@ -433,7 +433,7 @@ __device__ __forceinline__ float dd_bssrdf(const GMaterial& m, float3 xi, float3
 // samples at the exit point (colour / pi, the unflipped surface normal as
 // orienting normal).  The reference computes Fresnel factors here that it
 // does not apply.
-template <bool POINT>
+template <bool EXT>
 __device__ inline void sss_exit(const DevScene& S, const RenderCfg& cfg, const GMaterial& m, int in_ent,
                                 const FastHit& oh, const Vertex& ov, float3 dir, float rr2, float3 beta, int depth,
                                 Rng& rng, ShadowReq* sh, int& nsh, PathState& ps) {
@@ -458,13 +458,13 @@ __device__ inline void sss_exit(const DevScene& S, const RenderCfg& cfg, const G
   const float3 C = ld3(m.color);
   const float3 bw = beta * Tr * C * (1.0f / rr2);
   const bool nee = cfg.nee != 0;
-  if (S.n_lights > 0 && (nee || POINT)) {
+  if (S.n_lights > 0 && (nee || EXT)) {
     // without NEE only parallel, spot and infinity lights are sampled (:519-535)
     const float3 origin = offset_ray(ov.p, n);
     const float3 wn = bw * C * (0.31830988618379067154f / 3.0f);
     for (int i = 0; i < 3; i++) {
       const GLight& L = pick_light(S, rng);
-      if (POINT && L.kind != PR_LIGHT_AREA) {  // colour, not colour / pi
+      if (EXT && L.kind != PR_LIGHT_AREA) {  // colour, not colour / pi
         LightSample ls;
         if (point_light_sample(S, L, ov.p, n, origin, true, cfg.media != 0 && S.medium.on != 0, rng, ls))
           push_shadow(S, ls, wn * ls.k * 3.14159265358979323846f, L.mat, sh, nsh);
@@ -499,6 +499,118 @@ __device__ inline void sss_exit(const DevScene& S, const RenderCfg& cfg, const G
   ps.d = nd;
 }
 
+// ---- textures and IBL images on hits (sphere.h:104-240, plane.h:241-273)
+
+// the sphere's (u, v) of a mapping: the spherical angles, then the
+// equirectangular, angular and panoramic maps, each replacing the last where
+// set; ibl: the IBL block's order (u from theta, v from phi) and its clamp
+// of the angular map's cosine
+__device__ __forceinline__ void sphere_uv(int flags, float3 vv, bool ibl, float& u, float& v) {
+  const float kPi = 3.14159265358979323846f, kTwoPi = 6.28318530717958647692f;
+  const float th = acosf(fminf(1.0f, fmaxf(-1.0f, vv.z)));  // SphericalTheta (vector3d.h:259-261)
+  float ph = atan2f(vv.y, vv.x);                             // SphericalPhi (:262-267)
+  if (ph < 0.0f) ph += kTwoPi;
+  if (ph >= kTwoPi) ph = 0.0f;
+  u = ibl ? th / kPi : ph / kTwoPi;
+  v = ibl ? ph / kTwoPi : th / kPi;
+  if (flags & PR_MAP_EQUIRECTANGULAR) {
+    const float len = sqrtf(vv.x * vv.x + vv.y * vv.y + vv.z * vv.z);
+    if (len == 0.0f) {
+      u = 0.0f;
+      v = 0.5f;
+    } else {
+      const float lambda = atan2f(vv.z / len, vv.x / len);
+      const float phi = asinf(fmaxf(-1.0f, fminf(1.0f, vv.y / len)));
+      u = (lambda + kPi) / kTwoPi;
+      u = u - floorf(u);
+      v = fminf(1.0f, fmaxf(0.0f, (0.5f * kPi - phi) / kPi));
+    }
+  }
+  if (flags & PR_MAP_ANGULAR) {
+    const float c = ibl ? fminf(1.0f, fmaxf(-1.0f, vv.z)) : vv.z;
+    const float r = acosf(c) / kPi / sqrtf(vv.x * vv.x + vv.y * vv.y);
+    u = 0.5f * (vv.x * r) + 0.5f;
+    v = 0.5f * (vv.y * r) + 0.5f;
+  }
+  if (flags & PR_MAP_PANORAMIC) {
+    const float c = fminf(1.0f, fmaxf(-1.0f, vv.y));
+    u = 0.5f * (1.0f + atan2f(vv.x, -vv.z) / kPi);
+    v = 1.0f - acosf(c) / kPi;
+  }
+}
+
+// the repeat wrap (sphere.h:189-196): the fraction, negatives from 1
+__device__ __forceinline__ float tex_wrap(float x) {
+  if (x < 0.0f || x > 1.0f) x = x - truncf(x);
+  if (x < 0.0f) x = 1.0f - fabsf(x);
+  return x;
+}
+
+__device__ __forceinline__ int tex_clamp(int i, int n) { return min(max(i, 0), n - 1); }
+
+// The hit point's material where a texture or IBL image rewrites it: the
+// texture gives colour and specular, the IBL image colour and emission
+// (ibl_coef times the texel).  Returns true for a material with an IBL
+// image, whose hit the caller ends with its emission (radiance.h:45-50).
+__device__ inline bool hit_texture(const DevScene& S, const GMaterial& m, const GEntF& e, const GEntity& ed, float3 p,
+                                   float3& C, float3& E, float3& Sp) {
+  const bool has_ibl = m.ibl_off >= 0;
+  if (e.type == PR_ENT_UVPLANE) {
+    const float3 rel = p - f3(e.p[0], e.p[1], e.p[2]);
+    const float u = dot(rel, f3(e.u[0], e.u[1], e.u[2])) / e.u_length;
+    const float v = dot(rel, f3(e.v[0], e.v[1], e.v[2])) / e.v_length;
+    const float uu = tex_wrap(u * (float)m.repeat), vv = tex_wrap(v * (float)m.repeat);
+    if (m.tex_off >= 0) {
+      const float4 t = __ldg(S.texels + m.tex_off + (size_t)tex_clamp((int)((m.tex_h - 1) * vv), m.tex_h) * m.tex_w +
+                             tex_clamp((int)((m.tex_w - 1) * uu), m.tex_w));
+      C = Sp = f3(t.x, t.y, t.z);
+    }
+    if (has_ibl) {
+      const float4 t = __ldg(S.ibl_texels + m.ibl_off +
+                             (size_t)tex_clamp((int)((m.ibl_h - 1) * vv), m.ibl_h) * m.ibl_w +
+                             tex_clamp((int)((m.ibl_w - 1) * uu), m.ibl_w));
+      C = f3(t.x, t.y, t.z);
+      E = C * m.ibl_coef;
+    }
+    return has_ibl;
+  }
+  // sphere / hemisphere: hemisphere_map looks along y (x, y, z -> z, x, y)
+  const float r = (float)ed.radius;
+  const float3 q = p - f3(e.p[0], e.p[1], e.p[2]);
+  const bool hm = (m.map_flags & PR_MAP_HEMISPHERE) != 0;
+  const float px = hm ? q.z : q.x, py = hm ? q.x : q.y, pz = hm ? q.y : q.z;
+  if (!(fabsf(pz - r) > 1.0e-16f)) return has_ibl;  // at the pole the reference leaves the material
+  const float3 vv = f3(px / r, py / r, pz / r);
+  if (m.tex_off >= 0) {
+    float u, v;
+    sphere_uv(m.map_flags, vv, false, u, v);
+    if (ed.hemisphere) u *= 2.0f;
+    int j = (int)((m.tex_w - 1) * tex_wrap(u * (float)m.repeat));
+    int i = (int)((m.tex_h - 1) * tex_wrap(v * (float)m.repeat));
+    if (hm) {
+      j = (int)((float)((m.tex_w - 1) / 2) + (m.tex_w - 1) * 0.5f * px / r);
+      i = (int)((float)((m.tex_h - 1) / 2) + (m.tex_h - 1) * 0.5f * py / r);
+    }
+    const float4 t = __ldg(S.texels + m.tex_off + (size_t)tex_clamp(i, m.tex_h) * m.tex_w + tex_clamp(j, m.tex_w));
+    C = Sp = f3(t.x, t.y, t.z);
+  }
+  if (has_ibl) {
+    float u, v;
+    sphere_uv(m.map_flags, vv, true, u, v);
+    if (ed.hemisphere) u *= 2.0f;
+    int j = (int)((m.ibl_w - 1) * u);
+    int i = (int)((m.ibl_h - 1) * v);
+    if (hm) {
+      j = (int)((float)((m.ibl_w - 1) / 2) + (m.ibl_w - 1) * 0.5f * px / r);
+      i = (int)((float)((m.ibl_h - 1) / 2) + (m.ibl_h - 1) * 0.5f * py / r);
+    }
+    const float4 t = __ldg(S.ibl_texels + m.ibl_off + (size_t)tex_clamp(i, m.ibl_h) * m.ibl_w + tex_clamp(j, m.ibl_w));
+    C = f3(t.x, t.y, t.z);
+    E = C * m.ibl_coef;
+  }
+  return has_ibl;
+}
+
 // the Phong (kind 4) or Ward (kind 5) lobe towards ldir as the reference's
 // next-event samples evaluate it (directLight_radiance.h:211-256), with the
 // specular colour left to the caller; 0 where it gives nothing
@@ -520,13 +632,14 @@ __device__ __forceinline__ float glossy_lobe(int kind, const GMaterial& m, float
 
 // Shades the vertex found by the last closest-hit query of ps (SSS: with the
 // subsurface material case compiled in; GLOSSY: with the Ward and Phong
-// lobes; POINT: with parallel, spot and infinity lights; the plain form
-// keeps a leaner instantiation for scenes without them).  A tracer
+// lobes; EXT: with parallel, spot and infinity lights, textures and IBL
+// images; the plain form keeps a leaner instantiation for scenes without
+// them).  A tracer
 // that builds the vertex itself (the Kerr geodesic tracer) passes it as pre,
 // and the colour a miss returns as miss (radiance.h:30-43); straight-ray
 // callers leave both null.  ovr (colour, emission) replaces the material's
 // where the entity rewrote its hit point's copy (the accretion disk).
-template <bool SSS = false, bool GLOSSY = true, bool POINT = false>
+template <bool SSS = false, bool GLOSSY = true, bool EXT = false>
 __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& ps, bool hit, const FastHit& h,
                      uint64_t sample_id, ShadowReq* sh, int& nsh, PathState& child, uint32_t* err,
                      const Vertex* pre = nullptr, const float3* miss = nullptr, EmissionTap* tap = nullptr,
@@ -535,9 +648,9 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   const bool nee = cfg.nee != 0;
   const bool media = cfg.media != 0 && S.medium.on != 0;
   if (ps.dp) {  // light along a specular / refraction direction (directLight_radiance.h:516-556)
-    if (POINT) {
+    if (EXT) {
       int lm;
-      const float fl = perfect_direct<POINT>(S, ps.o, ps.d, hit, h, lm);
+      const float fl = perfect_direct<EXT>(S, ps.o, ps.d, hit, h, lm);
       if (lm >= 0 && fl > 0.0f) {
         // the medium attenuates a light entity's term over the hit distance (:549-552)
         const float3 w = ps.dpw * ((hit && media) ? medium_tr(S.medium, h.t) : f3(1, 1, 1)) * fl;
@@ -567,11 +680,18 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   else make_vertex(S, ps.o, ps.d, h, v);
   const GMaterial& m = S.mats[v.mat];
   const GEntF& ent = S.entf[v.ent];
-  const float3 E = ovr ? ovr[1] : ld3(m.emission), C = ovr ? ovr[0] : ld3(m.color);
+  float3 E = ovr ? ovr[1] : ld3(m.emission), C = ovr ? ovr[0] : ld3(m.color);
+  float3 Sp = ld3(m.specular);
+  if (EXT && (m.tex_off >= 0 || m.ibl_off >= 0) && hit_texture(S, m, ent, S.ents[v.ent], v.p, C, E, Sp)) {
+    // an object with an IBL image gives its hit point's emission and nothing
+    // else (radiance.h:45-50)
+    ps.L += ps.beta * E;
+    if (tap) tap->em(v.mat, ps.beta);
+    return SHADE_END;
+  }
   const float3 d = ps.d;
   const float3 on = dot(v.n, d) < 0.0f ? v.n : -v.n;
   // RR weight: emission + the reflectances the type can scatter with (radiance.h:79-89)
-  const float3 Sp = ld3(m.specular);
   float p_rr = maxc(m.type == PR_MAT_WARD ? E + C + Sp : m.type == PR_MAT_PHONG ? E + Sp : E + C);
   if (ps.depth > cfg.depth_limit) p_rr *= exp2f((float)(cfg.depth_limit - ps.depth));
   const float3 trr = media ? medium_tr(S.medium, v.t) : f3(1, 1, 1);
@@ -617,7 +737,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
         // emission / pi for area lights, emission for the other kinds
         for (int i = 0; i < 3; i++) {
           const GLight& L = pick_light(S, rng);
-          if (POINT && L.kind != PR_LIGHT_AREA) {
+          if (EXT && L.kind != PR_LIGHT_AREA) {
             LightSample ls;
             if (point_light_sample(S, L, npos, f3(0, 0, 0), npos, false, true, rng, ls))
               push_shadow(S, ls, ps.beta * f * ls.k * (1.0f / 3.0f), L.mat, sh, nsh);
@@ -692,14 +812,14 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     const float3 nd = normalize(u * (cs * r2s) + w2 * (sn * r2s) + on * sqrtf(1.0f - r2));
     const float3 origin = offset_ray(v.p, on);
     if (S.n_lights > 0) {
-      if (nee || POINT) {
+      if (nee || EXT) {
         // eval_direct_radiance (directLight_radiance.h:19-313), 3 samples
         // averaged; without NEE only parallel, spot and infinity lights
         // (brdf.h:590-605), which take the colour, not colour / pi
         const float3 w = ps.beta * tri * C * (inv_rr * 0.31830988618379067154f * (1.0f / 3.0f));
         for (int i = 0; i < 3; i++) {
           const GLight& L = pick_light(S, rng);
-          if (POINT && L.kind != PR_LIGHT_AREA) {
+          if (EXT && L.kind != PR_LIGHT_AREA) {
             LightSample ls;
             if (point_light_sample(S, L, v.p, on, origin, true, media, rng, ls))
               push_shadow(S, ls, w * ls.k * 3.14159265358979323846f, L.mat, sh, nsh);
@@ -787,12 +907,12 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
       return SHADE_END;
     }
     const float3 origin = offset_ray(v.p, on);
-    if (S.n_lights > 0 && (nee || POINT)) {
+    if (S.n_lights > 0 && (nee || EXT)) {
       // without NEE only parallel, spot and infinity lights (brdf.h:128-146)
       const float3 w = ps.beta * tri * Sp * (inv_rr * (1.0f / 3.0f));
       for (int i = 0; i < 3; i++) {
         const GLight& L = pick_light(S, rng);
-        if (POINT && L.kind != PR_LIGHT_AREA) {
+        if (EXT && L.kind != PR_LIGHT_AREA) {
           LightSample ls;
           if (!point_light_sample(S, L, v.p, on, origin, true, media, rng, ls)) continue;
           const float f = glossy_lobe(kind, m, refl, in, on, a, b, ls.ldir);
@@ -971,7 +1091,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
         if (oh.t < 1.0e-4f) {  // too thin to scatter: leave at once (no CUT0 on this result)
           make_vertex(S, org0, ts, oh, ov);
           if (frame) frame->open = 1;
-          sss_exit<POINT>(S, cfg, m, v.ent, oh, ov, ts, rr2a, bw1, ps.depth + 2, rng, sh, nsh, ps);
+          sss_exit<EXT>(S, cfg, m, v.ent, oh, ov, ts, rr2a, bw1, ps.depth + 2, rng, sh, nsh, ps);
           ps.draws = rng_draws(rng);
           return SHADE_CONTINUE;
         }
@@ -1021,7 +1141,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
             return SHADE_END;
           }
         }
-        sss_exit<POINT>(S, cfg, m, v.ent, wh, ov, nd, rr2b, bw2, ps.depth + 3, rng, sh, nsh, ps);
+        sss_exit<EXT>(S, cfg, m, v.ent, wh, ov, nd, rr2b, bw2, ps.depth + 3, rng, sh, nsh, ps);
         ps.draws = rng_draws(rng);
         return SHADE_CONTINUE;
       }
@@ -1033,7 +1153,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
                             dd_bssrdf(m, sp, on2, sw, v.p, on, 2));
       const float k = T12 * cos_wi_n * T21 / pdf_s / pdf_d / accept / p_rr / (1.0f - p_scat);
       const float3 origin_s = offset_ray(sp, on2);
-      if (S.n_lights > 0 && (nee || POINT)) {
+      if (S.n_lights > 0 && (nee || EXT)) {
         // direct_radiance_sample, 3 samples averaged: with NEE at the exit
         // point (the exit object's colour / pi); without it only parallel,
         // spot and infinity lights, at the ENTRY point with its own colour
@@ -1042,7 +1162,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
                           0.31830988618379067154f;
         for (int i = 0; i < 3; i++) {
           const GLight& L = pick_light(S, rng);
-          if (POINT && L.kind != PR_LIGHT_AREA) {
+          if (EXT && L.kind != PR_LIGHT_AREA) {
             const float3 rp = nee ? sp : v.p, rn = nee ? on2 : on;
             const float3 ro = nee ? origin_s : offset_ray(v.p, on);
             const float3 wp = ps.beta * tri * res * (k * (1.0f / 3.0f)) * ld3(S.mats[nee ? exit_mat : v.mat].color);

@@ -94,6 +94,14 @@ struct GMaterial {
   float specular[3];
   float ward_ax, ward_ay;  // Ward roughness along the orienting normal's u / v axes
   float phong_n;           // Phong exponent
+  // textures (sphere.h:104-240, plane.h:241-273): offsets of the texel
+  // records in DevScene::texels (RGB / 255, -1: none) and of the IBL
+  // image's in DevScene::ibl_texels (-1: none)
+  int32_t tex_off, tex_w, tex_h;
+  int32_t ibl_off, ibl_w, ibl_h;
+  float ibl_coef;
+  int32_t repeat;
+  int32_t map_flags;       // PR_MAP_*
 };
 
 struct GEntity {
@@ -122,7 +130,7 @@ struct GEntity {
   // accretion disk under the black hole (circle.h:240-335): set when the
   // disk's material has disk_map and the hole has a disk texture
   int32_t kerr_disk;
-  int32_t pad1;
+  int32_t hemisphere;      // 'hemisphere': only the half with y >= y_centre is hit (sphere.h:98-103)
   double du_axis[3], dv_axis[3];  // the base UVPlane's unit axes and lengths (plane.h:146-157)
   double du_len, dv_len;
   double disk_em[3];              // the material's emission, FP64
@@ -209,6 +217,8 @@ struct DevScene {
   const WNode* rnodes;     // the render path's trees (render_bvh.h)
   const float4* rtris;     // 3 per triangle slot of those
   const float* fnorm;      // 3 per face
+  const float4* texels;    // every material's texture, RGB / 255 (cell(i, j) order)
+  const float4* ibl_texels;  // every IBL image, IBL_Color(i, j) order
   int32_t n_ents;
   int32_t n_lights;
   int32_t n_point_lights;  // parallel, spot and infinity lights (sampled even without NEE)
@@ -221,6 +231,7 @@ struct DevScene {
   float scene_scale;       // max |coordinate| of the scene bounds
   int32_t has_sss;         // a subsurface (dipole) material is present
   int32_t has_glossy;      // a Ward or Phong material is present
+  int32_t has_tex;         // a material has a texture or an IBL image
   GEntF entf[kMaxEntities];
 };
 

@@ -196,8 +196,8 @@ cudaError_t launch_megakernel(const DevScene& S, const RenderCfg& cfg, float* ou
   const uint64_t threads = (uint64_t)cfg.tiles_x * cfg.tiles_y * 32ull * (uint64_t)cfg.chunks;
   const uint32_t blocks = (uint32_t)((threads + 127) / 128);
   // the fuller instantiation (subsurface frames, glossy lobes, parallel /
-  // spot / infinity lights) only where needed
-  if (S.has_sss || S.has_glossy || S.n_point_lights > 0)
+  // spot / infinity lights, textures) only where needed
+  if (S.has_sss || S.has_glossy || S.n_point_lights > 0 || S.has_tex)
     pt_megakernel<true><<<blocks, 128, 0, stream>>>(S, cfg, out, err, counters);
   else pt_megakernel<false><<<blocks, 128, 0, stream>>>(S, cfg, out, err, counters);
   return cudaGetLastError();

@@ -374,6 +374,42 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
     }
     g.roughness_d = pm.roughness;
     g.ior_d = pm.refractive_index;
+    // texture and IBL images (material.h:176-236): texels as float RGB, a
+    // bitmap's bytes / 255 (BitMap cell values), an HDR image's values
+    g.tex_off = g.ibl_off = -1;
+    g.repeat = pm.repeat;
+    g.map_flags = pm.map_flags;
+    g.ibl_coef = (float)pm.ibl_coef;
+    if (pm.texture) {
+      if (pm.texture_width <= 0 || pm.texture_height <= 0) { err = "texture size must be positive"; return PR_E_ARG; }
+      g.tex_off = (int32_t)hs.texels.size();
+      g.tex_w = pm.texture_width;
+      g.tex_h = pm.texture_height;
+      const size_t n = (size_t)g.tex_w * g.tex_h;
+      if (hs.texels.size() + n > (size_t)INT32_MAX) { err = "textures too large"; return PR_E_ARG; }
+      for (size_t k = 0; k < n; k++)
+        hs.texels.push_back(make_float4((float)(pm.texture[3 * k] / 255.0), (float)(pm.texture[3 * k + 1] / 255.0),
+                                        (float)(pm.texture[3 * k + 2] / 255.0), 0.0f));
+    }
+    if (pm.ibl_rgb8 || pm.ibl_rgbf) {
+      if (pm.ibl_rgb8 && pm.ibl_rgbf) { err = "an IBL image is either a bitmap or an HDR image"; return PR_E_ARG; }
+      if (pm.ibl_width <= 0 || pm.ibl_height <= 0) { err = "IBL image size must be positive"; return PR_E_ARG; }
+      g.ibl_off = (int32_t)hs.ibl_texels.size();
+      g.ibl_w = pm.ibl_width;
+      g.ibl_h = pm.ibl_height;
+      const size_t n = (size_t)g.ibl_w * g.ibl_h;
+      if (hs.ibl_texels.size() + n > (size_t)INT32_MAX) { err = "IBL images too large"; return PR_E_ARG; }
+      for (size_t k = 0; k < n; k++) {
+        float c[3];
+        for (int q = 0; q < 3; q++) c[q] = pm.ibl_rgb8 ? (float)(pm.ibl_rgb8[3 * k + q] / 255.0) : pm.ibl_rgbf[3 * k + q];
+        hs.ibl_texels.push_back(make_float4(c[0], c[1], c[2], 0.0f));
+      }
+      if (is_light(pm)) {
+        err = "an emitting material with an IBL image (a light whose emission the shadow ray's hit decides) is not "
+              "on this path";
+        return PR_E_UNSUPPORTED;
+      }
+    }
     if (pm.type == PR_MAT_SSS_REFRACTION || pm.type == PR_MAT_SSS_DIFFUSE || pm.type == PR_MAT_SSS_WARD) {
       const pr_medium& md = pm.medium;
       if (pm.type != PR_MAT_SSS_REFRACTION || (md.level != -2 && md.level != -1) || !md.use_bssrdf ||
@@ -525,10 +561,25 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
     g.material = pe.material;
     g.normal_inverse = pe.normal_inverse < 0 ? -1 : 1;
     const pr_material& pm = d->materials[pe.material];
+    const bool textured = pm.texture || pm.ibl_rgb8 || pm.ibl_rgbf;
+    if (textured && pe.type != PR_ENT_SPHERE && pe.type != PR_ENT_UVPLANE) {
+      err = "textures and IBL images are read on spheres, hemispheres and uvplanes only";
+      return PR_E_UNSUPPORTED;
+    }
+    if (textured && (hs.mats[pe.material].sss || d->kerr.enabled)) {
+      err = "textures on subsurface materials or under a black hole are not on this path";
+      return PR_E_UNSUPPORTED;
+    }
     if (pe.type == PR_ENT_SPHERE) {
       for (int k = 0; k < 3; k++) g.p[k] = pe.p[k];
       g.radius = pe.radius;
+      g.hemisphere = pe.hemisphere ? 1 : 0;
+      if (g.hemisphere && (is_light(pm) || d->kerr.enabled)) {
+        err = "hemispheres that emit, or under a black hole, are not on this path";
+        return PR_E_UNSUPPORTED;
+      }
       g.area = 12.5663706143591729538505735331180115 * pe.radius * pe.radius;  // PS_FORPI r^2
+      if (g.hemisphere) g.area *= 0.5;
       for (int k = 0; k < 3; k++) {  // Sphere::CreateBoundingBox (sphere.h:58-63)
         g.bb_min[k] = pe.p[k] - pe.radius - 0.01;
         g.bb_max[k] = pe.p[k] + pe.radius + 0.01;

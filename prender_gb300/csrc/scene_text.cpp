@@ -48,6 +48,9 @@ struct pr_scene_file {
   std::vector<std::vector<float>> fnormals;  // empty: the loader's rule at upload
   std::vector<pr_mesh> meshes;
   std::vector<uint8_t> bg_tex, disk_tex;
+  // per material: texture / IBL images (pointers set when the desc is made)
+  std::vector<std::vector<uint8_t>> tex8, ibl8;
+  std::vector<std::vector<float>> iblf;
   pr_scene_desc desc;
   pr_camera cam;
   pr_render_params prm;
@@ -225,6 +228,72 @@ void read_bmp(const std::string& path, int channels, std::vector<uint8_t>& out, 
   }
   if (channels == 4 && bpp == 32 && !any_alpha)
     for (size_t i = 3; i < out.size(); i += 4) out[i] = 255;
+}
+
+// HDRImage::load_unsafe (hdr.h:82-210): a Radiance file with the
+// '#?RADIANCE' line and '-Y H +X W', new-style run-length scanlines (reading
+// stops at the first scanline without the 2 2 marker; rows not read stay
+// zero), each value byte * 2^(e - 128) / 256 (e = 0 included), file row y
+// stored as image row H - 1 - y; out: float RGB in IBL_Color(i, j) order
+void read_hdr(const std::string& path, std::vector<float>& out, int& w, int& h) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) fail("cannot open " + path);
+  std::vector<uint8_t> d((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  size_t p = 0;
+  bool valid = false;
+  auto line = [&]() {
+    std::string l;
+    while (p < d.size() && d[p] != '\n') l += (char)d[p++];
+    if (p < d.size()) p++;
+    return l;
+  };
+  for (;;) {
+    if (p >= d.size()) fail("truncated HDR header: " + path);
+    const std::string l = line();
+    if (l == "#?RADIANCE") valid = true;
+    if (l.empty()) break;
+  }
+  if (!valid) fail("not a Radiance HDR file: " + path);
+  char a[64] = {0}, b[64] = {0};
+  int H = 0, W = 0;
+  const std::string res = line();
+  if (std::sscanf(res.c_str(), "%63s %d %63s %d", a, &H, b, &W) != 4 || std::string(a) != "-Y" ||
+      std::string(b) != "+X" || W <= 0 || H <= 0 || W > (1 << 16) || H > (1 << 16))
+    fail("unsupported HDR orientation or size (only '-Y H +X W'): " + path);
+  w = W;
+  h = H;
+  std::vector<uint8_t> tmp((size_t)W * H * 4, 0);
+  for (int y = 0; y < H; y++) {
+    if (p + 4 > d.size() || d[p] != 2 || d[p + 1] != 2) break;
+    const int lw = (d[p + 2] << 8) + d[p + 3];
+    p += 4;
+    int x = 0, c = 0;
+    for (;;) {
+      if (x >= lw) {
+        c++;
+        x = 0;
+        if (c == 4) break;
+      }
+      if (p >= d.size()) fail("truncated HDR data: " + path);
+      const int info = d[p++];
+      const int n = info <= 128 ? info : info - 128;
+      for (int k = 0; k < n; k++) {
+        if (x >= W) fail("HDR scanline longer than the image: " + path);
+        if (info <= 128 && p >= d.size()) fail("truncated HDR data: " + path);
+        const uint8_t v = info <= 128 ? d[p++] : d[p];
+        tmp[((size_t)y * W + x) * 4 + c] = v;
+        x++;
+      }
+      if (info > 128) p++;
+    }
+  }
+  out.assign((size_t)W * H * 3, 0.0f);
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++) {
+      const uint8_t* t = tmp.data() + ((size_t)y * W + x) * 4;
+      const double sc = std::pow(2.0, (double)t[3] - 128.0) / 256.0;
+      for (int c = 0; c < 3; c++) out[((size_t)(H - 1 - y) * W + x) * 3 + c] = (float)(t[c] * sc);
+    }
 }
 
 struct ObjMesh {
@@ -469,6 +538,8 @@ pr_material default_material() {
   m.medium = default_medium();
   m.ward_alpha[0] = m.ward_alpha[1] = 0.1;
   m.phong_exponent = 1.0;
+  m.ibl_coef = 1.0;  // material.h:84-89
+  m.repeat = 1;
   return m;
 }
 
@@ -685,9 +756,10 @@ class Loader {
       const std::vector<double> v = num_.many(after_key(g), 3);
       e.type = PR_ENT_INF_LIGHT;
       for (int i = 0; i < 3; i++) e.light_dir[i] = v[i];
-    } else if (starts(g, "sphere ")) {
+    } else if (starts(g, "sphere ") || starts(g, "hemisphere ")) {
       const std::vector<double> v = num_.many(after_key(g), 4);
       e.type = PR_ENT_SPHERE;
+      e.hemisphere = starts(g, "hemisphere ") ? 1 : 0;  // scene_env.h:935-939
       for (int i = 0; i < 3; i++) e.p[i] = v[i];
       e.radius = v[3];
     } else if (starts(g, "uvplane ")) {
@@ -721,12 +793,14 @@ class Loader {
     pr_material m = default_material();
     double material_scale = 1.0, scattering = 0.0;
     std::vector<M4> ms;
+    ObjTex tx;
     std::string b;
     while (r_.raw(b) && !b.empty()) {
       if (b[0] == '#') continue;
       const std::vector<std::string> bt = tokens(b);
       if (bt.empty()) continue;
       if (bt.size() == 1 && object_setting(bt[0], m, material_scale, scattering)) continue;
+      if (texture_line(b, bt, m, tx)) continue;
       object_line(b, bt, e, m, ms);
     }
     if (is_sss(m.type) && !(scattering > kEps))
@@ -758,7 +832,58 @@ class Loader {
     }
     e.material = (int)S_.mats.size();
     S_.mats.push_back(m);
+    S_.tex8.push_back(std::move(tx.tex8));
+    S_.ibl8.push_back(std::move(tx.ibl8));
+    S_.iblf.push_back(std::move(tx.iblf));
     S_.ents.push_back(e);
+  }
+
+  // an OBJECT's images (scene_env.h:984-1175): texture, ibl_texture (BMP or
+  // Radiance HDR), ibl_texture_coef, repeat and the four sphere mappings
+  struct ObjTex {
+    std::vector<uint8_t> tex8, ibl8;
+    std::vector<float> iblf;
+  };
+  bool texture_line(const std::string& b, const std::vector<std::string>& bt, pr_material& m, ObjTex& tx) {
+    const std::string& k = bt[0];
+    if (k == "texture" && bt.size() >= 2) {
+      int w = 0, h = 0;
+      read_bmp(resolve(b.substr(8), sdir_), 3, tx.tex8, w, h);
+      m.texture_width = w;
+      m.texture_height = h;
+    } else if (k == "ibl_texture" && bt.size() >= 2) {
+      const std::string file = resolve(b.substr(12), sdir_);
+      std::string ext = file.size() >= 4 ? file.substr(file.size() - 4) : std::string();
+      for (char& ch : ext) ch = (char)std::tolower((unsigned char)ch);
+      int w = 0, h = 0;
+      if (ext == ".bmp") {
+        read_bmp(file, 3, tx.ibl8, w, h);
+        tx.iblf.clear();
+      } else if (ext == ".hdr") {
+        read_hdr(file, tx.iblf, w, h);
+        tx.ibl8.clear();
+      } else {
+        fail("ibl_texture takes a .bmp or .hdr file: " + file);
+      }
+      m.ibl_width = w;
+      m.ibl_height = h;
+    } else if (k == "ibl_texture_coef") {
+      m.ibl_coef = num_.many(after_key(b), 1)[0];
+    } else if (k == "repeat") {
+      scan(b, "repeat %d", m.repeat);
+    } else if (k == "hemisphere_map" || k == "angular_map" || k == "panoramic_map" || k == "equirectangular_map") {
+      int on = 0;
+      scan(after_key(b), "%d", on);
+      const int bit = k == "hemisphere_map" ? PR_MAP_HEMISPHERE
+                      : k == "angular_map"  ? PR_MAP_ANGULAR
+                      : k == "panoramic_map" ? PR_MAP_PANORAMIC
+                                             : PR_MAP_EQUIRECTANGULAR;
+      // the flag is a char set from the value (scene_env.h:1135-1162)
+      m.map_flags = ((char)on != 0) ? (m.map_flags | bit) : (m.map_flags & ~bit);
+    } else {
+      return false;
+    }
+    return true;
   }
 
   // an OBJECT keyword alone on its line, value on the next (scene_env.h:1257-1367)
@@ -901,10 +1026,9 @@ class Loader {
       if (on != 0) refuse(b);
     } else if (k == "media_ignore_front_back") {
       if ((int)num_.many(after_key(b), 1)[0] != 0) refuse(b);
-    } else if (among(k, {"texture", "bump_texture", "ibl_texture", "equirectangular_map", "hemisphere_map",
-                         "angular_map", "panoramic_map"})) {
-      refuse(b);
-    } else if (among(k, {"back", "repeat", "ibl_texture_coef"})) {
+    } else if (among(k, {"texture", "bump_texture", "ibl_texture"})) {
+      refuse(b);  // bump maps (and an image keyword without a file)
+    } else if (among(k, {"back"})) {
       // not read by anything rendered here
     } else {
       S_.warnings += "skipped in OBJECT: " + b + "\n";
@@ -989,6 +1113,12 @@ class Loader {
     d.n_entities = (int32_t)S_.ents.size();
     d.n_meshes = (int32_t)S_.meshes.size();
     d.participating_media = participating_;
+    for (size_t i = 0; i < S_.mats.size(); i++) {
+      pr_material& mm = S_.mats[i];
+      mm.texture = S_.tex8[i].empty() ? nullptr : S_.tex8[i].data();
+      mm.ibl_rgb8 = S_.ibl8[i].empty() ? nullptr : S_.ibl8[i].data();
+      mm.ibl_rgbf = S_.iblf[i].empty() ? nullptr : S_.iblf[i].data();
+    }
     d.materials = S_.mats.data();
     d.entities = S_.ents.data();
     d.meshes = S_.meshes.data();

@@ -235,6 +235,8 @@ __device__ __forceinline__ bool sphere_t64(const GEntity& e, float3 o, float3 d,
 __device__ __forceinline__ bool fast_sphere(const GEntity& e, float3 o, float3 d, float tmax, float& t, float& rest) {
   double tt;
   if (!sphere_t64(e, o, d, tt) || !(tt < (double)tmax)) return false;
+  // a hemisphere keeps the hit only on its y >= y_centre half (sphere.h:98-103)
+  if (e.hemisphere && (double)o.y + tt * (double)d.y - e.p[1] < 0.0) return false;
   t = (float)tt;
   rest = (float)(tt - (double)t);
   return true;

@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(256) wf_reset(unsigned int n_slots) {
 // materials (the fuller shade() with the dipole and the single-scattering
 // walk, and the frames above); every camera sample then ends through its
 // sample slot, since frames may take radiance from any of its branches.
-template <bool SSS, bool POINT>
+template <bool SSS, bool EXT>
 __device__ __forceinline__ void wf_shade_impl() {
   const DevScene& S = c_scene;
   const RenderCfg& cfg = c_cfg;
@@ -314,7 +314,7 @@ __device__ __forceinline__ void wf_shade_impl() {
             nsh = 0;
           }
         } else {
-          r = shade<false, true, POINT>(S, cfg, ps, h.ent >= 0, h, sample_id, sh, nsh, child, B.err);
+          r = shade<false, true, EXT>(S, cfg, ps, h.ent >= 0, h, sample_id, sh, nsh, child, B.err);
         }
         for (int k = 0; k < 3; k++) {
           if (k < nsh) {
@@ -413,8 +413,8 @@ __device__ __forceinline__ void wf_shade_impl() {
 // over 4 / 5 / 6 / 7 / 8 / 10 blocks, mesh Cornell box 1024x768x64 spp,
 // wf_shade 108 / 99 / 94 / 96 / 102 / 110 ms per frame
 __global__ void __launch_bounds__(128, 6) wf_shade() { wf_shade_impl<false, false>(); }
-// scenes with parallel, spot or infinity lights
-__global__ void __launch_bounds__(128, 4) wf_shade_point() { wf_shade_impl<false, true>(); }
+// scenes with parallel, spot or infinity lights, textures or IBL images
+__global__ void __launch_bounds__(128, 4) wf_shade_ext() { wf_shade_impl<false, true>(); }
 // scenes with subsurface materials (any light kind)
 __global__ void __launch_bounds__(128, 3) wf_shade_sss() { wf_shade_impl<true, true>(); }
 
@@ -685,7 +685,7 @@ cudaError_t wf_set_constants(const DevScene& S, const RenderCfg& cfg, const WfBu
 
 static void launch_shade(const WfLaunch& L, cudaStream_t s) {
   if (L.sss) wf_shade_sss<<<L.shade_blocks, 128, 0, s>>>();
-  else if (L.point) wf_shade_point<<<L.shade_blocks, 128, 0, s>>>();
+  else if (L.ext) wf_shade_ext<<<L.shade_blocks, 128, 0, s>>>();
   else wf_shade<<<L.shade_blocks, 128, 0, s>>>();
 }
 

@@ -72,7 +72,7 @@ struct WfLaunch {
   unsigned int shade_blocks;
   unsigned int trace_blocks;
   int sss;    // the scene has subsurface materials: the fuller shading kernel with frames
-  int point;  // the scene has parallel, spot or infinity lights
+  int ext;    // the scene has parallel, spot or infinity lights, textures or IBL images
 };
 
 cudaError_t wf_set_constants(const DevScene& S, const RenderCfg& cfg, const WfBufs& B, cudaStream_t s);

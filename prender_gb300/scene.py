@@ -60,6 +60,15 @@ class Material:
     disk_map: int = 0
     ward_alpha: Sequence[float] = (0.1, 0.1)
     phong_exponent: float = 1.0
+    # textures (sphere.h:104-240, plane.h:241-273): texture (H, W, 3) uint8
+    # rows as BitMap::cell(y, x) reads them; ibl (H, W, 3) uint8 (a bitmap)
+    # or float32 (a Radiance HDR image, IBL_Color(i, j) order); map_flags
+    # PR_MAP_*; compared by identity, not value
+    texture: Optional[np.ndarray] = field(default=None, compare=False, repr=False)
+    ibl: Optional[np.ndarray] = field(default=None, compare=False, repr=False)
+    ibl_coef: float = 1.0
+    repeat: int = 1
+    map_flags: int = 0
 
     @staticmethod
     def diffuse(color, emission=(0.0, 0.0, 0.0)) -> "Material":
@@ -111,7 +120,9 @@ class Material:
         return (self.type == A.PR_MAT_DIFFUSE and math.sqrt(sum(c * c for c in self.color)) < 0.001
                 and math.sqrt(sum(e * e for e in self.emission)) > 0.001)
 
-    def to_c(self) -> A.pr_material:
+    def to_c(self, keep=None) -> A.pr_material:
+        """keep: a list that takes the texture arrays the struct points to
+        (without it the struct carries no textures)"""
         m = A.pr_material()
         m.type = int(self.type)
         m.color[:] = [float(x) for x in self.color]
@@ -124,6 +135,28 @@ class Material:
         m.disk_map = int(self.disk_map)
         m.ward_alpha[:] = [float(x) for x in self.ward_alpha]
         m.phong_exponent = float(self.phong_exponent)
+        m.ibl_coef = float(self.ibl_coef)
+        m.repeat = int(self.repeat)
+        m.map_flags = int(self.map_flags)
+        if keep is not None:
+            if self.texture is not None:
+                t = np.ascontiguousarray(self.texture, dtype=np.uint8)
+                if t.ndim != 3 or t.shape[2] != 3:
+                    raise ValueError("texture must be (H, W, 3) uint8")
+                keep.append(t)
+                m.texture = t.ctypes.data_as(C.POINTER(C.c_uint8))
+                m.texture_height, m.texture_width = t.shape[0], t.shape[1]
+            if self.ibl is not None:
+                if self.ibl.dtype == np.uint8:
+                    t = np.ascontiguousarray(self.ibl)
+                    m.ibl_rgb8 = t.ctypes.data_as(C.POINTER(C.c_uint8))
+                else:
+                    t = np.ascontiguousarray(self.ibl, dtype=np.float32)
+                    m.ibl_rgbf = t.ctypes.data_as(C.POINTER(C.c_float))
+                if t.ndim != 3 or t.shape[2] != 3:
+                    raise ValueError("ibl image must be (H, W, 3)")
+                keep.append(t)
+                m.ibl_height, m.ibl_width = t.shape[0], t.shape[1]
         return m
 
 
@@ -153,6 +186,7 @@ class Entity:
     spot_falloff: float = 0.0
     spot_attenuation: Sequence[float] = (0.0, 0.0, 1.0)
     light_dir_text: Optional[Sequence[float]] = field(default=None, compare=False, repr=False)
+    hemisphere: int = 0
 
     def to_c(self) -> A.pr_entity:
         e = A.pr_entity()
@@ -166,6 +200,7 @@ class Entity:
         e.blackhole_disk = int(self.blackhole_disk)
         e.parallel_light = int(self.parallel_light)
         e.spot_light = int(self.spot_light)
+        e.hemisphere = int(self.hemisphere)
         e.light_dir[:] = [float(x) for x in self.light_dir]
         e.spot_angle[:] = [float(x) for x in self.spot_angle]
         e.spot_falloff = float(self.spot_falloff)
@@ -265,7 +300,8 @@ class SceneDesc:
     """Holds a pr_scene_desc and every buffer it points to."""
 
     def __init__(self, scene: "Scene"):
-        self._mats = (A.pr_material * max(1, len(scene.materials)))(*[m.to_c() for m in scene.materials])
+        self._tex = []
+        self._mats = (A.pr_material * max(1, len(scene.materials)))(*[m.to_c(self._tex) for m in scene.materials])
         self._ents = (A.pr_entity * max(1, len(scene.entities)))(*[e.to_c() for e in scene.entities])
         self._mesh_arrays = []
         meshes = []
@@ -353,6 +389,13 @@ class Scene:
         self.entities.append(Entity(A.PR_ENT_SPHERE, self._mat(material), normal_inverse, p=tuple(center),
                                     radius=float(radius)))
         return len(self.entities) - 1
+
+    def add_hemisphere(self, center, radius, material: Material, normal_inverse: int = 1) -> int:
+        """'hemisphere x y z r': the half of the sphere with y >= y_centre
+        (sphere.h:98-103), e.g. a sky dome with an IBL image"""
+        i = self.add_sphere(center, radius, material, normal_inverse)
+        self.entities[i].hemisphere = 1
+        return i
 
     def add_uvplane(self, org, U, V, material: Material, normal_inverse: int = 1) -> int:
         self.entities.append(Entity(A.PR_ENT_UVPLANE, self._mat(material), normal_inverse, p=tuple(org),
@@ -504,7 +547,7 @@ class Scene:
             m = self.materials[e.material]
             out.append("OBJECT")
             if e.type == A.PR_ENT_SPHERE:
-                out.append(f"sphere {f3(e.p)} {_fmt(e.radius)}")
+                out.append(f"{'hemisphere' if e.hemisphere else 'sphere'} {f3(e.p)} {_fmt(e.radius)}")
             elif e.type == A.PR_ENT_UVPLANE:
                 out += [f"uvplane {f3(e.p)}", f"U {f3(e.u)}", f"V {f3(e.v)}"]
             elif e.type == A.PR_ENT_CIRCLE:
@@ -546,6 +589,26 @@ class Scene:
                     out.append(f"phong_brdf 1 1 {_fmt(m.phong_exponent)}")
             if m.disk_map:
                 out.append(f"disk_map {int(m.disk_map)}")
+            if m.texture is not None:
+                tp = os.path.join(directory, f"tex{ei}.bmp")
+                _write_bmp24(tp, np.asarray(m.texture, dtype=np.uint8))
+                out.append(f"texture {tp}")
+            if m.ibl is not None:
+                if m.ibl.dtype == np.uint8:
+                    ip = os.path.join(directory, f"ibl{ei}.bmp")
+                    _write_bmp24(ip, np.asarray(m.ibl))
+                else:
+                    ip = os.path.join(directory, f"ibl{ei}.hdr")
+                    write_hdr(ip, hdr_rgbe(np.asarray(m.ibl, dtype=np.float32))[::-1])
+                out.append(f"ibl_texture {ip}")
+                if float(m.ibl_coef) != 1.0:
+                    out.append(f"ibl_texture_coef {_fmt(m.ibl_coef)}")
+            if int(m.repeat) != 1:
+                out.append(f"repeat {int(m.repeat)}")
+            for bit, key in ((A.PR_MAP_HEMISPHERE, "hemisphere_map"), (A.PR_MAP_ANGULAR, "angular_map"),
+                             (A.PR_MAP_PANORAMIC, "panoramic_map"), (A.PR_MAP_EQUIRECTANGULAR, "equirectangular_map")):
+                if int(m.map_flags) & bit:
+                    out.append(f"{key} 1")
             ldir = e.light_dir_text if e.light_dir_text is not None else e.light_dir
             if e.parallel_light:
                 out.append("parallel_light 1")
@@ -597,6 +660,30 @@ def _rgba(tex) -> np.ndarray:
     if t.shape[2] == 3:
         t = np.concatenate([t, np.full(t.shape[:2] + (1,), 255, np.uint8)], axis=2)
     return np.ascontiguousarray(t)
+
+
+def hdr_rgbe(img: np.ndarray) -> np.ndarray:
+    """RGBE bytes (H, W, 4) that HDRImage::load_unsafe (hdr.h:82-210) reads
+    back as exactly these values (byte * 2^(e - 136) per channel); raises
+    if a value has no such form (more than 8 significant bits against the
+    texel's largest channel)"""
+    f = np.asarray(img, dtype=np.float64)
+    mx = f.max(axis=2)
+    m, e = np.frexp(mx)
+    ex = np.where(mx > 0, e + 128, 0).astype(np.int64)
+    if (ex < 0).any() or (ex > 255).any():
+        raise ValueError("value out of the RGBE exponent range")
+    b = np.where(mx[..., None] > 0, f * np.ldexp(1.0, (136 - ex))[..., None], 0.0)
+    if (b != np.floor(b)).any() or (b > 255).any():
+        raise ValueError("an HDR value that RGBE cannot hold exactly")
+    return np.concatenate([b.astype(np.uint8), ex.astype(np.uint8)[..., None]], axis=2)
+
+
+def rgbe_values(rgbe: np.ndarray) -> np.ndarray:
+    """the values HDRImage::load_unsafe gives RGBE bytes: byte *
+    pow(2, e - 128) / 256 (hdr.h:203-208; e = 0 included), as float32"""
+    q = np.asarray(rgbe, dtype=np.uint8)
+    return (q[..., :3].astype(np.float64) * np.ldexp(1.0, q[..., 3:4].astype(np.int64) - 136)).astype(np.float32)
 
 
 def write_hdr(path: str, rgbe: np.ndarray) -> None:

@@ -49,6 +49,13 @@ def _v(a, n=3):
     return tuple(float(a[i]) for i in range(n))
 
 
+def _image(ptr, h, w, dtype):
+    """a copy of an (h, w, 3) image the reader holds, or None"""
+    if not ptr or h <= 0 or w <= 0:
+        return None
+    return np.ctypeslib.as_array(ptr, shape=(h * w * 3,)).reshape(h, w, 3).astype(dtype, copy=True)
+
+
 def _medium(m: A.pr_medium) -> Medium:
     return Medium(sigma_s_rgb=_v(m.sigma_s_rgb), sigma_a_rgb=_v(m.sigma_a_rgb), phase_g=_v(m.phase_g),
                   eta=float(m.eta), scale=float(m.scale), r_max=float(m.r_max), level=int(m.level),
@@ -82,7 +89,11 @@ def load(path: str) -> Scene:
                 type=int(m.type), color=_v(m.color), emission=_v(m.emission), specular=_v(m.specular),
                 roughness=float(m.roughness), refractive_index=float(m.refractive_index), medium=_medium(m.medium),
                 r_refractive_index=float(m.r_refractive_index), disk_map=int(m.disk_map),
-                ward_alpha=_v(m.ward_alpha, 2), phong_exponent=float(m.phong_exponent)))
+                ward_alpha=_v(m.ward_alpha, 2), phong_exponent=float(m.phong_exponent),
+                texture=_image(m.texture, m.texture_height, m.texture_width, np.uint8),
+                ibl=(_image(m.ibl_rgb8, m.ibl_height, m.ibl_width, np.uint8) if m.ibl_rgb8
+                     else _image(m.ibl_rgbf, m.ibl_height, m.ibl_width, np.float32)),
+                ibl_coef=float(m.ibl_coef), repeat=int(m.repeat), map_flags=int(m.map_flags)))
         for i in range(d.n_entities):
             e = d.entities[i]
             s.entities.append(Entity(
@@ -91,7 +102,7 @@ def load(path: str) -> Scene:
                 radius_inner=float(e.radius_inner), blackhole_disk=int(e.blackhole_disk),
                 parallel_light=int(e.parallel_light), spot_light=int(e.spot_light), light_dir=_v(e.light_dir),
                 spot_angle=_v(e.spot_angle, 2), spot_falloff=float(e.spot_falloff),
-                spot_attenuation=_v(e.spot_attenuation)))
+                spot_attenuation=_v(e.spot_attenuation), hemisphere=int(e.hemisphere)))
         for i in range(d.n_meshes):
             pm = d.meshes[i]
             v = np.ctypeslib.as_array(pm.vertices, shape=(pm.n_vertices * 3,)).reshape(-1, 3).copy()

@@ -19,7 +19,9 @@ sss_l1_oracle.npz, glossy_oracle.npz, media_oracle.npz, mesh7_oracle.npz,
 batch_oracle.npz and lights_oracle.npz the same way; --media-only,
 --batch-only and --lights-only write the reference's own one-thread media,
 batch-variant and light-kind renders, --hdr-only its Render::OutputHdr file
-of a seeded image.
+of a seeded image; --textures-only and --textures-oracle do the same for the
+texture and image-based-lighting scenes (textures_render.npz,
+textures_oracle.npz).
 --scene-files-only writes the meshes and textures that the scene files in
 scene_files/ name, and scene_files.npz from the reference's renders of them.
 """
@@ -390,6 +392,44 @@ def lights_oracle_golden(nb=16):
     np.savez_compressed(os.path.join(HERE, "lights_oracle.npz"), **out)
 
 
+def textures_golden(d):
+    """texture and IBL scenes rendered by the reference, one thread (bit-exact)"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import texture_cases
+    out = {}
+    for name, sc in texture_cases.one_thread_cases().items():
+        dd = os.path.join(d, "t_" + name)
+        os.makedirs(dd)
+        img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+        out[name] = img
+        print("textures", name, info, float(img.mean()))
+    np.savez_compressed(os.path.join(HERE, "textures_render.npz"), **out)
+
+
+def textures_oracle_golden(nb=16):
+    """16 independent 256-spp renders of each texture scene by the oracle
+    (pinned bit-exact to the reference by textures_render.npz): per-pixel
+    mean and spread"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import texture_cases
+    from oracle import oracle as O
+    out = {}
+    for name in texture_cases.CASES:
+        sc = texture_cases.highspp_case(name)
+        o = O.OracleScene(sc)
+        imgs = []
+        for k in range(nb):
+            sc.settings.seed = 100 + k
+            img, _, _ = o.render(threads=os.cpu_count(), settings=sc.settings)
+            imgs.append(img)
+        b = np.stack(imgs)
+        out[f"{name}_mean"] = b.mean(0).astype(np.float32)
+        out[f"{name}_sd"] = b.std(0, ddof=1).astype(np.float32)
+        print("textures oracle", name, float(b.mean()))
+    out["batches"] = np.int32(nb)
+    np.savez_compressed(os.path.join(HERE, "textures_oracle.npz"), **out)
+
+
 def mesh7_oracle_golden(nb=16):
     """The benchmarked scene itself (327,680-triangle displaced icosphere,
     diffuse and glass) at 128 x 96, 16 independent 256-spp renders by the
@@ -513,7 +553,7 @@ def _image_size(path):
 KNOWN_FLAGS = {"--kerr-only", "--disk-only", "--sss-only", "--sss-l1-only", "--glossy-only", "--sss-oracle",
                "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle", "--scene-files-only", "--media-only",
                "--media-oracle", "--mesh7-oracle", "--batch-only", "--batch-oracle", "--hdr-only",
-               "--lights-only", "--lights-oracle"}
+               "--lights-only", "--lights-oracle", "--textures-only", "--textures-oracle"}
 
 
 def main():
@@ -525,6 +565,9 @@ def main():
         return
     if "--lights-oracle" in sys.argv:
         lights_oracle_golden()
+        return
+    if "--textures-oracle" in sys.argv:
+        textures_oracle_golden()
         return
     if "--mesh7-oracle" in sys.argv:
         mesh7_oracle_golden()
@@ -559,6 +602,10 @@ def main():
     if "--media-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             media_golden(d)
+        return
+    if "--textures-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            textures_golden(d)
         return
     if "--lights-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:

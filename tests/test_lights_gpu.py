@@ -58,7 +58,7 @@ def test_light_kinds_match_oracle_statistically(ctx, golden, name, mode):
 def test_light_kinds_wavefront_equals_megakernel(ctx, name):
     """Same shading code and streams in both forms; the two kernels that
     run it here (the megakernel's fuller instantiation, the wavefront's
-    point-light one) are compiled separately, so their float rounding can
+    extended one) are compiled separately, so their float rounding can
     differ in the last bit, now and then flipping a Russian-roulette or
     branch decision, and these scenes look straight at small bright
     emitters (a spot sphere of emission 120 behind the per-sample clamp),

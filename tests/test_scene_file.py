@@ -55,7 +55,9 @@ def _written_cases():
     }
     out.update({"glossy_" + k: v for k, v in glossy_cases.one_thread_cases().items()})
     import lights_cases
+    import texture_cases
     out.update({"lights_" + k: v for k, v in lights_cases.one_thread_cases().items()})
+    out.update({"tex_" + k: v for k, v in texture_cases.one_thread_cases().items()})
     return out
 
 
@@ -99,6 +101,55 @@ def test_light_kind_files_render_like_the_reference(tmp_path, golden, name):
     s = scene_file.load(sc.write_reference(str(tmp_path)))
     img, _, _ = O.OracleScene(s).render(threads=1)
     assert np.array_equal(img, golden["lights_render"][name])
+
+
+@pytest.mark.parametrize("name", ["tex_maps", "ibl_dome", "ibl_nonee", "ibl_panoramic"])
+def test_texture_files_render_like_the_reference(tmp_path, golden, name):
+    # the files the reference rendered for textures_render.npz (BMP textures,
+    # BMP and Radiance HDR IBL images, the mappings, repeat, hemispheres),
+    # read by this library's reader and rendered by the oracle
+    import texture_cases
+    sc = texture_cases.one_thread_cases()[name]
+    s = scene_file.load(sc.write_reference(str(tmp_path)))
+    for a, b in zip(sc.materials, s.materials):
+        for f in ("texture", "ibl"):
+            x, y = getattr(a, f), getattr(b, f)
+            assert (x is None) == (y is None)
+            if x is not None:
+                assert np.asarray(x).dtype == y.dtype and np.array_equal(np.asarray(x), y)
+    img, _, _ = O.OracleScene(s).render(threads=1)
+    assert np.array_equal(img, golden["textures_render"][name])
+
+
+def test_hdr_reader_rows_and_values(tmp_path):
+    # HDRImage::load_unsafe: byte * 2^(e - 128) / 256 per channel, file row y
+    # is image row H - 1 - y; IBL_Color(i, j) reads image row i
+    from prender_gb300.scene import hdr_rgbe, rgbe_values, write_hdr
+    rng = np.random.default_rng(5)
+    q = np.concatenate([rng.integers(0, 256, (9, 200, 3)), rng.integers(100, 160, (9, 200, 1))], 2).astype(np.uint8)
+    q[0, 0] = (0, 0, 0, 0)
+    vals = rgbe_values(q)
+    write_hdr(str(tmp_path / "i.hdr"), hdr_rgbe(vals)[::-1])
+    body = f"IMAGE\n8 6\n\nOBJECT\nsphere 0 0 0 1\ncolor 0 0 0\nreflection diffuse\nibl_texture {tmp_path / 'i.hdr'}\n\n"
+    s = scene_file.load(_scene(tmp_path, body))
+    assert s.materials[0].ibl.dtype == np.float32 and np.array_equal(s.materials[0].ibl, vals)
+
+
+@pytest.mark.parametrize("body,code,msg", [
+    ("disk 0 10 0 1\nnormal 0 -1 0\ntexture TEX\n", A.PR_E_UNSUPPORTED, "spheres, hemispheres and uvplanes"),
+    ("sphere 0 10 0 1\nemission 1 1 1\nibl_texture TEX\n", A.PR_E_UNSUPPORTED, "IBL image"),
+    ("hemisphere 0 10 0 1\nemission 1 1 1\n", A.PR_E_UNSUPPORTED, "hemispheres that emit"),
+])
+def test_textures_refused_where_not_rendered(tmp_path, body, code, msg):
+    from prender_gb300 import gpu
+    from prender_gb300.scene import _write_bmp24
+    _write_bmp24(str(tmp_path / "t.bmp"), np.full((4, 4, 3), 200, np.uint8))
+    body = body.replace("TEX", str(tmp_path / "t.bmp"))
+    text = "IMAGE\n8 6\n\nOBJECT\n" + body + "color 0 0 0\nreflection diffuse\n\n"
+    s = scene_file.load(_scene(tmp_path, text))
+    with pytest.raises(gpu.PrenderError) as e:
+        gpu.check_scene(s)
+    assert str(code) in str(e.value) and msg in str(e.value)
 
 
 @pytest.mark.parametrize("body,code,msg", [
@@ -203,13 +254,11 @@ def test_bad_values_are_errors_with_the_line(tmp_path, body, msg):
 
 
 @pytest.mark.parametrize("body", [
-    "OBJECT\nsphere 0 0 0 1\ntexture wood.bmp\n\n",
     "OBJECT\nsphere 0 0 0 1\nbump_texture b.bmp\n\n",
     "OBJECT\nsphere 0 0 0 1\nsmooth 1\n\n",
     "OBJECT\nsphere 0 0 0 1\nMATERIAL_SYMBOL\nKetchup\n\n",
     "OBJECT\nsphere 0 0 0 1\nreflection reflection1\n1 2 3 4 5 6\n\n",
     "OBJECT\nplane 0 0 0\nnormal 0 1 0\n\n",
-    "OBJECT\nhemisphere 0 0 0 1\n\n",
     "OBJECT\nuvplane 0 0 0\nU 1 0 0\nV 0 1 0\nrotation 0 10 0\n\n",
     "OBJECT\ndisk 0 0 0 1\nnormal 0 1 0\ntranslate 1 0 0\n\n",
     "OBJECT\nsphere 0 0 0 1\nreflection reflection\nreflection Subsurface_Scattering\n\n",
