@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define PR_ABI_VERSION 3
+#define PR_ABI_VERSION 4
 
 /* ---- status codes --------------------------------------------------- */
 enum {
@@ -120,8 +120,13 @@ typedef struct pr_material {
   const float* ibl_rgbf;
   int32_t ibl_width, ibl_height;
   double ibl_coef;         /* ibl_texture_coef (default 1)                   */
-  int32_t repeat;          /* 'repeat' (default 1; 0 is taken as 1)          */
+  int32_t repeat;          /* 'repeat' (default 1)                           */
   int32_t map_flags;
+  /* 'bump_texture file.bmp' (sphere.h:320-492, plane.h:274-360): RGB8 rows
+   * as BitMap::cell(y, x) reads them, square; the luminance gradient tilts
+   * a normal that scales the hit's scattered and next-event weights */
+  const uint8_t* bump;
+  int32_t bump_width, bump_height;
 } pr_material;
 
 /* texture mappings of spheres (material.h:188-192) */

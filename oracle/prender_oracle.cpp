@@ -120,6 +120,8 @@ struct Material {  // material.h:54-240
   double ibl_coef = 1.0;
   int repeat = 1;
   int map_flags = 0;
+  std::shared_ptr<const std::vector<unsigned char>> bump;  // bump_texture (cell(i, j) RGB), square
+  int bump_w = 0, bump_h = 0;
   // Material::isLight (material.h): diffuse, dark, emissive
   bool isLight() const {
     return type == PR_MAT_DIFFUSE && length(color) < 0.001 && length(emission) > 0.001;
@@ -139,6 +141,8 @@ struct Hit {  // IntersectionPos (intersection.h:11-30) + object_id
   V3 ov_color, ov_emission;
   bool ov_spec = false;  // a texture also rewrote the specular colour
   V3 ov_specular;
+  bool bump = false;     // IntersectionPos::bump / bump_new_normal
+  V3 bump_n;
 };
 
 struct Mesh {
@@ -286,6 +290,32 @@ inline V3 ibl_rgb(const Material& m, int i, int j) {
   return V3(t[0], t[1], t[2]);
 }
 
+// the bump normal from the central luminance differences around texel
+// (i, j) of a square bump map (sphere.h:411-492, plane.h:290-360; the
+// reference wraps the row above the first to W - 1, which a square map keeps
+// in range): n + (n x tdir) gx - (n x sdir) gy with n the entity's own
+// normal (before its inversion) and g the differences times 0.5 * scale
+void bump_normal(const Material& m, int i, int j, V3 n, V3 sdir, V3 tdir, double scale, Hit& h) {
+  int u0 = j - 1, u1 = j + 1, v0 = i - 1, v1 = i + 1;
+  if (u0 < 0) u0 = m.bump_w - 1;
+  if (v0 < 0) v0 = m.bump_w - 1;
+  if (u1 < 0) u1 = m.bump_h - 1;
+  if (v1 < 0) v1 = m.bump_h - 1;
+  if (u0 >= m.bump_w) u0 = 0;
+  if (u1 >= m.bump_w) u1 = 0;
+  if (v0 >= m.bump_h) v0 = 0;
+  if (v1 >= m.bump_h) v1 = 0;
+  auto px = [&](int a, int b) {
+    const unsigned char* t = &(*m.bump)[3 * ((size_t)a * m.bump_w + b)];
+    return V3((double)t[0], (double)t[1], (double)t[2]);
+  };
+  const V3 Y(0.299, 0.587, 0.114);
+  const double gx = scale * dot((px(i, u1) - px(i, u0)), Y) * 0.5;
+  const double gy = scale * dot((px(v1, j) - px(v0, j)), Y) * 0.5;
+  h.bump_n = n + cross(n, tdir) * gx - cross(n, sdir) * gy;
+  h.bump = true;
+}
+
 // the sphere's (u, v) of one mapping (sphere.h:117-180, :245-300): the
 // spherical angles, then equirectangular, angular and panoramic, each
 // replacing the last where set; swap_uv: the IBL block's (theta, phi) order
@@ -358,7 +388,7 @@ bool sphere_hit(const Scene& s, const Entity& e, V3 org, V3 dir, Hit& h) {
   const V3 p = h.position - e.position;
   if (e.hemisphere && p.y < 0.0) return false;
   const Material& m = s.mats[e.material];
-  if (!m.tex && !m.ibl) return true;
+  if (!m.tex && !m.ibl && !m.bump) return true;
   const double pp[3] = {p.x, p.y, p.z};
   int X = 0, Y = 1, Z = 2;
   if (m.map_flags & PR_MAP_HEMISPHERE) {
@@ -408,6 +438,21 @@ bool sphere_hit(const Scene& s, const Entity& e, V3 org, V3 dir, Hit& h) {
     emission = m.ibl_coef * color;
     rewrote = true;
   }
+  if (m.bump && std::fabs(p.z - e.radius) > EPS16) {  // the bump block tests the unmapped p.z
+    double u, v;
+    sphere_uv(m, vv, true, false, u, v);
+    if (e.hemisphere) u *= 2.0;
+    int j = trunc_int((m.bump_w - 1) * wrap01(u * (double)m.repeat));
+    int i = trunc_int((m.bump_h - 1) * wrap01(v * (double)m.repeat));
+    const double th = std::acos(std::max(-1.0, std::min(1.0, vv.z)));
+    double phi = std::atan2(vv.y, vv.x);
+    if (phi < 0.0) phi += TWOPI;
+    if (phi >= TWOPI) phi = 0.0;
+    const V3 sdir(std::cos(th) * std::cos(phi), std::cos(th) * std::sin(phi), -std::sin(th));
+    const V3 tdir(-std::sin(th) * std::sin(phi), std::sin(th) * std::cos(phi), 0.0);
+    const V3 n = e.normal_inverse < 0 ? h.normal * -1.0 : h.normal;
+    bump_normal(m, i, j, n, sdir, tdir, 0.1, h);
+  }
   if (rewrote) {
     h.ov = true;
     h.ov_color = color;
@@ -434,8 +479,11 @@ bool uvplane_hit(const Scene& s, const Entity& e, V3 org, V3 dir, Hit& h) {
   if (v < 0 || v > e.v_length) return false;
   // the texture and IBL parts (plane.h:241-273)
   const Material& m = s.mats[e.material];
-  if (!m.tex && !m.ibl) return true;
+  if (!m.tex && !m.ibl && !m.bump) return true;
   const double uu = wrap01(u * (double)m.repeat), vw = wrap01(v * (double)m.repeat);
+  if (m.bump)
+    bump_normal(m, trunc_int((m.bump_h - 1) * vw), trunc_int((m.bump_w - 1) * uu), e.normal, e.u_axis, e.v_axis, 1.0, h);
+  if (!m.tex && !m.ibl) return true;
   V3 color = m.color, emission = m.emission, specular = m.specular;
   if (m.tex) {
     texel_rgb(m, trunc_int((m.tex_h - 1) * vw), trunc_int((m.tex_w - 1) * uu), color);
@@ -826,6 +874,11 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
       for (size_t k = 0; k < n; k++) (*v)[k] = pm.ibl_rgb8 ? (double)pm.ibl_rgb8[k] / 255.0 : (double)pm.ibl_rgbf[k];
       m.ibl = v;
     }
+    if (pm.bump && pm.bump_width > 0 && pm.bump_height > 0) {
+      m.bump_w = pm.bump_width;
+      m.bump_h = pm.bump_height;
+      m.bump = std::make_shared<const std::vector<unsigned char>>(pm.bump, pm.bump + 3 * (size_t)m.bump_w * m.bump_h);
+    }
     m.ibl_coef = pm.ibl_coef;
     m.repeat = pm.repeat;
     m.map_flags = pm.map_flags;
@@ -1206,6 +1259,8 @@ V3 eval_direct(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal, V
       }
     }
   }
+  // a bump map scales the term by the tilted normal's cosine (directLight_radiance.h:303-310)
+  if (v0.bump) rad = (std::max(0.0, dot(light_dir, v0.bump_n)) / dot(light_dir, v0.normal)) * rad;
   return rad;
 }
 
@@ -1310,6 +1365,7 @@ V3 brdf_diffuse(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, d
   const V3 dir = normalize((u * std::cos(r1) * r2s + v * std::sin(r1) * r2s + w * std::sqrt(1.0 - r2)));
   V3 incoming = radiance(c, hp.position, dir, depth + 1);
   V3 weight = mat.color / p_rr / (1.0 - p_scat);
+  if (hp.bump) weight = weight * (std::max(0.1, dot(dir, hp.bump_n)) / dot(dir, hp.normal));  // brdf.h:552-557
   V3 direct;
   if (c.nee && !s.lights.empty()) {
     for (int i = 0; i < 3; i++) {  // SHADOW_RAY_SAMPLING (def.h:10)
@@ -1380,7 +1436,8 @@ V3 brdf_glossy(Ctx& c, V3 raydir, const Hit& hp, V3 on, double p_rr, double p_sc
     ww = dot(halfv, in) * std::pow(dot(halfv, on), 3) * std::sqrt(dot(dir, on) / dot(in, on));
   }
   V3 incoming = radiance(c, hp.position, dir, depth + 1);
-  const V3 weight = mat.specular * ww / p_rr / (1.0 - p_scat);
+  V3 weight = mat.specular * ww / p_rr / (1.0 - p_scat);
+  if (hp.bump) weight = weight * (std::max(0.1, dot(dir, hp.bump_n)) / dot(dir, hp.normal));  // brdf.h:102-108, :310-316
   V3 direct;
   if (c.nee && !s.lights.empty()) {
     for (int i = 0; i < 3; i++) {
@@ -1418,6 +1475,7 @@ V3 brdf_specular(Ctx& c, V3 raydir, const Hit& hp, double p_rr, double p_scat, i
   V3 incoming = radiance(c, hp.position, dir, depth + 1);
   V3 weight = mat.color / p_rr / (1.0 - p_scat);
   if (c.nee) incoming = incoming + direct_perfect(c, hp.position, dir, depth);
+  if (hp.bump) weight = weight * (std::max(0.1, dot(dir, hp.bump_n)) / dot(dir, hp.normal));  // brdf.h:740-745
   if (c.media && ins) {
     emission = trr * emission;
     incoming = trr * incoming;

@@ -83,6 +83,9 @@ class pr_material(C.Structure):
         ("ibl_coef", C.c_double),
         ("repeat", C.c_int32),
         ("map_flags", C.c_int32),
+        ("bump", C.POINTER(C.c_uint8)),
+        ("bump_width", C.c_int32),
+        ("bump_height", C.c_int32),
     ]
 
 

@@ -202,6 +202,7 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   // moves the wavefront pool, whose placement wf_shade is sensitive to)
   if (!h.texels.empty()) PR_CUDA(c, upload(o.texels, h.texels, c->stream));
   if (!h.ibl_texels.empty()) PR_CUDA(c, upload(o.ibl_texels, h.ibl_texels, c->stream));
+  if (!h.bump_texels.empty()) PR_CUDA(c, upload(o.bump_texels, h.bump_texels, c->stream));
   PR_CUDA(c, upload(o.kerr_tex, h.kerr_texture, c->stream));
   PR_CUDA(c, upload(o.kerr_disk_tex, h.kerr_disk_texture, c->stream));
   PR_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -219,6 +220,7 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   S.fnorm = (const float*)o.fnorm.p;
   S.texels = (const float4*)o.texels.p;
   S.ibl_texels = (const float4*)o.ibl_texels.p;
+  S.bump_texels = (const float*)o.bump_texels.p;
   S.n_ents = (int)h.ents.size();
   S.n_lights = (int)h.lights.size();
   S.n_point_lights = 0;
@@ -238,7 +240,7 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   for (const GMaterial& gm : h.mats) {
     S.has_sss |= gm.sss;
     S.has_glossy |= (gm.type == PR_MAT_WARD || gm.type == PR_MAT_PHONG) ? 1 : 0;
-    S.has_tex |= (gm.tex_off >= 0 || gm.ibl_off >= 0) ? 1 : 0;
+    S.has_tex |= (gm.tex_off >= 0 || gm.ibl_off >= 0 || gm.bump_off >= 0) ? 1 : 0;
   }
   for (int k = 0; k < 3; k++) {
     S.bg[k] = (float)h.background[k];

@@ -35,11 +35,12 @@ struct DevBuf {
 // one uploaded scene: host build, device copies, device view
 struct SceneObjData {
   HostScene host;
-  DevBuf ents, mats, nodes, tris, rnodes, rtris, fnorm, kerr_tex, kerr_disk_tex, texels, ibl_texels;
+  DevBuf ents, mats, nodes, tris, rnodes, rtris, fnorm, kerr_tex, kerr_disk_tex, texels, ibl_texels, bump_texels;
   DevScene dev{};
   GKerr kerr{};
   void release() {
-    for (DevBuf* b : {&ents, &mats, &nodes, &tris, &rnodes, &rtris, &fnorm, &kerr_tex, &kerr_disk_tex, &texels, &ibl_texels})
+    for (DevBuf* b : {&ents, &mats, &nodes, &tris, &rnodes, &rtris, &fnorm, &kerr_tex, &kerr_disk_tex, &texels, &ibl_texels,
+                      &bump_texels})
       b->release();
   }
 };

@@ -503,16 +503,16 @@ __device__ inline void sss_exit(const DevScene& S, const RenderCfg& cfg, const G
 
 // the sphere's (u, v) of a mapping: the spherical angles, then the
 // equirectangular, angular and panoramic maps, each replacing the last where
-// set; ibl: the IBL block's order (u from theta, v from phi) and its clamp
-// of the angular map's cosine
-__device__ __forceinline__ void sphere_uv(int flags, float3 vv, bool ibl, float& u, float& v) {
+// set; swap: the IBL and bump blocks' order (u from theta, v from phi);
+// clamp: the IBL block's clamp of the angular map's cosine
+__device__ __forceinline__ void sphere_uv(int flags, float3 vv, bool swap, bool clamp, float& u, float& v) {
   const float kPi = 3.14159265358979323846f, kTwoPi = 6.28318530717958647692f;
   const float th = acosf(fminf(1.0f, fmaxf(-1.0f, vv.z)));  // SphericalTheta (vector3d.h:259-261)
   float ph = atan2f(vv.y, vv.x);                             // SphericalPhi (:262-267)
   if (ph < 0.0f) ph += kTwoPi;
   if (ph >= kTwoPi) ph = 0.0f;
-  u = ibl ? th / kPi : ph / kTwoPi;
-  v = ibl ? ph / kTwoPi : th / kPi;
+  u = swap ? th / kPi : ph / kTwoPi;
+  v = swap ? ph / kTwoPi : th / kPi;
   if (flags & PR_MAP_EQUIRECTANGULAR) {
     const float len = sqrtf(vv.x * vv.x + vv.y * vv.y + vv.z * vv.z);
     if (len == 0.0f) {
@@ -527,7 +527,7 @@ __device__ __forceinline__ void sphere_uv(int flags, float3 vv, bool ibl, float&
     }
   }
   if (flags & PR_MAP_ANGULAR) {
-    const float c = ibl ? fminf(1.0f, fmaxf(-1.0f, vv.z)) : vv.z;
+    const float c = clamp ? fminf(1.0f, fmaxf(-1.0f, vv.z)) : vv.z;
     const float r = acosf(c) / kPi / sqrtf(vv.x * vv.x + vv.y * vv.y);
     u = 0.5f * (vv.x * r) + 0.5f;
     v = 0.5f * (vv.y * r) + 0.5f;
@@ -548,18 +548,45 @@ __device__ __forceinline__ float tex_wrap(float x) {
 
 __device__ __forceinline__ int tex_clamp(int i, int n) { return min(max(i, 0), n - 1); }
 
+// the bump map's tilted normal at texel (i, j): central luminance
+// differences (the reference's wrap at the edges, which a square map keeps
+// in range) times 0.5 * scale along the tangents (sphere.h:411-492,
+// plane.h:290-360); n is the entity's own normal before its inversion
+__device__ __forceinline__ float3 bump_tilt(const DevScene& S, const GMaterial& m, int i, int j, float3 n, float3 sdir,
+                                            float3 tdir, float scale) {
+  const int W = m.bump_w, H = m.bump_h;
+  i = tex_clamp(i, H);
+  j = tex_clamp(j, W);
+  int u0 = j - 1, u1 = j + 1, v0 = i - 1, v1 = i + 1;
+  if (u0 < 0) u0 = W - 1;
+  if (v0 < 0) v0 = W - 1;
+  if (u1 >= W) u1 = 0;
+  if (v1 >= H) v1 = 0;
+  const float* Y = S.bump_texels + m.bump_off;
+  const float gx = scale * (__ldg(Y + (size_t)i * W + u1) - __ldg(Y + (size_t)i * W + u0)) * 0.5f;
+  const float gy = scale * (__ldg(Y + (size_t)v1 * W + j) - __ldg(Y + (size_t)v0 * W + j)) * 0.5f;
+  return n + cross(n, tdir) * gx - cross(n, sdir) * gy;
+}
+
 // The hit point's material where a texture or IBL image rewrites it: the
 // texture gives colour and specular, the IBL image colour and emission
-// (ibl_coef times the texel).  Returns true for a material with an IBL
+// (ibl_coef times the texel); a bump map gives the tilted normal bn (and
+// bit 2 of the result).  Bit 1 of the result: the material has an IBL
 // image, whose hit the caller ends with its emission (radiance.h:45-50).
-__device__ inline bool hit_texture(const DevScene& S, const GMaterial& m, const GEntF& e, const GEntity& ed, float3 p,
-                                   float3& C, float3& E, float3& Sp) {
+__device__ inline int hit_texture(const DevScene& S, const GMaterial& m, const GEntF& e, const GEntity& ed, float3 p,
+                                  float3 n_hit, float3& C, float3& E, float3& Sp, float3& bn) {
   const bool has_ibl = m.ibl_off >= 0;
+  int res = has_ibl ? 1 : 0;
   if (e.type == PR_ENT_UVPLANE) {
     const float3 rel = p - f3(e.p[0], e.p[1], e.p[2]);
     const float u = dot(rel, f3(e.u[0], e.u[1], e.u[2])) / e.u_length;
     const float v = dot(rel, f3(e.v[0], e.v[1], e.v[2])) / e.v_length;
     const float uu = tex_wrap(u * (float)m.repeat), vv = tex_wrap(v * (float)m.repeat);
+    if (m.bump_off >= 0) {
+      bn = bump_tilt(S, m, (int)((m.bump_h - 1) * vv), (int)((m.bump_w - 1) * uu), f3(e.n[0], e.n[1], e.n[2]),
+                     f3(e.u[0], e.u[1], e.u[2]), f3(e.v[0], e.v[1], e.v[2]), 1.0f);
+      res |= 2;
+    }
     if (m.tex_off >= 0) {
       const float4 t = __ldg(S.texels + m.tex_off + (size_t)tex_clamp((int)((m.tex_h - 1) * vv), m.tex_h) * m.tex_w +
                              tex_clamp((int)((m.tex_w - 1) * uu), m.tex_w));
@@ -572,18 +599,35 @@ __device__ inline bool hit_texture(const DevScene& S, const GMaterial& m, const 
       C = f3(t.x, t.y, t.z);
       E = C * m.ibl_coef;
     }
-    return has_ibl;
+    return res;
   }
   // sphere / hemisphere: hemisphere_map looks along y (x, y, z -> z, x, y)
   const float r = (float)ed.radius;
   const float3 q = p - f3(e.p[0], e.p[1], e.p[2]);
   const bool hm = (m.map_flags & PR_MAP_HEMISPHERE) != 0;
   const float px = hm ? q.z : q.x, py = hm ? q.x : q.y, pz = hm ? q.y : q.z;
-  if (!(fabsf(pz - r) > 1.0e-16f)) return has_ibl;  // at the pole the reference leaves the material
   const float3 vv = f3(px / r, py / r, pz / r);
+  if (m.bump_off >= 0 && fabsf(q.z - r) > 1.0e-16f) {  // the bump block tests the unmapped z
+    float u, v;
+    sphere_uv(m.map_flags, vv, true, false, u, v);
+    if (ed.hemisphere) u *= 2.0f;
+    const int j = (int)((m.bump_w - 1) * tex_wrap(u * (float)m.repeat));
+    const int i = (int)((m.bump_h - 1) * tex_wrap(v * (float)m.repeat));
+    const float th = acosf(fminf(1.0f, fmaxf(-1.0f, vv.z)));
+    float ph = atan2f(vv.y, vv.x);
+    if (ph < 0.0f) ph += 6.28318530717958647692f;
+    if (ph >= 6.28318530717958647692f) ph = 0.0f;
+    float st, ct, sp, cp;
+    sincosf(th, &st, &ct);
+    sincosf(ph, &sp, &cp);
+    bn = bump_tilt(S, m, i, j, e.normal_inverse < 0 ? -n_hit : n_hit, f3(ct * cp, ct * sp, -st), f3(-st * sp, st * cp, 0.0f),
+                   0.1f);
+    res |= 2;
+  }
+  if (!(fabsf(pz - r) > 1.0e-16f)) return res;  // at the pole the reference leaves the material
   if (m.tex_off >= 0) {
     float u, v;
-    sphere_uv(m.map_flags, vv, false, u, v);
+    sphere_uv(m.map_flags, vv, false, false, u, v);
     if (ed.hemisphere) u *= 2.0f;
     int j = (int)((m.tex_w - 1) * tex_wrap(u * (float)m.repeat));
     int i = (int)((m.tex_h - 1) * tex_wrap(v * (float)m.repeat));
@@ -596,7 +640,7 @@ __device__ inline bool hit_texture(const DevScene& S, const GMaterial& m, const 
   }
   if (has_ibl) {
     float u, v;
-    sphere_uv(m.map_flags, vv, true, u, v);
+    sphere_uv(m.map_flags, vv, true, true, u, v);
     if (ed.hemisphere) u *= 2.0f;
     int j = (int)((m.ibl_w - 1) * u);
     int i = (int)((m.ibl_h - 1) * v);
@@ -608,7 +652,17 @@ __device__ inline bool hit_texture(const DevScene& S, const GMaterial& m, const 
     C = f3(t.x, t.y, t.z);
     E = C * m.ibl_coef;
   }
-  return has_ibl;
+  return res;
+}
+
+// a bump map's scale of a next-event term towards ldir
+// (directLight_radiance.h:303-310) and of a scattered weight along dir
+// (brdf.h:102-108, :552-557, :740-745); n is the hit's normal
+__device__ __forceinline__ float bump_nee(float3 bn, float3 n, float3 ldir) {
+  return fmaxf(0.0f, dot(ldir, bn)) / dot(ldir, n);
+}
+__device__ __forceinline__ float bump_weight(float3 bn, float3 n, float3 dir) {
+  return fmaxf(0.1f, dot(dir, bn)) / dot(dir, n);
 }
 
 // the Phong (kind 4) or Ward (kind 5) lobe towards ldir as the reference's
@@ -682,12 +736,18 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   const GEntF& ent = S.entf[v.ent];
   float3 E = ovr ? ovr[1] : ld3(m.emission), C = ovr ? ovr[0] : ld3(m.color);
   float3 Sp = ld3(m.specular);
-  if (EXT && (m.tex_off >= 0 || m.ibl_off >= 0) && hit_texture(S, m, ent, S.ents[v.ent], v.p, C, E, Sp)) {
-    // an object with an IBL image gives its hit point's emission and nothing
-    // else (radiance.h:45-50)
-    ps.L += ps.beta * E;
-    if (tap) tap->em(v.mat, ps.beta);
-    return SHADE_END;
+  float3 bn = f3(0, 0, 0);  // bump-tilted normal
+  bool bumped = false;
+  if (EXT && (m.tex_off >= 0 || m.ibl_off >= 0 || m.bump_off >= 0)) {
+    const int tx = hit_texture(S, m, ent, S.ents[v.ent], v.p, v.n, C, E, Sp, bn);
+    if (tx & 1) {
+      // an object with an IBL image gives its hit point's emission and
+      // nothing else (radiance.h:45-50)
+      ps.L += ps.beta * E;
+      if (tap) tap->em(v.mat, ps.beta);
+      return SHADE_END;
+    }
+    bumped = (tx & 2) != 0;
   }
   const float3 d = ps.d;
   const float3 on = dot(v.n, d) < 0.0f ? v.n : -v.n;
@@ -822,7 +882,8 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
           if (EXT && L.kind != PR_LIGHT_AREA) {
             LightSample ls;
             if (point_light_sample(S, L, v.p, on, origin, true, media, rng, ls))
-              push_shadow(S, ls, w * ls.k * 3.14159265358979323846f, L.mat, sh, nsh);
+              push_shadow(S, ls, w * ls.k * (3.14159265358979323846f * (bumped ? bump_nee(bn, v.n, ls.ldir) : 1.0f)),
+                          L.mat, sh, nsh);
             continue;
           }
           if (!nee) continue;
@@ -845,7 +906,8 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
             sh[nsh].o = origin;
             sh[nsh].d = dlo / disto;
             sh[nsh].tmax = disto - 1.0e-3f;
-            const float3 ew = w * (dot0 * dot1 / dist2 * le.area);
+            float3 ew = w * (dot0 * dot1 / dist2 * le.area);
+            if (EXT && bumped) ew = ew * bump_nee(bn, v.n, ldir);
             sh[nsh].contrib = ew * em;
             sh[nsh].ew = media ? ew * medium_tr(S.medium, dist) : ew;
             sh[nsh].lmat = le.material;
@@ -859,6 +921,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     ps.L += ps.beta * (env + tri * E);
     if (tap) tap->em(v.mat, ps.beta * tri);
     ps.beta = ps.beta * C * tri * inv_rr;
+    if (EXT && bumped) ps.beta = ps.beta * bump_weight(bn, v.n, nd);
     ps.o = origin;
     ps.d = nd;
     ps.depth++;
@@ -916,7 +979,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
           LightSample ls;
           if (!point_light_sample(S, L, v.p, on, origin, true, media, rng, ls)) continue;
           const float f = glossy_lobe(kind, m, refl, in, on, a, b, ls.ldir);
-          if (f > 0.0f) push_shadow(S, ls, w * ls.k * f, L.mat, sh, nsh);
+          if (f > 0.0f) push_shadow(S, ls, w * ls.k * (f * (bumped ? bump_nee(bn, v.n, ls.ldir) : 1.0f)), L.mat, sh, nsh);
           continue;
         }
         if (!nee) continue;
@@ -951,7 +1014,8 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
         sh[nsh].o = origin;
         sh[nsh].d = dlo / disto;
         sh[nsh].tmax = disto - 1.0e-3f;
-        const float3 ew = w * (f * dot0 * dot1 / dist2 * le.area);
+        float3 ew = w * (f * dot0 * dot1 / dist2 * le.area);
+        if (EXT && bumped) ew = ew * bump_nee(bn, v.n, ldir);
         sh[nsh].contrib = ew * em;
         sh[nsh].ew = media ? ew * medium_tr(S.medium, dist) : ew;
         sh[nsh].lmat = le.material;
@@ -961,6 +1025,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     ps.L += ps.beta * (env + tri * E);
     if (tap) tap->em(v.mat, ps.beta * tri);
     ps.beta = ps.beta * Sp * (ww * inv_rr) * tri;
+    if (EXT && bumped) ps.beta = ps.beta * bump_weight(bn, v.n, nd);
     ps.o = origin;
     ps.d = nd;
     ps.depth++;
@@ -973,6 +1038,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     ps.L += ps.beta * (env + tri * E);
     if (tap) tap->em(v.mat, ps.beta * tri);
     ps.beta = ps.beta * C * tri * inv_rr;
+    if (EXT && bumped) ps.beta = ps.beta * bump_weight(bn, v.n, nd);  // the mirror ray and its light term
     ps.dp = nee;
     ps.dpw = ps.beta;
     ps.o = offset_ray(v.p, dot(nd, v.n) > 0.0f ? v.n : -v.n);

@@ -102,6 +102,7 @@ struct GMaterial {
   float ibl_coef;
   int32_t repeat;
   int32_t map_flags;       // PR_MAP_*
+  int32_t bump_off, bump_w, bump_h;  // bump map texels in DevScene::bump_texels (-1: none)
 };
 
 struct GEntity {
@@ -219,6 +220,7 @@ struct DevScene {
   const float* fnorm;      // 3 per face
   const float4* texels;    // every material's texture, RGB / 255 (cell(i, j) order)
   const float4* ibl_texels;  // every IBL image, IBL_Color(i, j) order
+  const float* bump_texels;  // every bump map: the texel's luminance 0.299 r + 0.587 g + 0.114 b (0..255)
   int32_t n_ents;
   int32_t n_lights;
   int32_t n_point_lights;  // parallel, spot and infinity lights (sampled even without NEE)

@@ -376,7 +376,24 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
     g.ior_d = pm.refractive_index;
     // texture and IBL images (material.h:176-236): texels as float RGB, a
     // bitmap's bytes / 255 (BitMap cell values), an HDR image's values
-    g.tex_off = g.ibl_off = -1;
+    g.tex_off = g.ibl_off = g.bump_off = -1;
+    if (pm.bump) {
+      if (pm.bump_width <= 0 || pm.bump_height <= 0) { err = "bump map size must be positive"; return PR_E_ARG; }
+      if (pm.bump_width != pm.bump_height) {
+        err = "bump maps are square here (the reference wraps the row above the first to W - 1)";
+        return PR_E_UNSUPPORTED;
+      }
+      if (pm.type != PR_MAT_DIFFUSE && pm.type != PR_MAT_SPECULAR && pm.type != PR_MAT_WARD && pm.type != PR_MAT_PHONG) {
+        err = "bump maps on glass and subsurface materials are not on this path";
+        return PR_E_UNSUPPORTED;
+      }
+      g.bump_off = (int32_t)hs.bump_texels.size();
+      g.bump_w = pm.bump_width;
+      g.bump_h = pm.bump_height;
+      const size_t n = (size_t)g.bump_w * g.bump_h;
+      for (size_t k = 0; k < n; k++)
+        hs.bump_texels.push_back((float)(0.299 * pm.bump[3 * k] + 0.587 * pm.bump[3 * k + 1] + 0.114 * pm.bump[3 * k + 2]));
+    }
     g.repeat = pm.repeat;
     g.map_flags = pm.map_flags;
     g.ibl_coef = (float)pm.ibl_coef;
@@ -561,7 +578,7 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
     g.material = pe.material;
     g.normal_inverse = pe.normal_inverse < 0 ? -1 : 1;
     const pr_material& pm = d->materials[pe.material];
-    const bool textured = pm.texture || pm.ibl_rgb8 || pm.ibl_rgbf;
+    const bool textured = pm.texture || pm.ibl_rgb8 || pm.ibl_rgbf || pm.bump;
     if (textured && pe.type != PR_ENT_SPHERE && pe.type != PR_ENT_UVPLANE) {
       err = "textures and IBL images are read on spheres, hemispheres and uvplanes only";
       return PR_E_UNSUPPORTED;

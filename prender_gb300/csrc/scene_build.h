@@ -36,6 +36,7 @@ struct HostScene {
   std::vector<float> fnorm;
   std::vector<float4> texels;           // material textures, RGB / 255
   std::vector<float4> ibl_texels;       // material IBL images
+  std::vector<float> bump_texels;       // material bump maps (luminance)
   std::vector<GLight> lights;           // in the reference's sorted order
   std::vector<int32_t> light_id;        // per entity: registration index (-1: not a light)
   std::vector<MeshQbvh> mesh_qbvh;

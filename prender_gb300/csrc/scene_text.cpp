@@ -49,7 +49,7 @@ struct pr_scene_file {
   std::vector<pr_mesh> meshes;
   std::vector<uint8_t> bg_tex, disk_tex;
   // per material: texture / IBL images (pointers set when the desc is made)
-  std::vector<std::vector<uint8_t>> tex8, ibl8;
+  std::vector<std::vector<uint8_t>> tex8, ibl8, bump8;
   std::vector<std::vector<float>> iblf;
   pr_scene_desc desc;
   pr_camera cam;
@@ -835,13 +835,14 @@ class Loader {
     S_.tex8.push_back(std::move(tx.tex8));
     S_.ibl8.push_back(std::move(tx.ibl8));
     S_.iblf.push_back(std::move(tx.iblf));
+    S_.bump8.push_back(std::move(tx.bump8));
     S_.ents.push_back(e);
   }
 
   // an OBJECT's images (scene_env.h:984-1175): texture, ibl_texture (BMP or
   // Radiance HDR), ibl_texture_coef, repeat and the four sphere mappings
   struct ObjTex {
-    std::vector<uint8_t> tex8, ibl8;
+    std::vector<uint8_t> tex8, ibl8, bump8;
     std::vector<float> iblf;
   };
   bool texture_line(const std::string& b, const std::vector<std::string>& bt, pr_material& m, ObjTex& tx) {
@@ -867,6 +868,11 @@ class Loader {
       }
       m.ibl_width = w;
       m.ibl_height = h;
+    } else if (k == "bump_texture" && bt.size() >= 2) {
+      int w = 0, h = 0;
+      read_bmp(resolve(b.substr(13), sdir_), 3, tx.bump8, w, h);
+      m.bump_width = w;
+      m.bump_height = h;
     } else if (k == "ibl_texture_coef") {
       m.ibl_coef = num_.many(after_key(b), 1)[0];
     } else if (k == "repeat") {
@@ -1027,7 +1033,7 @@ class Loader {
     } else if (k == "media_ignore_front_back") {
       if ((int)num_.many(after_key(b), 1)[0] != 0) refuse(b);
     } else if (among(k, {"texture", "bump_texture", "ibl_texture"})) {
-      refuse(b);  // bump maps (and an image keyword without a file)
+      refuse(b);  // an image keyword without a file
     } else if (among(k, {"back"})) {
       // not read by anything rendered here
     } else {
@@ -1118,6 +1124,7 @@ class Loader {
       mm.texture = S_.tex8[i].empty() ? nullptr : S_.tex8[i].data();
       mm.ibl_rgb8 = S_.ibl8[i].empty() ? nullptr : S_.ibl8[i].data();
       mm.ibl_rgbf = S_.iblf[i].empty() ? nullptr : S_.iblf[i].data();
+      mm.bump = S_.bump8[i].empty() ? nullptr : S_.bump8[i].data();
     }
     d.materials = S_.mats.data();
     d.entities = S_.ents.data();

@@ -69,6 +69,7 @@ class Material:
     ibl_coef: float = 1.0
     repeat: int = 1
     map_flags: int = 0
+    bump: Optional[np.ndarray] = field(default=None, compare=False, repr=False)  # (N, N, 3) uint8
 
     @staticmethod
     def diffuse(color, emission=(0.0, 0.0, 0.0)) -> "Material":
@@ -157,6 +158,13 @@ class Material:
                     raise ValueError("ibl image must be (H, W, 3)")
                 keep.append(t)
                 m.ibl_height, m.ibl_width = t.shape[0], t.shape[1]
+            if self.bump is not None:
+                t = np.ascontiguousarray(self.bump, dtype=np.uint8)
+                if t.ndim != 3 or t.shape[2] != 3:
+                    raise ValueError("bump texture must be (H, W, 3) uint8")
+                keep.append(t)
+                m.bump = t.ctypes.data_as(C.POINTER(C.c_uint8))
+                m.bump_height, m.bump_width = t.shape[0], t.shape[1]
         return m
 
 
@@ -603,6 +611,10 @@ class Scene:
                 out.append(f"ibl_texture {ip}")
                 if float(m.ibl_coef) != 1.0:
                     out.append(f"ibl_texture_coef {_fmt(m.ibl_coef)}")
+            if m.bump is not None:
+                bp = os.path.join(directory, f"bump{ei}.bmp")
+                _write_bmp24(bp, np.asarray(m.bump, dtype=np.uint8))
+                out.append(f"bump_texture {bp}")
             if int(m.repeat) != 1:
                 out.append(f"repeat {int(m.repeat)}")
             for bit, key in ((A.PR_MAP_HEMISPHERE, "hemisphere_map"), (A.PR_MAP_ANGULAR, "angular_map"),

@@ -93,7 +93,8 @@ def load(path: str) -> Scene:
                 texture=_image(m.texture, m.texture_height, m.texture_width, np.uint8),
                 ibl=(_image(m.ibl_rgb8, m.ibl_height, m.ibl_width, np.uint8) if m.ibl_rgb8
                      else _image(m.ibl_rgbf, m.ibl_height, m.ibl_width, np.float32)),
-                ibl_coef=float(m.ibl_coef), repeat=int(m.repeat), map_flags=int(m.map_flags)))
+                ibl_coef=float(m.ibl_coef), repeat=int(m.repeat), map_flags=int(m.map_flags),
+                bump=_image(m.bump, m.bump_height, m.bump_width, np.uint8)))
         for i in range(d.n_entities):
             e = d.entities[i]
             s.entities.append(Entity(

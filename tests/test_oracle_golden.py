@@ -135,13 +135,14 @@ def test_light_kinds_render_one_thread_bit_exact(golden, name):
     assert ref.mean() > 0
 
 
-@pytest.mark.parametrize("name", ["tex_maps", "ibl_dome", "ibl_nonee", "ibl_panoramic"])
+@pytest.mark.parametrize("name", ["tex_maps", "ibl_dome", "ibl_nonee", "ibl_panoramic", "bump", "bump_nonee"])
 def test_texture_render_one_thread_bit_exact(golden, name):
     # textures on spheres in every mapping (spherical with repeat,
     # equirectangular, angular, panoramic, hemisphere_map), on a Ward sphere
     # (specular from the texel), a uvplane and a hemisphere; IBL domes from an
     # HDR image (angular map) and bitmaps (panoramic, equirectangular,
-    # hemisphere_map, a uvplane) whose hits return their emission
+    # hemisphere_map, a uvplane) whose hits return their emission; bump maps
+    # on diffuse, Ward and mirror surfaces, NEE on and off
     import texture_cases
     sc = texture_cases.one_thread_cases()[name]
     img, _, _ = O.OracleScene(sc).render(threads=1)

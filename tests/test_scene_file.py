@@ -103,7 +103,7 @@ def test_light_kind_files_render_like_the_reference(tmp_path, golden, name):
     assert np.array_equal(img, golden["lights_render"][name])
 
 
-@pytest.mark.parametrize("name", ["tex_maps", "ibl_dome", "ibl_nonee", "ibl_panoramic"])
+@pytest.mark.parametrize("name", ["tex_maps", "ibl_dome", "ibl_nonee", "ibl_panoramic", "bump", "bump_nonee"])
 def test_texture_files_render_like_the_reference(tmp_path, golden, name):
     # the files the reference rendered for textures_render.npz (BMP textures,
     # BMP and Radiance HDR IBL images, the mappings, repeat, hemispheres),
@@ -112,7 +112,7 @@ def test_texture_files_render_like_the_reference(tmp_path, golden, name):
     sc = texture_cases.one_thread_cases()[name]
     s = scene_file.load(sc.write_reference(str(tmp_path)))
     for a, b in zip(sc.materials, s.materials):
-        for f in ("texture", "ibl"):
+        for f in ("texture", "ibl", "bump"):
             x, y = getattr(a, f), getattr(b, f)
             assert (x is None) == (y is None)
             if x is not None:
@@ -254,7 +254,6 @@ def test_bad_values_are_errors_with_the_line(tmp_path, body, msg):
 
 
 @pytest.mark.parametrize("body", [
-    "OBJECT\nsphere 0 0 0 1\nbump_texture b.bmp\n\n",
     "OBJECT\nsphere 0 0 0 1\nsmooth 1\n\n",
     "OBJECT\nsphere 0 0 0 1\nMATERIAL_SYMBOL\nKetchup\n\n",
     "OBJECT\nsphere 0 0 0 1\nreflection reflection1\n1 2 3 4 5 6\n\n",

@@ -16,6 +16,12 @@ plane.h:241-273), shared by the golden-vector generator and the tests.
 * 'ibl_panoramic': a full sphere dome with a bitmap IBL image in the
   panoramic map, and the equirectangular and hemisphere_map variants on
   smaller spheres.
+* 'bump', 'bump_nonee': bump maps (square, smooth noise) on a diffuse
+  uvplane floor (nothing below it: the reference's weight divides by the
+  cosine to the plane's own normal, which a ray from underneath turns
+  negative), a diffuse, a Ward, a mirror and a textured sphere, with
+  next-event estimation on and off; the tilted normal scales each
+  scattered weight and next-event term.
 
 Textures are seeded synthetic images (checkerboards, gradients, noise);
 the HDR image holds values that RGBE stores exactly."""
@@ -24,7 +30,7 @@ import numpy as np
 from prender_gb300 import _abi as A
 from prender_gb300.scene import Camera, Material, RenderSettings, Scene, rgbe_values
 
-CASES = ["tex_maps", "ibl_dome", "ibl_nonee", "ibl_panoramic"]
+CASES = ["tex_maps", "ibl_dome", "ibl_nonee", "ibl_panoramic", "bump", "bump_nonee"]
 
 
 def checker(h, w, n, c0, c1, seed):
@@ -49,6 +55,16 @@ def sky_hdr(h, w, seed):
     e += rng.integers(-1, 2, (h, w))
     q[..., 3] = e
     return rgbe_values(q)
+
+
+def bump_map(n, seed, blur=3, amp=255.0):
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(0, 255, (n, n))
+    for _ in range(blur):  # smooth, wrapping
+        a = (a + np.roll(a, 1, 0) + np.roll(a, -1, 0) + np.roll(a, 1, 1) + np.roll(a, -1, 1)) / 5.0
+    a = (a - a.min()) / (a.max() - a.min() + 1e-9) * amp
+    g = np.clip(a, 0, 255).astype(np.uint8)
+    return np.stack([g, np.roll(g, 3, 1), g], axis=2)
 
 
 def _walls(s):
@@ -126,6 +142,32 @@ def build(name: str, width: int, height: int, samples: int, supersamples: int = 
         s.add_sphere((50, 12, 90), 8, Material.mirror((0.9, 0.9, 0.9)))
         s.camera = Camera(position=(50, 40, 220), dir=(0, -0.1, -1), angle=35, width=width, height=height)
         s.settings = RenderSettings(samples=samples, supersamples=supersamples, tent_filter=1, depth=5, nee=1, seed=0)
+        return s
+    if name in ("bump", "bump_nonee"):
+        s.add_sphere((100001, 40.8, 81.6), 100000, Material.diffuse((0.75, 0.25, 0.25)))
+        s.add_sphere((-99901, 40.8, 81.6), 100000, Material.diffuse((0.25, 0.25, 0.75)))
+        s.add_sphere((50, 40.8, 100000), 100000, Material.diffuse((0.75, 0.75, 0.75)))
+        s.add_sphere((50, -99918.4, 81.6), 100000, Material.diffuse((0.75, 0.75, 0.75)))
+        floor = Material.diffuse((0.7, 0.7, 0.7))
+        floor.bump = bump_map(32, 31, blur=4, amp=60.0)
+        floor.repeat = 3
+        s.add_uvplane((-20, 0.0, -20), (0, 0, 16), (16, 0, 0), floor)  # spans x, z in [-20, 236]
+        ball = Material.diffuse((0.3, 0.7, 0.4))
+        ball.bump = bump_map(32, 33)
+        s.add_sphere((30, 14, 90), 14, ball)
+        ward = Material.ward((0.2, 0.2, 0.3), (0.6, 0.6, 0.5), 0.15, 0.25)
+        ward.bump = bump_map(16, 32)
+        s.add_sphere((75, 10, 110), 10, ward)
+        mir = Material.mirror((0.9, 0.9, 0.9))
+        mir.bump = bump_map(16, 34, blur=1)
+        s.add_sphere((72, 14, 65), 14, mir)
+        tb = _textured(checker(32, 32, 4, (220, 80, 60), (60, 80, 220), 35), repeat=2)
+        tb.bump = bump_map(32, 36)
+        s.add_sphere((50, 42, 60), 8, tb)
+        s.add_sphere((50, 76, 81.6), 5, Material.diffuse((0, 0, 0), (36, 36, 36)))
+        s.camera = Camera(position=(50, 52, 220), dir=(0, -0.04, -1), angle=30, width=width, height=height)
+        s.settings = RenderSettings(samples=samples, supersamples=supersamples, tent_filter=1, depth=5,
+                                    nee=1 if name == "bump" else 0, seed=0)
         return s
     raise KeyError(name)
 
