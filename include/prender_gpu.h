@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define PR_ABI_VERSION 4
+#define PR_ABI_VERSION 5
 
 /* ---- status codes --------------------------------------------------- */
 enum {
@@ -227,6 +227,34 @@ typedef struct pr_kerr {
                                  from the clock, scene_env.h:306)             */
 } pr_kerr;
 
+/* A traversable wormhole (WormHole.h:126-540, scene_env.h:767-856,
+ * :2100-2145): the Dneg metric of James, von Tunzelmann, Franklin and
+ * Thorne ("Visualizing Interstellar's wormhole", 2015) with throat radius
+ * rho, length 2a and lensing width w (M = w / 1.42953).  Every scene query
+ * of radiance() follows a geodesic from the ray's origin (its mouth chosen
+ * by |origin| > 1e6), stepped by Cash-Karp RK45 and tested against the
+ * scene segment by segment; a ray that leaves ends on background 1 (l >= 0)
+ * or 2 (l < 0).  Renders without next-event estimation and media. */
+typedef struct pr_wormhole {
+  int32_t enabled;
+  int32_t max_steps;          /* geodesics_max_length                        */
+  double in[3];               /* 'in' mouth (position0); the reference's
+                                 default is CAMERA_POS + CAMERA_DIR * dist   */
+  double out[3];              /* 'out' mouth (position1; default 0 0 0)      */
+  double rho, a, w;           /* Rho, a, W                                   */
+  int32_t sign;               /* 'sign': a nonzero value multiplies the final
+                                 l before the side is read (usr_set_sign_)   */
+  int32_t pad0;
+  double camera[3];           /* camera_position the wormhole was built with
+                                 (its frame's x axis points from the mouth to it) */
+  const uint8_t* texture[2];  /* background_texture1 / 2, RGB8 rows as
+                                 BitMap::cell(y, x) reads them; NULL = none   */
+  int32_t texture_width[2];
+  int32_t texture_height[2];
+  double map_coef[2][4];      /* map_coef1 / map_coef2 (theta, phi) affine  */
+  double texture_coef[2];     /* coef1 / coef2                               */
+} pr_wormhole;
+
 typedef struct pr_scene_desc {
   int32_t n_materials;
   int32_t n_entities;
@@ -239,6 +267,7 @@ typedef struct pr_scene_desc {
   double environment_light[3];  /* ENVLIGHT                                 */
   pr_medium medium;             /* global SCATTERING / ABSORBING / PAHASE   */
   pr_kerr kerr;
+  pr_wormhole wormhole;
 } pr_scene_desc;
 
 /* CameraScreenPram (render.h:70-158) inputs, after SceneEnv::Load. */
@@ -484,6 +513,20 @@ int pr_kerr_trace(pr_ctx* ctx, const double* rays, int64_t n, int32_t* status,
 int pr_kerr_trace_dev(pr_ctx* ctx, const double* rays, int64_t n, int32_t* status,
                       double* final_bl, double* exit_dir, int32_t* steps,
                       int32_t* hit_entity, double* hit_t);
+
+/* ---- Wormhole geodesics ---------------------------------------------- */
+/* The wormhole branch of intersect_scene__ (scene.cpp:735-925) for n rays
+ * (FP64, 6 per ray).  Per ray: status (1 hit an entity, 0 ended on
+ * background 1 (final l >= 0), 3 on background 2 (l < 0)), final state
+ * (l, then theta and phi of the last polyline direction), that direction,
+ * steps taken and the hit entity (-1: none).  Host buffers; the _dev form
+ * takes device pointers.  Any output may be NULL. */
+int pr_wormhole_trace(pr_ctx* ctx, const double* rays, int64_t n, int32_t* status,
+                      double* final_y, double* exit_dir, int32_t* steps,
+                      int32_t* hit_entity);
+int pr_wormhole_trace_dev(pr_ctx* ctx, const double* rays, int64_t n, int32_t* status,
+                          double* final_y, double* exit_dir, int32_t* steps,
+                          int32_t* hit_entity);
 
 /* Ray-bundle Jacobian of the Kerr map (no reference counterpart).  The
  * initial direction d of each ray is perturbed as normalize(d + s e1 + t e2);

@@ -48,6 +48,7 @@ def lib():
         L.oracle_render_rows.argtypes = [vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp]
         L.oracle_light_count.argtypes = [vp]
         L.oracle_kerr_trace.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.oracle_wormhole_trace.argtypes = [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp, vp]
         L.oracle_kerr_trace_threads.argtypes = [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]
         L.oracle_kerr_disk_shade.argtypes = [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp]
         L.oracle_sample_hg.argtypes = [C.c_double, C.c_int, C.c_uint64, vp, C.c_int64, vp]
@@ -153,6 +154,20 @@ class OracleScene:
         rc = lib().oracle_kerr_trace_threads(self.h, int(threads), _p(rays), n, _p(out["status"]), _p(out["final_bl"]),
                                      _p(out["exit_dir"]), _p(out["steps"]), _p(out["hit_entity"]),
                                      _p(out["hit_t"]), _p(out["hit_color"]), _p(out["hit_emission"]))
+        assert rc == 0, rc
+        return out
+
+    def wormhole_trace(self, rays: np.ndarray, threads: int = 1):
+        """The wormhole branch of intersect_scene per ray: status 1 entity
+        hit, 0 background 1 (l >= 0), 3 background 2; final (l, theta, phi)
+        with the angles of the last polyline direction, that direction,
+        steps, hit entity"""
+        rays = np.ascontiguousarray(rays, dtype=np.float64)
+        n = rays.shape[0]
+        out = dict(status=np.empty(n, np.int32), final_y=np.empty((n, 3)), exit_dir=np.empty((n, 3)),
+                   steps=np.empty(n, np.int32), hit_entity=np.empty(n, np.int32))
+        rc = lib().oracle_wormhole_trace(self.h, int(threads), _p(rays), n, _p(out["status"]), _p(out["final_y"]),
+                                         _p(out["exit_dir"]), _p(out["steps"]), _p(out["hit_entity"]))
         assert rc == 0, rc
         return out
 

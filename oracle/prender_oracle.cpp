@@ -250,7 +250,21 @@ struct KerrBH {  // KerrBlackHole (KerrBlackHole.h:86-151) with M = 1, initial_c
   uint64_t disk_seed = 0;
 };
 
+struct Wormhole {  // WormHole (WormHole.h:126-540) as SceneEnv builds it (scene_env.h:2100-2145)
+  bool on = false;
+  V3 pos0, pos1;       // position0 ('in'), position1 ('out')
+  double Rho = 0, a = 0, M = 1, W = 0;
+  int max_steps = 10000;
+  int usr_sign = 0;
+  V3 camera;
+  std::vector<unsigned char> tex[2];
+  int tex_w[2] = {0, 0}, tex_h[2] = {0, 0};
+  double map_coef[2][4] = {{1, 0, 1, 0}, {1, 0, 1, 0}};
+  double tex_coef[2] = {1, 1};
+};
+
 struct Scene {
+  Wormhole worm;
   KerrBH kerr;
   std::vector<Material> mats;
   std::vector<Entity> ents;
@@ -1055,6 +1069,30 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
       return PR_E_UNSUPPORTED;
     }
     s.ents.push_back(std::move(e));
+  }
+  if (d->wormhole.enabled) {
+    const pr_wormhole& w = d->wormhole;
+    if (d->kerr.enabled) { err = "a scene has a black hole or a wormhole"; return PR_E_UNSUPPORTED; }
+    Wormhole& wh = s.worm;
+    wh.on = true;
+    wh.pos0 = V3(w.in[0], w.in[1], w.in[2]);
+    wh.pos1 = V3(w.out[0], w.out[1], w.out[2]);
+    wh.Rho = w.rho;
+    wh.W = w.w;
+    wh.a = std::fabs(w.a);
+    wh.M = wh.W / 1.42953;
+    wh.max_steps = w.max_steps;
+    wh.usr_sign = w.sign;
+    wh.camera = V3(w.camera[0], w.camera[1], w.camera[2]);
+    for (int k = 0; k < 2; k++) {
+      for (int q = 0; q < 4; q++) wh.map_coef[k][q] = w.map_coef[k][q];
+      wh.tex_coef[k] = w.texture_coef[k];
+      if (w.texture[k] && w.texture_width[k] > 0 && w.texture_height[k] > 0) {
+        wh.tex_w[k] = w.texture_width[k];
+        wh.tex_h[k] = w.texture_height[k];
+        wh.tex[k].assign(w.texture[k], w.texture[k] + 3 * (size_t)wh.tex_w[k] * wh.tex_h[k]);
+      }
+    }
   }
   if (d->kerr.enabled) {
     s.kerr.on = true;
@@ -2052,6 +2090,7 @@ V3 brdf_sss2(Ctx& c, V3 raydir, const Hit& hp, int ent, V3 on, double p_rr, doub
 // Kerr branch of intersect_scene (defined with the Kerr restatement below);
 // on a miss, miss_color is what radiance() returns for it (radiance.h:30-43)
 bool kerr_query(const Scene& s, V3 org, V3 dir, Hit& hit, V3& miss_color);
+bool worm_query(const Scene& s, V3 org, V3 dir, Hit& hit, V3& miss_color);
 
 // radiance() (radiance.h:25-556): diffuse / specular / refraction / media
 V3 radiance(Ctx& c, V3 org, V3 dir, int depth) {
@@ -2060,6 +2099,9 @@ V3 radiance(Ctx& c, V3 org, V3 dir, int depth) {
   if (s.kerr.on) {
     V3 miss;
     if (!kerr_query(s, org, dir, hp, miss)) return miss;
+  } else if (s.worm.on) {
+    V3 miss;
+    if (!worm_query(s, org, dir, hp, miss)) return miss;
   } else if (!intersect(s, org, dir, hp)) {
     return s.background;
   }
@@ -2892,6 +2934,326 @@ V3 kerr_background(const KerrBH& kb, const double* yy, const V3& bg) {
   return V3(kb.texture_coef * t[0] / 255.0, kb.texture_coef * t[1] / 255.0, kb.texture_coef * t[2] / 255.0);
 }
 
+// ------------------------------------------------------------ wormhole
+// WormHole.h restated: the Dneg wormhole's radius r(l) and dr/dl, the
+// inverse r -> l by Newton's method, the ray's frame (a basis whose x axis
+// points from the mouth to the camera) and its inverse by cofactors, the
+// geodesic equations (A7) with the initial conditions (A9), and Cash-Karp
+// RK45 with the class's own step control.
+
+inline V3 sph_to_cart(double r, double th, double ph) {  // Spherical::ToCartesian (vector3d.h:879-887)
+  const double sint = std::sin(th);
+  return V3(r * std::cos(ph) * sint, r * std::sin(ph) * sint, r * std::cos(th));
+}
+
+// Matrix4D * Vector3d (vector3d.h:760-768): the upper 3x3 block, row major
+inline V3 mat_mul3(const double* m, V3 v) {
+  return V3(v.x * m[0] + v.y * m[1] + v.z * m[2], v.x * m[4] + v.y * m[5] + v.z * m[6],
+            v.x * m[8] + v.y * m[9] + v.z * m[10]);
+}
+
+// InvertMatrix_ (vector3d.h:577-755): cofactors in the published (Mesa GLU)
+// order; a determinant below 1e-16 leaves B as it was
+bool invert4(const double* A, double* B) {
+  double inv[16];
+  inv[0] = A[5] * A[10] * A[15] - A[5] * A[11] * A[14] - A[9] * A[6] * A[15] + A[9] * A[7] * A[14] +
+           A[13] * A[6] * A[11] - A[13] * A[7] * A[10];
+  inv[4] = -A[4] * A[10] * A[15] + A[4] * A[11] * A[14] + A[8] * A[6] * A[15] - A[8] * A[7] * A[14] -
+           A[12] * A[6] * A[11] + A[12] * A[7] * A[10];
+  inv[8] = A[4] * A[9] * A[15] - A[4] * A[11] * A[13] - A[8] * A[5] * A[15] + A[8] * A[7] * A[13] +
+           A[12] * A[5] * A[11] - A[12] * A[7] * A[9];
+  inv[12] = -A[4] * A[9] * A[14] + A[4] * A[10] * A[13] + A[8] * A[5] * A[14] - A[8] * A[6] * A[13] -
+            A[12] * A[5] * A[10] + A[12] * A[6] * A[9];
+  inv[1] = -A[1] * A[10] * A[15] + A[1] * A[11] * A[14] + A[9] * A[2] * A[15] - A[9] * A[3] * A[14] -
+           A[13] * A[2] * A[11] + A[13] * A[3] * A[10];
+  inv[5] = A[0] * A[10] * A[15] - A[0] * A[11] * A[14] - A[8] * A[2] * A[15] + A[8] * A[3] * A[14] +
+           A[12] * A[2] * A[11] - A[12] * A[3] * A[10];
+  inv[9] = -A[0] * A[9] * A[15] + A[0] * A[11] * A[13] + A[8] * A[1] * A[15] - A[8] * A[3] * A[13] -
+           A[12] * A[1] * A[11] + A[12] * A[3] * A[9];
+  inv[13] = A[0] * A[9] * A[14] - A[0] * A[10] * A[13] - A[8] * A[1] * A[14] + A[8] * A[2] * A[13] +
+            A[12] * A[1] * A[10] - A[12] * A[2] * A[9];
+  inv[2] = A[1] * A[6] * A[15] - A[1] * A[7] * A[14] - A[5] * A[2] * A[15] + A[5] * A[3] * A[14] +
+           A[13] * A[2] * A[7] - A[13] * A[3] * A[6];
+  inv[6] = -A[0] * A[6] * A[15] + A[0] * A[7] * A[14] + A[4] * A[2] * A[15] - A[4] * A[3] * A[14] -
+           A[12] * A[2] * A[7] + A[12] * A[3] * A[6];
+  inv[10] = A[0] * A[5] * A[15] - A[0] * A[7] * A[13] - A[4] * A[1] * A[15] + A[4] * A[3] * A[13] +
+            A[12] * A[1] * A[7] - A[12] * A[3] * A[5];
+  inv[14] = -A[0] * A[5] * A[14] + A[0] * A[6] * A[13] + A[4] * A[1] * A[14] - A[4] * A[2] * A[13] -
+            A[12] * A[1] * A[6] + A[12] * A[2] * A[5];
+  inv[3] = -A[1] * A[6] * A[11] + A[1] * A[7] * A[10] + A[5] * A[2] * A[11] - A[5] * A[3] * A[10] -
+           A[9] * A[2] * A[7] + A[9] * A[3] * A[6];
+  inv[7] = A[0] * A[6] * A[11] - A[0] * A[7] * A[10] - A[4] * A[2] * A[11] + A[4] * A[3] * A[10] +
+           A[8] * A[2] * A[7] - A[8] * A[3] * A[6];
+  inv[11] = -A[0] * A[5] * A[11] + A[0] * A[7] * A[9] + A[4] * A[1] * A[11] - A[4] * A[3] * A[9] -
+            A[8] * A[1] * A[7] + A[8] * A[3] * A[5];
+  inv[15] = A[0] * A[5] * A[10] - A[0] * A[6] * A[9] - A[4] * A[1] * A[10] + A[4] * A[2] * A[9] +
+            A[8] * A[1] * A[6] - A[8] * A[2] * A[5];
+  double det = A[0] * inv[0] + A[1] * inv[4] + A[2] * inv[8] + A[3] * inv[12];
+  if (det < 1.0e-16) return false;
+  det = 1.0 / det;
+  for (int i = 0; i < 16; i++) B[i] = inv[i] * det;
+  return true;
+}
+
+struct WormRay {  // the per-ray copy of the class (scene.cpp:738)
+  const Wormhole& w;
+  double l0 = 0, theta0 = 0, phi0 = 0;
+  double n_l = 0, n_ph = 0, n_th = 0;
+  double Mat[16], invMat[16];
+  explicit WormRay(const Wormhole& w_) : w(w_) {}
+
+  double r_wh(double l) const {  // WormHole.h:172-180
+    const double x = 2.0 * (std::fabs(l) - w.a) / (PI * w.M);
+    if (std::fabs(l) > w.a) return w.Rho + w.M * (x * std::atan(x) - 0.5 * std::log(1.0 + x * x));
+    return w.Rho;
+  }
+  double drdl(double l) const {  // :182-193
+    double sg = 1;
+    if (l < 0) sg = -1;
+    if (l == 0.0) sg = 0.0;
+    if (std::fabs(l) > w.a) return (2.0 * std::atan((2.0 * (-w.a + std::fabs(l))) / (w.M * PI)) * sg) / PI;
+    return 0;
+  }
+  double rtol(double r, double linit) const {  // :195-238, Newton from the start, then from a
+    const double M = w.M, Rho = w.Rho;
+    double x = 2.0 * (std::fabs(linit) - w.a) / (PI * M);
+    int stat = -1;
+    for (int i = 0; i < 30; i++) {
+      const double xi = x;
+      x = x - (Rho + M * (x * std::atan(x) - 0.5 * std::log(1.0 + x * x)) - r) / (M * std::atan(x));
+      if (std::fabs(x - xi) < 1.0e-6) {
+        stat = 0;
+        break;
+      }
+      if (!std::isfinite(x)) break;
+    }
+    double l = x * PI * M * 0.5 + w.a;
+    if (stat != 0) {
+      x = w.a;
+      for (int i = 0; i < 30; i++) {
+        const double xi = x;
+        x = x - (Rho + M * (x * std::atan(x) - 0.5 * std::log(1.0 + x * x)) - r) / (M * std::atan(x));
+        if (std::fabs(x - xi) < 1.0e-6) {
+          l = x * PI * M * 0.5 + w.a;
+          break;
+        }
+        if (!std::isfinite(x)) break;
+      }
+    }
+    return (linit < 0) ? -std::fabs(l) : std::fabs(l);
+  }
+  // Setup (WormHole.h:321-395) with sgn: the ray's mouth
+  void setup(V3 org, double sgn) {
+    const V3 mouth = sgn >= 0 ? w.pos0 : w.pos1;
+    const V3 pos = org - mouth;
+    double pr, pth, pph;
+    cart_to_sph(pos.x, pos.y, pos.z, pr, pth, pph);
+    for (int i = 0; i < 16; i++) Mat[i] = invMat[i] = (i % 5 == 0) ? 1.0 : 0.0;
+    const V3 X = normalize(w.camera - mouth);
+    V3 Y = normalize(cross(V3(0, 0, 1), X));
+    if (length(Y) < 1.0e-16) Y = normalize(cross(V3(0, 1, 0), X));
+    const V3 Z = normalize(cross(X, Y));
+    // Matrix4D(X.x, Y.x, Z.x, 0, X.y, Y.y, Z.y, 0, X.z, Y.z, Z.z, 0, 0, 0, 0, 1) transposed
+    const double m0[16] = {X.x, Y.x, Z.x, 0, X.y, Y.y, Z.y, 0, X.z, Y.z, Z.z, 0, 0, 0, 0, 1.0};
+    for (int i = 0; i < 4; i++)
+      for (int j = 0; j < 4; j++) Mat[4 * i + j] = m0[4 * j + i];
+    (void)invert4(Mat, invMat);
+    const V3 pv = sph_to_cart(pr, pth, pph);
+    const V3 q = mat_mul3(Mat, pv);
+    double qr, qth, qph;
+    cart_to_sph(q.x, q.y, q.z, qr, qth, qph);
+    theta0 = qth;
+    phi0 = qph;
+    l0 = rtol(qr, sgn * w.a / 2);
+  }
+  // initial (WormHole.h:399-428): the direction in the frame, (A9)
+  void initial(double* y, double rr, double rth, double rph) {
+    const V3 rc = mat_mul3(Mat, sph_to_cart(rr, rth, rph));
+    double r_, th, ph;
+    cart_to_sph(rc.x, rc.y, rc.z, r_, th, ph);
+    const double sint = std::sin(th);
+    const double Nx = sint * std::cos(ph), Ny = sint * std::sin(ph), Nz = std::cos(th);
+    n_l = -Nx;
+    n_ph = -Ny;
+    n_th = Nz;
+    y[0] = l0;
+    y[1] = theta0;
+    y[2] = phi0;
+    y[3] = n_l;
+    y[4] = r_wh(l0) * n_th;
+  }
+  // geodesic (WormHole.h:462-488): (A7)
+  void geodesic(const double* y, double* dydx) const {
+    const double r = r_wh(y[0]);
+    const double r2 = r * r;
+    double sint = std::sin(y[1]);
+    if (std::fabs(sint) < 1.0e-8) sint = sint > 0.0 ? 1.0e-8 : -1.0e-8;
+    const double sint2 = sint * sint;
+    const double r_l0 = r_wh(l0);
+    const double b = r_l0 * std::sin(theta0) * n_ph;
+    const double B2 = r_l0 * r_l0 * (n_th * n_th + n_ph * n_ph);
+    const double invr2 = 1.0 / r2;
+    dydx[0] = y[3];
+    dydx[1] = y[4] * invr2;
+    dydx[2] = b * invr2 / sint2;
+    dydx[3] = B2 * drdl(y[0]) * invr2 / r;
+    dydx[4] = (b * b * invr2) * (std::cos(y[1]) / (sint * sint2));
+  }
+  // rkstep (WormHole.h:541-612): Cash-Karp with h negated (traceDir 1)
+  void rkstep(const double* y, const double* dydx, double h, double* yout, double* yerr) const {
+    double ak[5], t1[5], t2[5], t3[5], t4[5], t5[5];
+    h *= -1.0 * 1.0;
+    for (int i = 0; i < 5; i++) {
+      const double hd = h * dydx[i], yi = y[i];
+      t1[i] = yi + 0.2 * hd;
+      t2[i] = yi + (3.0 / 40.0) * hd;
+      t3[i] = yi + 0.3 * hd;
+      t4[i] = yi - (11.0 / 54.0) * hd;
+      t5[i] = yi + (1631.0 / 55296.0) * hd;
+      yout[i] = yi + (37.0 / 378.0) * hd;
+      yerr[i] = ((37.0 / 378.0) - (2825.0 / 27648.0)) * hd;
+    }
+    geodesic(t1, ak);
+    for (int i = 0; i < 5; i++) {
+      const double yt = h * ak[i];
+      t2[i] += (9.0 / 40.0) * yt;
+      t3[i] -= 0.9 * yt;
+      t4[i] += 2.5 * yt;
+      t5[i] += (175.0 / 512.0) * yt;
+    }
+    geodesic(t2, ak);
+    for (int i = 0; i < 5; i++) {
+      const double yt = h * ak[i];
+      t3[i] += 1.2 * yt;
+      t4[i] -= (70.0 / 27.0) * yt;
+      t5[i] += (575.0 / 13824.0) * yt;
+      yout[i] += (250.0 / 621.0) * yt;
+      yerr[i] += ((250.0 / 621.0) - (18575.0 / 48384.0)) * yt;
+    }
+    geodesic(t3, ak);
+    for (int i = 0; i < 5; i++) {
+      const double yt = h * ak[i];
+      t4[i] += (35.0 / 27.0) * yt;
+      t5[i] += (44275.0 / 110592.0) * yt;
+      yout[i] += (125.0 / 594.0) * yt;
+      yerr[i] += ((125.0 / 594.0) - (13525.0 / 55296.0)) * yt;
+    }
+    geodesic(t4, ak);
+    for (int i = 0; i < 5; i++) {
+      const double yt = h * ak[i];
+      t5[i] += (253.0 / 4096.0) * yt;
+      yerr[i] -= (277.0 / 14336.0) * yt;
+    }
+    geodesic(t5, ak);
+    for (int i = 0; i < 5; i++) {
+      const double yt = h * ak[i];
+      yout[i] += (512.0 / 1771.0) * yt;
+      yerr[i] += ((512.0 / 1771.0) - 0.25) * yt;
+    }
+  }
+  // NextPosition + rkqs (WormHole.h:490-535, :618-683): at most 2000 shrinks
+  double next_position(double* y, const double* dydx, double htry) const {
+    const double escal = 1e11;
+    double yscal[5], ytemp[5], yerr[5];
+    for (int i = 0; i < 5; i++) yscal[i] = std::fabs(y[i]) + std::fabs(dydx[i] * htry) + 1.0e-3;
+    double h = htry, errmax = 0.0, htemp;
+    int loops = 0;
+    while (loops < 2000) {
+      rkstep(y, dydx, h, ytemp, yerr);
+      errmax = 0.0;
+      for (int i = 0; i < 5; i++) {
+        const double temp = std::fabs(yerr[i] / yscal[i]);
+        if (temp > errmax) errmax = temp;
+      }
+      errmax *= escal;
+      if (errmax <= 1.0) break;
+      htemp = 0.9 * h / std::sqrt(std::sqrt(errmax));
+      h *= 0.1;
+      if (h >= 0.0) {
+        if (htemp > h) h = htemp;
+      } else {
+        if (htemp < h) h = htemp;
+      }
+      loops++;
+    }
+    const double hnext = errmax > 1.89e-4 ? 0.9 * h * std::pow(errmax, -0.2) : 5.0 * h;
+    for (int i = 0; i < 5; i++) y[i] = ytemp[i];
+    return hnext;
+  }
+  V3 world(V3 q, double sgn) const {  // WorldAxisSystem (WormHole.h:430-447)
+    return mat_mul3(invMat, q) + (sgn >= 0 ? w.pos0 : w.pos1);
+  }
+};
+
+// intersect_scene__ (scene.cpp:735-925): 1 entity hit; 0 background 1
+// (l >= 0); 3 background 2 (l < 0); y: the final state with (theta, phi)
+// of the last polyline direction
+int worm_trace_one(const Scene& s, V3 org, V3 dir, Hit& hit, double* y, V3& dir2, int& cnt) {
+  const Wormhole& wh = s.worm;
+  WormRay kb(wh);
+  double rr, rth, rph;
+  cart_to_sph(dir.x, dir.y, dir.z, rr, rth, rph);
+  const double sign = length(org) > 1000000 ? -1.0 : 1.0;
+  kb.setup(org, sign);
+  double dydx[5];
+  kb.initial(y, rr, rth, rph);
+  cnt = 0;
+  const int cntMax = wh.max_steps;
+  V3 org2 = org, org1 = org;
+  dir2 = dir;
+  double h_dist = 0.5;
+  if (std::fabs(y[0]) < wh.a || kb.r_wh(y[0]) <= wh.Rho) h_dist = h_dist * 0.15;
+  double h_step = h_dist;
+  while (cntMax < 0 ? true : cnt < cntMax) {
+    if (std::fabs(y[0]) > 1.0e10 || std::fabs(kb.r_wh(y[0])) > 1.0e10 || !std::isfinite(y[0])) break;
+    if (intersect(s, org1, dir2, hit) && hit.distance < h_dist) return 1;
+    kb.geodesic(y, dydx);
+    if (std::fabs(h_step) < 1.0e-14) h_step = 1.0e-14;
+    h_step = kb.next_position(y, dydx, h_step);
+    if (h_step > h_dist) h_step = h_dist;
+    org1 = org2;
+    org2 = kb.world(sph_to_cart(kb.r_wh(y[0]), y[1], y[2]), y[0]);
+    dir2 = normalize(org2 - org1);
+    cnt++;
+  }
+  if (wh.usr_sign) y[0] = wh.usr_sign * y[0];
+  double dr, dth, dph;
+  cart_to_sph(dir2.x, dir2.y, dir2.z, dr, dth, dph);
+  y[1] = dth;
+  y[2] = dph;
+  return y[0] >= 0 ? 0 : 3;
+}
+
+// the colour of a ray that ended on a background (scene.cpp:860-920 +
+// SphericalMapping::Map, circle.h:92-105); no texture: BACKGROUND
+V3 worm_background(const Wormhole& wh, int side, const double* yy, const V3& bg) {
+  if (wh.tex[side].empty()) return bg;
+  double y1 = yy[1] * wh.map_coef[side][0] + wh.map_coef[side][1];
+  double y2 = yy[2] * wh.map_coef[side][2] + wh.map_coef[side][3];
+  y1 = std::fmod(y1, PI);
+  y2 = std::fmod(y2, 2.0 * PI);
+  double phi = y2, theta = y1;
+  if (phi < 0.0) phi += 2.0 * PI;
+  if (theta < 0.0) theta = -theta;
+  if (!(phi == phi) || !(theta == theta)) return V3();
+  int x = (int)(phi / (2.0 * PI) * wh.tex_w[side]);
+  x = x % wh.tex_w[side];
+  const int yv = ((int)(theta / PI * wh.tex_h[side])) % wh.tex_h[side];
+  const unsigned char* t = &wh.tex[side][3 * ((size_t)yv * wh.tex_w[side] + x)];
+  const double c = wh.tex_coef[side];
+  return V3(c * t[0] / 255.0, c * t[1] / 255.0, c * t[2] / 255.0);
+}
+
+bool worm_query(const Scene& s, V3 org, V3 dir, Hit& hit, V3& miss_color) {
+  double y[5];
+  V3 dir2;
+  int cnt;
+  const int st = worm_trace_one(s, org, dir, hit, y, dir2, cnt);
+  if (st == 1) return true;
+  miss_color = worm_background(s.worm, st == 0 ? 0 : 1, y, s.background);
+  return false;
+}
+
 bool kerr_query(const Scene& s, V3 org, V3 dir, Hit& hit, V3& miss_color) {
   double y[6];
   V3 dir2;
@@ -2939,6 +3301,33 @@ static void kerr_trace_ray(OracleScene* o, const double* rays, int64_t q, int32_
       hit_emission[3 * q + k] = em[k];
     }
   }
+}
+
+// One wormhole trace per ray (intersect_scene__, scene.cpp:735-925):
+// status 1 entity hit, 0 background 1, 3 background 2; the final state
+// (l, theta, phi of the last polyline direction), that direction, the steps
+// and the hit entity (-1: none).  Rays are independent: threads split them.
+int oracle_wormhole_trace(void* h, int threads, const double* rays, int64_t n, int32_t* status, double* final_y,
+                          double* exit_dir, int32_t* steps, int32_t* hit_entity) {
+  auto* o = static_cast<OracleScene*>(h);
+  if (!o || !rays || n < 0 || !o->s.worm.on) return PR_E_ARG;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(threads > 0 ? threads : 1)
+  for (int64_t q = 0; q < n; q++) {
+    const double* rr = rays + 6 * q;
+    Hit hit;
+    double y[5];
+    V3 dir2;
+    int cnt = 0;
+    const int st = worm_trace_one(o->s, V3(rr[0], rr[1], rr[2]), V3(rr[3], rr[4], rr[5]), hit, y, dir2, cnt);
+    status[q] = st;
+    steps[q] = cnt;
+    for (int k = 0; k < 3; k++) final_y[3 * q + k] = y[k];
+    exit_dir[3 * q] = dir2.x;
+    exit_dir[3 * q + 1] = dir2.y;
+    exit_dir[3 * q + 2] = dir2.z;
+    hit_entity[q] = st == 1 ? hit.object_id : -1;
+  }
+  return PR_OK;
 }
 
 int oracle_kerr_trace(void* h, const double* rays, int64_t n, int32_t* status, double* final_bl, double* exit_dir,

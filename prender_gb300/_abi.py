@@ -145,6 +145,26 @@ class pr_kerr(C.Structure):
     ]
 
 
+class pr_wormhole(C.Structure):
+    _fields_ = [
+        ("enabled", C.c_int32),
+        ("max_steps", C.c_int32),
+        ("in_", D3),
+        ("out", D3),
+        ("rho", C.c_double),
+        ("a", C.c_double),
+        ("w", C.c_double),
+        ("sign", C.c_int32),
+        ("pad0", C.c_int32),
+        ("camera", D3),
+        ("texture", C.c_void_p * 2),
+        ("texture_width", C.c_int32 * 2),
+        ("texture_height", C.c_int32 * 2),
+        ("map_coef", (C.c_double * 4) * 2),
+        ("texture_coef", C.c_double * 2),
+    ]
+
+
 class pr_scene_desc(C.Structure):
     _fields_ = [
         ("n_materials", C.c_int32),
@@ -158,6 +178,7 @@ class pr_scene_desc(C.Structure):
         ("environment_light", D3),
         ("medium", pr_medium),
         ("kerr", pr_kerr),
+        ("wormhole", pr_wormhole),
     ]
 
 

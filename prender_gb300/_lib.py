@@ -16,7 +16,7 @@ EXPORTS = (
     "pr_create", "pr_destroy", "pr_last_error", "pr_abi_version", "pr_abi_sizeof",
     "pr_scene_upload", "pr_scene_check", "pr_qbvh_info", "pr_qbvh_export", "pr_qbvh_build_host", "pr_render_bvh_export",
     "pr_first_hit", "pr_first_hit_dev", "pr_trace_fast", "pr_render", "pr_render_dev", "pr_render_dev_noalloc", "pr_last_render_stats",
-    "pr_kerr_trace", "pr_kerr_trace_dev", "pr_render_adjoint", "pr_render_adjoint_dev",
+    "pr_kerr_trace", "pr_kerr_trace_dev", "pr_wormhole_trace", "pr_wormhole_trace_dev", "pr_render_adjoint", "pr_render_adjoint_dev",
     "pr_last_kernel_times", "pr_kerr_sensitivity", "pr_kerr_sensitivity_adjoint", "pr_kerr_disk_shade", "pr_image_to_rgb8", "pr_image_to_rgb8_dev", "pr_image_to_rgbe", "pr_image_to_rgbe_dev", "pr_autotune_wavefront",
     "pr_scene_create", "pr_scene_release", "pr_render_batch",
     "pr_scene_file_load", "pr_scene_file_desc", "pr_scene_file_camera", "pr_scene_file_warnings", "pr_scene_file_free",
@@ -64,6 +64,8 @@ def load():
     L.pr_last_render_stats.argtypes = [vp, C.POINTER(A.pr_render_stats)]
     L.pr_kerr_trace.argtypes = [vp, vp, i64, vp, vp, vp, vp, vp, vp]
     L.pr_kerr_trace_dev.argtypes = [vp, vp, i64, vp, vp, vp, vp, vp, vp]
+    L.pr_wormhole_trace.argtypes = [vp, vp, i64, vp, vp, vp, vp, vp]
+    L.pr_wormhole_trace_dev.argtypes = [vp, vp, i64, vp, vp, vp, vp, vp]
     L.pr_render_adjoint.argtypes = [vp, vp, vp, vp, C.c_uint64, vp, vp, vp]
     L.pr_render_adjoint_dev.argtypes = [vp, vp, vp, vp, C.c_uint64, vp, vp]
     L.pr_last_kernel_times.argtypes = [vp, vp, vp, C.c_int]

@@ -17,7 +17,7 @@ LIB = os.path.join(OUT_DIR, "libprender_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # per-file flags: the Kerr tracer keeps every FP64 multiply and add rounded
 # on its own (no FMA contraction), the operation order of the reference
-EXTRA = {"kerr.cu": ["-fmad=false"]}
+EXTRA = {"kerr.cu": ["-fmad=false"], "wormhole.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:

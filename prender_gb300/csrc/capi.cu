@@ -15,6 +15,7 @@
 #include "../../include/prender_gpu.h"
 #include "adjoint.h"
 #include "kerr.h"
+#include "wormhole.h"
 #include "pr_internal.h"
 #include "render_kernels.h"
 #include "scene_build.h"
@@ -205,7 +206,11 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   if (!h.bump_texels.empty()) PR_CUDA(c, upload(o.bump_texels, h.bump_texels, c->stream));
   PR_CUDA(c, upload(o.kerr_tex, h.kerr_texture, c->stream));
   PR_CUDA(c, upload(o.kerr_disk_tex, h.kerr_disk_texture, c->stream));
+  for (int k = 0; k < 2; k++)
+    if (!h.worm_tex[k].empty()) PR_CUDA(c, upload(o.worm_tex[k], h.worm_tex[k], c->stream));
   PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  o.worm = h.worm;
+  for (int k = 0; k < 2; k++) o.worm.tex[k] = h.worm_tex[k].empty() ? nullptr : (const unsigned char*)o.worm_tex[k].p;
   o.kerr = h.kerr;
   o.kerr.texture = h.kerr_texture.empty() ? nullptr : (const unsigned char*)o.kerr_tex.p;
   o.kerr.disk_tex = h.kerr_disk_texture.empty() ? nullptr : (const uchar4*)o.kerr_disk_tex.p;
@@ -494,7 +499,9 @@ int pr::prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* 
                 "UVPlane axes randomPoint reads, circle.h:110-134); render it without next-event estimation");
   if (sc.kerr.enabled && (p->nee || (p->media && sc.host.medium.on)))
     return fail(c, PR_E_UNSUPPORTED, "Kerr scenes render without next-event estimation and media");
-  if (sc.dev.has_sss && sc.kerr.enabled)
+  if (sc.worm.enabled && (p->nee || (p->media && sc.host.medium.on)))
+    return fail(c, PR_E_UNSUPPORTED, "wormhole scenes render without next-event estimation and media");
+  if (sc.dev.has_sss && (sc.kerr.enabled || sc.worm.enabled))
     return fail(c, PR_E_UNSUPPORTED, "subsurface (dipole) materials render in straight-ray scenes only");
   memset(&g, 0, sizeof(g));
   double dir[3] = {cam->dir[0], cam->dir[1], cam->dir[2]};
@@ -729,12 +736,16 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
   PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-  const bool kerr = c->cur.kerr.enabled != 0;
-  if (kerr) {
-    // every scene query of a Kerr scene is a geodesic trace: one form only
+  const bool kerr = c->cur.kerr.enabled != 0, worm = c->cur.worm.enabled != 0;
+  if (kerr || worm) {
+    // every scene query of a Kerr or wormhole scene is a geodesic trace: one form only
     PR_CUDA(c, c->partial.ensure(sizeof(float) * n3 * (size_t)g.chunks));
-    PR_CUDA(c, launch_kerr_render(c->cur.dev, c->cur.kerr, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
-                                  (unsigned long long*)c->counters.p, c->stream));
+    if (kerr)
+      PR_CUDA(c, launch_kerr_render(c->cur.dev, c->cur.kerr, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
+                                    (unsigned long long*)c->counters.p, c->stream));
+    else
+      PR_CUDA(c, launch_worm_render(c->cur.dev, c->cur.worm, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
+                                    (unsigned long long*)c->counters.p, c->stream));
     PR_CUDA(c, launch_reduce((const float*)c->partial.p, rgb_dev, (int)n3, g.chunks, accumulate, c->stream));
   } else if (p->mode == PR_MODE_WAVEFRONT) {
     st = render_wavefront(c, g, rgb_dev, accumulate);
@@ -751,7 +762,7 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   st = check_device_errors(c);
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-  const bool wf = p->mode == PR_MODE_WAVEFRONT && !kerr;
+  const bool wf = p->mode == PR_MODE_WAVEFRONT && !kerr && !worm;
   const uint64_t paths = wf ? (uint64_t)g.spp * g.width * g.height : cnt[0];
   // wavefront: reset per pass + 4 per iteration + resolve; megakernel: kernel + reduce
   const uint64_t launches = wf ? 4 * cnt[5] + c->wf_passes + 1 : 2;
@@ -783,7 +794,8 @@ int pr_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, float*
 
 static int adjoint_checks(pr_ctx* c, const pr_render_params* p) {
   if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
-  if (c->cur.kerr.enabled) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass traces straight rays only");
+  if (c->cur.kerr.enabled || c->cur.worm.enabled)
+    return fail(c, PR_E_UNSUPPORTED, "the adjoint pass traces straight rays only");
   if (p && p->media && c->cur.host.medium.on) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover media");
   if (c->cur.dev.has_sss) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover subsurface materials");
   if (c->cur.dev.n_point_lights > 0)
@@ -878,7 +890,8 @@ int pr_autotune_wavefront(pr_ctx* c, const pr_camera* cam, const pr_render_param
   if (!c) return PR_E_ARG;
   if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
   if (!cam || !p) return fail(c, PR_E_ARG, "null camera or parameters");
-  if (c->cur.kerr.enabled) return fail(c, PR_E_UNSUPPORTED, "Kerr scenes do not use the wavefront form");
+  if (c->cur.kerr.enabled || c->cur.worm.enabled)
+    return fail(c, PR_E_UNSUPPORTED, "Kerr and wormhole scenes do not use the wavefront form");
   const unsigned int cand_slots[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22};
   const unsigned int cand_bps[] = {kTraceBlocksPerSM / 2, kTraceBlocksPerSM, 2 * kTraceBlocksPerSM};
   // a tuning frame of the caller's scene with enough camera samples to keep
@@ -997,6 +1010,62 @@ int pr_kerr_trace(pr_ctx* c, const double* rays, int64_t n, int32_t* status, dou
   if (steps) PR_CUDA(c, cudaMemcpyAsync(steps, c->k_steps.p, 4 * sn, cudaMemcpyDeviceToHost, c->stream));
   if (hit_entity) PR_CUDA(c, cudaMemcpyAsync(hit_entity, c->k_ent.p, 4 * sn, cudaMemcpyDeviceToHost, c->stream));
   if (hit_t) PR_CUDA(c, cudaMemcpyAsync(hit_t, c->k_t.p, 8 * sn, cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PR_OK;
+}
+
+int pr_wormhole_trace_dev(pr_ctx* c, const double* rays, int64_t n, int32_t* status, double* final_y,
+                          double* exit_dir, int32_t* steps, int32_t* hit_entity) {
+  if (!c) return PR_E_ARG;
+  if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
+  if (!c->cur.worm.enabled) return fail(c, PR_E_SCENE, "the scene has no wormhole");
+  if (n < 0 || (n > 0 && !rays)) return fail(c, PR_E_ARG, "bad ray buffer");
+  if (n > (int64_t)1 << 31) return fail(c, PR_E_ARG, "at most 2^31 rays per call");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
+  PR_CUDA(c, cudaMemsetAsync(c->errword.p, 0, 4, c->stream));
+  PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  WormOut o{status, final_y, exit_dir, steps, hit_entity};
+  PR_CUDA(c, launch_worm_trace(c->cur.dev, c->cur.worm, rays, n, o, (uint32_t*)c->errword.p,
+                               (unsigned long long*)c->counters.p, c->stream));
+  PR_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  unsigned long long cnt[16];
+  PR_CUDA(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  int st = check_device_errors(c);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  // as pr_kerr_trace: paths = rays, segments = segment scene tests,
+  // nodes_visited = accepted steps, tri_tests = RK45 attempts
+  c->stats = pr_render_stats{cnt[0], cnt[3], cnt[1], cnt[2], ms, n > 0 ? 1ull : 0ull};
+  return st;
+}
+
+int pr_wormhole_trace(pr_ctx* c, const double* rays, int64_t n, int32_t* status, double* final_y, double* exit_dir,
+                      int32_t* steps, int32_t* hit_entity) {
+  if (!c) return PR_E_ARG;
+  if (n < 0 || (n > 0 && !rays)) return fail(c, PR_E_ARG, "bad ray buffer");
+  if (n > (int64_t)1 << 31) return fail(c, PR_E_ARG, "at most 2^31 rays per call");
+  PR_CUDA(c, cudaSetDevice(c->device));
+  cudaGetLastError();  // an error left by an unrelated earlier call is not this call's
+  const size_t un = (size_t)std::max<int64_t>(n, 1);
+  PR_CUDA(c, c->rays.ensure(48 * un));
+  PR_CUDA(c, c->k_status.ensure(4 * un));
+  PR_CUDA(c, c->k_bl.ensure(24 * un));
+  PR_CUDA(c, c->k_dir.ensure(24 * un));
+  PR_CUDA(c, c->k_steps.ensure(4 * un));
+  PR_CUDA(c, c->k_ent.ensure(4 * un));
+  if (n > 0) PR_CUDA(c, cudaMemcpyAsync(c->rays.p, rays, 48 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  int st = pr_wormhole_trace_dev(c, (const double*)c->rays.p, n, status ? (int32_t*)c->k_status.p : nullptr,
+                                 final_y ? (double*)c->k_bl.p : nullptr, exit_dir ? (double*)c->k_dir.p : nullptr,
+                                 steps ? (int32_t*)c->k_steps.p : nullptr, hit_entity ? (int32_t*)c->k_ent.p : nullptr);
+  if (st != PR_OK || n == 0) return st;
+  const size_t sn = (size_t)n;
+  if (status) PR_CUDA(c, cudaMemcpyAsync(status, c->k_status.p, 4 * sn, cudaMemcpyDeviceToHost, c->stream));
+  if (final_y) PR_CUDA(c, cudaMemcpyAsync(final_y, c->k_bl.p, 24 * sn, cudaMemcpyDeviceToHost, c->stream));
+  if (exit_dir) PR_CUDA(c, cudaMemcpyAsync(exit_dir, c->k_dir.p, 24 * sn, cudaMemcpyDeviceToHost, c->stream));
+  if (steps) PR_CUDA(c, cudaMemcpyAsync(steps, c->k_steps.p, 4 * sn, cudaMemcpyDeviceToHost, c->stream));
+  if (hit_entity) PR_CUDA(c, cudaMemcpyAsync(hit_entity, c->k_ent.p, 4 * sn, cudaMemcpyDeviceToHost, c->stream));
   PR_CUDA(c, cudaStreamSynchronize(c->stream));
   return PR_OK;
 }
@@ -1187,7 +1256,8 @@ int pr_render_batch(pr_ctx* c, int n, const pr_job* jobs) {
   // after another on the context's stream, after the graph of the others
   std::vector<char> wf_job((size_t)n, 0);
   for (int j = 0; j < n; j++)
-    wf_job[j] = jobs[j].params.mode == PR_MODE_WAVEFRONT && !jobs[j].scene->data.kerr.enabled;
+    wf_job[j] = jobs[j].params.mode == PR_MODE_WAVEFRONT && !jobs[j].scene->data.kerr.enabled &&
+                !jobs[j].scene->data.worm.enabled;
   PR_CUDA(c, c->batch_partial.ensure(sizeof(float) * std::max<size_t>(off[n], 1)));
   const int n_streams = std::min(n, 16);
   while ((int)c->batch_streams.size() < n_streams) {
@@ -1217,6 +1287,9 @@ int pr_render_batch(pr_ctx* c, int n, const pr_job* jobs) {
     const int n3 = cfg[j].width * cfg[j].height * 3;
     if (sc.kerr.enabled)
       e = launch_kerr_render(sc.dev, sc.kerr, cfg[j], part + off[j], (uint32_t*)c->errword.p,
+                             (unsigned long long*)c->counters.p, st);
+    else if (sc.worm.enabled)
+      e = launch_worm_render(sc.dev, sc.worm, cfg[j], part + off[j], (uint32_t*)c->errword.p,
                              (unsigned long long*)c->counters.p, st);
     else
       e = launch_megakernel(sc.dev, cfg[j], part + off[j], (uint32_t*)c->errword.p,

@@ -183,6 +183,25 @@ struct GMedium {
   int32_t on;
 };
 
+// WormHole state shared by every ray of a scene (WormHole.h:126-540 as
+// SceneEnv builds it, scene_env.h:2100-2145); mat / inv: the frame Setup
+// builds from the camera position for rays at mouth 0 ([0]) and mouth 1
+// ([1]) and its cofactor inverse, row major 4 x 4 (computed on the host)
+struct GWorm {
+  int32_t enabled;
+  int32_t max_steps;       // geodesics_max_length
+  double pos[2][3];        // position0 ('in'), position1 ('out')
+  double Rho, a, M;        // throat radius, half length, lensing (M = W / 1.42953)
+  int32_t usr_sign;        // 'sign'
+  int32_t pad;
+  double mat[2][16];
+  double inv[2][16];
+  const unsigned char* tex[2];  // backgrounds, RGB8 rows as cell(y, x) reads them; null = none
+  int32_t tex_w[2], tex_h[2];
+  double map_coef[2][4];
+  double tex_coef[2];
+};
+
 // KerrBlackHole state shared by every ray of a scene (KerrBlackHole.h:86-151;
 // M = 1 as SceneEnv constructs it, scene_env.h:2067)
 struct GKerr {

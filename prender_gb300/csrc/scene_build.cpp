@@ -353,6 +353,86 @@ int complete_exact_qbvh(HostScene& hs, std::string& err) {
   return PR_OK;
 }
 
+// WormHole as SceneEnv builds it (scene_env.h:2100-2145, WormHole.h:126-170)
+// and the two frames Setup makes (WormHole.h:321-395): a ray starting at
+// mouth m (the 'in' mouth unless it starts more than 1e6 from the origin)
+// turns into the basis whose rows are X = the unit vector from the mouth to
+// the camera, Y = unit(z x X) (y x X when that vanishes), Z = unit(X x Y);
+// its inverse is InvertMatrix_'s cofactor inverse, whose terms for a matrix
+// without translation reduce to the 3 x 3 cofactors below (a determinant
+// below 1e-16 leaves the identity, as the class does).
+static int build_wormhole(const pr_scene_desc* d, HostScene& hs, std::string& err) {
+  hs.worm = GWorm{};
+  for (auto& t : hs.worm_tex) t.clear();
+  const pr_wormhole& pw = d->wormhole;
+  if (!pw.enabled) return PR_OK;
+  if (d->kerr.enabled) { err = "a scene holds a black hole or a wormhole, not both"; return PR_E_UNSUPPORTED; }
+  if (pw.max_steps <= 0 || pw.max_steps > 10000000) {
+    err = "geodesics_max_length must be in 1..1e7 (an unbounded trace is not run on the GPU)";
+    return PR_E_ARG;
+  }
+  if (!(pw.rho > 0.0) || !(pw.w > 0.0) || !std::isfinite(pw.a)) {
+    err = "the wormhole needs Rho > 0, W > 0 and a finite a";
+    return PR_E_ARG;
+  }
+  GWorm& w = hs.worm;
+  w.enabled = 1;
+  w.max_steps = pw.max_steps;
+  for (int k = 0; k < 3; k++) {
+    w.pos[0][k] = pw.in[k];
+    w.pos[1][k] = pw.out[k];
+  }
+  w.Rho = pw.rho;
+  w.a = std::fabs(pw.a);
+  w.M = pw.w / 1.42953;
+  w.usr_sign = pw.sign;
+  const D3 cam = mk(pw.camera);
+  for (int m = 0; m < 2; m++) {
+    const D3 X = unit(sub(cam, mk(w.pos[m])));
+    D3 Y = unit(cross(D3{0.0, 0.0, 1.0}, X));
+    if (len(Y) < 1.0e-16) Y = unit(cross(D3{0.0, 1.0, 0.0}, X));
+    const D3 Z = unit(cross(X, Y));
+    double* A = w.mat[m];
+    double* B = w.inv[m];
+    for (int i = 0; i < 16; i++) A[i] = B[i] = (i % 5 == 0) ? 1.0 : 0.0;
+    const D3 rows[3] = {X, Y, Z};
+    for (int r = 0; r < 3; r++) {
+      A[4 * r] = rows[r].x;
+      A[4 * r + 1] = rows[r].y;
+      A[4 * r + 2] = rows[r].z;
+    }
+    double c[11];
+    c[0] = A[5] * A[10] - A[9] * A[6];
+    c[4] = A[8] * A[6] - A[4] * A[10];
+    c[8] = A[4] * A[9] - A[8] * A[5];
+    c[1] = A[9] * A[2] - A[1] * A[10];
+    c[5] = A[0] * A[10] - A[8] * A[2];
+    c[9] = A[8] * A[1] - A[0] * A[9];
+    c[2] = A[1] * A[6] - A[5] * A[2];
+    c[6] = A[4] * A[2] - A[0] * A[6];
+    c[10] = A[0] * A[5] - A[4] * A[1];
+    double det = (A[0] * c[0] + A[1] * c[4]) + A[2] * c[8];
+    if (!(det < 1.0e-16)) {
+      det = 1.0 / det;
+      for (int i : {0, 1, 2, 4, 5, 6, 8, 9, 10}) B[i] = c[i] * det;
+    }
+  }
+  for (int k = 0; k < 2; k++) {
+    for (int q = 0; q < 4; q++) w.map_coef[k][q] = pw.map_coef[k][q];
+    w.tex_coef[k] = pw.texture_coef[k];
+    if (pw.texture[k]) {
+      if (pw.texture_width[k] <= 0 || pw.texture_height[k] <= 0) {
+        err = "wormhole background texture size must be positive";
+        return PR_E_ARG;
+      }
+      hs.worm_tex[k].assign(pw.texture[k], pw.texture[k] + 3 * (size_t)pw.texture_width[k] * pw.texture_height[k]);
+      w.tex_w[k] = pw.texture_width[k];
+      w.tex_h[k] = pw.texture_height[k];
+    }
+  }
+  return PR_OK;
+}
+
 int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, const SceneBuildOptions& opt) {
   hs = HostScene();
   if (!d || d->n_entities < 0 || d->n_materials < 0 || d->n_meshes < 0) { err = "null or negative scene sizes"; return PR_E_ARG; }
@@ -583,16 +663,16 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
       err = "textures and IBL images are read on spheres, hemispheres and uvplanes only";
       return PR_E_UNSUPPORTED;
     }
-    if (textured && (hs.mats[pe.material].sss || d->kerr.enabled)) {
-      err = "textures on subsurface materials or under a black hole are not on this path";
+    if (textured && (hs.mats[pe.material].sss || d->kerr.enabled || d->wormhole.enabled)) {
+      err = "textures on subsurface materials or in a black hole or wormhole scene are not on this path";
       return PR_E_UNSUPPORTED;
     }
     if (pe.type == PR_ENT_SPHERE) {
       for (int k = 0; k < 3; k++) g.p[k] = pe.p[k];
       g.radius = pe.radius;
       g.hemisphere = pe.hemisphere ? 1 : 0;
-      if (g.hemisphere && (is_light(pm) || d->kerr.enabled)) {
-        err = "hemispheres that emit, or under a black hole, are not on this path";
+      if (g.hemisphere && (is_light(pm) || d->kerr.enabled || d->wormhole.enabled)) {
+        err = "hemispheres that emit, or in a black hole or wormhole scene, are not on this path";
         return PR_E_UNSUPPORTED;
       }
       g.area = 12.5663706143591729538505735331180115 * pe.radius * pe.radius;  // PS_FORPI r^2
@@ -672,7 +752,7 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
       else face_normals(pm_.vertices, pm_.faces, pm_.n_faces, fn);
       g.face_base = (int32_t)(hs.fnorm.size() / 3);
       g.n_faces = pm_.n_faces;
-      if (big && opt.defer_exact && !d->kerr.enabled) {
+      if (big && opt.defer_exact && !d->kerr.enabled && !d->wormhole.enabled) {
         g.node_base = -1;
         g.slot_base = -1;
         HostScene::DeferredMesh dm;
@@ -810,10 +890,10 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
   std::sort(lights.begin(), lights.end(), [](const L& a, const L& b) { return a.power > b.power; });
   if ((int)lights.size() > kMaxLights) { err = "too many lights"; return PR_E_ARG; }
   for (const L& l : lights) hs.lights.push_back(l.g);
-  if (d->kerr.enabled)
+  if (d->kerr.enabled || d->wormhole.enabled)
     for (const GLight& g : hs.lights)
       if (g.kind != PR_LIGHT_AREA) {
-        err = "parallel, spot and infinity lights are sampled along straight rays only (no black hole)";
+        err = "parallel, spot and infinity lights are sampled along straight rays only (no black hole or wormhole)";
         return PR_E_UNSUPPORTED;
       }
   hs.scene_scale = (float)ext;
@@ -920,7 +1000,7 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
       e.kerr_disk = 1;
     }
   }
-  return PR_OK;
+  return build_wormhole(d, hs, err);
 }
 
 }  // namespace pr

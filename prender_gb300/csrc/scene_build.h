@@ -48,6 +48,8 @@ struct HostScene {
   GKerr kerr{};
   std::vector<unsigned char> kerr_texture;
   std::vector<unsigned char> kerr_disk_texture;  // RGBA8
+  GWorm worm{};
+  std::vector<unsigned char> worm_tex[2];  // wormhole backgrounds (RGB8)
   bool disk_light = false;  // an emitting disk is registered as a light
   // meshes whose render tree the caller builds (pointers into the scene
   // description: valid during the upload call only)

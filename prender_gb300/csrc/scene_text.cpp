@@ -5,7 +5,8 @@
 // The reader follows the reference's line rules: an upper-case setting's
 // keyword on one line and its value on the next; one '#' comment line
 // skipped before a keyword (getLine, scene_env.h:141-149) and '#' lines
-// skipped inside blocks; OBJECT and BLACKHOLE blocks end at an empty line.
+// skipped inside blocks; OBJECT, BLACKHOLE and WORMHOLE blocks end at an
+// empty line.
 // Every value the reference reads through its expression evaluator is read
 // through the same rules here (scene_expr.h: VAR variables, arithmetic,
 // functions); values it reads with sscanf are read with sscanf.
@@ -14,10 +15,11 @@
 // uvplanes, disks, OBJ meshes; diffuse / specular / glass / Ward / Phong /
 // subsurface materials; rotation / translate / scale of spheres and meshes;
 // the global medium; TARGET_POS and CAMERA_MATRIX; the black hole with its
-// background and accretion-disk textures).  A keyword that changes the
-// image through a feature this library does not render (other lights,
-// object textures, transformed uvplanes and disks, lens, MLT / ERPT,
-// wormholes, dispersion ...) is refused with an error naming the line, so
+// background and accretion-disk textures; the wormhole with its two
+// backgrounds; spot, parallel and infinity lights; textures, IBL images and
+// bump maps).  A keyword that changes the image through a feature this
+// library does not render (transformed uvplanes and disks, lens, MLT / ERPT,
+// dispersion ...) is refused with an error naming the line, so
 // that no scene renders silently different; settings that do not change
 // the image (THREAD, OUTPUT, ...) are skipped.  The reference's overrides
 // of settings by environment variables (SAMPLING, IMAGE_X, USE_BSSRDF ...)
@@ -47,7 +49,7 @@ struct pr_scene_file {
   std::vector<std::vector<int32_t>> faces;
   std::vector<std::vector<float>> fnormals;  // empty: the loader's rule at upload
   std::vector<pr_mesh> meshes;
-  std::vector<uint8_t> bg_tex, disk_tex;
+  std::vector<uint8_t> bg_tex, disk_tex, worm_tex[2];
   // per material: texture / IBL images (pointers set when the desc is made)
   std::vector<std::vector<uint8_t>> tex8, ibl8, bump8;
   std::vector<std::vector<float>> iblf;
@@ -553,6 +555,16 @@ struct BlackHole {
   std::string bg_texture, disk_texture;
 };
 
+// the WORMHOLE block's settings with SceneEnv::Default's values
+// (scene_env.h:262-300, :767-856)
+struct Worm {
+  bool exists = false, pos_set = false;
+  double in[3] = {0, 0, 0}, out[3] = {0, 0, 0};
+  double rho = 1.3, a = 0.5, w = 0.05, sign = 0.0, dist = 10000.0;
+  double map_coef[2][4] = {{1.0, 0.0, 1.0, 0.0}, {1.0, 0.0, 1.0, 0.0}}, coef[2] = {1.0, 1.0};
+  std::string texture[2];
+};
+
 class Loader {
  public:
   Loader(pr_scene_file& S, const std::string& path) : S_(S), path_(path), sdir_(dir_of(path)), r_(path) {}
@@ -584,7 +596,8 @@ class Loader {
   double sensor_response_ = 1.0, doppler_ = 0.0;
   double background_[3] = {0, 0, 0}, envlight_[3] = {0, 0, 0};
   pr_medium gm_ = default_medium();
-  BlackHole bh_;
+  BlackHole bh_;  // bh_.steps is the one geodesics_max_length of both blocks
+  Worm wh_;
   int blackhole_disk_ = 0;  // a 'blackhole_disk' line holds for every later disk (scene_env.h:1177-1181)
 
   void refuse(const std::string& what) { fail("not rendered here: '" + what + "'"); }
@@ -620,7 +633,7 @@ class Loader {
       } else if (starts(line, "BLACKHOLE")) {
         read_black_hole(line);
       } else if (starts(line, "WORMHOLE")) {
-        refuse(line);
+        read_wormhole();
       } else if (background_line(line)) {
       } else {
         S_.warnings += "skipped: " + line + "\n";
@@ -738,6 +751,40 @@ class Loader {
           S_.warnings += "only the first accretion_disk_texture is read: " + b + "\n";
       } else if (!tokens(b).empty()) {
         S_.warnings += "skipped in BLACKHOLE: " + b + "\n";
+      }
+    }
+  }
+
+  void read_wormhole() {
+    wh_.exists = true;
+    std::string b;
+    while (r_.raw(b) && !b.empty()) {
+      if (b[0] == '#') continue;
+      if (starts(b, "in ") || starts(b, "out ")) {
+        const std::vector<double> v = num_.many(after_key(b), 3);
+        for (int i = 0; i < 3; i++) (starts(b, "in ") ? wh_.in : wh_.out)[i] = v[i];
+        wh_.pos_set = true;
+      } else if (starts(b, "Rho ")) {
+        wh_.rho = num_.many(after_key(b), 1)[0];
+      } else if (starts(b, "a ")) {
+        wh_.a = num_.many(after_key(b), 1)[0];
+      } else if (starts(b, "W ")) {
+        wh_.w = num_.many(after_key(b), 1)[0];
+      } else if (starts(b, "sign ")) {
+        wh_.sign = num_.many(after_key(b), 1)[0];
+      } else if (starts(b, "dist ")) {
+        wh_.dist = num_.many(after_key(b), 1)[0];
+      } else if (starts(b, "geodesics_max_length ")) {
+        bh_.steps = num_.many(after_key(b), 1)[0];
+      } else if (starts(b, "background_texture1 ") || starts(b, "background_texture2 ")) {
+        wh_.texture[b[18] == '1' ? 0 : 1] = b.substr(20);
+      } else if (starts(b, "map_coef1 ") || starts(b, "map_coef2 ")) {
+        const std::vector<double> v = num_.many(b.substr(10), 4);
+        for (int i = 0; i < 4; i++) wh_.map_coef[b[8] == '1' ? 0 : 1][i] = v[i];
+      } else if (starts(b, "coef1 ") || starts(b, "coef2 ")) {
+        wh_.coef[b[4] == '1' ? 0 : 1] = num_.many(b.substr(6), 1)[0];
+      } else if (!tokens(b).empty()) {
+        S_.warnings += "skipped in WORMHOLE: " + b + "\n";
       }
     }
   }
@@ -1134,6 +1181,36 @@ class Loader {
       d.environment_light[i] = envlight_[i];
     }
     d.medium = gm_;
+    pr_wormhole& ww = d.wormhole;
+    memset(&ww, 0, sizeof(ww));
+    ww.texture_coef[0] = ww.texture_coef[1] = 1.0;
+    if (wh_.exists) {
+      // without a mouth position 'in' sits dist along the camera direction
+      // (scene_env.h:2100-2110); the frame is built from CAMERA_POS
+      if (!wh_.pos_set)
+        for (int i = 0; i < 3; i++) wh_.in[i] = cpos_[i] + dir[i] * wh_.dist;
+      ww.enabled = 1;
+      ww.max_steps = (int32_t)bh_.steps;
+      for (int i = 0; i < 3; i++) {
+        ww.in[i] = wh_.in[i];
+        ww.out[i] = wh_.out[i];
+        ww.camera[i] = cpos_[i];
+      }
+      ww.rho = wh_.rho;
+      ww.a = wh_.a;
+      ww.w = wh_.w;
+      ww.sign = (int32_t)wh_.sign;
+      for (int k = 0; k < 2; k++) {
+        for (int i = 0; i < 4; i++) ww.map_coef[k][i] = wh_.map_coef[k][i];
+        ww.texture_coef[k] = wh_.coef[k];
+        if (wh_.texture[k].empty()) continue;
+        int w = 0, h = 0;
+        read_bmp(resolve(wh_.texture[k], sdir_), 3, S_.worm_tex[k], w, h);
+        ww.texture[k] = S_.worm_tex[k].data();
+        ww.texture_width[k] = w;
+        ww.texture_height[k] = h;
+      }
+    }
     pr_kerr& kk = d.kerr;
     memset(&kk, 0, sizeof(kk));
     kk.texture_coef = 1.0;

@@ -198,6 +198,17 @@ class Context:
                                          _p(out["hit_t"])))
         return out
 
+    def wormhole_trace(self, rays: np.ndarray) -> dict:
+        """The wormhole branch of intersect_scene__ per ray (FP64 geodesics);
+        status 1 entity hit, 0 background 1, 3 background 2."""
+        rays = np.ascontiguousarray(rays, dtype=np.float64)
+        n = rays.shape[0]
+        out = dict(status=np.empty(n, np.int32), final_y=np.empty((n, 3)), exit_dir=np.empty((n, 3)),
+                   steps=np.empty(n, np.int32), hit_entity=np.empty(n, np.int32))
+        self._check(self.L.pr_wormhole_trace(self.h, _p(rays), n, _p(out["status"]), _p(out["final_y"]),
+                                             _p(out["exit_dir"]), _p(out["steps"]), _p(out["hit_entity"])))
+        return out
+
     def kerr_sensitivity(self, rays: np.ndarray, basis: np.ndarray | None = None,
                          cotangent: np.ndarray | None = None) -> dict:
         """Ray-bundle Jacobian of the Kerr map: d(exit direction)/d(s, t)

@@ -369,6 +369,30 @@ class SceneDesc:
                 k.disk_texture = dt.ctypes.data
                 k.disk_texture_height, k.disk_texture_width = dt.shape[0], dt.shape[1]
         d.kerr = k
+        wm = A.pr_wormhole()
+        if scene.wormhole is not None:
+            w = scene.wormhole
+            wm.enabled = 1
+            wm.max_steps = int(w["max_steps"])
+            wm.in_[:] = list(w["in"])
+            wm.out[:] = list(w["out"])
+            wm.rho, wm.a, wm.w = w["rho"], w["a"], w["w"]
+            wm.sign = int(w["sign"])
+            cam_pos = w.get("camera") or scene.camera.position
+            wm.camera[:] = [float(x) for x in cam_pos]
+            for k2 in range(2):
+                tex = w["textures"][k2]
+                if tex is not None:
+                    tex = np.ascontiguousarray(tex, dtype=np.uint8)
+                    if tex.ndim != 3 or tex.shape[2] != 3:
+                        raise ValueError("wormhole background must be (H, W, 3) uint8")
+                    self._keep.append(tex)
+                    wm.texture[k2] = tex.ctypes.data
+                    wm.texture_height[k2], wm.texture_width[k2] = tex.shape[0], tex.shape[1]
+                for q in range(4):
+                    wm.map_coef[k2][q] = w["map_coef"][k2][q]
+                wm.texture_coef[k2] = w["texture_coef"][k2]
+        d.wormhole = wm
         self.desc = d
 
     def ptr(self):
@@ -385,6 +409,7 @@ class Scene:
     participating_media: int = 0
     medium: Medium = field(default_factory=Medium)
     kerr: Optional[dict] = None
+    wormhole: Optional[dict] = None
     camera: Camera = field(default_factory=Camera)
     settings: RenderSettings = field(default_factory=RenderSettings)
 
@@ -474,6 +499,22 @@ class Scene:
             e.light_dir_text = tuple(float(x) for x in direction)
             e.light_dir = tuple(_normalize_ref(e.light_dir_text))
 
+    def set_wormhole(self, in_pos, out_pos=(0.0, 0.0, 0.0), rho: float = 1.3, a: float = 0.5, w: float = 0.05,
+                     max_steps: int = 10000, sign: int = 0, textures=(None, None),
+                     map_coef=((1.0, 0.0, 1.0, 0.0), (1.0, 0.0, 1.0, 0.0)), texture_coef=(1.0, 1.0),
+                     camera=None) -> None:
+        """A wormhole ('WORMHOLE' block, scene_env.h:767-856): mouths in / out,
+        throat radius rho, length 2a, lensing width w; textures are the two
+        backgrounds as (H, W, 3) uint8 arrays indexed [y, x] as
+        BitMap::cell(y, x) reads them; camera: the camera position its frame
+        is built from (default: the scene camera's)"""
+        self.wormhole = {"in": tuple(float(x) for x in in_pos), "out": tuple(float(x) for x in out_pos),
+                         "rho": float(rho), "a": float(a), "w": float(w), "max_steps": int(max_steps),
+                         "sign": int(sign), "textures": tuple(textures),
+                         "map_coef": tuple(tuple(float(x) for x in m) for m in map_coef),
+                         "texture_coef": tuple(float(x) for x in texture_coef),
+                         "camera": None if camera is None else tuple(float(x) for x in camera)}
+
     def add_mesh(self, vertices, faces, material: Material, normal_inverse: int = 1) -> int:
         self.meshes.append(Mesh(vertices, faces))
         self.entities.append(Entity(A.PR_ENT_POLYGON, self._mat(material), normal_inverse,
@@ -543,6 +584,21 @@ class Scene:
                 out += ["use_accretion_disk_temperature", "1", ""]
             if k.get("doppler_effect", 0.0):
                 out += ["color_doppler_factor_effect", _fmt(k["doppler_effect"]), ""]
+        if self.wormhole is not None:
+            w = self.wormhole
+            if w.get("camera") is not None and tuple(w["camera"]) != tuple(float(x) for x in cam.position):
+                raise ValueError("the reference builds the wormhole's frame from CAMERA_POS")
+            out += ["WORMHOLE", f"in {f3(w['in'])}", f"out {f3(w['out'])}", f"Rho {_fmt(w['rho'])}",
+                    f"a {_fmt(w['a'])}", f"W {_fmt(w['w'])}", f"sign {int(w['sign'])}",
+                    f"geodesics_max_length {int(w['max_steps'])}"]
+            for k2 in range(2):
+                if w["textures"][k2] is not None:
+                    tp = os.path.join(directory, f"worm_bg{k2 + 1}.bmp")
+                    _write_bmp24(tp, np.asarray(w["textures"][k2], dtype=np.uint8))
+                    out.append(f"background_texture{k2 + 1} {tp}")
+                out.append(f"map_coef{k2 + 1} {f3(w['map_coef'][k2])}")
+                out.append(f"coef{k2 + 1} {_fmt(w['texture_coef'][k2])}")
+            out.append("")
         md = self.medium
         out += ["SCATTERING", "0", f3(md.sigma_s_rgb), "",
                 "ABSORBING", "0", f3(md.sigma_a_rgb), "",

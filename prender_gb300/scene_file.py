@@ -126,6 +126,15 @@ def load(path: str) -> Scene:
                       "disk_temperature": bool(k.use_accretion_disk_temperature),
                       "doppler_effect": float(k.color_doppler_factor_effect), "observer": _v(k.observer),
                       "disk_seed": int(k.disk_seed)}
+        w = d.wormhole
+        if w.enabled:
+            s.set_wormhole(_v(w.in_), _v(w.out), rho=float(w.rho), a=float(w.a), w=float(w.w),
+                           max_steps=int(w.max_steps), sign=int(w.sign),
+                           textures=tuple(_texture(w.texture[k], w.texture_width[k], w.texture_height[k], 3)
+                                          for k in range(2)),
+                           map_coef=tuple(tuple(float(x) for x in w.map_coef[k]) for k in range(2)),
+                           texture_coef=(float(w.texture_coef[0]), float(w.texture_coef[1])),
+                           camera=_v(w.camera))
         s.camera = ResolvedCamera(position=_v(cam.position), dir=_v(cam.dir), up=_v(cam.up),
                                   screen=(float(cam.screen_width), float(cam.screen_height), float(cam.screen_dist)),
                                   angle=None, width=int(cam.width), height=int(cam.height))

@@ -21,7 +21,9 @@ batch_oracle.npz and lights_oracle.npz the same way; --media-only,
 batch-variant and light-kind renders, --hdr-only its Render::OutputHdr file
 of a seeded image; --textures-only and --textures-oracle do the same for the
 texture and image-based-lighting scenes (textures_render.npz,
-textures_oracle.npz).
+textures_oracle.npz); --wormhole-only writes the reference's one-thread
+wormhole renders (wormhole_render.npz), --wormhole-oracle the oracle's
+16 batches of each wormhole scene (wormhole_oracle.npz).
 --scene-files-only writes the meshes and textures that the scene files in
 scene_files/ name, and scene_files.npz from the reference's renders of them.
 """
@@ -430,6 +432,44 @@ def textures_oracle_golden(nb=16):
     np.savez_compressed(os.path.join(HERE, "textures_oracle.npz"), **out)
 
 
+def wormhole_oracle_golden(nb=16):
+    """16 independent 64-spp renders of each wormhole scene by the oracle
+    (pinned bit-exact to the reference by wormhole_render.npz): per-pixel
+    mean and spread"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import wormhole_cases
+    from oracle import oracle as O
+    out = {}
+    for name in wormhole_cases.CASES:
+        sc = wormhole_cases.highspp_case(name)
+        o = O.OracleScene(sc)
+        imgs = []
+        for k in range(nb):
+            sc.settings.seed = 100 + k
+            img, _, _ = o.render(threads=os.cpu_count(), settings=sc.settings)
+            imgs.append(img)
+        b = np.stack(imgs)
+        out[f"{name}_mean"] = b.mean(0).astype(np.float32)
+        out[f"{name}_sd"] = b.std(0, ddof=1).astype(np.float32)
+        print("wormhole oracle", name, float(b.mean()))
+    out["batches"] = np.int32(nb)
+    np.savez_compressed(os.path.join(HERE, "wormhole_oracle.npz"), **out)
+
+
+def wormhole_golden(d):
+    """wormhole scenes rendered by the reference, one thread (bit-exact)"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import wormhole_cases
+    out = {}
+    for name, sc in wormhole_cases.one_thread_cases().items():
+        dd = os.path.join(d, "w_" + name)
+        os.makedirs(dd)
+        img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+        out[name] = img
+        print("wormhole", name, info, float(img.mean()))
+    np.savez_compressed(os.path.join(HERE, "wormhole_render.npz"), **out)
+
+
 def mesh7_oracle_golden(nb=16):
     """The benchmarked scene itself (327,680-triangle displaced icosphere,
     diffuse and glass) at 128 x 96, 16 independent 256-spp renders by the
@@ -553,7 +593,8 @@ def _image_size(path):
 KNOWN_FLAGS = {"--kerr-only", "--disk-only", "--sss-only", "--sss-l1-only", "--glossy-only", "--sss-oracle",
                "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle", "--scene-files-only", "--media-only",
                "--media-oracle", "--mesh7-oracle", "--batch-only", "--batch-oracle", "--hdr-only",
-               "--lights-only", "--lights-oracle", "--textures-only", "--textures-oracle"}
+               "--lights-only", "--lights-oracle", "--textures-only", "--textures-oracle", "--wormhole-only",
+               "--wormhole-oracle"}
 
 
 def main():
@@ -568,6 +609,9 @@ def main():
         return
     if "--textures-oracle" in sys.argv:
         textures_oracle_golden()
+        return
+    if "--wormhole-oracle" in sys.argv:
+        wormhole_oracle_golden()
         return
     if "--mesh7-oracle" in sys.argv:
         mesh7_oracle_golden()
@@ -602,6 +646,10 @@ def main():
     if "--media-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             media_golden(d)
+        return
+    if "--wormhole-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            wormhole_golden(d)
         return
     if "--textures-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:

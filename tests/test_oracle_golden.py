@@ -151,6 +151,32 @@ def test_texture_render_one_thread_bit_exact(golden, name):
     assert ref.mean() > 0
 
 
+@pytest.mark.parametrize("name", ["worm_bg", "worm_objects", "worm_sign"])
+def test_wormhole_render_one_thread_bit_exact(golden, name):
+    # the Dneg wormhole: both backgrounds seen through the throat, objects
+    # near both mouths (emissive, diffuse, mirror), the side forced by 'sign'
+    # with non-default map coefficients and no image on the far side
+    import wormhole_cases
+    sc = wormhole_cases.one_thread_cases()[name]
+    img, _, _ = O.OracleScene(sc).render(threads=1)
+    ref = golden["wormhole_render"][name]
+    assert np.array_equal(img, ref)
+    assert ref.mean() > 0
+
+
+def test_wormhole_trace_threads_agree():
+    # per-ray traces are independent: any thread count gives the same rays
+    import wormhole_cases
+    from prender_gb300 import scenes
+    sc = wormhole_cases.build("worm_objects", 16, 12, 1, 1, max_steps=200)
+    rays = scenes.camera_rays(sc)
+    o = O.OracleScene(sc)
+    a, b = o.wormhole_trace(rays, threads=1), o.wormhole_trace(rays, threads=4)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    assert set(np.unique(a["status"])) <= {0, 1, 3} and (a["status"] == 1).any()
+
+
 def _media_cases():
     import media_cases
     return media_cases

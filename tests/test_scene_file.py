@@ -58,6 +58,8 @@ def _written_cases():
     import texture_cases
     out.update({"lights_" + k: v for k, v in lights_cases.one_thread_cases().items()})
     out.update({"tex_" + k: v for k, v in texture_cases.one_thread_cases().items()})
+    import wormhole_cases
+    out.update(wormhole_cases.one_thread_cases())
     return out
 
 
@@ -87,6 +89,14 @@ def test_written_scene_reads_back_the_same(tmp_path, name):
         assert back.kerr["observer"] == tuple(s.camera.position)
         if s.kerr.get("disk_texture") is not None:
             assert np.array_equal(back.kerr["disk_texture"][:, :, :3], np.asarray(s.kerr["disk_texture"])[:, :, :3])
+    if s.wormhole is not None:
+        for k in ("in", "out", "rho", "a", "w", "max_steps", "sign", "map_coef", "texture_coef"):
+            assert back.wormhole[k] == s.wormhole[k], k
+        assert back.wormhole["camera"] == tuple(s.camera.position)
+        for a, b in zip(s.wormhole["textures"], back.wormhole["textures"]):
+            assert (a is None) == (b is None)
+            if a is not None:
+                assert np.array_equal(np.asarray(a), b)
 
 
 @pytest.mark.parametrize("name", ["spot", "spot_media", "parallel", "parallel_nonee", "infinity", "sss_spot",
@@ -119,6 +129,34 @@ def test_texture_files_render_like_the_reference(tmp_path, golden, name):
                 assert np.asarray(x).dtype == y.dtype and np.array_equal(np.asarray(x), y)
     img, _, _ = O.OracleScene(s).render(threads=1)
     assert np.array_equal(img, golden["textures_render"][name])
+
+
+@pytest.mark.parametrize("name", ["worm_bg", "worm_objects", "worm_sign"])
+def test_wormhole_files_render_like_the_reference(tmp_path, golden, name):
+    # the files the reference rendered for wormhole_render.npz (the WORMHOLE
+    # block: in, out, Rho, a, W, sign, geodesics_max_length, both background
+    # BMPs with their map_coef / coef lines), read by this library's reader
+    # and rendered by the oracle
+    import wormhole_cases
+    sc = wormhole_cases.one_thread_cases()[name]
+    s = scene_file.load(sc.write_reference(str(tmp_path)))
+    img, _, _ = O.OracleScene(s).render(threads=1)
+    assert np.array_equal(img, golden["wormhole_render"][name])
+
+
+def test_wormhole_placed_along_the_camera(tmp_path):
+    # without 'in' / 'out' the 'in' mouth sits dist along the camera
+    # direction and 'out' at the origin (scene_env.h:2100-2110); the block's
+    # geodesics_max_length is the black hole's setting too
+    s = scene_file.load(_scene(tmp_path, "CAMERA_POS\n0 0 10\n\nCAMERA_DIR\n0 0 -2\n\n"
+                                         "WORMHOLE\ndist 25\nRho 2\nsign -1\ngeodesics_max_length 500\n"
+                                         "map_coef2 1 0.5 2 0\ncoef1 3\nunknown 1\n\n"))
+    w = s.wormhole
+    assert w["in"] == (0.0, 0.0, -15.0) and w["out"] == (0.0, 0.0, 0.0)
+    assert w["rho"] == 2.0 and w["a"] == 0.5 and w["w"] == 0.05 and w["sign"] == -1 and w["max_steps"] == 500
+    assert w["map_coef"] == ((1.0, 0.0, 1.0, 0.0), (1.0, 0.5, 2.0, 0.0)) and w["texture_coef"] == (3.0, 1.0)
+    assert w["camera"] == (0.0, 0.0, 10.0)
+    assert "skipped in WORMHOLE: unknown 1" in s.file_warnings
 
 
 def test_hdr_reader_rows_and_values(tmp_path):
@@ -263,7 +301,6 @@ def test_bad_values_are_errors_with_the_line(tmp_path, body, msg):
     "OBJECT\nsphere 0 0 0 1\nreflection reflection\nreflection Subsurface_Scattering\n\n",
     "LENS\n0.5 100\n",
     "metropolisTransport\n1\n",
-    "WORMHOLE\n\n",
     "BLACKHOLE\ninitial_condition 1\n\n",
 ])
 def test_features_not_rendered_here_are_refused(tmp_path, body):
