@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define PR_ABI_VERSION 5
+#define PR_ABI_VERSION 6
 
 /* ---- status codes --------------------------------------------------- */
 enum {
@@ -173,17 +173,33 @@ typedef struct pr_entity {
   double spot_falloff;     /* spot_light_falloff exponent (parser default 0) */
   double spot_attenuation[3]; /* spot_attenuation a0 a1 a2: intensity divided by
                               a0 + d (a1 + a2 d) (parser default 0 0 1)      */
+  int32_t smooth;          /* PR_ENT_POLYGON: 'smooth 1' shades with the
+                              normal interpolated from the vertex normals
+                              (polygon.h:186-199)                            */
+  int32_t pad_smooth;
 } pr_entity;
 
 /* Triangle mesh as ObjLoader keeps it (ObjLoader.h:153-233): float vertices,
  * 0-based faces.  face_normals may be NULL, in which case they are derived
- * with the loader's rule (ObjLoader.cpp:577-700). */
+ * with the loader's rule (ObjLoader.cpp:577-700).  A smooth entity's
+ * vertex normals: vertex_normals[face_vn[3 f + k]] (the OBJ's vn lines and
+ * face ids); both NULL derives them with the loader's rule (the mean of the
+ * unnormalised face normals around each vertex, normalised; face_vn = the
+ * face's vertex ids).  Texture coordinates (vt lines, 2 floats each) with
+ * face_uv (3 ids per face) place textures and IBL images on the mesh
+ * (polygon.h:206-212, :507-528); NULL for none. */
 typedef struct pr_mesh {
   int32_t n_vertices;
   int32_t n_faces;
   const float* vertices;      /* 3 * n_vertices                              */
   const int32_t* faces;       /* 3 * n_faces                                 */
   const float* face_normals;  /* 3 * n_faces or NULL                         */
+  int32_t n_vertex_normals;
+  int32_t n_uv;
+  const float* vertex_normals;  /* 3 * n_vertex_normals or NULL              */
+  const int32_t* face_vn;       /* 3 * n_faces or NULL                       */
+  const float* uv;              /* 2 * n_uv or NULL                          */
+  const int32_t* face_uv;       /* 3 * n_faces or NULL                       */
 } pr_mesh;
 
 /* Kerr integrator precision: PR_KERR_FP64 runs the reference's FP64

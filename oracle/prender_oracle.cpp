@@ -149,6 +149,10 @@ struct Mesh {
   std::vector<float> vert;   // ObjLoader vert (float)
   std::vector<int> face;     // 0-based
   std::vector<float> fnorm;  // face normals (float, ObjLoader.cpp:577-700)
+  std::vector<float> norm;   // vertex normals (float): the vn lines, or the loader's rule
+  std::vector<int> norm_id;  // 3 per face
+  std::vector<float> uv;     // vt lines (2 per entry)
+  std::vector<int> uv_id;    // 3 per face (empty: no vt lines)
 };
 
 struct Tri {  // Triangle (polygon.h:22-708)
@@ -193,6 +197,7 @@ struct Entity {
   int blackhole_disk = 0;       // accretion-disk texture index (0 by default, scene_env.h:271)
   // mesh
   int mesh = -1;
+  int smooth = 0;  // Mesh::smooth ('smooth' of the OBJECT block)
   std::vector<Tri> tris;
   QBVH qbvh;
   double area = INF;
@@ -577,13 +582,50 @@ bool tri_hit(const Scene& s, const Entity& e, const Tri& tr, V3 org, V3 dir, Hit
     return false;
   }
   const double t = dot(edge2, q) * inv_det;
+  u *= inv_det;
+  v *= inv_det;
+  const double w = 1.0 - u - v;
   if (!(t > EPS)) return false;
   h.distance = t;
   h.position = org + dir * t;
   h.normal = V3(m.fnorm[3 * tr.face], m.fnorm[3 * tr.face + 1], m.fnorm[3 * tr.face + 2]);
+  if (e.smooth) {  // polygon.h:186-199
+    const int* ni = &m.norm_id[3 * tr.face];
+    const V3 n0(m.norm[3 * (size_t)ni[0]], m.norm[3 * (size_t)ni[0] + 1], m.norm[3 * (size_t)ni[0] + 2]);
+    const V3 n1(m.norm[3 * (size_t)ni[1]], m.norm[3 * (size_t)ni[1] + 1], m.norm[3 * (size_t)ni[1] + 2]);
+    const V3 n2(m.norm[3 * (size_t)ni[2]], m.norm[3 * (size_t)ni[2] + 1], m.norm[3 * (size_t)ni[2] + 2]);
+    h.normal = normalize(n0 * w + n1 * u + n2 * v);
+  }
   if (e.normal_inverse < 0) h.normal = h.normal * -1.0;
   h.material = e.material;
   h.prim = tr.face;
+  // the material's texture / IBL image at the interpolated texture
+  // coordinates (polygon.h:206-212, :507-528; no wrap: the coordinates of a
+  // textured mesh lie in [0, 1]); bump maps on meshes write the caller's
+  // record, which the returned hit overwrites (polygon.h:529-618)
+  const Material& mt = s.mats[e.material];
+  if ((mt.tex || mt.ibl) && !m.uv_id.empty()) {
+    const int* ti = &m.uv_id[3 * tr.face];
+    const double hu = m.uv[2 * (size_t)ti[0]] * w + m.uv[2 * (size_t)ti[1]] * u + m.uv[2 * (size_t)ti[2]] * v;
+    const double hv = m.uv[2 * (size_t)ti[0] + 1] * w + m.uv[2 * (size_t)ti[1] + 1] * u + m.uv[2 * (size_t)ti[2] + 1] * v;
+    V3 color = mt.color, emission = mt.emission;
+    if (mt.tex) {
+      int j = trunc_int((mt.tex_w - 1) * hu), i = trunc_int((mt.tex_h - 1) * hv);
+      i = std::min(std::max(i, 0), mt.tex_h - 1);
+      j = std::min(std::max(j, 0), mt.tex_w - 1);
+      texel_rgb(mt, i, j, color);
+    }
+    if (mt.ibl) {
+      int j = trunc_int((mt.ibl_w - 1) * hu), i = trunc_int((mt.ibl_h - 1) * hv);
+      i = std::min(std::max(i, 0), mt.ibl_h - 1);
+      j = std::min(std::max(j, 0), mt.ibl_w - 1);
+      color = ibl_rgb(mt, i, j);
+      emission = mt.ibl_coef * color;
+    }
+    h.ov = true;
+    h.ov_color = color;
+    h.ov_emission = emission;
+  }
   return true;
 }
 
@@ -922,8 +964,60 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
     m.vert.assign(pm.vertices, pm.vertices + 3 * (size_t)pm.n_vertices);
     m.face.assign(pm.faces, pm.faces + 3 * (size_t)pm.n_faces);
     m.fnorm.resize(3 * (size_t)pm.n_faces);
+    if (pm.vertex_normals && pm.face_vn) {
+      m.norm.assign(pm.vertex_normals, pm.vertex_normals + 3 * (size_t)pm.n_vertex_normals);
+      m.norm_id.assign(pm.face_vn, pm.face_vn + 3 * (size_t)pm.n_faces);
+    } else {
+      // Obj::CalcNormalVector without vn lines (ObjLoader.cpp:645-685): the
+      // unnormalised face normals summed at each vertex in face order, the
+      // mean normalised in float; norm_id = the face's vertex ids
+      const int nv = pm.n_vertices;
+      m.norm.assign(3 * (size_t)nv, 0.0f);
+      m.norm_id = m.face;
+      std::vector<int> count((size_t)nv, 0);
+      const float* V = m.vert.data();
+      for (int f = 0; f < pm.n_faces; f++) {
+        const int* fc = &m.face[3 * f];
+        float dx1 = V[3 * fc[1]] - V[3 * fc[0]], dy1 = V[3 * fc[1] + 1] - V[3 * fc[0] + 1],
+              dz1 = V[3 * fc[1] + 2] - V[3 * fc[0] + 2];
+        float dx2 = V[3 * fc[2]] - V[3 * fc[0]], dy2 = V[3 * fc[2] + 1] - V[3 * fc[0] + 1],
+              dz2 = V[3 * fc[2] + 2] - V[3 * fc[0] + 2];
+        const float fnv[3] = {dy1 * dz2 - dz1 * dy2, dz1 * dx2 - dx1 * dz2, dx1 * dy2 - dy1 * dx2};
+        for (int k = 0; k < 3; k++) {
+          for (int a = 0; a < 3; a++) m.norm[3 * (size_t)fc[k] + a] += fnv[a];
+          count[(size_t)fc[k]]++;
+        }
+      }
+      for (int i2 = 0; i2 < nv; i2++) {
+        if (count[(size_t)i2] == 0) continue;
+        float* n = &m.norm[3 * (size_t)i2];
+        for (int a = 0; a < 3; a++) n[a] /= (double)count[(size_t)i2];
+        float a = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        if (a != 0.0) { n[0] /= a; n[1] /= a; n[2] /= a; }
+      }
+    }
+    if (pm.uv && pm.face_uv) {
+      m.uv.assign(pm.uv, pm.uv + 2 * (size_t)pm.n_uv);
+      m.uv_id.assign(pm.face_uv, pm.face_uv + 3 * (size_t)pm.n_faces);
+    }
     if (pm.face_normals) {
       memcpy(m.fnorm.data(), pm.face_normals, sizeof(float) * 3 * (size_t)pm.n_faces);
+    } else if (pm.vertex_normals && pm.face_vn) {
+      // with vn lines: the normalised mean of the face's three (ObjLoader.cpp:617-641)
+      for (int f = 0; f < pm.n_faces; f++) {
+        float c[3];
+        for (int a = 0; a < 3; a++)
+          c[a] = (m.norm[3 * (size_t)m.norm_id[3 * f] + a] + m.norm[3 * (size_t)m.norm_id[3 * f + 1] + a] +
+                  m.norm[3 * (size_t)m.norm_id[3 * f + 2] + a]) / 3.0;
+        double ln = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+        if (ln > 1.0e-16) {
+          ln = std::sqrt(ln);
+          c[0] /= ln;
+          c[1] /= ln;
+          c[2] /= ln;
+        }
+        for (int a = 0; a < 3; a++) m.fnorm[3 * (size_t)f + a] = c[a];
+      }
     } else {
       // Obj::CalcNormalVector, no 'vn' lines (ObjLoader.cpp:582-598, :686-697)
       for (int f = 0; f < pm.n_faces; f++) {
@@ -1012,6 +1106,7 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
     } else if (pe.type == PR_ENT_POLYGON) {
       if (pe.mesh < 0 || pe.mesh >= (int)s.meshes.size()) { err = "entity mesh out of range"; return PR_E_SCENE; }
       e.mesh = pe.mesh;
+      e.smooth = pe.smooth;
       const Mesh& mesh = s.meshes[pe.mesh];
       const int nf = (int)mesh.face.size() / 3;
       // Polygon::MakeTrianglesEntity + Triangle::CreateBoundingBox (polygon.h:686-703, :912-969)

@@ -109,6 +109,8 @@ class pr_entity(C.Structure):
         ("spot_angle", C.c_double * 2),
         ("spot_falloff", C.c_double),
         ("spot_attenuation", D3),
+        ("smooth", C.c_int32),
+        ("pad_smooth", C.c_int32),
     ]
 
 
@@ -119,6 +121,12 @@ class pr_mesh(C.Structure):
         ("vertices", C.POINTER(C.c_float)),
         ("faces", C.POINTER(C.c_int32)),
         ("face_normals", C.POINTER(C.c_float)),
+        ("n_vertex_normals", C.c_int32),
+        ("n_uv", C.c_int32),
+        ("vertex_normals", C.POINTER(C.c_float)),
+        ("face_vn", C.POINTER(C.c_int32)),
+        ("uv", C.POINTER(C.c_float)),
+        ("face_uv", C.POINTER(C.c_int32)),
     ]
 
 

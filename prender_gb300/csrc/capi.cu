@@ -204,6 +204,8 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   if (!h.texels.empty()) PR_CUDA(c, upload(o.texels, h.texels, c->stream));
   if (!h.ibl_texels.empty()) PR_CUDA(c, upload(o.ibl_texels, h.ibl_texels, c->stream));
   if (!h.bump_texels.empty()) PR_CUDA(c, upload(o.bump_texels, h.bump_texels, c->stream));
+  if (!h.fvn.empty()) PR_CUDA(c, upload(o.fvn, h.fvn, c->stream));
+  if (!h.fuv.empty()) PR_CUDA(c, upload(o.fuv, h.fuv, c->stream));
   PR_CUDA(c, upload(o.kerr_tex, h.kerr_texture, c->stream));
   PR_CUDA(c, upload(o.kerr_disk_tex, h.kerr_disk_texture, c->stream));
   for (int k = 0; k < 2; k++)
@@ -247,6 +249,9 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
     S.has_glossy |= (gm.type == PR_MAT_WARD || gm.type == PR_MAT_PHONG) ? 1 : 0;
     S.has_tex |= (gm.tex_off >= 0 || gm.ibl_off >= 0 || gm.bump_off >= 0) ? 1 : 0;
   }
+  if (!h.fvn.empty()) S.has_tex |= 2;
+  S.fvn = h.fvn.empty() ? nullptr : (const float*)o.fvn.p;
+  S.fuv = h.fuv.empty() ? nullptr : (const float*)o.fuv.p;
   for (int k = 0; k < 3; k++) {
     S.bg[k] = (float)h.background[k];
     S.env[k] = (float)h.env_light[k];
@@ -800,8 +805,10 @@ static int adjoint_checks(pr_ctx* c, const pr_render_params* p) {
   if (c->cur.dev.has_sss) return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover subsurface materials");
   if (c->cur.dev.n_point_lights > 0)
     return fail(c, PR_E_UNSUPPORTED, "the adjoint pass covers area lights only (no parallel, spot or infinity lights)");
-  if (c->cur.dev.has_tex)
+  if (c->cur.dev.has_tex & 1)
     return fail(c, PR_E_UNSUPPORTED, "the adjoint pass differentiates material colours, not textures");
+  if (c->cur.dev.has_tex & 2)
+    return fail(c, PR_E_UNSUPPORTED, "the adjoint pass shades with face normals only (no smooth meshes)");
   for (const GMaterial& m : c->cur.host.mats)
     if (m.type == PR_MAT_WARD || m.type == PR_MAT_PHONG)
       return fail(c, PR_E_UNSUPPORTED, "the adjoint pass does not cover Ward or Phong materials (their lobes scale "

@@ -573,6 +573,41 @@ __device__ __forceinline__ float3 bump_tilt(const DevScene& S, const GMaterial& 
 // (ibl_coef times the texel); a bump map gives the tilted normal bn (and
 // bit 2 of the result).  Bit 1 of the result: the material has an IBL
 // image, whose hit the caller ends with its emission (radiance.h:45-50).
+// Triangle::intersect's smooth normal and texture coordinates (polygon.h:
+// 186-212) at a mesh hit with barycentrics (u, v): the normal interpolated
+// from the face's vertex normals (then the entity's inversion), and the
+// material's texture or IBL image at (W - 1) u, (H - 1) v of the
+// interpolated coordinates (polygon.h:507-528: the texel is the colour, the
+// specular colour stays; an IBL texel is the colour and, scaled, the
+// emission).  Bump maps on meshes do not reach the hit the reference
+// returns (polygon.h:529-618 writes the caller's record, which the hit
+// then overwrites), so none is read here.  True for an IBL hit.
+__device__ inline bool mesh_hit(const DevScene& S, const GMaterial& m, const GEntF& e, int flags, const FastHit& h,
+                                Vertex& v, float3& C, float3& E) {
+  const int face = e.face_base + __float_as_int(__ldg(S.rtris + 3 * (size_t)h.slot).w);
+  const float w = 1.0f - h.u - h.v;
+  if (flags & 1) {
+    const float* n = S.fvn + 9 * (size_t)face;
+    float3 ns = normalize(f3(n[0] * w + n[3] * h.u + n[6] * h.v, n[1] * w + n[4] * h.u + n[7] * h.v,
+                             n[2] * w + n[5] * h.u + n[8] * h.v));
+    v.n = e.normal_inverse < 0 ? -ns : ns;
+  }
+  if (!(flags & 2)) return false;
+  const float* t = S.fuv + 6 * (size_t)face;
+  const float tu = t[0] * w + t[2] * h.u + t[4] * h.v, tv = t[1] * w + t[3] * h.u + t[5] * h.v;
+  if (m.tex_off >= 0) {
+    const float4 x = __ldg(S.texels + m.tex_off + (size_t)tex_clamp((int)((m.tex_h - 1) * tv), m.tex_h) * m.tex_w +
+                           tex_clamp((int)((m.tex_w - 1) * tu), m.tex_w));
+    C = f3(x.x, x.y, x.z);
+  }
+  if (m.ibl_off < 0) return false;
+  const float4 x = __ldg(S.ibl_texels + m.ibl_off + (size_t)tex_clamp((int)((m.ibl_h - 1) * tv), m.ibl_h) * m.ibl_w +
+                         tex_clamp((int)((m.ibl_w - 1) * tu), m.ibl_w));
+  C = f3(x.x, x.y, x.z);
+  E = C * m.ibl_coef;
+  return true;
+}
+
 __device__ inline int hit_texture(const DevScene& S, const GMaterial& m, const GEntF& e, const GEntity& ed, float3 p,
                                   float3 n_hit, float3& C, float3& E, float3& Sp, float3& bn) {
   const bool has_ibl = m.ibl_off >= 0;
@@ -738,7 +773,14 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   float3 Sp = ld3(m.specular);
   float3 bn = f3(0, 0, 0);  // bump-tilted normal
   bool bumped = false;
-  if (EXT && (m.tex_off >= 0 || m.ibl_off >= 0 || m.bump_off >= 0)) {
+  if (EXT && !pre && ent.type == PR_ENT_POLYGON) {
+    const int mf = S.ents[v.ent].mesh_flags;
+    if (mf && mesh_hit(S, m, ent, mf, h, v, C, E)) {
+      ps.L += ps.beta * E;  // an IBL image on the mesh (radiance.h:45-50)
+      if (tap) tap->em(v.mat, ps.beta);
+      return SHADE_END;
+    }
+  } else if (EXT && (m.tex_off >= 0 || m.ibl_off >= 0 || m.bump_off >= 0)) {
     const int tx = hit_texture(S, m, ent, S.ents[v.ent], v.p, v.n, C, E, Sp, bn);
     if (tx & 1) {
       // an object with an IBL image gives its hit point's emission and

@@ -122,7 +122,7 @@ struct GEntity {
   int32_t node_base;       // root node index in the concatenated node array
   int32_t slot_base;       // first leaf slot of this mesh
   int32_t rnode_base;      // root of the mesh's render-path tree (DevScene::rnodes)
-  int32_t pad2;
+  int32_t mesh_flags;      // mesh: 1 smooth (DevScene::fvn), 2 textured (DevScene::fuv)
   int32_t face_base;       // first face-normal record of this mesh
   int32_t n_faces;
   float bmin[3], bmax[3];  // bounds (for scene extents)
@@ -240,6 +240,8 @@ struct DevScene {
   const float4* texels;    // every material's texture, RGB / 255 (cell(i, j) order)
   const float4* ibl_texels;  // every IBL image, IBL_Color(i, j) order
   const float* bump_texels;  // every bump map: the texel's luminance 0.299 r + 0.587 g + 0.114 b (0..255)
+  const float* fvn;        // 9 per face: the vertex normals of smooth meshes (null: none)
+  const float* fuv;        // 6 per face: the texture coordinates of textured meshes (null: none)
   int32_t n_ents;
   int32_t n_lights;
   int32_t n_point_lights;  // parallel, spot and infinity lights (sampled even without NEE)
@@ -252,7 +254,7 @@ struct DevScene {
   float scene_scale;       // max |coordinate| of the scene bounds
   int32_t has_sss;         // a subsurface (dipole) material is present
   int32_t has_glossy;      // a Ward or Phong material is present
-  int32_t has_tex;         // a material has a texture or an IBL image
+  int32_t has_tex;         // 1: a material has a texture, an IBL image or a bump map; 2: a mesh is smooth
   GEntF entf[kMaxEntities];
 };
 

@@ -289,6 +289,48 @@ void face_normals(const float* V, const int32_t* F, int n_faces, std::vector<flo
   }
 }
 
+void vertex_normals(const float* V, const int32_t* F, int n_faces, int n_vertices, std::vector<float>& out) {
+  out.assign(3 * (size_t)n_vertices, 0.0f);
+  std::vector<int> count((size_t)n_vertices, 0);
+  for (int f = 0; f < n_faces; f++) {
+    const int32_t* fc = F + 3 * (size_t)f;
+    const float dx1 = V[3 * fc[1]] - V[3 * fc[0]], dy1 = V[3 * fc[1] + 1] - V[3 * fc[0] + 1],
+                dz1 = V[3 * fc[1] + 2] - V[3 * fc[0] + 2];
+    const float dx2 = V[3 * fc[2]] - V[3 * fc[0]], dy2 = V[3 * fc[2] + 1] - V[3 * fc[0] + 1],
+                dz2 = V[3 * fc[2] + 2] - V[3 * fc[0] + 2];
+    const float n[3] = {dy1 * dz2 - dz1 * dy2, dz1 * dx2 - dx1 * dz2, dx1 * dy2 - dy1 * dx2};
+    for (int k = 0; k < 3; k++) {
+      for (int a = 0; a < 3; a++) out[3 * (size_t)fc[k] + a] += n[a];
+      count[(size_t)fc[k]]++;
+    }
+  }
+  for (int i = 0; i < n_vertices; i++) {
+    if (count[(size_t)i] == 0) continue;
+    float* n = &out[3 * (size_t)i];
+    for (int a = 0; a < 3; a++) n[a] = (float)((double)n[a] / (double)count[(size_t)i]);
+    const float a = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (a != 0.0f)
+      for (int k = 0; k < 3; k++) n[k] /= a;
+  }
+}
+
+void face_normals_vn(const float* VN, const int32_t* FVN, int n_faces, std::vector<float>& out) {
+  out.resize(3 * (size_t)n_faces);
+  for (int i = 0; i < n_faces; i++) {
+    float c[3];
+    for (int a = 0; a < 3; a++) {
+      const float s = (VN[3 * (size_t)FVN[3 * i] + a] + VN[3 * (size_t)FVN[3 * i + 1] + a]) + VN[3 * (size_t)FVN[3 * i + 2] + a];
+      c[a] = (float)(s / 3.0);
+    }
+    double ln = (double)((c[0] * c[0] + c[1] * c[1]) + c[2] * c[2]);
+    if (ln > 1.0e-16) {
+      ln = std::sqrt(ln);
+      for (int a = 0; a < 3; a++) c[a] = (float)(c[a] / ln);
+    }
+    for (int a = 0; a < 3; a++) out[3 * (size_t)i + a] = c[a];
+  }
+}
+
 static bool is_light(const pr_material& m) {  // Material::isLight (material.h)
   const D3 c = mk(m.color), e = mk(m.emission);
   return m.type == PR_MAT_DIFFUSE && len(c) < 0.001 && len(e) > 0.001;
@@ -649,6 +691,16 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
   }
   double ext = 1.0;
   auto grow = [&ext](double x) { ext = std::max(ext, std::fabs(x)); };
+  // meshes shaded with interpolated normals, and textured meshes: the
+  // per-face vertex-normal and texture-coordinate records exist only then
+  bool any_smooth = false, any_mesh_tex = false;
+  for (int i = 0; i < d->n_entities; i++) {
+    const pr_entity& pe = d->entities[i];
+    if (pe.type != PR_ENT_POLYGON || pe.material < 0 || pe.material >= d->n_materials) continue;
+    const pr_material& pm = d->materials[pe.material];
+    any_smooth = any_smooth || pe.smooth != 0;
+    any_mesh_tex = any_mesh_tex || pm.texture || pm.ibl_rgb8 || pm.ibl_rgbf;
+  }
   for (int i = 0; i < d->n_entities; i++) {
     const pr_entity& pe = d->entities[i];
     if (pe.material < 0 || pe.material >= d->n_materials) { err = "entity material out of range"; return PR_E_SCENE; }
@@ -659,8 +711,8 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
     g.normal_inverse = pe.normal_inverse < 0 ? -1 : 1;
     const pr_material& pm = d->materials[pe.material];
     const bool textured = pm.texture || pm.ibl_rgb8 || pm.ibl_rgbf || pm.bump;
-    if (textured && pe.type != PR_ENT_SPHERE && pe.type != PR_ENT_UVPLANE) {
-      err = "textures and IBL images are read on spheres, hemispheres and uvplanes only";
+    if (textured && pe.type != PR_ENT_SPHERE && pe.type != PR_ENT_UVPLANE && pe.type != PR_ENT_POLYGON) {
+      err = "textures and IBL images are read on spheres, hemispheres, uvplanes and meshes only";
       return PR_E_UNSUPPORTED;
     }
     if (textured && (hs.mats[pe.material].sss || d->kerr.enabled || d->wormhole.enabled)) {
@@ -747,9 +799,58 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
         if (pm_.faces[f] < 0 || pm_.faces[f] >= pm_.n_vertices) { err = "face index out of range"; return PR_E_SCENE; }
       if (is_light(pm)) { err = "mesh lights are not sampled by the reference's next-event estimation"; return PR_E_UNSUPPORTED; }
       const bool big = pm_.n_faces >= kGpuBuildMinFaces;
+      const int64_t n3 = 3 * (int64_t)pm_.n_faces;
+      if (pm_.vertex_normals || pm_.face_vn) {
+        if (!pm_.vertex_normals || !pm_.face_vn || pm_.n_vertex_normals <= 0) {
+          err = "vertex normals need the normals and their face ids";
+          return PR_E_SCENE;
+        }
+        for (int64_t f = 0; f < n3; f++)
+          if (pm_.face_vn[f] < 0 || pm_.face_vn[f] >= pm_.n_vertex_normals) {
+            err = "vertex-normal id out of range";
+            return PR_E_SCENE;
+          }
+      }
+      if (pm_.uv || pm_.face_uv) {
+        if (!pm_.uv || !pm_.face_uv || pm_.n_uv <= 0) { err = "texture coordinates need the values and their face ids"; return PR_E_SCENE; }
+        for (int64_t f = 0; f < n3; f++)
+          if (pm_.face_uv[f] < 0 || pm_.face_uv[f] >= pm_.n_uv) { err = "texture-coordinate id out of range"; return PR_E_SCENE; }
+      }
+      const bool mesh_tex = pm.texture || pm.ibl_rgb8 || pm.ibl_rgbf;
+      if (mesh_tex || pm.bump) {
+        // the reference indexes the image with (W - 1) u, (H - 1) v of the
+        // interpolated coordinates, with no wrap (polygon.h:507-618); a bump
+        // map's lookup runs too, though its normal does not reach the hit
+        if (!pm_.uv) { err = "a texture, IBL image or bump map on a mesh needs texture coordinates (vt)"; return PR_E_UNSUPPORTED; }
+        for (int64_t k = 0; k < 2 * (int64_t)pm_.n_uv; k++)
+          if (!(pm_.uv[k] >= 0.0f && pm_.uv[k] <= 1.0f)) {
+            err = "texture coordinates of a textured mesh must lie in [0, 1] (the reference reads no wrap there)";
+            return PR_E_UNSUPPORTED;
+          }
+      }
+      if (pe.smooth && (d->kerr.enabled || d->wormhole.enabled)) {
+        err = "smooth meshes in a black hole or wormhole scene are not on this path";
+        return PR_E_UNSUPPORTED;
+      }
       std::vector<float> fn;
       if (pm_.face_normals) fn.assign(pm_.face_normals, pm_.face_normals + 3 * (size_t)pm_.n_faces);
+      else if (pm_.vertex_normals) face_normals_vn(pm_.vertex_normals, pm_.face_vn, pm_.n_faces, fn);
       else face_normals(pm_.vertices, pm_.faces, pm_.n_faces, fn);
+      g.mesh_flags = (pe.smooth ? 1 : 0) | (mesh_tex ? 2 : 0);
+      if (any_smooth) {
+        std::vector<float> vn;
+        const float* VN = pm_.vertex_normals;
+        const int32_t* FVN = pm_.face_vn ? pm_.face_vn : pm_.faces;
+        if (pe.smooth && !VN) {
+          vertex_normals(pm_.vertices, pm_.faces, pm_.n_faces, pm_.n_vertices, vn);
+          VN = vn.data();
+        }
+        for (int64_t f = 0; f < n3; f++)
+          for (int a = 0; a < 3; a++) hs.fvn.push_back(pe.smooth ? VN[3 * (size_t)FVN[f] + a] : 0.0f);
+      }
+      if (any_mesh_tex)
+        for (int64_t f = 0; f < n3; f++)
+          for (int a = 0; a < 2; a++) hs.fuv.push_back(mesh_tex ? pm_.uv[2 * (size_t)pm_.face_uv[f] + a] : 0.0f);
       g.face_base = (int32_t)(hs.fnorm.size() / 3);
       g.n_faces = pm_.n_faces;
       if (big && opt.defer_exact && !d->kerr.enabled && !d->wormhole.enabled) {

@@ -34,6 +34,10 @@ struct HostScene {
   std::vector<WNode> rnodes;   // render-path trees
   std::vector<float4> rtris;
   std::vector<float> fnorm;
+  // per face (indexed like fnorm): the three vertex normals of smooth meshes
+  // (9 floats; empty when no mesh is smooth) and the three texture
+  // coordinates of meshes with them (6 floats; empty when no textured mesh)
+  std::vector<float> fvn, fuv;
   std::vector<float4> texels;           // material textures, RGB / 255
   std::vector<float4> ibl_texels;       // material IBL images
   std::vector<float> bump_texels;       // material bump maps (luminance)
@@ -81,5 +85,12 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err,
 int complete_exact_qbvh(HostScene& hs, std::string& err);
 int build_mesh_qbvh(const float* vertices, const int32_t* faces, int n_faces, MeshQbvh& out, std::string& err);
 void face_normals(const float* V, const int32_t* F, int n_faces, std::vector<float>& out);
+// Obj::CalcNormalVector without vn lines (ObjLoader.cpp:577-700): each
+// vertex's normal is the mean of the unnormalised face normals around it,
+// normalised, in float; out holds 3 per vertex
+void vertex_normals(const float* V, const int32_t* F, int n_faces, int n_vertices, std::vector<float>& out);
+// the same with vn lines (ObjLoader.cpp:617-641): a face's normal is the
+// normalised mean of its three vertex normals
+void face_normals_vn(const float* VN, const int32_t* FVN, int n_faces, std::vector<float>& out);
 
 }  // namespace pr

@@ -48,6 +48,10 @@ struct pr_scene_file {
   std::vector<std::vector<float>> verts;
   std::vector<std::vector<int32_t>> faces;
   std::vector<std::vector<float>> fnormals;  // empty: the loader's rule at upload
+  // per mesh: vertex normals with their face ids (empty: derived at upload)
+  // and texture coordinates with theirs (empty: none)
+  std::vector<std::vector<float>> vnormals, uvs;
+  std::vector<std::vector<int32_t>> face_vn, face_uv;
   std::vector<pr_mesh> meshes;
   std::vector<uint8_t> bg_tex, disk_tex, worm_tex[2];
   // per material: texture / IBL images (pointers set when the desc is made)
@@ -301,18 +305,23 @@ void read_hdr(const std::string& path, std::vector<float>& out, int& w, int& h) 
 struct ObjMesh {
   std::vector<float> v;      // 3 per vertex
   std::vector<float> vn;     // 3 per vertex normal
+  std::vector<float> vt;     // 2 per texture coordinate
   std::vector<int32_t> f;    // 3 per triangle, 0-based
   std::vector<int32_t> nid;  // 3 per triangle: vertex-normal ids (0 where the face gives none)
+  std::vector<int32_t> tid;  // 3 per triangle: texture-coordinate ids (empty without vt lines)
 };
 
-// Obj::Load (ObjLoader.cpp:125-470): 'v' and 'vn' lines as floats; faces in
-// the reference's order of attempts (v/vt/vn, v//vn, v/vt, v; four vertices
-// before three), a quad a b c d split into (a, b, c) and (c, d, a).
+// Obj::Load (ObjLoader.cpp:125-470): 'v', 'vn' and 'vt' lines as floats;
+// faces in the reference's order of attempts (v/vt/vn, v//vn, v/vt, v; four
+// vertices before three), a quad a b c d split into (a, b, c) and (c, d, a)
+// with its normal and texture ids alike; ids a face does not give are 0.
+// Vertex colours (a last 'v' line with six or more numbers makes the whole
+// mesh take them, ObjLoader.cpp:199-228) are refused.
 void read_obj(const std::string& path, ObjMesh& m) {
   std::ifstream f(path);
   if (!f) fail("cannot open " + path);
   std::string line, mtllib;
-  bool usemtl = false;
+  bool usemtl = false, vertex_colour = false;
   while (std::getline(f, line)) {
     size_t b = 0;
     while (b < line.size() && (line[b] == ' ' || line[b] == '\t')) b++;
@@ -326,21 +335,25 @@ void read_obj(const std::string& path, ObjMesh& m) {
       float x = 0, y = 0, z = 0;
       std::sscanf(c, "%*s %f %f %f", &x, &y, &z);
       m.vn.insert(m.vn.end(), {x, y, z});
+    } else if (s.size() > 1 && c[0] == 'v' && c[1] == 't') {
+      float x = 0, y = 0;
+      std::sscanf(c, "%*s %f %f", &x, &y);
+      m.vt.insert(m.vt.end(), {x, y});
     } else if (s.size() > 1 && c[0] == 'v' && c[1] == ' ') {
-      float x = 0, y = 0, z = 0;
-      std::sscanf(c, "%*s %f %f %f", &x, &y, &z);
+      float x = 0, y = 0, z = 0, cr[3];
+      vertex_colour = std::sscanf(c, "%*s %f %f %f %f %f %f", &x, &y, &z, &cr[0], &cr[1], &cr[2]) == 6;
       m.v.insert(m.v.end(), {x, y, z});
     } else if (s.size() > 1 && c[0] == 'f' && c[1] == ' ') {
       const char* p = c + 2;
       int a[4], t[4], n[4];
-      bool has_n = false;
+      bool has_n = false, has_t = false;
       int k = 0;
       if (std::sscanf(p, "%d/%d/%d %d/%d/%d %d/%d/%d %d/%d/%d", &a[0], &t[0], &n[0], &a[1], &t[1], &n[1], &a[2], &t[2],
                       &n[2], &a[3], &t[3], &n[3]) == 12) {
-        k = 4, has_n = true;
+        k = 4, has_n = has_t = true;
       } else if (std::sscanf(p, "%d/%d/%d %d/%d/%d %d/%d/%d", &a[0], &t[0], &n[0], &a[1], &t[1], &n[1], &a[2], &t[2],
                              &n[2]) == 9) {
-        k = 3, has_n = true;
+        k = 3, has_n = has_t = true;
       } else if (std::sscanf(p, "%d//%d %d//%d %d//%d %d//%d", &a[0], &n[0], &a[1], &n[1], &a[2], &n[2], &a[3],
                              &n[3]) == 8) {
         k = 4, has_n = true;
@@ -348,9 +361,9 @@ void read_obj(const std::string& path, ObjMesh& m) {
         k = 3, has_n = true;
       } else if (std::sscanf(p, "%d/%d %d/%d %d/%d %d/%d", &a[0], &t[0], &a[1], &t[1], &a[2], &t[2], &a[3], &t[3]) ==
                  8) {
-        k = 4;
+        k = 4, has_t = true;
       } else if (std::sscanf(p, "%d/%d %d/%d %d/%d", &a[0], &t[0], &a[1], &t[1], &a[2], &t[2]) == 6) {
-        k = 3;
+        k = 3, has_t = true;
       } else if (std::sscanf(p, "%d %d %d %d", &a[0], &a[1], &a[2], &a[3]) == 4) {
         k = 4;
       } else if (std::sscanf(p, "%d %d %d", &a[0], &a[1], &a[2]) == 3) {
@@ -360,11 +373,14 @@ void read_obj(const std::string& path, ObjMesh& m) {
       }
       if (!has_n)
         for (int i = 0; i < 4; i++) n[i] = 1;  // no ids: the reference's zero-initialised norm_id
+      if (!has_t)
+        for (int i = 0; i < 4; i++) t[i] = 1;  // and texture_id
       const int tri[2][3] = {{0, 1, 2}, {2, 3, 0}};
       for (int q = 0; q < (k == 4 ? 2 : 1); q++)
         for (int j = 0; j < 3; j++) {
           m.f.push_back(a[tri[q][j]] - 1);
           m.nid.push_back(n[tri[q][j]] - 1);
+          m.tid.push_back(t[tri[q][j]] - 1);
         }
     }
   }
@@ -374,6 +390,11 @@ void read_obj(const std::string& path, ObjMesh& m) {
   if (nn > 0)
     for (int32_t i : m.nid)
       if (i < 0 || i >= nn) fail("vertex-normal index outside the normals in " + path);
+  const int64_t nt = (int64_t)(m.vt.size() / 2);
+  if (nt == 0) m.tid.clear();  // no vt lines: no texture ids (ObjLoader.cpp:474-478)
+  for (int32_t i : m.tid)
+    if (i < 0 || i >= nt) fail("texture-coordinate index outside the vt lines in " + path);
+  if (vertex_colour) fail("OBJ vertex colours are not rendered here: " + path);
   if (m.f.empty()) fail("no faces in " + path);
   if (usemtl && !mtllib.empty() && (readable(mtllib) || readable(dir_of(path) + mtllib)))
     fail("OBJ materials (mtllib / usemtl) are not rendered here: " + path);
@@ -499,7 +520,7 @@ M4 normal_matrix(const M4& M) {
 // Polygon::MatrixTransformation (polygon.h:749-772): each matrix in turn
 // moves the float vertices (through double) and carries the float face
 // normals, renormalised
-void transform_mesh(const std::vector<M4>& ms, std::vector<float>& v, std::vector<float>& fn) {
+void transform_mesh(const std::vector<M4>& ms, std::vector<float>& v, std::vector<float>& fn, std::vector<float>& vn) {
   for (const M4& m : ms) {
     for (size_t i = 0; i < v.size(); i += 3) {
       const double p[3] = {v[i], v[i + 1], v[i + 2]};
@@ -508,13 +529,15 @@ void transform_mesh(const std::vector<M4>& ms, std::vector<float>& v, std::vecto
       for (int a = 0; a < 3; a++) v[i + a] = (float)o[a];
     }
     const M4 g = normal_matrix(m);
-    for (size_t i = 0; i < fn.size(); i += 3) {
-      const double n[3] = {fn[i], fn[i + 1], fn[i + 2]};
-      double o[3];
-      apply(g, n, o);
-      const double inv = 1.0 / std::sqrt((o[0] * o[0] + o[2] * o[2]) + o[1] * o[1]);
-      for (int a = 0; a < 3; a++) fn[i + a] = (float)(o[a] * inv);
-    }
+    for (std::vector<float>* nn : {&fn, &vn})  // face normals, then vertex normals (polygon.h:749-783)
+      for (size_t i = 0; i < nn->size(); i += 3) {
+        float* x = nn->data() + i;
+        const double n[3] = {x[0], x[1], x[2]};
+        double o[3];
+        apply(g, n, o);
+        const double inv = 1.0 / std::sqrt((o[0] * o[0] + o[2] * o[2]) + o[1] * o[1]);
+        for (int a = 0; a < 3; a++) x[a] = (float)(o[a] * inv);
+      }
   }
 }
 
@@ -866,16 +889,32 @@ class Loader {
       }
     }
     if (e.type == PR_ENT_POLYGON) {
-      std::vector<float> fn;
-      if (!mesh.vn.empty())
+      // Obj's normals are made at load (ObjLoader.cpp:493), then moved with
+      // the vertices (Polygon::MatrixTransformation)
+      std::vector<float> fn, vn;
+      std::vector<int32_t> fvn;
+      const int nf = (int)(mesh.f.size() / 3);
+      if (!mesh.vn.empty()) {
         face_normals_from_vn(mesh, fn);
-      else if (!ms.empty())
-        pr::face_normals(mesh.v.data(), mesh.f.data(), (int)(mesh.f.size() / 3), fn);
-      transform_mesh(ms, mesh.v, fn);
+        vn = mesh.vn;
+        fvn = mesh.nid;
+      } else if (!ms.empty()) {
+        pr::face_normals(mesh.v.data(), mesh.f.data(), nf, fn);
+        if (e.smooth) {
+          pr::vertex_normals(mesh.v.data(), mesh.f.data(), nf, (int)(mesh.v.size() / 3), vn);
+          fvn = mesh.f;
+        }
+      }
+      transform_mesh(ms, mesh.v, fn, vn);
+      if (tx.tex_alpha) fail("a 32-bit texture with transparent texels on a mesh (the reference's alpha test) is not rendered here");
       e.mesh = (int)S_.verts.size();
       S_.verts.push_back(std::move(mesh.v));
       S_.faces.push_back(std::move(mesh.f));
       S_.fnormals.push_back(std::move(fn));
+      S_.vnormals.push_back(std::move(vn));
+      S_.face_vn.push_back(std::move(fvn));
+      S_.uvs.push_back(std::move(mesh.vt));
+      S_.face_uv.push_back(std::move(mesh.tid));
     }
     e.material = (int)S_.mats.size();
     S_.mats.push_back(m);
@@ -891,12 +930,20 @@ class Loader {
   struct ObjTex {
     std::vector<uint8_t> tex8, ibl8, bump8;
     std::vector<float> iblf;
+    bool tex_alpha = false;  // the texture has texels with alpha below 255 (read by mesh hits)
   };
   bool texture_line(const std::string& b, const std::vector<std::string>& bt, pr_material& m, ObjTex& tx) {
     const std::string& k = bt[0];
     if (k == "texture" && bt.size() >= 2) {
       int w = 0, h = 0;
-      read_bmp(resolve(b.substr(8), sdir_), 3, tx.tex8, w, h);
+      std::vector<uint8_t> rgba;
+      read_bmp(resolve(b.substr(8), sdir_), 4, rgba, w, h);
+      tx.tex8.resize(3 * (size_t)w * h);
+      tx.tex_alpha = false;
+      for (size_t q = 0; q < (size_t)w * h; q++) {
+        for (int a = 0; a < 3; a++) tx.tex8[3 * q + a] = rgba[4 * q + a];
+        tx.tex_alpha |= rgba[4 * q + 3] != 255;
+      }
       m.texture_width = w;
       m.texture_height = h;
     } else if (k == "ibl_texture" && bt.size() >= 2) {
@@ -1073,7 +1120,9 @@ class Loader {
     } else if (k == "spot_attenuation") {
       const std::vector<double> v = num_.many(after_key(b), 3);
       for (int i = 0; i < 3; i++) e.spot_attenuation[i] = v[i];
-    } else if (among(k, {"background", "smooth", "shadow"})) {
+    } else if (k == "smooth") {
+      scan(after_key(b), "%d", e.smooth);  // sscanf "smooth %d" (scene_env.h:1195-1198)
+    } else if (among(k, {"background", "shadow"})) {
       int on = 0;
       scan(after_key(b), "%d", on);
       if (on != 0) refuse(b);
@@ -1159,6 +1208,16 @@ class Loader {
       mm.vertices = S_.verts[i].data();
       mm.faces = S_.faces[i].data();
       mm.face_normals = S_.fnormals[i].empty() ? nullptr : S_.fnormals[i].data();
+      if (!S_.vnormals[i].empty()) {
+        mm.n_vertex_normals = (int32_t)(S_.vnormals[i].size() / 3);
+        mm.vertex_normals = S_.vnormals[i].data();
+        mm.face_vn = S_.face_vn[i].data();
+      }
+      if (!S_.uvs[i].empty() && !S_.face_uv[i].empty()) {
+        mm.n_uv = (int32_t)(S_.uvs[i].size() / 2);
+        mm.uv = S_.uvs[i].data();
+        mm.face_uv = S_.face_uv[i].data();
+      }
     }
     pr_scene_desc& d = S_.desc;
     memset(&d, 0, sizeof(d));

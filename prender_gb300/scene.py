@@ -195,6 +195,7 @@ class Entity:
     spot_attenuation: Sequence[float] = (0.0, 0.0, 1.0)
     light_dir_text: Optional[Sequence[float]] = field(default=None, compare=False, repr=False)
     hemisphere: int = 0
+    smooth: int = 0  # meshes: 'smooth 1', normals interpolated from the vertex normals
 
     def to_c(self) -> A.pr_entity:
         e = A.pr_entity()
@@ -213,6 +214,7 @@ class Entity:
         e.spot_angle[:] = [float(x) for x in self.spot_angle]
         e.spot_falloff = float(self.spot_falloff)
         e.spot_attenuation[:] = [float(x) for x in self.spot_attenuation]
+        e.smooth = int(self.smooth)
         return e
 
 
@@ -232,6 +234,16 @@ class Mesh:
     # rule from the vertices (an OBJ file with vertex normals, or a mesh
     # moved by rotation / scale, carries its own)
     face_normals: Optional[np.ndarray] = None
+    # vn lines (k, 3) float32 with their ids per face (m, 3); None: a smooth
+    # entity derives them with the loader's rule from the vertices.  Given
+    # vertex normals also decide the face normals (the normalised mean of a
+    # face's three, ObjLoader.cpp:617-641) unless face_normals is given.
+    vertex_normals: Optional[np.ndarray] = None
+    face_vn: Optional[np.ndarray] = None
+    # vt lines (k, 2) float32 with their ids per face (m, 3): where textures
+    # and IBL images land on the mesh
+    uv: Optional[np.ndarray] = None
+    face_uv: Optional[np.ndarray] = None
 
     def __post_init__(self):
         self.vertices = np.ascontiguousarray(self.vertices, dtype=np.float32)
@@ -240,6 +252,15 @@ class Mesh:
             self.face_normals = np.ascontiguousarray(self.face_normals, dtype=np.float32).reshape(-1, 3)
             if self.face_normals.shape[0] != self.faces.shape[0]:
                 raise ValueError("face_normals needs one normal per face")
+        for arr, ids, k, what in (("vertex_normals", "face_vn", 3, "vertex normals"), ("uv", "face_uv", 2, "uv")):
+            a, i = getattr(self, arr), getattr(self, ids)
+            if (a is None) != (i is None):
+                raise ValueError(f"{what} need both the values and their face ids")
+            if a is not None:
+                setattr(self, arr, np.ascontiguousarray(a, dtype=np.float32).reshape(-1, k))
+                setattr(self, ids, np.ascontiguousarray(i, dtype=np.int32).reshape(-1, 3))
+                if getattr(self, ids).shape[0] != self.faces.shape[0]:
+                    raise ValueError(f"{what}: one id triple per face")
 
 
 @dataclass
@@ -326,6 +347,18 @@ class SceneDesc:
                 fn = np.ascontiguousarray(m.face_normals, dtype=np.float32)
                 self._mesh_arrays.append(fn)
                 pm.face_normals = fn.ctypes.data_as(C.POINTER(C.c_float))
+            if m.vertex_normals is not None:
+                vn, fv = m.vertex_normals, m.face_vn
+                self._mesh_arrays += [vn, fv]
+                pm.n_vertex_normals = vn.shape[0]
+                pm.vertex_normals = vn.ctypes.data_as(C.POINTER(C.c_float))
+                pm.face_vn = fv.ctypes.data_as(C.POINTER(C.c_int32))
+            if m.uv is not None:
+                uv, fu = m.uv, m.face_uv
+                self._mesh_arrays += [uv, fu]
+                pm.n_uv = uv.shape[0]
+                pm.uv = uv.ctypes.data_as(C.POINTER(C.c_float))
+                pm.face_uv = fu.ctypes.data_as(C.POINTER(C.c_int32))
             meshes.append(pm)
         self._meshes = (A.pr_mesh * max(1, len(meshes)))(*meshes)
         d = A.pr_scene_desc()
@@ -515,10 +548,12 @@ class Scene:
                          "texture_coef": tuple(float(x) for x in texture_coef),
                          "camera": None if camera is None else tuple(float(x) for x in camera)}
 
-    def add_mesh(self, vertices, faces, material: Material, normal_inverse: int = 1) -> int:
-        self.meshes.append(Mesh(vertices, faces))
+    def add_mesh(self, vertices, faces, material: Material, normal_inverse: int = 1, smooth: int = 0,
+                 vertex_normals=None, face_vn=None, uv=None, face_uv=None) -> int:
+        self.meshes.append(Mesh(vertices, faces, vertex_normals=vertex_normals, face_vn=face_vn, uv=uv,
+                                face_uv=face_uv))
         self.entities.append(Entity(A.PR_ENT_POLYGON, self._mat(material), normal_inverse,
-                                    mesh=len(self.meshes) - 1))
+                                    mesh=len(self.meshes) - 1, smooth=int(smooth)))
         return len(self.entities) - 1
 
     def to_desc(self) -> SceneDesc:
@@ -626,6 +661,8 @@ class Scene:
                 objname = f"mesh{e.mesh}.obj"
                 _write_obj(os.path.join(directory, objname), self.meshes[e.mesh])
                 out.append(f"objfile {os.path.join(directory, objname)}")
+                if e.smooth:
+                    out.append(f"smooth {int(e.smooth)}")
             else:
                 raise ValueError("entity type has no reference writer")
             if m.type in (A.PR_MAT_REFRACTION, A.PR_MAT_SSS_REFRACTION) and m.refractive_index != 1.5:
@@ -813,5 +850,21 @@ def _write_obj(path: str, mesh: Mesh) -> None:
     with open(path, "w", newline="\n") as fh:
         for v in mesh.vertices:
             fh.write("v %.9g %.9g %.9g\n" % (float(v[0]), float(v[1]), float(v[2])))
-        for f in mesh.faces:
-            fh.write("f %d %d %d\n" % (int(f[0]) + 1, int(f[1]) + 1, int(f[2]) + 1))
+        if mesh.vertex_normals is not None:
+            for n in mesh.vertex_normals:
+                fh.write("vn %.9g %.9g %.9g\n" % (float(n[0]), float(n[1]), float(n[2])))
+        if mesh.uv is not None:
+            for t in mesh.uv:
+                fh.write("vt %.9g %.9g\n" % (float(t[0]), float(t[1])))
+        for q, f in enumerate(mesh.faces):
+            corners = []
+            for k in range(3):
+                c = "%d" % (int(f[k]) + 1)
+                if mesh.uv is not None and mesh.vertex_normals is not None:
+                    c += "/%d/%d" % (int(mesh.face_uv[q][k]) + 1, int(mesh.face_vn[q][k]) + 1)
+                elif mesh.vertex_normals is not None:
+                    c += "//%d" % (int(mesh.face_vn[q][k]) + 1)
+                elif mesh.uv is not None:
+                    c += "/%d" % (int(mesh.face_uv[q][k]) + 1)
+                corners.append(c)
+            fh.write("f %s\n" % " ".join(corners))

@@ -103,7 +103,7 @@ def load(path: str) -> Scene:
                 radius_inner=float(e.radius_inner), blackhole_disk=int(e.blackhole_disk),
                 parallel_light=int(e.parallel_light), spot_light=int(e.spot_light), light_dir=_v(e.light_dir),
                 spot_angle=_v(e.spot_angle, 2), spot_falloff=float(e.spot_falloff),
-                spot_attenuation=_v(e.spot_attenuation), hemisphere=int(e.hemisphere)))
+                spot_attenuation=_v(e.spot_attenuation), hemisphere=int(e.hemisphere), smooth=int(e.smooth)))
         for i in range(d.n_meshes):
             pm = d.meshes[i]
             v = np.ctypeslib.as_array(pm.vertices, shape=(pm.n_vertices * 3,)).reshape(-1, 3).copy()
@@ -111,7 +111,14 @@ def load(path: str) -> Scene:
             fn = None
             if pm.face_normals:
                 fn = np.ctypeslib.as_array(pm.face_normals, shape=(pm.n_faces * 3,)).reshape(-1, 3).copy()
-            s.meshes.append(Mesh(v, fc, fn))
+            vn = fvn = uv = fuv = None
+            if pm.vertex_normals and pm.face_vn:
+                vn = np.ctypeslib.as_array(pm.vertex_normals, shape=(pm.n_vertex_normals * 3,)).reshape(-1, 3).copy()
+                fvn = np.ctypeslib.as_array(pm.face_vn, shape=(pm.n_faces * 3,)).reshape(-1, 3).copy()
+            if pm.uv and pm.face_uv:
+                uv = np.ctypeslib.as_array(pm.uv, shape=(pm.n_uv * 2,)).reshape(-1, 2).copy()
+                fuv = np.ctypeslib.as_array(pm.face_uv, shape=(pm.n_faces * 3,)).reshape(-1, 3).copy()
+            s.meshes.append(Mesh(v, fc, fn, vertex_normals=vn, face_vn=fvn, uv=uv, face_uv=fuv))
         s.background = _v(d.background)
         s.environment_light = _v(d.environment_light)
         s.participating_media = int(d.participating_media)

@@ -23,7 +23,9 @@ of a seeded image; --textures-only and --textures-oracle do the same for the
 texture and image-based-lighting scenes (textures_render.npz,
 textures_oracle.npz); --wormhole-only writes the reference's one-thread
 wormhole renders (wormhole_render.npz), --wormhole-oracle the oracle's
-16 batches of each wormhole scene (wormhole_oracle.npz).
+16 batches of each wormhole scene (wormhole_oracle.npz); --meshtex-only and
+--meshtex-oracle do the same for smooth and textured meshes
+(meshtex_render.npz, meshtex_oracle.npz).
 --scene-files-only writes the meshes and textures that the scene files in
 scene_files/ name, and scene_files.npz from the reference's renders of them.
 """
@@ -408,6 +410,44 @@ def textures_golden(d):
     np.savez_compressed(os.path.join(HERE, "textures_render.npz"), **out)
 
 
+def meshtex_golden(d):
+    """smooth and textured meshes rendered by the reference, one thread (bit-exact)"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import meshtex_cases
+    out = {}
+    for name, sc in meshtex_cases.one_thread_cases().items():
+        dd = os.path.join(d, "m_" + name)
+        os.makedirs(dd)
+        img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+        out[name] = img
+        print("meshtex", name, info, float(img.mean()))
+    np.savez_compressed(os.path.join(HERE, "meshtex_render.npz"), **out)
+
+
+def meshtex_oracle_golden(nb=16):
+    """16 independent 256-spp renders of each smooth / textured mesh scene
+    by the oracle (pinned bit-exact to the reference by meshtex_render.npz):
+    per-pixel mean and spread"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import meshtex_cases
+    from oracle import oracle as O
+    out = {}
+    for name in meshtex_cases.CASES:
+        sc = meshtex_cases.highspp_case(name)
+        o = O.OracleScene(sc)
+        imgs = []
+        for k in range(nb):
+            sc.settings.seed = 100 + k
+            img, _, _ = o.render(threads=os.cpu_count(), settings=sc.settings)
+            imgs.append(img)
+        b = np.stack(imgs)
+        out[f"{name}_mean"] = b.mean(0).astype(np.float32)
+        out[f"{name}_sd"] = b.std(0, ddof=1).astype(np.float32)
+        print("meshtex oracle", name, float(b.mean()))
+    out["batches"] = np.int32(nb)
+    np.savez_compressed(os.path.join(HERE, "meshtex_oracle.npz"), **out)
+
+
 def textures_oracle_golden(nb=16):
     """16 independent 256-spp renders of each texture scene by the oracle
     (pinned bit-exact to the reference by textures_render.npz): per-pixel
@@ -594,7 +634,7 @@ KNOWN_FLAGS = {"--kerr-only", "--disk-only", "--sss-only", "--sss-l1-only", "--g
                "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle", "--scene-files-only", "--media-only",
                "--media-oracle", "--mesh7-oracle", "--batch-only", "--batch-oracle", "--hdr-only",
                "--lights-only", "--lights-oracle", "--textures-only", "--textures-oracle", "--wormhole-only",
-               "--wormhole-oracle"}
+               "--wormhole-oracle", "--meshtex-only", "--meshtex-oracle"}
 
 
 def main():
@@ -612,6 +652,9 @@ def main():
         return
     if "--wormhole-oracle" in sys.argv:
         wormhole_oracle_golden()
+        return
+    if "--meshtex-oracle" in sys.argv:
+        meshtex_oracle_golden()
         return
     if "--mesh7-oracle" in sys.argv:
         mesh7_oracle_golden()
@@ -650,6 +693,10 @@ def main():
     if "--wormhole-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             wormhole_golden(d)
+        return
+    if "--meshtex-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            meshtex_golden(d)
         return
     if "--textures-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:

@@ -151,6 +151,20 @@ def test_texture_render_one_thread_bit_exact(golden, name):
     assert ref.mean() > 0
 
 
+@pytest.mark.parametrize("name", ["smooth", "smooth_nonee", "mesh_tex", "mesh_tex_nonee"])
+def test_mesh_smooth_and_texture_render_one_thread_bit_exact(golden, name):
+    # 'smooth 1' meshes (vertex normals by the loader's rule and from vn
+    # lines, glass, normal -1), textured meshes through vt lines (a texture
+    # on diffuse and Phong meshes, an IBL image, a bump map that the mesh
+    # hit drops), NEE on and off
+    import meshtex_cases
+    sc = meshtex_cases.one_thread_cases()[name]
+    img, _, _ = O.OracleScene(sc).render(threads=1)
+    ref = golden["meshtex_render"][name]
+    assert np.array_equal(img, ref)
+    assert ref.mean() > 0
+
+
 @pytest.mark.parametrize("name", ["worm_bg", "worm_objects", "worm_sign"])
 def test_wormhole_render_one_thread_bit_exact(golden, name):
     # the Dneg wormhole: both backgrounds seen through the throat, objects

@@ -60,6 +60,8 @@ def _written_cases():
     out.update({"tex_" + k: v for k, v in texture_cases.one_thread_cases().items()})
     import wormhole_cases
     out.update(wormhole_cases.one_thread_cases())
+    import meshtex_cases
+    out.update({"meshtex_" + k: v for k, v in meshtex_cases.one_thread_cases().items()})
     return out
 
 
@@ -72,7 +74,13 @@ def test_written_scene_reads_back_the_same(tmp_path, name):
     assert len(back.meshes) == len(s.meshes)
     for a, b in zip(back.meshes, s.meshes):
         assert np.array_equal(a.vertices, b.vertices) and np.array_equal(a.faces, b.faces)
-        assert a.face_normals is None
+        for f in ("vertex_normals", "face_vn", "uv", "face_uv"):
+            x, y = getattr(a, f), getattr(b, f)
+            assert (x is None) == (y is None), f
+            if x is not None:
+                assert np.array_equal(x, y), f
+        # a mesh with vn lines gets its face normals from them in the reader
+        assert (a.face_normals is None) == (b.vertex_normals is None)
     assert back.background == tuple(s.background) and back.environment_light == tuple(s.environment_light)
     assert back.participating_media == int(s.participating_media and s.settings.media)
     assert back.medium == s.medium
@@ -131,6 +139,45 @@ def test_texture_files_render_like_the_reference(tmp_path, golden, name):
     assert np.array_equal(img, golden["textures_render"][name])
 
 
+@pytest.mark.parametrize("name", ["smooth", "smooth_nonee", "mesh_tex", "mesh_tex_nonee"])
+def test_mesh_texture_files_render_like_the_reference(tmp_path, golden, name):
+    # the files the reference rendered for meshtex_render.npz (OBJ vn / vt
+    # lines and their face ids, 'smooth 1', textures, IBL images and bump
+    # maps on meshes), read by this library's reader and rendered by the oracle
+    import meshtex_cases
+    sc = meshtex_cases.one_thread_cases()[name]
+    s = scene_file.load(sc.write_reference(str(tmp_path)))
+    assert [e.smooth for e in s.entities] == [e.smooth for e in sc.entities]
+    img, _, _ = O.OracleScene(s).render(threads=1)
+    assert np.array_equal(img, golden["meshtex_render"][name])
+
+
+def test_obj_texture_ids_quads_and_transforms(tmp_path):
+    # quads split as (a, b, c), (c, d, a) with their vt and vn ids alike;
+    # faces without ids take id 0; vt lines make texture ids, none make none;
+    # rotation moves the vn lines with the vertices; a smooth mesh without vn
+    # lines under a transform gets the loader's vertex normals, moved
+    obj = ("v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nvt 0 0\nvt 1 0\nvt 1 1\nvt 0 1\n"
+           "vn 0 0 1\nvn 0 1 0\nf 1/1/1 2/2/1 3/3/2 4/4/2\nf 1//2 3//1 4//2\n")
+    (tmp_path / "q.obj").write_text(obj)
+    s = scene_file.load(_scene(tmp_path, "OBJECT\nobjfile q.obj\nsmooth 1\nrotation 90 0 0\n\n"))
+    m = s.meshes[0]
+    assert m.faces.tolist() == [[0, 1, 2], [2, 3, 0], [0, 2, 3]]
+    assert m.face_uv.tolist() == [[0, 1, 2], [2, 3, 0], [0, 0, 0]]
+    assert m.face_vn.tolist() == [[0, 0, 1], [1, 1, 0], [1, 0, 1]]
+    assert np.allclose(m.vertex_normals[1], (0, 0, 1), atol=1e-6)  # +y turned to +z by 90 degrees about x
+    assert s.entities[0].smooth == 1
+    (tmp_path / "p.obj").write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nv 0 0 1\nf 1 2 3\nf 1 4 2\n")
+    s = scene_file.load(_scene(tmp_path, "OBJECT\nobjfile p.obj\nsmooth 1\ntranslate 1 2 3\n\n"))
+    m = s.meshes[0]
+    assert m.uv is None and m.face_vn.tolist() == m.faces.tolist()
+    # vertex 0 joins the faces of normals +z and +y: the mean (0, 1, 1) / 2, normalised
+    assert np.allclose(m.vertex_normals[0], (0, 2 ** -0.5, 2 ** -0.5), atol=1e-6)
+    (tmp_path / "c.obj").write_text("v 0 0 0 1 0 0\nv 1 0 0 1 0 0\nv 0 1 0 1 0 0\nf 1 2 3\n")
+    with pytest.raises(scene_file.SceneFileError, match="vertex colours"):
+        scene_file.load(_scene(tmp_path, "OBJECT\nobjfile c.obj\n\n"))
+
+
 @pytest.mark.parametrize("name", ["worm_bg", "worm_objects", "worm_sign"])
 def test_wormhole_files_render_like_the_reference(tmp_path, golden, name):
     # the files the reference rendered for wormhole_render.npz (the WORMHOLE
@@ -174,7 +221,8 @@ def test_hdr_reader_rows_and_values(tmp_path):
 
 
 @pytest.mark.parametrize("body,code,msg", [
-    ("disk 0 10 0 1\nnormal 0 -1 0\ntexture TEX\n", A.PR_E_UNSUPPORTED, "spheres, hemispheres and uvplanes"),
+    ("disk 0 10 0 1\nnormal 0 -1 0\ntexture TEX\n", A.PR_E_UNSUPPORTED, "spheres, hemispheres, uvplanes and meshes"),
+    ("objfile OBJ\ntexture TEX\n", A.PR_E_UNSUPPORTED, "needs texture coordinates"),
     ("sphere 0 10 0 1\nemission 1 1 1\nibl_texture TEX\n", A.PR_E_UNSUPPORTED, "IBL image"),
     ("hemisphere 0 10 0 1\nemission 1 1 1\n", A.PR_E_UNSUPPORTED, "hemispheres that emit"),
 ])
@@ -183,6 +231,11 @@ def test_textures_refused_where_not_rendered(tmp_path, body, code, msg):
     from prender_gb300.scene import _write_bmp24
     _write_bmp24(str(tmp_path / "t.bmp"), np.full((4, 4, 3), 200, np.uint8))
     body = body.replace("TEX", str(tmp_path / "t.bmp"))
+    from prender_gb300.scenes import icosphere
+    v, f = icosphere(1)  # a mesh without vt lines
+    (tmp_path / "m.obj").write_text("".join("v %r %r %r\n" % tuple(map(float, x)) for x in v) +
+                                    "".join("f %d %d %d\n" % tuple(int(i) + 1 for i in x) for x in f))
+    body = body.replace("OBJ", str(tmp_path / "m.obj"))
     text = "IMAGE\n8 6\n\nOBJECT\n" + body + "color 0 0 0\nreflection diffuse\n\n"
     s = scene_file.load(_scene(tmp_path, text))
     with pytest.raises(gpu.PrenderError) as e:
@@ -292,7 +345,6 @@ def test_bad_values_are_errors_with_the_line(tmp_path, body, msg):
 
 
 @pytest.mark.parametrize("body", [
-    "OBJECT\nsphere 0 0 0 1\nsmooth 1\n\n",
     "OBJECT\nsphere 0 0 0 1\nMATERIAL_SYMBOL\nKetchup\n\n",
     "OBJECT\nsphere 0 0 0 1\nreflection reflection1\n1 2 3 4 5 6\n\n",
     "OBJECT\nplane 0 0 0\nnormal 0 1 0\n\n",
