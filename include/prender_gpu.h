@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define PR_ABI_VERSION 6
+#define PR_ABI_VERSION 7
 
 /* ---- status codes --------------------------------------------------- */
 enum {
@@ -298,7 +298,15 @@ typedef struct pr_camera {
 } pr_camera;
 
 /* render modes */
-enum { PR_MODE_MEGAKERNEL = 0, PR_MODE_WAVEFRONT = 1 };
+/* PR_MODE_MLT: primary-sample-space Metropolis light transport
+ * (Render::RunMLT, render.h:363-785; Kelemen et al. 2002) over the same
+ * radiance estimator: many independent chains on the GPU sharing one
+ * bootstrap (W H pre_sample x samples seed paths; b their mean luminance),
+ * each started from a seed drawn by luminance and running its share of the
+ * samples x W x H x mutation mutations (p_large 0.5, Kelemen's weights); the
+ * tent filter and the x 1/4 sensor scale of the reference's MLT set-up
+ * apply; no luminance clamp. */
+enum { PR_MODE_MEGAKERNEL = 0, PR_MODE_WAVEFRONT = 1, PR_MODE_MLT = 2 };
 
 /* Render::Run (render.h:1125-1455) parameters. */
 typedef struct pr_render_params {
@@ -321,6 +329,12 @@ typedef struct pr_render_params {
                                  weight 1/total_spp and so the luminance
                                  clamp (render.h:1139, :1375-1384)          */
   int32_t pad1;
+  double mlt_mutation;        /* PR_MODE_MLT: mutations per pixel and chain
+                                 ('mutation', default 2)                     */
+  double mlt_pre_sample;      /* seed paths per pixel and chain ('pre_sample',
+                                 default 0.4)                                */
+  int32_t mlt_chains;         /* GPU chains (0: enough to fill the device)   */
+  int32_t pad2;
 } pr_render_params;
 
 enum {

@@ -48,6 +48,7 @@ def lib():
         L.oracle_render_rows.argtypes = [vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp]
         L.oracle_light_count.argtypes = [vp]
         L.oracle_kerr_trace.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.oracle_render_mlt.argtypes = [vp, vp, vp, C.c_double, C.c_double, vp]
         L.oracle_wormhole_trace.argtypes = [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp, vp]
         L.oracle_kerr_trace_threads.argtypes = [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]
         L.oracle_kerr_disk_shade.argtypes = [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp]
@@ -118,6 +119,18 @@ class OracleScene:
                                  C.byref(secs), C.byref(segs))
         assert rc == 0, rc
         return img, secs.value, segs.value
+
+    def render_mlt(self, settings=None):
+        """Render::RunMLT on one thread (the reference's chains in order);
+        settings.samples chains of settings.mutation / pre_sample per pixel."""
+        st = settings or self.scene.settings
+        cam = self.scene.camera.to_c()
+        prm = st.to_c()
+        img = np.zeros((cam.height, cam.width, 3), np.float64)
+        rc = lib().oracle_render_mlt(self.h, C.byref(cam), C.byref(prm), float(st.mutation), float(st.pre_sample),
+                                     _p(img))
+        assert rc == 0, rc
+        return img
 
     def render_rows(self, rows, threads: int = 1, settings=None):
         """Render::Run over the given image rows only (the rest stays zero)."""

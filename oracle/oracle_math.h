@@ -65,9 +65,19 @@ inline void onb(V3 n, V3& w, V3& u, V3& v) {
   v = normalize(cross(w, u));
 }
 
+// The Random interface radiance() draws from (random.h:16-23): a stream
+// generator, or the Metropolis sampler's primary samples (mlt.h:86-168).
+struct Sampler {
+  virtual double next01() = 0;
+  // Random::Next01: the stream itself even under MLT (KelemenMLT::Next01,
+  // mlt.h:166), which the light choice and the surface NEE point draw from
+  virtual double Next01() { return next01(); }
+  virtual ~Sampler() {}
+};
+
 // MT19937-64 (Matsumoto & Nishimura), the generator behind the reference's
 // MTRandom (random.h:73-186, random.cpp:204-311); next01 is genrand64_real1.
-struct MT64 {
+struct MT64 : Sampler {
   static constexpr int NN = 312, MM = 156;
   uint64_t mt[NN];
   int mti = NN + 1;
@@ -102,7 +112,7 @@ struct MT64 {
     x ^= (x >> 43);
     return x;
   }
-  double next01() { return (double)(next_u64() >> 11) * (1.0 / 9007199254740991.0); }
+  double next01() override { return (double)(next_u64() >> 11) * (1.0 / 9007199254740991.0); }
 };
 
 }  // namespace orc

@@ -1279,7 +1279,7 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
 // --------------------------------------------------------------- radiance
 struct Ctx {
   const Scene& s;
-  MT64& rnd;
+  Sampler& rnd;
   int nee, media;
   int depth_cfg, depth_limit;
   int hg_correct;
@@ -1289,7 +1289,7 @@ V3 radiance(Ctx& c, V3 org, V3 dir, int depth);
 
 // LightList::randomLight (light.h:132-155): probability reported as 1
 const Light& random_light(Ctx& c) {
-  const double next = c.rnd.next01();
+  const double next = c.rnd.Next01();
   const int n = (int)c.s.lights.size();
   int index = (int)((next) * (double)(n - 1) + 0.5);
   if (index >= n) index = n - 1;
@@ -1403,14 +1403,14 @@ V3 direct_sample(Ctx& c, const Light& light, const Hit& v0, V3 orienting_normal,
   V3 light_pos;  // an infinity light draws no point (light_pos stays zero)
   if (light.infinity) return eval_direct(c, light, v0, orienting_normal, light_pos, depth, brdf, ray_dir);
   const Entity& le = c.s.ents[light.entity];
-  if (le.type == PR_ENT_SPHERE) {
-    const double r1 = TWOPI * c.rnd.next01();
-    const double r2 = 1.0 - 2.0 * c.rnd.next01();
+  if (le.type == PR_ENT_SPHERE) {  // rnd->Next01() (directLight_radiance.h:343-360)
+    const double r1 = TWOPI * c.rnd.Next01();
+    const double r2 = 1.0 - 2.0 * c.rnd.Next01();
     const double sq = std::sqrt(1.0 - r2 * r2);
     light_pos = le.position + ((le.radius + EPS) * V3(sq * std::cos(r1), sq * std::sin(r1), r2));
   } else if (le.type == PR_ENT_UVPLANE) {
-    const double t = le.v_length * c.rnd.next01();
-    const double s = le.u_length * c.rnd.next01();
+    const double t = le.v_length * c.rnd.Next01();
+    const double s = le.u_length * c.rnd.Next01();
     light_pos = le.org + le.u_axis * s + le.v_axis * t + le.normal * EPS;
   }
   return eval_direct(c, light, v0, orienting_normal, light_pos, depth, brdf, ray_dir);
@@ -2493,6 +2493,242 @@ static int render_rows(OracleScene* o, const pr_camera* cam, const pr_render_par
   if (segments) *segments = seg_total.load();
   for (size_t i = 0; i < img.size(); i++) {
     image[3 * i] = img[i].x; image[3 * i + 1] = img[i].y; image[3 * i + 2] = img[i].z;
+  }
+  return PR_OK;
+}
+
+// ---------------------------------------------------------------- PSSMLT
+}  // extern "C"
+
+namespace {
+
+// Mutate0 (mlt.h:40-53): the step from LuxRender, |2r - 1| through fabsf
+double mlt_mutate0(MT64& rnd, double x) {
+  const double r = rnd.next01();
+  const double s1 = 1.0 / 512.0, s2 = 1.0 / 16.0;
+  const double dx = s1 / (s1 / s2 + (double)std::fabs((float)(2.0 * r - 1.0))) - s1 / (s1 / s2 + 1.0);
+  if (r < 0.5) {
+    const double x1 = x + dx;
+    return (x1 < 1.0) ? x1 : x1 - 1.0;
+  }
+  const double x1 = x - dx;
+  return (x1 < 0.0) ? x1 + 1.0 : x1;
+}
+
+// KelemenMLT (mlt.h:86-168): primary samples with lazy mutation, a stack
+// of the values a rejected proposal restores; every draw of the
+// primary-sample generator (construction, growth, mutations) comes from the
+// thread's MTRandom, as random() returns it
+struct KelemenSampler : Sampler {
+  struct PS {
+    int modify_time = 0;
+    double value = 0.0;
+  };
+  MT64& rnd;
+  int global_time = 0, large_step = 0, large_step_time = 0, used = 0;
+  std::vector<PS> ps;
+  std::vector<PS> stack;
+  explicit KelemenSampler(MT64& r) : rnd(r) { grow(128); }
+  double Next01() override { return rnd.next01(); }
+  void grow(size_t n) {  // vector::resize: each new PrimarySample draws its value
+    const size_t old = ps.size();
+    ps.resize(n);
+    for (size_t i = old; i < n; i++) {
+      ps[i].modify_time = 0;
+      ps[i].value = rnd.next01();
+    }
+  }
+  double next01() override {
+    if (ps.size() <= (size_t)used) grow((size_t)(ps.size() * 1.5));
+    PS& p = ps[(size_t)used];
+    if (p.modify_time < global_time) {
+      if (large_step > 0) {
+        stack.push_back(p);
+        p.modify_time = global_time;
+        p.value = rnd.next01();
+      } else {
+        if (p.modify_time < large_step_time) {
+          p.modify_time = large_step_time;
+          p.value = rnd.next01();
+        }
+        while (p.modify_time < global_time - 1) {
+          p.value = mlt_mutate0(rnd, p.value);
+          p.modify_time++;
+        }
+        stack.push_back(p);
+        p.value = mlt_mutate0(rnd, p.value);
+        p.modify_time = global_time;
+      }
+    }
+    used++;
+    return ps[(size_t)used - 1].value;
+  }
+  void restore() {
+    int idx = used - 1;
+    while (!stack.empty()) {
+      ps[(size_t)idx--] = stack.back();
+      stack.pop_back();
+    }
+  }
+};
+
+struct MltPath {  // PathSample (mlt.h:177-190)
+  int x = 0, y = 0;
+  double weight = 0.0;
+  V3 F;
+  bool cancel = true;
+};
+
+struct MltCamera {
+  V3 cpos, center, sx, sy;
+  double iw, ih;
+  int W, H;
+};
+
+// generate_new_path (render.h:195-357) with its image-plane branch off (the
+// `if (0 && ...)`): pixel and sub-pixel from primary samples, the tent
+// filter the MLT set-up forces, radiance() drawing from the sampler
+MltPath mlt_new_path(Ctx& c, KelemenSampler& k, const MltCamera& cam) {
+  double pdf = 1.0;
+  pdf *= cam.W;
+  pdf *= cam.H;
+  float x, y;
+  do {
+    x = (float)(k.next01() * cam.W);
+    y = (float)(k.next01() * cam.H);
+  } while (x < 0 || cam.W <= x || y < 0 || cam.H <= y);
+  const int xx = (int)x, yy = (int)y;
+  const int sxx = k.next01() < 0.5 ? 0 : 1;
+  const int syy = k.next01() < 0.5 ? 0 : 1;
+  const double rr1 = 2.0 * k.next01();
+  const double rr2 = 2.0 * k.next01();
+  const double dx = rr1 < 1.0 ? std::sqrt(rr1) - 1.0 : 1.0 - std::sqrt(2.0 - rr1);
+  const double dy = rr2 < 1.0 ? std::sqrt(rr2) - 1.0 : 1.0 - std::sqrt(2.0 - rr2);
+  pdf *= 4.0;
+  const double r1 = (sxx + 0.5 + dx) * 0.5;
+  const double r2 = (syy + 0.5 + dy) * 0.5;
+  const V3 sp = cam.center + cam.sx * ((r1 + xx) * cam.iw - 0.5) + cam.sy * ((r2 + yy) * cam.ih - 0.5);
+  const V3 dir = normalize(sp - cam.cpos);
+  MltPath p;
+  p.x = xx;
+  p.y = yy;
+  p.F = radiance(c, cam.cpos, dir, 0) * 1.0;
+  p.weight = pdf;
+  p.cancel = p.F.x == 0.0 && p.F.y == 0.0 && p.F.z == 0.0;
+  return p;
+}
+
+inline double mlt_luminance(V3 c) { return dot(V3(0.2126, 0.7152, 0.0722), c); }  // mlt.h:171-174
+
+}  // namespace
+
+extern "C" {
+
+// Render::RunMLT (render.h:363-785) on one thread: `samples` chains, each
+// with W H pre_sample seed paths (large steps), a start path drawn by
+// luminance (SPPMLTSamplingPath, mlt.h:201-219), b = their mean luminance,
+// and (int)(W H mutation) mutations with p_large 0.5 and Kelemen's weights
+// of the proposal and the current path; every chain's image is added up and
+// scaled by sensor_response / 4 (scene_env.h:1956) / samples.  The primary
+// samples' generator is MTRandom seeded prime_numbers[32] = 137.
+int oracle_render_mlt(void* h, const pr_camera* cam, const pr_render_params* prm, double mutation, double pre_sample,
+                      double* image) {
+  auto* o = static_cast<OracleScene*>(h);
+  if (!o || !cam || !prm || !image) return PR_E_ARG;
+  const Scene& s = o->s;
+  MltCamera mc;
+  mc.W = cam->width;
+  mc.H = cam->height;
+  mc.cpos = V3(cam->position[0], cam->position[1], cam->position[2]);
+  V3 cdir(cam->dir[0], cam->dir[1], cam->dir[2]);
+  const V3 cup(cam->up[0], cam->up[1], cam->up[2]);
+  double cam_phi = std::atan2(cdir.y, cdir.x);
+  if (cam_phi < 0.0) cam_phi += 2.0 * PI;
+  if (std::fabs(cam_phi - PI) < 1.0e-6 || cam_phi < 1.0e-6 || std::fabs(cam_phi - 2.0 * PI) < 1.0e-6) {
+    cdir.y += 1.0e-6;
+    const double len = std::sqrt(cdir.x * cdir.x + cdir.y * cdir.y + cdir.z * cdir.z);
+    cdir.x /= len; cdir.y /= len; cdir.z /= len;
+  }
+  const double sw = cam->screen_width * mc.W / mc.H;
+  mc.sx = normalize(cross(cdir, cup)) * sw;
+  mc.sy = normalize(cross(mc.sx, cdir)) * cam->screen_height;
+  mc.center = mc.cpos + cdir * cam->screen_dist;
+  mc.iw = 1.0 / mc.W;
+  mc.ih = 1.0 / mc.H;
+  const int size = mc.W * mc.H;
+  const int seeds = (int)(size * pre_sample);
+  const int M = (int)(size * mutation);
+  // the reference prints progress every seeds / 10 and M / 10 steps (a
+  // division by zero below ten)
+  if (seeds < 10 || M < 10 || prm->samples < 1) return PR_E_ARG;
+  MT64 rnd((uint64_t)(unsigned)137);
+  tl_disk_rnd = &rnd;
+  std::vector<V3> img((size_t)size);
+  for (int chain = 0; chain < prm->samples; chain++) {
+    std::vector<V3> tmp((size_t)size);
+    KelemenSampler k(rnd);
+    k.large_step = 1;
+    Ctx c{s, k, prm->nee, prm->media && s.media_on, prm->depth, prm->depth_limit,
+          (prm->flags & PR_FLAG_HG_CORRECT) != 0};
+    std::vector<MltPath> seed((size_t)seeds);
+    double sumI = 0.0;
+    for (int i = 0; i < seeds; i++) {
+      k.used = 0;
+      seed[(size_t)i] = mlt_new_path(c, k, mc);
+      k.global_time++;
+      k.stack.clear();
+      sumI += mlt_luminance(seed[(size_t)i].F);
+    }
+    if (sumI < 1.0e-14) continue;
+    auto pick = [&]() {
+      const double r = rnd.next01() * sumI;
+      int sel = (int)(rnd.next01() * seeds);
+      if (sel >= seeds) sel = seeds - 1;
+      double acc = 0.0;
+      for (int i = 0; i < seeds; i++) {
+        acc += mlt_luminance(seed[(size_t)i].F);
+        if (r <= acc) {
+          sel = i;
+          break;
+        }
+      }
+      return sel;
+    };
+    int sel = pick();
+    for (int q = 0; q < seeds && seed[(size_t)sel].cancel; q++) sel = pick();
+    const double b = sumI / seeds;
+    const double p_large = 0.5;
+    const double iM = 1.0 / M;
+    MltPath old = seed[(size_t)sel];
+    for (int i = 0; i < M; i++) {
+      k.used = 0;
+      k.large_step = (rnd.next01() < p_large) ? 1 : 0;
+      const MltPath np = mlt_new_path(c, k, mc);
+      const double Lnew = mlt_luminance(np.F), Lold = mlt_luminance(old.F);
+      double a = 1.0;
+      if (Lold > 1.0e-16) a = std::min(1.0, Lnew / Lold);
+      const double wn = (a + k.large_step) / (Lnew / b + p_large) * iM;
+      const double wo = (1.0 - a) / (Lold / b + p_large) * iM;
+      const size_t ni = (size_t)((mc.H - np.y - 1) * mc.W + np.x), oi = (size_t)((mc.H - old.y - 1) * mc.W + old.x);
+      tmp[oi] = tmp[oi] + wo * old.weight * old.F;
+      tmp[ni] = tmp[ni] + wn * np.weight * np.F;
+      if (rnd.next01() < a) {
+        old = np;
+        if (k.large_step) k.large_step_time = k.global_time;
+        k.global_time++;
+        k.stack.clear();
+      } else {
+        k.restore();
+      }
+    }
+    for (int i = 0; i < size; i++) img[(size_t)i] = img[(size_t)i] + tmp[(size_t)i];
+  }
+  const double w = 0.25 * prm->sensor_response / (double)prm->samples;
+  for (int i = 0; i < size; i++) {
+    const V3 v = img[(size_t)i] * w;
+    image[3 * i] = v.x;
+    image[3 * i + 1] = v.y;
+    image[3 * i + 2] = v.z;
   }
   return PR_OK;
 }

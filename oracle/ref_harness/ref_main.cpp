@@ -5,7 +5,9 @@
 // It runs the reference code unchanged and writes its results as raw binary
 // so that the Python tests can freeze golden fixtures from them.
 //
-//   prender_ref render   <scene.txt> <image.f64>          Render::Run() (render.h:1125)
+//   prender_ref render   <scene.txt> <image.f64>          Render::Run() (render.h:1125), or
+//                                                          Render::RunMLT() (render.h:363) for a
+//                                                          scene with metropolisTransport 1
 //   prender_ref firsthit <scene.txt> <rays.f64> <out.bin>  intersect_scene_ (scene.cpp:83)
 //                                                          + QBVH::CheckIntersection (QBVH.cpp:17)
 //   prender_ref qbvh     <scene.txt> <entity> <out.bin>    QBVH node + leaf arrays (QBVH.h:53)
@@ -29,6 +31,8 @@
 #include <vector>
 
 using namespace prender;
+
+void init_prime_numbers();  // QMC.cpp:7
 
 thread_local KerrProbe prender_kerr_probe;
 
@@ -70,7 +74,14 @@ int main(int argc, char** argv) {
     SceneEnv* env = load(argv[2]);
     Render r(*env);
     double t0 = omp_get_wtime();
-    r.Run();
+    if (env->metropolisTransport) {
+      // main.cpp:48, :193-196: RunMLT seeds its primary-sample generators
+      // from the prime table
+      ::init_prime_numbers();
+      r.RunMLT();
+    } else {
+      r.Run();
+    }
     double t1 = omp_get_wtime();
     int w = env->image_width, h = env->image_height;
     // Render's first two data members (render.h:163-164) are implicitly

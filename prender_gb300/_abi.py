@@ -40,6 +40,7 @@ PR_MAP_EQUIRECTANGULAR = 8
 
 PR_MODE_MEGAKERNEL = 0
 PR_MODE_WAVEFRONT = 1
+PR_MODE_MLT = 2
 
 PR_FLAG_HG_CORRECT = 1
 PR_FLAG_EXACT_HITS = 2
@@ -220,6 +221,10 @@ class pr_render_params(C.Structure):
         ("flags", C.c_int32),
         ("total_spp", C.c_int32),
         ("pad1", C.c_int32),
+        ("mlt_mutation", C.c_double),
+        ("mlt_pre_sample", C.c_double),
+        ("mlt_chains", C.c_int32),
+        ("pad2", C.c_int32),
     ]
 
 

@@ -614,7 +614,8 @@ class Loader {
   bool target_set_ = false, angle_set_ = false;
   double screen_[3] = {30.0, 30.0, 40.0}, angle_ = 0.0;
   int width_ = 320, height_ = 240, samples_ = 8, supersamples_ = 2, tent_ = 0, depth_ = 8, depth_limit_ = 64;
-  int nee_ = 0, participating_ = 0, use_temp_ = 0;
+  int nee_ = 0, participating_ = 0, use_temp_ = 0, mlt_ = 0;
+  double mutation_ = 2.0, pre_sample_ = 0.4;  // SceneEnv::Default (scene_env.h:312-313)
   float luminance_cutoff_ = 0.025f;  // a float in the reference (scene_env.h:221)
   double sensor_response_ = 1.0, doppler_ = 0.0;
   double background_[3] = {0, 0, 0}, envlight_[3] = {0, 0, 0};
@@ -721,7 +722,13 @@ class Loader {
       if (v[0] > 0.0) refuse("LENS " + std::to_string(v[0]));
     } else if (among(k, {"use_mollweide_projection", "special_relativity_effects"})) {
       if (num_.integer(r_.value(k)) != 0) refuse(k);
-    } else if (among(k, {"metropolisTransport", "energyRedistributionPathTracing"})) {
+    } else if (k == "metropolisTransport") {
+      scan(r_.value(k), "%d", mlt_);  // sscanf (scene_env.h:642-646)
+    } else if (k == "mutation") {
+      mutation_ = num_.one(r_.value(k));
+    } else if (k == "pre_sample") {
+      pre_sample_ = num_.one(r_.value(k));
+    } else if (among(k, {"energyRedistributionPathTracing"})) {
       int on = 0;
       scan(r_.value(k), "%d", on);
       if (on != 0) refuse(k);
@@ -736,7 +743,7 @@ class Loader {
           camera_ms_.push_back(translation(v[0], v[1], v[2]));
         }
       }
-    } else if (among(k, {"THREAD", "IMAGEDUMP", "TIMELIMIT", "mutation", "pre_sample"})) {
+    } else if (among(k, {"THREAD", "IMAGEDUMP", "TIMELIMIT"})) {
       (void)num_.one(r_.value(k));  // does not change the image
     } else if (among(k, {"OUTPUT", "mlt_r1r2", "velocity"})) {
       (void)r_.value(k);  // does not change the image rendered here
@@ -1190,6 +1197,17 @@ class Loader {
     p.depth_limit = depth_limit_;
     p.nee = nee_;
     p.mode = PR_MODE_MEGAKERNEL;
+    if (mlt_) {
+      // the MLT set-up (scene_env.h:1946-1957): default seeds and mutations
+      // for non-positive values, the tent filter; its 1/4 sensor scale is
+      // part of the PR_MODE_MLT estimator
+      p.mode = PR_MODE_MLT;
+      p.tent_filter = 1;
+      if (pre_sample_ <= 0.0) pre_sample_ = 0.4;
+      if (mutation_ <= 0.0) mutation_ = 32;
+    }
+    p.mlt_mutation = mutation_;
+    p.mlt_pre_sample = pre_sample_;
     p.luminance_cutoff = (double)luminance_cutoff_;
     p.sensor_response = sensor_response_;
     // participatingMedia is cleared when the global medium has no extinction

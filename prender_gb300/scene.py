@@ -309,6 +309,11 @@ class RenderSettings:
     max_path_vertices: int = 0
     flags: int = 0
     total_spp: int = 0
+    # PR_MODE_MLT (metropolisTransport): mutations and seed paths per pixel
+    # and chain (the reference's 'mutation' and 'pre_sample'), GPU chains
+    mutation: float = 2.0
+    pre_sample: float = 0.4
+    mlt_chains: int = 0
 
     def to_c(self) -> A.pr_render_params:
         p = A.pr_render_params()
@@ -318,6 +323,9 @@ class RenderSettings:
         p.seed = int(self.seed)
         p.luminance_cutoff = float(self.luminance_cutoff)
         p.sensor_response = float(self.sensor_response)
+        p.mlt_mutation = float(self.mutation)
+        p.mlt_pre_sample = float(self.pre_sample)
+        p.mlt_chains = int(self.mlt_chains)
         return p
 
     @property
@@ -582,6 +590,10 @@ class Scene:
             "luminance_cutoff", _fmt(st.luminance_cutoff), "",
             "sensor_response", _fmt(st.sensor_response), "",
             "nextEventEstimation", str(st.nee), "",
+            "metropolisTransport", str(1 if st.mode == A.PR_MODE_MLT else 0), "",
+            "mutation", _fmt(st.mutation), "",
+            "pre_sample", _fmt(st.pre_sample), "",
+            "IMAGEDUMP", "1000000", "",
             "participatingMedia", str(int(self.participating_media and st.media)), "",
             "CAMERA_POS", f3(cam.position), "",
             "CAMERA_DIR", f3(cam.dir), "",

@@ -148,7 +148,8 @@ def load(path: str) -> Scene:
         s.settings = RenderSettings(samples=prm.samples, supersamples=prm.supersamples, tent_filter=prm.tent_filter,
                                     depth=prm.depth, depth_limit=prm.depth_limit, nee=prm.nee, media=prm.media,
                                     mode=prm.mode, seed=int(prm.seed), luminance_cutoff=float(prm.luminance_cutoff),
-                                    sensor_response=float(prm.sensor_response))
+                                    sensor_response=float(prm.sensor_response), mutation=float(prm.mlt_mutation),
+                                    pre_sample=float(prm.mlt_pre_sample))
         s.gamma_offset = float(gamma.value)
         s.file_warnings = warnings
         return s

@@ -25,7 +25,8 @@ textures_oracle.npz); --wormhole-only writes the reference's one-thread
 wormhole renders (wormhole_render.npz), --wormhole-oracle the oracle's
 16 batches of each wormhole scene (wormhole_oracle.npz); --meshtex-only and
 --meshtex-oracle do the same for smooth and textured meshes
-(meshtex_render.npz, meshtex_oracle.npz).
+(meshtex_render.npz, meshtex_oracle.npz); --mlt-only writes the reference's
+one-thread Metropolis renders (mlt_render.npz).
 --scene-files-only writes the meshes and textures that the scene files in
 scene_files/ name, and scene_files.npz from the reference's renders of them.
 """
@@ -424,6 +425,20 @@ def meshtex_golden(d):
     np.savez_compressed(os.path.join(HERE, "meshtex_render.npz"), **out)
 
 
+def mlt_golden(d):
+    """Metropolis (RunMLT) renders by the reference, one thread (bit-exact)"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import mlt_cases
+    out = {}
+    for name, sc in mlt_cases.one_thread_cases().items():
+        dd = os.path.join(d, "l_" + name)
+        os.makedirs(dd)
+        img, info = ref_render(sc.write_reference(dd), (sc.camera.width, sc.camera.height), dd, threads=1)
+        out[name] = img
+        print("mlt", name, info, float(img.mean()))
+    np.savez_compressed(os.path.join(HERE, "mlt_render.npz"), **out)
+
+
 def meshtex_oracle_golden(nb=16):
     """16 independent 256-spp renders of each smooth / textured mesh scene
     by the oracle (pinned bit-exact to the reference by meshtex_render.npz):
@@ -634,7 +649,8 @@ KNOWN_FLAGS = {"--kerr-only", "--disk-only", "--sss-only", "--sss-l1-only", "--g
                "--sss-l1-oracle", "--disk-oracle", "--glossy-oracle", "--scene-files-only", "--media-only",
                "--media-oracle", "--mesh7-oracle", "--batch-only", "--batch-oracle", "--hdr-only",
                "--lights-only", "--lights-oracle", "--textures-only", "--textures-oracle", "--wormhole-only",
-               "--wormhole-oracle", "--meshtex-only", "--meshtex-oracle"}
+               "--wormhole-oracle", "--meshtex-only", "--meshtex-oracle",
+               "--mlt-only"}
 
 
 def main():
@@ -697,6 +713,10 @@ def main():
     if "--meshtex-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:
             meshtex_golden(d)
+        return
+    if "--mlt-only" in sys.argv:
+        with tempfile.TemporaryDirectory() as d:
+            mlt_golden(d)
         return
     if "--textures-only" in sys.argv:
         with tempfile.TemporaryDirectory() as d:

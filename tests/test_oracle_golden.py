@@ -151,6 +151,20 @@ def test_texture_render_one_thread_bit_exact(golden, name):
     assert ref.mean() > 0
 
 
+@pytest.mark.parametrize("name", ["mlt_spheres", "mlt_caustic", "mlt_glossy"])
+def test_mlt_render_one_thread_bit_exact(golden, name):
+    # Render::RunMLT: two Kelemen chains per scene (seed paths, luminance-
+    # drawn start, lazy small steps, large steps, the stack a rejection
+    # restores, the light choice and surface NEE points from the stream
+    # itself), NEE on and off, glossy lobes and a textured floor
+    import mlt_cases
+    sc = mlt_cases.one_thread_cases()[name]
+    img = O.OracleScene(sc).render_mlt()
+    ref = golden["mlt_render"][name]
+    assert np.array_equal(img, ref)
+    assert ref.mean() > 0
+
+
 @pytest.mark.parametrize("name", ["smooth", "smooth_nonee", "mesh_tex", "mesh_tex_nonee"])
 def test_mesh_smooth_and_texture_render_one_thread_bit_exact(golden, name):
     # 'smooth 1' meshes (vertex normals by the loader's rule and from vn

@@ -139,6 +139,20 @@ def test_texture_files_render_like_the_reference(tmp_path, golden, name):
     assert np.array_equal(img, golden["textures_render"][name])
 
 
+@pytest.mark.parametrize("name", ["mlt_spheres", "mlt_caustic", "mlt_glossy"])
+def test_mlt_files_render_like_the_reference(tmp_path, golden, name):
+    # the files the reference rendered with RunMLT for mlt_render.npz
+    # (metropolisTransport, mutation, pre_sample), read by this library's
+    # reader and rendered by the oracle's RunMLT
+    import mlt_cases
+    sc = mlt_cases.one_thread_cases()[name]
+    s = scene_file.load(sc.write_reference(str(tmp_path)))
+    assert s.settings.mode == A.PR_MODE_MLT and s.settings.tent_filter == 1
+    assert (s.settings.mutation, s.settings.pre_sample) == (sc.settings.mutation, sc.settings.pre_sample)
+    img = O.OracleScene(s).render_mlt()
+    assert np.array_equal(img, golden["mlt_render"][name])
+
+
 @pytest.mark.parametrize("name", ["smooth", "smooth_nonee", "mesh_tex", "mesh_tex_nonee"])
 def test_mesh_texture_files_render_like_the_reference(tmp_path, golden, name):
     # the files the reference rendered for meshtex_render.npz (OBJ vn / vt
@@ -352,7 +366,7 @@ def test_bad_values_are_errors_with_the_line(tmp_path, body, msg):
     "OBJECT\ndisk 0 0 0 1\nnormal 0 1 0\ntranslate 1 0 0\n\n",
     "OBJECT\nsphere 0 0 0 1\nreflection reflection\nreflection Subsurface_Scattering\n\n",
     "LENS\n0.5 100\n",
-    "metropolisTransport\n1\n",
+    "energyRedistributionPathTracing\n1\n",
     "BLACKHOLE\ninitial_condition 1\n\n",
 ])
 def test_features_not_rendered_here_are_refused(tmp_path, body):
