@@ -2410,6 +2410,8 @@ int oracle_render_rows(void* h, const pr_camera* cam, const pr_render_params* pr
   return render_rows(o, cam, prm, threads, r, image, seconds, segments);
 }
 
+constexpr int32_t kOracleTentSubpixels = 1 << 16;
+
 static int render_rows(OracleScene* o, const pr_camera* cam, const pr_render_params* prm, int threads,
                        const std::vector<int>& rows, double* image, double* seconds, uint64_t* segments) {
   const Scene& s = o->s;
@@ -2434,7 +2436,13 @@ static int render_rows(OracleScene* o, const pr_camera* cam, const pr_render_par
   const double iw = 1.0 / W, ih = 1.0 / H;
   int samples = prm->samples, ss = prm->supersamples;
   double rate = (1.0 / ss);
-  if (prm->tent_filter) { samples = samples * (ss * ss); ss = 1; rate = 0.5; }
+  // Render::Run folds the sub-pixels into the samples under the tent filter
+  // (render.h:1180-1186), which leaves every sample in sub-pixel (0, 0);
+  // kOracleTentSubpixels keeps the 2 x 2 sub-pixels instead, the footprint
+  // of generate_new_path (render.h:273-293): the expectation of the
+  // Metropolis image (a test-only switch of this oracle)
+  if (prm->tent_filter && !(prm->flags & kOracleTentSubpixels)) { samples = samples * (ss * ss); ss = 1; rate = 0.5; }
+  else if (prm->tent_filter) rate = 0.5;
   const double smp = 1.0 / samples / (ss * ss);
   const float cutoff = (float)prm->luminance_cutoff;
   std::vector<V3> img((size_t)W * H);

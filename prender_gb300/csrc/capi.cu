@@ -16,6 +16,7 @@
 #include "adjoint.h"
 #include "kerr.h"
 #include "wormhole.h"
+#include "mlt.h"
 #include "pr_internal.h"
 #include "render_kernels.h"
 #include "scene_build.h"
@@ -508,6 +509,13 @@ int pr::prepare_render(pr_ctx* c, const pr_camera* cam, const pr_render_params* 
     return fail(c, PR_E_UNSUPPORTED, "wormhole scenes render without next-event estimation and media");
   if (sc.dev.has_sss && (sc.kerr.enabled || sc.worm.enabled))
     return fail(c, PR_E_UNSUPPORTED, "subsurface (dipole) materials render in straight-ray scenes only");
+  if (p->mode == PR_MODE_MLT) {
+    if (sc.kerr.enabled || sc.worm.enabled)
+      return fail(c, PR_E_UNSUPPORTED, "Metropolis light transport traces straight rays only");
+    if (sc.dev.has_sss) return fail(c, PR_E_UNSUPPORTED, "Metropolis light transport does not cover subsurface materials");
+    if (!(p->mlt_mutation > 0.0) || !(p->mlt_pre_sample > 0.0) || p->mlt_chains < 0 || p->mlt_chains > (1 << 24))
+      return fail(c, PR_E_ARG, "Metropolis parameters: mutation and pre_sample must be positive, chains in 0..2^24");
+  }
   memset(&g, 0, sizeof(g));
   double dir[3] = {cam->dir[0], cam->dir[1], cam->dir[2]};
   double phi = std::atan2(dir[1], dir[0]);
@@ -587,6 +595,78 @@ static unsigned int wavefront_slots() {
   long v = e ? strtol(e, nullptr, 10) : 0;
   if (v < 1024 || v > (1L << 24)) v = 1L << 21;
   return (unsigned int)v;
+}
+
+// PR_MODE_MLT (Render::RunMLT's estimator as parallel chains, mlt.cu): the
+// bootstrap of samples x (int)(W H pre_sample) paths on the GPU, their
+// luminances read back for b and for the chains' starts (systematic
+// resampling in proportion to luminance), then samples x (int)(W H
+// mutation) mutations spread over the chains in launches of a few
+// iterations; the image is the chains' mean times the sensor response / 4.
+static int render_mlt(pr_ctx* c, const RenderCfg& g0, const pr_render_params* p, float* rgb_dev, int accumulate,
+                      uint64_t& paths_out, uint64_t& launches_out) {
+  RenderCfg g = g0;
+  g.tent = 1;
+  const int64_t size = (int64_t)g.width * g.height;
+  const int64_t seeds64 = (int64_t)p->samples * (int64_t)(size * p->mlt_pre_sample);
+  const int64_t total = (int64_t)p->samples * (int64_t)(size * p->mlt_mutation);
+  if (seeds64 < 1 || total < 1) return fail(c, PR_E_ARG, "Metropolis: no seed paths or no mutations at this size");
+  if (seeds64 > ((int64_t)1 << 28)) return fail(c, PR_E_ARG, "Metropolis: at most 2^28 seed paths");
+  MltCfg m;
+  memset(&m, 0, sizeof(m));
+  m.seeds = (int)seeds64;
+  int64_t chains = p->mlt_chains > 0 ? p->mlt_chains : 65536;
+  chains = std::max<int64_t>(1, std::min<int64_t>(chains, total));
+  m.chains = (int)chains;
+  m.mutations = (total + chains - 1) / chains;
+  m.p_large = 0.5f;
+  m.pdf = (float)(4.0 * (double)size);
+  m.chain_scale = (float)(1.0 / (double)m.mutations);
+  m.seed = g.seed + g.sample_offset * 0x9E3779B97F4A7C15ull;
+  g.seed = m.seed;
+  const size_t n3 = (size_t)size * 3;
+  PR_CUDA(c, c->mlt_lum.ensure(sizeof(float) * (size_t)m.seeds));
+  PR_CUDA(c, c->mlt_path.ensure(sizeof(float4) * (size_t)m.seeds));
+  PR_CUDA(c, c->mlt_start.ensure(sizeof(int32_t) * (size_t)m.chains));
+  PR_CUDA(c, c->mlt_u.ensure(sizeof(float) * (size_t)m.chains * kMltDims));
+  PR_CUDA(c, c->mlt_cur.ensure(sizeof(float4) * (size_t)m.chains));
+  PR_CUDA(c, c->mlt_acc.ensure(sizeof(float) * n3));
+  PR_CUDA(c, cudaMemsetAsync(c->mlt_acc.p, 0, sizeof(float) * n3, c->stream));
+  const DevScene& S = c->cur.dev;
+  uint32_t* err = (uint32_t*)c->errword.p;
+  unsigned long long* cnt = (unsigned long long*)c->counters.p;
+  PR_CUDA(c, launch_mlt_seeds(S, g, m, (float*)c->mlt_lum.p, (float4*)c->mlt_path.p, err, cnt, c->stream));
+  std::vector<float> lum((size_t)m.seeds);
+  PR_CUDA(c, cudaMemcpyAsync(lum.data(), c->mlt_lum.p, sizeof(float) * lum.size(), cudaMemcpyDeviceToHost, c->stream));
+  PR_CUDA(c, cudaStreamSynchronize(c->stream));
+  double sum = 0.0;
+  for (float v : lum) sum += (double)v;
+  paths_out = (uint64_t)m.seeds;
+  launches_out = 2;  // bootstrap, resolve
+  if (sum >= 1.0e-14) {  // a black bootstrap leaves the image black (render.h:528-531)
+    m.b = (float)(sum / m.seeds);
+    std::vector<int32_t> start((size_t)m.chains);
+    double acc = 0.0;
+    size_t i = 0;
+    for (int k = 0; k < m.chains; k++) {
+      const double target = (k + 0.5) / m.chains * sum;
+      while (i + 1 < lum.size() && acc + (double)lum[i] < target) acc += (double)lum[i++];
+      start[(size_t)k] = (int32_t)i;
+    }
+    PR_CUDA(c, cudaMemcpyAsync(c->mlt_start.p, start.data(), sizeof(int32_t) * start.size(), cudaMemcpyHostToDevice,
+                               c->stream));
+    PR_CUDA(c, launch_mlt_init(m, (const int32_t*)c->mlt_start.p, (const float4*)c->mlt_path.p,
+                               (const float*)c->mlt_lum.p, (float*)c->mlt_u.p, (float4*)c->mlt_cur.p, c->stream));
+    const int64_t per_launch = 8;
+    for (int64_t it = 0; it < m.mutations; it += per_launch)
+      PR_CUDA(c, launch_mlt_chains(S, g, m, it, std::min<int64_t>(m.mutations, it + per_launch), (float*)c->mlt_u.p,
+                                   (float4*)c->mlt_cur.p, (float*)c->mlt_acc.p, err, cnt, c->stream));
+    paths_out += (uint64_t)m.chains * (uint64_t)m.mutations;
+    launches_out += 1 + (uint64_t)((m.mutations + per_launch - 1) / per_launch);
+  }
+  const float scale = (float)(0.25 * p->sensor_response / (double)m.chains);
+  PR_CUDA(c, launch_mlt_resolve((const float*)c->mlt_acc.p, rgb_dev, (int)n3, scale, accumulate, c->stream));
+  return PR_OK;
 }
 
 static int render_wavefront(pr_ctx* c, const RenderCfg& g, float* rgb_dev, int accumulate,
@@ -731,7 +811,8 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   if (!c) return PR_E_ARG;
   if (!c->scene_ready) return fail(c, PR_E_SCENE, "no scene uploaded");
   if (!rgb_dev) return fail(c, PR_E_ARG, "null output");
-  if (p && p->mode != PR_MODE_MEGAKERNEL && p->mode != PR_MODE_WAVEFRONT) return fail(c, PR_E_ARG, "unknown render mode");
+  if (p && p->mode != PR_MODE_MEGAKERNEL && p->mode != PR_MODE_WAVEFRONT && p->mode != PR_MODE_MLT)
+    return fail(c, PR_E_ARG, "unknown render mode");
   RenderCfg g;
   int st = prepare_render(c, cam, p, sample_offset, g);
   if (st != PR_OK) return st;
@@ -742,6 +823,7 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   PR_CUDA(c, cudaMemsetAsync(c->counters.p, 0, 128, c->stream));
   PR_CUDA(c, cudaEventRecord(c->ev0, c->stream));
   const bool kerr = c->cur.kerr.enabled != 0, worm = c->cur.worm.enabled != 0;
+  uint64_t mlt_paths = 0, mlt_launches = 0;
   if (kerr || worm) {
     // every scene query of a Kerr or wormhole scene is a geodesic trace: one form only
     PR_CUDA(c, c->partial.ensure(sizeof(float) * n3 * (size_t)g.chunks));
@@ -752,6 +834,9 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
       PR_CUDA(c, launch_worm_render(c->cur.dev, c->cur.worm, g, (float*)c->partial.p, (uint32_t*)c->errword.p,
                                     (unsigned long long*)c->counters.p, c->stream));
     PR_CUDA(c, launch_reduce((const float*)c->partial.p, rgb_dev, (int)n3, g.chunks, accumulate, c->stream));
+  } else if (p->mode == PR_MODE_MLT) {
+    st = render_mlt(c, g, p, rgb_dev, accumulate, mlt_paths, mlt_launches);
+    if (st != PR_OK) return st;
   } else if (p->mode == PR_MODE_WAVEFRONT) {
     st = render_wavefront(c, g, rgb_dev, accumulate);
     if (st != PR_OK) return st;
@@ -768,9 +853,12 @@ int pr_render_dev(pr_ctx* c, const pr_camera* cam, const pr_render_params* p, fl
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
   const bool wf = p->mode == PR_MODE_WAVEFRONT && !kerr && !worm;
-  const uint64_t paths = wf ? (uint64_t)g.spp * g.width * g.height : cnt[0];
-  // wavefront: reset per pass + 4 per iteration + resolve; megakernel: kernel + reduce
-  const uint64_t launches = wf ? 4 * cnt[5] + c->wf_passes + 1 : 2;
+  const bool mlt = p->mode == PR_MODE_MLT && !kerr && !worm;
+  // MLT: paths = bootstrap paths + proposals
+  const uint64_t paths = wf ? (uint64_t)g.spp * g.width * g.height : mlt ? mlt_paths : cnt[0];
+  // wavefront: reset per pass + 4 per iteration + resolve; megakernel: kernel + reduce;
+  // MLT: bootstrap, chain start, the chains' launches, resolve
+  const uint64_t launches = wf ? 4 * cnt[5] + c->wf_passes + 1 : mlt ? mlt_launches : 2;
   // Kerr counters: [1] accepted RK steps, [2] RK attempts, [3] segment scene
   // tests, reported as pr_kerr_trace does (segments, nodes_visited, tri_tests)
   c->stats = kerr ? pr_render_stats{paths, cnt[3], cnt[1], cnt[2], ms, launches}
@@ -1251,6 +1339,8 @@ int pr_render_batch(pr_ctx* c, int n, const pr_job* jobs) {
     if (!J.scene) return fail(c, PR_E_ARG, "job " + std::to_string(j) + ": null scene");
     all_kerr = all_kerr && J.scene->data.kerr.enabled;
     if (!J.rgb_dev) return fail(c, PR_E_ARG, "job " + std::to_string(j) + ": null output");
+    if (J.params.mode == PR_MODE_MLT)
+      return fail(c, PR_E_UNSUPPORTED, "job " + std::to_string(j) + ": Metropolis renders run through pr_render");
     int st = prepare_render(c, &J.camera, &J.params, J.sample_offset, cfg[j], &J.scene->data);
     if (st != PR_OK) return fail(c, st, "job " + std::to_string(j) + ": " + c->err);
     // the batch fills the GPU with many jobs: fewer sample chunks per job

@@ -64,6 +64,7 @@ struct pr_ctx {
   pr::DevBuf partial, out, rays, ires, jres, dres;
   pr::DevBuf k_status, k_bl, k_dir, k_steps, k_ent, k_t;  // pr_kerr_trace staging
   pr::DevBuf k_sens;                                        // pr_kerr_sensitivity staging
+  pr::DevBuf mlt_lum, mlt_path, mlt_start, mlt_u, mlt_cur, mlt_acc;  // PR_MODE_MLT state
   pr::DevBuf adj_scratch, adj_grad;                         // adjoint outputs
   double kernel_ms[4] = {0, 0, 0, 0};        // wavefront shade / extend / shadow / control (host-driven loop)
   unsigned long long shadow_counts[3] = {0, 0, 0};  // shadow rays, nodes, triangles of the last wavefront frame

@@ -117,7 +117,8 @@ __device__ __forceinline__ void make_vertex(const DevScene& S, float3 o, float3 
 
 // a point on light entity le (direct_radiance_sample, directLight_radiance.h:326-377;
 // the media variant omits the uvplane's normal * PS_EPS lift, ParticipatingMedia.h:213-224)
-__device__ __forceinline__ float3 sample_light(const GEntF& le, Rng& rng, bool lift) {
+template <class R>
+__device__ __forceinline__ float3 sample_light(const GEntF& le, R& rng, bool lift) {
   if (le.type == PR_ENT_SPHERE) {
     const float r1 = 6.28318530717958647692f * rng.next();
     const float r2 = 1.0f - 2.0f * rng.next();
@@ -142,7 +143,8 @@ __device__ __forceinline__ float3 light_normal(const GEntF& le, float3 lp, bool 
 }
 
 // LightList::randomLight (light.h:132-155): rounded index, probability 1
-__device__ __forceinline__ const GLight& pick_light(const DevScene& S, Rng& rng) {
+template <class R>
+__device__ __forceinline__ const GLight& pick_light(const DevScene& S, R& rng) {
   int idx = (int)(rng.next() * (float)(S.n_lights - 1) + 0.5f);
   idx = min(max(idx, 0), S.n_lights - 1);
   return S.lights[idx];
@@ -187,8 +189,9 @@ struct LightSample {
 
 // parallel, spot and infinity lights (compiled into the shading
 // instantiations for scenes that have them)
+template <class R>
 __device__ __forceinline__ bool point_light_sample(const DevScene& S, const GLight& L, float3 p, float3 on,
-                                                   float3 origin, bool surface, bool media, Rng& rng,
+                                                   float3 origin, bool surface, bool media, R& rng,
                                                    LightSample& ls) {
   ls.area = false;
   ls.so = origin;
@@ -288,7 +291,8 @@ __device__ __forceinline__ float perfect_direct(const DevScene& S, float3 o, flo
 
 
 // sampleHG (sampler.h:24-93); the reference's cos expression is (g/2)(...)
-__device__ __forceinline__ float3 sample_hg(float3 raydir, float g, Rng& rng, bool correct) {
+template <class R>
+__device__ __forceinline__ float3 sample_hg(float3 raydir, float g, R& rng, bool correct) {
   float3 u, v;
   onb(raydir, u, v);
   const float r1 = 6.28318530717958647692f * rng.next();
@@ -301,7 +305,8 @@ __device__ __forceinline__ float3 sample_hg(float3 raydir, float g, Rng& rng, bo
   return normalize(u * (sint * cs) + v * (sint * sn) + raydir * cost);
 }
 
-__device__ __forceinline__ float3 sample_sphere_dir(Rng& rng) {
+template <class R>
+__device__ __forceinline__ float3 sample_sphere_dir(R& rng) {
   const float r1 = 6.28318530717958647692f * rng.next();
   const float r2 = 1.0f - 2.0f * rng.next();
   const float sq = sqrtf(fmaxf(0.0f, 1.0f - r2 * r2));
@@ -433,10 +438,10 @@ __device__ __forceinline__ float dd_bssrdf(const GMaterial& m, float3 xi, float3
 // samples at the exit point (colour / pi, the unflipped surface normal as
 // orienting normal).  The reference computes Fresnel factors here that it
 // does not apply.
-template <bool EXT>
+template <bool EXT, class R>
 __device__ inline void sss_exit(const DevScene& S, const RenderCfg& cfg, const GMaterial& m, int in_ent,
                                 const FastHit& oh, const Vertex& ov, float3 dir, float rr2, float3 beta, int depth,
-                                Rng& rng, ShadowReq* sh, int& nsh, PathState& ps) {
+                                R& rng, ShadowReq* sh, int& nsh, PathState& ps) {
   const float3 Tr = f3(expf(-m.sss_tr[0] * oh.t), expf(-m.sss_tr[1] * oh.t), expf(-m.sss_tr[2] * oh.t));
   ps.dp = 0;
   ps.depth = depth;
@@ -728,7 +733,7 @@ __device__ __forceinline__ float glossy_lobe(int kind, const GMaterial& m, float
 // and the colour a miss returns as miss (radiance.h:30-43); straight-ray
 // callers leave both null.  ovr (colour, emission) replaces the material's
 // where the entity rewrote its hit point's copy (the accretion disk).
-template <bool SSS = false, bool GLOSSY = true, bool EXT = false>
+template <bool SSS = false, bool GLOSSY = true, bool EXT = false, class R = Rng>
 __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& ps, bool hit, const FastHit& h,
                      uint64_t sample_id, ShadowReq* sh, int& nsh, PathState& child, uint32_t* err,
                      const Vertex* pre = nullptr, const float3* miss = nullptr, EmissionTap* tap = nullptr,
@@ -762,7 +767,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
     atomicOr(err, PR_DEV_LOOP_CAP);
     return SHADE_END;
   }
-  Rng rng;
+  R rng;
   rng_at(rng, cfg.seed, sample_id, ps.branch, ps.draws);
   Vertex v;
   if (pre) v = *pre;

@@ -26,7 +26,8 @@ wormhole renders (wormhole_render.npz), --wormhole-oracle the oracle's
 16 batches of each wormhole scene (wormhole_oracle.npz); --meshtex-only and
 --meshtex-oracle do the same for smooth and textured meshes
 (meshtex_render.npz, meshtex_oracle.npz); --mlt-only writes the reference's
-one-thread Metropolis renders (mlt_render.npz).
+one-thread Metropolis renders (mlt_render.npz), --mlt-oracle the oracle's
+path-traced expectation of the GPU Metropolis scenes (mlt_oracle.npz).
 --scene-files-only writes the meshes and textures that the scene files in
 scene_files/ name, and scene_files.npz from the reference's renders of them.
 """
@@ -439,6 +440,31 @@ def mlt_golden(d):
     np.savez_compressed(os.path.join(HERE, "mlt_render.npz"), **out)
 
 
+def mlt_oracle_golden(nb=16):
+    """16 independent 256-spp path-traced renders (no luminance clamp) of each
+    Metropolis scene by the oracle: the expectation the Metropolis image
+    converges to, per-pixel mean and spread"""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import mlt_cases
+    from oracle import oracle as O
+    out = {}
+    for name in mlt_cases.CASES:
+        sc = mlt_cases.gpu_case(name)
+        o = O.OracleScene(sc)
+        st = mlt_cases.pt_settings(sc)
+        imgs = []
+        for k in range(nb):
+            st.seed = 100 + k
+            img, _, _ = o.render(threads=os.cpu_count(), settings=st)
+            imgs.append(img)
+        b = np.stack(imgs)
+        out[f"{name}_mean"] = b.mean(0).astype(np.float32)
+        out[f"{name}_sd"] = b.std(0, ddof=1).astype(np.float32)
+        print("mlt oracle", name, float(b.mean()))
+    out["batches"] = np.int32(nb)
+    np.savez_compressed(os.path.join(HERE, "mlt_oracle.npz"), **out)
+
+
 def meshtex_oracle_golden(nb=16):
     """16 independent 256-spp renders of each smooth / textured mesh scene
     by the oracle (pinned bit-exact to the reference by meshtex_render.npz):
@@ -650,7 +676,7 @@ KNOWN_FLAGS = {"--kerr-only", "--disk-only", "--sss-only", "--sss-l1-only", "--g
                "--media-oracle", "--mesh7-oracle", "--batch-only", "--batch-oracle", "--hdr-only",
                "--lights-only", "--lights-oracle", "--textures-only", "--textures-oracle", "--wormhole-only",
                "--wormhole-oracle", "--meshtex-only", "--meshtex-oracle",
-               "--mlt-only"}
+               "--mlt-only", "--mlt-oracle"}
 
 
 def main():
@@ -671,6 +697,9 @@ def main():
         return
     if "--meshtex-oracle" in sys.argv:
         meshtex_oracle_golden()
+        return
+    if "--mlt-oracle" in sys.argv:
+        mlt_oracle_golden()
         return
     if "--mesh7-oracle" in sys.argv:
         mesh7_oracle_golden()
