@@ -560,6 +560,73 @@ def run_kerr(args):
     return 0
 
 
+def run_curved_or_mlt(args):
+    """Two non-headline workloads, one JSON line each:
+    mlt: Metropolis light transport (PR_MODE_MLT) of the sphere Cornell box,
+    256 x 192, 16 x W H x 16 mutations and 16 x W H x 0.4 bootstrap paths
+    per step; Mpaths/s counts proposals and bootstrap paths; the CPU baseline
+    is the oracle's RunMLT (the reference's sequential chains) on one thread.
+    wormhole: a wormhole render (objects on both sides), 512 x 384, 4 tent
+    samples per pixel, geodesics of up to 300 FP64 Cash-Karp steps each."""
+    import torch
+    import __graft_entry__ as g
+    g.build_library()
+    from prender_gb300 import gpu, scenes
+    from prender_gb300 import _abi as A
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    torch.cuda.set_device(0)
+    ctx = gpu.Context(0)
+    if args.workload == "mlt":
+        s = scenes.cornell_spheres(width=256, height=192, samples=16, supersamples=1)
+        s.settings.mode = A.PR_MODE_MLT
+        s.settings.mutation, s.settings.pre_sample, s.settings.nee = 16.0, 0.4, 1
+        name = "cornell_spheres_256x192_mlt_16x16_mutations_per_pixel"
+    else:
+        import wormhole_cases
+        s = wormhole_cases.build("worm_objects", 512, 384, 1, 2, max_steps=300)
+        name = "wormhole_objects_512x384_4spp_300_steps"
+    ctx.upload(s)
+    for i in range(args.warmup):
+        ctx.render(s, sample_offset=i)
+    clk = ClockSampler(0)
+    clk.start()
+    walls, paths, launches = [], 0, 0
+    for i in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.render(s, sample_offset=args.warmup + i)
+        torch.cuda.synchronize()
+        walls.append(time.perf_counter() - t0)
+        st = ctx.stats()
+        paths, launches = st["paths"], st["kernel_launches"]
+    clocks = clk.stop()
+    ms = 1e3 * statistics.mean(walls)
+    cpu = None
+    if args.workload == "mlt":
+        from oracle import oracle as O
+        O.build()
+        small = scenes.cornell_spheres(width=64, height=48, samples=2, supersamples=1)
+        small.settings.mode = A.PR_MODE_MLT
+        small.settings.mutation, small.settings.pre_sample, small.settings.nee = 16.0, 0.4, 1
+        t0 = time.perf_counter()
+        O.OracleScene(small).render_mlt()
+        wall = time.perf_counter() - t0
+        n = 2 * int(64 * 48 * 16) + 2 * int(64 * 48 * 0.4)
+        cpu = {"value": round(n / wall / 1e6, 5), "unit": "Mpaths/s", "cores": 1, "kind": "port",
+               "sample": "oracle RunMLT, 64 x 48, 2 chains x (1228 seeds + 49152 mutations), one thread"}
+    line = {
+        "metric": "Mpaths/s, " + ("Metropolis light transport" if args.workload == "mlt" else "wormhole geodesic renders"),
+        "value": round(paths / (ms / 1e3) / 1e6, 4), "unit": "Mpaths/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if args.workload == "mlt" else "f64", "data": "synthetic",
+        "config": {"workload": name, "paths_per_step": int(paths), "gpu_launches": int(launches)},
+        "cpu_baseline": cpu, "clocks": clocks,
+    }
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def run_batch(args):
     """The media + BSSRDF batch: 32 Cornell variants (global HG medium with
     sigma_s U(0.05, 0.5), sigma_a 0.01, g U(-0.6, 0.8); a 20,480-triangle
@@ -643,14 +710,17 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default wavefront pool size and traversal grid")
     ap.add_argument("--ref-rows", type=int, default=48)
-    ap.add_argument("--workload", default="mesh", choices=["mesh", "kerr", "batch"],
-                    help="kerr: the Kerr lensing renders; batch: the media + BSSRDF batch (not the headline workload)")
+    ap.add_argument("--workload", default="mesh", choices=["mesh", "kerr", "batch", "mlt", "wormhole"],
+                    help="kerr: the Kerr lensing renders; batch: the media + BSSRDF batch; mlt: Metropolis light "
+                         "transport; wormhole: wormhole renders (none of them the headline workload)")
     ap.add_argument("--kerr-jobs", type=int, default=16)
     args = ap.parse_args()
     if args.workload == "kerr":
         return run_kerr(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload in ("mlt", "wormhole"):
+        return run_curved_or_mlt(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
