@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define PR_ABI_VERSION 7
+#define PR_ABI_VERSION 8
 
 /* ---- status codes --------------------------------------------------- */
 enum {
@@ -188,6 +188,30 @@ typedef struct pr_entity {
  * face's vertex ids).  Texture coordinates (vt lines, 2 floats each) with
  * face_uv (3 ids per face) place textures and IBL images on the mesh
  * (polygon.h:206-212, :507-528); NULL for none. */
+/* An OBJ material (newmtl in an mtllib file, ObjLoader.cpp:704-900;
+ * ObjMaterial, ObjLoader.h:94-150) that faces select with usemtl.  A face's
+ * hit takes the entity's material and then, as Triangle::intersect does
+ * (polygon.h:228-400): the colour Kd and specular Ks (0 for a diffuse
+ * entity material), or with a map_Kd texture the entity colour times the
+ * texel; with '#REFLECTION t' also the type t, '#EMISSION', Ni, '#ROUGHNESS',
+ * '#WARD' / Ns and the type's colours (texel-scaled with a texture). */
+typedef struct pr_obj_material {
+  double diffuse[3];          /* Kd (or '#COLOR')                            */
+  double alpha;               /* d (or 1 - Tr); -1: none                     */
+  double specular[3];         /* Ks (or '#SPECULAR')                         */
+  double emission[3];         /* '#EMISSION'                                 */
+  double refraction_index;    /* Ni (0 default; 1.5 for '#REFLECTION 2')     */
+  double shininess;           /* Ns (default 5)                              */
+  double roughness;           /* '#ROUGHNESS' (0; '#REFLECTION 0/1' set 0)    */
+  double ward[2];             /* '#WARD ax ay'                               */
+  int32_t reflection;         /* '#REFLECTION' type (-1: none)               */
+  int32_t smooth;             /* '#SMOOTH': 0 unset, 1 on, 2 off             */
+  int32_t repeat;             /* '#REPEAT' (default 1)                       */
+  int32_t texture_width, texture_height;
+  int32_t pad0;
+  const uint8_t* texture;     /* map_Kd, RGB8 as BitMap::cell(y, x) reads it */
+} pr_obj_material;
+
 typedef struct pr_mesh {
   int32_t n_vertices;
   int32_t n_faces;
@@ -200,6 +224,10 @@ typedef struct pr_mesh {
   const int32_t* face_vn;       /* 3 * n_faces or NULL                       */
   const float* uv;              /* 2 * n_uv or NULL                          */
   const int32_t* face_uv;       /* 3 * n_faces or NULL                       */
+  int32_t n_obj_materials;
+  int32_t pad_obj;
+  const pr_obj_material* obj_materials;  /* usemtl targets or NULL           */
+  const int32_t* face_obj_material;      /* per face, -1: none; NULL: none   */
 } pr_mesh;
 
 /* Kerr integrator precision: PR_KERR_FP64 runs the reference's FP64

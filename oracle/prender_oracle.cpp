@@ -143,6 +143,8 @@ struct Hit {  // IntersectionPos (intersection.h:11-30) + object_id
   V3 ov_specular;
   bool bump = false;     // IntersectionPos::bump / bump_new_normal
   V3 bump_n;
+  bool ov_full = false;  // the hit's whole material copy (a face's OBJ material)
+  Material ovm;
 };
 
 struct Mesh {
@@ -153,6 +155,15 @@ struct Mesh {
   std::vector<int> norm_id;  // 3 per face
   std::vector<float> uv;     // vt lines (2 per entry)
   std::vector<int> uv_id;    // 3 per face (empty: no vt lines)
+  struct ObjMat {            // ObjMaterial (ObjLoader.h:94-150)
+    V3 diffuse, specular, emission;
+    double alpha = -1.0, ni = 0.0, ns = 5.0, rough = 0.0, ward[2] = {0, 0};
+    int refl = -1, smooth = 0, repeat = 1;
+    std::vector<unsigned char> tex;  // map_Kd (RGB, cell(i, j))
+    int tw = 0, th = 0;
+  };
+  std::vector<ObjMat> omats;
+  std::vector<int> face_omat;  // per face, -1: none (empty: no usemtl)
 };
 
 struct Tri {  // Triangle (polygon.h:22-708)
@@ -589,7 +600,11 @@ bool tri_hit(const Scene& s, const Entity& e, const Tri& tr, V3 org, V3 dir, Hit
   h.distance = t;
   h.position = org + dir * t;
   h.normal = V3(m.fnorm[3 * tr.face], m.fnorm[3 * tr.face + 1], m.fnorm[3 * tr.face + 2]);
-  if (e.smooth) {  // polygon.h:186-199
+  const Mesh::ObjMat* om = nullptr;  // the face's OBJ material (usemtl)
+  if (!m.face_omat.empty() && m.face_omat[(size_t)tr.face] >= 0) om = &m.omats[(size_t)m.face_omat[(size_t)tr.face]];
+  int smooth = e.smooth;
+  if (om && om->smooth) smooth = om->smooth == 1 ? 1 : 0;  // polygon.h:178-188
+  if (smooth) {  // polygon.h:186-199
     const int* ni = &m.norm_id[3 * tr.face];
     const V3 n0(m.norm[3 * (size_t)ni[0]], m.norm[3 * (size_t)ni[0] + 1], m.norm[3 * (size_t)ni[0] + 2]);
     const V3 n1(m.norm[3 * (size_t)ni[1]], m.norm[3 * (size_t)ni[1] + 1], m.norm[3 * (size_t)ni[1] + 2]);
@@ -604,6 +619,83 @@ bool tri_hit(const Scene& s, const Entity& e, const Tri& tr, V3 org, V3 dir, Hit
   // textured mesh lie in [0, 1]); bump maps on meshes write the caller's
   // record, which the returned hit overwrites (polygon.h:529-618)
   const Material& mt = s.mats[e.material];
+  if (om) {
+    // the OBJ material's block of Triangle::intersect (polygon.h:228-400),
+    // then the entity's own texture and IBL image (:505-528)
+    Material q = mt;
+    double hu = 0, hv = 0;
+    if (!m.uv_id.empty()) {
+      const int* ti = &m.uv_id[3 * tr.face];
+      hu = m.uv[2 * (size_t)ti[0]] * w + m.uv[2 * (size_t)ti[1]] * u + m.uv[2 * (size_t)ti[2]] * v;
+      hv = m.uv[2 * (size_t)ti[0] + 1] * w + m.uv[2 * (size_t)ti[1] + 1] * u + m.uv[2 * (size_t)ti[2] + 1] * v;
+    }
+    if (!om->tex.empty()) {
+      const double uu = wrap01(hu * om->repeat), vv = wrap01(hv * om->repeat);
+      const int j = trunc_int((om->tw - 1) * uu), i = trunc_int((om->th - 1) * vv);
+      const unsigned char* t = &om->tex[3 * ((size_t)i * om->tw + j)];
+      // base.x * (double)cell.r / 255.0, left to right (polygon.h:257-304)
+      auto scaled = [t](V3 b) {
+        return V3(b.x * (double)t[0] / 255.0, b.y * (double)t[1] / 255.0, b.z * (double)t[2] / 255.0);
+      };
+      q.color = scaled(mt.color);
+      q.emission = mt.emission;
+      if (om->refl >= 0) {
+        q.emission = scaled(om->emission);
+        q.type = om->refl;
+        q.specular = scaled(om->specular);
+        q.refractive_index = om->ni;
+        q.roughness = om->rough;
+        if (q.type == PR_MAT_SPECULAR || q.type == PR_MAT_REFRACTION) q.color = om->specular;
+        if (q.type == PR_MAT_WARD) {
+          q.ward_ax = om->ward[0];
+          q.ward_ay = om->ward[1];
+          q.color = scaled(om->diffuse);
+        }
+        if (q.type == PR_MAT_PHONG) {
+          q.phong_n = om->ns;
+          q.color = scaled(om->diffuse);
+        }
+      }
+    } else {
+      q.color = om->diffuse;
+      q.specular = om->specular;
+      if (q.type == PR_MAT_DIFFUSE) q.specular = V3();
+      q.emission = mt.emission;
+      if (om->refl >= 0) {
+        q.emission = om->emission;
+        q.type = om->refl;
+        q.specular = om->specular;
+        q.refractive_index = om->ni;
+        q.roughness = om->rough;
+        if (q.type == PR_MAT_SPECULAR || q.type == PR_MAT_REFRACTION) q.color = om->specular;
+        if (q.type == PR_MAT_WARD) {
+          q.ward_ax = om->ward[0];
+          q.ward_ay = om->ward[1];
+          q.color = om->diffuse;
+        }
+        if (q.type == PR_MAT_PHONG) {
+          q.phong_n = om->ns;
+          q.color = om->diffuse;
+        }
+      }
+    }
+    if (mt.tex) {
+      int j = trunc_int((mt.tex_w - 1) * hu), i = trunc_int((mt.tex_h - 1) * hv);
+      i = std::min(std::max(i, 0), mt.tex_h - 1);
+      j = std::min(std::max(j, 0), mt.tex_w - 1);
+      texel_rgb(mt, i, j, q.color);
+    }
+    if (mt.ibl) {
+      int j = trunc_int((mt.ibl_w - 1) * hu), i = trunc_int((mt.ibl_h - 1) * hv);
+      i = std::min(std::max(i, 0), mt.ibl_h - 1);
+      j = std::min(std::max(j, 0), mt.ibl_w - 1);
+      q.color = ibl_rgb(mt, i, j);
+      q.emission = mt.ibl_coef * q.color;
+    }
+    h.ov_full = true;
+    h.ovm = q;
+    return true;
+  }
   if ((mt.tex || mt.ibl) && !m.uv_id.empty()) {
     const int* ti = &m.uv_id[3 * tr.face];
     const double hu = m.uv[2 * (size_t)ti[0]] * w + m.uv[2 * (size_t)ti[1]] * u + m.uv[2 * (size_t)ti[2]] * v;
@@ -999,6 +1091,31 @@ int build_scene(const pr_scene_desc* d, Scene& s, std::string& err) {
     if (pm.uv && pm.face_uv) {
       m.uv.assign(pm.uv, pm.uv + 2 * (size_t)pm.n_uv);
       m.uv_id.assign(pm.face_uv, pm.face_uv + 3 * (size_t)pm.n_faces);
+    }
+    if (pm.obj_materials && pm.face_obj_material && pm.n_obj_materials > 0) {
+      for (int k = 0; k < pm.n_obj_materials; k++) {
+        const pr_obj_material& q = pm.obj_materials[k];
+        Mesh::ObjMat om;
+        om.diffuse = V3(q.diffuse[0], q.diffuse[1], q.diffuse[2]);
+        om.specular = V3(q.specular[0], q.specular[1], q.specular[2]);
+        om.emission = V3(q.emission[0], q.emission[1], q.emission[2]);
+        om.alpha = q.alpha;
+        om.ni = q.refraction_index;
+        om.ns = q.shininess;
+        om.rough = q.roughness;
+        om.ward[0] = q.ward[0];
+        om.ward[1] = q.ward[1];
+        om.refl = q.reflection;
+        om.smooth = q.smooth;
+        om.repeat = q.repeat;
+        if (q.texture && q.texture_width > 0 && q.texture_height > 0) {
+          om.tw = q.texture_width;
+          om.th = q.texture_height;
+          om.tex.assign(q.texture, q.texture + 3 * (size_t)om.tw * om.th);
+        }
+        m.omats.push_back(std::move(om));
+      }
+      m.face_omat.assign(pm.face_obj_material, pm.face_obj_material + pm.n_faces);
     }
     if (pm.face_normals) {
       memcpy(m.fnorm.data(), pm.face_normals, sizeof(float) * 3 * (size_t)pm.n_faces);
@@ -1462,6 +1579,7 @@ bool inside_dir(V3 normal, V3 raydir) {
 
 // the material of a hit point: the scene's, or the copy the entity rewrote
 Material hit_mat(const Scene& s, const Hit& h) {
+  if (h.ov_full) return h.ovm;
   Material m = s.mats[h.material];
   if (h.ov) {
     m.color = h.ov_color;

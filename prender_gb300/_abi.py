@@ -115,6 +115,26 @@ class pr_entity(C.Structure):
     ]
 
 
+class pr_obj_material(C.Structure):
+    _fields_ = [
+        ("diffuse", D3),
+        ("alpha", C.c_double),
+        ("specular", D3),
+        ("emission", D3),
+        ("refraction_index", C.c_double),
+        ("shininess", C.c_double),
+        ("roughness", C.c_double),
+        ("ward", C.c_double * 2),
+        ("reflection", C.c_int32),
+        ("smooth", C.c_int32),
+        ("repeat", C.c_int32),
+        ("texture_width", C.c_int32),
+        ("texture_height", C.c_int32),
+        ("pad0", C.c_int32),
+        ("texture", C.c_void_p),
+    ]
+
+
 class pr_mesh(C.Structure):
     _fields_ = [
         ("n_vertices", C.c_int32),
@@ -128,6 +148,10 @@ class pr_mesh(C.Structure):
         ("face_vn", C.POINTER(C.c_int32)),
         ("uv", C.POINTER(C.c_float)),
         ("face_uv", C.POINTER(C.c_int32)),
+        ("n_obj_materials", C.c_int32),
+        ("pad_obj", C.c_int32),
+        ("obj_materials", C.POINTER(pr_obj_material)),
+        ("face_obj_material", C.POINTER(C.c_int32)),
     ]
 
 

@@ -207,6 +207,7 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   if (!h.bump_texels.empty()) PR_CUDA(c, upload(o.bump_texels, h.bump_texels, c->stream));
   if (!h.fvn.empty()) PR_CUDA(c, upload(o.fvn, h.fvn, c->stream));
   if (!h.fuv.empty()) PR_CUDA(c, upload(o.fuv, h.fuv, c->stream));
+  if (!h.fmat.empty()) PR_CUDA(c, upload(o.fmat, h.fmat, c->stream));
   PR_CUDA(c, upload(o.kerr_tex, h.kerr_texture, c->stream));
   PR_CUDA(c, upload(o.kerr_disk_tex, h.kerr_disk_texture, c->stream));
   for (int k = 0; k < 2; k++)
@@ -253,6 +254,8 @@ static int build_device_scene(pr_ctx* c, const pr_scene_desc* d, SceneObjData& o
   if (!h.fvn.empty()) S.has_tex |= 2;
   S.fvn = h.fvn.empty() ? nullptr : (const float*)o.fvn.p;
   S.fuv = h.fuv.empty() ? nullptr : (const float*)o.fuv.p;
+  S.fmat = h.fmat.empty() ? nullptr : (const int32_t*)o.fmat.p;
+  if (!h.fmat.empty()) S.has_tex |= 2;
   for (int k = 0; k < 3; k++) {
     S.bg[k] = (float)h.background[k];
     S.env[k] = (float)h.env_light[k];

@@ -36,13 +36,13 @@ struct DevBuf {
 struct SceneObjData {
   HostScene host;
   DevBuf ents, mats, nodes, tris, rnodes, rtris, fnorm, kerr_tex, kerr_disk_tex, texels, ibl_texels, bump_texels;
-  DevBuf worm_tex[2], fvn, fuv;
+  DevBuf worm_tex[2], fvn, fuv, fmat;
   DevScene dev{};
   GKerr kerr{};
   GWorm worm{};
   void release() {
     for (DevBuf* b : {&ents, &mats, &nodes, &tris, &rnodes, &rtris, &fnorm, &kerr_tex, &kerr_disk_tex, &texels, &ibl_texels,
-                      &bump_texels, &worm_tex[0], &worm_tex[1], &fvn, &fuv})
+                      &bump_texels, &worm_tex[0], &worm_tex[1], &fvn, &fuv, &fmat})
       b->release();
   }
 };

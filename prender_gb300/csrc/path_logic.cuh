@@ -588,10 +588,12 @@ __device__ __forceinline__ float3 bump_tilt(const DevScene& S, const GMaterial& 
 // returns (polygon.h:529-618 writes the caller's record, which the hit
 // then overwrites), so none is read here.  True for an IBL hit.
 __device__ inline bool mesh_hit(const DevScene& S, const GMaterial& m, const GEntF& e, int flags, const FastHit& h,
-                                Vertex& v, float3& C, float3& E) {
+                                Vertex& v, float3& C, float3& E, float3& Sp) {
   const int face = e.face_base + __float_as_int(__ldg(S.rtris + 3 * (size_t)h.slot).w);
   const float w = 1.0f - h.u - h.v;
-  if (flags & 1) {
+  // an OBJ material's '#SMOOTH' overrides the entity's 'smooth' (polygon.h:178-188)
+  const bool smooth = (flags & 4) && m.mesh_smooth ? m.mesh_smooth == 1 : (flags & 1) != 0;
+  if (smooth && (flags & 8)) {
     const float* n = S.fvn + 9 * (size_t)face;
     float3 ns = normalize(f3(n[0] * w + n[3] * h.u + n[6] * h.v, n[1] * w + n[4] * h.u + n[7] * h.v,
                              n[2] * w + n[5] * h.u + n[8] * h.v));
@@ -600,6 +602,17 @@ __device__ inline bool mesh_hit(const DevScene& S, const GMaterial& m, const GEn
   if (!(flags & 2)) return false;
   const float* t = S.fuv + 6 * (size_t)face;
   const float tu = t[0] * w + t[2] * h.u + t[4] * h.v, tv = t[1] * w + t[3] * h.u + t[5] * h.v;
+  if ((flags & 4) && m.mtex_off >= 0) {
+    // map_Kd: the texel at the repeated, wrapped coordinates scales the
+    // derived colours the mask names (polygon.h:236-305)
+    const float uu = tex_wrap(tu * (float)m.mtex_repeat), vv = tex_wrap(tv * (float)m.mtex_repeat);
+    const float4 x = __ldg(S.texels + m.mtex_off + (size_t)tex_clamp((int)((m.mtex_h - 1) * vv), m.mtex_h) * m.mtex_w +
+                           tex_clamp((int)((m.mtex_w - 1) * uu), m.mtex_w));
+    const float3 tx = f3(x.x, x.y, x.z);
+    if (m.mtex_mask & 1) C = C * tx;
+    if (m.mtex_mask & 2) Sp = Sp * tx;
+    if (m.mtex_mask & 4) E = E * tx;
+  }
   if (m.tex_off >= 0) {
     const float4 x = __ldg(S.texels + m.tex_off + (size_t)tex_clamp((int)((m.tex_h - 1) * tv), m.tex_h) * m.tex_w +
                            tex_clamp((int)((m.tex_w - 1) * tu), m.tex_w));
@@ -772,6 +785,11 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   Vertex v;
   if (pre) v = *pre;
   else make_vertex(S, ps.o, ps.d, h, v);
+  if (EXT && !pre && S.fmat && S.entf[v.ent].type == PR_ENT_POLYGON) {
+    // the face's OBJ material (usemtl) selects a derived material
+    const int fm = S.fmat[S.entf[v.ent].face_base + __float_as_int(__ldg(S.rtris + 3 * (size_t)h.slot).w)];
+    if (fm >= 0) v.mat = fm;
+  }
   const GMaterial& m = S.mats[v.mat];
   const GEntF& ent = S.entf[v.ent];
   float3 E = ovr ? ovr[1] : ld3(m.emission), C = ovr ? ovr[0] : ld3(m.color);
@@ -780,7 +798,7 @@ __device__ inline int shade(const DevScene& S, const RenderCfg& cfg, PathState& 
   bool bumped = false;
   if (EXT && !pre && ent.type == PR_ENT_POLYGON) {
     const int mf = S.ents[v.ent].mesh_flags;
-    if (mf && mesh_hit(S, m, ent, mf, h, v, C, E)) {
+    if (mf && mesh_hit(S, m, ent, mf, h, v, C, E, Sp)) {
       ps.L += ps.beta * E;  // an IBL image on the mesh (radiance.h:45-50)
       if (tap) tap->em(v.mat, ps.beta);
       return SHADE_END;

@@ -103,6 +103,11 @@ struct GMaterial {
   int32_t repeat;
   int32_t map_flags;       // PR_MAP_*
   int32_t bump_off, bump_w, bump_h;  // bump map texels in DevScene::bump_texels (-1: none)
+  // a material derived for the faces of an OBJ material (polygon.h:228-400):
+  // its map_Kd texture (texels in DevScene::texels, -1: none), '#REPEAT',
+  // which of colour / specular / emission (1 / 2 / 4) the texel scales, and
+  // '#SMOOTH' (0 the entity's choice, 1 on, 2 off)
+  int32_t mtex_off, mtex_w, mtex_h, mtex_repeat, mtex_mask, mesh_smooth;
 };
 
 struct GEntity {
@@ -122,7 +127,8 @@ struct GEntity {
   int32_t node_base;       // root node index in the concatenated node array
   int32_t slot_base;       // first leaf slot of this mesh
   int32_t rnode_base;      // root of the mesh's render-path tree (DevScene::rnodes)
-  int32_t mesh_flags;      // mesh: 1 smooth (DevScene::fvn), 2 textured (DevScene::fuv)
+  int32_t mesh_flags;      // mesh: 1 smooth, 2 texture coordinates (DevScene::fuv), 4 OBJ
+                           // materials (DevScene::fmat), 8 vertex normals (DevScene::fvn)
   int32_t face_base;       // first face-normal record of this mesh
   int32_t n_faces;
   float bmin[3], bmax[3];  // bounds (for scene extents)
@@ -242,6 +248,7 @@ struct DevScene {
   const float* bump_texels;  // every bump map: the texel's luminance 0.299 r + 0.587 g + 0.114 b (0..255)
   const float* fvn;        // 9 per face: the vertex normals of smooth meshes (null: none)
   const float* fuv;        // 6 per face: the texture coordinates of textured meshes (null: none)
+  const int32_t* fmat;     // per face: the derived material of its OBJ material (-1: the entity's; null: none)
   int32_t n_ents;
   int32_t n_lights;
   int32_t n_point_lights;  // parallel, spot and infinity lights (sampled even without NEE)

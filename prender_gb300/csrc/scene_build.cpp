@@ -336,6 +336,115 @@ static bool is_light(const pr_material& m) {  // Material::isLight (material.h)
   return m.type == PR_MAT_DIFFUSE && len(c) < 0.001 && len(e) > 0.001;
 }
 
+// The material a face of OBJ material O shows (Triangle::intersect,
+// polygon.h:228-400) on an entity of material B (pm / base): with a map_Kd
+// texture the colour is B's times the texel, else O's Kd and Ks (Ks 0 for a
+// diffuse B); a '#REFLECTION' type also takes its type, '#EMISSION' (times
+// the texel with a texture), Ks (likewise), Ni and '#ROUGHNESS', and the
+// type's own colours: Ks for mirrors and glass, Kd (times the texel) for
+// Ward ('#WARD') and Phong (Ns).  Appended to hs.mats; out = its index.
+static int derive_obj_material(HostScene& hs, const pr_material& pm, const GMaterial& base, const pr_obj_material& o,
+                               int32_t& out, std::string& err) {
+  if (o.alpha >= 0.0 && o.alpha < 1.0) {
+    err = "OBJ materials with d < 1 (the reference's stochastic alpha test) are not rendered here";
+    return PR_E_UNSUPPORTED;
+  }
+  if (o.reflection >= 0 && o.reflection != PR_MAT_DIFFUSE && o.reflection != PR_MAT_SPECULAR &&
+      o.reflection != PR_MAT_REFRACTION && o.reflection != PR_MAT_WARD && o.reflection != PR_MAT_PHONG) {
+    err = "OBJ material '#REFLECTION " + std::to_string(o.reflection) + "' is not on this path";
+    return PR_E_UNSUPPORTED;
+  }
+  if (pm.type == PR_MAT_SSS_REFRACTION || base.sss) {
+    err = "OBJ materials on subsurface entities are not on this path";
+    return PR_E_UNSUPPORTED;
+  }
+  GMaterial g = base;
+  double C[3], Sp[3], E[3];
+  for (int k = 0; k < 3; k++) {
+    C[k] = pm.color[k];
+    Sp[k] = pm.specular[k];
+    E[k] = pm.emission[k];
+  }
+  int mask = 0;
+  double rough = pm.roughness, ior = pm.refractive_index, wx = pm.ward_alpha[0], wy = pm.ward_alpha[1];
+  double pn = pm.phong_exponent;
+  int type = pm.type;
+  if (o.texture) {
+    if (o.texture_width <= 0 || o.texture_height <= 0) { err = "map_Kd texture size must be positive"; return PR_E_ARG; }
+    mask = 1;  // B's colour times the texel
+    if (o.reflection >= 0) {
+      for (int k = 0; k < 3; k++) {
+        E[k] = o.emission[k];
+        Sp[k] = o.specular[k];
+      }
+      mask |= 2 | 4;
+    }
+  } else {
+    for (int k = 0; k < 3; k++) {
+      C[k] = o.diffuse[k];
+      Sp[k] = pm.type == PR_MAT_DIFFUSE ? 0.0 : o.specular[k];
+    }
+    if (o.reflection >= 0)
+      for (int k = 0; k < 3; k++) {
+        E[k] = o.emission[k];
+        Sp[k] = o.specular[k];
+      }
+  }
+  if (o.reflection >= 0) {
+    type = o.reflection;
+    ior = o.refraction_index;
+    rough = o.roughness;
+    if (type == PR_MAT_SPECULAR || type == PR_MAT_REFRACTION) {
+      for (int k = 0; k < 3; k++) C[k] = o.specular[k];
+      mask &= ~1;
+    }
+    if (type == PR_MAT_WARD) {
+      wx = o.ward[0];
+      wy = o.ward[1];
+    }
+    if (type == PR_MAT_PHONG) pn = o.shininess;
+    if (type == PR_MAT_WARD || type == PR_MAT_PHONG) {
+      for (int k = 0; k < 3; k++) C[k] = o.diffuse[k];
+      if (o.texture) mask |= 1;
+    }
+    if (type == PR_MAT_REFRACTION && !(ior > 0.0)) { err = "OBJ glass needs Ni > 0"; return PR_E_ARG; }
+    if (type == PR_MAT_WARD && !(wx > 0.0 && wy > 0.0)) { err = "OBJ Ward material needs '#WARD ax ay' > 0"; return PR_E_ARG; }
+  }
+  g.type = type;
+  for (int k = 0; k < 3; k++) {
+    g.color[k] = (float)C[k];
+    g.color_d[k] = C[k];
+    g.emission[k] = (float)E[k];
+    g.emission_d[k] = E[k];
+    g.specular[k] = (float)Sp[k];
+  }
+  g.roughness = (float)rough;
+  g.roughness_d = rough;
+  g.ior = (float)ior;
+  g.ior_d = ior;
+  g.ward_ax = (float)wx;
+  g.ward_ay = (float)wy;
+  g.phong_n = (float)pn;
+  g.mtex_off = -1;
+  g.mtex_mask = mask;
+  g.mtex_repeat = o.repeat;
+  g.mesh_smooth = o.smooth == 1 ? 1 : (o.smooth == 2 ? 2 : 0);
+  if (o.texture) {
+    g.mtex_off = (int32_t)hs.texels.size();
+    g.mtex_w = o.texture_width;
+    g.mtex_h = o.texture_height;
+    const size_t n = (size_t)g.mtex_w * g.mtex_h;
+    if (hs.texels.size() + n > (size_t)INT32_MAX) { err = "textures too large"; return PR_E_ARG; }
+    for (size_t k = 0; k < n; k++)
+      hs.texels.push_back(make_float4((float)(o.texture[3 * k] / 255.0), (float)(o.texture[3 * k + 1] / 255.0),
+                                      (float)(o.texture[3 * k + 2] / 255.0), 0.0f));
+  }
+  out = (int32_t)hs.mats.size();
+  hs.mats.push_back(g);
+  return PR_OK;
+}
+
+
 // The reference-layout QBVH of one mesh (QBVH.cpp:161-302) into the exact
 // path's arrays, and the entity's indexes into them.
 static int append_exact_qbvh(HostScene& hs, GEntity& g, int entity, const float* vertices, const int32_t* faces,
@@ -498,7 +607,7 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
     g.ior_d = pm.refractive_index;
     // texture and IBL images (material.h:176-236): texels as float RGB, a
     // bitmap's bytes / 255 (BitMap cell values), an HDR image's values
-    g.tex_off = g.ibl_off = g.bump_off = -1;
+    g.tex_off = g.ibl_off = g.bump_off = g.mtex_off = -1;
     if (pm.bump) {
       if (pm.bump_width <= 0 || pm.bump_height <= 0) { err = "bump map size must be positive"; return PR_E_ARG; }
       if (pm.bump_width != pm.bump_height) {
@@ -693,13 +802,22 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
   auto grow = [&ext](double x) { ext = std::max(ext, std::fabs(x)); };
   // meshes shaded with interpolated normals, and textured meshes: the
   // per-face vertex-normal and texture-coordinate records exist only then
-  bool any_smooth = false, any_mesh_tex = false;
+  bool any_smooth = false, any_mesh_tex = false, any_obj_mat = false;
   for (int i = 0; i < d->n_entities; i++) {
     const pr_entity& pe = d->entities[i];
     if (pe.type != PR_ENT_POLYGON || pe.material < 0 || pe.material >= d->n_materials) continue;
+    if (pe.mesh < 0 || pe.mesh >= d->n_meshes) continue;
     const pr_material& pm = d->materials[pe.material];
+    const pr_mesh& pm_ = d->meshes[pe.mesh];
     any_smooth = any_smooth || pe.smooth != 0;
     any_mesh_tex = any_mesh_tex || pm.texture || pm.ibl_rgb8 || pm.ibl_rgbf;
+    if (pm_.obj_materials && pm_.face_obj_material && pm_.n_obj_materials > 0) {
+      any_obj_mat = true;
+      for (int k = 0; k < pm_.n_obj_materials; k++) {
+        any_smooth = any_smooth || pm_.obj_materials[k].smooth == 1;
+        any_mesh_tex = any_mesh_tex || pm_.obj_materials[k].texture;
+      }
+    }
   }
   for (int i = 0; i < d->n_entities; i++) {
     const pr_entity& pe = d->entities[i];
@@ -816,7 +934,28 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
         for (int64_t f = 0; f < n3; f++)
           if (pm_.face_uv[f] < 0 || pm_.face_uv[f] >= pm_.n_uv) { err = "texture-coordinate id out of range"; return PR_E_SCENE; }
       }
-      const bool mesh_tex = pm.texture || pm.ibl_rgb8 || pm.ibl_rgbf;
+      // OBJ materials (usemtl): one derived material per material the faces use
+      const bool obj_mats = pm_.obj_materials && pm_.face_obj_material && pm_.n_obj_materials > 0;
+      bool obj_tex = false, obj_smooth = false;
+      std::vector<int32_t> derived;
+      if (obj_mats) {
+        if (d->kerr.enabled || d->wormhole.enabled) {
+          err = "OBJ materials in a black hole or wormhole scene are not on this path";
+          return PR_E_UNSUPPORTED;
+        }
+        derived.assign((size_t)pm_.n_obj_materials, -2);
+        for (int64_t f = 0; f < (int64_t)pm_.n_faces; f++) {
+          const int32_t k = pm_.face_obj_material[f];
+          if (k < -1 || k >= pm_.n_obj_materials) { err = "face OBJ-material index out of range"; return PR_E_SCENE; }
+          if (k >= 0 && derived[(size_t)k] == -2) {
+            int st = derive_obj_material(hs, pm, hs.mats[(size_t)pe.material], pm_.obj_materials[k], derived[(size_t)k], err);
+            if (st != PR_OK) return st;
+            obj_tex = obj_tex || pm_.obj_materials[k].texture;
+            obj_smooth = obj_smooth || pm_.obj_materials[k].smooth == 1;
+          }
+        }
+      }
+      const bool mesh_tex = pm.texture || pm.ibl_rgb8 || pm.ibl_rgbf || obj_tex;
       if (mesh_tex || pm.bump) {
         // the reference indexes the image with (W - 1) u, (H - 1) v of the
         // interpolated coordinates, with no wrap (polygon.h:507-618); a bump
@@ -828,7 +967,7 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
             return PR_E_UNSUPPORTED;
           }
       }
-      if (pe.smooth && (d->kerr.enabled || d->wormhole.enabled)) {
+      if ((pe.smooth || obj_smooth) && (d->kerr.enabled || d->wormhole.enabled)) {
         err = "smooth meshes in a black hole or wormhole scene are not on this path";
         return PR_E_UNSUPPORTED;
       }
@@ -836,18 +975,24 @@ int build_host_scene(const pr_scene_desc* d, HostScene& hs, std::string& err, co
       if (pm_.face_normals) fn.assign(pm_.face_normals, pm_.face_normals + 3 * (size_t)pm_.n_faces);
       else if (pm_.vertex_normals) face_normals_vn(pm_.vertex_normals, pm_.face_vn, pm_.n_faces, fn);
       else face_normals(pm_.vertices, pm_.faces, pm_.n_faces, fn);
-      g.mesh_flags = (pe.smooth ? 1 : 0) | (mesh_tex ? 2 : 0);
+      const bool needs_vn = pe.smooth || obj_smooth;
+      g.mesh_flags = (pe.smooth ? 1 : 0) | (mesh_tex ? 2 : 0) | (obj_mats ? 4 : 0) | (needs_vn ? 8 : 0);
       if (any_smooth) {
         std::vector<float> vn;
         const float* VN = pm_.vertex_normals;
         const int32_t* FVN = pm_.face_vn ? pm_.face_vn : pm_.faces;
-        if (pe.smooth && !VN) {
+        if (needs_vn && !VN) {
           vertex_normals(pm_.vertices, pm_.faces, pm_.n_faces, pm_.n_vertices, vn);
           VN = vn.data();
         }
         for (int64_t f = 0; f < n3; f++)
-          for (int a = 0; a < 3; a++) hs.fvn.push_back(pe.smooth ? VN[3 * (size_t)FVN[f] + a] : 0.0f);
+          for (int a = 0; a < 3; a++) hs.fvn.push_back(needs_vn ? VN[3 * (size_t)FVN[f] + a] : 0.0f);
       }
+      if (any_obj_mat)
+        for (int64_t f = 0; f < (int64_t)pm_.n_faces; f++) {
+          const int32_t k = obj_mats ? pm_.face_obj_material[f] : -1;
+          hs.fmat.push_back(k >= 0 ? derived[(size_t)k] : -1);
+        }
       if (any_mesh_tex)
         for (int64_t f = 0; f < n3; f++)
           for (int a = 0; a < 2; a++) hs.fuv.push_back(mesh_tex ? pm_.uv[2 * (size_t)pm_.face_uv[f] + a] : 0.0f);

@@ -38,6 +38,7 @@ struct HostScene {
   // (9 floats; empty when no mesh is smooth) and the three texture
   // coordinates of meshes with them (6 floats; empty when no textured mesh)
   std::vector<float> fvn, fuv;
+  std::vector<int32_t> fmat;  // per face (like fnorm): derived OBJ-material index, -1 none
   std::vector<float4> texels;           // material textures, RGB / 255
   std::vector<float4> ibl_texels;       // material IBL images
   std::vector<float> bump_texels;       // material bump maps (luminance)

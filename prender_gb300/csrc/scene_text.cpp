@@ -52,6 +52,10 @@ struct pr_scene_file {
   // and texture coordinates with theirs (empty: none)
   std::vector<std::vector<float>> vnormals, uvs;
   std::vector<std::vector<int32_t>> face_vn, face_uv;
+  // per mesh: OBJ materials, their map_Kd images, each face's material
+  std::vector<std::vector<pr_obj_material>> omats;
+  std::vector<std::vector<std::vector<uint8_t>>> omat_tex;
+  std::vector<std::vector<int32_t>> fmat;
   std::vector<pr_mesh> meshes;
   std::vector<uint8_t> bg_tex, disk_tex, worm_tex[2];
   // per material: texture / IBL images (pointers set when the desc is made)
@@ -303,6 +307,10 @@ void read_hdr(const std::string& path, std::vector<float>& out, int& w, int& h) 
 }
 
 struct ObjMesh {
+  std::vector<pr_obj_material> mats;         // newmtl entries (mtllib)
+  std::vector<std::string> mat_names;
+  std::vector<std::vector<uint8_t>> mat_tex;  // map_Kd images (RGB)
+  std::vector<int32_t> fmat;                  // per triangle: usemtl index, -1 none
   std::vector<float> v;      // 3 per vertex
   std::vector<float> vn;     // 3 per vertex normal
   std::vector<float> vt;     // 2 per texture coordinate
@@ -317,20 +325,140 @@ struct ObjMesh {
 // with its normal and texture ids alike; ids a face does not give are 0.
 // Vertex colours (a last 'v' line with six or more numbers makes the whole
 // mesh take them, ObjLoader.cpp:199-228) are refused.
+// Obj::LoadMTLFile (ObjLoader.cpp:704-900): lines after leading blanks,
+// dispatched on the first character as the reference does (any line that
+// starts with 'n' opens a material; K a/d/s, d, Tr, Ni, Ns, map_Kd,
+// map_Bump and the '#' extensions); a map_Kd name is tried as given, then
+// beside the MTL file (Polygon::LoadTexture, polygon.h:971-1030).
+void read_mtl(const std::string& file, ObjMesh& m) {
+  std::ifstream f(file);
+  if (!f) return;
+  std::string line;
+  pr_obj_material* cur = nullptr;
+  while (std::getline(f, line)) {
+    size_t b = 0;
+    while (b < line.size() && (line[b] == ' ' || line[b] == '\t')) b++;
+    const std::string s = trim_eol(line.substr(b));
+    if (s.empty()) continue;
+    const char* c = s.c_str();
+    float x = 0, y = 0, z = 0;
+    switch (c[0]) {
+      case 'n': {
+        pr_obj_material o;
+        memset(&o, 0, sizeof(o));
+        o.alpha = -1.0;
+        o.shininess = 5.0;
+        o.reflection = -1;
+        o.repeat = 1;
+        m.mats.push_back(o);
+        char name[128] = {0};
+        std::sscanf(c, "newmtl %127s", name);
+        m.mat_names.push_back(name);
+        m.mat_tex.emplace_back();
+        cur = &m.mats.back();
+        break;
+      }
+      case 'K':
+        if (!cur) break;
+        if (c[1] == 'd') {
+          const int n = std::sscanf(c, "Kd %f %f %f", &x, &y, &z);
+          const double v3[3] = {x, y, z};
+          for (int i = 0; i < n; i++) cur->diffuse[i] = v3[i];
+        } else if (c[1] == 's') {
+          const int n = std::sscanf(c, "Ks %f %f %f", &x, &y, &z);
+          const double v3[3] = {x, y, z};
+          for (int i = 0; i < n; i++) cur->specular[i] = v3[i];
+        }
+        break;
+      case 'd':
+        if (cur && std::sscanf(c, "d %f", &x) == 1) cur->alpha = x;
+        break;
+      case 'T':
+        if (cur && c[1] == 'r' && std::sscanf(c, "Tr %f", &x) == 1) cur->alpha = std::max(0.0, 1.0 - x);
+        break;
+      case 'N':
+        if (cur && c[1] == 'i' && std::sscanf(c, "Ni %f", &x) == 1) cur->refraction_index = x;
+        if (cur && c[1] == 's' && std::sscanf(c, "Ns %f", &x) == 1) cur->shininess = x;
+        break;
+      case 'm':
+        if (cur && starts(s, "map_Kd") && s.size() > 7) {
+          std::string name = s.substr(7);
+          const std::string p = readable(name) ? name : dir_of(file) + name;
+          int w = 0, h = 0;
+          std::vector<uint8_t> rgba;
+          read_bmp(p, 4, rgba, w, h);
+          for (size_t q = 0; q < (size_t)w * h; q++)
+            if (rgba[4 * q + 3] != 255) fail("a map_Kd texture with transparent texels is not rendered here: " + p);
+          std::vector<uint8_t>& t = m.mat_tex.back();
+          t.resize(3 * (size_t)w * h);
+          for (size_t q = 0; q < (size_t)w * h; q++)
+            for (int a = 0; a < 3; a++) t[3 * q + a] = rgba[4 * q + a];
+          cur->texture_width = w;
+          cur->texture_height = h;
+        }
+        break;
+      case '#': {
+        if (!cur) break;
+        int iv = 0;
+        if (starts(s, "#SMOOTH ") && std::sscanf(c, "#SMOOTH %d", &iv) >= 0) cur->smooth = iv ? 1 : 2;
+        if (starts(s, "#REFLECTION ")) {
+          std::sscanf(c, "#REFLECTION %d", &cur->reflection);
+          if (cur->reflection == 0 || cur->reflection == 1) cur->roughness = 0.0;
+          if (cur->reflection == 2 && (float)cur->refraction_index == 0.0f) cur->refraction_index = 1.5;
+        }
+        if (starts(s, "#EMISSION ")) {
+          const int n = std::sscanf(c, "#EMISSION %f %f %f", &x, &y, &z);
+          const double v3[3] = {x, y, z};
+          for (int i = 0; i < n; i++) cur->emission[i] = v3[i];
+        }
+        if (starts(s, "#COLOR ")) {
+          const int n = std::sscanf(c, "#COLOR %f %f %f", &x, &y, &z);
+          const double v3[3] = {x, y, z};
+          for (int i = 0; i < n; i++) cur->diffuse[i] = v3[i];
+        }
+        if (starts(s, "#WARD ")) {
+          const int n = std::sscanf(c, "#WARD %f %f", &x, &y);
+          if (n >= 1) cur->ward[0] = x;
+          if (n >= 2) cur->ward[1] = y;
+        }
+        if (starts(s, "#SPECULAR ")) {
+          const int n = std::sscanf(c, "#SPECULAR %f %f %f", &x, &y, &z);
+          const double v3[3] = {x, y, z};
+          for (int i = 0; i < n; i++) cur->specular[i] = v3[i];
+        }
+        if (starts(s, "#ROUGHNESS ") && std::sscanf(c, "#ROUGHNESS %f", &x) == 1) cur->roughness = x;
+        if (starts(s, "#REPEAT ")) std::sscanf(c, "#REPEAT %d", &cur->repeat);
+        break;
+      }
+      default:
+        break;
+    }
+  }
+}
+
 void read_obj(const std::string& path, ObjMesh& m) {
   std::ifstream f(path);
   if (!f) fail("cannot open " + path);
   std::string line, mtllib;
-  bool usemtl = false, vertex_colour = false;
+  bool vertex_colour = false;
+  int32_t cur_mat = -1;
   while (std::getline(f, line)) {
     size_t b = 0;
     while (b < line.size() && (line[b] == ' ' || line[b] == '\t')) b++;
     const std::string s = line.substr(b);
     const char* c = s.c_str();
-    if (starts(s, "mtllib ")) {
+    if (starts(s, "mtllib ")) {  // the file as given, else beside the OBJ (ObjLoader.cpp:137-157)
       mtllib = trim_eol(s.substr(7));
-    } else if (starts(s, "usemtl ")) {
-      usemtl = true;
+      read_mtl(readable(mtllib) ? mtllib : dir_of(path) + mtllib, m);
+    } else if (starts(s, "usemtl ")) {  // the last material of that name, case-insensitive (:159-180)
+      const std::string name = trim_eol(s.substr(7));
+      cur_mat = -1;
+      for (size_t i = 0; i < m.mat_names.size(); i++) {
+        const std::string& a = m.mat_names[i];
+        bool eq = a.size() == name.size();
+        for (size_t q = 0; eq && q < a.size(); q++) eq = std::tolower((unsigned char)a[q]) == std::tolower((unsigned char)name[q]);
+        if (eq) cur_mat = (int32_t)i;
+      }
     } else if (s.size() > 1 && c[0] == 'v' && c[1] == 'n') {
       float x = 0, y = 0, z = 0;
       std::sscanf(c, "%*s %f %f %f", &x, &y, &z);
@@ -382,6 +510,7 @@ void read_obj(const std::string& path, ObjMesh& m) {
           m.nid.push_back(n[tri[q][j]] - 1);
           m.tid.push_back(t[tri[q][j]] - 1);
         }
+      for (int q = 0; q < (k == 4 ? 2 : 1); q++) m.fmat.push_back(cur_mat);
     }
   }
   const int64_t nv = (int64_t)(m.v.size() / 3), nn = (int64_t)(m.vn.size() / 3);
@@ -396,8 +525,7 @@ void read_obj(const std::string& path, ObjMesh& m) {
     if (i < 0 || i >= nt) fail("texture-coordinate index outside the vt lines in " + path);
   if (vertex_colour) fail("OBJ vertex colours are not rendered here: " + path);
   if (m.f.empty()) fail("no faces in " + path);
-  if (usemtl && !mtllib.empty() && (readable(mtllib) || readable(dir_of(path) + mtllib)))
-    fail("OBJ materials (mtllib / usemtl) are not rendered here: " + path);
+  if (m.mats.empty()) m.fmat.clear();
 }
 
 // Obj::CalcNormalVector with vertex normals (ObjLoader.cpp:617-641): the
@@ -922,6 +1050,9 @@ class Loader {
       S_.face_vn.push_back(std::move(fvn));
       S_.uvs.push_back(std::move(mesh.vt));
       S_.face_uv.push_back(std::move(mesh.tid));
+      S_.omats.push_back(std::move(mesh.mats));
+      S_.omat_tex.push_back(std::move(mesh.mat_tex));
+      S_.fmat.push_back(std::move(mesh.fmat));
     }
     e.material = (int)S_.mats.size();
     S_.mats.push_back(m);
@@ -1235,6 +1366,13 @@ class Loader {
         mm.n_uv = (int32_t)(S_.uvs[i].size() / 2);
         mm.uv = S_.uvs[i].data();
         mm.face_uv = S_.face_uv[i].data();
+      }
+      if (!S_.omats[i].empty() && !S_.fmat[i].empty()) {
+        for (size_t k = 0; k < S_.omats[i].size(); k++)
+          S_.omats[i][k].texture = S_.omat_tex[i][k].empty() ? nullptr : S_.omat_tex[i][k].data();
+        mm.n_obj_materials = (int32_t)S_.omats[i].size();
+        mm.obj_materials = S_.omats[i].data();
+        mm.face_obj_material = S_.fmat[i].data();
       }
     }
     pr_scene_desc& d = S_.desc;

@@ -227,6 +227,44 @@ def _normalize_ref(v):
 
 
 @dataclass
+class ObjMaterial:
+    """An OBJ material (newmtl, ObjLoader.cpp:704-900) with the loader's
+    defaults; texture is the map_Kd image ((H, W, 3) uint8, cell(y, x) rows)."""
+    diffuse: Sequence[float] = (0.0, 0.0, 0.0)
+    alpha: float = -1.0
+    specular: Sequence[float] = (0.0, 0.0, 0.0)
+    emission: Sequence[float] = (0.0, 0.0, 0.0)
+    refraction_index: float = 0.0
+    shininess: float = 5.0
+    roughness: float = 0.0
+    ward: Sequence[float] = (0.0, 0.0)
+    reflection: int = -1
+    smooth: int = 0
+    repeat: int = 1
+    texture: Optional[np.ndarray] = field(default=None, compare=False, repr=False)
+    name: str = ""
+
+    def to_c(self, keep: list) -> A.pr_obj_material:
+        # ObjMaterial keeps floats (the MTL reader's sscanf %f)
+        def f32(x):
+            return float(np.float32(x))
+        o = A.pr_obj_material()
+        o.diffuse[:] = [f32(x) for x in self.diffuse]
+        o.alpha = f32(self.alpha)
+        o.specular[:] = [f32(x) for x in self.specular]
+        o.emission[:] = [f32(x) for x in self.emission]
+        o.refraction_index, o.shininess, o.roughness = f32(self.refraction_index), f32(self.shininess), f32(self.roughness)
+        o.ward[:] = [f32(x) for x in self.ward]
+        o.reflection, o.smooth, o.repeat = int(self.reflection), int(self.smooth), int(self.repeat)
+        if self.texture is not None:
+            t = np.ascontiguousarray(self.texture, dtype=np.uint8)
+            keep.append(t)
+            o.texture = t.ctypes.data
+            o.texture_height, o.texture_width = t.shape[0], t.shape[1]
+        return o
+
+
+@dataclass
 class Mesh:
     vertices: np.ndarray  # (n, 3) float32
     faces: np.ndarray     # (m, 3) int32, 0-based
@@ -244,6 +282,9 @@ class Mesh:
     # and IBL images land on the mesh
     uv: Optional[np.ndarray] = None
     face_uv: Optional[np.ndarray] = None
+    # OBJ materials (mtllib) and each face's (usemtl; -1 none)
+    obj_materials: Optional[list] = None
+    face_material: Optional[np.ndarray] = None
 
     def __post_init__(self):
         self.vertices = np.ascontiguousarray(self.vertices, dtype=np.float32)
@@ -261,6 +302,12 @@ class Mesh:
                 setattr(self, ids, np.ascontiguousarray(i, dtype=np.int32).reshape(-1, 3))
                 if getattr(self, ids).shape[0] != self.faces.shape[0]:
                     raise ValueError(f"{what}: one id triple per face")
+        if (self.obj_materials is None) != (self.face_material is None):
+            raise ValueError("OBJ materials need both the materials and each face's index")
+        if self.face_material is not None:
+            self.face_material = np.ascontiguousarray(self.face_material, dtype=np.int32).reshape(-1)
+            if self.face_material.shape[0] != self.faces.shape[0]:
+                raise ValueError("face_material: one index per face")
 
 
 @dataclass
@@ -367,6 +414,13 @@ class SceneDesc:
                 pm.n_uv = uv.shape[0]
                 pm.uv = uv.ctypes.data_as(C.POINTER(C.c_float))
                 pm.face_uv = fu.ctypes.data_as(C.POINTER(C.c_int32))
+            if m.obj_materials is not None:
+                om = (A.pr_obj_material * max(1, len(m.obj_materials)))(*[o.to_c(self._tex) for o in m.obj_materials])
+                fm = m.face_material
+                self._mesh_arrays += [om, fm]
+                pm.n_obj_materials = len(m.obj_materials)
+                pm.obj_materials = C.cast(om, C.POINTER(A.pr_obj_material))
+                pm.face_obj_material = fm.ctypes.data_as(C.POINTER(C.c_int32))
             meshes.append(pm)
         self._meshes = (A.pr_mesh * max(1, len(meshes)))(*meshes)
         d = A.pr_scene_desc()
@@ -857,9 +911,47 @@ def _write_bmp24(path: str, tex: np.ndarray) -> None:
             fh.write(tex[y, :, ::-1].tobytes() + b"\0" * pad)
 
 
+def _write_mtl(path: str, mats, texdir: str) -> None:
+    with open(path, "w", newline="\n") as fh:
+        for i, o in enumerate(mats):
+            fh.write(f"newmtl m{i}\n")
+            fh.write("Kd %.9g %.9g %.9g\n" % tuple(float(x) for x in o.diffuse))
+            fh.write("Ks %.9g %.9g %.9g\n" % tuple(float(x) for x in o.specular))
+            if float(o.alpha) >= 0.0:
+                fh.write("d %.9g\n" % float(o.alpha))
+            if float(o.shininess) != 5.0:
+                fh.write("Ns %.9g\n" % float(o.shininess))
+            if o.texture is not None:
+                tp = f"mtex{i}.bmp"
+                _write_bmp24(os.path.join(texdir, tp), np.asarray(o.texture, dtype=np.uint8))
+                fh.write(f"map_Kd {tp}\n")
+            if int(o.smooth):
+                fh.write(f"#SMOOTH {1 if int(o.smooth) == 1 else 0}\n")
+            if int(o.repeat) != 1:
+                fh.write(f"#REPEAT {int(o.repeat)}\n")
+            if any(float(x) for x in o.emission):
+                fh.write("#EMISSION %.9g %.9g %.9g\n" % tuple(float(x) for x in o.emission))
+            if any(float(x) for x in o.ward):
+                fh.write("#WARD %.9g %.9g\n" % tuple(float(x) for x in o.ward))
+            if int(o.reflection) >= 0:
+                # Ni before '#REFLECTION 2' keeps an explicit index; the
+                # loader then sets 0.0 to 1.5 and '#REFLECTION 0/1' the roughness to 0
+                if float(o.refraction_index) != 0.0:
+                    fh.write("Ni %.9g\n" % float(o.refraction_index))
+                fh.write(f"#REFLECTION {int(o.reflection)}\n")
+            elif float(o.refraction_index) != 0.0:
+                fh.write("Ni %.9g\n" % float(o.refraction_index))
+            if float(o.roughness) != 0.0:
+                fh.write("#ROUGHNESS %.9g\n" % float(o.roughness))
+
+
 def _write_obj(path: str, mesh: Mesh) -> None:
     # %.9g round-trips float32 exactly through sscanf("%f")
     with open(path, "w", newline="\n") as fh:
+        if mesh.obj_materials is not None:
+            mtl = os.path.splitext(path)[0] + ".mtl"
+            _write_mtl(mtl, mesh.obj_materials, os.path.dirname(path))
+            fh.write(f"mtllib {os.path.basename(mtl)}\n")
         for v in mesh.vertices:
             fh.write("v %.9g %.9g %.9g\n" % (float(v[0]), float(v[1]), float(v[2])))
         if mesh.vertex_normals is not None:
@@ -868,7 +960,11 @@ def _write_obj(path: str, mesh: Mesh) -> None:
         if mesh.uv is not None:
             for t in mesh.uv:
                 fh.write("vt %.9g %.9g\n" % (float(t[0]), float(t[1])))
+        cur_mtl = None
         for q, f in enumerate(mesh.faces):
+            if mesh.face_material is not None and int(mesh.face_material[q]) != cur_mtl:
+                cur_mtl = int(mesh.face_material[q])
+                fh.write(f"usemtl m{cur_mtl}\n" if cur_mtl >= 0 else "usemtl none\n")
             corners = []
             for k in range(3):
                 c = "%d" % (int(f[k]) + 1)

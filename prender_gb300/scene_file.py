@@ -21,7 +21,7 @@ import numpy as np
 
 from . import _abi as A
 from ._lib import load as _load_lib
-from .scene import Camera, Entity, Material, Medium, Mesh, RenderSettings, Scene
+from .scene import Camera, Entity, Material, Medium, Mesh, ObjMaterial, RenderSettings, Scene
 
 
 class SceneFileError(ValueError):
@@ -118,7 +118,20 @@ def load(path: str) -> Scene:
             if pm.uv and pm.face_uv:
                 uv = np.ctypeslib.as_array(pm.uv, shape=(pm.n_uv * 2,)).reshape(-1, 2).copy()
                 fuv = np.ctypeslib.as_array(pm.face_uv, shape=(pm.n_faces * 3,)).reshape(-1, 3).copy()
-            s.meshes.append(Mesh(v, fc, fn, vertex_normals=vn, face_vn=fvn, uv=uv, face_uv=fuv))
+            oms = fm = None
+            if pm.obj_materials and pm.face_obj_material and pm.n_obj_materials > 0:
+                oms = []
+                for k in range(pm.n_obj_materials):
+                    q = pm.obj_materials[k]
+                    oms.append(ObjMaterial(diffuse=_v(q.diffuse), alpha=float(q.alpha), specular=_v(q.specular),
+                                           emission=_v(q.emission), refraction_index=float(q.refraction_index),
+                                           shininess=float(q.shininess), roughness=float(q.roughness),
+                                           ward=_v(q.ward, 2), reflection=int(q.reflection), smooth=int(q.smooth),
+                                           repeat=int(q.repeat),
+                                           texture=_texture(q.texture, q.texture_width, q.texture_height, 3)))
+                fm = np.ctypeslib.as_array(pm.face_obj_material, shape=(pm.n_faces,)).copy()
+            s.meshes.append(Mesh(v, fc, fn, vertex_normals=vn, face_vn=fvn, uv=uv, face_uv=fuv, obj_materials=oms,
+                                 face_material=fm))
         s.background = _v(d.background)
         s.environment_light = _v(d.environment_light)
         s.participating_media = int(d.participating_media)

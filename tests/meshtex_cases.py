@@ -12,16 +12,21 @@ golden-vector generator and the tests.
   return the texel's emission), and a ball with a bump map (which the
   reference's mesh hit does not keep; without vt lines its lookup reads
   outside the map), NEE on and off.
+* 'obj_mtl', 'obj_mtl_nonee': OBJ materials chosen per face (usemtl): Kd
+  over a diffuse entity (its Ks dropped), a '#REFLECTION 4' Phong, a map_Kd
+  texture with '#REPEAT 2' (the entity colour times the texel), a mirror; on
+  a panel a textured Ward with '#EMISSION' (colour, specular and emission
+  times the texel), a '#SMOOTH 1' material and a glass one.
 
 Textures are seeded synthetic images."""
 import numpy as np
 
-from prender_gb300.scene import Camera, Material, RenderSettings, Scene
+from prender_gb300.scene import Camera, Material, ObjMaterial, RenderSettings, Scene
 from prender_gb300.scenes import icosphere
 
 from texture_cases import _walls, bump_map, checker
 
-CASES = ["smooth", "smooth_nonee", "mesh_tex", "mesh_tex_nonee"]
+CASES = ["smooth", "smooth_nonee", "mesh_tex", "mesh_tex_nonee", "obj_mtl", "obj_mtl_nonee"]
 
 
 def _ball(subdiv, center, radius):
@@ -91,6 +96,31 @@ def build(name: str, width: int, height: int, samples: int, supersamples: int = 
         bm = Material.diffuse((0.3, 0.5, 0.8))
         bm.bump = bump_map(16, 44)
         s.add_mesh(bv, bf, bm, uv=_sphere_uv(bunit), face_uv=bf)
+    elif name in ("obj_mtl", "obj_mtl_nonee"):
+        # OBJ materials (usemtl) over a diffuse entity material
+        base = Material.diffuse((0.5, 0.5, 0.5))
+        mats = [
+            ObjMaterial(diffuse=(0.8, 0.3, 0.2), specular=(0.4, 0.4, 0.4)),                # Kd; Ks dropped (diffuse B)
+            ObjMaterial(diffuse=(0.2, 0.5, 0.2), specular=(0.5, 0.5, 0.5), shininess=20.0,
+                        reflection=4, roughness=0.3),                                      # Phong
+            ObjMaterial(texture=checker(16, 32, 4, (250, 220, 60), (40, 60, 220), 61), repeat=2),  # B colour x texel
+            ObjMaterial(specular=(0.9, 0.9, 0.9), reflection=1),                           # mirror
+        ]
+        v, f, unit = _ball(2, (27, 14, 60), 14)
+        fm = (np.arange(len(f)) % 5 - 1).astype(np.int32)  # -1, 0, 1, 2, 3 in turn
+        s.add_mesh(v, f, base, uv=_sphere_uv(unit), face_uv=f)
+        s.meshes[-1].obj_materials, s.meshes[-1].face_material = mats, fm
+        pv, pf, pvn, puv = _wavy_panel((66, 1.0, 80), 40, 4, 12)
+        pmats = [
+            ObjMaterial(diffuse=(0.3, 0.6, 0.8), specular=(0.5, 0.4, 0.3), emission=(0.2, 0.1, 0.0),
+                        ward=(0.1, 0.25), reflection=3,
+                        texture=checker(16, 16, 4, (240, 240, 240), (90, 90, 90), 62)),   # Ward, texel-scaled
+            ObjMaterial(diffuse=(0.7, 0.7, 0.3), smooth=1),                                # '#SMOOTH 1'
+            ObjMaterial(refraction_index=1.4, specular=(0.95, 0.95, 0.95), reflection=2),  # glass
+        ]
+        pfm = (np.arange(len(pf)) % 3).astype(np.int32)
+        s.add_mesh(pv, pf, Material.diffuse((0.6, 0.6, 0.6)), vertex_normals=pvn, face_vn=pf, uv=puv, face_uv=pf)
+        s.meshes[-1].obj_materials, s.meshes[-1].face_material = pmats, pfm
     else:
         raise KeyError(name)
     s.camera = Camera(position=(50, 52, 220), dir=(0, -0.04, -1), angle=30, width=width, height=height)

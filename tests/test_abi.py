@@ -46,7 +46,7 @@ def test_struct_layouts_match(lib):
     for i, s in enumerate(structs):
         assert lib.pr_abi_sizeof(i) == C.sizeof(s), s.__name__
     assert lib.pr_abi_sizeof(9) == C.sizeof(A.pr_job)
-    assert lib.pr_abi_version() == 7
+    assert lib.pr_abi_version() == 8
 
 
 def test_no_gpu_context_is_an_error_not_a_fallback(lib):

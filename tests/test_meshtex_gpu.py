@@ -1,5 +1,5 @@
-"""Smooth and textured meshes (polygon.h:178-528) on the GPU against the
-oracle, through the C ABI, in both render forms.
+"""Smooth and textured meshes and OBJ materials (polygon.h:178-528) on the
+GPU against the oracle, through the C ABI, in both render forms.
 
 The oracle renders every scene of meshtex_cases bit-exactly like the
 reference on one thread (tests/test_oracle_golden.py, meshtex_render.npz);

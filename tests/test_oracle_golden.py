@@ -165,7 +165,7 @@ def test_mlt_render_one_thread_bit_exact(golden, name):
     assert ref.mean() > 0
 
 
-@pytest.mark.parametrize("name", ["smooth", "smooth_nonee", "mesh_tex", "mesh_tex_nonee"])
+@pytest.mark.parametrize("name", ["smooth", "smooth_nonee", "mesh_tex", "mesh_tex_nonee", "obj_mtl", "obj_mtl_nonee"])
 def test_mesh_smooth_and_texture_render_one_thread_bit_exact(golden, name):
     # 'smooth 1' meshes (vertex normals by the loader's rule and from vn
     # lines, glass, normal -1), textured meshes through vt lines (a texture

@@ -81,6 +81,18 @@ def test_written_scene_reads_back_the_same(tmp_path, name):
                 assert np.array_equal(x, y), f
         # a mesh with vn lines gets its face normals from them in the reader
         assert (a.face_normals is None) == (b.vertex_normals is None)
+        assert (a.obj_materials is None) == (b.obj_materials is None)
+        if b.obj_materials is not None:
+            assert np.array_equal(a.face_material, b.face_material)
+            for x, y in zip(a.obj_materials, b.obj_materials):
+                yc, xc = y.to_c([]), x.to_c([])
+                for f in ("diffuse", "specular", "emission", "ward"):
+                    assert list(getattr(xc, f)) == list(getattr(yc, f)), f
+                for f in ("alpha", "refraction_index", "shininess", "roughness", "reflection", "smooth", "repeat"):
+                    assert getattr(xc, f) == getattr(yc, f), f
+                assert (x.texture is None) == (y.texture is None)
+                if x.texture is not None:
+                    assert np.array_equal(np.asarray(x.texture), np.asarray(y.texture))
     assert back.background == tuple(s.background) and back.environment_light == tuple(s.environment_light)
     assert back.participating_media == int(s.participating_media and s.settings.media)
     assert back.medium == s.medium
@@ -153,7 +165,7 @@ def test_mlt_files_render_like_the_reference(tmp_path, golden, name):
     assert np.array_equal(img, golden["mlt_render"][name])
 
 
-@pytest.mark.parametrize("name", ["smooth", "smooth_nonee", "mesh_tex", "mesh_tex_nonee"])
+@pytest.mark.parametrize("name", ["smooth", "smooth_nonee", "mesh_tex", "mesh_tex_nonee", "obj_mtl", "obj_mtl_nonee"])
 def test_mesh_texture_files_render_like_the_reference(tmp_path, golden, name):
     # the files the reference rendered for meshtex_render.npz (OBJ vn / vt
     # lines and their face ids, 'smooth 1', textures, IBL images and bump
@@ -455,10 +467,36 @@ def test_obj_vertex_normals_give_the_face_normal(tmp_path):
     assert fn[1].tolist() == [1.0, 0.0, 0.0]
 
 
-def test_obj_materials_are_refused(tmp_path):
-    (tmp_path / "m.mtl").write_text("newmtl red\nKd 1 0 0\n")
-    with pytest.raises(scene_file.SceneFileError, match="mtllib"):
-        _obj_scene(tmp_path, "mtllib m.mtl\nusemtl red\nv 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+def test_obj_materials_are_read_as_the_loader_reads_them(tmp_path):
+    # LoadMTLFile's first-character dispatch: Kd / Ks, d, Tr, Ni / Ns and the
+    # '#' extensions; '#REFLECTION 2' with Ni 0 sets 1.5 and '#REFLECTION 1'
+    # the roughness 0; usemtl takes the last material of a name, ignoring
+    # case; faces before any usemtl (or after an unknown name) get none
+    (tmp_path / "m.mtl").write_text(
+        "newmtl red\n  Kd 1 0 0\nKs 0.5 0.5 0.5\nd 1\nNs 12\n#ROUGHNESS 0.4\n#REFLECTION 1\n"
+        "newmtl Glass\nTr 0\n#REFLECTION 2\n#SMOOTH 0\n#REPEAT 3\n#EMISSION 1 2 3\n#WARD 0.1 0.2\n"
+        "newmtl red\nKd 0 1 0\n#COLOR 0 0 1\n#SMOOTH 1\n")
+    obj = ("mtllib m.mtl\nv 0 0 0\nv 1 0 0\nv 0 1 0\nv 1 1 0\nf 1 2 3\nusemtl RED\nf 2 4 3\n"
+           "usemtl glass\nf 1 2 4 3\nusemtl nothing\nf 1 3 4\n")
+    s = _obj_scene(tmp_path, obj)
+    m = s.meshes[0]
+    assert m.face_material.tolist() == [-1, 2, 1, 1, -1]
+    red0, glass, red1 = m.obj_materials
+    assert tuple(red0.diffuse) == (1.0, 0.0, 0.0) and tuple(red0.specular) == (0.5, 0.5, 0.5)
+    assert red0.alpha == 1.0 and red0.shininess == 12.0 and red0.reflection == 1 and red0.roughness == 0.0
+    assert glass.alpha == 1.0 and glass.reflection == 2 and glass.refraction_index == 1.5 and glass.smooth == 2
+    assert glass.repeat == 3 and tuple(glass.emission) == (1.0, 2.0, 3.0) and tuple(glass.ward) == (
+        float(np.float32(0.1)), float(np.float32(0.2)))
+    assert tuple(red1.diffuse) == (0.0, 0.0, 1.0) and red1.smooth == 1 and red1.reflection == -1
+
+
+def test_obj_material_refusals(tmp_path):
+    from prender_gb300 import gpu
+    (tmp_path / "m.mtl").write_text("newmtl half\nKd 1 0 0\nd 0.5\n")
+    s = _obj_scene(tmp_path, "mtllib m.mtl\nusemtl half\nv 0 0 0\nv 1 0 0\nv 0 1 0\nv 1 1 0\nf 1 2 3\nf 2 4 3\n"
+                             "f 1 2 4\nf 1 3 4\nf 1 4 2\n")
+    with pytest.raises(gpu.PrenderError, match="alpha"):
+        gpu.check_scene(s)
 
 
 def test_mesh_transforms_move_vertices_in_float_steps(tmp_path):
