@@ -25,7 +25,8 @@ namespace pr {
 namespace {
 
 constexpr uint32_t kTagFresh = 0x4d4c5401u, kTagMutate = 0x4d4c5402u, kTagStep = 0x4d4c5403u;
-constexpr uint32_t kTagExtra = 0x4d4c5500u;  // + branch
+constexpr uint32_t kTagExtra = 0x4d4c5500u;   // + branch
+constexpr uint32_t kTagStream = 0x4d4c5600u;  // + branch
 constexpr uint64_t kLargeBit = 1ull << 62, kSeedBit = 1ull << 63;
 
 // the chains' primary samples (coordinate-major: u[k * chains + chain])
@@ -70,10 +71,16 @@ __device__ __forceinline__ float pss_value(uint64_t seed, uint64_t sample, int k
 struct PssRng {
   uint64_t seed, sample;
   uint32_t branch, draws;
+  uint32_t vstart, sdraws;  // the vertex's first draw; its stream draws so far
   __device__ __forceinline__ float next() {
     const uint32_t k = draws++;
     if (branch == 0 && k + 6u < (uint32_t)kMltDims) return pss_value(seed, sample, (int)k + 6);
     return u01(phx(seed, kTagExtra + (branch & 0xFFu), sample & ~kLargeBit, k));
+  }
+  // the light choice and surface NEE point: fresh in every proposal, as the
+  // reference's Next01 draws them from its stream under MLT
+  __device__ __forceinline__ float next_stream() {
+    return u01(phx(seed, kTagStream + (branch & 0xFFu), sample & ~kLargeBit, (vstart << 6) + (sdraws++ & 63u)));
   }
 };
 __device__ __forceinline__ void rng_at(PssRng& r, uint64_t seed, uint64_t sample, uint32_t branch, uint32_t draws) {
@@ -81,7 +88,10 @@ __device__ __forceinline__ void rng_at(PssRng& r, uint64_t seed, uint64_t sample
   r.sample = sample;
   r.branch = branch;
   r.draws = draws;
+  r.vstart = draws;
+  r.sdraws = 0;
 }
+__device__ __forceinline__ float rng_stream(PssRng& r) { return r.next_stream(); }
 __device__ __forceinline__ uint32_t rng_draws(const PssRng& r) { return r.draws; }
 
 namespace {

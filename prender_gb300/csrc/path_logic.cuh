@@ -115,20 +115,26 @@ __device__ __forceinline__ void make_vertex(const DevScene& S, float3 o, float3 
   if (e.normal_inverse < 0) v.n = -v.n;
 }
 
+// The reference's light choice and surface NEE point draw with Next01,
+// which under Metropolis light transport is the thread's stream rather than
+// a primary sample (mlt.h:166, light.h:147, directLight_radiance.h:343-371):
+// a sampler may route those draws elsewhere; the stream samplers do not.
+__device__ __forceinline__ float rng_stream(Rng& r) { return r.next(); }
+
 // a point on light entity le (direct_radiance_sample, directLight_radiance.h:326-377;
 // the media variant omits the uvplane's normal * PS_EPS lift, ParticipatingMedia.h:213-224)
 template <class R>
 __device__ __forceinline__ float3 sample_light(const GEntF& le, R& rng, bool lift) {
   if (le.type == PR_ENT_SPHERE) {
-    const float r1 = 6.28318530717958647692f * rng.next();
-    const float r2 = 1.0f - 2.0f * rng.next();
+    const float r1 = 6.28318530717958647692f * (lift ? rng_stream(rng) : rng.next());
+    const float r2 = 1.0f - 2.0f * (lift ? rng_stream(rng) : rng.next());
     const float sq = sqrtf(fmaxf(0.0f, 1.0f - r2 * r2));
     float sn, cs;
     sincosf(r1, &sn, &cs);
     return f3(le.p[0], le.p[1], le.p[2]) + f3(sq * cs, sq * sn, r2) * le.radius_eps;
   }
-  const float t = le.v_length * rng.next();  // v first, then u (directLight_radiance.h:359-360)
-  const float s = le.u_length * rng.next();
+  const float t = le.v_length * (lift ? rng_stream(rng) : rng.next());  // v first, then u (directLight_radiance.h:359-360)
+  const float s = le.u_length * (lift ? rng_stream(rng) : rng.next());
   float3 lp = f3(le.p[0], le.p[1], le.p[2]) + f3(le.u[0], le.u[1], le.u[2]) * s + f3(le.v[0], le.v[1], le.v[2]) * t;
   if (lift) lp = lp + f3(le.n[0], le.n[1], le.n[2]) * 1.0e-6f;
   return lp;
@@ -145,7 +151,7 @@ __device__ __forceinline__ float3 light_normal(const GEntF& le, float3 lp, bool 
 // LightList::randomLight (light.h:132-155): rounded index, probability 1
 template <class R>
 __device__ __forceinline__ const GLight& pick_light(const DevScene& S, R& rng) {
-  int idx = (int)(rng.next() * (float)(S.n_lights - 1) + 0.5f);
+  int idx = (int)(rng_stream(rng) * (float)(S.n_lights - 1) + 0.5f);
   idx = min(max(idx, 0), S.n_lights - 1);
   return S.lights[idx];
 }
