@@ -14,6 +14,9 @@ from prender_gb300.scene import Material
 from texture_cases import checker
 
 CASES = ["mlt_spheres", "mlt_caustic", "mlt_glossy"]
+# pinned against the reference on the oracle only: the global medium (HG,
+# NEE from medium points) under the Metropolis sampler
+ORACLE_CASES = CASES + ["mlt_media"]
 
 
 def build(name: str, width: int, height: int, chains: int, mutation: float = 2.0, pre_sample: float = 0.4):
@@ -42,6 +45,12 @@ def build(name: str, width: int, height: int, chains: int, mutation: float = 2.0
         # a panel 1 above the floor: the radius-1e5 floor sphere's FP32 hit
         # distance at grazing angles is not good to a few hundredths
         s.add_uvplane((2, 1.0, 40), (0, 0, 16), (16, 0, 0), floor)
+    elif name == "mlt_media":
+        s.participating_media = 1
+        s.medium.sigma_s_rgb = (0.004, 0.004, 0.004)
+        s.medium.sigma_a_rgb = (0.001, 0.001, 0.001)
+        s.medium.phase_g = (0.5, 0.5, 0.5)
+        st.media = 1
     elif name not in ("mlt_spheres", "mlt_caustic"):
         raise KeyError(name)
     return s
@@ -50,7 +59,7 @@ def build(name: str, width: int, height: int, chains: int, mutation: float = 2.0
 def one_thread_cases():
     """name -> scene for the reference's one-thread MLT (bit-exact): 32 x 24,
     two chains of 307 seed paths and 1536 mutations each"""
-    return {k: build(k, 32, 24, 2) for k in CASES}
+    return {k: build(k, 32, 24, 2) for k in ORACLE_CASES}
 
 
 ORACLE_TENT_SUBPIXELS = 1 << 16  # the oracle's test-only full 2 x 2 sub-pixel footprint

@@ -151,12 +151,13 @@ def test_texture_render_one_thread_bit_exact(golden, name):
     assert ref.mean() > 0
 
 
-@pytest.mark.parametrize("name", ["mlt_spheres", "mlt_caustic", "mlt_glossy"])
+@pytest.mark.parametrize("name", ["mlt_spheres", "mlt_caustic", "mlt_glossy", "mlt_media"])
 def test_mlt_render_one_thread_bit_exact(golden, name):
     # Render::RunMLT: two Kelemen chains per scene (seed paths, luminance-
     # drawn start, lazy small steps, large steps, the stack a rejection
     # restores, the light choice and surface NEE points from the stream
-    # itself), NEE on and off, glossy lobes and a textured floor
+    # itself), NEE on and off, glossy lobes and a textured floor, the global
+    # medium
     import mlt_cases
     sc = mlt_cases.one_thread_cases()[name]
     img = O.OracleScene(sc).render_mlt()

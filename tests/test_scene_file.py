@@ -151,7 +151,7 @@ def test_texture_files_render_like_the_reference(tmp_path, golden, name):
     assert np.array_equal(img, golden["textures_render"][name])
 
 
-@pytest.mark.parametrize("name", ["mlt_spheres", "mlt_caustic", "mlt_glossy"])
+@pytest.mark.parametrize("name", ["mlt_spheres", "mlt_caustic", "mlt_glossy", "mlt_media"])
 def test_mlt_files_render_like_the_reference(tmp_path, golden, name):
     # the files the reference rendered with RunMLT for mlt_render.npz
     # (metropolisTransport, mutation, pre_sample), read by this library's
